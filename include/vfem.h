@@ -1,0 +1,187 @@
+/*
+ * vfem.h -- C ABI of the GB300 VoxelFEM solve-and-sensitivity library (libvfem.so).
+ *
+ * Drop-in boundary for VoxelFEM's pybind11 module `pyVoxelFEM`
+ * (python_bindings/VoxelFEM.cc) on the hot path: TensorProductSimulator<double,1,1,1>,
+ * MultigridSolver<double,1,1,1>, the compliance objective / filter chain / volume
+ * constraint of TopologyOptimizationProblem and the OC optimiser.
+ *
+ * Conventions
+ *   - Every function returns an int status (VFEM_OK on success). On failure the
+ *     thread-local message of vfem_last_error() holds the text the reference would
+ *     throw (std::runtime_error / std::logic_error in the reference).
+ *   - Nodal vector fields are (numNodes, 3) arrays in column-major order: component c
+ *     of node n at [c * numNodes + n] (the reference's Eigen ColMajor VField,
+ *     TensorProductSimulator.hh:180). Element fields are flat row-major grid order.
+ *   - Node (i, j, k) has index (i * ny1 + j) * nz1 + k (NDVector.hh:249-265).
+ *   - Array arguments may be host or device pointers (detected per call); host arrays
+ *     are staged and the call returns after the result is back in host memory.
+ *   - Handles are not thread safe; one handle is used by one thread at a time.
+ */
+#ifndef VFEM_H
+#define VFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VFEM_OK 0
+#define VFEM_ERR_ARG 1      /* invalid argument or size (std::runtime_error in the reference) */
+#define VFEM_ERR_CUDA 2     /* CUDA runtime failure */
+#define VFEM_ERR_NAN 3      /* "NaN encountered" (std::logic_error, MultigridSolver.hh:1082-1084) */
+#define VFEM_ERR_STATE 4    /* e.g. "Must call setVars first!" */
+#define VFEM_ERR_NOT_SPD 5  /* coarsest operator not positive definite (CHOLMOD failure) */
+
+#define VFEM_PREC_FP64 0    /* the method as the reference runs it, FP64 throughout */
+#define VFEM_PREC_MIXED 1   /* FP32 V-cycle inside FP64 outer CG */
+
+#define VFEM_MATVEC_FP64 0  /* outer CG matvec in native FP64 */
+#define VFEM_MATVEC_DF 1    /* outer CG matvec in double-float (FP64-class accuracy on FP32 units) */
+
+typedef struct vfem_grid vfem_grid; /* TensorProductSimulator<double, 1, 1, 1> */
+typedef struct vfem_mg vfem_mg;     /* MultigridSolver<double, 1, 1, 1> */
+typedef struct vfem_problem vfem_problem; /* TopologyOptimizationProblem + MultigridComplianceObjective */
+
+typedef struct vfem_pcg_stats {
+    int64_t iterations;  /* CG iterations executed */
+    double relres;       /* final ||r|| / ||b|| over non-detached nodes */
+    double rsq;          /* final ||r||^2 */
+    double bnorm2;       /* ||b||^2 */
+} vfem_pcg_stats;
+
+/* Per-iteration callback (it_callback / residual_cb, MultigridSolver.hh:1147-1150):
+ * receives the iteration, ||r|| and device pointers to x and r (valid during the call).
+ * A nonzero return stops the iteration. */
+typedef int (*vfem_pcg_callback)(void *user, int64_t it, double rnorm, const double *x_dev, const double *r_dev);
+
+const char *vfem_last_error(void);
+int vfem_version(void);
+int vfem_device_synchronize(void);
+
+/* ---------------- TensorProductSimulator (TensorProductSimulator.hh) ---------------- */
+/* factory TensorProductSimulator([1,1,1], bbox, dims) (VoxelFEM.cc:423-430; ctor TensorProductSimulator.hh:209-279) */
+int vfem_grid_create(const int64_t elems[3], const double bbox_min[3], const double bbox_max[3], vfem_grid **out);
+int vfem_grid_destroy(vfem_grid *g);
+/* numNodes / numElements / NbElementsPerDimension (VoxelFEM.cc:77-78, 113-115) */
+int vfem_grid_dims(const vfem_grid *g, int64_t elems[3], int64_t *num_nodes, int64_t *num_elements);
+/* ETensor setter = readMaterial of an isotropic material (TensorProductSimulator.hh:333-347) */
+int vfem_grid_set_etensor(vfem_grid *g, double young, double poisson);
+int vfem_grid_get_etensor(const vfem_grid *g, double *young, double *poisson);
+/* fullDensityElementStiffnessMatrix (TensorProductSimulator.hh:658), 24x24 row-major */
+int vfem_grid_get_k0(const vfem_grid *g, double *out576);
+/* E_0, E_min, gamma, q, interpolationLaw properties (VoxelFEM.cc:116-121, TensorProductSimulator.hh:160-164) */
+int vfem_grid_set_material_params(vfem_grid *g, double E0, double Emin, double gamma, double q, int law);
+int vfem_grid_get_material_params(const vfem_grid *g, double *E0, double *Emin, double *gamma, double *q, int *law);
+/* setDensities / getDensities / setUniformDensities (TensorProductSimulator.hh:296-371) */
+int vfem_grid_set_densities(vfem_grid *g, const double *rho);
+int vfem_grid_get_densities(vfem_grid *g, double *rho_out);
+int vfem_grid_set_uniform_densities(vfem_grid *g, double value);
+/* getYoungModulusScaleFactor (TensorProductSimulator.hh:550) */
+int vfem_grid_get_young_moduli(vfem_grid *g, double *out);
+/* addDirichletCondition(u, minCorner, maxCorner, componentMask) (TensorProductSimulator.hh:241-252);
+ * component_mask bit c constrains component c ("xyz" = 7) */
+int vfem_grid_add_dirichlet(vfem_grid *g, const double u[3], const double min_corner[3], const double max_corner[3],
+                            uint32_t component_mask);
+/* applySymmetryConditions (TensorProductSimulator.hh:2042-2053) */
+int vfem_grid_apply_symmetry(vfem_grid *g, const int axes[3], const int max_face[3]);
+/* nodal force boundary conditions (BCBuilder::setForce, TensorProductSimulator.hh:95): dense (nn, 3) field */
+int vfem_grid_set_nodal_forces(vfem_grid *g, const double *forces);
+/* getDirichletMask (TensorProductSimulator.hh:256-263): per node, bit c set if component c is constrained */
+int vfem_grid_get_dirichlet_mask(const vfem_grid *g, uint8_t *mask_out);
+/* gravity property (TensorProductSimulator.hh:216-217) */
+int vfem_grid_set_gravity(vfem_grid *g, const double gravity[3]);
+int vfem_grid_get_gravity(const vfem_grid *g, double gravity[3]);
+/* setFabricationMaskHeightByLayer / getFabricationMaskHeight (TensorProductSimulator.hh:326-331) */
+int vfem_grid_set_mask_layer(vfem_grid *g, int64_t layer);
+int vfem_grid_get_mask_height(const vfem_grid *g, double *height);
+/* applyK(u) (TensorProductSimulator.hh:1411-1438, TPSStencils.hh:431-728) */
+int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out);
+/* buildLoadVector (TensorProductSimulator.hh:1269-1288) */
+int vfem_grid_build_load(vfem_grid *g, double *out);
+/* complianceGradient(u) (TensorProductSimulator.hh:973-1005) */
+int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_out);
+/* elementEnergyDensity(u) (TensorProductSimulator.hh:638-654) */
+int vfem_grid_element_energy(vfem_grid *g, const double *u, double *out);
+
+/* ---------------- MultigridSolver (MultigridSolver.hh) ---------------- */
+/* tps.multigridSolver(numCoarseningLevels) (VoxelFEM.cc:93, MultigridSolver.hh:35-121) */
+int vfem_mg_create(vfem_grid *g, int num_coarsening_levels, vfem_mg **out);
+int vfem_mg_destroy(vfem_mg *mg);
+int vfem_mg_num_levels(const vfem_mg *mg, int *levels);
+/* getSimulator(l).NbElementsPerDimension (VoxelFEM.cc:156) */
+int vfem_mg_level_dims(const vfem_mg *mg, int level, int64_t elems[3]);
+/* coarsened Dirichlet mask of level l (MultigridSolver.hh:58-103) */
+int vfem_mg_level_dirichlet_mask(const vfem_mg *mg, int level, uint8_t *mask_out);
+/* precision of the V-cycle (VFEM_PREC_*) and kind of outer matvec (VFEM_MATVEC_*); no reference counterpart */
+int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec);
+/* CUDA-graph capture of the CG iteration (default on); no reference counterpart */
+int vfem_mg_set_use_graphs(vfem_mg *mg, int use);
+/* setSymmetricGaussSeidel (MultigridSolver.hh:123-125) */
+int vfem_mg_set_symmetric_gs(vfem_mg *mg, int symmetric);
+/* setFabricationMaskHeightByLayer (MultigridSolver.hh:1022-1028) */
+int vfem_mg_set_mask_layer(vfem_mg *mg, int64_t layer);
+/* updateStiffnessMatrices (MultigridSolver.hh:846-905) */
+int vfem_mg_update_stiffness(vfem_mg *mg);
+/* applyK(l, u) (MultigridSolver.hh:471-504) */
+int vfem_mg_apply_k(vfem_mg *mg, int level, const double *u, double *out);
+/* computeResidual(l, u, b) (MultigridSolver.hh:527-541) */
+int vfem_mg_residual(vfem_mg *mg, int level, const double *u, const double *b, double *r_out);
+/* one multicoloured Gauss-Seidel sweep smoothingMulticoloredGS(l, u, b, forward) (MultigridSolver.hh:452-458) */
+int vfem_mg_smooth(vfem_mg *mg, int level, double *u_inout, const double *b, int forward);
+/* restriction(l -> l+1) (MultigridSolver.hh:217-275) */
+int vfem_mg_restrict(vfem_mg *mg, int level, const double *fine, double *coarse_out);
+/* accum_interpolation / interpolation (l+1 -> l) (MultigridSolver.hh:179-212) */
+int vfem_mg_interpolate(vfem_mg *mg, int level, const double *coarse, double *fine_inout, int accumulate);
+/* coarsest direct solve (TensorProductSimulator::solve, TensorProductSimulator.hh:1198-1230) */
+int vfem_mg_coarse_solve(vfem_mg *mg, const double *b, double *x_out);
+/* zeroOutDirichletComponents(l, u) (MultigridSolver.hh:508-511) */
+int vfem_mg_zero_dirichlet(vfem_mg *mg, int level, double *u_inout);
+/* solve(u, f, numSteps, numSmoothingSteps, stiffnessUpdated, zeroDirichlet, fullMultigrid) (MultigridSolver.hh:547-573) */
+int vfem_mg_solve(vfem_mg *mg, const double *u, const double *f, int64_t num_steps, int64_t num_smoothing_steps,
+                  int zero_dirichlet, int full_multigrid, double *x_out);
+/* preconditionedConjugateGradient(u, b, maxIter, tol, it_callback, mgIterations, mgSmoothingIterations,
+ * fullMultigrid, dirichletAlreadySatisfied) (MultigridSolver.hh:1047-1152, VoxelFEM.cc:174-191); x in/out */
+int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter, double tol, int64_t mg_iterations,
+                int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
+                vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats);
+
+/* ---------------- filters (TopologyOptimizationFilter.hh) ---------------- */
+/* SmoothingFilter::apply (= backprop) (TopologyOptimizationFilter.hh:285-400); type 0 Const, 1 Linear */
+int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out);
+/* ProjectionFilter::apply / backprop (TopologyOptimizationFilter.hh:199-225) */
+int vfem_projection_apply(int64_t n, double beta, const double *in, double *out);
+int vfem_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out);
+
+/* ---------------- topology optimisation problem ---------------- */
+/* TopologyOptimizationProblem(sim, MultigridComplianceObjective(mg), [TotalVolumeConstraint(volfrac)], filters)
+ * (VoxelFEM.cc:221-277, TopologyOptimizationProblem.hh:17-155); filter i is a smoothing filter
+ * (kinds[i] = 0: radii[i], types[i]) or a projection (kinds[i] = 1: betas[i]). */
+int vfem_problem_create(vfem_mg *mg, int num_filters, const int *kinds, const int *radii, const int *types,
+                        const double *betas, double volume_fraction, vfem_problem **out);
+int vfem_problem_destroy(vfem_problem *p);
+/* MultigridComplianceObjective fields cgIter, tol, mgIterations, mgSmoothingIterations, fullMultigrid, zeroInit
+ * (TopologyOptimizationObjective.hh:98-104) */
+int vfem_problem_set_solver(vfem_problem *p, int64_t cg_iter, double tol, int64_t mg_iterations,
+                            int64_t mg_smoothing_iterations, int full_multigrid, int zero_init);
+/* setVars (TopologyOptimizationProblem.hh:41-50) */
+int vfem_problem_set_vars(vfem_problem *p, const double *x);
+int vfem_problem_get_vars(vfem_problem *p, double *x_out);
+/* evaluateObjective (= compliance 1/2 f.u) / evaluateObjectiveGradient (TopologyOptimizationProblem.hh:69-84) */
+int vfem_problem_objective(vfem_problem *p, double *value);
+int vfem_problem_gradient(vfem_problem *p, double *grad_out);
+/* evaluateConstraints / evaluateConstraintsJacobian (TopologyOptimizationProblem.hh:90-121) */
+int vfem_problem_constraint(vfem_problem *p, double *value);
+int vfem_problem_jacobian(vfem_problem *p, double *jac_out);
+/* ComplianceObjective::u() and FilterChain::physicalVars() */
+int vfem_problem_get_u(vfem_problem *p, double *u_out);
+int vfem_problem_get_physical(vfem_problem *p, double *x_out);
+int vfem_problem_last_solve(vfem_problem *p, vfem_pcg_stats *stats);
+/* OCOptimizer::step(m, p, ctol) (OptimalityCriterion.hh:51-138); probes = constraint evaluations */
+int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, int64_t *probes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VFEM_H */

@@ -1,0 +1,202 @@
+"""GPU parity: the CUDA library (through its C ABI, via voxelfem_gb300.pyVoxelFEM)
+against the CPU oracle on the same seeded inputs.
+
+Tolerances: single operators (applyK, residual, one smoothing sweep, transfers,
+coarse solve, sensitivities, filters) agree to 1e-12 relative (FP64; only the
+summation order differs); the FP64 MG-PCG follows the same iterations and its
+displacements and compliance agree to 1e-8 relative; sensitivities to 1e-6.
+"""
+import numpy as np
+import pytest
+
+from voxelfem_gb300 import pyVoxelFEM as pv
+from voxelfem_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def make_pair(oracle, ne, rho_lo=0.3, seed=0, levels=None, mask_layer=None):
+    bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
+    g = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
+    o = oracle.Sim(ne)
+    wl.setup_cantilever(g, ne, rho_lo, seed)
+    wl.setup_cantilever(o, ne, rho_lo, seed)
+    if mask_layer is not None:
+        g.setFabricationMaskHeightByLayer(mask_layer)
+        o.setFabricationMaskHeightByLayer(mask_layer)
+    if levels is None:
+        return g, o
+    gm = g.multigridSolver(levels)
+    om = oracle.MG(o, levels)
+    if mask_layer is not None:
+        gm.setFabricationMaskHeightByLayer(mask_layer)
+        om.setFabricationMaskHeightByLayer(mask_layer)
+    return g, o, gm, om
+
+
+@pytest.mark.parametrize("ne", [(4, 2, 2), (6, 5, 3), (16, 8, 8)])
+def test_applyk_fine(gpu, oracle, ne):
+    g, o = make_pair(oracle, ne)
+    np.testing.assert_array_equal(g.fullDensityElementStiffnessMatrix().shape, (24, 24))
+    assert rel(g.fullDensityElementStiffnessMatrix(), o.K0()) < 1e-14
+    assert rel(g.getYoungModulusScaleFactor(), o.youngModuli()) < 1e-15
+    u = np.random.default_rng(1).standard_normal((g.numNodes(), 3))
+    assert rel(g.applyK(u), o.applyK(u)) < 1e-12
+
+
+def test_dirichlet_and_load(gpu, oracle):
+    ne = (8, 4, 6)
+    g, o = make_pair(oracle, ne)
+    gm = g.getDirichletMask()
+    om = o.dirichletMask()
+    bits = gm[:, 0] * 1 + gm[:, 1] * 2 + gm[:, 2] * 4
+    np.testing.assert_array_equal(bits.astype(np.uint8), om)
+    np.testing.assert_array_equal(g.buildLoadVector(), o.buildLoadVector())
+
+
+def test_level_operators(gpu, oracle):
+    ne = (16, 8, 8)
+    g, o, gm, om = make_pair(oracle, ne, levels=3)
+    om.updateStiffnessMatrices()
+    gm.updateStiffnessMatrices()
+    rng = np.random.default_rng(2)
+    for l in range(gm.numLevels):
+        assert np.array_equal(gm.getSimulator(l).NbElementsPerDimension, om.levelElems(l))
+        if l > 0:
+            m = gm.getSimulator(l).getDirichletMask()
+            bits = (m[:, 0] * 1 + m[:, 1] * 2 + m[:, 2] * 4).astype(np.uint8)
+            np.testing.assert_array_equal(bits, om.levelDirichletMask(l))
+        nn = om.levelNodes(l)
+        u = rng.standard_normal((nn, 3))
+        b = rng.standard_normal((nn, 3))
+        assert rel(gm.applyK(l, u), om.applyK(l, u)) < 1e-12, l
+        assert rel(gm.computeResidual(l, u, b), om.computeResidual(l, u, b)) < 1e-12, l
+        if l < gm.numLevels - 1:
+            for fwd in (True, False):
+                assert rel(gm.smoothingMulticoloredGS(l, u, b, fwd), om.smooth(l, u, b, fwd)) < 1e-11, (l, fwd)
+            assert rel(gm.restriction(l, u), om.restrict(l, u)) < 1e-13
+            c = rng.standard_normal((om.levelNodes(l + 1), 3))
+            assert rel(gm.interpolation(l, c, u, accumulate=True), om.interpolate(l, c, u, True)) < 1e-13
+            assert rel(gm.interpolation(l, c, None, accumulate=False), om.interpolate(l, c, None, False)) < 1e-13
+    nc = om.levelNodes(gm.numLevels - 1)
+    bc = rng.standard_normal((nc, 3))
+    assert rel(gm.coarseSolve(bc), om.coarseSolve(bc)) < 1e-10
+
+
+@pytest.mark.parametrize("ne,levels", [((16, 8, 8), 2), ((32, 16, 16), 3)])
+def test_pcg_fp64(gpu, oracle, ne, levels):
+    g, o, gm, om = make_pair(oracle, ne, levels=levels)
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    xg = gm.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    xo = om.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    assert gm.lastStats.iterations == om.lastIterations
+    assert gm.lastStats.relres <= 1e-8
+    assert rel(xg, xo) < 1e-8
+    cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
+    assert abs(cg - co) / abs(co) < 1e-8
+    # sensitivities and element energy at the solution
+    assert rel(g.complianceGradient(xg), o.complianceGradient(xo)) < 1e-6
+    assert rel(g.complianceGradient(xo), o.complianceGradient(xo)) < 1e-12
+    assert rel(g.elementEnergyDensity(xo), o.elementEnergyDensity(xo)) < 1e-12
+
+
+def test_pcg_fmg_and_multiple_cycles(gpu, oracle):
+    ne = (16, 8, 8)
+    g, o, gm, om = make_pair(oracle, ne, levels=2)
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    xg = gm.preconditionedConjugateGradient(x0, b, 50, 1e-9, None, 2, 1, True)
+    xo = om.preconditionedConjugateGradient(x0, b, 50, 1e-9, None, 2, 1, True)
+    assert gm.lastStats.iterations == om.lastIterations
+    assert rel(xg, xo) < 1e-8
+
+
+def test_mg_solve_vcycles(gpu, oracle):
+    ne = (16, 8, 8)
+    g, o, gm, om = make_pair(oracle, ne, levels=2)
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    assert rel(gm.solve(x0, b, 3, 2), om.solve(x0, b, 3, 2)) < 1e-10
+    assert rel(gm.solve(x0, b, 2, 1, fullMultigrid=True), om.solve(x0, b, 2, 1, fullMultigrid=True)) < 1e-10
+
+
+def test_masked_layers(gpu, oracle):
+    ne = (16, 16, 8)
+    g, o, gm, om = make_pair(oracle, ne, levels=2, mask_layer=9)
+    assert rel(g.getYoungModulusScaleFactor(), o.youngModuli()) < 1e-15
+    u = np.random.default_rng(3).standard_normal((g.numNodes(), 3))
+    assert rel(g.applyK(u), o.applyK(u)) < 1e-12
+    b = g.buildLoadVector()
+    xg = gm.preconditionedConjugateGradient(np.zeros_like(b), b, 100, 1e-8, None, 1, 2, False)
+    xo = om.preconditionedConjugateGradient(np.zeros_like(b), b, 100, 1e-8, None, 1, 2, False)
+    assert gm.lastStats.iterations == om.lastIterations
+    assert rel(xg, xo) < 1e-8
+
+
+def test_pcg_mixed_precision(gpu, oracle):
+    ne = (32, 16, 16)
+    g, o, gm, om = make_pair(oracle, ne, levels=3)
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    xo = om.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    for matvec in ("df", "fp64"):
+        gm.setPrecision("mixed", matvec)
+        xg = gm.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+        assert gm.lastStats.relres <= 1e-8
+        # true residual of the mixed solution, evaluated in FP64
+        r = b - g.applyK(xg)
+        r[g.getDirichletMask()] = 0
+        assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-8
+        cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
+        assert abs(cg - co) / abs(co) < 1e-6
+    gm.setPrecision("fp64")
+
+
+@pytest.mark.parametrize("radius,ftype", [(1, 0), (2, 1), (3, 1)])
+def test_filters(gpu, oracle, radius, ftype):
+    dims = (10, 7, 5)
+    x = np.random.default_rng(4).uniform(0, 1, int(np.prod(dims)))
+    sf = pv.SmoothingFilter(radius, ftype)
+    sf.setInputDimensions(dims)
+    assert rel(sf.apply(x), oracle.smoothing_filter(x, dims, radius, ftype)) < 1e-14
+    pf = pv.ProjectionFilter(3.0)
+    assert rel(pf.apply(x), oracle.projection_apply(x, 3.0)) < 1e-14
+    g = np.random.default_rng(5).standard_normal(x.size)
+    assert rel(pf.backprop(g, x), oracle.projection_backprop(g, x, 3.0)) < 1e-14
+
+
+def test_topopt_oc(gpu, oracle):
+    ne = (16, 8, 8)
+    bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
+    g = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
+    o = oracle.Sim(ne)
+    wl.setup_mbb(g, ne)
+    wl.setup_mbb(o, ne)
+    gm = g.multigridSolver(2)
+    om = oracle.MG(o, 2)
+    obj = pv.MultigridComplianceObjective(gm)
+    obj.tol = 1e-10
+    obj.cgIter = 200
+    top = pv.TopologyOptimizationProblem(g, obj, [pv.TotalVolumeConstraint(0.3)],
+                                         [pv.SmoothingFilter(2, pv.SmoothingFilter.Type.Linear), pv.ProjectionFilter(1.0)])
+    otop = oracle.TOP(om, [("smoothing", 2, 1), ("projection", 1.0)], 0.3)
+    otop.setSolver(cgIter=200, tol=1e-10)
+    x = np.full(g.numElements(), 0.3)
+    top.setVars(x)
+    otop.setVars(x)
+    assert abs(top.evaluateObjective() - otop.evaluateObjective()) / abs(otop.evaluateObjective()) < 1e-8
+    assert rel(top.evaluateObjectiveGradient(), otop.evaluateObjectiveGradient()) < 1e-6
+    assert abs(top.evaluateConstraints()[0] - otop.evaluateConstraints()[0]) < 1e-12
+    assert rel(top.evaluateConstraintsJacobian(), otop.evaluateConstraintsJacobian()) < 1e-12
+    oc = pv.OCOptimizer(top)
+    for _ in range(3):
+        oc.step()
+        otop.ocStep()
+        assert rel(top.getVars(), otop.designVars()) < 1e-6
+    assert abs(top.evaluateConstraints()[0]) < 1e-6

@@ -1,0 +1,535 @@
+// Fine-level (L0) kernels: matrix-free SIMP applyK, residual, coloured block
+// Gauss-Seidel, Young's moduli, compliance sensitivity and element energy.
+//
+// Node-centric gather, one thread per node: the (up to) 8 incident elements are
+// visited in the order of the reference's guarded stencil path
+// (TPSStencils.hh:577-659): element (i-a, j-b, k-c) for a, b, c in {0,1}, in which
+// the node has local index 4a+2b+c. K0 is a by-value kernel parameter (constant
+// bank); its symmetry lets every thread scan a column K0[:, row].
+#include "vfem_kernels.hpp"
+#include "vfem_reduce.cuh"
+
+namespace vfem {
+
+namespace {
+
+constexpr int BS = 256;
+
+__device__ __forceinline__ void decode_node(const Geom &g, int64_t n, int &i, int &j, int &k) {
+    k = (int)(n % g.nn[2]);
+    const int64_t t = n / g.nn[2];
+    j = (int)(t % g.nn[1]);
+    i = (int)(t / g.nn[1]);
+}
+
+// acc[r] (+/-)= E * sum_t K0[t][3*ln + r] * u_e[t] for element (ei,ej,ek).
+template <typename T, int LN>
+__device__ __forceinline__ void elem_rows(const Geom &g, const Mat24<T> &K, const T *__restrict__ u, int64_t base,
+                                          T &c0, T &c1, T &c2) {
+    const int64_t ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    c0 = c1 = c2 = T(0);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
+        const T u0 = u[nm], u1 = u[ld + nm], u2 = u[2 * ld + nm];
+        c0 += K.a[(3 * m + 0) * 24 + 3 * LN + 0] * u0;
+        c0 += K.a[(3 * m + 1) * 24 + 3 * LN + 0] * u1;
+        c0 += K.a[(3 * m + 2) * 24 + 3 * LN + 0] * u2;
+        c1 += K.a[(3 * m + 0) * 24 + 3 * LN + 1] * u0;
+        c1 += K.a[(3 * m + 1) * 24 + 3 * LN + 1] * u1;
+        c1 += K.a[(3 * m + 2) * 24 + 3 * LN + 1] * u2;
+        c2 += K.a[(3 * m + 0) * 24 + 3 * LN + 2] * u0;
+        c2 += K.a[(3 * m + 1) * 24 + 3 * LN + 2] * u1;
+        c2 += K.a[(3 * m + 2) * 24 + 3 * LN + 2] * u2;
+    }
+}
+
+template <typename T, int A, int B, int Cc, bool Negate>
+__device__ __forceinline__ void visit_elem(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y,
+                                           const T *__restrict__ u, int i, int j, int k, T &f0, T &f1, T &f2) {
+    const int ei = i - A, ej = j - B, ek = k - Cc;
+    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
+    const T E = Y[g.elem(ei, ej, ek)];
+    T c0, c1, c2;
+    elem_rows<T, 4 * A + 2 * B + Cc>(g, K, u, g.node(ei, ej, ek), c0, c1, c2);
+    if (Negate) { f0 -= E * c0; f1 -= E * c1; f2 -= E * c2; }
+    else        { f0 += E * c0; f1 += E * c1; f2 += E * c2; }
+}
+
+template <typename T, bool Negate>
+__device__ __forceinline__ void gather_ku(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y,
+                                          const T *__restrict__ u, int i, int j, int k, T &f0, T &f1, T &f2) {
+    visit_elem<T, 0, 0, 0, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 0, 0, 1, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 0, 1, 0, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 0, 1, 1, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 1, 0, 0, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 1, 0, 1, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 1, 1, 0, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+    visit_elem<T, 1, 1, 1, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+}
+
+template <typename T, bool ZeroInit, bool Negate, bool WithDot>
+__global__ void __launch_bounds__(BS) applyk_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
+                                                         T *__restrict__ out, const uint8_t *__restrict__ dmask,
+                                                         int zeroDir, double *__restrict__ partials,
+                                                         const Mat24<T> K) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    double dot = 0.0;
+    if (n < g.NN) {
+        int i, j, k;
+        decode_node(g, n, i, j, k);
+        const int64_t ld = g.ld;
+        if (j < g.nyv()) {
+            T f0 = ZeroInit ? T(0) : out[n];
+            T f1 = ZeroInit ? T(0) : out[ld + n];
+            T f2 = ZeroInit ? T(0) : out[2 * ld + n];
+            gather_ku<T, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+            if (zeroDir) {
+                const uint8_t dm = dmask[n];
+                if (dm & 1) f0 = T(0);
+                if (dm & 2) f1 = T(0);
+                if (dm & 4) f2 = T(0);
+            }
+            out[n] = f0;
+            out[ld + n] = f1;
+            out[2 * ld + n] = f2;
+            if (WithDot) dot = (double)u[n] * f0 + (double)u[ld + n] * f1 + (double)u[2 * ld + n] * f2;
+        } else if (ZeroInit) {
+            out[n] = T(0);
+            out[ld + n] = T(0);
+            out[2 * ld + n] = T(0);
+        }
+    }
+    if (WithDot) {
+        const double s = block_sum<BS>(dot);
+        if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    }
+}
+
+// r = b - K u (MultigridSolver.hh:527-541): b copied, stencil subtracted, Dirichlet zeroed.
+template <typename T>
+__global__ void __launch_bounds__(BS) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
+                                                           const T *__restrict__ b, T *__restrict__ r,
+                                                           const uint8_t *__restrict__ dmask, const Mat24<T> K) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (n >= g.NN) return;
+    int i, j, k;
+    decode_node(g, n, i, j, k);
+    const int64_t ld = g.ld;
+    T f0 = b[n], f1 = b[ld + n], f2 = b[2 * ld + n];
+    if (j < g.nyv()) gather_ku<T, true>(g, K, Y, u, i, j, k, f0, f1, f2);
+    const uint8_t dm = dmask[n];
+    if (dm & 1) f0 = T(0);
+    if (dm & 2) f1 = T(0);
+    if (dm & 4) f2 = T(0);
+    r[n] = f0;
+    r[ld + n] = f1;
+    r[2 * ld + n] = f2;
+}
+
+// Block Gauss-Seidel node update (MultigridSolver.hh:348-378).
+template <typename T>
+__device__ __forceinline__ void smooth_node_solve(uint8_t dm, T s0, T s1, T s2, const T *M, bool forward, T &u0, T &u1,
+                                                  T &u2) {
+    if (dm) {
+        T d[3] = {T(0), T(0), T(0)};
+        const T bs[3] = {s0, s1, s2};
+        if (forward) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
+                       (T(!((dm >> q) & 1)) / M[4 * q]);
+        } else {
+#pragma unroll
+            for (int q = 2; q >= 0; --q)
+                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
+                       (T(!((dm >> q) & 1)) / M[4 * q]);
+        }
+        u0 += d[0];
+        u1 += d[1];
+        u2 += d[2];
+    } else {
+        // adjugate inverse of the 3x3 diagonal block
+        const T c00 = M[4] * M[8] - M[5] * M[7];
+        const T c01 = M[5] * M[6] - M[3] * M[8];
+        const T c02 = M[3] * M[7] - M[4] * M[6];
+        const T det = M[0] * c00 + M[1] * c01 + M[2] * c02;
+        const T id = T(1) / det;
+        const T i00 = c00 * id, i01 = (M[2] * M[7] - M[1] * M[8]) * id, i02 = (M[1] * M[5] - M[2] * M[4]) * id;
+        const T i10 = c01 * id, i11 = (M[0] * M[8] - M[2] * M[6]) * id, i12 = (M[2] * M[3] - M[0] * M[5]) * id;
+        const T i20 = c02 * id, i21 = (M[1] * M[6] - M[0] * M[7]) * id, i22 = (M[0] * M[4] - M[1] * M[3]) * id;
+        u0 += i00 * s0 + i01 * s1 + i02 * s2;
+        u1 += i10 * s0 + i11 * s1 + i12 * s2;
+        u2 += i20 * s0 + i21 * s1 + i22 * s2;
+    }
+}
+
+template <typename T, int A, int B, int Cc>
+__device__ __forceinline__ void gs_visit(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y, const T *u, int i,
+                                         int j, int k, T &s0, T &s1, T &s2, T *M) {
+    const int ei = i - A, ej = j - B, ek = k - Cc;
+    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
+    constexpr int LN = 4 * A + 2 * B + Cc;
+    const T E = Y[g.elem(ei, ej, ek)];
+    T c0, c1, c2;
+    elem_rows<T, LN>(g, K, u, g.node(ei, ej, ek), c0, c1, c2);
+    s0 -= E * c0;
+    s1 -= E * c1;
+    s2 -= E * c2;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) M[3 * r + c] += E * K.a[(3 * LN + r) * 24 + 3 * LN + c];
+}
+
+// One colour (x%2, y%2, z%2) = (cx, cy, cz) of multicoloured block Gauss-Seidel
+// (MultigridSolver.hh:409-458); incident elements in elementsAdjacentNode order
+// (TPSStencils.hh:47-73).
+template <typename T>
+__global__ void __launch_bounds__(BS) gs_fine_color_kernel(Geom g, const T *__restrict__ Y, T *u,
+                                                           const T *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                           int cx, int cy, int cz, int forward, const Mat24<T> K) {
+    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
+    const int kk = (int)(t % n2);
+    const int64_t q = t / n2;
+    const int jj = (int)(q % n1), ii = (int)(q / n1);
+    const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    T M[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+    gs_visit<T, 1, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 0, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 1, 0, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 0, 0, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 1, 1, 0>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 0, 1, 0>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 1, 0, 0>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    gs_visit<T, 0, 0, 0>(g, K, Y, u, i, j, k, s0, s1, s2, M);
+    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    smooth_node_solve<T>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
+// ---------------- double-float FP64-accurate matvec ----------------
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ void df_split(double v, float &hi, float &lo) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+}
+
+// (sh, sl) += a*b with a = (ah, al), b = (bh, bl) (error-free product of the high parts)
+__device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float bl, float &sh, float &sl) {
+    const float p = ah * bh;
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = sh + p;
+    const float bp = t - sh;
+    const float err = (sh - (t - bp)) + (p - bp);
+    sh = t;
+    sl += err + e;
+}
+
+template <int LN>
+__device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const double *__restrict__ u, int64_t base,
+                                        float *ch, float *cl) {
+    const int64_t ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) { ch[r] = 0.f; cl[r] = 0.f; }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float uh, ul;
+            df_split(u[c * ld + nm], uh, ul);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                df_fma_acc(K.hi[(3 * m + c) * 24 + 3 * LN + r], K.lo[(3 * m + c) * 24 + 3 * LN + r], uh, ul, ch[r],
+                           cl[r]);
+        }
+    }
+}
+
+template <int A, int B, int Cc>
+__device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const double *__restrict__ Y,
+                                         const double *__restrict__ u, int i, int j, int k, float *fh, float *fl) {
+    const int ei = i - A, ej = j - B, ek = k - Cc;
+    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
+    float eh, el;
+    df_split(Y[g.elem(ei, ej, ek)], eh, el);
+    float ch[3], cl[3];
+    df_elem<4 * A + 2 * B + Cc>(g, K, u, g.node(ei, ej, ek), ch, cl);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        // normalise the element sum, then accumulate E * contrib
+        const float s = ch[r] + cl[r];
+        const float sl = cl[r] - (s - ch[r]);
+        df_fma_acc(eh, el, s, sl, fh[r], fl[r]);
+    }
+}
+
+__global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const double *__restrict__ Y,
+                                                            const double *__restrict__ u, double *__restrict__ out,
+                                                            const uint8_t *__restrict__ dmask, int zeroDir,
+                                                            double *__restrict__ partials, int withDot,
+                                                            const Mat24DF K) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    double dot = 0.0;
+    if (n < g.NN) {
+        int i, j, k;
+        decode_node(g, n, i, j, k);
+        const int64_t ld = g.ld;
+        double f[3] = {0.0, 0.0, 0.0};
+        if (j < g.nyv()) {
+            float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
+            df_visit<0, 0, 0>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<0, 0, 1>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<0, 1, 0>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<0, 1, 1>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<1, 0, 0>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<1, 0, 1>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<1, 1, 0>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<1, 1, 1>(g, K, Y, u, i, j, k, fh, fl);
+            const uint8_t dm = zeroDir ? dmask[n] : 0;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) f[r] = ((dm >> r) & 1) ? 0.0 : (double)fh[r] + (double)fl[r];
+            if (withDot) dot = u[n] * f[0] + u[ld + n] * f[1] + u[2 * ld + n] * f[2];
+        }
+        out[n] = f[0];
+        out[ld + n] = f[1];
+        out[2 * ld + n] = f[2];
+    }
+    if (withDot) {
+        const double s = block_sum<BS>(dot);
+        if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    }
+}
+
+// ---------------- element-wise kernels ----------------
+template <typename T>
+__global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restrict__ Y, double E0, double Emin,
+                             double gamma, double q, int law, int masking) {
+    const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (e >= g.NE) return;
+    const int ej = (int)((e / g.ne[2]) % g.ne[1]);
+    double v;
+    if (masking && ej >= g.firstMaskedE) {
+        v = 0.0;
+    } else {
+        const double r = rho[e];
+        if (law == 0) v = Emin + pow(r, gamma) * (E0 - Emin);
+        else v = Emin + r * (E0 - Emin) / (1 + q * (1 - r));
+    }
+    Y[e] = (T)v;
+}
+
+// TensorProductSimulator.hh:973-1005
+__global__ void __launch_bounds__(BS) compliance_grad_kernel(Geom g, const double *__restrict__ rho,
+                                                             const double *__restrict__ u, double *__restrict__ grad,
+                                                             double E0, double Emin, double gamma, double q, int law,
+                                                             double gx, double gy, double gz, double vol,
+                                                             const Mat24<double> K) {
+    const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (e >= g.NE) return;
+    const int ek = (int)(e % g.ne[2]);
+    const int64_t t = e / g.ne[2];
+    const int ej = (int)(t % g.ne[1]), ei = (int)(t / g.ne[1]);
+    if (ej >= g.firstMaskedE) { grad[e] = 0.0; return; }
+    const int64_t base = g.node(ei, ej, ek), ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    double ue[24];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
+        ue[3 * m] = u[nm];
+        ue[3 * m + 1] = u[ld + nm];
+        ue[3 * m + 2] = u[2 * ld + nm];
+    }
+    double uKu = 0.0;
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+        double acc = 0.0;
+#pragma unroll
+        for (int c = 0; c < 24; ++c) acc += K.a[r * 24 + c] * ue[c];
+        uKu += ue[r] * acc;
+    }
+    const double rh = rho[e];
+    double val;
+    if (law == 0) val = -0.5 * gamma * pow(rh, gamma - 1.0) * (E0 - Emin) * uKu;
+    else val = -0.5 * (1 + q) * (E0 - Emin) / ((1 + q * (1 - rh)) * (1 + q * (1 - rh))) * uKu;
+    if (gx != 0.0 || gy != 0.0 || gz != 0.0) {
+#pragma unroll
+        for (int l = 0; l < 8; ++l) val += 0.125 * (gx * ue[3 * l] + gy * ue[3 * l + 1] + gz * ue[3 * l + 2]) * vol;
+    }
+    grad[e] = val;
+}
+
+__global__ void __launch_bounds__(BS) element_energy_kernel(Geom g, const double *__restrict__ Y,
+                                                            const double *__restrict__ u, double *__restrict__ out,
+                                                            const Mat24<double> K) {
+    const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (e >= g.NE) return;
+    const int ek = (int)(e % g.ne[2]);
+    const int64_t t = e / g.ne[2];
+    const int ej = (int)(t % g.ne[1]), ei = (int)(t / g.ne[1]);
+    const int64_t base = g.node(ei, ej, ek), ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    double ue[24];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
+        ue[3 * m] = u[nm];
+        ue[3 * m + 1] = u[ld + nm];
+        ue[3 * m + 2] = u[2 * ld + nm];
+    }
+    double uKu = 0.0;
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+        double acc = 0.0;
+#pragma unroll
+        for (int c = 0; c < 24; ++c) acc += K.a[r * 24 + c] * ue[c];
+        uKu += ue[r] * acc;
+    }
+    out[e] = 0.5 * Y[e] * uKu;
+}
+
+// Self-weight load (TensorProductSimulator.hh:1275-1286) gathered per node.
+__global__ void gravity_load_kernel(Geom g, const double *__restrict__ rho, double *__restrict__ f, double gx,
+                                    double gy, double gz, double vol) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (n >= g.NN) return;
+    int i, j, k;
+    decode_node(g, n, i, j, k);
+    double acc0 = 0, acc1 = 0, acc2 = 0;
+    for (int a = 1; a >= 0; --a)
+        for (int b = 1; b >= 0; --b)
+            for (int c = 1; c >= 0; --c) {
+                const int ei = i - a, ej = j - b, ek = k - c;
+                if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) continue;
+                if (ej >= g.firstMaskedE) continue;
+                const double w = 0.125 * rho[g.elem(ei, ej, ek)] * vol;
+                acc0 += gx * w;
+                acc1 += gy * w;
+                acc2 += gz * w;
+            }
+    f[n] += acc0;
+    f[g.ld + n] += acc1;
+    f[2 * g.ld + n] += acc2;
+}
+
+template <typename T>
+__global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ dst, int64_t n) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t < n) dst[t] = (T)src[t];
+}
+
+}  // namespace
+
+template <typename T>
+void launch_young_moduli(const Geom &g, const double *rho, T *Y, double E0, double Emin, double gamma, double q,
+                         int law, bool masking, cudaStream_t st) {
+    young_kernel<T><<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, Y, E0, Emin, gamma, q, law, masking ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_convert(const void *src, bool srcDouble, T *dst, int64_t n, cudaStream_t st) {
+    if (!srcDouble) throw Error(ERR_ARG, "launch_convert expects an FP64 source");
+    convert_kernel<T><<<gridFor(n, BS), BS, 0, st>>>((const double *)src, dst, n);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat24<T> &K0, bool zeroInit, bool negate,
+                        const uint8_t *dmask, bool zeroDirichlet, double *partialDot, int partialBlocks,
+                        cudaStream_t st) {
+    const unsigned grid = gridFor(g.NN, BS);
+    const int zd = zeroDirichlet ? 1 : 0;
+    if (partialDot) {
+        if ((int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
+        applyk_fine_kernel<T, true, false, true><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, partialDot, K0);
+    } else if (zeroInit) {
+        if (negate) applyk_fine_kernel<T, true, true, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+        else applyk_fine_kernel<T, true, false, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+    } else {
+        if (negate) applyk_fine_kernel<T, false, true, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+        else applyk_fine_kernel<T, false, false, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+    }
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
+                          const uint8_t *dmask, cudaStream_t st) {
+    residual_fine_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
+                          const Mat24<T> &K0, cudaStream_t st) {
+    const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
+    const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
+    if (n1 <= 0) return;
+    gs_fine_color_kernel<T><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz, forward ? 1 : 0,
+                                                                       K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_applyk_fine_df(const Geom &g, const double *Y, const double *u, double *out, const Mat24DF &K0,
+                           const uint8_t *dmask, bool zeroDirichlet, double *partialDot, int partialBlocks,
+                           cudaStream_t st) {
+    const unsigned grid = gridFor(g.NN, BS);
+    if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
+    applyk_fine_df_kernel<<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zeroDirichlet ? 1 : 0, partialDot,
+                                               partialDot ? 1 : 0, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_compliance_gradient(const Geom &g, const double *rho, const double *u, double *grad,
+                                const Mat24<double> &K0, double E0, double Emin, double gamma, double q, int law,
+                                const double *grav, double vol, cudaStream_t st) {
+    compliance_grad_kernel<<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, u, grad, E0, Emin, gamma, q, law, grav[0],
+                                                             grav[1], grav[2], vol, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_element_energy(const Geom &g, const double *Y, const double *u, double *out, const Mat24<double> &K0,
+                           cudaStream_t st) {
+    element_energy_kernel<<<gridFor(g.NE, BS), BS, 0, st>>>(g, Y, u, out, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_build_gravity_load(const Geom &g, const double *rho, double *f, const double *grav, double vol,
+                               cudaStream_t st) {
+    gravity_load_kernel<<<gridFor(g.NN, BS), BS, 0, st>>>(g, rho, f, grav[0], grav[1], grav[2], vol);
+    VFEM_LAUNCH_CHECK();
+}
+
+#define VFEM_INST_FINE(T)                                                                                              \
+    template void launch_young_moduli<T>(const Geom &, const double *, T *, double, double, double, double, int, bool, \
+                                         cudaStream_t);                                                                \
+    template void launch_convert<T>(const void *, bool, T *, int64_t, cudaStream_t);                                   \
+    template void launch_applyk_fine<T>(const Geom &, const T *, const T *, T *, const Mat24<T> &, bool, bool,        \
+                                        const uint8_t *, bool, double *, int, cudaStream_t);                           \
+    template void launch_residual_fine<T>(const Geom &, const T *, const T *, const T *, T *, const Mat24<T> &,       \
+                                          const uint8_t *, cudaStream_t);                                              \
+    template void launch_gs_fine_color<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, bool,        \
+                                          const Mat24<T> &, cudaStream_t);
+VFEM_INST_FINE(double)
+VFEM_INST_FINE(float)
+
+}  // namespace vfem

@@ -1,0 +1,147 @@
+// Topology-optimisation element kernels: the reflecting linear/constant density
+// filter (TopologyOptimizationFilter.hh:285-400), the tanh Heaviside projection and
+// its derivative (:189-245) and the optimality-criteria update
+// (OptimalityCriterion.hh:64-83).
+#include <vector>
+
+#include "vfem_kernels.hpp"
+#include "vfem_reduce.cuh"
+
+namespace vfem {
+
+namespace {
+
+constexpr int BS = 256;
+
+__device__ __forceinline__ int reflect_index(int i, int s) {
+    // reflect across the min/max faces: -2,-1,0,1,2 -> 1,0,0,1,2 (repeated for narrow grids)
+    for (int guard = 0; guard < 64 && (i < 0 || i >= s); ++guard) {
+        if (i >= s) i = 2 * s - i - 1;
+        if (i < 0) i = -i - 1;
+    }
+    return i;
+}
+
+__global__ void __launch_bounds__(BS) smoothing_filter_kernel(int d0, int d1, int d2, const double *__restrict__ in,
+                                                              double *__restrict__ out, const int *__restrict__ offs,
+                                                              const double *__restrict__ w, int ntaps, double W) {
+    const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (e >= (int64_t)d0 * d1 * d2) return;
+    const int k = (int)(e % d2);
+    const int64_t t = e / d2;
+    const int j = (int)(t % d1), i = (int)(t / d1);
+    double acc = 0.0;
+    for (int q = 0; q < ntaps; ++q) {
+        const int ni = reflect_index(i + offs[3 * q], d0);
+        const int nj = reflect_index(j + offs[3 * q + 1], d1);
+        const int nk = reflect_index(k + offs[3 * q + 2], d2);
+        acc += w[q] * in[((int64_t)ni * d1 + nj) * d2 + nk];
+    }
+    out[e] = acc / W;
+}
+
+__global__ void projection_kernel(int64_t n, double beta, double th, const double *__restrict__ in,
+                                  double *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (i < n) out[i] = (th + tanh(beta * (in[i] - 0.5))) / (2 * th);
+}
+
+__global__ void projection_backprop_kernel(int64_t n, double beta, double scale, const double *__restrict__ in,
+                                           const double *__restrict__ vars, double *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (i < n) {
+        const double t = tanh(beta * (vars[i] - 0.5));
+        out[i] = in[i] * (1.0 - t * t) * scale;
+    }
+}
+
+__global__ void oc_update_kernel(int64_t n, const double *__restrict__ x0, const double *__restrict__ dJ,
+                                 const double *__restrict__ dc, double lambda, double m, double p,
+                                 double *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (i >= n) return;
+    const double x = x0[i];
+    const double raw = x * pow(dJ[i] / (dc[i] * lambda), p);
+    double r = fmin(fmax(fmin(fmax(raw, x - m), x + m), 0.0), 1.0);
+    // fmin/fmax would drop a NaN; the reference keeps x0 for a non-finite update
+    // (an infinite update is clamped to x0 + m, which is finite).
+    if (isnan(raw)) r = x;
+    out[i] = r;
+}
+
+__global__ void __launch_bounds__(BS) sum_kernel(const double *__restrict__ x, int64_t n, double *__restrict__ partials) {
+    double acc = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) acc += x[t];
+    const double s = block_sum<BS>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+struct TapCache {
+    int radius = -1, type = -1;
+    DevBuf<int> offs;
+    DevBuf<double> w;
+    int ntaps = 0;
+    double W = 0;
+};
+
+thread_local TapCache g_taps;
+
+}  // namespace
+
+void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st) {
+    if (radius < 0) throw Error(ERR_ARG, "negative filter radius");
+    if (g_taps.radius != radius || g_taps.type != type) {
+        std::vector<int> offs;
+        std::vector<double> ws;
+        const double rp1 = 1.0 + radius;
+        double W = 0;
+        for (int a = -radius; a <= radius; ++a)
+            for (int b = -radius; b <= radius; ++b)
+                for (int c = -radius; c <= radius; ++c) {
+                    const double w = type == 1 ? rp1 - std::sqrt((double)(a * a + b * b + c * c)) : 1.0;
+                    if (w <= 0) continue;
+                    offs.push_back(a);
+                    offs.push_back(b);
+                    offs.push_back(c);
+                    ws.push_back(w);
+                    W += w;
+                }
+        g_taps.offs.alloc(offs.size());
+        g_taps.w.alloc(ws.size());
+        VFEM_CUDA(cudaMemcpy(g_taps.offs.p, offs.data(), offs.size() * sizeof(int), cudaMemcpyHostToDevice));
+        VFEM_CUDA(cudaMemcpy(g_taps.w.p, ws.data(), ws.size() * sizeof(double), cudaMemcpyHostToDevice));
+        g_taps.ntaps = (int)ws.size();
+        g_taps.W = W;
+        g_taps.radius = radius;
+        g_taps.type = type;
+    }
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+    smoothing_filter_kernel<<<gridFor(n, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], in, out, g_taps.offs.p,
+                                                           g_taps.w.p, g_taps.ntaps, g_taps.W);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_projection(int64_t n, double beta, const double *in, double *out, cudaStream_t st) {
+    projection_kernel<<<gridFor(n, BS), BS, 0, st>>>(n, beta, std::tanh(0.5 * beta), in, out);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out,
+                                cudaStream_t st) {
+    const double scale = 1.0 / (2 * std::tanh(0.5 * beta) / beta);
+    projection_backprop_kernel<<<gridFor(n, BS), BS, 0, st>>>(n, beta, scale, in, vars, out);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_oc_update(int64_t n, const double *x0, const double *dJ, const double *dc, double lambda, double m,
+                      double p, double *out, cudaStream_t st) {
+    oc_update_kernel<<<gridFor(n, BS), BS, 0, st>>>(n, x0, dJ, dc, lambda, m, p, out);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_sum_partials(const double *x, int64_t n, double *partials, cudaStream_t st) {
+    sum_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(x, n, partials);
+    VFEM_LAUNCH_CHECK();
+}
+
+}  // namespace vfem

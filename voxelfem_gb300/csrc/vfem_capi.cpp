@@ -1,0 +1,358 @@
+// extern "C" boundary over the host engine; see include/vfem.h.
+#include "../../include/vfem.h"
+
+#include <cstring>
+#include <string>
+
+#include "vfem_engine.hpp"
+
+using namespace vfem;
+
+struct vfem_grid {
+    Grid g;
+    vfem_grid(const int ne[3], const double mn[3], const double mx[3]) : g(ne, mn, mx) {}
+};
+struct vfem_mg {
+    MG m;
+    vfem_mg(Grid *g, int l) : m(g, l) {}
+};
+struct vfem_problem {
+    Problem p;
+    vfem_problem(MG *m, const std::vector<FilterSpec> &f, double v) : p(m, f, v) {}
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        f();
+        return VFEM_OK;
+    } catch (const vfem::Error &e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::exception &e) {
+        g_last_error = e.what();
+        return VFEM_ERR_ARG;
+    } catch (...) {
+        g_last_error = "unknown error";
+        return VFEM_ERR_ARG;
+    }
+}
+
+void need(const void *p, const char *what) {
+    if (!p) throw Error(ERR_ARG, std::string("null ") + what);
+}
+}  // namespace
+
+extern "C" {
+
+const char *vfem_last_error(void) { return g_last_error.c_str(); }
+int vfem_version(void) { return 1; }
+int vfem_device_synchronize(void) {
+    return guarded([&] { VFEM_CUDA(cudaDeviceSynchronize()); });
+}
+
+int vfem_grid_create(const int64_t elems[3], const double bbox_min[3], const double bbox_max[3], vfem_grid **out) {
+    return guarded([&] {
+        need(elems, "elems"); need(bbox_min, "bbox"); need(bbox_max, "bbox"); need(out, "out");
+        int ne[3];
+        for (int d = 0; d < 3; ++d) {
+            if (elems[d] <= 0 || elems[d] > (1 << 20)) throw Error(ERR_ARG, "invalid elementsPerDimension");
+            ne[d] = (int)elems[d];
+        }
+        *out = new vfem_grid(ne, bbox_min, bbox_max);
+    });
+}
+int vfem_grid_destroy(vfem_grid *g) {
+    return guarded([&] { delete g; });
+}
+int vfem_grid_dims(const vfem_grid *g, int64_t elems[3], int64_t *num_nodes, int64_t *num_elements) {
+    return guarded([&] {
+        need(g, "grid");
+        for (int d = 0; d < 3; ++d) elems[d] = g->g.g.ne[d];
+        if (num_nodes) *num_nodes = g->g.g.NN;
+        if (num_elements) *num_elements = g->g.g.NE;
+    });
+}
+int vfem_grid_set_etensor(vfem_grid *g, double young, double poisson) {
+    return guarded([&] { need(g, "grid"); g->g.setETensor(young, poisson); });
+}
+int vfem_grid_get_etensor(const vfem_grid *g, double *young, double *poisson) {
+    return guarded([&] { need(g, "grid"); *young = g->g.Eyoung; *poisson = g->g.nu; });
+}
+int vfem_grid_get_k0(const vfem_grid *g, double *out576) {
+    return guarded([&] { need(g, "grid"); need(out576, "out"); std::memcpy(out576, g->g.K0.a, 576 * sizeof(double)); });
+}
+int vfem_grid_set_material_params(vfem_grid *g, double E0, double Emin, double gamma, double q, int law) {
+    return guarded([&] {
+        need(g, "grid");
+        if (law != 0 && law != 1) throw Error(ERR_ARG, "unknown interpolation law");
+        g->g.setParams(E0, Emin, gamma, q, law);
+        VFEM_CUDA(cudaStreamSynchronize(g->g.stream));
+    });
+}
+int vfem_grid_get_material_params(const vfem_grid *g, double *E0, double *Emin, double *gamma, double *q, int *law) {
+    return guarded([&] {
+        need(g, "grid");
+        *E0 = g->g.E0; *Emin = g->g.Emin; *gamma = g->g.gamma; *q = g->g.q; *law = g->g.law;
+    });
+}
+int vfem_grid_set_densities(vfem_grid *g, const double *rho) {
+    return guarded([&] { need(g, "grid"); need(rho, "rho"); g->g.setDensities(rho, false); });
+}
+int vfem_grid_get_densities(vfem_grid *g, double *rho_out) {
+    return guarded([&] { need(g, "grid"); need(rho_out, "out"); g->g.getDensities(rho_out); });
+}
+int vfem_grid_set_uniform_densities(vfem_grid *g, double value) {
+    return guarded([&] { need(g, "grid"); g->g.setUniformDensities(value); });
+}
+int vfem_grid_get_young_moduli(vfem_grid *g, double *out) {
+    return guarded([&] { need(g, "grid"); need(out, "out"); g->g.getYoungModuli(out); });
+}
+int vfem_grid_add_dirichlet(vfem_grid *g, const double u[3], const double min_corner[3], const double max_corner[3],
+                            uint32_t component_mask) {
+    return guarded([&] {
+        need(g, "grid"); need(u, "u"); need(min_corner, "minCorner"); need(max_corner, "maxCorner");
+        if (component_mask > 7) throw Error(ERR_ARG, "invalid component mask");
+        g->g.addDirichlet(u, min_corner, max_corner, component_mask);
+    });
+}
+int vfem_grid_apply_symmetry(vfem_grid *g, const int axes[3], const int max_face[3]) {
+    return guarded([&] { need(g, "grid"); need(axes, "axes"); need(max_face, "maxFace"); g->g.applySymmetry(axes, max_face); });
+}
+int vfem_grid_set_nodal_forces(vfem_grid *g, const double *forces) {
+    return guarded([&] { need(g, "grid"); need(forces, "forces"); g->g.setForces(forces); });
+}
+int vfem_grid_get_dirichlet_mask(const vfem_grid *g, uint8_t *mask_out) {
+    return guarded([&] { need(g, "grid"); need(mask_out, "out"); g->g.getDirichletMask(mask_out); });
+}
+int vfem_grid_set_gravity(vfem_grid *g, const double gravity[3]) {
+    return guarded([&] { need(g, "grid"); need(gravity, "gravity"); g->g.setGravity(gravity); });
+}
+int vfem_grid_get_gravity(const vfem_grid *g, double gravity[3]) {
+    return guarded([&] { need(g, "grid"); for (int c = 0; c < 3; ++c) gravity[c] = g->g.grav[c]; });
+}
+int vfem_grid_set_mask_layer(vfem_grid *g, int64_t layer) {
+    return guarded([&] {
+        need(g, "grid");
+        g->g.setMaskLayer(layer);
+        VFEM_CUDA(cudaStreamSynchronize(g->g.stream));
+    });
+}
+int vfem_grid_get_mask_height(const vfem_grid *g, double *height) {
+    return guarded([&] { need(g, "grid"); *height = g->g.maskH; });
+}
+int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.applyK(u, out); });
+}
+int vfem_grid_build_load(vfem_grid *g, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.buildLoad(out); });
+}
+int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_out) {
+    return guarded([&] { need(g, "grid"); g->g.complianceGradient(u, grad_out); });
+}
+int vfem_grid_element_energy(vfem_grid *g, const double *u, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.elementEnergy(u, out); });
+}
+
+int vfem_mg_create(vfem_grid *g, int num_coarsening_levels, vfem_mg **out) {
+    return guarded([&] { need(g, "grid"); need(out, "out"); *out = new vfem_mg(&g->g, num_coarsening_levels); });
+}
+int vfem_mg_destroy(vfem_mg *mg) {
+    return guarded([&] { delete mg; });
+}
+int vfem_mg_num_levels(const vfem_mg *mg, int *levels) {
+    return guarded([&] { need(mg, "mg"); *levels = mg->m.L(); });
+}
+int vfem_mg_level_dims(const vfem_mg *mg, int level, int64_t elems[3]) {
+    return guarded([&] {
+        need(mg, "mg");
+        if (level < 0 || level >= mg->m.L()) throw Error(ERR_ARG, "level out of range");
+        for (int d = 0; d < 3; ++d) elems[d] = mg->m.lv[level].g.ne[d];
+    });
+}
+int vfem_mg_level_dirichlet_mask(const vfem_mg *mg, int level, uint8_t *mask_out) {
+    return guarded([&] {
+        need(mg, "mg");
+        if (level < 0 || level >= mg->m.L()) throw Error(ERR_ARG, "level out of range");
+        const std::vector<uint8_t> &m = level == 0 ? mg->m.fine->dmask_h : mg->m.lv[level].dmask_h;
+        std::memcpy(mask_out, m.data(), m.size());
+    });
+}
+int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec) {
+    return guarded([&] {
+        need(mg, "mg");
+        if (outer_matvec != MATVEC_FP64 && outer_matvec != MATVEC_DF) throw Error(ERR_ARG, "unknown matvec kind");
+        mg->m.setPrecision(precision);
+        if (mg->m.outerMatvec != outer_matvec) mg->m.clearGraphs();
+        mg->m.outerMatvec = outer_matvec;
+    });
+}
+int vfem_mg_set_use_graphs(vfem_mg *mg, int use) {
+    return guarded([&] { need(mg, "mg"); mg->m.useGraphs = use != 0; mg->m.clearGraphs(); });
+}
+int vfem_mg_set_symmetric_gs(vfem_mg *mg, int symmetric) {
+    return guarded([&] { need(mg, "mg"); mg->m.symmetricGS = symmetric != 0; });
+}
+int vfem_mg_set_mask_layer(vfem_mg *mg, int64_t layer) {
+    return guarded([&] {
+        need(mg, "mg");
+        mg->m.setMaskLayer(layer);
+        VFEM_CUDA(cudaStreamSynchronize(mg->m.fine->stream));
+    });
+}
+int vfem_mg_update_stiffness(vfem_mg *mg) {
+    return guarded([&] { need(mg, "mg"); mg->m.updateStiffness(); });
+}
+int vfem_mg_apply_k(vfem_mg *mg, int level, const double *u, double *out) {
+    return guarded([&] { need(mg, "mg"); mg->m.applyK(level, u, out); });
+}
+int vfem_mg_residual(vfem_mg *mg, int level, const double *u, const double *b, double *r_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.residual(level, u, b, r_out); });
+}
+int vfem_mg_smooth(vfem_mg *mg, int level, double *u_inout, const double *b, int forward) {
+    return guarded([&] { need(mg, "mg"); mg->m.smooth(level, u_inout, b, forward != 0); });
+}
+int vfem_mg_restrict(vfem_mg *mg, int level, const double *fine, double *coarse_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.restrictTo(level, fine, coarse_out); });
+}
+int vfem_mg_interpolate(vfem_mg *mg, int level, const double *coarse, double *fine_inout, int accumulate) {
+    return guarded([&] { need(mg, "mg"); mg->m.interpolate(level, coarse, fine_inout, accumulate != 0); });
+}
+int vfem_mg_coarse_solve(vfem_mg *mg, const double *b, double *x_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.coarseSolve(b, x_out); });
+}
+int vfem_mg_zero_dirichlet(vfem_mg *mg, int level, double *u_inout) {
+    return guarded([&] { need(mg, "mg"); mg->m.zeroDirichlet(level, u_inout); });
+}
+int vfem_mg_solve(vfem_mg *mg, const double *u, const double *f, int64_t num_steps, int64_t num_smoothing_steps,
+                  int zero_dirichlet, int full_multigrid, double *x_out) {
+    return guarded([&] {
+        need(mg, "mg");
+        mg->m.solve(u, f, num_steps, num_smoothing_steps, zero_dirichlet != 0, full_multigrid != 0, x_out);
+    });
+}
+int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter, double tol, int64_t mg_iterations,
+                int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
+                vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats) {
+    return guarded([&] {
+        need(mg, "mg"); need(x_inout, "x"); need(b, "b");
+        if (max_iter < 0 || mg_iterations < 0 || mg_smoothing_iterations < 0) throw Error(ERR_ARG, "negative count");
+        PcgStats s = mg->m.pcg(x_inout, b, max_iter, tol, mg_iterations, mg_smoothing_iterations, full_multigrid != 0,
+                               dirichlet_already_satisfied != 0, cb, user);
+        if (stats) {
+            stats->iterations = s.iterations;
+            stats->relres = s.relres;
+            stats->rsq = s.rsq;
+            stats->bnorm2 = s.bnorm2;
+        }
+    });
+}
+
+int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out) {
+    return guarded([&] {
+        need(dims, "dims");
+        int d[3];
+        for (int i = 0; i < 3; ++i) {
+            if (dims[i] <= 0) throw Error(ERR_ARG, "invalid dims");
+            d[i] = (int)dims[i];
+        }
+        if (type != 0 && type != 1) throw Error(ERR_ARG, "Unexpected smoothing kernel type");
+        const int64_t n = (int64_t)d[0] * d[1] * d[2];
+        cudaStream_t st = nullptr;
+        View vi, vo;
+        viewIn(vi, in, n * sizeof(double), st);
+        viewOut(vo, out, n * sizeof(double));
+        launch_smoothing_filter(d, radius, type, (const double *)vi.d, (double *)vo.d, st);
+        finishOut(vo, st);
+    });
+}
+int vfem_projection_apply(int64_t n, double beta, const double *in, double *out) {
+    return guarded([&] {
+        if (!(beta > 0)) throw Error(ERR_ARG, "Beta parameter has to be positive");
+        View vi, vo;
+        viewIn(vi, in, n * sizeof(double), nullptr);
+        viewOut(vo, out, n * sizeof(double));
+        launch_projection(n, beta, (const double *)vi.d, (double *)vo.d, nullptr);
+        finishOut(vo, nullptr);
+    });
+}
+int vfem_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out) {
+    return guarded([&] {
+        if (!(beta > 0)) throw Error(ERR_ARG, "Beta parameter has to be positive");
+        View vi, vv, vo;
+        viewIn(vi, in, n * sizeof(double), nullptr);
+        viewIn(vv, vars, n * sizeof(double), nullptr);
+        viewOut(vo, out, n * sizeof(double));
+        launch_projection_backprop(n, beta, (const double *)vi.d, (const double *)vv.d, (double *)vo.d, nullptr);
+        finishOut(vo, nullptr);
+    });
+}
+
+int vfem_problem_create(vfem_mg *mg, int num_filters, const int *kinds, const int *radii, const int *types,
+                        const double *betas, double volume_fraction, vfem_problem **out) {
+    return guarded([&] {
+        need(mg, "mg"); need(out, "out");
+        std::vector<FilterSpec> f;
+        for (int i = 0; i < num_filters; ++i) f.push_back({kinds[i], radii[i], types[i], betas[i]});
+        *out = new vfem_problem(&mg->m, f, volume_fraction);
+    });
+}
+int vfem_problem_destroy(vfem_problem *p) {
+    return guarded([&] { delete p; });
+}
+int vfem_problem_set_solver(vfem_problem *p, int64_t cg_iter, double tol, int64_t mg_iterations,
+                            int64_t mg_smoothing_iterations, int full_multigrid, int zero_init) {
+    return guarded([&] {
+        need(p, "problem");
+        p->p.cgIter = cg_iter; p->p.tol = tol; p->p.mgIter = mg_iterations; p->p.mgSweeps = mg_smoothing_iterations;
+        p->p.fmg = full_multigrid != 0; p->p.zeroInit = zero_init != 0;
+    });
+}
+int vfem_problem_set_vars(vfem_problem *p, const double *x) {
+    return guarded([&] { need(p, "problem"); need(x, "x"); p->p.setVars(x, isDevicePtr(x)); });
+}
+int vfem_problem_get_vars(vfem_problem *p, double *x_out) {
+    return guarded([&] {
+        need(p, "problem");
+        VFEM_CUDA(cudaMemcpy(x_out, p->p.vars[0].p, p->p.grid->g.NE * sizeof(double), cudaMemcpyDefault));
+    });
+}
+int vfem_problem_objective(vfem_problem *p, double *value) {
+    return guarded([&] { need(p, "problem"); *value = p->p.objective(); });
+}
+int vfem_problem_gradient(vfem_problem *p, double *grad_out) {
+    return guarded([&] { need(p, "problem"); p->p.gradient(grad_out, isDevicePtr(grad_out)); });
+}
+int vfem_problem_constraint(vfem_problem *p, double *value) {
+    return guarded([&] { need(p, "problem"); *value = p->p.constraint(); });
+}
+int vfem_problem_jacobian(vfem_problem *p, double *jac_out) {
+    return guarded([&] { need(p, "problem"); p->p.jacobian(jac_out, isDevicePtr(jac_out)); });
+}
+int vfem_problem_get_u(vfem_problem *p, double *u_out) {
+    return guarded([&] { need(p, "problem"); p->p.getU(u_out, isDevicePtr(u_out)); });
+}
+int vfem_problem_get_physical(vfem_problem *p, double *x_out) {
+    return guarded([&] { need(p, "problem"); p->p.getPhysical(x_out, isDevicePtr(x_out)); });
+}
+int vfem_problem_last_solve(vfem_problem *p, vfem_pcg_stats *stats) {
+    return guarded([&] {
+        need(p, "problem");
+        stats->iterations = p->p.lastStats.iterations;
+        stats->relres = p->p.lastStats.relres;
+        stats->rsq = p->p.lastStats.rsq;
+        stats->bnorm2 = p->p.lastStats.bnorm2;
+    });
+}
+int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, int64_t *probes) {
+    return guarded([&] {
+        need(p, "problem");
+        const int64_t n = p->p.ocStep(m, pexp, ctol);
+        if (probes) *probes = n;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Common device/host helpers for the VoxelFEM GB300 kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace vfem {
+
+// Error carrying a status code back through the C ABI.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+enum Status { OK = 0, ERR_ARG = 1, ERR_CUDA = 2, ERR_NAN = 3, ERR_STATE = 4, ERR_NOT_SPD = 5 };
+
+inline void cudaCheck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define VFEM_CUDA(x) ::vfem::cudaCheck((x), #x)
+#define VFEM_LAUNCH_CHECK() ::vfem::cudaCheck(cudaGetLastError(), "kernel launch")
+
+constexpr int BUILD_DIR = 1;         // layers are stacked along y (TensorProductSimulator.hh:1851)
+constexpr int64_t LAYER_MASK_NONE = 2147483647;
+constexpr int MARGIN = 4;            // detached-node margin copied with b (MultigridSolver.hh:532)
+constexpr int NUM_SMS = 152;
+
+// Geometry of one level of the voxel hierarchy (Q1 hexahedra).
+struct Geom {
+    int ne[3];       // elements per axis
+    int nn[3];       // nodes per axis = ne + 1
+    int64_t NE, NN;  // element / node counts
+    int64_t ld;      // leading dimension of a nodal SoA vector (component stride), padded
+    int firstMaskedE;  // first masked element layer along y (or LAYER_MASK_NONE)
+    int firstDetN;     // first detached node layer along y
+    __host__ __device__ int nyv() const { return firstDetN < nn[1] ? firstDetN : nn[1]; }  // nondetached node rows
+    __host__ __device__ int nev() const { return firstMaskedE < ne[1] ? firstMaskedE : ne[1]; }
+    __host__ __device__ int64_t node(int i, int j, int k) const { return ((int64_t)i * nn[1] + j) * nn[2] + k; }
+    __host__ __device__ int64_t elem(int i, int j, int k) const { return ((int64_t)i * ne[1] + j) * ne[2] + k; }
+};
+
+inline int64_t padTo(int64_t n, int64_t a) { return (n + a - 1) / a * a; }
+
+inline Geom makeGeom(const int ne[3]) {
+    Geom g;
+    for (int d = 0; d < 3; ++d) { g.ne[d] = ne[d]; g.nn[d] = ne[d] + 1; }
+    g.NE = (int64_t)ne[0] * ne[1] * ne[2];
+    g.NN = (int64_t)g.nn[0] * g.nn[1] * g.nn[2];
+    g.ld = g.NN;  // SoA component stride: exactly the (nn, 3) column-major VField layout
+    g.firstMaskedE = (int)LAYER_MASK_NONE;
+    g.firstDetN = (int)LAYER_MASK_NONE;
+    return g;
+}
+
+inline unsigned gridFor(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 2147483647LL) g = 2147483647LL;
+    return (unsigned)g;
+}
+
+// Owning device buffer.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count) VFEM_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+}  // namespace vfem

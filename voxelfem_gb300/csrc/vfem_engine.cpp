@@ -1,0 +1,1137 @@
+// Host engine: grid state, multigrid hierarchy, MG-preconditioned CG and the
+// topology-optimisation problem. See vfem_engine.hpp.
+#include "vfem_engine.hpp"
+
+#include <algorithm>
+#include <cstring>
+
+#include "vfem_element.hpp"
+
+namespace vfem {
+
+// ---------------------------------------------------------------------------
+// caller-memory views
+// ---------------------------------------------------------------------------
+bool isDevicePtr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void viewIn(View &v, const void *p, size_t bytes, cudaStream_t st) {
+    if (!p && bytes) throw Error(ERR_ARG, "null input pointer");
+    v.user = const_cast<void *>(p);
+    v.bytes = bytes;
+    if (isDevicePtr(p)) {
+        v.d = const_cast<void *>(p);
+        v.staged = false;
+    } else {
+        v.tmp.alloc(bytes);
+        v.d = v.tmp.p;
+        v.staged = true;
+        if (bytes) VFEM_CUDA(cudaMemcpyAsync(v.d, p, bytes, cudaMemcpyHostToDevice, st));
+    }
+}
+
+void viewOut(View &v, void *p, size_t bytes) {
+    if (!p && bytes) throw Error(ERR_ARG, "null output pointer");
+    v.user = p;
+    v.bytes = bytes;
+    if (isDevicePtr(p)) {
+        v.d = p;
+        v.staged = false;
+    } else {
+        v.tmp.alloc(bytes);
+        v.d = v.tmp.p;
+        v.staged = true;
+    }
+}
+
+void viewInOut(View &v, void *p, size_t bytes, cudaStream_t st) {
+    viewIn(v, p, bytes, st);
+}
+
+void finishOut(View &v, cudaStream_t st) {
+    if (v.staged && v.bytes) VFEM_CUDA(cudaMemcpyAsync(v.user, v.d, v.bytes, cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---------------------------------------------------------------------------
+// Grid (TensorProductSimulator<double, 1, 1, 1>)
+// ---------------------------------------------------------------------------
+Grid::Grid(const int ne[3], const double bmin_[3], const double bmax_[3]) {
+    for (int d = 0; d < 3; ++d) {
+        if (ne[d] <= 0) throw Error(ERR_ARG, "elementsPerDimension must be positive");
+        if (!(bmax_[d] > bmin_[d])) throw Error(ERR_ARG, "invalid domain bounding box");
+        bmin[d] = bmin_[d];
+        bmax[d] = bmax_[d];
+        h[d] = (bmax[d] - bmin[d]) / ne[d];
+    }
+    g = makeGeom(ne);
+    VFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    rho.alloc(g.NE);
+    Y.alloc(g.NE);
+    VFEM_CUDA(cudaMemsetAsync(rho.p, 0, rho.bytes(), stream));  // NDVector zero-initialises densities
+    dmask_h.assign(g.NN, 0);
+    dval_h.assign(3 * g.NN, 0.0);
+    force_h.assign(3 * g.NN, 0.0);
+    dmask.alloc(g.NN);
+    dval.alloc(3 * g.NN);
+    uploadBC();
+    setETensor(1.0, 0.0);
+    updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+Grid::~Grid() {
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void Grid::setETensor(double E, double nu_) {
+    if (!(nu_ < 0.5) || !(nu_ > -1.0)) throw Error(ERR_ARG, "Poisson ratio must lie in (-1, 0.5)");
+    Eyoung = E;
+    nu = nu_;
+    element_stiffness(E, nu, h, K0.a);
+    for (int t = 0; t < 576; ++t) {
+        K0f.a[t] = (float)K0.a[t];
+        K0df.hi[t] = (float)K0.a[t];
+        K0df.lo[t] = (float)(K0.a[t] - (double)K0df.hi[t]);
+    }
+    ++densVersion;  // stiffness depends on K0
+}
+
+void Grid::setParams(double E0_, double Emin_, double gamma_, double q_, int law_) {
+    E0 = E0_;
+    Emin = Emin_;
+    gamma = gamma_;
+    q = q_;
+    law = law_;
+    updateYoungModuli();
+}
+
+void Grid::updateYoungModuli() {
+    const bool masking = maskH < bmax[BUILD_DIR];
+    launch_young_moduli<double>(g, rho.p, Y.p, E0, Emin, gamma, q, law, masking, stream);
+    YfValid = false;
+    ++densVersion;
+}
+
+const float *Grid::youngF() {
+    if (!YfValid) {
+        Yf.alloc(g.NE);
+        const bool masking = maskH < bmax[BUILD_DIR];
+        launch_young_moduli<float>(g, rho.p, Yf.p, E0, Emin, gamma, q, law, masking, stream);
+        YfValid = true;
+    }
+    return Yf.p;
+}
+
+void Grid::setDensities(const double *r, bool checkRange) {
+    if (checkRange) {
+        std::vector<double> hostCopy(g.NE);
+        if (isDevicePtr(r)) VFEM_CUDA(cudaMemcpy(hostCopy.data(), r, g.NE * sizeof(double), cudaMemcpyDeviceToHost));
+        else std::memcpy(hostCopy.data(), r, g.NE * sizeof(double));
+        for (double v : hostCopy)
+            if (v > 1.0 || v < 0.0) throw Error(ERR_ARG, "Density value has to be in between 0 and 1");
+    }
+    VFEM_CUDA(cudaMemcpyAsync(rho.p, r, g.NE * sizeof(double), cudaMemcpyDefault, stream));
+    updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::setUniformDensities(double v) {
+    if (v > 1.0 || v < 0.0) throw Error(ERR_ARG, "Density value has to be in between 0 and 1");
+    std::vector<double> hv(g.NE, v);
+    VFEM_CUDA(cudaMemcpyAsync(rho.p, hv.data(), g.NE * sizeof(double), cudaMemcpyHostToDevice, stream));
+    updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::getDensities(double *out) {
+    VFEM_CUDA(cudaMemcpyAsync(out, rho.p, g.NE * sizeof(double), cudaMemcpyDefault, stream));
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::getYoungModuli(double *out) {
+    VFEM_CUDA(cudaMemcpyAsync(out, Y.p, g.NE * sizeof(double), cudaMemcpyDefault, stream));
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::uploadBC() {
+    VFEM_CUDA(cudaMemcpyAsync(dmask.p, dmask_h.data(), g.NN, cudaMemcpyHostToDevice, stream));
+    VFEM_CUDA(cudaMemcpyAsync(dval.p, dval_h.data(), 3 * g.NN * sizeof(double), cudaMemcpyHostToDevice, stream));
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+    dvalNonzero = std::any_of(dval_h.begin(), dval_h.end(), [](double v) { return v != 0.0; });
+    ++bcVersion;
+}
+
+// TensorProductSimulator.hh:241-252 with BCBuilder::setDirichlet (:73-88).
+void Grid::addDirichlet(const double u[3], const double mn[3], const double mx[3], unsigned cmask) {
+    std::vector<uint8_t> m = dmask_h;
+    std::vector<double> v = dval_h;
+    const int64_t NN = g.NN;
+    for (int i = 0; i < g.nn[0]; ++i) {
+        const double px = bmin[0] + i * h[0];
+        if (px < mn[0] || px > mx[0]) continue;
+        for (int j = 0; j < g.nn[1]; ++j) {
+            const double py = bmin[1] + j * h[1];
+            if (py < mn[1] || py > mx[1]) continue;
+            for (int k = 0; k < g.nn[2]; ++k) {
+                const double pz = bmin[2] + k * h[2];
+                if (pz < mn[2] || pz > mx[2]) continue;
+                const int64_t n = g.node(i, j, k);
+                for (int c = 0; c < 3; ++c) {
+                    if (!((cmask >> c) & 1)) continue;
+                    if (!((m[n] >> c) & 1)) {
+                        m[n] |= (uint8_t)(1u << c);
+                        v[c * NN + n] = u[c];
+                    } else if (std::abs(v[c * NN + n] - u[c]) > 1e-10) {
+                        throw Error(ERR_ARG, "Conflicting dirichlet displacements.");
+                    }
+                }
+            }
+        }
+    }
+    dmask_h.swap(m);
+    dval_h.swap(v);
+    uploadBC();
+}
+
+// TensorProductSimulator.hh:2042-2053
+void Grid::applySymmetry(const int axes[3], const int maxFace[3]) {
+    for (int64_t n = 0; n < g.NN; ++n) {
+        const int k = (int)(n % g.nn[2]);
+        const int j = (int)((n / g.nn[2]) % g.nn[1]);
+        const int i = (int)(n / ((int64_t)g.nn[1] * g.nn[2]));
+        const int idx[3] = {i, j, k};
+        for (int d = 0; d < 3; ++d) {
+            if (!axes[d]) continue;
+            const double p = bmin[d] + idx[d] * h[d];
+            if (std::abs(p - (maxFace[d] ? bmax[d] : bmin[d])) < 1e-10) {
+                dmask_h[n] |= (uint8_t)(1u << d);
+                dval_h[d * g.NN + n] = 0.0;
+            }
+        }
+    }
+    uploadBC();
+}
+
+void Grid::setForces(const double *f) {
+    if (isDevicePtr(f)) VFEM_CUDA(cudaMemcpy(force_h.data(), f, 3 * g.NN * sizeof(double), cudaMemcpyDeviceToHost));
+    else std::memcpy(force_h.data(), f, 3 * g.NN * sizeof(double));
+}
+
+void Grid::getDirichletMask(uint8_t *out) const {
+    if (isDevicePtr(out)) VFEM_CUDA(cudaMemcpy(out, dmask_h.data(), g.NN, cudaMemcpyHostToDevice));
+    else std::memcpy(out, dmask_h.data(), g.NN);
+}
+
+void Grid::setGravity(const double gv[3]) {
+    for (int c = 0; c < 3; ++c) grav[c] = gv[c];
+}
+
+// TensorProductSimulator.hh:290-303
+void Grid::setMaskHeight(double hgt, bool update) {
+    if (hgt < 0 || hgt > bmax[BUILD_DIR])
+        throw Error(ERR_ARG, "Fabrication height has to be in between 0 and the domain height");
+    maskH = hgt;
+    const double fl = std::ceil(hgt / h[BUILD_DIR] - 1e-10);
+    g.firstMaskedE = (int)fl;
+    g.firstDetN = g.firstMaskedE + 1;
+    ++maskVersion;
+    if (update) updateYoungModuli();
+}
+
+void Grid::setMaskLayer(int64_t l) { setMaskHeight(h[BUILD_DIR] * (double)l, true); }
+
+void Grid::applyK(const double *u, double *out) {
+    View vu, vo;
+    viewIn(vu, u, 3 * g.NN * sizeof(double), stream);
+    viewOut(vo, out, 3 * g.NN * sizeof(double));
+    launch_applyk_fine<double>(g, Y.p, (const double *)vu.d, (double *)vo.d, K0, true, false, dmask.p, false,
+                               nullptr, 0, stream);
+    finishOut(vo, stream);
+}
+
+void Grid::buildLoadDev(double *f) {
+    VFEM_CUDA(cudaMemcpyAsync(f, force_h.data(), 3 * g.NN * sizeof(double), cudaMemcpyHostToDevice, stream));
+    if (grav[0] * grav[0] + grav[1] * grav[1] + grav[2] * grav[2] != 0)
+        launch_build_gravity_load(g, rho.p, f, grav, vol(), stream);
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::buildLoad(double *out) {
+    View vo;
+    viewOut(vo, out, 3 * g.NN * sizeof(double));
+    buildLoadDev((double *)vo.d);
+    finishOut(vo, stream);
+}
+
+void Grid::complianceGradient(const double *u, double *out) {
+    View vu, vo;
+    viewIn(vu, u, 3 * g.NN * sizeof(double), stream);
+    viewOut(vo, out, g.NE * sizeof(double));
+    launch_compliance_gradient(g, rho.p, (const double *)vu.d, (double *)vo.d, K0, E0, Emin, gamma, q, law, grav,
+                               vol(), stream);
+    finishOut(vo, stream);
+}
+
+void Grid::elementEnergy(const double *u, double *out) {
+    View vu, vo;
+    viewIn(vu, u, 3 * g.NN * sizeof(double), stream);
+    viewOut(vo, out, g.NE * sizeof(double));
+    launch_element_energy(g, Y.p, (const double *)vu.d, (double *)vo.d, K0, stream);
+    finishOut(vo, stream);
+}
+
+// ---------------------------------------------------------------------------
+// MG (MultigridSolver<double, 1, 1, 1>)
+// ---------------------------------------------------------------------------
+MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
+    if (coarsenings < 0) throw Error(ERR_ARG, "numCoarseningLevels must be >= 0");
+    lv.resize(coarsenings + 1);
+    lv[0].g = fine->g;
+    for (int d = 0; d < 3; ++d) lv[0].h[d] = fine->h[d];
+    int ne[3] = {fine->g.ne[0], fine->g.ne[1], fine->g.ne[2]};
+    for (int l = 1; l <= coarsenings; ++l) {
+        for (int d = 0; d < 3; ++d) {
+            if (ne[d] % 2 == 1)
+                throw Error(ERR_ARG,
+                            "Grid size currently must be divisible by 2^numCoarseningLevels (nonuniform coarsening "
+                            "not yet implemented)");
+            ne[d] /= 2;
+        }
+        lv[l].g = makeGeom(ne);
+        for (int d = 0; d < 3; ++d) lv[l].h[d] = (fine->bmax[d] - fine->bmin[d]) / ne[d];
+    }
+    lv[0].dmask_h = fine->dmask_h;
+    coarsenDirichlet();
+    for (int l = 1; l < L(); ++l) {
+        lv[l].dmask.alloc(lv[l].g.NN);
+        VFEM_CUDA(cudaMemcpy(lv[l].dmask.p, lv[l].dmask_h.data(), lv[l].g.NN, cudaMemcpyHostToDevice));
+    }
+    // propagate an existing fabrication mask (MultigridSolver.hh:1022-1028)
+    if (fine->maskH < std::numeric_limits<double>::infinity()) {
+        for (int l = 1; l < L(); ++l) {
+            const double fl = std::ceil(fine->maskH / lv[l].h[BUILD_DIR] - 1e-10);
+            lv[l].g.firstMaskedE = (int)fl;
+            lv[l].g.firstDetN = lv[l].g.firstMaskedE + 1;
+        }
+    }
+    const int64_t NN = fine->g.NN;
+    rbuf.alloc(3 * NN);
+    s.alloc(3 * NN);
+    dvec.alloc(3 * NN);
+    Ad.alloc(3 * NN);
+    partialCount = std::max<int>(REDUCE_BLOCKS, (int)gridFor(NN, 256));
+    partials.alloc(partialCount);
+    sc.alloc(16);
+    VFEM_CUDA(cudaMallocHost(&hostSc, 16 * sizeof(double)));
+    std::memset(hostSc, 0, 16 * sizeof(double));
+    setupCoarsestIndex();
+}
+
+MG::~MG() {
+    clearGraphs();
+    if (hostSc) cudaFreeHost(hostSc);
+}
+
+void MG::clearGraphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    graphX = nullptr;
+}
+
+// Dirichlet coarsening (MultigridSolver.hh:58-103): a fine constrained node on a coarse
+// element's vertex/edge/face constrains every coarse node of that vertex/edge/face.
+void MG::coarsenDirichlet() {
+    for (int l = 1; l < L(); ++l) {
+        const Level &F = lv[l - 1];
+        Level &Cl = lv[l];
+        Cl.dmask_h.assign(Cl.g.NN, 0);
+        for (int64_t fn = 0; fn < F.g.NN; ++fn) {
+            const uint8_t fm = F.dmask_h[fn];
+            if (!fm) continue;
+            const int fidx[3] = {(int)(fn / ((int64_t)F.g.nn[1] * F.g.nn[2])), (int)((fn / F.g.nn[2]) % F.g.nn[1]),
+                                 (int)(fn % F.g.nn[2])};
+            int e[3], pob[3];
+            for (int d = 0; d < 3; ++d) {
+                const double p = fine->bmin[d] + fidx[d] * F.h[d];
+                const double fi = (p - fine->bmin[d]) / Cl.h[d];
+                int ed;
+                if (std::abs(fi - Cl.g.ne[d]) < 1e-10) ed = Cl.g.ne[d] - 1;
+                else ed = (int)fi;
+                if (ed >= Cl.g.ne[d]) throw Error(ERR_ARG, "Point out of bounds");
+                e[d] = ed;
+                const double cref = (p - (fine->bmin[d] + ed * Cl.h[d])) / Cl.h[d];
+                pob[d] = std::abs(cref) < 1e-9 ? 0 : (std::abs(cref - 1.0) < 1e-9 ? 1 : -1);
+            }
+            for (int ln = 0; ln < 8; ++ln) {
+                const int lb[3] = {(ln >> 2) & 1, (ln >> 1) & 1, ln & 1};
+                bool ok = true;
+                for (int d = 0; d < 3; ++d)
+                    if (pob[d] != -1 && pob[d] != lb[d]) ok = false;
+                if (!ok) continue;
+                Cl.dmask_h[Cl.g.node(e[0] + lb[0], e[1] + lb[1], e[2] + lb[2])] |= fm;
+            }
+        }
+    }
+}
+
+// Fixed coarsest DOFs: Dirichlet components plus every component of a detached node
+// (TensorProductSimulator.hh:1181-1195).
+void MG::setupCoarsestIndex() {
+    const Level &C = lv.back();
+    const std::vector<uint8_t> &dm = (L() == 1) ? fine->dmask_h : C.dmask_h;
+    std::vector<int> red(3 * C.g.NN, -1), fr;
+    const int nyv = C.g.nyv();
+    for (int64_t n = 0; n < C.g.NN; ++n) {
+        const int j = (int)((n / C.g.nn[2]) % C.g.nn[1]);
+        for (int c = 0; c < 3; ++c) {
+            if ((dm[n] >> c) & 1) continue;
+            if (j >= nyv) continue;
+            red[3 * n + c] = (int)fr.size();
+            fr.push_back((int)(3 * n + c));
+        }
+    }
+    if (L() == 1 && fine->dvalNonzero) throw Error(ERR_ARG, "Nonzero Dirichlet constraints currently unsupported");
+    if (fr.size() > 30000) throw Error(ERR_ARG, "coarsest level too large for the dense direct solve; use more coarsening levels");
+    const int nf = (int)fr.size();
+    if (nf != nfree || !freeIdx.p) {
+        clearGraphs();
+        nfree = nf;
+        freeIdx.alloc(std::max(nf, 1));
+        Ainv.alloc(std::max<size_t>((size_t)nf * nf, 1));
+        work.alloc(std::max<size_t>((size_t)nf * nf, 1));
+        cscratch.alloc(std::max(nf, 1));
+        status.alloc(1);
+    }
+    redIdx.alloc(red.size());
+    VFEM_CUDA(cudaMemcpy(redIdx.p, red.data(), red.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (nf) VFEM_CUDA(cudaMemcpy(freeIdx.p, fr.data(), fr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    stiffnessValid = false;
+}
+
+void MG::setPrecision(int p) {
+    if (p != PREC_FP64 && p != PREC_MIXED) throw Error(ERR_ARG, "unknown precision");
+    if (p != precision) {
+        precision = p;
+        stiffnessValid = false;
+        clearGraphs();
+    }
+}
+
+void MG::setMaskLayer(int64_t layer) {
+    fine->setMaskLayer(layer);
+    lv[0].g = fine->g;
+    for (int l = 1; l < L(); ++l) {
+        const double fl = std::ceil(fine->maskH / lv[l].h[BUILD_DIR] - 1e-10);
+        lv[l].g.firstMaskedE = (int)fl;
+        lv[l].g.firstDetN = lv[l].g.firstMaskedE + 1;
+    }
+    clearGraphs();
+    setupCoarsestIndex();
+}
+
+void MG::allocLevels() {
+    for (int l = 0; l < L(); ++l) {
+        const int64_t n3 = 3 * lv[l].g.NN;
+        if (precision == PREC_FP64) {
+            auto &D = lv[l].d64;
+            D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
+        } else {
+            auto &D = lv[l].d32;
+            D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
+        }
+    }
+}
+
+static void syncFineGeom(MG &mg) {
+    // the fine level shares the grid's (possibly masked) geometry
+    mg.lv[0].g = mg.fine->g;
+}
+
+template <typename T>
+struct Tr;
+template <>
+struct Tr<double> {
+    static const double *Y(Grid &g) { return g.Y.p; }
+    static const Mat24<double> &K0(Grid &g) { return g.K0; }
+    static DevBuf<double> &Kc(MG &m) { return m.Kc64; }
+    static DevBuf<double> &phis(MG &m) { return m.phis64; }
+};
+template <>
+struct Tr<float> {
+    static const float *Y(Grid &g) { return g.youngF(); }
+    static const Mat24<float> &K0(Grid &g) { return g.K0f; }
+    static DevBuf<float> &Kc(MG &m) { return m.Kc32; }
+    static DevBuf<float> &phis(MG &m) { return m.phis32; }
+};
+
+template <typename T>
+static void uploadConst(DevBuf<T> &dst, const double *src, size_t n) {
+    std::vector<T> tmp(src, src + n);
+    dst.alloc(n);
+    VFEM_CUDA(cudaMemcpy(dst.p, tmp.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// MultigridSolver.hh:846-905: element matrices level by level, assembled stencils for the
+// smoothing levels, and the dense inverse of the reduced coarsest operator.
+template <typename T>
+void MG::updateStiffnessT() {
+    syncFineGeom(*this);
+    allocLevels();
+    cudaStream_t st = fine->stream;
+    double phis[8][64];
+    interpolation_phis(phis);
+    std::vector<double> Kc(8 * 576, 0.0);
+    for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[fi], fine->K0.a, &Kc[fi * 576]);
+    uploadConst(Tr<T>::Kc(*this), Kc.data(), Kc.size());
+    uploadConst(Tr<T>::phis(*this), &phis[0][0], 512);
+    const T *Y0 = Tr<T>::Y(*fine);
+    if (L() == 1) {
+        // direct solve on the fine grid: Ke = Y K0 (TensorProductSimulator.hh:1198-1230)
+        auto &D = lv[0].data<T>();
+        D.Ke.alloc((size_t)lv[0].g.NE * 576);
+        D.S.alloc((size_t)243 * lv[0].g.NN);
+        std::vector<double> k0(fine->K0.a, fine->K0.a + 576);
+        DevBuf<T> K0d;
+        uploadConst(K0d, k0.data(), 576);
+        launch_ke_scaled<T>(lv[0].g, Y0, K0d.p, D.Ke.p, st);
+        launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, st);
+        VFEM_CUDA(cudaStreamSynchronize(st));
+    } else {
+        for (int l = 1; l < L(); ++l) {
+            auto &D = lv[l].data<T>();
+            D.Ke.alloc((size_t)lv[l].g.NE * 576);
+            D.S.alloc((size_t)243 * lv[l].g.NN);
+            if (l == 1) launch_ke_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Ke.p, st);
+            else launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p, st);
+            launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, st);
+        }
+    }
+    // dense reduced coarsest operator, FP64 inverse
+    const Level &C = lv.back();
+    if (nfree > 0) {
+        launch_dense_from_stencil<T>(C.g, lv.back().data<T>().S.p, redIdx.p, Ainv.p, nfree, st);
+        launch_symmetrize(Ainv.p, nfree, st);
+        VFEM_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+        dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st);
+        int hs = 0;
+        VFEM_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        VFEM_CUDA(cudaStreamSynchronize(st));
+        if (hs) throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
+    }
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    stiffnessValid = true;
+    stiffnessPrecision = precision;
+    stiffnessDensVersion = fine->densVersion;
+    stiffnessMaskVersion = fine->maskVersion;
+}
+
+void MG::updateStiffness() {
+    if (precision == PREC_FP64) updateStiffnessT<double>();
+    else updateStiffnessT<float>();
+}
+
+void MG::ensureStiffness() {
+    syncFineGeom(*this);
+    if (!stiffnessValid || stiffnessPrecision != precision || stiffnessDensVersion != fine->densVersion ||
+        stiffnessMaskVersion != fine->maskVersion)
+        updateStiffness();
+}
+
+template <typename T>
+void MG::smoothT(int l, bool forward) {
+    cudaStream_t st = fine->stream;
+    auto &D = lv[l].data<T>();
+    const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+    for (int c = 0; c < 8; ++c) {
+        const int color = forward ? c : 7 - c;
+        if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);
+        else launch_gs_stencil_color<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, color, forward, st);
+    }
+}
+
+template <typename T>
+void MG::residualT(int l) {
+    cudaStream_t st = fine->stream;
+    auto &D = lv[l].data<T>();
+    if (l == 0) launch_residual_fine<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, D.r.p, Tr<T>::K0(*fine), fine->dmask.p, st);
+    else launch_stencil_residual<T>(lv[l].g, D.S.p, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, st);
+}
+
+// MultigridSolver.hh:617-658
+template <typename T>
+void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
+    cudaStream_t st = fine->stream;
+    auto &D = lv[l].data<T>();
+    if (l == L() - 1) {
+        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfree, D.b.p, D.x.p, cscratch.p, st);
+        return;
+    }
+    const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+    if (residualSystem || l > 0 || !fine->dvalNonzero) launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
+    else launch_enforce_dirichlet<T>(lv[l].g, D.x.p, dm, fine->dval.p, st);
+    for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, true);
+    residualT<T>(l);
+    auto &Dc = lv[l + 1].data<T>();
+    launch_restrict<T>(lv[l].g, lv[l + 1].g, D.r.p, Dc.b.p, st);
+    launch_masked_zero<T>(lv[l + 1].g, Dc.x.p, MARGIN, st);
+    vcycleT<T>(l + 1, sweeps, true);
+    launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dc.x.p, D.x.p, true, st);
+    for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, !symmetricGS);
+}
+
+// MultigridSolver.hh:587-609
+template <typename T>
+void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
+    cudaStream_t st = fine->stream;
+    auto &D = lv[l].data<T>();
+    if (l == L() - 1) {
+        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfree, D.b.p, D.x.p, cscratch.p, st);
+        return;
+    }
+    auto &Dc = lv[l + 1].data<T>();
+    launch_restrict<T>(lv[l].g, lv[l + 1].g, D.b.p, Dc.b.p, st);
+    fmgT<T>(l + 1, sweeps, residualSystem);
+    launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dc.x.p, D.x.p, false, st);
+    vcycleT<T>(l, sweeps, residualSystem);
+}
+
+// Preconditioner s = M^{-1} r (MultigridSolver.hh:547-580): zero initial guess,
+// residual system, mgIter V-cycles (or FMG + mgIter-1 V-cycles).
+template <typename T>
+void MG::preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg) {
+    cudaStream_t st = fine->stream;
+    if (sweeps == 0) return;  // applyPreconditionerInv returns without touching the MG iterate
+    auto &D = lv[0].data<T>();
+    const int64_t n3 = 3 * lv[0].g.NN;
+    launch_fill<T>(D.x.p, T(0), n3, st);
+    if (mgIter == 0) return;
+    if (std::is_same<T, double>::value) launch_copy((double *)D.b.p, r, n3, st);
+    else launch_cast<float, double>(r, (float *)D.b.p, n3, st);
+    if (fmg) {
+        fmgT<T>(0, sweeps, true);
+        for (int64_t i = 1; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
+    } else {
+        for (int64_t i = 0; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
+    }
+}
+
+// One PCG iteration (MultigridSolver.hh:1108-1144), enqueued without host synchronisation.
+void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
+    if (mgIter > 0) {
+        if (precision == PREC_FP64) {
+            preconditionT<double>(rbuf.p, mgIter, sweeps, fmg);
+            launch_cg_precond_out<double>(g, lv[0].d64.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+        } else {
+            preconditionT<float>(rbuf.p, mgIter, sweeps, fmg);
+            launch_cg_precond_out<float>(g, lv[0].d32.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+        }
+    } else {
+        launch_cg_precond_out<double>(g, rbuf.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+    }
+    launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
+    launch_cg_direction(g, s.p, dvec.p, sc.p, st);
+    const int nb = (int)gridFor(g.NN, 256);
+    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF)
+        launch_applyk_fine_df(g, fine->Y.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true, partials.p, partialCount, st);
+    else
+        launch_applyk_fine<double>(g, fine->Y.p, dvec.p, Ad.p, fine->K0, true, false, fine->dmask.p, true, partials.p,
+                                   partialCount, st);
+    launch_cg_alpha(partials.p, nb, sc.p, st);
+    launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
+    launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
+    VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+}
+
+static double readScalar(double *dev, cudaStream_t st) {
+    double v = 0;
+    VFEM_CUDA(cudaMemcpyAsync(&v, dev, sizeof(double), cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    return v;
+}
+
+// MultigridSolver.hh:1047-1152
+PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
+                       bool fmg, bool dirichletSatisfied, PcgCallback cb, void *user) {
+    syncFineGeom(*this);
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
+    PcgStats stats;
+    if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
+    launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
+    const double bnorm2 = readScalar(sc.p + 7, st);
+    launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
+    launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
+    double rsq = readScalar(sc.p + 5, st);
+    if (std::isnan(rsq)) throw Error(ERR_NAN, "NaN encountered");
+    stats.bnorm2 = bnorm2;
+
+    if (L() == 1) {
+        // direct solve branch (MultigridSolver.hh:1056-1064)
+        if (!(rsq < tol * tol * bnorm2)) {
+            ensureStiffness();
+            if (precision == PREC_FP64) launch_coarse_solve<double>(g, Ainv.p, freeIdx.p, nfree, b, x, cscratch.p, st);
+            else throw Error(ERR_ARG, "numCoarseningLevels == 0 requires FP64 precision");
+            launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
+            launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
+            launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
+            rsq = readScalar(sc.p + 5, st);
+            stats.iterations = 1;
+            if (cb) cb(user, 1, std::sqrt(rsq), x, rbuf.p);
+        }
+        stats.rsq = rsq;
+        stats.relres = bnorm2 > 0 ? std::sqrt(rsq / bnorm2) : std::sqrt(rsq);
+        return stats;
+    }
+
+    // CG scalars: first-iteration flag set, r.Minv.r = 0
+    double init[16] = {0};
+    init[5] = rsq;
+    init[6] = 1.0;
+    init[7] = bnorm2;
+    VFEM_CUDA(cudaMemcpyAsync(sc.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
+    VFEM_CUDA(cudaStreamSynchronize(st));
+
+    const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec, fine->maskVersion,
+                       nfree};
+    bool updated = false;
+    int64_t i = 0;
+    while ((i++ < maxIter) && (rsq > tol * tol * bnorm2)) {
+        if (mgIter > 0 && !updated) {
+            ensureStiffness();
+            updated = true;
+        }
+        if (useGraphs) {
+            if (graphX != x) clearGraphs();
+            auto it = graphs.find(key);
+            if (it == graphs.end()) {
+                cudaGraph_t graph;
+                VFEM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                try {
+                    cgIteration(x, mgIter, sweeps, fmg);
+                } catch (...) {
+                    cudaStreamEndCapture(st, &graph);
+                    throw;
+                }
+                VFEM_CUDA(cudaStreamEndCapture(st, &graph));
+                cudaGraphExec_t exec;
+                VFEM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+                cudaGraphDestroy(graph);
+                it = graphs.emplace(key, exec).first;
+                graphX = x;
+            }
+            VFEM_CUDA(cudaGraphLaunch(it->second, st));
+        } else {
+            cgIteration(x, mgIter, sweeps, fmg);
+        }
+        VFEM_CUDA(cudaStreamSynchronize(st));
+        rsq = hostSc[5];
+        if (std::isnan(rsq)) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string(i));
+        if (cb) {
+            if (cb(user, i, std::sqrt(rsq), x, rbuf.p)) break;
+        }
+    }
+    stats.iterations = i - 1;
+    stats.rsq = rsq;
+    stats.relres = bnorm2 > 0 ? std::sqrt(rsq / bnorm2) : std::sqrt(rsq);
+    return stats;
+}
+
+PcgStats MG::pcg(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                 bool dirichletSatisfied, PcgCallback cb, void *user) {
+    cudaStream_t st = fine->stream;
+    const size_t bytes = 3 * fine->g.NN * sizeof(double);
+    View vb;
+    viewIn(vb, b, bytes, st);
+    // iterate in an internal buffer so that captured graphs stay valid across calls
+    xbuf.alloc(3 * fine->g.NN);
+    DevBuf<double> &xb = xbuf;
+    VFEM_CUDA(cudaMemcpyAsync(xb.p, x, bytes, cudaMemcpyDefault, st));
+    PcgStats stats = pcgDevice(xb.p, (const double *)vb.d, maxIter, tol, mgIter, sweeps, fmg, dirichletSatisfied, cb,
+                               user);
+    VFEM_CUDA(cudaMemcpyAsync(x, xb.p, bytes, cudaMemcpyDefault, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    return stats;
+}
+
+
+// ---------------------------------------------------------------------------
+// Per-level operations on caller FP64 vectors (MultigridSolver python bindings,
+// VoxelFEM.cc:155-195). In mixed precision the level kernels run in FP32.
+// ---------------------------------------------------------------------------
+enum LevelOpKind { OP_APPLYK = 0, OP_RESIDUAL = 1, OP_SMOOTH = 2, OP_RESTRICT = 3, OP_INTERP = 4, OP_COARSE = 5,
+                   OP_ZERODIR = 6 };
+
+template <typename T>
+static void toT(const double *src, T *dst, int64_t n, cudaStream_t st) {
+    if (std::is_same<T, double>::value) VFEM_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else launch_cast<float, double>(src, (float *)dst, n, st);
+}
+template <typename T>
+static void fromT(const T *src, double *dst, int64_t n, cudaStream_t st) {
+    if (std::is_same<T, double>::value) VFEM_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else launch_cast<double, float>((const float *)src, dst, n, st);
+}
+
+template <typename T>
+void MG::applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate) {
+    cudaStream_t st = fine->stream;
+    if (l == 0)
+        launch_applyk_fine<T>(lv[0].g, Tr<T>::Y(*fine), u, out, Tr<T>::K0(*fine), zeroInit, negate, fine->dmask.p, false,
+                              nullptr, 0, st);
+    else launch_stencil_apply<T>(lv[l].g, lv[l].data<T>().S.p, u, out, zeroInit, negate, st);
+}
+
+template <typename T>
+void MG::levelOp(int l, int op, const double *a, const double *b, double *out, bool flag) {
+    cudaStream_t st = fine->stream;
+    if (l < 0 || l >= L()) throw Error(ERR_ARG, "level out of range");
+    if (op == OP_RESTRICT || op == OP_INTERP) {
+        if (l + 1 >= L()) throw Error(ERR_ARG, "no coarser level");
+    }
+    if (l > 0 || op == OP_COARSE || L() == 1) ensureStiffness();
+    syncFineGeom(*this);
+    allocLevels();
+    auto &D = lv[l].data<T>();
+    const int64_t n3 = 3 * lv[l].g.NN;
+    const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+    switch (op) {
+    case OP_APPLYK: {
+        toT<T>(a, D.x.p, n3, st);
+        applyKLevelT<T>(l, D.x.p, D.r.p, true, false);
+        fromT<T>(D.r.p, out, n3, st);
+        break;
+    }
+    case OP_RESIDUAL: {
+        toT<T>(a, D.x.p, n3, st);
+        toT<T>(b, D.b.p, n3, st);
+        residualT<T>(l);
+        fromT<T>(D.r.p, out, n3, st);
+        break;
+    }
+    case OP_SMOOTH: {
+        toT<T>(a, D.x.p, n3, st);
+        toT<T>(b, D.b.p, n3, st);
+        smoothT<T>(l, flag);
+        fromT<T>(D.x.p, out, n3, st);
+        break;
+    }
+    case OP_RESTRICT: {
+        auto &Dc = lv[l + 1].data<T>();
+        toT<T>(a, D.r.p, n3, st);
+        launch_restrict<T>(lv[l].g, lv[l + 1].g, D.r.p, Dc.b.p, st);
+        fromT<T>(Dc.b.p, out, 3 * lv[l + 1].g.NN, st);
+        break;
+    }
+    case OP_INTERP: {
+        auto &Dc = lv[l + 1].data<T>();
+        toT<T>(a, Dc.x.p, 3 * lv[l + 1].g.NN, st);
+        toT<T>(b, D.x.p, n3, st);
+        launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dc.x.p, D.x.p, flag, st);
+        fromT<T>(D.x.p, out, n3, st);
+        break;
+    }
+    case OP_COARSE: {
+        auto &Dc = lv.back().data<T>();
+        const int64_t nc = 3 * lv.back().g.NN;
+        toT<T>(a, Dc.b.p, nc, st);
+        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+        fromT<T>(Dc.x.p, out, nc, st);
+        break;
+    }
+    case OP_ZERODIR: {
+        toT<T>(a, D.x.p, n3, st);
+        launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
+        fromT<T>(D.x.p, out, n3, st);
+        break;
+    }
+    }
+}
+
+static int64_t levelNN(const MG &m, int l) {
+    if (l < 0 || l >= m.L()) throw Error(ERR_ARG, "level out of range");
+    return m.lv[l].g.NN;
+}
+
+#define VFEM_LEVEL_CALL(l, op, A, nA, B, nB, OUT, nOUT, flag)                                                    \
+    do {                                                                                                         \
+        cudaStream_t st_ = fine->stream;                                                                         \
+        View va_, vb_, vo_;                                                                                      \
+        viewIn(va_, A, (nA) * sizeof(double), st_);                                                              \
+        if (B) viewIn(vb_, B, (nB) * sizeof(double), st_);                                                       \
+        viewOut(vo_, OUT, (nOUT) * sizeof(double));                                                              \
+        if (precision == PREC_FP64)                                                                              \
+            levelOp<double>(l, op, (const double *)va_.d, (const double *)vb_.d, (double *)vo_.d, flag);         \
+        else levelOp<float>(l, op, (const double *)va_.d, (const double *)vb_.d, (double *)vo_.d, flag);         \
+        finishOut(vo_, st_);                                                                                     \
+    } while (0)
+
+void MG::applyK(int l, const double *u, double *out) {
+    const int64_t n = 3 * levelNN(*this, l);
+    VFEM_LEVEL_CALL(l, OP_APPLYK, u, n, (const double *)nullptr, 0, out, n, false);
+}
+void MG::residual(int l, const double *u, const double *b, double *r) {
+    const int64_t n = 3 * levelNN(*this, l);
+    VFEM_LEVEL_CALL(l, OP_RESIDUAL, u, n, b, n, r, n, false);
+}
+void MG::smooth(int l, double *u, const double *b, bool forward) {
+    const int64_t n = 3 * levelNN(*this, l);
+    if (l == L() - 1 && L() > 1) throw Error(ERR_ARG, "the coarsest level is solved directly, not smoothed");
+    VFEM_LEVEL_CALL(l, OP_SMOOTH, u, n, b, n, u, n, forward);
+}
+void MG::restrictTo(int l, const double *f, double *c) {
+    const int64_t n = 3 * levelNN(*this, l);
+    const int64_t nc = 3 * levelNN(*this, l + 1);
+    VFEM_LEVEL_CALL(l, OP_RESTRICT, f, n, (const double *)nullptr, 0, c, nc, false);
+}
+void MG::interpolate(int l, const double *c, double *f, bool accumulate) {
+    const int64_t n = 3 * levelNN(*this, l);
+    const int64_t nc = 3 * levelNN(*this, l + 1);
+    VFEM_LEVEL_CALL(l, OP_INTERP, c, nc, f, n, f, n, accumulate);
+}
+void MG::coarseSolve(const double *b, double *x) {
+    const int64_t n = 3 * levelNN(*this, L() - 1);
+    VFEM_LEVEL_CALL(L() - 1, OP_COARSE, b, n, (const double *)nullptr, 0, x, n, false);
+}
+void MG::zeroDirichlet(int l, double *u) {
+    const int64_t n = 3 * levelNN(*this, l);
+    VFEM_LEVEL_CALL(l, OP_ZERODIR, u, n, (const double *)nullptr, 0, u, n, false);
+}
+
+// MultigridSolver.hh:547-573 (stiffness matrices rebuilt unless unchanged)
+void MG::solve(const double *u0, const double *f, int64_t steps, int64_t sweeps, bool zeroDirichletFlag, bool fmg,
+               double *out) {
+    cudaStream_t st = fine->stream;
+    const int64_t n3 = 3 * fine->g.NN;
+    View vu, vf, vo;
+    viewIn(vu, u0, n3 * sizeof(double), st);
+    viewIn(vf, f, n3 * sizeof(double), st);
+    viewOut(vo, out, n3 * sizeof(double));
+    ensureStiffness();
+    syncFineGeom(*this);
+    allocLevels();
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        auto &D = lv[0].data<T>();
+        toT<T>((const double *)vu.d, D.x.p, n3, st);
+        if (steps > 0) {
+            toT<T>((const double *)vf.d, D.b.p, n3, st);
+            if (fmg) {
+                fmgT<T>(0, sweeps, zeroDirichletFlag);
+                for (int64_t i = 1; i < steps; ++i) vcycleT<T>(0, sweeps, zeroDirichletFlag);
+            } else {
+                for (int64_t i = 0; i < steps; ++i) vcycleT<T>(0, sweeps, zeroDirichletFlag);
+            }
+        }
+        fromT<T>(D.x.p, (double *)vo.d, n3, st);
+    };
+    if (precision == PREC_FP64) run(double());
+    else run(float());
+    finishOut(vo, st);
+}
+
+// ---------------------------------------------------------------------------
+// Problem: MG compliance objective + filter chain + total volume constraint
+// ---------------------------------------------------------------------------
+Problem::Problem(MG *mg_, const std::vector<FilterSpec> &filters_, double volfrac_)
+    : mg(mg_), grid(mg_->fine), filters(filters_), volfrac(volfrac_) {
+    for (const auto &f : filters) {
+        if (f.kind == 0 && f.radius < 0) throw Error(ERR_ARG, "negative filter radius");
+        if (f.kind == 1 && !(f.beta > 0)) throw Error(ERR_ARG, "Beta parameter has to be positive");
+        if (f.kind != 0 && f.kind != 1) throw Error(ERR_ARG, "unknown filter kind");
+    }
+    const int64_t ne = grid->g.NE, n3 = 3 * grid->g.NN;
+    vars.resize(filters.size() + 1);
+    for (auto &v : vars) v.alloc(ne);
+    f.alloc(n3);
+    u.alloc(n3);
+    gradBuf.alloc(ne);
+    scratch.alloc(ne);
+    scratch2.alloc(ne);
+    stepped.alloc(ne);
+    x0.alloc(ne);
+    dJ.alloc(ne);
+    dc.alloc(ne);
+    partials.alloc(REDUCE_BLOCKS + 8);
+    // the load is fixed when the objective is built (TopologyOptimizationObjective.hh:34-37)
+    grid->buildLoadDev(f.p);
+    launch_fill<double>(u.p, 0.0, n3, grid->stream);
+    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+void Problem::filterApply(const double *x, double *out) {
+    cudaStream_t st = grid->stream;
+    const int64_t ne = grid->g.NE;
+    if (filters.empty()) {
+        VFEM_CUDA(cudaMemcpyAsync(out, x, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        return;
+    }
+    const double *src = x;
+    for (size_t i = 0; i < filters.size(); ++i) {
+        double *dst = (i + 1 == filters.size()) ? out : ((i % 2 == 0) ? scratch.p : scratch2.p);
+        if (filters[i].kind == 0) launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, src, dst, st);
+        else launch_projection(ne, filters[i].beta, src, dst, st);
+        src = dst;
+    }
+}
+
+// FilterChain::backprop (TopologyOptimizationFilter.hh:162-175); g is overwritten.
+void Problem::backprop(double *g) {
+    cudaStream_t st = grid->stream;
+    const int64_t ne = grid->g.NE;
+    for (size_t i = filters.size(); i-- > 0;) {
+        if (filters[i].kind == 0) launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, g, scratch.p, st);
+        else launch_projection_backprop(ne, filters[i].beta, g, vars[i].p, scratch.p, st);
+        VFEM_CUDA(cudaMemcpyAsync(g, scratch.p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+}
+
+double Problem::meanDev(const double *x) {
+    cudaStream_t st = grid->stream;
+    launch_sum_partials(x, grid->g.NE, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, partials.p + REDUCE_BLOCKS, st);
+    double v = 0;
+    VFEM_CUDA(cudaMemcpyAsync(&v, partials.p + REDUCE_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    return v / (double)grid->g.NE;
+}
+
+// TopologyOptimizationProblem.hh:41-50 and MultigridComplianceObjective::updateCache
+void Problem::setVars(const double *x, bool /*device*/) {
+    cudaStream_t st = grid->stream;
+    const int64_t ne = grid->g.NE;
+    VFEM_CUDA(cudaMemcpyAsync(vars[0].p, x, ne * sizeof(double), cudaMemcpyDefault, st));
+    for (size_t i = 0; i < filters.size(); ++i) {
+        if (filters[i].kind == 0)
+            launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, vars[i].p, vars[i + 1].p, st);
+        else launch_projection(ne, filters[i].beta, vars[i].p, vars[i + 1].p, st);
+    }
+    VFEM_CUDA(cudaMemcpyAsync(grid->rho.p, vars.back().p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    grid->updateYoungModuli();
+    if (zeroInit) launch_fill<double>(u.p, 0.0, 3 * grid->g.NN, st);
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    lastStats = mg->pcgDevice(u.p, f.p, cgIter, tol, mgIter, mgSweeps, fmg, false, nullptr, nullptr);
+    varsSet = true;
+}
+
+double Problem::objective() {
+    if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
+    cudaStream_t st = grid->stream;
+    Geom gall = grid->g;
+    gall.firstDetN = (int)LAYER_MASK_NONE;  // 0.5 f.u over all nodes (TopologyOptimizationObjective.hh:41-43)
+    launch_masked_dot_partials<double, double>(gall, f.p, u.p, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, partials.p + REDUCE_BLOCKS, st);
+    double v = 0;
+    VFEM_CUDA(cudaMemcpyAsync(&v, partials.p + REDUCE_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    return 0.5 * v;
+}
+
+void Problem::gradientDev(double *out) {
+    cudaStream_t st = grid->stream;
+    launch_compliance_gradient(grid->g, grid->rho.p, u.p, out, grid->K0, grid->E0, grid->Emin, grid->gamma, grid->q,
+                               grid->law, grid->grav, grid->vol(), st);
+    backprop(out);
+}
+
+void Problem::gradient(double *out, bool /*device*/) {
+    if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
+    gradientDev(gradBuf.p);
+    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
+    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+double Problem::constraint() {
+    if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
+    return 1.0 - meanDev(vars.back().p) / volfrac;
+}
+
+void Problem::jacobianDev(double *out) {
+    launch_fill<double>(out, -1.0 / (volfrac * (double)grid->g.NE), grid->g.NE, grid->stream);
+    backprop(out);
+}
+
+void Problem::jacobian(double *out, bool /*device*/) {
+    if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
+    jacobianDev(gradBuf.p);
+    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
+    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+// TopologyOptimizationProblem::evaluateOCConstraintAtVars (TopologyOptimizationProblem.hh:58-66)
+double Problem::constraintAtVars(const double *x) {
+    filterApply(x, gradBuf.p);
+    return 1.0 - meanDev(gradBuf.p) / volfrac;
+}
+
+// OptimalityCriterion.hh:51-138
+int64_t Problem::ocStep(double m, double p, double ctol) {
+    if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
+    cudaStream_t st = grid->stream;
+    const int64_t ne = grid->g.NE;
+    gradientDev(dJ.p);
+    jacobianDev(dc.p);
+    VFEM_CUDA(cudaMemcpyAsync(x0.p, vars[0].p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    int64_t probes = 0;
+    auto ceval = [&](double lambda) {
+        ++probes;
+        launch_oc_update(ne, x0.p, dJ.p, dc.p, lambda, m, p, stepped.p, st);
+        return constraintAtVars(stepped.p);
+    };
+    const double dilation = 32;
+    const int64_t guard = 100;
+    double lmid = 0.5 * (lambda_min + lambda_max);
+    lambda_max = dilation * lambda_max + (1 - dilation) * lmid;
+    lambda_min = std::max(dilation * lambda_min + (1 - dilation) * lmid, 0.01);
+    int64_t nit = 0;
+    for (; nit < guard; ++nit) {
+        if (ceval(lambda_min) < 0) break;
+        lambda_max = lambda_min;
+        lambda_min /= 2;
+    }
+    if (nit == guard) throw Error(ERR_STATE, "Bracketing constraint(lambda_min) < 0 failed (100 times).");
+    if (nit == 0)
+        for (; nit < guard; ++nit) {
+            if (ceval(lambda_max) > 0) break;
+            lambda_min = lambda_max;
+            lambda_max *= 2;
+        }
+    if (nit == guard) throw Error(ERR_STATE, "Bracketing constraint(lambda_max) > 0 failed (100 times).");
+    double viol;
+    for (int64_t bis = 0;; ++bis) {
+        lmid = 0.5 * (lambda_min + lambda_max);
+        viol = ceval(lmid);
+        if (std::abs(viol) <= ctol) break;
+        if (bis > 2000) throw Error(ERR_STATE, "OC bisection did not reach the constraint tolerance");
+        if (viol < 0) lambda_min = lmid;
+        if (viol > 0) lambda_max = lmid;
+    }
+    // stepped holds the accepted update; setVars overwrites scratch buffers, so copy first
+    VFEM_CUDA(cudaMemcpyAsync(x0.p, stepped.p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    setVars(x0.p, true);
+    return probes;
+}
+
+void Problem::getU(double *out, bool /*device*/) {
+    VFEM_CUDA(cudaMemcpyAsync(out, u.p, 3 * grid->g.NN * sizeof(double), cudaMemcpyDefault, grid->stream));
+    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+void Problem::getPhysical(double *out, bool /*device*/) {
+    VFEM_CUDA(cudaMemcpyAsync(out, vars.back().p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
+    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+}  // namespace vfem

@@ -1,0 +1,259 @@
+// Host engine of the GB300 VoxelFEM solve path: the voxel grid (TensorProductSimulator),
+// the geometric multigrid hierarchy with its MG-preconditioned CG (MultigridSolver) and
+// the topology-optimisation problem with the OC optimiser. All state lives on the device;
+// this layer only sequences kernels on one CUDA stream and captures CUDA graphs.
+#pragma once
+#include <cmath>
+#include <limits>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "vfem_common.cuh"
+#include "vfem_kernels.hpp"
+
+namespace vfem {
+
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+enum OuterMatvec { MATVEC_FP64 = 0, MATVEC_DF = 1 };
+
+bool isDevicePtr(const void *p);
+
+// Device-accessible view of caller memory; host memory is staged through a device buffer.
+struct View {
+    void *user = nullptr;
+    void *d = nullptr;
+    size_t bytes = 0;
+    bool staged = false;
+    DevBuf<char> tmp;
+};
+void viewIn(View &v, const void *p, size_t bytes, cudaStream_t st);
+void viewOut(View &v, void *p, size_t bytes);
+void viewInOut(View &v, void *p, size_t bytes, cudaStream_t st);
+void finishOut(View &v, cudaStream_t st);
+
+class Grid {
+public:
+    Grid(const int ne[3], const double bmin[3], const double bmax[3]);
+    ~Grid();
+    Grid(const Grid &) = delete;
+    Grid &operator=(const Grid &) = delete;
+
+    Geom g;
+    double bmin[3], bmax[3], h[3];
+    double Eyoung = 1.0, nu = 0.0;  // ETensor(1, 0) default (TensorProductSimulator.hh:2114)
+    Mat24<double> K0;
+    Mat24<float> K0f;
+    Mat24DF K0df;
+    double E0 = 1.0, Emin = 1e-4, gamma = 3.0, q = 3.0;  // TensorProductSimulator.hh:2137-2141
+    int law = 0;                                          // 0 SIMP, 1 RAMP
+    double maskH = std::numeric_limits<double>::infinity();
+    double grav[3] = {0, 0, 0};
+
+    DevBuf<double> rho, Y;
+    DevBuf<float> Yf;
+    bool YfValid = false;
+    std::vector<uint8_t> dmask_h;
+    std::vector<double> dval_h;   // SoA, stride NN
+    std::vector<double> force_h;  // dense nodal forces, SoA
+    DevBuf<uint8_t> dmask;
+    DevBuf<double> dval;
+    bool dvalNonzero = false;
+    uint64_t densVersion = 1, bcVersion = 1, maskVersion = 1;
+    cudaStream_t stream = nullptr;
+
+    void setETensor(double E, double nu);
+    void setParams(double E0_, double Emin_, double gamma_, double q_, int law_);
+    void setDensities(const double *rho, bool checkRange);
+    void setUniformDensities(double v);
+    void getDensities(double *out);
+    void getYoungModuli(double *out);
+    void updateYoungModuli();
+    const float *youngF();
+    void addDirichlet(const double u[3], const double mn[3], const double mx[3], unsigned cmask);
+    void applySymmetry(const int axes[3], const int maxFace[3]);
+    void setForces(const double *f);
+    void getDirichletMask(uint8_t *out) const;
+    void setGravity(const double gv[3]);
+    void setMaskLayer(int64_t l);
+    void setMaskHeight(double hgt, bool update);
+    void applyK(const double *u, double *out);
+    void buildLoad(double *out);
+    void complianceGradient(const double *u, double *out);
+    void elementEnergy(const double *u, double *out);
+    double vol() const { return h[0] * h[1] * h[2]; }
+
+    // device-side helpers
+    void buildLoadDev(double *f_dev);
+    void uploadBC();
+};
+
+template <typename T>
+struct LevelData {
+    DevBuf<T> x, b, r, S, Ke;
+};
+
+struct Level {
+    Geom g;
+    double h[3];
+    std::vector<uint8_t> dmask_h;
+    DevBuf<uint8_t> dmask;
+    LevelData<double> d64;
+    LevelData<float> d32;
+    template <typename T>
+    LevelData<T> &data();
+};
+template <>
+inline LevelData<double> &Level::data<double>() { return d64; }
+template <>
+inline LevelData<float> &Level::data<float>() { return d32; }
+
+struct PcgStats {
+    int64_t iterations = 0;
+    double relres = 0;
+    double rsq = 0, bnorm2 = 0;
+    int status = 0;
+};
+
+using PcgCallback = int (*)(void *user, int64_t it, double rnorm, const double *x_dev, const double *r_dev);
+
+class MG {
+public:
+    MG(Grid *fine, int coarsenings);
+    ~MG();
+    MG(const MG &) = delete;
+    MG &operator=(const MG &) = delete;
+
+    Grid *fine;
+    std::vector<Level> lv;
+    int precision = PREC_FP64;
+    int outerMatvec = MATVEC_DF;
+    bool symmetricGS = true;
+    bool useGraphs = true;
+
+    int L() const { return (int)lv.size(); }
+    void setPrecision(int p);
+    void setMaskLayer(int64_t l);
+    void updateStiffness();
+
+    // per-level operations on caller FP64 vectors (level sizes)
+    void applyK(int l, const double *u, double *out);
+    void residual(int l, const double *u, const double *b, double *r);
+    void smooth(int l, double *u, const double *b, bool forward);
+    void restrictTo(int l, const double *fine, double *coarse);
+    void interpolate(int l, const double *coarse, double *fine, bool accumulate);
+    void coarseSolve(const double *b, double *x);
+    void zeroDirichlet(int l, double *u);
+    void solve(const double *u0, const double *f, int64_t steps, int64_t sweeps, bool zeroDirichletFlag, bool fmg,
+               double *out);
+    PcgStats pcg(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                 bool dirichletSatisfied, PcgCallback cb, void *user);
+    // PCG on device-resident FP64 buffers (no staging); used by pcg() and by the problem layer.
+    PcgStats pcgDevice(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
+                       bool fmg, bool dirichletSatisfied, PcgCallback cb, void *user);
+    double lastTrueRelres = -1;
+
+    // coarsest level
+    int nfree = 0;
+    DevBuf<int> freeIdx, redIdx;
+    DevBuf<double> Ainv, work, cscratch;
+    DevBuf<int> status;
+    bool stiffnessValid = false;
+    int stiffnessPrecision = -1;
+    uint64_t stiffnessDensVersion = 0, stiffnessMaskVersion = 0, stiffnessBcVersion = 0;
+
+    // CG workspace
+    DevBuf<double> rbuf, s, dvec, Ad, partials, sc, xbuf;
+    double *hostSc = nullptr;  // pinned mirror of sc
+    int partialCount = 0;
+
+    // Galerkin constants
+    DevBuf<double> Kc64, phis64;
+    DevBuf<float> Kc32, phis32;
+
+    // CUDA graphs of one preconditioned CG iteration, keyed by solver options
+    struct GraphKey {
+        int64_t mgIter, sweeps;
+        int fmg, sym, prec, matvec;
+        uint64_t maskVersion;
+        int nfree;
+        bool operator<(const GraphKey &o) const {
+            return std::tie(mgIter, sweeps, fmg, sym, prec, matvec, maskVersion, nfree) <
+                   std::tie(o.mgIter, o.sweeps, o.fmg, o.sym, o.prec, o.matvec, o.maskVersion, o.nfree);
+        }
+    };
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    const double *graphX = nullptr;  // buffers baked into captured graphs
+    void clearGraphs();
+
+private:
+    void allocLevels();
+    void coarsenDirichlet();
+    void setupCoarsestIndex();
+    template <typename T>
+    void updateStiffnessT();
+    template <typename T>
+    void smoothT(int l, bool forward);
+    template <typename T>
+    void residualT(int l);
+    template <typename T>
+    void vcycleT(int l, int64_t sweeps, bool residualSystem);
+    template <typename T>
+    void fmgT(int l, int64_t sweeps, bool residualSystem);
+    template <typename T>
+    void preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg);
+    template <typename T>
+    void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
+    void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg);
+    void ensureStiffness();
+    template <typename T>
+    void levelOp(int l, int op, const double *a, const double *b, double *out, bool flag);
+};
+
+// Topology optimisation problem: MG compliance objective, a filter chain and one total-volume
+// constraint (TopologyOptimizationProblem.hh, TopologyOptimizationObjective.hh:71-105,
+// TopologyOptimizationConstraint.hh:24-40) with the OC step (OptimalityCriterion.hh:51-138).
+struct FilterSpec {
+    int kind;  // 0 smoothing, 1 projection
+    int radius;
+    int type;  // smoothing: 0 Const, 1 Linear
+    double beta;
+};
+
+class Problem {
+public:
+    Problem(MG *mg, const std::vector<FilterSpec> &filters, double volfrac);
+    MG *mg;
+    Grid *grid;
+    std::vector<FilterSpec> filters;
+    double volfrac;
+    int64_t cgIter = 100;
+    double tol = 1e-5;
+    int64_t mgIter = 1, mgSweeps = 2;
+    bool fmg = true, zeroInit = false;
+    bool varsSet = false;
+    PcgStats lastStats;
+    double lambda_min = 1, lambda_max = 2;
+    std::vector<DevBuf<double>> vars;  // chain intermediates [0] design ... [nf] physical
+    DevBuf<double> f, u, gradBuf, scratch, scratch2, partials, stepped, x0, dJ, dc;
+
+    void setVars(const double *x, bool device);
+    double objective();
+    void gradient(double *out, bool device);
+    double constraint();
+    void jacobian(double *out, bool device);
+    int64_t ocStep(double m, double p, double ctol);
+    void getU(double *out, bool device);
+    void getPhysical(double *out, bool device);
+    void filterApply(const double *x_dev, double *out_dev);
+    void backprop(double *g_dev);
+
+private:
+    double meanDev(const double *x);
+    double constraintAtVars(const double *x_dev);
+    void gradientDev(double *out);
+    void jacobianDev(double *out);
+};
+
+}  // namespace vfem

@@ -1,0 +1,126 @@
+// Launchers for the VoxelFEM GB300 kernels (sm_103a). All nodal vectors are SoA with
+// component stride Geom::ld; element fields are flat row-major (x slowest, z fastest).
+#pragma once
+#include "vfem_common.cuh"
+
+namespace vfem {
+
+// Dense 24x24 element matrix passed by value: kernel parameters live in the constant
+// bank, so warp-uniform indexing is a broadcast.
+template <typename T>
+struct Mat24 {
+    T a[576];
+};
+
+// Double-float copy of K0 for the FP64-accurate FP32 matvec.
+struct Mat24DF {
+    float hi[576];
+    float lo[576];
+};
+
+// ---------------- fine level (k_fine.cu) ----------------
+template <typename T>
+void launch_young_moduli(const Geom &g, const double *rho, T *Y, double E0, double Emin, double gamma, double q,
+                         int law, bool masking, cudaStream_t st);
+template <typename T>
+void launch_convert(const void *src, bool srcDouble, T *dst, int64_t n, cudaStream_t st);
+
+// out = +-K u (+ out if !zeroInit). zeroDirichlet zeroes constrained components of out.
+// partialDot (optional, FP64 path only) receives per-block partials of sum(u . out) over nondetached rows.
+template <typename T>
+void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat24<T> &K0, bool zeroInit,
+                        bool negate, const uint8_t *dmask, bool zeroDirichlet, double *partialDot,
+                        int partialBlocks, cudaStream_t st);
+// r = b - K u on nondetached rows, r = b elsewhere; constrained components zeroed.
+template <typename T>
+void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
+                          const uint8_t *dmask, cudaStream_t st);
+// One colour pass of block Gauss-Seidel on the fine level.
+template <typename T>
+void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
+                          const Mat24<T> &K0, cudaStream_t st);
+// FP64-accurate matvec in double-float arithmetic: out = K u (FP64 in/out), Y in FP64.
+void launch_applyk_fine_df(const Geom &g, const double *Y, const double *u, double *out, const Mat24DF &K0,
+                           const uint8_t *dmask, bool zeroDirichlet, double *partialDot, int partialBlocks,
+                           cudaStream_t st);
+
+void launch_compliance_gradient(const Geom &g, const double *rho, const double *u, double *grad, const Mat24<double> &K0,
+                                double E0, double Emin, double gamma, double q, int law, const double *grav,
+                                double vol, cudaStream_t st);
+void launch_element_energy(const Geom &g, const double *Y, const double *u, double *out, const Mat24<double> &K0,
+                           cudaStream_t st);
+void launch_build_gravity_load(const Geom &g, const double *rho, double *f, const double *grav, double vol,
+                               cudaStream_t st);
+
+// ---------------- coarse levels (k_coarse.cu) ----------------
+template <typename T>
+void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, cudaStream_t st);
+template <typename T>
+void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask,
+                             cudaStream_t st);
+template <typename T>
+void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
+                             cudaStream_t st);
+template <typename T>
+void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st);
+template <typename T>
+void launch_interpolate(const Geom &gf, const Geom &gc, const T *coarse, T *fine, bool accumulate, cudaStream_t st);
+template <typename T>
+void launch_zero_dirichlet(const Geom &g, T *u, const uint8_t *dmask, cudaStream_t st);
+template <typename T>
+void launch_masked_zero(const Geom &g, T *u, int margin, cudaStream_t st);
+template <typename T>
+void launch_fill(T *p, T v, int64_t n, cudaStream_t st);
+// Galerkin coarsening. Element matrices are stored element-major: Ke[e * 576 + 24*row + col].
+template <typename T>
+void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc /*8*576*/, T *Ke1, cudaStream_t st);
+template <typename T>
+void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis /*8*64*/, T *Kec, cudaStream_t st);
+template <typename T>
+void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_t st);
+template <typename T>
+void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, cudaStream_t st);
+template <typename Tdst, typename Tsrc>
+void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st);
+
+// ---------------- dense coarsest solve + vector ops (k_linalg.cu) ----------------
+template <typename T>
+void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, cudaStream_t st);
+void launch_symmetrize(double *A, int n, cudaStream_t st);
+// In place: A (n x n, row-major) -> A^{-1} via blocked Cholesky; status[0] set nonzero if not SPD.
+void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st);
+template <typename T>
+void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, int nfree, const T *b, T *x,
+                         double *scratch, cudaStream_t st);
+
+// Deterministic masked reductions: fixed grid of REDUCE_BLOCKS partials, then one block.
+constexpr int REDUCE_BLOCKS = 4 * NUM_SMS;
+template <typename Ta, typename Tb>
+void launch_masked_dot_partials(const Geom &g, const Ta *a, const Tb *b, double *partials, cudaStream_t st);
+// scalars layout for the CG loop (double[16]):
+//   0 rMr, 1 rMr_old, 2 beta, 3 alpha, 4 dAd, 5 rsq, 6 first, 7 bnorm2
+void launch_finalize(const double *partials, int n, double *out, cudaStream_t st);
+void launch_cg_beta(const double *partials, int n, double *sc, cudaStream_t st);
+void launch_cg_alpha(const double *partials, int n, double *sc, cudaStream_t st);
+void launch_cg_rsq(const double *partials, int n, double *sc, double *hostMirror, cudaStream_t st);
+// s <- (s with Dirichlet comps zeroed) where s comes from src (FP64 or FP32); partials of r.s (masked)
+template <typename Ts>
+void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
+                           double *partials, cudaStream_t st);
+void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, cudaStream_t st);
+void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
+                      double *partials, cudaStream_t st);
+void launch_copy(double *dst, const double *src, int64_t n, cudaStream_t st);
+template <typename T>
+void launch_enforce_dirichlet(const Geom &g, T *u, const uint8_t *dmask, const double *dval, cudaStream_t st);
+
+// ---------------- topology optimisation (k_topopt.cu) ----------------
+void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st);
+void launch_projection(int64_t n, double beta, const double *in, double *out, cudaStream_t st);
+void launch_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out,
+                                cudaStream_t st);
+void launch_oc_update(int64_t n, const double *x0, const double *dJ, const double *dc, double lambda, double m,
+                      double p, double *out, cudaStream_t st);
+void launch_sum_partials(const double *x, int64_t n, double *partials, cudaStream_t st);
+
+}  // namespace vfem

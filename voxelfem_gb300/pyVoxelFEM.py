@@ -1,0 +1,840 @@
+"""Drop-in counterpart of VoxelFEM's pybind11 module ``pyVoxelFEM`` for the solve path.
+
+Names, arguments, defaults, return shapes and error behaviour follow
+python_bindings/VoxelFEM.cc (pyVoxelFEM) so that reference scripts run
+unchanged on the GB300 library. Every numerical operation runs in the CUDA
+library through the C ABI of include/vfem.h; nodal fields are float64 arrays of
+shape (numNodes, 3) and element fields flat (numElements,) arrays in row-major
+grid order, as the reference's Eigen type casters produce.
+
+Scope: 3D trilinear voxels in double precision ([1, 1, 1], NumberType.DOUBLE).
+Multigrid solvers additionally expose a mixed-precision mode
+(``setPrecision("mixed")``: FP32 V-cycle inside FP64 CG) that the reference
+does not have.
+"""
+import ctypes as C
+import enum
+import json
+import os
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, ptr
+
+
+class NumberType(enum.IntEnum):
+    DOUBLE = 0
+    FLOAT = 1
+
+
+class InterpolationLaw(enum.IntEnum):
+    SIMP = 0
+    RAMP = 1
+
+
+SIMP = InterpolationLaw.SIMP
+RAMP = InterpolationLaw.RAMP
+
+
+def _lib():
+    return _capi.load()
+
+
+def _as_vfield(u, nn):
+    a = np.asarray(u, dtype=np.float64)
+    if a.shape != (nn, 3):
+        if a.size == 3 * nn and a.ndim == 1:
+            a = a.reshape(nn, 3)
+        else:
+            raise RuntimeError("Invalid input size")
+    return np.asfortranarray(a)
+
+
+def _new_vfield(nn):
+    return np.zeros((nn, 3), order="F")
+
+
+def _as_elems(x, ne):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
+    if a.size != ne:
+        raise RuntimeError("Invalid input size")
+    return a
+
+
+def _cmask(mask):
+    bits = 0
+    for ch in mask:
+        if ch not in "xyz":
+            raise RuntimeError("Invalid component mask " + mask)
+        bits |= 1 << "xyz".index(ch)
+    return bits
+
+
+def _arr3(v):
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(3))
+    return a
+
+
+def TensorProductSimulator(degreesPerDimension, domainBBox, elementsPerDimension, numberType=NumberType.DOUBLE):
+    """Factory of pyVoxelFEM.TensorProductSimulator (VoxelFEM.cc:423-430)."""
+    degs = [int(d) for d in degreesPerDimension]
+    if degs != [1, 1, 1] or int(numberType) != int(NumberType.DOUBLE):
+        raise RuntimeError("No template instantiation matching degreesPerDimension/number type!")
+    return TensorProductSimulator_3D(domainBBox, elementsPerDimension)
+
+
+class TensorProductSimulator_3D:
+    """TensorProductSimulator<double, 1, 1, 1> (TensorProductSimulator.hh:166-623)."""
+
+    def __init__(self, domainBBox, elementsPerDimension):
+        bb = [np.asarray(domainBBox[0], dtype=np.float64).reshape(3), np.asarray(domainBBox[1], dtype=np.float64).reshape(3)]
+        ne = np.ascontiguousarray(np.asarray(elementsPerDimension, dtype=np.int64).reshape(3))
+        h = C.c_void_p()
+        check(_lib().vfem_grid_create(ne.ctypes.data_as(_capi._i64), _capi.dptr(np.ascontiguousarray(bb[0])),
+                                      _capi.dptr(np.ascontiguousarray(bb[1])), C.byref(h)))
+        self._h = h
+        self._bbox = (bb[0].copy(), bb[1].copy())
+        self._ne = tuple(int(v) for v in ne)
+        self._nn = (self._ne[0] + 1) * (self._ne[1] + 1) * (self._ne[2] + 1)
+        self._nel = self._ne[0] * self._ne[1] * self._ne[2]
+        self._forces = np.zeros((self._nn, 3), order="F")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_grid_destroy(h)
+            self._h = None
+
+    # --- sizes / geometry ---
+    def numNodes(self):
+        return self._nn
+
+    def numElements(self):
+        return self._nel
+
+    @property
+    def gridShape(self):
+        return np.array(self._ne)
+
+    @property
+    def NbElementsPerDimension(self):
+        return np.array(self._ne)
+
+    @property
+    def NbNodesPerDimension(self):
+        return np.array([n + 1 for n in self._ne])
+
+    @property
+    def domain(self):
+        return (self._bbox[0].copy(), self._bbox[1].copy())
+
+    bbox = domain
+
+    @property
+    def dx(self):
+        return (self._bbox[1] - self._bbox[0]) / np.array(self._ne)
+
+    @property
+    def elementVolume(self):
+        return float(np.prod(self.dx))
+
+    def nodePosition(self, ni):
+        nn = self.NbNodesPerDimension
+        i, rem = divmod(int(ni), nn[1] * nn[2])
+        j, k = divmod(rem, nn[2])
+        return self._bbox[0] + np.array([i, j, k]) * self.dx
+
+    def elementNodes(self, ei):
+        ne = self._ne
+        i, rem = divmod(int(ei), ne[1] * ne[2])
+        j, k = divmod(rem, ne[2])
+        nn = self.NbNodesPerDimension
+        return np.array([((i + (l >> 2 & 1)) * nn[1] + j + (l >> 1 & 1)) * nn[2] + k + (l & 1) for l in range(8)])
+
+    def elemNodeGlobalIndex(self, ei, n):
+        return int(self.elementNodes(ei)[int(n)])
+
+    def elementIndexForGridCell(self, cellIdxs):
+        i, j, k = (int(v) for v in cellIdxs)
+        return (i * self._ne[1] + j) * self._ne[2] + k
+
+    # --- material ---
+    def readMaterial(self, materialPath):
+        with open(materialPath) as f:
+            mat = json.load(f)
+        if mat.get("type", "isotropic_material") not in ("isotropic_material", "isotropic"):
+            raise RuntimeError("Only isotropic materials are supported")
+        self.ETensor = (float(mat["young"]), float(mat["poisson"]))
+
+    @property
+    def ETensor(self):
+        E, nu = C.c_double(), C.c_double()
+        check(_lib().vfem_grid_get_etensor(self._h, C.byref(E), C.byref(nu)))
+        return (E.value, nu.value)
+
+    @ETensor.setter
+    def ETensor(self, value):
+        E, nu = value
+        check(_lib().vfem_grid_set_etensor(self._h, float(E), float(nu)))
+
+    def _params(self):
+        v = [C.c_double() for _ in range(4)]
+        law = C.c_int()
+        check(_lib().vfem_grid_get_material_params(self._h, *[C.byref(x) for x in v], C.byref(law)))
+        return [x.value for x in v] + [law.value]
+
+    def _set_param(self, idx, value):
+        p = self._params()
+        p[idx] = value
+        check(_lib().vfem_grid_set_material_params(self._h, p[0], p[1], p[2], p[3], int(p[4])))
+
+    E_0 = property(lambda self: self._params()[0], lambda self, v: self._set_param(0, float(v)))
+    E_min = property(lambda self: self._params()[1], lambda self, v: self._set_param(1, float(v)))
+    gamma = property(lambda self: self._params()[2], lambda self, v: self._set_param(2, float(v)))
+    q = property(lambda self: self._params()[3], lambda self, v: self._set_param(3, float(v)))
+    interpolationLaw = property(lambda self: InterpolationLaw(self._params()[4]),
+                                lambda self, v: self._set_param(4, int(v)))
+
+    @property
+    def gravity(self):
+        g = np.zeros(3)
+        check(_lib().vfem_grid_get_gravity(self._h, _capi.dptr(g)))
+        return g
+
+    @gravity.setter
+    def gravity(self, g):
+        check(_lib().vfem_grid_set_gravity(self._h, _capi.dptr(_arr3(g))))
+
+    def fullDensityElementStiffnessMatrix(self):
+        K = np.empty(576)
+        check(_lib().vfem_grid_get_k0(self._h, _capi.dptr(K)))
+        return K.reshape(24, 24)
+
+    def elementStiffnessMatrix(self, ei):
+        return self.elementYoungModulusScaleFactor(ei) * self.fullDensityElementStiffnessMatrix()
+
+    # --- densities ---
+    def getDensities(self):
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid_get_densities(self._h, ptr(out)))
+        return out
+
+    def setDensities(self, rho):
+        if np.asarray(rho).size != self._nel:
+            raise RuntimeError("Incorrect rho size")
+        a = _as_elems(rho, self._nel)
+        check(_lib().vfem_grid_set_densities(self._h, ptr(a)))
+
+    def setUniformDensities(self, density):
+        check(_lib().vfem_grid_set_uniform_densities(self._h, float(density)))
+
+    def setDensity(self, ei, value):
+        if value > 1.0 or value < 0:
+            raise RuntimeError("Density value (%g) has to be in between 0 and 1" % value)
+        rho = self.getDensities()
+        rho[int(ei)] = value
+        self.setDensities(rho)
+
+    def elementDensity(self, ei):
+        return float(self.getDensities()[int(ei)])
+
+    def getYoungModulusScaleFactor(self):
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid_get_young_moduli(self._h, ptr(out)))
+        return out
+
+    def elementYoungModulusScaleFactor(self, ei):
+        return float(self.getYoungModulusScaleFactor()[int(ei)])
+
+    # --- boundary conditions ---
+    def addDirichletCondition(self, u, minCorner, maxCorner, componentMask="xyz"):
+        check(_lib().vfem_grid_add_dirichlet(self._h, _capi.dptr(_arr3(u)), _capi.dptr(_arr3(minCorner)),
+                                             _capi.dptr(_arr3(maxCorner)), _cmask(componentMask)))
+
+    def applySymmetryConditions(self, symmetry_axes, minMaxFace=(False, False, False)):
+        ax = (C.c_int * 3)(*[int(bool(v)) for v in symmetry_axes])
+        mf = (C.c_int * 3)(*[int(bool(v)) for v in minMaxFace])
+        check(_lib().vfem_grid_apply_symmetry(self._h, ax, mf))
+
+    def setNodalForces(self, forces):
+        """Dense nodal force boundary condition (BCBuilder::setForce for every node)."""
+        f = _as_vfield(forces, self._nn)
+        self._forces = f.copy(order="F")
+        check(_lib().vfem_grid_set_nodal_forces(self._h, ptr(f)))
+
+    def applyDisplacementsAndLoadsFromFile(self, bcPath):
+        apply_bc_file(self, bcPath)
+
+    def getDirichletMask(self):
+        m = np.zeros(self._nn, dtype=np.uint8)
+        check(_lib().vfem_grid_get_dirichlet_mask(self._h, m.ctypes.data_as(_capi._u8)))
+        return np.stack([(m >> c) & 1 for c in range(3)], axis=1).astype(bool)
+
+    def getForceMask(self):
+        return self._forces != 0
+
+    def getDirichletVarsAndValues(self):
+        m = self.getDirichletMask()
+        nodes, comps = np.nonzero(m)
+        return (list(3 * nodes + comps), [0.0] * len(nodes))
+
+    # --- layer-by-layer fabrication mask ---
+    def setFabricationMaskHeightByLayer(self, l):
+        check(_lib().vfem_grid_set_mask_layer(self._h, int(l)))
+
+    def getFabricationMaskHeight(self):
+        h = C.c_double()
+        check(_lib().vfem_grid_get_mask_height(self._h, C.byref(h)))
+        return h.value
+
+    # --- physics ---
+    def applyK(self, u):
+        u = _as_vfield(u, self._nn)
+        out = _new_vfield(self._nn)
+        check(_lib().vfem_grid_apply_k(self._h, ptr(u), ptr(out)))
+        return out
+
+    def buildLoadVector(self):
+        out = _new_vfield(self._nn)
+        check(_lib().vfem_grid_build_load(self._h, ptr(out)))
+        return out
+
+    def complianceGradient(self, u):
+        u = _as_vfield(u, self._nn)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid_compliance_gradient(self._h, ptr(u), ptr(out)))
+        return out
+
+    def elementEnergyDensity(self, u):
+        u = _as_vfield(u, self._nn)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid_element_energy(self._h, ptr(u), ptr(out)))
+        return out
+
+    def solve(self, f):
+        """Direct solve (TensorProductSimulator::solve) through a zero-coarsening hierarchy."""
+        mg = self.multigridSolver(0)
+        return mg.preconditionedConjugateGradient(np.zeros((self._nn, 3)), f, 1, 0.0)
+
+    def multigridSolver(self, numCoarseningLevels):
+        return MultigridSolver(self, int(numCoarseningLevels))
+
+
+def apply_bc_file(tps, path):
+    """Minimal reader of the reference's `.bc` JSON regions ("box%" or "box"; types
+    "dirichlet[x|y|z...]" and "force"; forces split equally over the region's nodes,
+    TensorProductSimulator.hh:600-652)."""
+    with open(path) as f:
+        spec = json.load(f)
+    lo, hi = tps.domain
+    size = hi - lo
+    nn = tps.NbNodesPerDimension
+    dx = tps.dx
+    I, J, K = np.meshgrid(np.arange(nn[0]), np.arange(nn[1]), np.arange(nn[2]), indexing="ij")
+    pos = np.stack([lo[0] + I.ravel() * dx[0], lo[1] + J.ravel() * dx[1], lo[2] + K.ravel() * dx[2]], axis=1)
+    forces = np.zeros((tps.numNodes(), 3))
+    have_force = False
+    for reg in spec["regions"]:
+        if "box%" in reg:
+            b = reg["box%"]
+            mn = lo + np.asarray(b["minCorner"], dtype=float) * size
+            mx = lo + np.asarray(b["maxCorner"], dtype=float) * size
+        elif "box" in reg:
+            mn = np.asarray(reg["box"]["minCorner"], dtype=float)
+            mx = np.asarray(reg["box"]["maxCorner"], dtype=float)
+        else:
+            raise RuntimeError("Unsupported boundary condition region")
+        typ = reg["type"]
+        val = np.asarray(reg["value"], dtype=float)
+        inside = np.all((pos >= mn) & (pos <= mx), axis=1)
+        if typ.startswith("dirichlet"):
+            comps = typ[len("dirichlet"):] or "xyz"
+            if not inside.any():
+                raise RuntimeError("Dirichlet region unmatched")
+            tps.addDirichletCondition(val, mn, mx, comps)
+        elif typ == "force":
+            idx = np.nonzero(inside)[0]
+            if idx.size == 0:
+                raise RuntimeError("Force constraint region unmatched")
+            forces[idx] = val / idx.size
+            have_force = True
+        else:
+            raise RuntimeError('Illegal constraint type, only "dirichlet" and "force" accepted')
+    if have_force:
+        tps.setNodalForces(forces)
+
+
+class _LevelSimulator:
+    """Read-only view of a coarse level (MultigridSolver::getSimulator(l), l > 0)."""
+
+    def __init__(self, mg, l):
+        self._mg, self._l = mg, l
+        ne = np.zeros(3, dtype=np.int64)
+        check(_lib().vfem_mg_level_dims(mg._h, l, ne.ctypes.data_as(_capi._i64)))
+        self._ne = tuple(int(v) for v in ne)
+
+    def numNodes(self):
+        return int(np.prod([n + 1 for n in self._ne]))
+
+    def numElements(self):
+        return int(np.prod(self._ne))
+
+    @property
+    def NbElementsPerDimension(self):
+        return np.array(self._ne)
+
+    gridShape = NbElementsPerDimension
+
+    @property
+    def NbNodesPerDimension(self):
+        return np.array([n + 1 for n in self._ne])
+
+    def getDirichletMask(self):
+        m = np.zeros(self.numNodes(), dtype=np.uint8)
+        check(_lib().vfem_mg_level_dirichlet_mask(self._mg._h, self._l, m.ctypes.data_as(_capi._u8)))
+        return np.stack([(m >> c) & 1 for c in range(3)], axis=1).astype(bool)
+
+
+class MultigridSolver:
+    """MultigridSolver<double, 1, 1, 1> (MultigridSolver.hh); created by tps.multigridSolver(levels)."""
+
+    def __init__(self, tps, numCoarseningLevels):
+        h = C.c_void_p()
+        check(_lib().vfem_mg_create(tps._h, int(numCoarseningLevels), C.byref(h)))
+        self._h = h
+        self._tps = tps  # keeps the fine simulator alive (MultigridSolver.hh:1164)
+        n = C.c_int()
+        check(_lib().vfem_mg_num_levels(h, C.byref(n)))
+        self.numLevels = n.value
+        self._prec = "fp64"
+        self.lastStats = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_mg_destroy(h)
+            self._h = None
+
+    def _nn(self, l):
+        return self.getSimulator(l).numNodes()
+
+    def getSimulator(self, l):
+        if l == 0:
+            return self._tps
+        if l < 0 or l >= self.numLevels:
+            raise IndexError("level out of range")
+        return _LevelSimulator(self, l)
+
+    def setPrecision(self, precision="fp64", outerMatvec="df"):
+        """'fp64' (the reference's method) or 'mixed' (FP32 V-cycle in FP64 CG); the outer
+        matvec of the mixed mode is 'df' (double-float) or 'fp64'."""
+        p = {"fp64": 0, "mixed": 1}[precision]
+        m = {"fp64": 0, "df": 1}[outerMatvec]
+        check(_lib().vfem_mg_set_precision(self._h, p, m))
+        self._prec = precision
+
+    def setUseGraphs(self, use):
+        check(_lib().vfem_mg_set_use_graphs(self._h, int(bool(use))))
+
+    def setSymmetricGaussSeidel(self, symmetric):
+        check(_lib().vfem_mg_set_symmetric_gs(self._h, int(bool(symmetric))))
+
+    def setFabricationMaskHeightByLayer(self, h):
+        check(_lib().vfem_mg_set_mask_layer(self._h, int(h)))
+
+    def updateStiffnessMatrices(self):
+        check(_lib().vfem_mg_update_stiffness(self._h))
+
+    def applyK(self, l, u):
+        nn = self._nn(l)
+        u = _as_vfield(u, nn)
+        out = _new_vfield(nn)
+        check(_lib().vfem_mg_apply_k(self._h, int(l), ptr(u), ptr(out)))
+        return out
+
+    def computeResidual(self, l, u, b):
+        nn = self._nn(l)
+        u, b = _as_vfield(u, nn), _as_vfield(b, nn)
+        out = _new_vfield(nn)
+        check(_lib().vfem_mg_residual(self._h, int(l), ptr(u), ptr(b), ptr(out)))
+        return out
+
+    def zeroOutDirichletComponents(self, l, u):
+        u = _as_vfield(u, self._nn(l)).copy(order="F")
+        check(_lib().vfem_mg_zero_dirichlet(self._h, int(l), ptr(u)))
+        return u
+
+    def smoothingMulticoloredGS(self, l, u, b, forwardSweep=True):
+        nn = self._nn(l)
+        u = _as_vfield(u, nn).copy(order="F")
+        b = _as_vfield(b, nn)
+        check(_lib().vfem_mg_smooth(self._h, int(l), ptr(u), ptr(b), int(bool(forwardSweep))))
+        return u
+
+    def restriction(self, l, fine):
+        fine = _as_vfield(fine, self._nn(l))
+        out = _new_vfield(self._nn(l + 1))
+        check(_lib().vfem_mg_restrict(self._h, int(l), ptr(fine), ptr(out)))
+        return out
+
+    def interpolation(self, l, coarse, fine=None, accumulate=False):
+        coarse = _as_vfield(coarse, self._nn(l + 1))
+        out = _new_vfield(self._nn(l)) if fine is None else _as_vfield(fine, self._nn(l)).copy(order="F")
+        check(_lib().vfem_mg_interpolate(self._h, int(l), ptr(coarse), ptr(out), int(bool(accumulate))))
+        return out
+
+    def coarseSolve(self, b):
+        nn = self._nn(self.numLevels - 1)
+        b = _as_vfield(b, nn)
+        out = _new_vfield(nn)
+        check(_lib().vfem_mg_coarse_solve(self._h, ptr(b), ptr(out)))
+        return out
+
+    def solve(self, u, f, numSteps, numSmoothingSteps, stiffnessUpdated=False, zeroDirichlet=False,
+              it_callback=None, fullMultigrid=False):
+        nn = self._nn(0)
+        u, f = _as_vfield(u, nn), _as_vfield(f, nn)
+        if it_callback is None:
+            out = _new_vfield(nn)
+            check(_lib().vfem_mg_solve(self._h, ptr(u), ptr(f), int(numSteps), int(numSmoothingSteps),
+                                       int(bool(zeroDirichlet)), int(bool(fullMultigrid)), ptr(out)))
+            return out
+        # per-step callbacks: one cycle at a time (FMG only on the first step)
+        x = u
+        for i in range(int(numSteps)):
+            out = _new_vfield(nn)
+            check(_lib().vfem_mg_solve(self._h, ptr(x), ptr(f), 1, int(numSmoothingSteps), int(bool(zeroDirichlet)),
+                                       int(bool(fullMultigrid) and i == 0), ptr(out)))
+            it_callback(i, out)
+            x = out
+        return x
+
+    def preconditionedConjugateGradient(self, u, b, maxIter, tol, it_callback=None, mgIterations=1,
+                                        mgSmoothingIterations=1, fullMultigrid=False):
+        nn = self._nn(0)
+        x = _as_vfield(u, nn).copy(order="F")
+        b = _as_vfield(b, nn)
+        stats = _capi.PcgStats()
+        cb = _capi.PCG_CALLBACK()
+        if it_callback is not None:
+            def _cb(user, it, rnorm, xdev, rdev):
+                xa = _device_to_host(xdev, nn)
+                ra = _device_to_host(rdev, nn)
+                it_callback(int(it), xa, ra)
+                return 0
+            cb = _capi.PCG_CALLBACK(_cb)
+        check(_lib().vfem_mg_pcg(self._h, ptr(x), ptr(b), int(maxIter), float(tol), int(mgIterations),
+                                 int(mgSmoothingIterations), int(bool(fullMultigrid)), 0, cb, None, C.byref(stats)))
+        self.lastStats = stats
+        return x
+
+
+_cudart = None
+
+
+def _device_to_host(dev_ptr, nn):
+    """Copy a device FP64 (nn, 3) field to a new host array (used by per-iteration callbacks)."""
+    global _cudart
+    if _cudart is None:
+        import ctypes.util
+        name = ctypes.util.find_library("cudart") or "libcudart.so"
+        try:
+            _cudart = C.CDLL(name)
+        except OSError:
+            import glob
+            cands = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+            _cudart = C.CDLL(cands[0])
+    out = np.empty((nn, 3), order="F")
+    rc = _cudart.cudaMemcpy(C.c_void_p(out.ctypes.data), C.c_void_p(dev_ptr), C.c_size_t(out.nbytes), 4)
+    if rc != 0:
+        raise RuntimeError("cudaMemcpy failed in callback")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Topology optimisation layer
+# ---------------------------------------------------------------------------
+class Filter:
+    def apply(self, x):
+        raise NotImplementedError
+
+
+class SmoothingFilter(Filter):
+    """SmoothingFilter(radius=1, type=Const) (TopologyOptimizationFilter.hh:285-400)."""
+
+    class Type(enum.IntEnum):
+        Const = 0
+        Linear = 1
+
+    def __init__(self, radius=1, type=None):
+        self.radius = int(radius)
+        self.type = SmoothingFilter.Type.Const if type is None else SmoothingFilter.Type(int(type))
+        self._dims = None
+
+    def setInputDimensions(self, gridDims):
+        self._dims = tuple(int(v) for v in gridDims)
+
+    setOutputDimensions = setInputDimensions
+
+    @property
+    def inputDimensions(self):
+        return np.array(self._dims)
+
+    outputDimensions = inputDimensions
+
+    def apply(self, x):
+        if self._dims is None:
+            raise RuntimeError("Filter grid dimensions not set. Initialize a TopologyOptimizationProblem object "
+                               "with this filter before using it.")
+        a = _as_elems(x, int(np.prod(self._dims)))
+        out = np.empty_like(a)
+        dims = np.array(self._dims, dtype=np.int64)
+        check(_lib().vfem_smoothing_filter(dims.ctypes.data_as(_capi._i64), self.radius, int(self.type), ptr(a),
+                                           ptr(out)))
+        return out
+
+    backprop = lambda self, g, vars_=None: self.apply(g)
+
+
+class ProjectionFilter(Filter):
+    """ProjectionFilter(beta) (TopologyOptimizationFilter.hh:189-245)."""
+
+    def __init__(self, beta=1.0):
+        if beta <= 0:
+            raise RuntimeError("Beta parameter has to be positive (received beta = %g)" % beta)
+        self._beta = float(beta)
+        self._dims = None
+
+    @property
+    def beta(self):
+        return self._beta
+
+    @beta.setter
+    def beta(self, b):
+        if b <= 0:
+            raise RuntimeError("Beta parameter has to be positive (received beta = %g)" % b)
+        self._beta = float(b)
+
+    def setInputDimensions(self, gridDims):
+        self._dims = tuple(int(v) for v in gridDims)
+
+    setOutputDimensions = setInputDimensions
+
+    def apply(self, x):
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
+        out = np.empty_like(a)
+        check(_lib().vfem_projection_apply(a.size, self._beta, ptr(a), ptr(out)))
+        return out
+
+    def backprop(self, g, vars_):
+        g = np.ascontiguousarray(np.asarray(g, dtype=np.float64).reshape(-1))
+        v = np.ascontiguousarray(np.asarray(vars_, dtype=np.float64).reshape(-1))
+        out = np.empty_like(g)
+        check(_lib().vfem_projection_backprop(g.size, self._beta, ptr(g), ptr(v), ptr(out)))
+        return out
+
+    def invert(self, filteredValue):
+        if filteredValue > 1.0 or filteredValue < 0.0:
+            raise RuntimeError("ProjectionFilter::invert domain error: target density for inversion is outside [0, 1].")
+        return np.arctanh((2 * filteredValue - 1) * np.tanh(0.5 * self._beta)) / self._beta + 0.5
+
+
+class FilterChain:
+    """FilterChain (TopologyOptimizationFilter.hh:90-187), host-side composition of device filters."""
+
+    def __init__(self, filters, outGridDimensions):
+        self.filters = list(filters)
+        for f in self.filters:
+            f.setInputDimensions(outGridDimensions)
+        self._dims = tuple(int(v) for v in outGridDimensions)
+        self._vars = None
+
+    def numVars(self):
+        return int(np.prod(self._dims))
+
+    numPhysicalVars = numVars
+
+    def gridDims(self):
+        return np.array(self._dims)
+
+    physicalGridDims = gridDims
+
+    def setDesignVars(self, xDesign):
+        v = [_as_elems(xDesign, self.numVars())]
+        for f in self.filters:
+            v.append(f.apply(v[-1]))
+        self._vars = v
+
+    def designVars(self):
+        return self._vars[0].copy()
+
+    def physicalVars(self):
+        return self._vars[-1].copy()
+
+    def backprop(self, g):
+        g = _as_elems(g, self.numVars())
+        for i in range(len(self.filters) - 1, -1, -1):
+            g = self.filters[i].backprop(g, self._vars[i])
+        return g
+
+
+class TotalVolumeConstraint:
+    """TotalVolumeConstraint(volumeFraction) (TopologyOptimizationConstraint.hh:24-40)."""
+
+    def __init__(self, volumeFraction):
+        self.volumeFraction = float(volumeFraction)
+
+    def evaluate(self, x):
+        return 1.0 - np.mean(x) / self.volumeFraction
+
+
+class MultigridComplianceObjective:
+    """MultigridComplianceObjective(mg) (TopologyOptimizationObjective.hh:71-105)."""
+
+    def __init__(self, mg_solver):
+        self.mg = mg_solver
+        self.cgIter = 100
+        self.tol = 1e-5
+        self.mgIterations = 1
+        self.mgSmoothingIterations = 2
+        self.fullMultigrid = True
+        self.zeroInit = False
+        self.residual_cb = None
+        tps = mg_solver.getSimulator(0)
+        self._f = tps.buildLoadVector()
+        self._problem = None
+        # the reference solves once at construction (updateCache of the current densities)
+        self._u = mg_solver.preconditionedConjugateGradient(np.zeros_like(self._f), self._f, self.cgIter, self.tol,
+                                                            None, self.mgIterations, self.mgSmoothingIterations,
+                                                            self.fullMultigrid)
+
+    def u(self):
+        if self._problem is not None:
+            return self._problem._get_u()
+        return self._u
+
+    def f(self):
+        return self._f
+
+    def compliance(self):
+        return 0.5 * float(np.sum(self.f() * self.u()))
+
+    def gradient(self):
+        return self.mg.getSimulator(0).complianceGradient(self.u())
+
+
+def ComplianceObjective(simulator):
+    """ComplianceObjective(sim): direct solve; served by a zero-coarsening MG objective."""
+    return MultigridComplianceObjective(simulator.multigridSolver(0))
+
+
+class TopologyOptimizationProblem:
+    """TopologyOptimizationProblem(simulator, objective, constraints, filters) (TopologyOptimizationProblem.hh)."""
+
+    def __init__(self, simulator, objective, constraints, filters):
+        if len(constraints) != 1 or not isinstance(constraints[0], TotalVolumeConstraint):
+            raise RuntimeError("Applicable only for a topology optimization with a single (volume) constraint")
+        self._sim = simulator
+        self._objective = objective
+        self.constraints = list(constraints)
+        self.filters = list(filters)
+        self.filterChain = FilterChain(self.filters, simulator.NbElementsPerDimension)
+        kinds, radii, types, betas = [], [], [], []
+        for f in self.filters:
+            if isinstance(f, SmoothingFilter):
+                kinds.append(0); radii.append(f.radius); types.append(int(f.type)); betas.append(0.0)
+            elif isinstance(f, ProjectionFilter):
+                kinds.append(1); radii.append(0); types.append(0); betas.append(f.beta)
+            else:
+                raise RuntimeError("Unsupported filter type " + type(f).__name__)
+        n = max(len(kinds), 1)
+        h = C.c_void_p()
+        check(_lib().vfem_problem_create(objective.mg._h, len(kinds), (C.c_int * n)(*kinds), (C.c_int * n)(*radii),
+                                         (C.c_int * n)(*types), (C.c_double * n)(*betas),
+                                         self.constraints[0].volumeFraction, C.byref(h)))
+        self._h = h
+        objective._problem = self
+        self._ne = simulator.numElements()
+        self._varsSet = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_problem_destroy(h)
+            self._h = None
+
+    @property
+    def objective(self):
+        return self._objective
+
+    def _sync_solver(self):
+        o = self._objective
+        check(_lib().vfem_problem_set_solver(self._h, int(o.cgIter), float(o.tol), int(o.mgIterations),
+                                             int(o.mgSmoothingIterations), int(bool(o.fullMultigrid)),
+                                             int(bool(o.zeroInit))))
+
+    def numVars(self):
+        return self._ne
+
+    def getVars(self):
+        out = np.empty(self._ne)
+        check(_lib().vfem_problem_get_vars(self._h, ptr(out)))
+        return out
+
+    def setVars(self, x, forceUpdate=False):
+        self._sync_solver()
+        a = _as_elems(x, self._ne)
+        check(_lib().vfem_problem_set_vars(self._h, ptr(a)))
+        self.filterChain.setDesignVars(a)
+        self._varsSet = True
+        return True
+
+    def _get_u(self):
+        nn = self._sim.numNodes()
+        out = _new_vfield(nn)
+        check(_lib().vfem_problem_get_u(self._h, ptr(out)))
+        return out
+
+    def evaluateObjective(self):
+        v = C.c_double()
+        check(_lib().vfem_problem_objective(self._h, C.byref(v)))
+        return v.value
+
+    def evaluateObjectiveGradient(self):
+        out = np.empty(self._ne)
+        check(_lib().vfem_problem_gradient(self._h, ptr(out)))
+        return out
+
+    def evaluateConstraints(self):
+        v = C.c_double()
+        check(_lib().vfem_problem_constraint(self._h, C.byref(v)))
+        return np.array([v.value])
+
+    def evaluateConstraintsJacobian(self):
+        out = np.empty(self._ne)
+        check(_lib().vfem_problem_jacobian(self._h, ptr(out)))
+        return out.reshape(1, -1)
+
+    def getDensities(self):
+        return self._sim.getDensities()
+
+    def lastSolveStats(self):
+        s = _capi.PcgStats()
+        check(_lib().vfem_problem_last_solve(self._h, C.byref(s)))
+        return s
+
+
+class OCOptimizer:
+    """OCOptimizer(problem).step(m=0.2, p=0.5, ctol=1e-6, inplace=True) (OptimalityCriterion.hh:51-138)."""
+
+    def __init__(self, problem):
+        self.problem = problem
+        self.lastProbes = 0
+
+    def step(self, m=0.2, p=0.5, ctol=1e-6, inplace=True):
+        probes = C.c_int64()
+        self.problem._sync_solver()
+        check(_lib().vfem_problem_oc_step(self.problem._h, float(m), float(p), float(ctol), C.byref(probes)))
+        self.lastProbes = probes.value
+        self.problem.filterChain.setDesignVars(self.problem.getVars())
