@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the VoxelFEM solve path on GB300.
+
+Workload: the 3D cantilever at 256x128x128 trilinear voxels (12.83M DOF),
+densities uniform[0.01, 1] (seed 0), E0 = 1, Emin = 1e-9, nu = 0.3, SIMP p = 3,
+6-level geometric multigrid (5 coarsenings), mgIterations = 1, 2 pre- and 2
+post-sweeps of the coloured block Gauss-Seidel, plain V-cycles, x0 = 0,
+relative residual 1e-8.
+
+A step is one MG-PCG solve from PCG entry to ||r||/||b|| <= 1e-8, including the
+density upload and the Galerkin rebuild of the hierarchy it triggers. ``value``
+is the mixed-precision (FP32 V-cycle, FP64 outer CG) time per solve with all
+inputs resident in HBM; the FP64 solve (the reference's method) is timed beside
+it. ``e2e`` is the same step through the public API with pinned host buffers.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--config c1|c2]
+
+With N > 1 (torchrun), every rank solves its own replica; the line reports the
+aggregate time per solve (max-over-ranks duration / (N * K)).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "MG-PCG time-to-1e-8 residual (mixed vs FP64, 12.7M DOF); applyK HBM GB/s"
+CONFIGS = {
+    # name: (elements, rho_lo, coarsenings)
+    "c2": ((256, 128, 128), 0.01, 5),
+    "c1": ((64, 32, 32), 0.3, 3),
+}
+# FP64 MG-PCG iterations to 1e-8 of these workloads, from full solves of the CPU oracle
+# (same algorithm as the GPU FP64 path, which reports its own count in every run).
+FP64_ITERATIONS = {"c2": None, "c1": 10}
+TOL = 1e-8
+KERNEL_NAMES = {0: "applyk_fine_fp64", 1: "applyk_fine_fp32", 2: "applyk_fine_df", 3: "gs_fine_sweep_fp32",
+                4: "gs_fine_sweep_fp64", 5: "residual_fine_fp32", 6: "gs_level1_sweep_fp32",
+                7: "residual_level1_fp32"}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline_sample(cfg_name, iterations_to_tol, threads=None):
+    """Time the CPU oracle (a restatement of the reference's solver) on a bounded sample of
+    the workload: set-up plus the first PCG iterations, extrapolated to the iteration count
+    of the full solve."""
+    from oracle import pyoracle as po
+    from voxelfem_gb300 import workloads as wl
+    ne, rho_lo, levels = CONFIGS[cfg_name]
+    threads = threads or os.cpu_count()
+    po.set_num_threads(threads)
+    sim = po.Sim(ne)
+    wl.setup_cantilever(sim, ne, rho_lo, 0)
+    mg = po.MG(sim, levels)
+    b = sim.buildLoadVector()
+    stamps = []
+    sample_iters = 3 if cfg_name == "c2" else 100
+    t0 = time.perf_counter()
+    mg.preconditionedConjugateGradient(np.zeros_like(b), b, sample_iters, TOL, lambda i, r: stamps.append(time.perf_counter()),
+                                       1, 2, False)
+    t1 = time.perf_counter()
+    done = mg.lastIterations
+    if iterations_to_tol is None or done >= iterations_to_tol or mg.lastRelativeResidual <= TOL:
+        est = t1 - t0
+        n_it = done
+        how = "full solve"
+    else:
+        first = stamps[0] - t0
+        per = (stamps[-1] - stamps[0]) / max(len(stamps) - 1, 1)
+        est = first + (iterations_to_tol - 1) * per
+        n_it = iterations_to_tol
+        how = "set-up + %d PCG iterations timed (%.2f s), extrapolated to %d iterations" % (done, t1 - t0, n_it)
+    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
+            "sample": "CPU oracle FP64 MG-PCG, %s cantilever %dx%dx%d, %s" % (cfg_name, ne[0], ne[1], ne[2], how),
+            "iterations": n_it, "sample_seconds": t1 - t0}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfg = args.config
+    vals, last = [], None
+    for _ in range(args.steps):
+        last = cpu_baseline_sample(cfg, FP64_ITERATIONS.get(cfg))
+        vals.append(last["value"])
+    v = float(np.mean(vals))
+    ne = CONFIGS[cfg][0]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1000, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cantilever %dx%dx%d Q1, rho U[%g,1] seed 0, %d coarsenings, FP64 MG-PCG to 1e-8"
+                       % (ne[0], ne[1], ne[2], CONFIGS[cfg][1], CONFIGS[cfg][2])},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": last["cores"], "kind": last["kind"],
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group(backend="nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    from voxelfem_gb300 import _capi
+    from voxelfem_gb300 import pyVoxelFEM as pv
+    from voxelfem_gb300 import workloads as wl
+
+    lib = _capi.load()
+    ne, rho_lo, levels = CONFIGS[args.config]
+    bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
+    sim = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
+    rho, f = wl.setup_cantilever(sim, ne, rho_lo, 0)
+    mg = sim.multigridSolver(levels)
+    nn, nel = sim.numNodes(), sim.numElements()
+    b_host = sim.buildLoadVector()
+    # device-resident inputs: SoA (3, nn) is the (nn, 3) column-major VField layout
+    b_d = torch.from_numpy(np.ascontiguousarray(b_host.T)).to("cuda")
+    rho_d = torch.from_numpy(rho).to("cuda")
+    x_d = torch.zeros(3, nn, dtype=torch.float64, device="cuda")
+    sptr = C.c_void_p()
+    _capi.check(lib.vfem_mg_get_stream(mg._h, C.byref(sptr)))
+    stream = torch.cuda.ExternalStream(sptr.value)
+    stats = _capi.PcgStats()
+    cb = _capi.PCG_CALLBACK()
+
+    def step_device():
+        with torch.cuda.stream(stream):
+            x_d.zero_()
+        _capi.check(lib.vfem_grid_set_densities(sim._h, C.c_void_p(rho_d.data_ptr())))
+        _capi.check(lib.vfem_mg_pcg(mg._h, C.c_void_p(x_d.data_ptr()), C.c_void_p(b_d.data_ptr()), 500, TOL, 1, 2,
+                                    0, 0, cb, None, C.byref(stats)))
+        return stats.iterations, stats.relres
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, k):
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        out = None
+        for _ in range(k):
+            out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        t1 = time.perf_counter()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / 1000.0, (t1 - t0), out
+
+    # ---------------- FP64 (the reference's method) ----------------
+    mg.setPrecision("fp64")
+    step_device()  # warm-up: hierarchy, graphs
+    k64 = max(1, min(args.steps, 2 if args.config == "c2" else args.steps))
+    t64, _, (it64, rr64) = timed(step_device, k64)
+    t64 /= k64
+    x64 = x_d.clone()
+    comp64 = 0.5 * float(torch.dot(b_d.flatten(), x64.flatten()))
+
+    # ---------------- mixed precision (headline) ----------------
+    mg.setPrecision("mixed", "df")
+    for _ in range(args.warmup):
+        step_device()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    cnt0 = C.c_uint64()
+    _capi.check(lib.vfem_kernel_launch_count(C.byref(cnt0)))
+    tmix, wall, (itmix, rrmix) = timed(step_device, args.steps)
+    cnt1 = C.c_uint64()
+    _capi.check(lib.vfem_kernel_launch_count(C.byref(cnt1)))
+    clk = clocks.stop()
+    tmix_step = tmix / args.steps
+    xm = x_d.clone()
+    compm = 0.5 * float(torch.dot(b_d.flatten(), xm.flatten()))
+    # true residual of the mixed solution in FP64
+    xm_host = xm.cpu().numpy().T.copy(order="F")
+    r = b_host - sim.applyK(xm_host)
+    r[sim.getDirichletMask()] = 0
+    true_rel = float(np.linalg.norm(r) / np.linalg.norm(b_host))
+
+    # ---------------- end to end through the public API, pinned host buffers ----------------
+    rho_p = torch.from_numpy(rho).pin_memory()
+    b_p = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
+    x_p = torch.zeros(3, nn, dtype=torch.float64).pin_memory()
+
+    def step_host():
+        x_p.zero_()
+        _capi.check(lib.vfem_grid_set_densities(sim._h, C.c_void_p(rho_p.data_ptr())))
+        _capi.check(lib.vfem_mg_pcg(mg._h, C.c_void_p(x_p.data_ptr()), C.c_void_p(b_p.data_ptr()), 500, TOL, 1, 2,
+                                    0, 0, cb, None, C.byref(stats)))
+        return 0.5 * float(np.dot(b_p.numpy().ravel(), x_p.numpy().ravel()))
+
+    step_host()
+    _, e2e_wall, _ = timed(step_host, args.steps)
+    e2e = e2e_wall / args.steps
+    h2d = rho.nbytes + 2 * 3 * nn * 8  # densities, b, x0
+    d2h = 3 * nn * 8
+
+    # ---------------- hot kernels: device time per launch (CUDA events on the solver stream) ----------------
+    hbm, peak_kind = peaks()
+    kernels = {}
+    for kid in (1, 2, 0, 3, 5, 6, 7):
+        ms = C.c_double()
+        nbytes = C.c_double()
+        reps = 3 if kid == 0 else 20
+        _capi.check(lib.vfem_mg_time_kernel(mg._h, kid, reps, C.byref(ms), C.byref(nbytes)))
+        kernels[KERNEL_NAMES[kid]] = {"ms": ms.value, "bytes": nbytes.value,
+                                      "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
+    # share per solve of the kernels of the mixed V-cycle (2 pre + 2 post sweeps per level)
+    per_iter = {
+        "gs_fine_sweep_fp32": 4 * kernels["gs_fine_sweep_fp32"]["ms"],
+        "applyk_fine_df": kernels["applyk_fine_df"]["ms"],
+        "residual_fine_fp32": kernels["residual_fine_fp32"]["ms"],
+        "gs_level1_sweep_fp32": 4 * kernels["gs_level1_sweep_fp32"]["ms"],
+    }
+    dom = max(per_iter, key=per_iter.get)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "kernel_traffic_%s.json" % args.config)
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(dom)
+    kd = kernels[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": kd["gbs"], "peak": hbm, "unit": "GB/s",
+                "frac": kd["gbs"] / hbm, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": kd["bytes"], "ms_per_launch": kd["ms"]}
+
+    line = {"metric": METRIC, "value": tmix_step if ws == 1 else tmix / (ws * args.steps), "unit": "s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmix_step * 1000,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "cantilever %dx%dx%d Q1 (%d DOF), rho U[%g,1] seed 0, %d coarsenings, mixed FP32 "
+                                   "V-cycle (2+2 block-GS sweeps) in FP64 CG, double-float outer matvec, tol 1e-8"
+                                   % (ne[0], ne[1], ne[2], 3 * nn, rho_lo, levels),
+                       "l2": "no flush: working set of every step (> 2 GB) exceeds the 129 MB L2"},
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roofline,
+            "clocks": clk,
+            "gpu_launches": int(cnt1.value - cnt0.value),
+            "mixed": {"s_per_solve": tmix_step, "iterations": int(itmix), "relres": rrmix, "true_relres": true_rel,
+                      "compliance": compm},
+            "fp64": {"s_per_solve": t64, "iterations": int(it64), "relres": rr64, "compliance": comp64,
+                     "steps": k64},
+            "speedup_mixed_vs_fp64": t64 / tmix_step,
+            "compliance_rel_err_mixed_vs_fp64": abs(compm - comp64) / abs(comp64),
+            "applyk_gbs": {"fp32": kernels["applyk_fine_fp32"]["gbs"], "fp64": kernels["applyk_fine_fp64"]["gbs"],
+                           "df": kernels["applyk_fine_df"]["gbs"]},
+            "kernels": kernels}
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -147,6 +147,16 @@ int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter,
                 int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
                 vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats);
 
+/* Benchmark hooks (no reference counterpart): the CUDA stream the solver launches on, the
+ * average device time of one launch of a hot kernel (ids in vfem_mg_time_kernel's comment
+ * in vfem_engine.cpp: 0 fine applyK FP64, 1 fine applyK FP32, 2 fine applyK double-float,
+ * 3/4 fine GS sweep FP32/FP64, 5 fine residual FP32, 6 level-1 GS sweep FP32,
+ * 7 level-1 residual FP32) with its algorithmic bytes, and a counter of the library's
+ * kernel launches (graph replays included). */
+int vfem_mg_get_stream(const vfem_mg *mg, void **stream);
+int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *bytes);
+int vfem_kernel_launch_count(uint64_t *count);
+
 /* ---------------- filters (TopologyOptimizationFilter.hh) ---------------- */
 /* SmoothingFilter::apply (= backprop) (TopologyOptimizationFilter.hh:285-400); type 0 Const, 1 Linear */
 int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out);

@@ -251,6 +251,21 @@ int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter,
     });
 }
 
+int vfem_mg_get_stream(const vfem_mg *mg, void **stream) {
+    return guarded([&] { need(mg, "mg"); *stream = (void *)mg->m.fine->stream; });
+}
+int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *bytes) {
+    return guarded([&] {
+        need(mg, "mg");
+        const double t = mg->m.timeKernel(kernel, reps);
+        if (ms) *ms = t;
+        if (bytes) *bytes = mg->m.kernelBytes(kernel);
+    });
+}
+int vfem_kernel_launch_count(uint64_t *count) {
+    return guarded([&] { *count = launchCounter(); });
+}
+
 int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out) {
     return guarded([&] {
         need(dims, "dims");

@@ -21,7 +21,14 @@ inline void cudaCheck(cudaError_t e, const char *what) {
     if (e != cudaSuccess) throw Error(ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 #define VFEM_CUDA(x) ::vfem::cudaCheck((x), #x)
-#define VFEM_LAUNCH_CHECK() ::vfem::cudaCheck(cudaGetLastError(), "kernel launch")
+// Every kernel launch goes through this check, which also counts it (graph replays are
+// counted from the captured node count).
+uint64_t &launchCounter();
+#define VFEM_LAUNCH_CHECK()                                              \
+    do {                                                                 \
+        ::vfem::cudaCheck(cudaGetLastError(), "kernel launch");          \
+        ++::vfem::launchCounter();                                       \
+    } while (0)
 
 constexpr int BUILD_DIR = 1;         // layers are stacked along y (TensorProductSimulator.hh:1851)
 constexpr int64_t LAYER_MASK_NONE = 2147483647;

@@ -9,6 +9,11 @@
 
 namespace vfem {
 
+uint64_t &launchCounter() {
+    static uint64_t counter = 0;
+    return counter;
+}
+
 // ---------------------------------------------------------------------------
 // caller-memory views
 // ---------------------------------------------------------------------------
@@ -343,6 +348,7 @@ MG::~MG() {
 void MG::clearGraphs() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+    graphKernels.clear();
     graphX = nullptr;
 }
 
@@ -728,11 +734,24 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
                 VFEM_CUDA(cudaStreamEndCapture(st, &graph));
                 cudaGraphExec_t exec;
                 VFEM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+                size_t nNodes = 0;
+                VFEM_CUDA(cudaGraphGetNodes(graph, nullptr, &nNodes));
+                std::vector<cudaGraphNode_t> nodes(nNodes);
+                VFEM_CUDA(cudaGraphGetNodes(graph, nodes.data(), &nNodes));
+                uint64_t kernels = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType ty;
+                    VFEM_CUDA(cudaGraphNodeGetType(nd, &ty));
+                    if (ty == cudaGraphNodeTypeKernel) ++kernels;
+                }
                 cudaGraphDestroy(graph);
                 it = graphs.emplace(key, exec).first;
+                graphKernels[key] = kernels;
+                launchCounter() -= kernels;  // the capture itself launched nothing
                 graphX = x;
             }
             VFEM_CUDA(cudaGraphLaunch(it->second, st));
+            launchCounter() += graphKernels[key];
         } else {
             cgIteration(x, mgIter, sweeps, fmg);
         }
@@ -1132,6 +1151,83 @@ void Problem::getU(double *out, bool /*device*/) {
 void Problem::getPhysical(double *out, bool /*device*/) {
     VFEM_CUDA(cudaMemcpyAsync(out, vars.back().p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
     VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+}
+
+
+// ---------------------------------------------------------------------------
+// Benchmark hook: time one hot kernel on the solver stream with CUDA events.
+//   0 fine applyK FP64      1 fine applyK FP32     2 fine applyK double-float
+//   3 fine GS sweep FP32    4 fine GS sweep FP64   5 fine residual FP32
+//   6 level-1 GS sweep FP32 7 level-1 residual FP32
+// ---------------------------------------------------------------------------
+double MG::kernelBytes(int which) const {
+    const double nn = (double)lv[0].g.NN, ne = (double)lv[0].g.NE;
+    switch (which) {
+    case 0: return 8.0 * (6 * nn + ne);
+    case 1: return 4.0 * (6 * nn + ne);
+    case 2: return 8.0 * (6 * nn + ne);
+    case 3: return 4.0 * (9 * nn + ne);
+    case 4: return 8.0 * (9 * nn + ne);
+    case 5: return 4.0 * (9 * nn + ne);
+    case 6: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 243 * n1); }
+    case 7: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 243 * n1); }
+    }
+    return 0;
+}
+
+double MG::timeKernel(int which, int reps) {
+    if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
+    if ((which == 6 || which == 7) && L() < 3) throw Error(ERR_ARG, "level-1 kernels need at least two coarsenings");
+    syncFineGeom(*this);
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
+    const int64_t n3 = 3 * g.NN;
+    auto &F = lv[0].d32;
+    auto &D = lv[0].d64;
+    const bool need32 = which == 1 || which == 3 || which == 5 || which == 6 || which == 7;
+    if (need32) {
+        if (which >= 6) {
+            if (precision != PREC_MIXED) throw Error(ERR_ARG, "level-1 FP32 kernels need mixed precision");
+            ensureStiffness();
+        }
+        for (int l = 0; l < (which >= 6 ? 2 : 1); ++l) {
+            auto &Q = lv[l].d32;
+            const int64_t m3 = 3 * lv[l].g.NN;
+            Q.x.alloc(m3); Q.b.alloc(m3); Q.r.alloc(m3);
+            launch_fill<float>(Q.x.p, 0.5f, m3, st);
+            launch_fill<float>(Q.b.p, 1.0f, m3, st);
+        }
+    } else {
+        D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
+        launch_fill<double>(D.x.p, 0.5, n3, st);
+        launch_fill<double>(D.b.p, 1.0, n3, st);
+    }
+    auto run = [&]() {
+        switch (which) {
+        case 0: launch_applyk_fine<double>(g, fine->Y.p, D.x.p, D.r.p, fine->K0, true, false, fine->dmask.p, false, nullptr, 0, st); break;
+        case 1: launch_applyk_fine<float>(g, fine->youngF(), F.x.p, F.r.p, fine->K0f, true, false, fine->dmask.p, false, nullptr, 0, st); break;
+        case 2: launch_applyk_fine_df(g, fine->Y.p, D.x.p, D.r.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st); break;
+        case 3: smoothT<float>(0, true); break;
+        case 4: smoothT<double>(0, true); break;
+        case 5: residualT<float>(0); break;
+        case 6: smoothT<float>(1, true); break;
+        case 7: residualT<float>(1); break;
+        default: throw Error(ERR_ARG, "unknown kernel id");
+        }
+    };
+    run();  // warm-up
+    cudaEvent_t e0, e1;
+    VFEM_CUDA(cudaEventCreate(&e0));
+    VFEM_CUDA(cudaEventCreate(&e1));
+    VFEM_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < reps; ++r) run();
+    VFEM_CUDA(cudaEventRecord(e1, st));
+    VFEM_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    VFEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
 }
 
 }  // namespace vfem

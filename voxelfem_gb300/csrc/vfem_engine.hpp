@@ -153,6 +153,11 @@ public:
     PcgStats pcgDevice(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
                        bool fmg, bool dirichletSatisfied, PcgCallback cb, void *user);
     double lastTrueRelres = -1;
+    // Average device time (ms) of one launch of a hot kernel, timed with CUDA events on the
+    // solver stream (benchmark hook).
+    double timeKernel(int which, int reps);
+    // Sum of algorithmic bytes for the kernels of timeKernel().
+    double kernelBytes(int which) const;
 
     // coarsest level
     int nfree = 0;
@@ -184,6 +189,7 @@ public:
         }
     };
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, uint64_t> graphKernels;  // kernel nodes per captured graph
     const double *graphX = nullptr;  // buffers baked into captured graphs
     void clearGraphs();
 
