@@ -156,6 +156,11 @@ int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter,
 int vfem_mg_get_stream(const vfem_mg *mg, void **stream);
 int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *bytes);
 int vfem_kernel_launch_count(uint64_t *count);
+/* Warm-cache phase breakdown of one PCG iteration (per level and per CG kernel) and of the
+ * hierarchy rebuild, averaged over reps: up to max_entries '\n'-separated names in names_out
+ * (capacity names_cap bytes) and times in ms_out; the count is returned in num_entries. */
+int vfem_mg_profile(vfem_mg *mg, int64_t mg_iterations, int64_t mg_smoothing_iterations, int reps, char *names_out,
+                    int64_t names_cap, double *ms_out, int max_entries, int *num_entries);
 
 /* ---------------- filters (TopologyOptimizationFilter.hh) ---------------- */
 /* SmoothingFilter::apply (= backprop) (TopologyOptimizationFilter.hh:285-400); type 0 Const, 1 Linear */

@@ -200,3 +200,39 @@ def test_topopt_oc(gpu, oracle):
         otop.ocStep()
         assert rel(top.getVars(), otop.designVars()) < 1e-6
     assert abs(top.evaluateConstraints()[0]) < 1e-6
+
+
+def _c2_golden():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cantilever_256x128x128_oracle.json")
+    with open(path) as f:
+        return json.load(f)
+
+
+def test_full_size_fp64_and_mixed_against_oracle_golden(gpu):
+    """256x128x128 (12.8M DOF): the FP64 GPU solve takes the oracle's iterations and agrees on compliance to
+    1e-8; the mixed solve reaches 1e-8 and agrees to 1e-8; size-independent properties of applyK hold."""
+    gold = _c2_golden()
+    ne = (256, 128, 128)
+    g = pv.TensorProductSimulator([1, 1, 1], [[0.0, 0.0, 0.0], [256.0, 128.0, 128.0]], ne)
+    wl.setup_cantilever(g, ne, 0.01, 0)
+    mg = g.multigridSolver(5)
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    x = mg.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    assert mg.lastStats.iterations == gold["iterations"]
+    c = 0.5 * np.sum(b * x)
+    assert abs(c - gold["compliance"]) / abs(gold["compliance"]) < 1e-8
+    mg.setPrecision("mixed")
+    xm = mg.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    assert mg.lastStats.relres <= 1e-8
+    cm = 0.5 * np.sum(b * xm)
+    assert abs(cm - gold["compliance"]) / abs(gold["compliance"]) < 1e-8
+    # applyK at full size: rigid translation in the null space, symmetry
+    t = np.zeros_like(b)
+    t[:, 0] = 1.0
+    assert np.abs(g.applyK(t)).max() < 1e-12
+    rng = np.random.default_rng(11)
+    u, v = rng.standard_normal(b.shape), rng.standard_normal(b.shape)
+    assert abs(np.sum(u * g.applyK(v)) - np.sum(v * g.applyK(u))) < 1e-12 * np.sum(np.abs(u * g.applyK(u)))

@@ -23,15 +23,20 @@ __device__ __forceinline__ void decode(const int64_t n, const int nn1, const int
     i = (int)(t / nn1);
 }
 
+// Branch-free row gather: neighbours outside the grid are clamped to a valid node; their
+// stencil blocks are exactly zero (no element contains both nodes), so they add nothing and
+// every load of the row can be in flight at once.
 template <typename T, bool Negate>
 __device__ __forceinline__ void stencil_row(const Geom &g, const T *__restrict__ S, const T *__restrict__ u, int64_t n,
                                             int i, int j, int k, T &f0, T &f1, T &f2) {
     const int64_t ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    const int64_t dx[3] = {i > 0 ? -sx : 0, 0, i + 1 < g.nn[0] ? sx : 0};
+    const int64_t dy[3] = {j > 0 ? -sy : 0, 0, j + 1 < g.nn[1] ? sy : 0};
+    const int64_t dz[3] = {k > 0 ? -1 : 0, 0, k + 1 < g.nn[2] ? 1 : 0};
 #pragma unroll
     for (int o = 0; o < 27; ++o) {
-        const int ni = i + o / 9 - 1, nj = j + (o / 3) % 3 - 1, nk = k + o % 3 - 1;
-        if (ni < 0 || nj < 0 || nk < 0 || ni >= g.nn[0] || nj >= g.nn[1] || nk >= g.nn[2]) continue;
-        const int64_t m = g.node(ni, nj, nk);
+        const int64_t m = n + dx[o / 9] + dy[(o / 3) % 3] + dz[o % 3];
         const T u0 = u[m], u1 = u[ld + m], u2 = u[2 * ld + m];
         const T *blk = S + (int64_t)(o * 9) * ld + n;
         const T v0 = blk[0] * u0 + blk[ld] * u1 + blk[2 * ld] * u2;
@@ -253,25 +258,60 @@ __global__ void cast_kernel(const Tsrc *__restrict__ s, Tdst *__restrict__ d, in
 }
 
 // Level-1 element matrices: Ke_c = sum_fi E_fi * Kc_fi (MultigridSolver.hh:724-738).
+// One block per coarse element, thread t writes entry t.
 template <typename T>
-__global__ void __launch_bounds__(BS) ke_level1_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
-                                                       const T *__restrict__ Kc, T *__restrict__ Ke1) {
-    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (t >= g1.NE * 576) return;
-    const int64_t e = t / 576;
-    const int idx = (int)(t % 576);
+__global__ void __launch_bounds__(576) ke_level1_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
+                                                        const T *__restrict__ Kc, T *__restrict__ Ke1) {
+    __shared__ T sE[8];
+    const int64_t e = blockIdx.x;
+    const int t = threadIdx.x;
     const int ek = (int)(e % g1.ne[2]);
     const int64_t q = e / g1.ne[2];
     const int ej = (int)(q % g1.ne[1]), ei = (int)(q / g1.ne[1]);
+    if (t < 8) sE[t] = Y0[g0.elem(2 * ei + ((t >> 2) & 1), 2 * ej + ((t >> 1) & 1), 2 * ek + (t & 1))];
+    __syncthreads();
     T acc = T(0);
     if (ej < g1.firstMaskedE) {
 #pragma unroll
-        for (int fi = 0; fi < 8; ++fi) {
-            const T E = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
-            acc += E * Kc[fi * 576 + idx];
-        }
+        for (int fi = 0; fi < 8; ++fi) acc += sE[fi] * Kc[fi * 576 + t];
     }
-    Ke1[t] = acc;
+    Ke1[e * 576 + t] = acc;
+}
+
+// Level-1 27-point stencil straight from the fine Young's moduli: block (n, n+o)(r, c) =
+// sum over coarse elements e holding both nodes of sum_fi E_f(e, fi) Kc_fi[3ln+r][3lm+c]
+// (the assembly of MultigridSolver.hh:724-738 without storing the element matrices).
+// Thread per (node n, entry q), q = blockIdx.y: the Kc index is warp-uniform.
+template <typename T>
+__global__ void __launch_bounds__(BS) stencil_level1_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
+                                                            const T *__restrict__ Kc, T *__restrict__ S) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    const int q = blockIdx.y;
+    if (n >= g1.NN) return;
+    int i, j, k;
+    decode(n, g1.nn[1], g1.nn[2], i, j, k);
+    const int o = q / 9, rc = q % 9, r = rc / 3, c = rc % 3;
+    const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+    T acc = T(0);
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int cc = 0; cc < 2; ++cc) {
+                const int ma = a + oo[0], mb = b + oo[1], mc = cc + oo[2];
+                if (ma < 0 || ma > 1 || mb < 0 || mb > 1 || mc < 0 || mc > 1) continue;
+                const int ei = i - a, ej = j - b, ek = k - cc;
+                if (ei < 0 || ej < 0 || ek < 0 || ei >= g1.ne[0] || ej >= g1.ne[1] || ek >= g1.ne[2]) continue;
+                if (ej >= g1.firstMaskedE) continue;
+                const int idx = (3 * (4 * a + 2 * b + cc) + r) * 24 + 3 * (4 * ma + 2 * mb + mc) + c;
+#pragma unroll
+                for (int fi = 0; fi < 8; ++fi) {
+                    const T E = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
+                    acc += E * Kc[fi * 576 + idx];
+                }
+            }
+    S[(int64_t)q * g1.ld + n] = acc;
 }
 
 // Ke_c = sum_fi Phi_fi^T Ke_child(fi) Phi_fi (MultigridSolver.hh:712-722, 745-819).
@@ -435,7 +475,15 @@ void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st) {
 
 template <typename T>
 void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *Ke1, cudaStream_t st) {
-    ke_level1_kernel<T><<<gridFor(g1.NE * 576, BS), BS, 0, st>>>(g1, g0, Y0, Kc, Ke1);
+    if (g1.NE > 2147483647LL) throw Error(ERR_ARG, "too many coarse elements");
+    ke_level1_kernel<T><<<(unsigned)g1.NE, 576, 0, st>>>(g1, g0, Y0, Kc, Ke1);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, cudaStream_t st) {
+    dim3 grid(gridFor(g1.NN, BS), 243);
+    stencil_level1_kernel<T><<<grid, BS, 0, st>>>(g1, g0, Y0, Kc, S);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -471,6 +519,7 @@ void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, cudaStream_t st) {
     template void launch_masked_zero<T>(const Geom &, T *, int, cudaStream_t);                                        \
     template void launch_fill<T>(T *, T, int64_t, cudaStream_t);                                                      \
     template void launch_ke_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);           \
+    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);      \
     template void launch_ke_coarsen<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);          \
     template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, cudaStream_t);                              \
     template void launch_ke_scaled<T>(const Geom &, const T *, const T *, T *, cudaStream_t);

@@ -45,14 +45,17 @@ __device__ __forceinline__ void elem_rows(const Geom &g, const Mat24<T> &K, cons
     }
 }
 
+// Element (i-A, j-B, k-Cc); an element outside the grid is clamped onto a valid one and
+// weighted by E = 0, which keeps the gather branch-free (0 * finite adds nothing).
 template <typename T, int A, int B, int Cc, bool Negate>
 __device__ __forceinline__ void visit_elem(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y,
                                            const T *__restrict__ u, int i, int j, int k, T &f0, T &f1, T &f2) {
     const int ei = i - A, ej = j - B, ek = k - Cc;
-    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
-    const T E = Y[g.elem(ei, ej, ek)];
+    const bool inb = ei >= 0 && ej >= 0 && ek >= 0 && ei < g.ne[0] && ej < g.ne[1] && ek < g.ne[2];
+    const int ci = min(max(ei, 0), g.ne[0] - 1), cj = min(max(ej, 0), g.ne[1] - 1), ck = min(max(ek, 0), g.ne[2] - 1);
+    const T E = inb ? Y[g.elem(ci, cj, ck)] : T(0);
     T c0, c1, c2;
-    elem_rows<T, 4 * A + 2 * B + Cc>(g, K, u, g.node(ei, ej, ek), c0, c1, c2);
+    elem_rows<T, 4 * A + 2 * B + Cc>(g, K, u, g.node(ci, cj, ck), c0, c1, c2);
     if (Negate) { f0 -= E * c0; f1 -= E * c1; f2 -= E * c2; }
     else        { f0 += E * c0; f1 += E * c1; f2 += E * c2; }
 }
@@ -170,11 +173,12 @@ template <typename T, int A, int B, int Cc>
 __device__ __forceinline__ void gs_visit(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y, const T *u, int i,
                                          int j, int k, T &s0, T &s1, T &s2, T *M) {
     const int ei = i - A, ej = j - B, ek = k - Cc;
-    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
+    const bool inb = ei >= 0 && ej >= 0 && ek >= 0 && ei < g.ne[0] && ej < g.ne[1] && ek < g.ne[2];
+    const int ci = min(max(ei, 0), g.ne[0] - 1), cj = min(max(ej, 0), g.ne[1] - 1), ck = min(max(ek, 0), g.ne[2] - 1);
     constexpr int LN = 4 * A + 2 * B + Cc;
-    const T E = Y[g.elem(ei, ej, ek)];
+    const T E = inb ? Y[g.elem(ci, cj, ck)] : T(0);
     T c0, c1, c2;
-    elem_rows<T, LN>(g, K, u, g.node(ei, ej, ek), c0, c1, c2);
+    elem_rows<T, LN>(g, K, u, g.node(ci, cj, ck), c0, c1, c2);
     s0 -= E * c0;
     s1 -= E * c1;
     s2 -= E * c2;
@@ -242,8 +246,8 @@ __device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float b
 }
 
 template <int LN>
-__device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const double *__restrict__ u, int64_t base,
-                                        float *ch, float *cl) {
+__device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const float *__restrict__ uh_,
+                                        const float *__restrict__ ul_, int64_t base, float *ch, float *cl) {
     const int64_t ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
 #pragma unroll
@@ -253,8 +257,7 @@ __device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const d
         const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            float uh, ul;
-            df_split(u[c * ld + nm], uh, ul);
+            const float uh = uh_[c * ld + nm], ul = ul_[c * ld + nm];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
                 df_fma_acc(K.hi[(3 * m + c) * 24 + 3 * LN + r], K.lo[(3 * m + c) * 24 + 3 * LN + r], uh, ul, ch[r],
@@ -264,14 +267,16 @@ __device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const d
 }
 
 template <int A, int B, int Cc>
-__device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const double *__restrict__ Y,
-                                         const double *__restrict__ u, int i, int j, int k, float *fh, float *fl) {
+__device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const float *__restrict__ Yh,
+                                         const float *__restrict__ Yl, const float *__restrict__ uh,
+                                         const float *__restrict__ ul, int i, int j, int k, float *fh, float *fl) {
     const int ei = i - A, ej = j - B, ek = k - Cc;
-    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) return;
-    float eh, el;
-    df_split(Y[g.elem(ei, ej, ek)], eh, el);
+    const bool inb = ei >= 0 && ej >= 0 && ek >= 0 && ei < g.ne[0] && ej < g.ne[1] && ek < g.ne[2];
+    const int ci = min(max(ei, 0), g.ne[0] - 1), cj = min(max(ej, 0), g.ne[1] - 1), ck = min(max(ek, 0), g.ne[2] - 1);
+    const int64_t e = g.elem(ci, cj, ck);
+    const float eh = inb ? Yh[e] : 0.f, el = inb ? Yl[e] : 0.f;
     float ch[3], cl[3];
-    df_elem<4 * A + 2 * B + Cc>(g, K, u, g.node(ei, ej, ek), ch, cl);
+    df_elem<4 * A + 2 * B + Cc>(g, K, uh, ul, g.node(ci, cj, ck), ch, cl);
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
         // normalise the element sum, then accumulate E * contrib
@@ -281,7 +286,12 @@ __device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const 
     }
 }
 
-__global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const double *__restrict__ Y,
+// out = K u with u given as its double-float split (uh + ul) and E as (Yh + Yl); out and the
+// optional partial dot products u.out are FP64. No FP64 arithmetic in the inner loops.
+__global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float *__restrict__ Yh,
+                                                            const float *__restrict__ Yl,
+                                                            const float *__restrict__ uh,
+                                                            const float *__restrict__ ul,
                                                             const double *__restrict__ u, double *__restrict__ out,
                                                             const uint8_t *__restrict__ dmask, int zeroDir,
                                                             double *__restrict__ partials, int withDot,
@@ -295,14 +305,14 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const double
         double f[3] = {0.0, 0.0, 0.0};
         if (j < g.nyv()) {
             float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
-            df_visit<0, 0, 0>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<0, 0, 1>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<0, 1, 0>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<0, 1, 1>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<1, 0, 0>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<1, 0, 1>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<1, 1, 0>(g, K, Y, u, i, j, k, fh, fl);
-            df_visit<1, 1, 1>(g, K, Y, u, i, j, k, fh, fl);
+            df_visit<0, 0, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 0, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 1, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 1, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 0, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 0, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 1, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 1, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
             const uint8_t dm = zeroDir ? dmask[n] : 0;
 #pragma unroll
             for (int r = 0; r < 3; ++r) f[r] = ((dm >> r) & 1) ? 0.0 : (double)fh[r] + (double)fl[r];
@@ -316,6 +326,16 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const double
         const double s = block_sum<BS>(dot);
         if (threadIdx.x == 0) partials[blockIdx.x] = s;
     }
+}
+
+__global__ void split_df_kernel(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo,
+                                int64_t n) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= n) return;
+    float h, l;
+    df_split(src[t], h, l);
+    hi[t] = h;
+    lo[t] = l;
 }
 
 // ---------------- element-wise kernels ----------------
@@ -489,13 +509,18 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
     VFEM_LAUNCH_CHECK();
 }
 
-void launch_applyk_fine_df(const Geom &g, const double *Y, const double *u, double *out, const Mat24DF &K0,
-                           const uint8_t *dmask, bool zeroDirichlet, double *partialDot, int partialBlocks,
-                           cudaStream_t st) {
+void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, const float *uh, const float *ul,
+                           const double *u, double *out, const Mat24DF &K0, const uint8_t *dmask, bool zeroDirichlet,
+                           double *partialDot, int partialBlocks, cudaStream_t st) {
     const unsigned grid = gridFor(g.NN, BS);
     if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
-    applyk_fine_df_kernel<<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zeroDirichlet ? 1 : 0, partialDot,
+    applyk_fine_df_kernel<<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0, partialDot,
                                                partialDot ? 1 : 0, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStream_t st) {
+    split_df_kernel<<<gridFor(n, BS), BS, 0, st>>>(src, hi, lo, n);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -43,31 +43,21 @@ __global__ void symmetrize_kernel(double *A, int n) {
     A[(int64_t)j * n + i] = v;
 }
 
-// ---------------- blocked left-looking Cholesky (lower, in place, row-major) ----------------
-// acc(tile rows R, tile rows C) = A[R][C] - sum_{t < kb} L[R][t] L[C][t]
-__device__ void tile_update(const double *A, int n, int r0, int c0, int kb, double (*sa)[TB + 1],
-                            double (*sb)[TB + 1], double &acc) {
+// ---------------- blocked right-looking Cholesky (lower, in place, row-major) ----------------
+// Step k: factor the diagonal tile, solve the tiles below it, then update every trailing
+// lower tile with one 32x32x32 product per block, so each step spreads over all SMs.
+__device__ __forceinline__ void load_tile(const double *A, int n, int r0, int c0, double (*t)[TB + 1]) {
     const int ty = threadIdx.y, tx = threadIdx.x;
-    const int gr = r0 + ty, gc = c0 + tx;
-    acc = (gr < n && gc < n) ? A[(int64_t)gr * n + gc] : 0.0;
-    for (int t0 = 0; t0 < kb; t0 += TB) {
-        const int tc = t0 + tx;
-        sa[ty][tx] = (r0 + ty < n && tc < kb) ? A[(int64_t)(r0 + ty) * n + tc] : 0.0;
-        sb[ty][tx] = (c0 + ty < n && tc < kb) ? A[(int64_t)(c0 + ty) * n + tc] : 0.0;
-        __syncthreads();
-#pragma unroll 8
-        for (int q = 0; q < TB; ++q) acc -= sa[ty][q] * sb[tx][q];
-        __syncthreads();
-    }
+    t[ty][tx] = (r0 + ty < n && c0 + tx < n) ? A[(int64_t)(r0 + ty) * n + c0 + tx] : 0.0;
 }
 
-__global__ void chol_diag_kernel(double *A, int n, int kb, int *status) {
-    __shared__ double sa[TB][TB + 1], sb[TB][TB + 1], sl[TB][TB + 1];
-    double acc;
-    tile_update(A, n, kb, kb, kb, sa, sb, acc);
+__global__ void chol_diag_kernel(double *A, int n, int k, int *status) {
+    __shared__ double sl[TB][TB + 1];
     const int ty = threadIdx.y, tx = threadIdx.x;
+    const int kb = k * TB;
     const int nb = min(TB, n - kb);
-    sl[ty][tx] = (ty < nb && tx < nb) ? acc : (ty == tx ? 1.0 : 0.0);
+    load_tile(A, n, kb, kb, sl);
+    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
         if (ty == 0 && tx == 0) {
@@ -84,17 +74,16 @@ __global__ void chol_diag_kernel(double *A, int n, int kb, int *status) {
     if (ty < nb && tx < nb) A[(int64_t)(kb + ty) * n + kb + tx] = (tx <= ty) ? sl[ty][tx] : 0.0;
 }
 
-__global__ void chol_panel_kernel(double *A, int n, int kb) {
-    __shared__ double sa[TB][TB + 1], sb[TB][TB + 1], sl[TB][TB + 1], sx[TB][TB + 1];
-    const int r0 = kb + TB * (1 + blockIdx.x);
-    double acc;
-    tile_update(A, n, r0, kb, kb, sa, sb, acc);
+// tiles (i, k), i > k: X L_kk^T = A_ik
+__global__ void chol_trsm_kernel(double *A, int n, int k) {
+    __shared__ double sl[TB][TB + 1], sx[TB][TB + 1];
     const int ty = threadIdx.y, tx = threadIdx.x;
+    const int kb = k * TB, r0 = kb + TB * (1 + blockIdx.x);
     const int nb = min(TB, n - kb);
-    sl[ty][tx] = (ty < nb && tx < nb) ? A[(int64_t)(kb + ty) * n + kb + tx] : (ty == tx ? 1.0 : 0.0);
-    sx[ty][tx] = acc;
+    load_tile(A, n, kb, kb, sl);
+    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    load_tile(A, n, r0, kb, sx);
     __syncthreads();
-    // X L^T = acc: x_j = (acc_j - sum_{t<j} x_t L[j][t]) / L[j][j]
     for (int j = 0; j < nb; ++j) {
         if (tx == j) {
             double v = sx[ty][j];
@@ -106,37 +95,72 @@ __global__ void chol_panel_kernel(double *A, int n, int kb) {
     if (r0 + ty < n && tx < nb) A[(int64_t)(r0 + ty) * n + kb + tx] = sx[ty][tx];
 }
 
-// Z = L^{-1}: block row bi, block column bj <= bi:
-// Z[bi][bj] = L[bi][bi]^{-1} (delta - sum_{bj <= bk < bi} L[bi][bk] Z[bk][bj])
-__global__ void trinv_row_kernel(const double *L, double *Z, int n, int bi) {
-    __shared__ double sa[TB][TB + 1], sb[TB][TB + 1], sl[TB][TB + 1], sx[TB][TB + 1];
-    const int bj = blockIdx.x;
+__device__ __forceinline__ void lower_tile_of(int idx, int &ii, int &jj) {
+    ii = 0;
+    while (idx > ii) { idx -= ii + 1; ++ii; }
+    jj = idx;
+}
+
+// trailing tiles (i, j), k < j <= i: A_ij -= L_ik L_jk^T
+__global__ void chol_syrk_kernel(double *A, int n, int k) {
+    __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
+    int ii, jj;
+    lower_tile_of(blockIdx.x, ii, jj);
+    const int i = k + 1 + ii, j = k + 1 + jj;
     const int ty = threadIdx.y, tx = threadIdx.x;
-    const int r0 = bi * TB, c0 = bj * TB;
-    double acc = (r0 + ty == c0 + tx && r0 + ty < n) ? 1.0 : 0.0;
-    for (int bk = bj; bk < bi; ++bk) {
-        const int k0 = bk * TB;
-        sa[ty][tx] = (r0 + ty < n && k0 + tx < n) ? L[(int64_t)(r0 + ty) * n + k0 + tx] : 0.0;
-        sb[ty][tx] = (k0 + ty < n && c0 + tx < n) ? Z[(int64_t)(k0 + ty) * n + c0 + tx] : 0.0;
-        __syncthreads();
-#pragma unroll 8
-        for (int q = 0; q < TB; ++q) acc -= sa[ty][q] * sb[q][tx];
-        __syncthreads();
-    }
-    const int nb = min(TB, n - r0);
-    sl[ty][tx] = (ty < nb && tx < nb) ? L[(int64_t)(r0 + ty) * n + r0 + tx] : (ty == tx ? 1.0 : 0.0);
-    sx[ty][tx] = acc;
+    const int kb = k * TB;
+    load_tile(A, n, i * TB, kb, sa);
+    load_tile(A, n, j * TB, kb, sb);
     __syncthreads();
-    // forward substitution down the rows of the tile: x_i = (acc_i - sum_{t<i} L[i][t] x_t) / L[i][i]
-    for (int i = 0; i < TB; ++i) {
-        if (ty == i) {
-            double v = sx[i][tx];
-            for (int t = 0; t < i; ++t) v -= sl[i][t] * sx[t][tx];
-            sx[i][tx] = v / sl[i][i];
+    double acc = 0.0;
+#pragma unroll 8
+    for (int q = 0; q < TB; ++q) acc += sa[ty][q] * sb[tx][q];
+    const int gr = i * TB + ty, gc = j * TB + tx;
+    if (gr < n && gc < n) A[(int64_t)gr * n + gc] -= acc;
+}
+
+// Z = L^{-1}, right-looking over block columns of L. Step k: Z[k][c] = L_kk^{-1} Z[k][c] (c <= k),
+// then Z[i][c] -= L[i][k] Z[k][c] for i > k.
+__global__ void trinv_diag_kernel(const double *L, double *Z, int n, int k) {
+    __shared__ double sl[TB][TB + 1], sx[TB][TB + 1];
+    const int c = blockIdx.x;
+    const int ty = threadIdx.y, tx = threadIdx.x;
+    const int r0 = k * TB, c0 = c * TB;
+    const int nb = min(TB, n - r0);
+    load_tile(L, n, r0, r0, sl);
+    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    load_tile(Z, n, r0, c0, sx);
+    __syncthreads();
+    for (int r = 0; r < TB; ++r) {
+        if (ty == r) {
+            double v = sx[r][tx];
+            for (int t = 0; t < r; ++t) v -= sl[r][t] * sx[t][tx];
+            sx[r][tx] = v / sl[r][r];
         }
         __syncthreads();
     }
     if (r0 + ty < n && c0 + tx < n) Z[(int64_t)(r0 + ty) * n + c0 + tx] = sx[ty][tx];
+}
+
+__global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
+    __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
+    const int c = blockIdx.x % (k + 1);
+    const int i = k + 1 + blockIdx.x / (k + 1);
+    const int ty = threadIdx.y, tx = threadIdx.x;
+    load_tile(L, n, i * TB, k * TB, sa);
+    load_tile(Z, n, k * TB, c * TB, sb);
+    __syncthreads();
+    double acc = 0.0;
+#pragma unroll 8
+    for (int q = 0; q < TB; ++q) acc += sa[ty][q] * sb[q][tx];
+    const int gr = i * TB + ty, gc = c * TB + tx;
+    if (gr < n && gc < n) Z[(int64_t)gr * n + gc] -= acc;
+}
+
+__global__ void identity_kernel(double *Z, int n) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= (int64_t)n * n) return;
+    Z[t] = (t / n == t % n) ? 1.0 : 0.0;
 }
 
 // Ainv = Z^T Z (lower tiles computed, mirrored). Z is lower triangular.
@@ -281,11 +305,18 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
 }
 
 __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double *__restrict__ d,
-                                    const double *__restrict__ sc) {
+                                    const double *__restrict__ sc, float *__restrict__ dh, float *__restrict__ dl) {
     const double beta = sc[2];
     const int64_t N3 = 3 * g.ld;
-    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS)
-        d[t] = beta * d[t] + s[t];
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS) {
+        const double v = beta * d[t] + s[t];
+        d[t] = v;
+        if (dh) {
+            const float h = __double2float_rn(v);
+            dh[t] = h;
+            dl[t] = __double2float_rn(v - (double)h);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restrict__ x, double *__restrict__ r,
@@ -344,21 +375,29 @@ void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t
     if (n <= 0) return;
     const dim3 tb(TB, TB);
     const int nbt = (n + TB - 1) / TB;
-    for (int bj = 0; bj < nbt; ++bj) {
-        const int kb = bj * TB;
-        chol_diag_kernel<<<1, tb, 0, st>>>(A, n, kb, status);
+    for (int k = 0; k < nbt; ++k) {
+        chol_diag_kernel<<<1, tb, 0, st>>>(A, n, k, status);
         VFEM_LAUNCH_CHECK();
-        if (bj + 1 < nbt) {
-            chol_panel_kernel<<<nbt - bj - 1, tb, 0, st>>>(A, n, kb);
+        const int m = nbt - k - 1;
+        if (m > 0) {
+            chol_trsm_kernel<<<m, tb, 0, st>>>(A, n, k);
+            VFEM_LAUNCH_CHECK();
+            chol_syrk_kernel<<<m * (m + 1) / 2, tb, 0, st>>>(A, n, k);
             VFEM_LAUNCH_CHECK();
         }
     }
     zero_upper_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(A, n);
     VFEM_LAUNCH_CHECK();
-    VFEM_CUDA(cudaMemsetAsync(work, 0, sizeof(double) * (size_t)n * n, st));
-    for (int bi = 0; bi < nbt; ++bi) {
-        trinv_row_kernel<<<bi + 1, tb, 0, st>>>(A, work, n, bi);
+    identity_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(work, n);
+    VFEM_LAUNCH_CHECK();
+    for (int k = 0; k < nbt; ++k) {
+        trinv_diag_kernel<<<k + 1, tb, 0, st>>>(A, work, n, k);
         VFEM_LAUNCH_CHECK();
+        const int m = nbt - k - 1;
+        if (m > 0) {
+            trinv_update_kernel<<<m * (k + 1), tb, 0, st>>>(A, work, n, k);
+            VFEM_LAUNCH_CHECK();
+        }
     }
     ztz_kernel<<<nbt * (nbt + 1) / 2, tb, 0, st>>>(work, A, n, nbt);
     VFEM_LAUNCH_CHECK();
@@ -405,8 +444,9 @@ void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double
     VFEM_LAUNCH_CHECK();
 }
 
-void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, cudaStream_t st) {
-    cg_direction_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, s, d, sc);
+void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
+                         cudaStream_t st) {
+    cg_direction_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, s, d, sc, dh, dl);
     VFEM_LAUNCH_CHECK();
 }
 

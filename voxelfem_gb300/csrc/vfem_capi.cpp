@@ -262,6 +262,23 @@ int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *b
         if (bytes) *bytes = mg->m.kernelBytes(kernel);
     });
 }
+int vfem_mg_profile(vfem_mg *mg, int64_t mg_iterations, int64_t mg_smoothing_iterations, int reps, char *names_out,
+                    int64_t names_cap, double *ms_out, int max_entries, int *num_entries) {
+    return guarded([&] {
+        need(mg, "mg"); need(names_out, "names"); need(ms_out, "ms"); need(num_entries, "count");
+        auto prof = mg->m.profile(mg_iterations, mg_smoothing_iterations, reps);
+        std::string names;
+        int n = 0;
+        for (const auto &kv : prof) {
+            if (n >= max_entries) break;
+            names += kv.first + "\n";
+            ms_out[n++] = kv.second;
+        }
+        if ((int64_t)names.size() + 1 > names_cap) throw Error(ERR_ARG, "name buffer too small");
+        std::memcpy(names_out, names.c_str(), names.size() + 1);
+        *num_entries = n;
+    });
+}
 int vfem_kernel_launch_count(uint64_t *count) {
     return guarded([&] { *count = launchCounter(); });
 }

@@ -122,7 +122,19 @@ void Grid::updateYoungModuli() {
     const bool masking = maskH < bmax[BUILD_DIR];
     launch_young_moduli<double>(g, rho.p, Y.p, E0, Emin, gamma, q, law, masking, stream);
     YfValid = false;
+    YdfValid = false;
     ++densVersion;
+}
+
+void Grid::youngDF(const float **hi, const float **lo) {
+    if (!YdfValid) {
+        Yhi.alloc(g.NE);
+        Ylo.alloc(g.NE);
+        launch_split_df(Y.p, Yhi.p, Ylo.p, g.NE, stream);
+        YdfValid = true;
+    }
+    *hi = Yhi.p;
+    *lo = Ylo.p;
 }
 
 const float *Grid::youngF() {
@@ -332,6 +344,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     s.alloc(3 * NN);
     dvec.alloc(3 * NN);
     Ad.alloc(3 * NN);
+    dhi.alloc(3 * NN);
+    dlo.alloc(3 * NN);
     partialCount = std::max<int>(REDUCE_BLOCKS, (int)gridFor(NN, 256));
     partials.alloc(partialCount);
     sc.alloc(16);
@@ -513,11 +527,20 @@ void MG::updateStiffnessT() {
     } else {
         for (int l = 1; l < L(); ++l) {
             auto &D = lv[l].data<T>();
-            D.Ke.alloc((size_t)lv[l].g.NE * 576);
             D.S.alloc((size_t)243 * lv[l].g.NN);
-            if (l == 1) launch_ke_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Ke.p, st);
-            else launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p, st);
-            launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, st);
+            if (l == 1) {
+                // the level-1 stencil comes straight from the fine moduli; its element matrices
+                // are only needed as the input of the next coarsening
+                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, st);
+                if (L() > 2) {
+                    D.Ke.alloc((size_t)lv[l].g.NE * 576);
+                    launch_ke_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Ke.p, st);
+                }
+            } else {
+                D.Ke.alloc((size_t)lv[l].g.NE * 576);
+                launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p, st);
+                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, st);
+            }
         }
     }
     // dense reduced coarsest operator, FP64 inverse
@@ -645,11 +668,15 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
         launch_cg_precond_out<double>(g, rbuf.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
     }
     launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
-    launch_cg_direction(g, s.p, dvec.p, sc.p, st);
+    const bool df = precision == PREC_MIXED && outerMatvec == MATVEC_DF;
+    launch_cg_direction(g, s.p, dvec.p, sc.p, df ? dhi.p : nullptr, df ? dlo.p : nullptr, st);
     const int nb = (int)gridFor(g.NN, 256);
-    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF)
-        launch_applyk_fine_df(g, fine->Y.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true, partials.p, partialCount, st);
-    else
+    if (df) {
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true, partials.p,
+                              partialCount, st);
+    } else
         launch_applyk_fine<double>(g, fine->Y.p, dvec.p, Ad.p, fine->K0, true, false, fine->dmask.p, true, partials.p,
                                    partialCount, st);
     launch_cg_alpha(partials.p, nb, sc.p, st);
@@ -710,6 +737,13 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
     launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
     VFEM_CUDA(cudaStreamSynchronize(st));
 
+    // everything the iteration reads must exist before a graph is captured (no allocation while capturing)
+    if (precision == PREC_MIXED) {
+        fine->youngF();
+        const float *yh, *yl;
+        if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
+        allocLevels();
+    }
     const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec, fine->maskVersion,
                        nfree};
     bool updated = false;
@@ -1201,12 +1235,18 @@ double MG::timeKernel(int which, int reps) {
         D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
         launch_fill<double>(D.x.p, 0.5, n3, st);
         launch_fill<double>(D.b.p, 1.0, n3, st);
+        if (which == 2) launch_split_df(D.x.p, dhi.p, dlo.p, n3, st);
     }
     auto run = [&]() {
         switch (which) {
         case 0: launch_applyk_fine<double>(g, fine->Y.p, D.x.p, D.r.p, fine->K0, true, false, fine->dmask.p, false, nullptr, 0, st); break;
         case 1: launch_applyk_fine<float>(g, fine->youngF(), F.x.p, F.r.p, fine->K0f, true, false, fine->dmask.p, false, nullptr, 0, st); break;
-        case 2: launch_applyk_fine_df(g, fine->Y.p, D.x.p, D.r.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st); break;
+        case 2: {
+            const float *yh, *yl;
+            fine->youngDF(&yh, &yl);
+            launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, D.x.p, D.r.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st);
+            break;
+        }
         case 3: smoothT<float>(0, true); break;
         case 4: smoothT<double>(0, true); break;
         case 5: residualT<float>(0); break;
@@ -1228,6 +1268,121 @@ double MG::timeKernel(int which, int reps) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return ms / reps;
+}
+
+
+// ---------------------------------------------------------------------------
+// Phase breakdown (benchmark hook)
+// ---------------------------------------------------------------------------
+std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t sweeps, int reps) {
+    if (L() < 2) throw Error(ERR_ARG, "profile needs at least one coarsening level");
+    syncFineGeom(*this);
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
+    std::vector<std::pair<std::string, double>> out;
+    std::map<std::string, double> acc;
+    std::vector<std::string> order;
+    cudaEvent_t ev[2];
+    VFEM_CUDA(cudaEventCreate(&ev[0]));
+    VFEM_CUDA(cudaEventCreate(&ev[1]));
+    auto timed = [&](const std::string &name, auto &&fn) {
+        VFEM_CUDA(cudaEventRecord(ev[0], st));
+        fn();
+        VFEM_CUDA(cudaEventRecord(ev[1], st));
+        VFEM_CUDA(cudaEventSynchronize(ev[1]));
+        float ms = 0;
+        VFEM_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        if (!acc.count(name)) order.push_back(name);
+        acc[name] += ms;
+    };
+    // hierarchy rebuild
+    for (int r = 0; r < reps; ++r) {
+        timed("galerkin+coarse_inverse", [&] { updateStiffness(); });
+    }
+    if (precision == PREC_MIXED) {
+        fine->youngF();
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+    }
+    allocLevels();
+    launch_fill<double>(rbuf.p, 1e-3, 3 * g.NN, st);
+    launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
+    xbuf.alloc(3 * g.NN);
+    launch_fill<double>(xbuf.p, 0.0, 3 * g.NN, st);
+    auto body = [&](auto tag) {
+        using T = decltype(tag);
+        auto &D0 = lv[0].data<T>();
+        const int64_t n3 = 3 * g.NN;
+        timed("precond:init", [&] {
+            launch_fill<T>(D0.x.p, T(0), n3, st);
+            if (std::is_same<T, double>::value) launch_copy((double *)D0.b.p, rbuf.p, n3, st);
+            else launch_cast<float, double>(rbuf.p, (float *)D0.b.p, n3, st);
+        });
+        for (int l = 0; l < L() - 1; ++l) {
+            auto &D = lv[l].data<T>();
+            auto &Dc = lv[l + 1].data<T>();
+            const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+            const std::string tagl = "L" + std::to_string(l) + ":";
+            timed(tagl + "presmooth", [&] {
+                launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
+                for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, true);
+            });
+            timed(tagl + "residual", [&] { residualT<T>(l); });
+            timed(tagl + "restrict", [&] {
+                launch_restrict<T>(lv[l].g, lv[l + 1].g, D.r.p, Dc.b.p, st);
+                launch_masked_zero<T>(lv[l + 1].g, Dc.x.p, MARGIN, st);
+            });
+        }
+        {
+            auto &Dc = lv.back().data<T>();
+            timed("coarsest:solve", [&] {
+                launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+            });
+        }
+        for (int l = L() - 2; l >= 0; --l) {
+            auto &D = lv[l].data<T>();
+            auto &Dc = lv[l + 1].data<T>();
+            const std::string tagl = "L" + std::to_string(l) + ":";
+            timed(tagl + "interp", [&] { launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dc.x.p, D.x.p, true, st); });
+            timed(tagl + "postsmooth", [&] {
+                for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, !symmetricGS);
+            });
+        }
+        timed("cg:precond_out+beta", [&] {
+            launch_cg_precond_out<T>(g, D0.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+            launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
+        });
+    };
+    VFEM_CUDA(cudaMemsetAsync(sc.p, 0, 16 * sizeof(double), st));
+    for (int r = 0; r < reps; ++r) {
+        if (precision == PREC_FP64) body(double());
+        else body(float());
+        const bool df = precision == PREC_MIXED && outerMatvec == MATVEC_DF;
+        timed("cg:direction", [&] {
+            launch_cg_direction(g, s.p, dvec.p, sc.p, df ? dhi.p : nullptr, df ? dlo.p : nullptr, st);
+        });
+        timed("cg:matvec+alpha", [&] {
+            const int nb = (int)gridFor(g.NN, 256);
+            if (df) {
+                const float *yh, *yl;
+                fine->youngDF(&yh, &yl);
+                launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true,
+                                      partials.p, partialCount, st);
+            } else {
+                launch_applyk_fine<double>(g, fine->Y.p, dvec.p, Ad.p, fine->K0, true, false, fine->dmask.p, true,
+                                           partials.p, partialCount, st);
+            }
+            launch_cg_alpha(partials.p, nb, sc.p, st);
+        });
+        timed("cg:update+rsq", [&] {
+            launch_cg_update(g, xbuf.p, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
+            launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
+        });
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    for (const auto &name : order) out.emplace_back(name, acc[name] / reps);
+    return out;
 }
 
 }  // namespace vfem

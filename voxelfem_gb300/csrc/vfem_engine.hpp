@@ -6,6 +6,8 @@
 #include <cmath>
 #include <limits>
 #include <map>
+#include <string>
+#include <utility>
 #include <memory>
 #include <tuple>
 #include <vector>
@@ -52,8 +54,8 @@ public:
     double grav[3] = {0, 0, 0};
 
     DevBuf<double> rho, Y;
-    DevBuf<float> Yf;
-    bool YfValid = false;
+    DevBuf<float> Yf, Yhi, Ylo;
+    bool YfValid = false, YdfValid = false;
     std::vector<uint8_t> dmask_h;
     std::vector<double> dval_h;   // SoA, stride NN
     std::vector<double> force_h;  // dense nodal forces, SoA
@@ -71,6 +73,7 @@ public:
     void getYoungModuli(double *out);
     void updateYoungModuli();
     const float *youngF();
+    void youngDF(const float **hi, const float **lo);  // double-float split of Y
     void addDirichlet(const double u[3], const double mn[3], const double mx[3], unsigned cmask);
     void applySymmetry(const int axes[3], const int maxFace[3]);
     void setForces(const double *f);
@@ -158,6 +161,9 @@ public:
     double timeKernel(int which, int reps);
     // Sum of algorithmic bytes for the kernels of timeKernel().
     double kernelBytes(int which) const;
+    // Warm-cache breakdown of one PCG iteration and of the hierarchy rebuild: (phase, ms) pairs,
+    // averaged over reps, each phase bracketed by CUDA events on the solver stream.
+    std::vector<std::pair<std::string, double>> profile(int64_t mgIter, int64_t sweeps, int reps);
 
     // coarsest level
     int nfree = 0;
@@ -170,6 +176,7 @@ public:
 
     // CG workspace
     DevBuf<double> rbuf, s, dvec, Ad, partials, sc, xbuf;
+    DevBuf<float> dhi, dlo;  // double-float split of the search direction
     double *hostSc = nullptr;  // pinned mirror of sc
     int partialCount = 0;
 

@@ -39,10 +39,13 @@ void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *
 template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                           const Mat24<T> &K0, cudaStream_t st);
-// FP64-accurate matvec in double-float arithmetic: out = K u (FP64 in/out), Y in FP64.
-void launch_applyk_fine_df(const Geom &g, const double *Y, const double *u, double *out, const Mat24DF &K0,
-                           const uint8_t *dmask, bool zeroDirichlet, double *partialDot, int partialBlocks,
-                           cudaStream_t st);
+// FP64-accurate matvec in double-float arithmetic: out = K u with u = uh + ul and Y = Yh + Yl
+// given as float pairs; out (and the partial dots u.out) in FP64.
+void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, const float *uh, const float *ul,
+                           const double *u, double *out, const Mat24DF &K0, const uint8_t *dmask, bool zeroDirichlet,
+                           double *partialDot, int partialBlocks, cudaStream_t st);
+// hi = fl(v), lo = fl(v - hi)
+void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStream_t st);
 
 void launch_compliance_gradient(const Geom &g, const double *rho, const double *u, double *grad, const Mat24<double> &K0,
                                 double E0, double Emin, double gamma, double q, int law, const double *grav,
@@ -74,6 +77,9 @@ void launch_fill(T *p, T v, int64_t n, cudaStream_t st);
 // Galerkin coarsening. Element matrices are stored element-major: Ke[e * 576 + 24*row + col].
 template <typename T>
 void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc /*8*576*/, T *Ke1, cudaStream_t st);
+// Level-1 stencil assembled directly from the fine Young's moduli (no element matrices).
+template <typename T>
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, cudaStream_t st);
 template <typename T>
 void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis /*8*64*/, T *Kec, cudaStream_t st);
 template <typename T>
@@ -107,7 +113,9 @@ void launch_cg_rsq(const double *partials, int n, double *sc, double *hostMirror
 template <typename Ts>
 void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                            double *partials, cudaStream_t st);
-void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, cudaStream_t st);
+// d = beta d + s; when dh is given also writes the double-float split of d into (dh, dl).
+void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
+                         cudaStream_t st);
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
                       double *partials, cudaStream_t st);
 void launch_copy(double *dst, const double *src, int64_t n, cudaStream_t st);
