@@ -165,6 +165,18 @@ int vfem_mg_profile(vfem_mg *mg, int64_t mg_iterations, int64_t mg_smoothing_ite
 /* ---------------- filters (TopologyOptimizationFilter.hh) ---------------- */
 /* SmoothingFilter::apply (= backprop) (TopologyOptimizationFilter.hh:285-400); type 0 Const, 1 Linear */
 int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out);
+/* Allocation-free variant of vfem_smoothing_filter; it has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (code capturing the filter into its own CUDA graph,
+ * code under a fixed device-memory budget, loops that cannot afford the device synchronisation
+ * of cudaMalloc/cudaFree). It allocates nothing: the tap table lives in a fixed device array
+ * inside libvfem.so, held by every GPU that loads the library until exit, which bounds the
+ * radius to 6 (larger radii are rejected with VFEM_ERR_ARG). in_dev and out_dev must be device
+ * pointers; the work is enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the
+ * call returns without waiting. The first call on a device looks up the array's device address
+ * and should come before any stream capture. Calls share the array: calls that overlap on the
+ * GPU (e.g. on two streams) race on it. */
+int vfem_smoothing_filter_noalloc(const int64_t dims[3], int radius, int type, const double *in_dev, double *out_dev,
+                                  void *stream);
 /* ProjectionFilter::apply / backprop (TopologyOptimizationFilter.hh:199-225) */
 int vfem_projection_apply(int64_t n, double beta, const double *in, double *out);
 int vfem_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out);

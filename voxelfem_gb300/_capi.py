@@ -81,6 +81,7 @@ _SIGS = {
     "vfem_kernel_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
     "vfem_mg_profile": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int, C.c_char_p, C.c_int64, _d, C.c_int, _i32]),
     "vfem_smoothing_filter": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp]),
+    "vfem_smoothing_filter_noalloc": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp, _vp]),
     "vfem_projection_apply": (C.c_int, [C.c_int64, C.c_double, _vp, _vp]),
     "vfem_projection_backprop": (C.c_int, [C.c_int64, C.c_double, _vp, _vp, _vp]),
     "vfem_problem_create": (C.c_int, [_vp, C.c_int, _i32, _i32, _i32, _d, C.c_double, C.POINTER(_vp)]),

@@ -2,6 +2,7 @@
 // filter (TopologyOptimizationFilter.hh:285-400), the tanh Heaviside projection and
 // its derivative (:189-245) and the optimality-criteria update
 // (OptimalityCriterion.hh:64-83).
+#include <mutex>
 #include <vector>
 
 #include "vfem_kernels.hpp"
@@ -76,6 +77,72 @@ __global__ void __launch_bounds__(BS) sum_kernel(const double *__restrict__ x, i
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the density filter.
+//
+// For callers that cannot call cudaMalloc: code that captures the filter into its own CUDA
+// graph (allocation is illegal during stream capture), code running under a fixed device
+// memory budget or a caching allocator that must not be bypassed, and loops that cannot
+// afford the implicit device synchronisation of cudaMalloc/cudaFree (e.g. the tens of filter
+// applications of every OC bisection). The tap table lives in the file-scope array below,
+// which every GPU that loads this library holds until the process exits. Its size bounds the
+// filter radius to NOALLOC_MAX_RADIUS. Every call rewrites the table on the caller's stream,
+// so calls that overlap on the GPU (different streams) race on it.
+// ---------------------------------------------------------------------------
+constexpr int NOALLOC_MAX_RADIUS = 6;
+constexpr int NOALLOC_MAX_TAPS = (2 * NOALLOC_MAX_RADIUS + 1) * (2 * NOALLOC_MAX_RADIUS + 1) *
+                                 (2 * NOALLOC_MAX_RADIUS + 1);
+// [0] = total weight, then 4 doubles per candidate offset: dx, dy, dz, weight (0 if discarded)
+constexpr int NOALLOC_SCRATCH_DOUBLES = 1 + 4 * NOALLOC_MAX_TAPS;
+static __device__ __align__(256) double g_filter_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+// One thread writes the candidate offsets of [-r, r]^3 in the reference's lexicographic order
+// with weight max(w, 0) and sums the positive weights in that same order.
+__global__ void noalloc_taps_kernel(int radius, int type, double *scratch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double rp1 = 1.0 + radius;
+    double W = 0.0;
+    int q = 0;
+    for (int a = -radius; a <= radius; ++a)
+        for (int b = -radius; b <= radius; ++b)
+            for (int c = -radius; c <= radius; ++c, ++q) {
+                double w = type == 1 ? rp1 - sqrt((double)(a * a + b * b + c * c)) : 1.0;
+                if (!(w > 0)) w = 0.0;
+                else W += w;
+                double *t = scratch + 1 + 4 * q;
+                t[0] = a;
+                t[1] = b;
+                t[2] = c;
+                t[3] = w;
+            }
+    scratch[0] = W;
+}
+
+// Zero-weight candidates add exactly 0 to the accumulator, so the sum equals the one over the
+// positive taps only (the allocating entry point's compacted table).
+__global__ void __launch_bounds__(BS) smoothing_filter_noalloc_kernel(int d0, int d1, int d2,
+                                                                      const double *__restrict__ in,
+                                                                      double *__restrict__ out,
+                                                                      const double *__restrict__ scratch,
+                                                                      int ncand) {
+    const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (e >= (int64_t)d0 * d1 * d2) return;
+    const int k = (int)(e % d2);
+    const int64_t t = e / d2;
+    const int j = (int)(t % d1), i = (int)(t / d1);
+    double acc = 0.0;
+    for (int q = 0; q < ncand; ++q) {
+        const double *tp = scratch + 1 + 4 * q;
+        const double w = tp[3];
+        if (w == 0.0) continue;
+        const int ni = reflect_index(i + (int)tp[0], d0);
+        const int nj = reflect_index(j + (int)tp[1], d1);
+        const int nk = reflect_index(k + (int)tp[2], d2);
+        acc += w * in[((int64_t)ni * d1 + nj) * d2 + nk];
+    }
+    out[e] = acc / scratch[0];
+}
+
 struct TapCache {
     int radius = -1, type = -1;
     DevBuf<int> offs;
@@ -141,6 +208,41 @@ void launch_oc_update(int64_t n, const double *x0, const double *dJ, const doubl
 
 void launch_sum_partials(const double *x, int64_t n, double *partials, cudaStream_t st) {
     sum_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(x, n, partials);
+    VFEM_LAUNCH_CHECK();
+}
+
+
+// Device address of the filter scratch array, looked up once per device (with that device
+// current) by the first call on it.
+static double *noalloc_scratch_address() {
+    static std::mutex mu;
+    static double *addr[64] = {nullptr};
+    int dev = 0;
+    VFEM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error(ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        VFEM_CUDA(cudaGetSymbolAddress(&p, g_filter_scratch));
+        addr[dev] = (double *)p;
+    }
+    return addr[dev];
+}
+
+int noalloc_filter_max_radius() { return NOALLOC_MAX_RADIUS; }
+
+void launch_smoothing_filter_noalloc(const int dims[3], int radius, int type, const double *in, double *out,
+                                     cudaStream_t st) {
+    if (radius < 0 || radius > NOALLOC_MAX_RADIUS)
+        throw Error(ERR_ARG, "filter radius " + std::to_string(radius) + " exceeds the maximum " +
+                                 std::to_string(NOALLOC_MAX_RADIUS) + " of the allocation-free filter");
+    double *scratch = noalloc_scratch_address();
+    const int ncand = (2 * radius + 1) * (2 * radius + 1) * (2 * radius + 1);
+    noalloc_taps_kernel<<<1, 32, 0, st>>>(radius, type, scratch);
+    VFEM_LAUNCH_CHECK();
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+    smoothing_filter_noalloc_kernel<<<gridFor(n, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], in, out, scratch,
+                                                                    ncand);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -301,6 +301,21 @@ int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const dou
         finishOut(vo, st);
     });
 }
+int vfem_smoothing_filter_noalloc(const int64_t dims[3], int radius, int type, const double *in_dev,
+                                  double *out_dev, void *stream) {
+    return guarded([&] {
+        need(dims, "dims"); need(in_dev, "in"); need(out_dev, "out");
+        int d[3];
+        for (int i = 0; i < 3; ++i) {
+            if (dims[i] <= 0 || dims[i] > (1 << 20)) throw Error(ERR_ARG, "invalid dims");
+            d[i] = (int)dims[i];
+        }
+        if (type != 0 && type != 1) throw Error(ERR_ARG, "Unexpected smoothing kernel type");
+        if (!isDevicePtr(in_dev) || !isDevicePtr(out_dev))
+            throw Error(ERR_ARG, "the allocation-free filter takes device pointers only (host arrays would need staging)");
+        launch_smoothing_filter_noalloc(d, radius, type, in_dev, out_dev, (cudaStream_t)stream);
+    });
+}
 int vfem_projection_apply(int64_t n, double beta, const double *in, double *out) {
     return guarded([&] {
         if (!(beta > 0)) throw Error(ERR_ARG, "Beta parameter has to be positive");

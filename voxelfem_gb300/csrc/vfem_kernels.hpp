@@ -124,6 +124,10 @@ void launch_enforce_dirichlet(const Geom &g, T *u, const uint8_t *dmask, const d
 
 // ---------------- topology optimisation (k_topopt.cu) ----------------
 void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st);
+// Allocation-free density filter: taps in a file-scope device array (radius <= noalloc_filter_max_radius()).
+void launch_smoothing_filter_noalloc(const int dims[3], int radius, int type, const double *in, double *out,
+                                     cudaStream_t st);
+int noalloc_filter_max_radius();
 void launch_projection(int64_t n, double beta, const double *in, double *out, cudaStream_t st);
 void launch_projection_backprop(int64_t n, double beta, const double *in, const double *vars, double *out,
                                 cudaStream_t st);
