@@ -270,7 +270,10 @@ def run_ours(args):
     clocks.start()
     cnt0 = C.c_uint64()
     _capi.check(lib.vfem_kernel_launch_count(C.byref(cnt0)))
+    # NVTX range: lets a profiler restrict its launch list to the timed mixed solves
+    torch.cuda.nvtx.range_push("vfem_mixed_solve")
     tmix, wall, (itmix, rrmix) = timed(step_device, args.steps)
+    torch.cuda.nvtx.range_pop()
     cnt1 = C.c_uint64()
     _capi.check(lib.vfem_kernel_launch_count(C.byref(cnt1)))
     clk = clocks.stop()
@@ -364,6 +367,29 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_kernel_case(args):
+    """One hot kernel of the workload, launched a handful of times (profiler captures)."""
+    import ctypes as C
+
+    import torch
+
+    torch.cuda.set_device(0)
+    from voxelfem_gb300 import _capi
+    from voxelfem_gb300 import pyVoxelFEM as pv
+    from voxelfem_gb300 import workloads as wl
+
+    lib = _capi.load()
+    ne, rho_lo, levels = CONFIGS[args.config]
+    bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
+    sim = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
+    wl.setup_cantilever(sim, ne, rho_lo, 0)
+    mg = sim.multigridSolver(levels)
+    mg.setPrecision("mixed", "df")
+    ms, nbytes = C.c_double(), C.c_double()
+    _capi.check(lib.vfem_mg_time_kernel(mg._h, args.kernel_case, 1, C.byref(ms), C.byref(nbytes)))
+    print(json.dumps({"kernel": KERNEL_NAMES[args.kernel_case], "ms": ms.value, "bytes": nbytes.value}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -372,11 +398,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--kernel-case", type=int, default=None,
+                    help="only set up the workload and launch one hot kernel (id of vfem_mg_time_kernel) twice")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.kernel_case is not None:
+        run_kernel_case(args)
     else:
         run_ours(args)
 

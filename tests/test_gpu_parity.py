@@ -59,7 +59,15 @@ def test_dirichlet_and_load(gpu, oracle):
     np.testing.assert_array_equal(g.buildLoadVector(), o.buildLoadVector())
 
 
-def test_level_operators(gpu, oracle):
+@pytest.fixture(params=["rows", "planes"])
+def stencil_layout(request, monkeypatch):
+    """Assembled coarse stencils as node-contiguous rows (small levels) or colour-ordered
+    planes (large levels): force one layout on every level of the solver under test."""
+    monkeypatch.setenv("VFEM_STENCIL_ROWS_MAX_NODES", "1000000000" if request.param == "rows" else "0")
+    return request.param
+
+
+def test_level_operators(gpu, oracle, stencil_layout):
     ne = (16, 8, 8)
     g, o, gm, om = make_pair(oracle, ne, levels=3)
     om.updateStiffnessMatrices()
@@ -89,7 +97,7 @@ def test_level_operators(gpu, oracle):
 
 
 @pytest.mark.parametrize("ne,levels", [((16, 8, 8), 2), ((32, 16, 16), 3)])
-def test_pcg_fp64(gpu, oracle, ne, levels):
+def test_pcg_fp64(gpu, oracle, stencil_layout, ne, levels):
     g, o, gm, om = make_pair(oracle, ne, levels=levels)
     b = g.buildLoadVector()
     x0 = np.zeros_like(b)
@@ -126,9 +134,10 @@ def test_mg_solve_vcycles(gpu, oracle):
     assert rel(gm.solve(x0, b, 2, 1, fullMultigrid=True), om.solve(x0, b, 2, 1, fullMultigrid=True)) < 1e-10
 
 
-def test_masked_layers(gpu, oracle):
+@pytest.mark.parametrize("levels", [2, 3])
+def test_masked_layers(gpu, oracle, stencil_layout, levels):
     ne = (16, 16, 8)
-    g, o, gm, om = make_pair(oracle, ne, levels=2, mask_layer=9)
+    g, o, gm, om = make_pair(oracle, ne, levels=levels, mask_layer=9)
     assert rel(g.getYoungModulusScaleFactor(), o.youngModuli()) < 1e-15
     u = np.random.default_rng(3).standard_normal((g.numNodes(), 3))
     assert rel(g.applyK(u), o.applyK(u)) < 1e-12
@@ -139,7 +148,7 @@ def test_masked_layers(gpu, oracle):
     assert rel(xg, xo) < 1e-8
 
 
-def test_pcg_mixed_precision(gpu, oracle):
+def test_pcg_mixed_precision(gpu, oracle, stencil_layout):
     ne = (32, 16, 16)
     g, o, gm, om = make_pair(oracle, ne, levels=3)
     b = g.buildLoadVector()

@@ -3,126 +3,106 @@
 // prolongation (MultigridSolver.hh:163-275) and Galerkin coarsening of element
 // matrices (MultigridSolver.hh:712-819).
 //
-// Stencil layout: S[(o*9 + 3r + c) * ld + n] is block (n, n+o)(r, c) with
-// o = (ox+1)*9 + (oy+1)*3 + (oz+1); rows are visited in ascending neighbour
-// index, the order of the reference's CSC columns.
+// Stencil layouts, block (n, n+o)(r, c) with o = (ox+1)*9 + (oy+1)*3 + (oz+1) (ascending
+// neighbour index, the order of the reference's CSC columns):
+//  * rows (small levels): S[n * 256 + o*9 + 3r + c], node-contiguous, padded to 256 entries;
+//    one warp per node;
+//  * planes (large levels): S[(o*9 + 3r + c) * NN + p], p the node's colour-ordered position
+//    (stencil::colour_pos); one thread per node, and a colour pass reads contiguous slices.
 // Element-matrix layout (levels >= 1): Ke[e*576 + 24*row + col].
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
+#include "vfem_stencil.cuh"
 
 namespace vfem {
 
 namespace {
 
 constexpr int BS = 256;
-
-__device__ __forceinline__ void decode(const int64_t n, const int nn1, const int nn2, int &i, int &j, int &k) {
-    k = (int)(n % nn2);
-    const int64_t t = n / nn2;
-    j = (int)(t % nn1);
-    i = (int)(t / nn1);
-}
-
-// Branch-free row gather: neighbours outside the grid are clamped to a valid node; their
-// stencil blocks are exactly zero (no element contains both nodes), so they add nothing and
-// every load of the row can be in flight at once.
-template <typename T, bool Negate>
-__device__ __forceinline__ void stencil_row(const Geom &g, const T *__restrict__ S, const T *__restrict__ u, int64_t n,
-                                            int i, int j, int k, T &f0, T &f1, T &f2) {
-    const int64_t ld = g.ld;
-    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
-    const int64_t dx[3] = {i > 0 ? -sx : 0, 0, i + 1 < g.nn[0] ? sx : 0};
-    const int64_t dy[3] = {j > 0 ? -sy : 0, 0, j + 1 < g.nn[1] ? sy : 0};
-    const int64_t dz[3] = {k > 0 ? -1 : 0, 0, k + 1 < g.nn[2] ? 1 : 0};
-#pragma unroll
-    for (int o = 0; o < 27; ++o) {
-        const int64_t m = n + dx[o / 9] + dy[(o / 3) % 3] + dz[o % 3];
-        const T u0 = u[m], u1 = u[ld + m], u2 = u[2 * ld + m];
-        const T *blk = S + (int64_t)(o * 9) * ld + n;
-        const T v0 = blk[0] * u0 + blk[ld] * u1 + blk[2 * ld] * u2;
-        const T v1 = blk[3 * ld] * u0 + blk[4 * ld] * u1 + blk[5 * ld] * u2;
-        const T v2 = blk[6 * ld] * u0 + blk[7 * ld] * u1 + blk[8 * ld] * u2;
-        if (Negate) { f0 -= v0; f1 -= v1; f2 -= v2; }
-        else        { f0 += v0; f1 += v1; f2 += v2; }
-    }
-}
+using stencil::decode;
+using stencil::node_solve;
+using stencil::ROW;
+constexpr int WPB = BS / 32;  // warps (rows) per block
 
 template <typename T, bool ZeroInit, bool Negate>
 __global__ void __launch_bounds__(BS) stencil_apply_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u,
                                                            T *__restrict__ out) {
-    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t n = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n >= g.NN) return;
     int i, j, k;
     decode(n, g.nn[1], g.nn[2], i, j, k);
-    const int64_t ld = g.ld;
-    T f0 = ZeroInit ? T(0) : out[n], f1 = ZeroInit ? T(0) : out[ld + n], f2 = ZeroInit ? T(0) : out[2 * ld + n];
-    stencil_row<T, Negate>(g, S, u, n, i, j, k, f0, f1, f2);
-    out[n] = f0;
-    out[ld + n] = f1;
-    out[2 * ld + n] = f2;
+    T v[8], f0, f1, f2;
+    stencil::row_times_u<T>(g, S, u, n, i, j, k, lane, v, f0, f1, f2);
+    if (lane == 0) {
+        const int64_t ld = g.ld;
+        const T s = Negate ? T(-1) : T(1);
+        out[n] = (ZeroInit ? T(0) : out[n]) + s * f0;
+        out[ld + n] = (ZeroInit ? T(0) : out[ld + n]) + s * f1;
+        out[2 * ld + n] = (ZeroInit ? T(0) : out[2 * ld + n]) + s * f2;
+    }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(BS) stencil_residual_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u,
                                                               const T *__restrict__ b, T *__restrict__ r,
                                                               const uint8_t *__restrict__ dmask) {
-    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t n = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n >= g.NN) return;
     int i, j, k;
     decode(n, g.nn[1], g.nn[2], i, j, k);
-    const int64_t ld = g.ld;
-    T f0 = b[n], f1 = b[ld + n], f2 = b[2 * ld + n];
-    if (j < g.nyv()) stencil_row<T, true>(g, S, u, n, i, j, k, f0, f1, f2);
-    const uint8_t dm = dmask[n];
-    if (dm & 1) f0 = T(0);
-    if (dm & 2) f1 = T(0);
-    if (dm & 4) f2 = T(0);
-    r[n] = f0;
-    r[ld + n] = f1;
-    r[2 * ld + n] = f2;
+    stencil::residual_node_warp<T>(g, S, u, b, r, dmask, n, i, j, k, lane);
 }
 
-template <typename T>
-__device__ __forceinline__ void node_solve(uint8_t dm, T s0, T s1, T s2, const T *M, bool forward, T &u0, T &u1,
-                                           T &u2) {
-    if (dm) {
-        T d[3] = {T(0), T(0), T(0)};
-        const T bs[3] = {s0, s1, s2};
-        if (forward) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q)
-                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
-                       (T(!((dm >> q) & 1)) / M[4 * q]);
-        } else {
-#pragma unroll
-            for (int q = 2; q >= 0; --q)
-                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
-                       (T(!((dm >> q) & 1)) / M[4 * q]);
-        }
-        u0 += d[0];
-        u1 += d[1];
-        u2 += d[2];
-    } else {
-        const T c00 = M[4] * M[8] - M[5] * M[7];
-        const T c01 = M[5] * M[6] - M[3] * M[8];
-        const T c02 = M[3] * M[7] - M[4] * M[6];
-        const T det = M[0] * c00 + M[1] * c01 + M[2] * c02;
-        const T id = T(1) / det;
-        const T i00 = c00 * id, i01 = (M[2] * M[7] - M[1] * M[8]) * id, i02 = (M[1] * M[5] - M[2] * M[4]) * id;
-        const T i10 = c01 * id, i11 = (M[0] * M[8] - M[2] * M[6]) * id, i12 = (M[2] * M[3] - M[0] * M[5]) * id;
-        const T i20 = c02 * id, i21 = (M[1] * M[6] - M[0] * M[7]) * id, i22 = (M[0] * M[4] - M[1] * M[3]) * id;
-        u0 += i00 * s0 + i01 * s1 + i02 * s2;
-        u1 += i10 * s0 + i11 * s1 + i12 * s2;
-        u2 += i20 * s0 + i21 * s1 + i22 * s2;
-    }
-}
-
-// Block Gauss-Seidel colour pass from stencil rows (MultigridSolver.hh:323-334, 348-378).
+// Block Gauss-Seidel colour pass from stencil rows (MultigridSolver.hh:323-334, 348-378),
+// one warp per node of the colour.
 template <typename T>
 __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *__restrict__ S, T *u,
                                                               const T *__restrict__ b,
                                                               const uint8_t *__restrict__ dmask, int cx, int cy,
                                                               int cz, int forward) {
+    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    const int lane = threadIdx.x & 31;
+    const int64_t t = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
+    if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
+    const int kk = (int)(t % n2);
+    const int64_t q = t / n2;
+    const int jj = (int)(q % n1), ii = (int)(q / n1);
+    stencil::gs_node_warp<T>(g, S, u, b, dmask, cx + 2 * ii, cy + 2 * jj, cz + 2 * kk, forward != 0, lane);
+}
+
+template <typename T, bool ZeroInit, bool Negate>
+__global__ void __launch_bounds__(BS) stencil_apply_soa_kernel(Geom g, const T *__restrict__ S,
+                                                               const T *__restrict__ u, T *__restrict__ out) {
+    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (p >= g.NN) return;
+    int i, j, k;
+    stencil::colour_node(g, p, i, j, k);
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    T f0 = ZeroInit ? T(0) : out[n], f1 = ZeroInit ? T(0) : out[ld + n], f2 = ZeroInit ? T(0) : out[2 * ld + n];
+    stencil::stencil_row_soa<T, Negate>(g, S, u, n, p, i, j, k, f0, f1, f2);
+    out[n] = f0;
+    out[ld + n] = f1;
+    out[2 * ld + n] = f2;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BS) stencil_residual_soa_kernel(Geom g, const T *__restrict__ S,
+                                                                  const T *__restrict__ u, const T *__restrict__ b,
+                                                                  T *__restrict__ r, const uint8_t *__restrict__ dmask) {
+    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (p >= g.NN) return;
+    int i, j, k;
+    stencil::colour_node(g, p, i, j, k);
+    stencil::residual_node_soa<T>(g, S, u, b, r, dmask, g.node(i, j, k), p, i, j, k);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BS) gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u,
+                                                                  const T *__restrict__ b,
+                                                                  const uint8_t *__restrict__ dmask, int cx, int cy,
+                                                                  int cz, int forward) {
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
@@ -130,19 +110,7 @@ __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *_
     const int64_t q = t / n2;
     const int jj = (int)(q % n1), ii = (int)(q / n1);
     const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
-    const int64_t n = g.node(i, j, k), ld = g.ld;
-    const uint8_t dm = dmask[n];
-    if (dm == 7) return;
-    T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
-    stencil_row<T, true>(g, S, u, n, i, j, k, s0, s1, s2);
-    T M[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + n];
-    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
-    node_solve<T>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
-    u[n] = u0;
-    u[ld + n] = u1;
-    u[2 * ld + n] = u2;
+    stencil::gs_node_soa<T>(g, S, u, b, dmask, i, j, k, stencil::colour_pos(g, i, j, k), forward != 0);
 }
 
 // Full-weighting restriction (MultigridSolver.hh:217-275): coarse node gathers the
@@ -157,30 +125,7 @@ __global__ void __launch_bounds__(BS) restrict_kernel(Geom gf, Geom gc, const T 
     if (t >= (int64_t)gc.nn[0] * rows * gc.nn[2]) return;
     int i, j, k;
     decode(t, rows, gc.nn[2], i, j, k);
-    const int64_t cn = gc.node(i, j, k);
-    T v0 = T(0), v1 = T(0), v2 = T(0);
-    if (j < cyv) {
-        const int fyv = gf.nyv();
-        const int lo0 = max(2 * i - 1, 0), lo1 = max(2 * j - 1, 0), lo2 = max(2 * k - 1, 0);
-        const int hi0 = min(2 * i + 2, gf.nn[0]), hi1 = min(2 * j + 2, fyv), hi2 = min(2 * k + 2, gf.nn[2]);
-        const int64_t ld = gf.ld;
-        for (int a = lo0; a < hi0; ++a) {
-            const T wa = T(1) - T(abs(a - 2 * i)) * T(0.5);
-            for (int bb = lo1; bb < hi1; ++bb) {
-                const T wb = wa * (T(1) - T(abs(bb - 2 * j)) * T(0.5));
-                for (int c = lo2; c < hi2; ++c) {
-                    const T w = wb * (T(1) - T(abs(c - 2 * k)) * T(0.5));
-                    const int64_t fn = gf.node(a, bb, c);
-                    v0 += w * fine[fn];
-                    v1 += w * fine[ld + fn];
-                    v2 += w * fine[2 * ld + fn];
-                }
-            }
-        }
-    }
-    coarse[cn] = v0;
-    coarse[gc.ld + cn] = v1;
-    coarse[2 * gc.ld + cn] = v2;
+    stencil::restrict_node<T>(gf, gc, fine, coarse, i, j, k);
 }
 
 // Trilinear prolongation (MultigridSolver.hh:163-212).
@@ -192,34 +137,7 @@ __global__ void __launch_bounds__(BS) interp_kernel(Geom gf, Geom gc, const T *_
     if (t >= (int64_t)gf.nn[0] * rows * gf.nn[2]) return;
     int f[3];
     decode(t, rows, gf.nn[2], f[0], f[1], f[2]);
-    int ec[3], lf[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        ec[d] = min(f[d] / 2, gc.ne[d]);
-        lf[d] = f[d] - 2 * ec[d];
-    }
-    const int64_t fn = gf.node(f[0], f[1], f[2]);
-    const int64_t fld = gf.ld, cld = gc.ld;
-    T a0 = Accumulate ? fine[fn] : T(0), a1 = Accumulate ? fine[fld + fn] : T(0),
-      a2 = Accumulate ? fine[2 * fld + fn] : T(0);
-#pragma unroll
-    for (int cnl = 0; cnl < 8; ++cnl) {
-        const int cb[3] = {(cnl >> 2) & 1, (cnl >> 1) & 1, cnl & 1};
-        T coeff = T(1);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T phi = (lf[d] == 1) ? T(0.5) : ((lf[d] == 0) ? (cb[d] ? T(0) : T(1)) : (cb[d] ? T(1) : T(0)));
-            coeff *= phi;
-        }
-        if (coeff == T(0)) continue;
-        const int64_t cidx = gc.node(ec[0] + cb[0], ec[1] + cb[1], ec[2] + cb[2]);
-        a0 += coeff * coarse[cidx];
-        a1 += coeff * coarse[cld + cidx];
-        a2 += coeff * coarse[2 * cld + cidx];
-    }
-    fine[fn] = a0;
-    fine[fld + fn] = a1;
-    fine[2 * fld + fn] = a2;
+    stencil::interp_node<T, Accumulate>(gf, gc, coarse, fine, f);
 }
 
 template <typename T>
@@ -281,18 +199,58 @@ __global__ void __launch_bounds__(576) ke_level1_kernel(Geom g1, Geom g0, const 
 // Level-1 27-point stencil straight from the fine Young's moduli: block (n, n+o)(r, c) =
 // sum over coarse elements e holding both nodes of sum_fi E_f(e, fi) Kc_fi[3ln+r][3lm+c]
 // (the assembly of MultigridSolver.hh:724-738 without storing the element matrices).
-// Thread per (node n, entry q), q = blockIdx.y: the Kc index is warp-uniform.
+// One block per node, thread q writes row entry q (coalesced 1 KB row).
 template <typename T>
-__global__ void __launch_bounds__(BS) stencil_level1_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
-                                                            const T *__restrict__ Kc, T *__restrict__ S) {
-    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
-    const int q = blockIdx.y;
-    if (n >= g1.NN) return;
+__global__ void __launch_bounds__(ROW) stencil_level1_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
+                                                             const T *__restrict__ Kc, T *__restrict__ S) {
+    __shared__ T sE[8][8];  // fine moduli of the 8 coarse elements around the node
+    const int64_t n = blockIdx.x;
+    const int q = threadIdx.x;
     int i, j, k;
     decode(n, g1.nn[1], g1.nn[2], i, j, k);
-    const int o = q / 9, rc = q % 9, r = rc / 3, c = rc % 3;
-    const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+    if (q < 64) {
+        const int slot = q >> 3, fi = q & 7;
+        const int a = (slot >> 2) & 1, b = (slot >> 1) & 1, cc = slot & 1;
+        const int ei = i - a, ej = j - b, ek = k - cc;
+        T E = T(0);
+        if (ei >= 0 && ej >= 0 && ek >= 0 && ei < g1.ne[0] && ej < g1.ne[1] && ek < g1.ne[2] && ej < g1.firstMaskedE)
+            E = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
+        sE[slot][fi] = E;
+    }
+    __syncthreads();
     T acc = T(0);
+    if (q < stencil::ROW_USED) {
+        const int o = q / 9, rc = q % 9, r = rc / 3, c = rc % 3;
+        const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+#pragma unroll
+        for (int slot = 0; slot < 8; ++slot) {
+            const int a = (slot >> 2) & 1, b = (slot >> 1) & 1, cc = slot & 1;
+            const int ma = a + oo[0], mb = b + oo[1], mc = cc + oo[2];
+            if (ma < 0 || ma > 1 || mb < 0 || mb > 1 || mc < 0 || mc > 1) continue;
+            const int idx = (3 * (4 * a + 2 * b + cc) + r) * 24 + 3 * (4 * ma + 2 * mb + mc) + c;
+#pragma unroll
+            for (int fi = 0; fi < 8; ++fi) acc += sE[slot][fi] * Kc[fi * 576 + idx];
+        }
+    }
+    S[n * ROW + q] = acc;
+}
+
+// Plane-layout variant: thread per (position p, neighbour offset o), o = blockIdx.y, writing
+// the nine entries of block (n, n+o). The Kc indices are warp-uniform (constant-cache
+// broadcasts) and the eight fine moduli of each shared coarse element are loaded once for
+// all nine entries.
+template <typename T>
+__global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
+                                                                const T *__restrict__ Kc, T *__restrict__ S) {
+    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
+    const int o = blockIdx.y;
+    if (p >= g1.NN) return;
+    int i, j, k;
+    stencil::colour_node(g1, p, i, j, k);
+    const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+    T acc[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) acc[e] = T(0);
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -304,14 +262,67 @@ __global__ void __launch_bounds__(BS) stencil_level1_kernel(Geom g1, Geom g0, co
                 const int ei = i - a, ej = j - b, ek = k - cc;
                 if (ei < 0 || ej < 0 || ek < 0 || ei >= g1.ne[0] || ej >= g1.ne[1] || ek >= g1.ne[2]) continue;
                 if (ej >= g1.firstMaskedE) continue;
-                const int idx = (3 * (4 * a + 2 * b + cc) + r) * 24 + 3 * (4 * ma + 2 * mb + mc) + c;
+                T E[8];
 #pragma unroll
-                for (int fi = 0; fi < 8; ++fi) {
-                    const T E = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
-                    acc += E * Kc[fi * 576 + idx];
-                }
+                for (int fi = 0; fi < 8; ++fi)
+                    E[fi] = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
+                const int ln = 4 * a + 2 * b + cc, lm = 4 * ma + 2 * mb + mc;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const int idx = (3 * ln + r) * 24 + 3 * lm + c;
+                        T v = acc[3 * r + c];
+#pragma unroll
+                        for (int fi = 0; fi < 8; ++fi) v += E[fi] * Kc[fi * 576 + idx];
+                        acc[3 * r + c] = v;
+                    }
             }
-    S[(int64_t)q * g1.ld + n] = acc;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) S[(int64_t)(o * 9 + e) * g1.ld + p] = acc[e];
+}
+
+// Level-2 element matrices straight from the fine moduli: Ke_2(e) = sum over the 64 fine
+// elements f inside e of E_f K2_f, K2_f = Phi_c^T Phi_fi^T K0 Phi_fi Phi_c for f in child c,
+// position fi (the two coarsenings of MultigridSolver.hh:712-738 folded into one constant
+// table). Children at or above the level-1 masked layer contribute nothing, as their level-1
+// element matrices are zero. One block per EB2 elements, thread t owns entry t; each K2 entry
+// is loaded once per block and applied to all EB2 elements.
+constexpr int EB2 = 8;
+template <typename T>
+__global__ void __launch_bounds__(576) ke_level2_kernel(Geom g2, Geom g1, Geom g0, const T *__restrict__ Y0,
+                                                        const T *__restrict__ K2, T *__restrict__ Ke2) {
+    __shared__ T sY[EB2][64];
+    const int t = threadIdx.x;
+    const int64_t e0 = (int64_t)blockIdx.x * EB2;
+    for (int q = t; q < EB2 * 64; q += 576) {
+        const int eb = q >> 6, f = q & 63;
+        const int64_t e = e0 + eb;
+        T v = T(0);
+        if (e < g2.NE) {
+            const int ek = (int)(e % g2.ne[2]);
+            const int64_t r = e / g2.ne[2];
+            const int ej = (int)(r % g2.ne[1]), ei = (int)(r / g2.ne[1]);
+            const int c = f >> 3, fi = f & 7;
+            const int i1 = 2 * ei + ((c >> 2) & 1), j1 = 2 * ej + ((c >> 1) & 1), k1 = 2 * ek + (c & 1);
+            if (ej < g2.firstMaskedE && j1 < g1.firstMaskedE)
+                v = Y0[g0.elem(2 * i1 + ((fi >> 2) & 1), 2 * j1 + ((fi >> 1) & 1), 2 * k1 + (fi & 1))];
+        }
+        sY[eb][f] = v;
+    }
+    __syncthreads();
+    T acc[EB2];
+#pragma unroll
+    for (int eb = 0; eb < EB2; ++eb) acc[eb] = T(0);
+#pragma unroll 4
+    for (int f = 0; f < 64; ++f) {
+        const T kv = K2[f * 576 + t];
+#pragma unroll
+        for (int eb = 0; eb < EB2; ++eb) acc[eb] += sY[eb][f] * kv;
+    }
+#pragma unroll
+    for (int eb = 0; eb < EB2; ++eb)
+        if (e0 + eb < g2.NE) Ke2[(e0 + eb) * 576 + t] = acc[eb];
 }
 
 // Ke_c = sum_fi Phi_fi^T Ke_child(fi) Phi_fi (MultigridSolver.hh:712-722, 745-819).
@@ -367,18 +378,47 @@ __global__ void __launch_bounds__(BS) ke_scaled_kernel(Geom g, const T *__restri
 }
 
 // Assemble the 27-point block stencil from element matrices (TensorProductSimulator.hh:885-930).
-// Thread per (node n, stencil entry q); q = blockIdx.y.
+// One block per node, thread q writes row entry q.
 template <typename T>
-__global__ void __launch_bounds__(BS) stencil_from_ke_kernel(Geom g, const T *__restrict__ Ke, T *__restrict__ S) {
-    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
-    const int q = blockIdx.y;
-    if (n >= g.NN) return;
+__global__ void __launch_bounds__(ROW) stencil_from_ke_kernel(Geom g, const T *__restrict__ Ke, T *__restrict__ S) {
+    const int64_t n = blockIdx.x;
+    const int q = threadIdx.x;
     int i, j, k;
     decode(n, g.nn[1], g.nn[2], i, j, k);
-    const int o = q / 9, rc = q % 9, r = rc / 3, c = rc % 3;
-    const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
     T acc = T(0);
-    // incident elements (i-a, j-b, k-cc): node local index ln = 4a+2b+cc; neighbour local = ln + o
+    if (q < stencil::ROW_USED) {
+        const int o = q / 9, rc = q % 9, r = rc / 3, c = rc % 3;
+        const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+        // incident elements (i-a, j-b, k-cc): node local index ln = 4a+2b+cc; neighbour local = ln + o
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc) {
+                    const int ma = a + oo[0], mb = b + oo[1], mc = cc + oo[2];
+                    if (ma < 0 || ma > 1 || mb < 0 || mb > 1 || mc < 0 || mc > 1) continue;
+                    const int ei = i - a, ej = j - b, ek = k - cc;
+                    if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) continue;
+                    const int ln = 4 * a + 2 * b + cc, lm = 4 * ma + 2 * mb + mc;
+                    acc += Ke[g.elem(ei, ej, ek) * 576 + (3 * ln + r) * 24 + 3 * lm + c];
+                }
+    }
+    S[n * ROW + q] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T *__restrict__ Ke,
+                                                                 T *__restrict__ S) {
+    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
+    const int o = blockIdx.y;
+    if (p >= g.NN) return;
+    int i, j, k;
+    stencil::colour_node(g, p, i, j, k);
+    const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+    T acc[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) acc[e] = T(0);
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -390,16 +430,34 @@ __global__ void __launch_bounds__(BS) stencil_from_ke_kernel(Geom g, const T *__
                 const int ei = i - a, ej = j - b, ek = k - cc;
                 if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) continue;
                 const int ln = 4 * a + 2 * b + cc, lm = 4 * ma + 2 * mb + mc;
-                acc += Ke[g.elem(ei, ej, ek) * 576 + (3 * ln + r) * 24 + 3 * lm + c];
+                const T *ke = Ke + g.elem(ei, ej, ek) * 576;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) acc[3 * r + c] += ke[(3 * ln + r) * 24 + 3 * lm + c];
             }
-    S[(int64_t)q * g.ld + n] = acc;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) S[(int64_t)(o * 9 + e) * g.ld + p] = acc[e];
 }
 
 }  // namespace
 
 template <typename T>
-void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, cudaStream_t st) {
-    const unsigned grid = gridFor(g.NN, BS);
+void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
+                          cudaStream_t st) {
+    if (!rows) {
+        const unsigned gs = gridFor(g.NN, BS);
+        if (zeroInit) {
+            if (negate) stencil_apply_soa_kernel<T, true, true><<<gs, BS, 0, st>>>(g, S, u, out);
+            else stencil_apply_soa_kernel<T, true, false><<<gs, BS, 0, st>>>(g, S, u, out);
+        } else {
+            if (negate) stencil_apply_soa_kernel<T, false, true><<<gs, BS, 0, st>>>(g, S, u, out);
+            else stencil_apply_soa_kernel<T, false, false><<<gs, BS, 0, st>>>(g, S, u, out);
+        }
+        VFEM_LAUNCH_CHECK();
+        return;
+    }
+    const unsigned grid = gridFor(g.NN, WPB);
     if (zeroInit) {
         if (negate) stencil_apply_kernel<T, true, true><<<grid, BS, 0, st>>>(g, S, u, out);
         else stencil_apply_kernel<T, true, false><<<grid, BS, 0, st>>>(g, S, u, out);
@@ -411,20 +469,25 @@ void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool ze
 }
 
 template <typename T>
-void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask,
+void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st) {
-    stencil_residual_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, S, u, b, r, dmask);
+    if (rows) stencil_residual_kernel<T><<<gridFor(g.NN, WPB), BS, 0, st>>>(g, S, u, b, r, dmask);
+    else stencil_residual_soa_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, S, u, b, r, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
-                             cudaStream_t st) {
+                             bool rows, cudaStream_t st) {
     const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
     const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
-    gs_stencil_color_kernel<T><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
-                                                                          forward ? 1 : 0);
+    if (rows)
+        gs_stencil_color_kernel<T><<<gridFor(n0 * n1 * n2, WPB), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
+                                                                               forward ? 1 : 0);
+    else
+        gs_stencil_color_soa_kernel<T><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
+                                                                                  forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -481,9 +544,10 @@ void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, 
 }
 
 template <typename T>
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, cudaStream_t st) {
-    dim3 grid(gridFor(g1.NN, BS), 243);
-    stencil_level1_kernel<T><<<grid, BS, 0, st>>>(g1, g0, Y0, Kc, S);
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st) {
+    if (g1.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
+    if (rows) stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
+    else stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), 27), BS, 0, st>>>(g1, g0, Y0, Kc, S);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -495,33 +559,42 @@ void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *ph
 }
 
 template <typename T>
+void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st) {
+    ke_level2_kernel<T><<<gridFor(g2.NE, EB2), 576, 0, st>>>(g2, g1, g0, Y0, K2, Ke2);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
 void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_t st) {
     ke_scaled_kernel<T><<<gridFor(g.NE * 576, BS), BS, 0, st>>>(g, Y, K0, Ke);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, cudaStream_t st) {
-    dim3 grid(gridFor(g.NN, BS), 243);
-    stencil_from_ke_kernel<T><<<grid, BS, 0, st>>>(g, Ke, S);
+void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st) {
+    if (g.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
+    if (rows) stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
+    else stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), 27), BS, 0, st>>>(g, Ke, S);
     VFEM_LAUNCH_CHECK();
 }
 
 #define VFEM_INST_COARSE(T)                                                                                           \
-    template void launch_stencil_apply<T>(const Geom &, const T *, const T *, T *, bool, bool, cudaStream_t);         \
+    template void launch_stencil_apply<T>(const Geom &, const T *, const T *, T *, bool, bool, bool, cudaStream_t);   \
     template void launch_stencil_residual<T>(const Geom &, const T *, const T *, const T *, T *, const uint8_t *,     \
-                                             cudaStream_t);                                                           \
+                                             bool, cudaStream_t);                                                     \
     template void launch_gs_stencil_color<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, bool,     \
-                                             cudaStream_t);                                                           \
+                                             bool, cudaStream_t);                                                     \
     template void launch_restrict<T>(const Geom &, const Geom &, const T *, T *, cudaStream_t);                       \
     template void launch_interpolate<T>(const Geom &, const Geom &, const T *, T *, bool, cudaStream_t);              \
     template void launch_zero_dirichlet<T>(const Geom &, T *, const uint8_t *, cudaStream_t);                         \
     template void launch_masked_zero<T>(const Geom &, T *, int, cudaStream_t);                                        \
     template void launch_fill<T>(T *, T, int64_t, cudaStream_t);                                                      \
     template void launch_ke_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);           \
-    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);      \
+    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, bool, cudaStream_t); \
     template void launch_ke_coarsen<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);          \
-    template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, cudaStream_t);                              \
+    template void launch_ke_level2<T>(const Geom &, const Geom &, const Geom &, const T *, const T *, T *,            \
+                                      cudaStream_t);                                                                  \
+    template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, bool, cudaStream_t);                        \
     template void launch_ke_scaled<T>(const Geom &, const T *, const T *, T *, cudaStream_t);
 VFEM_INST_COARSE(double)
 VFEM_INST_COARSE(float)

@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float 
                                                             const double *__restrict__ u, double *__restrict__ out,
                                                             const uint8_t *__restrict__ dmask, int zeroDir,
                                                             double *__restrict__ partials, int withDot,
-                                                            const Mat24DF K) {
+                                                            const double *__restrict__ rhs, const Mat24DF K) {
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     double dot = 0.0;
     if (n < g.NN) {
@@ -317,6 +317,12 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float 
 #pragma unroll
             for (int r = 0; r < 3; ++r) f[r] = ((dm >> r) & 1) ? 0.0 : (double)fh[r] + (double)fl[r];
             if (withDot) dot = u[n] * f[0] + u[ld + n] * f[1] + u[2 * ld + n] * f[2];
+        }
+        if (rhs) {
+            // residual form: rhs - K u, zero on constrained components
+            const uint8_t dm = dmask[n];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) f[r] = ((dm >> r) & 1) ? 0.0 : rhs[r * ld + n] - f[r];
         }
         out[n] = f[0];
         out[ld + n] = f[1];
@@ -341,7 +347,7 @@ __global__ void split_df_kernel(const double *__restrict__ src, float *__restric
 // ---------------- element-wise kernels ----------------
 template <typename T>
 __global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restrict__ Y, double E0, double Emin,
-                             double gamma, double q, int law, int masking) {
+                             double gamma, double q, int law, int masking, int ipow) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= g.NE) return;
     const int ej = (int)((e / g.ne[2]) % g.ne[1]);
@@ -350,7 +356,16 @@ __global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restri
         v = 0.0;
     } else {
         const double r = rho[e];
-        if (law == 0) v = Emin + pow(r, gamma) * (E0 - Emin);
+        if (law == 0) {
+            // integer SIMP exponents (the usual 3) as repeated products: FP64 pow is a long
+            // dependent sequence on this part; the product differs from it by an ulp or two
+            double pw = r;
+            if (ipow > 0)
+                for (int t = 1; t < ipow; ++t) pw *= r;
+            else
+                pw = pow(r, gamma);
+            v = Emin + pw * (E0 - Emin);
+        }
         else v = Emin + r * (E0 - Emin) / (1 + q * (1 - r));
     }
     Y[e] = (T)v;
@@ -461,7 +476,8 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
 template <typename T>
 void launch_young_moduli(const Geom &g, const double *rho, T *Y, double E0, double Emin, double gamma, double q,
                          int law, bool masking, cudaStream_t st) {
-    young_kernel<T><<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, Y, E0, Emin, gamma, q, law, masking ? 1 : 0);
+    const int ipow = (gamma >= 1.0 && gamma <= 8.0 && gamma == (double)(int)gamma) ? (int)gamma : 0;
+    young_kernel<T><<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, Y, E0, Emin, gamma, q, law, masking ? 1 : 0, ipow);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -511,11 +527,11 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
 
 void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, const float *uh, const float *ul,
                            const double *u, double *out, const Mat24DF &K0, const uint8_t *dmask, bool zeroDirichlet,
-                           double *partialDot, int partialBlocks, cudaStream_t st) {
+                           double *partialDot, int partialBlocks, cudaStream_t st, const double *rhs) {
     const unsigned grid = gridFor(g.NN, BS);
     if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
     applyk_fine_df_kernel<<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0, partialDot,
-                                               partialDot ? 1 : 0, K0);
+                                               partialDot ? 1 : 0, rhs, K0);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -4,6 +4,7 @@
 // (MultigridSolver.hh:1047-1152, TensorProductSimulator.hh:414-459).
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
+#include "vfem_stencil.cuh"
 
 namespace vfem {
 
@@ -15,12 +16,12 @@ constexpr int TB = 32;  // dense tile size
 // ---------------- dense assembly ----------------
 template <typename T>
 __global__ void dense_from_stencil_kernel(Geom g, const T *__restrict__ S, const int *__restrict__ red,
-                                          double *__restrict__ A, int nfree) {
+                                          double *__restrict__ A, int nfree, int rows) {
     // thread per (row dof of a node, stencil entry): row = 3n + r
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= g.NN * 243) return;
     const int64_t n = t / 243;
-    const int q = (int)(t % 243);
+    const int q = (int)(t % 243);  // row entry of the node-contiguous stencil
     const int o = q / 9, r = (q % 9) / 3, c = q % 3;
     const int k = (int)(n % g.nn[2]);
     const int64_t tt = n / g.nn[2];
@@ -30,7 +31,7 @@ __global__ void dense_from_stencil_kernel(Geom g, const T *__restrict__ S, const
     const int64_t m = g.node(ni, nj, nk);
     const int ra = red[3 * n + r], cb = red[3 * m + c];
     if (ra < 0 || cb < 0) return;
-    A[(int64_t)ra * nfree + cb] = (double)S[(int64_t)q * g.ld + n];
+    A[(int64_t)ra * nfree + cb] = (double)(rows ? S[n * 256 + q] : S[(int64_t)q * g.ld + stencil::colour_pos(g, i, j, k)]);
 }
 
 __global__ void symmetrize_kernel(double *A, int n) {
@@ -44,55 +45,112 @@ __global__ void symmetrize_kernel(double *A, int n) {
 }
 
 // ---------------- blocked right-looking Cholesky (lower, in place, row-major) ----------------
-// Step k: factor the diagonal tile, solve the tiles below it, then update every trailing
-// lower tile with one 32x32x32 product per block, so each step spreads over all SMs.
+// Step k: factor the diagonal tile and invert it (tile factor L_kk and its inverse), then
+// the tiles below it are X = A_ik L_kk^{-T} and every trailing lower tile is updated with
+// one 32x32x32 product per block. Dependent FP64 operations cost tens of cycles and a
+// division or square root hundreds on this part, so the only sequential chains are the
+// 32 pivot steps of each diagonal tile; panel solves and the triangular inverse become
+// plain tile products against the inverted diagonal tiles.
 __device__ __forceinline__ void load_tile(const double *A, int n, int r0, int c0, double (*t)[TB + 1]) {
     const int ty = threadIdx.y, tx = threadIdx.x;
     t[ty][tx] = (r0 + ty < n && c0 + tx < n) ? A[(int64_t)(r0 + ty) * n + c0 + tx] : 0.0;
 }
 
-__global__ void chol_diag_kernel(double *A, int n, int k, int *status) {
-    __shared__ double sl[TB][TB + 1];
+// 1/sqrt(d): single-precision seed refined by two Newton-Raphson steps,
+// y <- y + y (1 - d y^2) / 2, each doubling the number of correct bits (24 -> 48 -> full).
+// Pivots outside the single-precision normal range take the plain quotient.
+__device__ __forceinline__ double rsqrt_newton(double d) {
+    if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+    double y = (double)rsqrtf((float)d);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const double t = d * y;
+        const double e = fma(-t, y, 1.0);
+        y = fma(0.5 * y, e, y);
+    }
+    return y;
+}
+
+// One block of 32x32 threads: factor tile (k, k) in shared memory, write L_kk (lower) back
+// to A and L_kk^{-1} (lower) to Dinv[k]. FP64 issue rate is a few operations per clock per
+// SM, so each pivot reciprocal is formed once, by the thread that owns the pivot, as soon
+// as its last update lands; one barrier per pivot step.
+__device__ __forceinline__ void chol_pivot(int j, double d, int nb, double *rinv, double *rr, double *piv,
+                                           int *status) {
+    if (!(d > 0.0)) {
+        if (j < nb) atomicExch(status, 1);
+        d = 1.0;
+    }
+    const double r = rsqrt_newton(d);
+    rinv[j] = r;
+    rr[j] = r * r;
+    piv[j] = d * r;
+}
+
+__global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *status) {
+    __shared__ double sa[TB][TB + 1], sL[TB][TB + 1];
+    __shared__ double rinv[TB], rr[TB], piv[TB];
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int kb = k * TB;
     const int nb = min(TB, n - kb);
-    load_tile(A, n, kb, kb, sl);
-    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    load_tile(A, n, kb, kb, sa);
+    if (!(ty < nb && tx < nb)) sa[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    sL[ty][tx] = 0.0;
     __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        if (ty == 0 && tx == 0) {
-            const double d = sl[j][j];
-            if (!(d > 0.0)) { atomicExch(status, 1); sl[j][j] = 1.0; }
-            else sl[j][j] = sqrt(d);
+    if (ty == 0 && tx == 0) chol_pivot(0, sa[0][0], nb, rinv, rr, piv, status);
+    __syncthreads();
+    // step j: column j of L, and the rank-one update of the trailing lower triangle made
+    // from the unscaled column (a_yx -= a_yj a_xj / a_jj), so column j is only read
+    for (int j = 0; j < TB; ++j) {
+        if (tx == j && ty >= j) {
+            sL[ty][j] = (ty == j) ? piv[j] : sa[ty][j] * rinv[j];
+        } else if (tx > j && ty >= tx) {
+            const double v = fma(-sa[ty][j] * rr[j], sa[tx][j], sa[ty][tx]);
+            sa[ty][tx] = v;
+            if (ty == j + 1 && tx == j + 1) chol_pivot(j + 1, v, nb, rinv, rr, piv, status);
         }
         __syncthreads();
-        if (tx == 0 && ty > j && ty < nb) sl[ty][j] /= sl[j][j];
-        __syncthreads();
-        if (ty > j && tx > j && tx <= ty && ty < nb) sl[ty][tx] -= sl[ty][j] * sl[tx][j];
+    }
+    // L Z = I: with W_r = L_rr Z_r, W = I - (strictly lower sweep) W_y -= (L_yr / L_rr) W_r;
+    // row r of W is final after step r - 1 and only read in step r
+    double w = (ty == tx) ? 1.0 : 0.0;
+    sa[ty][tx] = w;
+    __syncthreads();
+    for (int r = 0; r + 1 < TB; ++r) {
+        if (ty > r && tx <= r) {
+            w = fma(-sL[ty][r] * rinv[r], sa[r][tx], w);
+            sa[ty][tx] = w;
+        }
         __syncthreads();
     }
-    if (ty < nb && tx < nb) A[(int64_t)(kb + ty) * n + kb + tx] = (tx <= ty) ? sl[ty][tx] : 0.0;
+    if (ty < nb && tx < nb) A[(int64_t)(kb + ty) * n + kb + tx] = (tx <= ty) ? sL[ty][tx] : 0.0;
+    Dinv[(int64_t)k * TB * TB + ty * TB + tx] = (tx <= ty) ? w * rinv[ty] : 0.0;
 }
 
-// tiles (i, k), i > k: X L_kk^T = A_ik
-__global__ void chol_trsm_kernel(double *A, int n, int k) {
-    __shared__ double sl[TB][TB + 1], sx[TB][TB + 1];
+// 32-term dot product of rows of two shared tiles, four independent chains
+__device__ __forceinline__ double tile_dot(const double *a, int sa, const double *b, int sb) {
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+#pragma unroll
+    for (int q = 0; q < TB; q += 4) {
+        c0 = fma(a[q * sa], b[q * sb], c0);
+        c1 = fma(a[(q + 1) * sa], b[(q + 1) * sb], c1);
+        c2 = fma(a[(q + 2) * sa], b[(q + 2) * sb], c2);
+        c3 = fma(a[(q + 3) * sa], b[(q + 3) * sb], c3);
+    }
+    return (c0 + c1) + (c2 + c3);
+}
+
+// tiles (i, k), i > k: L_ik = A_ik L_kk^{-T}
+__global__ void chol_trsm_kernel(double *A, const double *Dinv, int n, int k) {
+    __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int kb = k * TB, r0 = kb + TB * (1 + blockIdx.x);
     const int nb = min(TB, n - kb);
-    load_tile(A, n, kb, kb, sl);
-    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    sz[ty][tx] = Dinv[(int64_t)k * TB * TB + ty * TB + tx];
     load_tile(A, n, r0, kb, sx);
     __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        if (tx == j) {
-            double v = sx[ty][j];
-            for (int t = 0; t < j; ++t) v -= sx[ty][t] * sl[j][t];
-            sx[ty][j] = v / sl[j][j];
-        }
-        __syncthreads();
-    }
-    if (r0 + ty < n && tx < nb) A[(int64_t)(r0 + ty) * n + kb + tx] = sx[ty][tx];
+    const double v = tile_dot(&sx[ty][0], 1, &sz[tx][0], 1);
+    if (r0 + ty < n && tx < nb) A[(int64_t)(r0 + ty) * n + kb + tx] = v;
 }
 
 __device__ __forceinline__ void lower_tile_of(int idx, int &ii, int &jj) {
@@ -112,34 +170,23 @@ __global__ void chol_syrk_kernel(double *A, int n, int k) {
     load_tile(A, n, i * TB, kb, sa);
     load_tile(A, n, j * TB, kb, sb);
     __syncthreads();
-    double acc = 0.0;
-#pragma unroll 8
-    for (int q = 0; q < TB; ++q) acc += sa[ty][q] * sb[tx][q];
+    const double acc = tile_dot(&sa[ty][0], 1, &sb[tx][0], 1);
     const int gr = i * TB + ty, gc = j * TB + tx;
     if (gr < n && gc < n) A[(int64_t)gr * n + gc] -= acc;
 }
 
-// Z = L^{-1}, right-looking over block columns of L. Step k: Z[k][c] = L_kk^{-1} Z[k][c] (c <= k),
+// Z = L^{-1}, right-looking over block rows. Step k: Z[k][c] = L_kk^{-1} Z[k][c] (c <= k),
 // then Z[i][c] -= L[i][k] Z[k][c] for i > k.
-__global__ void trinv_diag_kernel(const double *L, double *Z, int n, int k) {
-    __shared__ double sl[TB][TB + 1], sx[TB][TB + 1];
+__global__ void trinv_diag_kernel(const double *Dinv, double *Z, int n, int k) {
+    __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
     const int c = blockIdx.x;
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int r0 = k * TB, c0 = c * TB;
-    const int nb = min(TB, n - r0);
-    load_tile(L, n, r0, r0, sl);
-    if (!(ty < nb && tx < nb)) sl[ty][tx] = (ty == tx) ? 1.0 : 0.0;
+    sz[ty][tx] = Dinv[(int64_t)k * TB * TB + ty * TB + tx];
     load_tile(Z, n, r0, c0, sx);
     __syncthreads();
-    for (int r = 0; r < TB; ++r) {
-        if (ty == r) {
-            double v = sx[r][tx];
-            for (int t = 0; t < r; ++t) v -= sl[r][t] * sx[t][tx];
-            sx[r][tx] = v / sl[r][r];
-        }
-        __syncthreads();
-    }
-    if (r0 + ty < n && c0 + tx < n) Z[(int64_t)(r0 + ty) * n + c0 + tx] = sx[ty][tx];
+    const double v = tile_dot(&sz[ty][0], 1, &sx[0][tx], TB + 1);
+    if (r0 + ty < n && c0 + tx < n) Z[(int64_t)(r0 + ty) * n + c0 + tx] = v;
 }
 
 __global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
@@ -150,9 +197,7 @@ __global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
     load_tile(L, n, i * TB, k * TB, sa);
     load_tile(Z, n, k * TB, c * TB, sb);
     __syncthreads();
-    double acc = 0.0;
-#pragma unroll 8
-    for (int q = 0; q < TB; ++q) acc += sa[ty][q] * sb[q][tx];
+    const double acc = tile_dot(&sa[ty][0], 1, &sb[0][tx], TB + 1);
     const int gr = i * TB + ty, gc = c * TB + tx;
     if (gr < n && gc < n) Z[(int64_t)gr * n + gc] -= acc;
 }
@@ -360,9 +405,10 @@ __global__ void enforce_dirichlet_kernel(Geom g, T *__restrict__ u, const uint8_
 }  // namespace
 
 template <typename T>
-void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, cudaStream_t st) {
+void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, bool rows,
+                               cudaStream_t st) {
     VFEM_CUDA(cudaMemsetAsync(A, 0, sizeof(double) * (size_t)nfree * nfree, st));
-    dense_from_stencil_kernel<T><<<gridFor(g.NN * 243, BS), BS, 0, st>>>(g, S, redIdx, A, nfree);
+    dense_from_stencil_kernel<T><<<gridFor(g.NN * 243, BS), BS, 0, st>>>(g, S, redIdx, A, nfree, rows ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -371,36 +417,45 @@ void launch_symmetrize(double *A, int n, cudaStream_t st) {
     VFEM_LAUNCH_CHECK();
 }
 
-void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st) {
+void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
+                       const std::function<void(const std::string &)> &mark) {
     if (n <= 0) return;
     const dim3 tb(TB, TB);
     const int nbt = (n + TB - 1) / TB;
+    double *Dinv = work + (size_t)n * n;
     for (int k = 0; k < nbt; ++k) {
-        chol_diag_kernel<<<1, tb, 0, st>>>(A, n, k, status);
+        chol_diag_kernel<<<1, tb, 0, st>>>(A, Dinv, n, k, status);
         VFEM_LAUNCH_CHECK();
+        if (mark) mark("coarsest:chol diag tiles");
         const int m = nbt - k - 1;
         if (m > 0) {
-            chol_trsm_kernel<<<m, tb, 0, st>>>(A, n, k);
+            chol_trsm_kernel<<<m, tb, 0, st>>>(A, Dinv, n, k);
             VFEM_LAUNCH_CHECK();
+            if (mark) mark("coarsest:chol panel solves");
             chol_syrk_kernel<<<m * (m + 1) / 2, tb, 0, st>>>(A, n, k);
             VFEM_LAUNCH_CHECK();
+            if (mark) mark("coarsest:chol trailing updates");
         }
     }
     zero_upper_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(A, n);
     VFEM_LAUNCH_CHECK();
     identity_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(work, n);
     VFEM_LAUNCH_CHECK();
+    if (mark) mark("coarsest:inverse init");
     for (int k = 0; k < nbt; ++k) {
-        trinv_diag_kernel<<<k + 1, tb, 0, st>>>(A, work, n, k);
+        trinv_diag_kernel<<<k + 1, tb, 0, st>>>(Dinv, work, n, k);
         VFEM_LAUNCH_CHECK();
+        if (mark) mark("coarsest:trinv diag solves");
         const int m = nbt - k - 1;
         if (m > 0) {
             trinv_update_kernel<<<m * (k + 1), tb, 0, st>>>(A, work, n, k);
             VFEM_LAUNCH_CHECK();
+            if (mark) mark("coarsest:trinv updates");
         }
     }
     ztz_kernel<<<nbt * (nbt + 1) / 2, tb, 0, st>>>(work, A, n, nbt);
     VFEM_LAUNCH_CHECK();
+    if (mark) mark("coarsest:Z^T Z");
 }
 
 template <typename T>
@@ -467,8 +522,10 @@ void launch_enforce_dirichlet(const Geom &g, T *u, const uint8_t *dmask, const d
     VFEM_LAUNCH_CHECK();
 }
 
-template void launch_dense_from_stencil<double>(const Geom &, const double *, const int *, double *, int, cudaStream_t);
-template void launch_dense_from_stencil<float>(const Geom &, const float *, const int *, double *, int, cudaStream_t);
+template void launch_dense_from_stencil<double>(const Geom &, const double *, const int *, double *, int, bool,
+                                               cudaStream_t);
+template void launch_dense_from_stencil<float>(const Geom &, const float *, const int *, double *, int, bool,
+                                              cudaStream_t);
 template void launch_coarse_solve<double>(const Geom &, const double *, const int *, int, const double *, double *,
                                           double *, cudaStream_t);
 template void launch_coarse_solve<float>(const Geom &, const double *, const int *, int, const float *, float *,

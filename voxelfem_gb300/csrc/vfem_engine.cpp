@@ -2,6 +2,8 @@
 // topology-optimisation problem. See vfem_engine.hpp.
 #include "vfem_engine.hpp"
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cstring>
 
@@ -140,8 +142,8 @@ void Grid::youngDF(const float **hi, const float **lo) {
 const float *Grid::youngF() {
     if (!YfValid) {
         Yf.alloc(g.NE);
-        const bool masking = maskH < bmax[BUILD_DIR];
-        launch_young_moduli<float>(g, rho.p, Yf.p, E0, Emin, gamma, q, law, masking, stream);
+        // the FP32 moduli are the rounded FP64 ones
+        launch_cast<float, double>(Y.p, Yf.p, g.NE, stream);
         YfValid = true;
     }
     return Yf.p;
@@ -310,6 +312,9 @@ void Grid::elementEnergy(const double *u, double *out) {
 // ---------------------------------------------------------------------------
 MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     if (coarsenings < 0) throw Error(ERR_ARG, "numCoarseningLevels must be >= 0");
+    // Stencil layout switch-over (node count up to which a level keeps node-contiguous rows);
+    // VFEM_STENCIL_ROWS_MAX_NODES overrides it, e.g. 0 puts every assembled level in planes.
+    if (const char *env = std::getenv("VFEM_STENCIL_ROWS_MAX_NODES")) rowsMaxNodes = std::atoll(env);
     lv.resize(coarsenings + 1);
     lv[0].g = fine->g;
     for (int d = 0; d < 3; ++d) lv[0].h[d] = fine->h[d];
@@ -426,7 +431,7 @@ void MG::setupCoarsestIndex() {
         nfree = nf;
         freeIdx.alloc(std::max(nf, 1));
         Ainv.alloc(std::max<size_t>((size_t)nf * nf, 1));
-        work.alloc(std::max<size_t>((size_t)nf * nf, 1));
+        work.alloc(std::max<size_t>(dense_inverse_work_size(nf), 1));
         cscratch.alloc(std::max(nf, 1));
         status.alloc(1);
     }
@@ -482,6 +487,7 @@ struct Tr<double> {
     static const double *Y(Grid &g) { return g.Y.p; }
     static const Mat24<double> &K0(Grid &g) { return g.K0; }
     static DevBuf<double> &Kc(MG &m) { return m.Kc64; }
+    static DevBuf<double> &K2(MG &m) { return m.K2_64; }
     static DevBuf<double> &phis(MG &m) { return m.phis64; }
 };
 template <>
@@ -489,6 +495,7 @@ struct Tr<float> {
     static const float *Y(Grid &g) { return g.youngF(); }
     static const Mat24<float> &K0(Grid &g) { return g.K0f; }
     static DevBuf<float> &Kc(MG &m) { return m.Kc32; }
+    static DevBuf<float> &K2(MG &m) { return m.K2_32; }
     static DevBuf<float> &phis(MG &m) { return m.phis32; }
 };
 
@@ -512,44 +519,66 @@ void MG::updateStiffnessT() {
     for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[fi], fine->K0.a, &Kc[fi * 576]);
     uploadConst(Tr<T>::Kc(*this), Kc.data(), Kc.size());
     uploadConst(Tr<T>::phis(*this), &phis[0][0], 512);
+    if (L() > 2) {
+        // K2[8c + fi] = Phi_c^T Kc[fi] Phi_c: the fine element at position fi of level-1 child c
+        std::vector<double> K2(64 * 576, 0.0);
+        for (int c = 0; c < 8; ++c)
+            for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[c], &Kc[fi * 576], &K2[(8 * c + fi) * 576]);
+        uploadConst(Tr<T>::K2(*this), K2.data(), K2.size());
+    }
     const T *Y0 = Tr<T>::Y(*fine);
+    auto mark = [&](const std::string &name) {
+        if (!stiffMarks) return;
+        cudaEvent_t e;
+        VFEM_CUDA(cudaEventCreate(&e));
+        VFEM_CUDA(cudaEventRecord(e, st));
+        stiffMarks->emplace_back(name, e);
+    };
+    mark("start");
     if (L() == 1) {
         // direct solve on the fine grid: Ke = Y K0 (TensorProductSimulator.hh:1198-1230)
         auto &D = lv[0].data<T>();
         D.Ke.alloc((size_t)lv[0].g.NE * 576);
-        D.S.alloc((size_t)243 * lv[0].g.NN);
+        lv[0].rows = lv[0].g.NN <= rowsMaxNodes;
+        D.S.alloc((size_t)(lv[0].rows ? 256 : 243) * lv[0].g.NN);
         std::vector<double> k0(fine->K0.a, fine->K0.a + 576);
         DevBuf<T> K0d;
         uploadConst(K0d, k0.data(), 576);
         launch_ke_scaled<T>(lv[0].g, Y0, K0d.p, D.Ke.p, st);
-        launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, st);
+        launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, lv[0].rows, st);
         VFEM_CUDA(cudaStreamSynchronize(st));
     } else {
         for (int l = 1; l < L(); ++l) {
             auto &D = lv[l].data<T>();
-            D.S.alloc((size_t)243 * lv[l].g.NN);
+            lv[l].rows = lv[l].g.NN <= rowsMaxNodes;
+            D.S.alloc((size_t)(lv[l].rows ? 256 : 243) * lv[l].g.NN);
             if (l == 1) {
-                // the level-1 stencil comes straight from the fine moduli; its element matrices
-                // are only needed as the input of the next coarsening
-                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, st);
-                if (L() > 2) {
-                    D.Ke.alloc((size_t)lv[l].g.NE * 576);
-                    launch_ke_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Ke.p, st);
-                }
+                // the level-1 stencil comes straight from the fine moduli; no level-1 element
+                // matrices are stored
+                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, st);
+                mark("galerkin:L1 stencil");
             } else {
                 D.Ke.alloc((size_t)lv[l].g.NE * 576);
-                launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p, st);
-                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, st);
+                if (l == 2)
+                    launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, st);
+                else
+                    launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p,
+                                         st);
+                mark("galerkin:L" + std::to_string(l) + " element matrices");
+                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, st);
+                mark("galerkin:L" + std::to_string(l) + " stencil");
             }
         }
     }
     // dense reduced coarsest operator, FP64 inverse
     const Level &C = lv.back();
     if (nfree > 0) {
-        launch_dense_from_stencil<T>(C.g, lv.back().data<T>().S.p, redIdx.p, Ainv.p, nfree, st);
+        launch_dense_from_stencil<T>(C.g, lv.back().data<T>().S.p, redIdx.p, Ainv.p, nfree, lv.back().rows, st);
         launch_symmetrize(Ainv.p, nfree, st);
         VFEM_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
-        dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st);
+        mark("coarsest:dense assembly");
+        if (stiffMarks) dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st, mark);
+        else dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st);
         int hs = 0;
         VFEM_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         VFEM_CUDA(cudaStreamSynchronize(st));
@@ -582,7 +611,7 @@ void MG::smoothT(int l, bool forward) {
     for (int c = 0; c < 8; ++c) {
         const int color = forward ? c : 7 - c;
         if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);
-        else launch_gs_stencil_color<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, color, forward, st);
+        else launch_gs_stencil_color<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, color, forward, lv[l].rows, st);
     }
 }
 
@@ -591,7 +620,13 @@ void MG::residualT(int l) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (l == 0) launch_residual_fine<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, D.r.p, Tr<T>::K0(*fine), fine->dmask.p, st);
-    else launch_stencil_residual<T>(lv[l].g, D.S.p, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, st);
+    else launch_stencil_residual<T>(lv[l].g, D.S.p, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, lv[l].rows, st);
+}
+
+int MG::tailStart() const {
+    int t = L() - 1;  // the coarsest level always ends the tail
+    while (t - 1 >= 1 && lv[t - 1].g.NN <= tailMaxNodes) --t;
+    return (t < L() - 1) ? t : L();
 }
 
 // MultigridSolver.hh:617-658
@@ -599,6 +634,24 @@ template <typename T>
 void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
+    if (std::is_same<T, float>::value && residualSystem && l >= 1 && l == tailStart()) {
+        // small levels: one CTA runs the down leg, the dense solve runs on the whole GPU,
+        // one CTA runs the up leg
+        TailParams<T> P;
+        P.nlev = L() - l;
+        if (P.nlev > MAX_TAIL_LEVELS) throw Error(ERR_ARG, "too many tail levels");
+        P.sweeps = (int)sweeps;
+        P.symmetric = symmetricGS ? 1 : 0;
+        for (int t = 0; t < P.nlev; ++t) {
+            auto &Q = lv[l + t].data<T>();
+            P.lv[t] = TailLevel<T>{lv[l + t].g, Q.S.p, Q.x.p, Q.b.p, Q.r.p, lv[l + t].dmask.p};
+        }
+        launch_tail_down<T>(P, st);
+        auto &Dc = lv.back().data<T>();
+        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+        launch_tail_up<T>(P, st);
+        return;
+    }
     if (l == L() - 1) {
         launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfree, D.b.p, D.x.p, cscratch.p, st);
         return;
@@ -703,7 +756,15 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
     const double bnorm2 = readScalar(sc.p + 7, st);
-    launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
+    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF && L() > 1) {
+        // initial residual through the double-float operator, like every later product
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+        launch_split_df(x, dhi.p, dlo.p, 3 * g.ld, st);
+        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, x, rbuf.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st, b);
+    } else {
+        launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
+    }
     launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
     double rsq = readScalar(sc.p + 5, st);
@@ -844,7 +905,7 @@ void MG::applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate) {
     if (l == 0)
         launch_applyk_fine<T>(lv[0].g, Tr<T>::Y(*fine), u, out, Tr<T>::K0(*fine), zeroInit, negate, fine->dmask.p, false,
                               nullptr, 0, st);
-    else launch_stencil_apply<T>(lv[l].g, lv[l].data<T>().S.p, u, out, zeroInit, negate, st);
+    else launch_stencil_apply<T>(lv[l].g, lv[l].data<T>().S.p, u, out, zeroInit, negate, lv[l].rows, st);
 }
 
 template <typename T>
@@ -1203,8 +1264,8 @@ double MG::kernelBytes(int which) const {
     case 3: return 4.0 * (9 * nn + ne);
     case 4: return 8.0 * (9 * nn + ne);
     case 5: return 4.0 * (9 * nn + ne);
-    case 6: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 243 * n1); }
-    case 7: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 243 * n1); }
+    case 6: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 256 * n1); }
+    case 7: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 256 * n1); }
     }
     return 0;
 }
@@ -1295,9 +1356,24 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
         if (!acc.count(name)) order.push_back(name);
         acc[name] += ms;
     };
-    // hierarchy rebuild
+    // hierarchy rebuild, with the step marks of updateStiffnessT
     for (int r = 0; r < reps; ++r) {
-        timed("galerkin+coarse_inverse", [&] { updateStiffness(); });
+        std::vector<std::pair<std::string, cudaEvent_t>> marks;
+        stiffMarks = &marks;
+        try {
+            timed("galerkin+coarse_inverse", [&] { updateStiffness(); });
+        } catch (...) {
+            stiffMarks = nullptr;
+            throw;
+        }
+        stiffMarks = nullptr;
+        for (size_t q = 1; q < marks.size(); ++q) {
+            float ms = 0;
+            VFEM_CUDA(cudaEventElapsedTime(&ms, marks[q - 1].second, marks[q].second));
+            if (!acc.count(marks[q].first)) order.push_back(marks[q].first);
+            acc[marks[q].first] += ms;
+        }
+        for (auto &m : marks) cudaEventDestroy(m.second);
     }
     if (precision == PREC_MIXED) {
         fine->youngF();
@@ -1318,7 +1394,8 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
             if (std::is_same<T, double>::value) launch_copy((double *)D0.b.p, rbuf.p, n3, st);
             else launch_cast<float, double>(rbuf.p, (float *)D0.b.p, n3, st);
         });
-        for (int l = 0; l < L() - 1; ++l) {
+        const int ts = std::is_same<T, float>::value ? std::min(tailStart(), L() - 1) : L() - 1;
+        for (int l = 0; l < ts; ++l) {
             auto &D = lv[l].data<T>();
             auto &Dc = lv[l + 1].data<T>();
             const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
@@ -1333,13 +1410,16 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
                 launch_masked_zero<T>(lv[l + 1].g, Dc.x.p, MARGIN, st);
             });
         }
-        {
+        if (ts < L() - 1) {
+            timed("tail:L" + std::to_string(ts) + "..coarsest (down, dense solve, up)",
+                  [&] { vcycleT<T>(ts, sweeps, true); });
+        } else {
             auto &Dc = lv.back().data<T>();
             timed("coarsest:solve", [&] {
                 launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
             });
         }
-        for (int l = L() - 2; l >= 0; --l) {
+        for (int l = ts - 1; l >= 0; --l) {
             auto &D = lv[l].data<T>();
             auto &Dc = lv[l + 1].data<T>();
             const std::string tagl = "L" + std::to_string(l) + ":";

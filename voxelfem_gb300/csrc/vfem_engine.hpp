@@ -100,6 +100,7 @@ struct LevelData {
 struct Level {
     Geom g;
     double h[3];
+    bool rows = true;  // stencil layout: node-contiguous rows (small levels) or planes (large)
     std::vector<uint8_t> dmask_h;
     DevBuf<uint8_t> dmask;
     LevelData<double> d64;
@@ -134,6 +135,13 @@ public:
     int outerMatvec = MATVEC_DF;
     bool symmetricGS = true;
     bool useGraphs = true;
+    // Levels from tailStart to the coarsest run in the single-CTA tail kernels (FP32 V-cycle only;
+    // L() when no level is small enough).
+    int tailStart() const;
+    int64_t tailMaxNodes = 0;
+    int64_t rowsMaxNodes = 200000;  // levels up to this size store node-contiguous stencil rows
+    // When set, the stiffness update records a CUDA event after each of its steps (profiling).
+    std::vector<std::pair<std::string, cudaEvent_t>> *stiffMarks = nullptr;
 
     int L() const { return (int)lv.size(); }
     void setPrecision(int p);
@@ -181,8 +189,8 @@ public:
     int partialCount = 0;
 
     // Galerkin constants
-    DevBuf<double> Kc64, phis64;
-    DevBuf<float> Kc32, phis32;
+    DevBuf<double> Kc64, K2_64, phis64;
+    DevBuf<float> Kc32, K2_32, phis32;
 
     // CUDA graphs of one preconditioned CG iteration, keyed by solver options
     struct GraphKey {

@@ -1,6 +1,9 @@
 // Launchers for the VoxelFEM GB300 kernels (sm_103a). All nodal vectors are SoA with
 // component stride Geom::ld; element fields are flat row-major (x slowest, z fastest).
 #pragma once
+#include <functional>
+#include <string>
+
 #include "vfem_common.cuh"
 
 namespace vfem {
@@ -41,9 +44,10 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
                           const Mat24<T> &K0, cudaStream_t st);
 // FP64-accurate matvec in double-float arithmetic: out = K u with u = uh + ul and Y = Yh + Yl
 // given as float pairs; out (and the partial dots u.out) in FP64.
+// With rhs given, out = rhs - K u with constrained components zeroed (residual form).
 void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, const float *uh, const float *ul,
                            const double *u, double *out, const Mat24DF &K0, const uint8_t *dmask, bool zeroDirichlet,
-                           double *partialDot, int partialBlocks, cudaStream_t st);
+                           double *partialDot, int partialBlocks, cudaStream_t st, const double *rhs = nullptr);
 // hi = fl(v), lo = fl(v - hi)
 void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStream_t st);
 
@@ -56,14 +60,17 @@ void launch_build_gravity_load(const Geom &g, const double *rho, double *f, cons
                                cudaStream_t st);
 
 // ---------------- coarse levels (k_coarse.cu) ----------------
+// Stencil kernels take the level's layout: rows (node-contiguous, 256 entries per node, one
+// warp per node) or planes (243 planes of NN, one thread per node).
 template <typename T>
-void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, cudaStream_t st);
+void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
+                          cudaStream_t st);
 template <typename T>
-void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask,
+void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st);
 template <typename T>
 void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
-                             cudaStream_t st);
+                             bool rows, cudaStream_t st);
 template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st);
 template <typename T>
@@ -79,22 +86,51 @@ template <typename T>
 void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc /*8*576*/, T *Ke1, cudaStream_t st);
 // Level-1 stencil assembled directly from the fine Young's moduli (no element matrices).
 template <typename T>
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, cudaStream_t st);
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st);
+// Level-2 element matrices from the fine moduli and the 64 folded constant matrices K2.
+template <typename T>
+void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st);
 template <typename T>
 void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis /*8*64*/, T *Kec, cudaStream_t st);
 template <typename T>
 void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_t st);
 template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, cudaStream_t st);
+void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st);
 template <typename Tdst, typename Tsrc>
 void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st);
 
+// ---------------- single-CTA coarse tail of the V-cycle (k_tail.cu) ----------------
+constexpr int MAX_TAIL_LEVELS = 8;
+template <typename T>
+struct TailLevel {
+    Geom g;
+    const T *S;
+    T *x, *b, *r;
+    const uint8_t *dmask;
+};
+template <typename T>
+struct TailParams {
+    int nlev;  // tail levels including the coarsest (solved between the two launches)
+    int sweeps;
+    int symmetric;
+    TailLevel<T> lv[MAX_TAIL_LEVELS];
+};
+template <typename T>
+void launch_tail_down(const TailParams<T> &P, cudaStream_t st);
+template <typename T>
+void launch_tail_up(const TailParams<T> &P, cudaStream_t st);
+
 // ---------------- dense coarsest solve + vector ops (k_linalg.cu) ----------------
 template <typename T>
-void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, cudaStream_t st);
+void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, bool rows,
+                               cudaStream_t st);
 void launch_symmetrize(double *A, int n, cudaStream_t st);
 // In place: A (n x n, row-major) -> A^{-1} via blocked Cholesky; status[0] set nonzero if not SPD.
-void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st);
+// work holds dense_inverse_work_size(n) doubles.
+// mark(name), when given, is called after each phase has been enqueued (profiling).
+inline size_t dense_inverse_work_size(int n) { return (size_t)n * n + (size_t)32 * 32 * ((n + 31) / 32); }
+void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
+                       const std::function<void(const std::string &)> &mark = nullptr);
 template <typename T>
 void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, int nfree, const T *b, T *x,
                          double *scratch, cudaStream_t st);

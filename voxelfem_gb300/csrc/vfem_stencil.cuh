@@ -1,0 +1,338 @@
+// Device building blocks of the assembled 27-point block-stencil levels, shared by the
+// per-colour kernels (k_coarse.cu) and the coarse-tail kernels (k_tail.cu).
+#pragma once
+#include "vfem_common.cuh"
+
+namespace vfem {
+namespace stencil {
+
+__device__ __forceinline__ void decode(const int64_t n, const int nn1, const int nn2, int &i, int &j, int &k) {
+    k = (int)(n % nn2);
+    const int64_t t = n / nn2;
+    j = (int)(t % nn1);
+    i = (int)(t / nn1);
+}
+
+// Assembled stencil rows are stored node-contiguous: the 27 blocks of node n occupy
+// S[n * ROW + e], e = o*9 + 3r + c (o = (ox+1)*9 + (oy+1)*3 + (oz+1)), padded to ROW = 256
+// entries (1 KB in FP32) so every row starts 16-byte aligned. One warp handles one row:
+// lane l owns entries [8l, 8l+8) and a warp reduction sums the three row components, so a
+// node costs one coalesced 1 KB read and a single memory round trip.
+constexpr int ROW = 256;
+constexpr int ROW_USED = 243;
+
+__device__ __forceinline__ int64_t neighbour(const Geom &g, int64_t n, int i, int j, int k, int o) {
+    // out-of-grid neighbours are clamped onto the node itself; their blocks are exactly zero
+    // (no element contains both nodes), so they add nothing
+    const int ox = o / 9 - 1, oy = (o / 3) % 3 - 1, oz = o % 3 - 1;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    int64_t m = n;
+    if ((ox < 0 && i > 0) || (ox > 0 && i + 1 < g.nn[0])) m += ox * sx;
+    if ((oy < 0 && j > 0) || (oy > 0 && j + 1 < g.nn[1])) m += oy * sy;
+    if ((oz < 0 && k > 0) || (oz > 0 && k + 1 < g.nn[2])) m += oz;
+    return m;
+}
+
+template <typename T>
+struct RowVec;
+template <>
+struct RowVec<float> {
+    static __device__ __forceinline__ void load(const float *p, float *v) {
+        const float4 a = reinterpret_cast<const float4 *>(p)[0];
+        const float4 b = reinterpret_cast<const float4 *>(p)[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
+};
+template <>
+struct RowVec<double> {
+    static __device__ __forceinline__ void load(const double *p, double *v) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double2 a = reinterpret_cast<const double2 *>(p)[q];
+            v[2 * q] = a.x;
+            v[2 * q + 1] = a.y;
+        }
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_reduce(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Lane-partial products of row n with u; v receives the lane's 8 row entries. After the
+// call every lane holds the full sums (butterfly reduction).
+template <typename T>
+__device__ __forceinline__ void row_times_u(const Geom &g, const T *__restrict__ S, const T *__restrict__ u, int64_t n,
+                                            int i, int j, int k, int lane, T *v, T &f0, T &f1, T &f2) {
+    RowVec<T>::load(S + n * ROW + lane * 8, v);
+    const int64_t ld = g.ld;
+    T p0 = T(0), p1 = T(0), p2 = T(0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int e = lane * 8 + q;
+        if (e < ROW_USED) {
+            const int o = e / 9, rc = e % 9, r = rc / 3;
+            const int64_t m = neighbour(g, n, i, j, k, o);
+            const T prod = v[q] * u[(rc % 3) * ld + m];
+            p0 += (r == 0) ? prod : T(0);
+            p1 += (r == 1) ? prod : T(0);
+            p2 += (r == 2) ? prod : T(0);
+        }
+    }
+    f0 = warp_reduce(p0);
+    f1 = warp_reduce(p1);
+    f2 = warp_reduce(p2);
+}
+
+template <typename T>
+__device__ __forceinline__ void node_solve(uint8_t dm, T s0, T s1, T s2, const T *M, bool forward, T &u0, T &u1,
+                                           T &u2) {
+    if (dm) {
+        T d[3] = {T(0), T(0), T(0)};
+        const T bs[3] = {s0, s1, s2};
+        if (forward) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
+                       (T(!((dm >> q) & 1)) / M[4 * q]);
+        } else {
+#pragma unroll
+            for (int q = 2; q >= 0; --q)
+                d[q] = (bs[q] - (M[3 * q] * d[0] + M[3 * q + 1] * d[1] + M[3 * q + 2] * d[2])) *
+                       (T(!((dm >> q) & 1)) / M[4 * q]);
+        }
+        u0 += d[0];
+        u1 += d[1];
+        u2 += d[2];
+    } else {
+        const T c00 = M[4] * M[8] - M[5] * M[7];
+        const T c01 = M[5] * M[6] - M[3] * M[8];
+        const T c02 = M[3] * M[7] - M[4] * M[6];
+        const T det = M[0] * c00 + M[1] * c01 + M[2] * c02;
+        const T id = T(1) / det;
+        const T i00 = c00 * id, i01 = (M[2] * M[7] - M[1] * M[8]) * id, i02 = (M[1] * M[5] - M[2] * M[4]) * id;
+        const T i10 = c01 * id, i11 = (M[0] * M[8] - M[2] * M[6]) * id, i12 = (M[2] * M[3] - M[0] * M[5]) * id;
+        const T i20 = c02 * id, i21 = (M[1] * M[6] - M[0] * M[7]) * id, i22 = (M[0] * M[4] - M[1] * M[3]) * id;
+        u0 += i00 * s0 + i01 * s1 + i02 * s2;
+        u1 += i10 * s0 + i11 * s1 + i12 * s2;
+        u2 += i20 * s0 + i21 * s1 + i22 * s2;
+    }
+}
+
+
+// Block Gauss-Seidel update of node (i, j, k) by one warp (MultigridSolver.hh:323-378).
+template <typename T>
+__device__ __forceinline__ void gs_node_warp(const Geom &g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+                                             const uint8_t *__restrict__ dmask, int i, int j, int k, bool forward,
+                                             int lane) {
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;  // warp-uniform
+    T v[8], f0, f1, f2;
+    row_times_u<T>(g, S, u, n, i, j, k, lane, v, f0, f1, f2);
+    // diagonal block entries 117..125 live in lanes 14 and 15
+    T M[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) M[q] = __shfl_sync(0xffffffffu, v[(117 + q) % 8], (117 + q) / 8);
+    if (lane == 0) {
+        T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+        node_solve<T>(dm, b[n] - f0, b[ld + n] - f1, b[2 * ld + n] - f2, M, forward, u0, u1, u2);
+        u[n] = u0;
+        u[ld + n] = u1;
+        u[2 * ld + n] = u2;
+    }
+}
+
+// r = b - S u on nondetached rows, r = b elsewhere; Dirichlet components zeroed (one warp).
+template <typename T>
+__device__ __forceinline__ void residual_node_warp(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+                                                   const T *__restrict__ b, T *__restrict__ r,
+                                                   const uint8_t *__restrict__ dmask, int64_t n, int i, int j, int k,
+                                                   int lane) {
+    const int64_t ld = g.ld;
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    if (j < g.nyv()) {
+        T v[8];
+        row_times_u<T>(g, S, u, n, i, j, k, lane, v, f0, f1, f2);
+    }
+    if (lane == 0) {
+        const uint8_t dm = dmask[n];
+        r[n] = (dm & 1) ? T(0) : b[n] - f0;
+        r[ld + n] = (dm & 2) ? T(0) : b[ld + n] - f1;
+        r[2 * ld + n] = (dm & 4) ? T(0) : b[2 * ld + n] - f2;
+    }
+}
+
+
+// ---- plane layout (large levels): S[(o*9 + 3r + c) * ld + p], one thread per node ----
+// p is the node's colour-ordered position: nodes grouped by colour (i&1, j&1, k&1), colours in
+// ascending order 4cx+2cy+cz, each colour's nodes in lexicographic (i>>1, j>>1, k>>1) order.
+// A Gauss-Seidel colour pass then streams a contiguous slice of every plane.
+__device__ __forceinline__ int half_count(int nn, int b) { return (nn + 1 - b) >> 1; }
+
+__device__ __forceinline__ int64_t colour_pos(const Geom &g, int i, int j, int k) {
+    const int cx = i & 1, cy = j & 1, cz = k & 1;
+    const int c1 = half_count(g.nn[1], cy), c2 = half_count(g.nn[2], cz);
+    const int64_t off = (cx ? (int64_t)half_count(g.nn[0], 0) * g.nn[1] * g.nn[2] : 0) +
+                        (int64_t)half_count(g.nn[0], cx) *
+                            ((cy ? (int64_t)half_count(g.nn[1], 0) * g.nn[2] : 0) + (int64_t)c1 * (cz ? half_count(g.nn[2], 0) : 0));
+    return off + ((int64_t)(i >> 1) * c1 + (j >> 1)) * c2 + (k >> 1);
+}
+
+__device__ __forceinline__ void colour_node(const Geom &g, int64_t p, int &i, int &j, int &k) {
+    const int64_t A = (int64_t)half_count(g.nn[0], 0) * g.nn[1] * g.nn[2];
+    const int cx = p >= A;
+    if (cx) p -= A;
+    const int64_t B = (int64_t)half_count(g.nn[0], cx) * half_count(g.nn[1], 0) * g.nn[2];
+    const int cy = p >= B;
+    if (cy) p -= B;
+    const int c1 = half_count(g.nn[1], cy);
+    const int64_t C = (int64_t)half_count(g.nn[0], cx) * c1 * half_count(g.nn[2], 0);
+    const int cz = p >= C;
+    if (cz) p -= C;
+    const int c2 = half_count(g.nn[2], cz);
+    const int kk = (int)(p % c2);
+    const int64_t q = p / c2;
+    i = 2 * (int)(q / c1) + cx;
+    j = 2 * (int)(q % c1) + cy;
+    k = 2 * kk + cz;
+}
+
+// The 27 blocks are consumed in three batches of nine; each batch issues its 27 u loads and
+// 81 stencil loads before any arithmetic, so a thread waits on three memory round trips
+// instead of twenty-seven.
+template <typename T, bool Negate>
+__device__ __forceinline__ void stencil_row_soa(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+                                                int64_t n, int64_t p, int i, int j, int k, T &f0, T &f1, T &f2) {
+    const int64_t ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    const int64_t dx[3] = {i > 0 ? -sx : 0, 0, i + 1 < g.nn[0] ? sx : 0};
+    const int64_t dy[3] = {j > 0 ? -sy : 0, 0, j + 1 < g.nn[1] ? sy : 0};
+    const int64_t dz[3] = {k > 0 ? -1 : 0, 0, k + 1 < g.nn[2] ? 1 : 0};
+#pragma unroll
+    for (int bx = 0; bx < 3; ++bx) {
+        T uu[9][3], ss[9][9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const int64_t m = n + dx[bx] + dy[t / 3] + dz[t % 3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) uu[t][c] = u[c * ld + m];
+            const T *blk = S + (int64_t)((bx * 9 + t) * 9) * ld + p;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) ss[t][e] = blk[e * ld];
+        }
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const T v0 = ss[t][0] * uu[t][0] + ss[t][1] * uu[t][1] + ss[t][2] * uu[t][2];
+            const T v1 = ss[t][3] * uu[t][0] + ss[t][4] * uu[t][1] + ss[t][5] * uu[t][2];
+            const T v2 = ss[t][6] * uu[t][0] + ss[t][7] * uu[t][1] + ss[t][8] * uu[t][2];
+            if (Negate) { f0 -= v0; f1 -= v1; f2 -= v2; }
+            else        { f0 += v0; f1 += v1; f2 += v2; }
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void gs_node_soa(const Geom &g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+                                            const uint8_t *__restrict__ dmask, int i, int j, int k, int64_t p,
+                                            bool forward) {
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    stencil_row_soa<T, true>(g, S, u, n, p, i, j, k, s0, s1, s2);
+    T M[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
+    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    node_solve<T>(dm, s0, s1, s2, M, forward, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
+template <typename T>
+__device__ __forceinline__ void residual_node_soa(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+                                                  const T *__restrict__ b, T *__restrict__ r,
+                                                  const uint8_t *__restrict__ dmask, int64_t n, int64_t p, int i, int j,
+                                                  int k) {
+    const int64_t ld = g.ld;
+    T f0 = b[n], f1 = b[ld + n], f2 = b[2 * ld + n];
+    if (j < g.nyv()) stencil_row_soa<T, true>(g, S, u, n, p, i, j, k, f0, f1, f2);
+    const uint8_t dm = dmask[n];
+    r[n] = (dm & 1) ? T(0) : f0;
+    r[ld + n] = (dm & 2) ? T(0) : f1;
+    r[2 * ld + n] = (dm & 4) ? T(0) : f2;
+}
+
+// Full-weighting restriction onto coarse node (i, j, k) (MultigridSolver.hh:217-275); rows at or
+// above the coarse nondetached height get zero.
+template <typename T>
+__device__ __forceinline__ void restrict_node(const Geom &gf, const Geom &gc, const T *__restrict__ fine,
+                                              T *__restrict__ coarse, int i, int j, int k) {
+    const int64_t cn = gc.node(i, j, k);
+    T v0 = T(0), v1 = T(0), v2 = T(0);
+    if (j < gc.nyv()) {
+        const int fyv = gf.nyv();
+        const int lo0 = max(2 * i - 1, 0), lo1 = max(2 * j - 1, 0), lo2 = max(2 * k - 1, 0);
+        const int hi0 = min(2 * i + 2, gf.nn[0]), hi1 = min(2 * j + 2, fyv), hi2 = min(2 * k + 2, gf.nn[2]);
+        const int64_t ld = gf.ld;
+        for (int a = lo0; a < hi0; ++a) {
+            const T wa = T(1) - T(abs(a - 2 * i)) * T(0.5);
+            for (int bb = lo1; bb < hi1; ++bb) {
+                const T wb = wa * (T(1) - T(abs(bb - 2 * j)) * T(0.5));
+                for (int c = lo2; c < hi2; ++c) {
+                    const T w = wb * (T(1) - T(abs(c - 2 * k)) * T(0.5));
+                    const int64_t fn = gf.node(a, bb, c);
+                    v0 += w * fine[fn];
+                    v1 += w * fine[ld + fn];
+                    v2 += w * fine[2 * ld + fn];
+                }
+            }
+        }
+    }
+    coarse[cn] = v0;
+    coarse[gc.ld + cn] = v1;
+    coarse[2 * gc.ld + cn] = v2;
+}
+
+// Trilinear prolongation into fine node f (MultigridSolver.hh:163-212).
+template <typename T, bool Accumulate>
+__device__ __forceinline__ void interp_node(const Geom &gf, const Geom &gc, const T *__restrict__ coarse,
+                                            T *__restrict__ fine, const int f[3]) {
+    int ec[3], lf[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        ec[d] = min(f[d] / 2, gc.ne[d]);
+        lf[d] = f[d] - 2 * ec[d];
+    }
+    const int64_t fn = gf.node(f[0], f[1], f[2]);
+    const int64_t fld = gf.ld, cld = gc.ld;
+    T a0 = Accumulate ? fine[fn] : T(0), a1 = Accumulate ? fine[fld + fn] : T(0),
+      a2 = Accumulate ? fine[2 * fld + fn] : T(0);
+#pragma unroll
+    for (int cnl = 0; cnl < 8; ++cnl) {
+        const int cb[3] = {(cnl >> 2) & 1, (cnl >> 1) & 1, cnl & 1};
+        T coeff = T(1);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T phi = (lf[d] == 1) ? T(0.5) : ((lf[d] == 0) ? (cb[d] ? T(0) : T(1)) : (cb[d] ? T(1) : T(0)));
+            coeff *= phi;
+        }
+        if (coeff == T(0)) continue;
+        const int64_t cidx = gc.node(ec[0] + cb[0], ec[1] + cb[1], ec[2] + cb[2]);
+        a0 += coeff * coarse[cidx];
+        a1 += coeff * coarse[cld + cidx];
+        a2 += coeff * coarse[2 * cld + cidx];
+    }
+    fine[fn] = a0;
+    fine[fld + fn] = a1;
+    fine[2 * fld + fn] = a2;
+}
+
+}  // namespace stencil
+}  // namespace vfem
