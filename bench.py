@@ -46,7 +46,7 @@ FP64_ITERATIONS = {"c2": 16, "c1": 10}
 TOL = 1e-8
 KERNEL_NAMES = {0: "applyk_fine_fp64", 1: "applyk_fine_fp32", 2: "applyk_fine_df", 3: "gs_fine_sweep_fp32",
                 4: "gs_fine_sweep_fp64", 5: "residual_fine_fp32", 6: "gs_level1_sweep_fp32",
-                7: "residual_level1_fp32"}
+                7: "residual_level1_fp32", 8: "gs_level2_sweep_fp32", 9: "residual_level2_fp32"}
 
 
 def peaks():
@@ -312,7 +312,7 @@ def run_ours(args):
     # ---------------- hot kernels: device time per launch (CUDA events on the solver stream) ----------------
     hbm, peak_kind = peaks()
     kernels = {}
-    for kid in (1, 2, 0, 3, 5, 6, 7):
+    for kid in (1, 2, 0, 3, 5, 6, 7, 8, 9):
         ms = C.c_double()
         nbytes = C.c_double()
         reps = 3 if kid == 0 else 20
@@ -325,6 +325,8 @@ def run_ours(args):
         "applyk_fine_df": kernels["applyk_fine_df"]["ms"],
         "residual_fine_fp32": kernels["residual_fine_fp32"]["ms"],
         "gs_level1_sweep_fp32": 4 * kernels["gs_level1_sweep_fp32"]["ms"],
+        "residual_level1_fp32": kernels["residual_level1_fp32"]["ms"],
+        "gs_level2_sweep_fp32": 4 * kernels["gs_level2_sweep_fp32"]["ms"],
     }
     dom = max(per_iter, key=per_iter.get)
     traffic = None

@@ -71,6 +71,9 @@ int vfem_grid_set_etensor(vfem_grid *g, double young, double poisson);
 int vfem_grid_get_etensor(const vfem_grid *g, double *young, double *poisson);
 /* fullDensityElementStiffnessMatrix (TensorProductSimulator.hh:658), 24x24 row-major */
 int vfem_grid_get_k0(const vfem_grid *g, double *out576);
+/* Diagnostic (no reference counterpart): *cube = 1 when K0 has the equal-edge (cube) structure the
+ * fine-level FP32 and double-float kernels exploit (10 distinct entries up to sign), else 0. */
+int vfem_grid_k0_is_cube(const vfem_grid *g, int *cube);
 /* E_0, E_min, gamma, q, interpolationLaw properties (VoxelFEM.cc:116-121, TensorProductSimulator.hh:160-164) */
 int vfem_grid_set_material_params(vfem_grid *g, double E0, double Emin, double gamma, double q, int law);
 int vfem_grid_get_material_params(const vfem_grid *g, double *E0, double *Emin, double *gamma, double *q, int *law);
@@ -150,8 +153,8 @@ int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter,
 /* Benchmark hooks (no reference counterpart): the CUDA stream the solver launches on, the
  * average device time of one launch of a hot kernel (ids in vfem_mg_time_kernel's comment
  * in vfem_engine.cpp: 0 fine applyK FP64, 1 fine applyK FP32, 2 fine applyK double-float,
- * 3/4 fine GS sweep FP32/FP64, 5 fine residual FP32, 6 level-1 GS sweep FP32,
- * 7 level-1 residual FP32) with its algorithmic bytes, and a counter of the library's
+ * 3/4 fine GS sweep FP32/FP64, 5 fine residual FP32, 6/7 level-1 GS sweep / residual FP32,
+ * 8/9 level-2 GS sweep / residual FP32) with its algorithmic bytes, and a counter of the library's
  * kernel launches (graph replays included). */
 int vfem_mg_get_stream(const vfem_mg *mg, void **stream);
 int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *bytes);

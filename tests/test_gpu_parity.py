@@ -20,10 +20,11 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-def make_pair(oracle, ne, rho_lo=0.3, seed=0, levels=None, mask_layer=None):
-    bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
+def make_pair(oracle, ne, rho_lo=0.3, seed=0, levels=None, mask_layer=None, bbox=None):
+    if bbox is None:
+        bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
     g = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
-    o = oracle.Sim(ne)
+    o = oracle.Sim(ne, bbox)
     wl.setup_cantilever(g, ne, rho_lo, seed)
     wl.setup_cantilever(o, ne, rho_lo, seed)
     if mask_layer is not None:
@@ -42,6 +43,7 @@ def make_pair(oracle, ne, rho_lo=0.3, seed=0, levels=None, mask_layer=None):
 @pytest.mark.parametrize("ne", [(4, 2, 2), (6, 5, 3), (16, 8, 8)])
 def test_applyk_fine(gpu, oracle, ne):
     g, o = make_pair(oracle, ne)
+    assert g.k0IsCube()  # unit-cube voxels: the fine FP32 kernels hold K0 as 10 class values
     np.testing.assert_array_equal(g.fullDensityElementStiffnessMatrix().shape, (24, 24))
     assert rel(g.fullDensityElementStiffnessMatrix(), o.K0()) < 1e-14
     assert rel(g.getYoungModulusScaleFactor(), o.youngModuli()) < 1e-15
@@ -165,6 +167,30 @@ def test_pcg_mixed_precision(gpu, oracle, stencil_layout):
         cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
         assert abs(cg - co) / abs(co) < 1e-6
     gm.setPrecision("fp64")
+
+
+def test_pcg_mixed_precision_stretched_voxels(gpu, oracle):
+    """Unequal element edges: K0 lacks the cube structure and the fine FP32 / double-float
+    kernels read the full 24 x 24 table."""
+    ne = (16, 8, 8)
+    bbox = [[0.0, 0.0, 0.0], [16.0, 4.0, 12.0]]
+    g, o, gm, om = make_pair(oracle, ne, levels=3, bbox=bbox)
+    assert not g.k0IsCube()
+    assert rel(g.fullDensityElementStiffnessMatrix(), o.K0()) < 1e-14
+    b = g.buildLoadVector()
+    x0 = np.zeros_like(b)
+    xo = om.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    gm.setPrecision("mixed", "df")
+    xg = gm.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    r = b - g.applyK(xg)
+    r[g.getDirichletMask()] = 0
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-8
+    cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
+    assert abs(cg - co) / abs(co) < 1e-6
+    gm.setPrecision("fp64")
+    xg = gm.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    assert gm.lastStats.iterations == om.lastIterations
+    assert rel(xg, xo) < 1e-8
 
 
 @pytest.mark.parametrize("radius,ftype", [(1, 0), (2, 1), (3, 1)])

@@ -38,6 +38,7 @@ _SIGS = {
     "vfem_grid_set_etensor": (C.c_int, [_vp, C.c_double, C.c_double]),
     "vfem_grid_get_etensor": (C.c_int, [_vp, _d, _d]),
     "vfem_grid_get_k0": (C.c_int, [_vp, _d]),
+    "vfem_grid_k0_is_cube": (C.c_int, [_vp, _i32]),
     "vfem_grid_set_material_params": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),
     "vfem_grid_get_material_params": (C.c_int, [_vp, _d, _d, _d, _d, _i32]),
     "vfem_grid_set_densities": (C.c_int, [_vp, _vp]),

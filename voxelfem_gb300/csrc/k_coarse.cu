@@ -66,51 +66,108 @@ __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *_
     const int lane = threadIdx.x & 31;
     const int64_t t = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
-    const int kk = (int)(t % n2);
-    const int64_t q = t / n2;
-    const int jj = (int)(q % n1), ii = (int)(q / n1);
+    int ii, jj, kk;
+    decode(t, n1, n2, ii, jj, kk);
     stencil::gs_node_warp<T>(g, S, u, b, dmask, cx + 2 * ii, cy + 2 * jj, cz + 2 * kk, forward != 0, lane);
 }
 
+// Plane-layout kernels: blocks of SPLIT_SUB warps x 32 nodes (stencil::stencil_row_part).
+// Apply / residual walk the colour-ordered positions p; a Gauss-Seidel colour pass walks the
+// nodes of one colour, whose positions are contiguous.
+using stencil::SPLIT_NODES;
+using stencil::SPLIT_SUB;
+constexpr int SPLIT_BS = SPLIT_SUB * SPLIT_NODES;
+
 template <typename T, bool ZeroInit, bool Negate>
-__global__ void __launch_bounds__(BS) stencil_apply_soa_kernel(Geom g, const T *__restrict__ S,
-                                                               const T *__restrict__ u, T *__restrict__ out) {
-    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (p >= g.NN) return;
-    int i, j, k;
-    stencil::colour_node(g, p, i, j, k);
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) stencil_apply_soa_kernel(Geom g, const T *__restrict__ S,
+                                                                     const T *__restrict__ u, T *__restrict__ out) {
+    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
+    const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
+    const bool valid = p < g.NN;
+    int i = 0, j = 0, k = 0;
+    if (valid) stencil::colour_node(g, p, i, j, k);
     const int64_t n = g.node(i, j, k), ld = g.ld;
-    T f0 = ZeroInit ? T(0) : out[n], f1 = ZeroInit ? T(0) : out[ld + n], f2 = ZeroInit ? T(0) : out[2 * ld + n];
-    stencil::stencil_row_soa<T, Negate>(g, S, u, n, p, i, j, k, f0, f1, f2);
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
+    part[0][sub][lane] = f0;
+    part[1][sub][lane] = f1;
+    part[2][sub][lane] = f2;
+    __syncthreads();
+    if (sub != 0 || !valid) return;
+    stencil::split_sum<T>(part, lane, f0, f1, f2);
+    if (Negate) { f0 = -f0; f1 = -f1; f2 = -f2; }
+    if (!ZeroInit) { f0 += out[n]; f1 += out[ld + n]; f2 += out[2 * ld + n]; }
     out[n] = f0;
     out[ld + n] = f1;
     out[2 * ld + n] = f2;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BS) stencil_residual_soa_kernel(Geom g, const T *__restrict__ S,
-                                                                  const T *__restrict__ u, const T *__restrict__ b,
-                                                                  T *__restrict__ r, const uint8_t *__restrict__ dmask) {
-    const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (p >= g.NN) return;
-    int i, j, k;
-    stencil::colour_node(g, p, i, j, k);
-    stencil::residual_node_soa<T>(g, S, u, b, r, dmask, g.node(i, j, k), p, i, j, k);
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) stencil_residual_soa_kernel(Geom g, const T *__restrict__ S,
+                                                                        const T *__restrict__ u,
+                                                                        const T *__restrict__ b, T *__restrict__ r,
+                                                                        const uint8_t *__restrict__ dmask) {
+    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
+    const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
+    const bool valid = p < g.NN;
+    int i = 0, j = 0, k = 0;
+    if (valid) stencil::colour_node(g, p, i, j, k);
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const bool active = valid && j < g.nyv();
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    if (active) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
+    part[0][sub][lane] = f0;
+    part[1][sub][lane] = f1;
+    part[2][sub][lane] = f2;
+    __syncthreads();
+    if (sub != 0 || !valid) return;
+    stencil::split_sum<T>(part, lane, f0, f1, f2);
+    const uint8_t dm = dmask[n];
+    r[n] = (dm & 1) ? T(0) : b[n] - f0;
+    r[ld + n] = (dm & 2) ? T(0) : b[ld + n] - f1;
+    r[2 * ld + n] = (dm & 4) ? T(0) : b[2 * ld + n] - f2;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BS) gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u,
-                                                                  const T *__restrict__ b,
-                                                                  const uint8_t *__restrict__ dmask, int cx, int cy,
-                                                                  int cz, int forward) {
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u,
+                                                                        const T *__restrict__ b,
+                                                                        const uint8_t *__restrict__ dmask, int cx,
+                                                                        int cy, int cz, int forward) {
+    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
-    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
-    const int kk = (int)(t % n2);
-    const int64_t q = t / n2;
-    const int jj = (int)(q % n1), ii = (int)(q / n1);
-    const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
-    stencil::gs_node_soa<T>(g, S, u, b, dmask, i, j, k, stencil::colour_pos(g, i, j, k), forward != 0);
+    const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    const int64_t t = blockIdx.x * (int64_t)SPLIT_NODES + lane;
+    const bool valid = n1 > 0 && t < (int64_t)n0 * n1 * n2;
+    int i = cx, j = cy, k = cz;
+    if (valid) {
+        int ii, jj, kk;
+        decode(t, n1, n2, ii, jj, kk);
+        i = cx + 2 * ii;
+        j = cy + 2 * jj;
+        k = cz + 2 * kk;
+    }
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const int64_t p = stencil::colour_pos(g, i, j, k);
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
+    part[0][sub][lane] = f0;
+    part[1][sub][lane] = f1;
+    part[2][sub][lane] = f2;
+    __syncthreads();
+    if (sub != 0 || !valid) return;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    stencil::split_sum<T>(part, lane, f0, f1, f2);
+    T M[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
+    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    stencil::node_solve<T>(dm, b[n] - f0, b[ld + n] - f1, b[2 * ld + n] - f2, M, forward != 0, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
 }
 
 // Full-weighting restriction (MultigridSolver.hh:217-275): coarse node gathers the
@@ -446,13 +503,13 @@ template <typename T>
 void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
                           cudaStream_t st) {
     if (!rows) {
-        const unsigned gs = gridFor(g.NN, BS);
+        const unsigned gs = gridFor(g.NN, SPLIT_NODES);
         if (zeroInit) {
-            if (negate) stencil_apply_soa_kernel<T, true, true><<<gs, BS, 0, st>>>(g, S, u, out);
-            else stencil_apply_soa_kernel<T, true, false><<<gs, BS, 0, st>>>(g, S, u, out);
+            if (negate) stencil_apply_soa_kernel<T, true, true><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
+            else stencil_apply_soa_kernel<T, true, false><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
         } else {
-            if (negate) stencil_apply_soa_kernel<T, false, true><<<gs, BS, 0, st>>>(g, S, u, out);
-            else stencil_apply_soa_kernel<T, false, false><<<gs, BS, 0, st>>>(g, S, u, out);
+            if (negate) stencil_apply_soa_kernel<T, false, true><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
+            else stencil_apply_soa_kernel<T, false, false><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
         }
         VFEM_LAUNCH_CHECK();
         return;
@@ -472,7 +529,7 @@ template <typename T>
 void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st) {
     if (rows) stencil_residual_kernel<T><<<gridFor(g.NN, WPB), BS, 0, st>>>(g, S, u, b, r, dmask);
-    else stencil_residual_soa_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, S, u, b, r, dmask);
+    else stencil_residual_soa_kernel<T><<<gridFor(g.NN, SPLIT_NODES), SPLIT_BS, 0, st>>>(g, S, u, b, r, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -486,8 +543,8 @@ void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const 
         gs_stencil_color_kernel<T><<<gridFor(n0 * n1 * n2, WPB), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
                                                                                forward ? 1 : 0);
     else
-        gs_stencil_color_soa_kernel<T><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
-                                                                                  forward ? 1 : 0);
+        gs_stencil_color_soa_kernel<T><<<gridFor(n0 * n1 * n2, SPLIT_NODES), SPLIT_BS, 0, st>>>(
+            g, S, u, b, dmask, cx, cy, cz, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -9,17 +9,26 @@
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 
+#include <type_traits>
+
 namespace vfem {
 
 namespace {
 
 constexpr int BS = 256;
 
+// 32-bit unsigned decode of a flat index into (i, j, k) for dimensions (., n1, n2): counts stay
+// below 2^31 (checked when a grid is created); 64-bit division is a long software sequence.
+__device__ __forceinline__ void decode3(int64_t n, int n1, int n2, int &i, int &j, int &k) {
+    const uint32_t u = (uint32_t)n, t = u / (uint32_t)n2;
+    k = (int)(u - t * (uint32_t)n2);
+    const uint32_t q = t / (uint32_t)n1;
+    j = (int)(t - q * (uint32_t)n1);
+    i = (int)q;
+}
+
 __device__ __forceinline__ void decode_node(const Geom &g, int64_t n, int &i, int &j, int &k) {
-    k = (int)(n % g.nn[2]);
-    const int64_t t = n / g.nn[2];
-    j = (int)(t % g.nn[1]);
-    i = (int)(t / g.nn[1]);
+    decode3(n, g.nn[1], g.nn[2], i, j, k);
 }
 
 // acc[r] (+/-)= E * sum_t K0[t][3*ln + r] * u_e[t] for element (ei,ej,ek).
@@ -73,8 +82,154 @@ __device__ __forceinline__ void gather_ku(const Geom &g, const Mat24<T> &K, cons
     visit_elem<T, 1, 1, 1, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
 }
 
-template <typename T, bool ZeroInit, bool Negate, bool WithDot>
-__global__ void __launch_bounds__(BS) applyk_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
+// ---- K0 access inside unrolled loops ----
+// The full table (a by-value kernel parameter; each entry is a constant-bank load) or, for
+// cube elements, the 10 class values of k0_cube_class held in registers.
+template <typename T, bool Cube>
+struct K0View {
+    const Mat24<T> &K;
+    __device__ explicit K0View(const Mat24<T> &K_) : K(K_) {}
+    __device__ __forceinline__ T operator()(int row, int col) const { return K.a[row * 24 + col]; }
+};
+template <typename T>
+struct K0View<T, true> {
+    T kv[10];
+    __device__ explicit K0View(const Mat24<T> &K) {
+#pragma unroll
+        for (int c = 0; c < 10; ++c) kv[c] = K.cube[c];
+    }
+    __device__ __forceinline__ T operator()(int row, int col) const {
+        const int c = k0_cube_class(row, col);
+        return (c & 16) ? -kv[c & 15] : kv[c & 15];
+    }
+};
+
+template <bool Cube>
+struct K0DFView {
+    const Mat24DF &K;
+    __device__ explicit K0DFView(const Mat24DF &K_) : K(K_) {}
+    __device__ __forceinline__ float hi(int row, int col) const { return K.hi[row * 24 + col]; }
+    __device__ __forceinline__ float lo(int row, int col) const { return K.lo[row * 24 + col]; }
+};
+template <>
+struct K0DFView<true> {
+    float h[10], l[10];
+    __device__ explicit K0DFView(const Mat24DF &K) {
+#pragma unroll
+        for (int c = 0; c < 10; ++c) {
+            h[c] = K.cubeHi[c];
+            l[c] = K.cubeLo[c];
+        }
+    }
+    __device__ __forceinline__ float hi(int row, int col) const {
+        const int c = k0_cube_class(row, col);
+        return (c & 16) ? -h[c & 15] : h[c & 15];
+    }
+    __device__ __forceinline__ float lo(int row, int col) const {
+        const int c = k0_cube_class(row, col);
+        return (c & 16) ? -l[c & 15] : l[c & 15];
+    }
+};
+
+// ---- neighbourhood form (FP32 levels of the mixed preconditioner) ----
+// The 27 neighbours' displacements are loaded once into registers (81 loads instead of
+// 8 elements x 8 nodes x 3 = 192), then every incident element's rows are formed from
+// registers. The FP32 vectors carry a zeroed guard of Geom::nodeGuard() elements on either
+// side and the FP32 moduli a ghost layer of zeros (Geom::padElem), so neither the loads nor
+// the moduli need bounds checks: a neighbour outside the grid reads some finite value that
+// only elements outside the grid use, and those carry E = 0.
+
+// One x-plane (i + a - 1) of the 3x3x3 neighbourhood: P[3b + c][d] = u_d(i+a-1, j+b-1, k+c-1).
+template <typename T>
+__device__ __forceinline__ void load_plane(const Geom &g, const T *__restrict__ u, int64_t n, int a, T (&P)[9][3]) {
+    const int64_t ld = g.ld;
+    const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
+    const T *c0 = u + n + (a - 1) * sx;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        const T *row = c0 + (b - 1) * sy;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T *rd = row + d * ld;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) P[3 * b + c][d] = rd[c - 1];
+        }
+    }
+}
+
+// E of element (i-A, j-B, k-C) at slot 4A+2B+C from the zero-padded moduli.
+template <typename T>
+__device__ __forceinline__ void load_elem_moduli(const Geom &g, const T *__restrict__ Yp, int i, int j, int k,
+                                                 T (&E)[8]) {
+    const int64_t px = (int64_t)(g.ne[1] + 2) * (g.ne[2] + 2), py = g.ne[2] + 2;
+    const T *base = Yp + g.padElem(i, j, k);
+#pragma unroll
+    for (int s = 0; s < 8; ++s) E[s] = base[-(((s >> 2) & 1) * px) - ((s >> 1) & 1) * py - (s & 1)];
+}
+
+// rows 3LN..3LN+2 of K0 times the displacements of element (i-A, j-B, k-C), whose local
+// node m sits at neighbour offset (ma - A, mb - B, mc - C): x-plane Plo (ma = 0) or Phi (ma = 1)
+template <typename T, int A, int B, int C, typename KV>
+__device__ __forceinline__ void elem_rows_planes(const KV &K, const T (&Plo)[9][3], const T (&Phi)[9][3], T &c0,
+                                                 T &c1, T &c2) {
+    constexpr int LN = 4 * A + 2 * B + C;
+    c0 = c1 = c2 = T(0);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int ma = (m >> 2) & 1, mb = (m >> 1) & 1, mc = m & 1;
+        const int q = (mb - B + 1) * 3 + (mc - C + 1);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T v = ma ? Phi[q][d] : Plo[q][d];
+            c0 += K(3 * m + d, 3 * LN + 0) * v;
+            c1 += K(3 * m + d, 3 * LN + 1) * v;
+            c2 += K(3 * m + d, 3 * LN + 2) * v;
+        }
+    }
+}
+
+template <typename T, int A, int B, int C, bool Negate, typename KV>
+__device__ __forceinline__ void visit_planes(const KV &K, const T (&Plo)[9][3], const T (&Phi)[9][3],
+                                             const T (&E)[8], T &f0, T &f1, T &f2) {
+    T c0, c1, c2;
+    elem_rows_planes<T, A, B, C>(K, Plo, Phi, c0, c1, c2);
+    const T e = E[4 * A + 2 * B + C];
+    if (Negate) { f0 -= e * c0; f1 -= e * c1; f2 -= e * c2; }
+    else        { f0 += e * c0; f1 += e * c1; f2 += e * c2; }
+}
+
+// Elements behind the node in x (A = 1) use planes i-1 and i, those in front (A = 0) planes
+// i and i+1, so at most two planes (54 values) are live at a time.
+template <typename T, bool Negate, typename KV>
+__device__ __forceinline__ void gather_ku_nbhd(const Geom &g, const KV &K, const T *__restrict__ Y,
+                                               const T *__restrict__ u, int i, int j, int k, T &f0, T &f1, T &f2) {
+    const int64_t n = g.node(i, j, k);
+    T E[8], Pa[9][3], Pb[9][3];
+    load_elem_moduli<T>(g, Y, i, j, k, E);
+    load_plane<T>(g, u, n, 0, Pa);
+    load_plane<T>(g, u, n, 1, Pb);
+    visit_planes<T, 1, 0, 0, Negate>(K, Pa, Pb, E, f0, f1, f2);
+    visit_planes<T, 1, 0, 1, Negate>(K, Pa, Pb, E, f0, f1, f2);
+    visit_planes<T, 1, 1, 0, Negate>(K, Pa, Pb, E, f0, f1, f2);
+    visit_planes<T, 1, 1, 1, Negate>(K, Pa, Pb, E, f0, f1, f2);
+    load_plane<T>(g, u, n, 2, Pa);
+    visit_planes<T, 0, 0, 0, Negate>(K, Pb, Pa, E, f0, f1, f2);
+    visit_planes<T, 0, 0, 1, Negate>(K, Pb, Pa, E, f0, f1, f2);
+    visit_planes<T, 0, 1, 0, Negate>(K, Pb, Pa, E, f0, f1, f2);
+    visit_planes<T, 0, 1, 1, Negate>(K, Pb, Pa, E, f0, f1, f2);
+}
+
+// K u at a node: neighbourhood form in FP32, element-by-element loads in FP64 (where the
+// 81 register neighbourhood would spill)
+template <typename T, bool Negate, bool Cube>
+__device__ __forceinline__ void gather_ku_any(const Geom &g, const Mat24<T> &K, const T *__restrict__ Y,
+                                              const T *__restrict__ u, int i, int j, int k, T &f0, T &f1, T &f2) {
+    if constexpr (sizeof(T) == 4) gather_ku_nbhd<T, Negate>(g, K0View<T, Cube>(K), Y, u, i, j, k, f0, f1, f2);
+    else gather_ku<T, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+}
+
+template <typename T, bool ZeroInit, bool Negate, bool WithDot, bool Cube>
+__global__ void __launch_bounds__(BS, 2) applyk_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
                                                          T *__restrict__ out, const uint8_t *__restrict__ dmask,
                                                          int zeroDir, double *__restrict__ partials,
                                                          const Mat24<T> K) {
@@ -88,7 +243,7 @@ __global__ void __launch_bounds__(BS) applyk_fine_kernel(Geom g, const T *__rest
             T f0 = ZeroInit ? T(0) : out[n];
             T f1 = ZeroInit ? T(0) : out[ld + n];
             T f2 = ZeroInit ? T(0) : out[2 * ld + n];
-            gather_ku<T, Negate>(g, K, Y, u, i, j, k, f0, f1, f2);
+            gather_ku_any<T, Negate, Cube>(g, K, Y, u, i, j, k, f0, f1, f2);
             if (zeroDir) {
                 const uint8_t dm = dmask[n];
                 if (dm & 1) f0 = T(0);
@@ -112,8 +267,8 @@ __global__ void __launch_bounds__(BS) applyk_fine_kernel(Geom g, const T *__rest
 }
 
 // r = b - K u (MultigridSolver.hh:527-541): b copied, stencil subtracted, Dirichlet zeroed.
-template <typename T>
-__global__ void __launch_bounds__(BS) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
+template <typename T, bool Cube>
+__global__ void __launch_bounds__(BS, 2) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
                                                            const T *__restrict__ b, T *__restrict__ r,
                                                            const uint8_t *__restrict__ dmask, const Mat24<T> K) {
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
@@ -122,7 +277,7 @@ __global__ void __launch_bounds__(BS) residual_fine_kernel(Geom g, const T *__re
     decode_node(g, n, i, j, k);
     const int64_t ld = g.ld;
     T f0 = b[n], f1 = b[ld + n], f2 = b[2 * ld + n];
-    if (j < g.nyv()) gather_ku<T, true>(g, K, Y, u, i, j, k, f0, f1, f2);
+    if (j < g.nyv()) gather_ku_any<T, true, Cube>(g, K, Y, u, i, j, k, f0, f1, f2);
     const uint8_t dm = dmask[n];
     if (dm & 1) f0 = T(0);
     if (dm & 2) f1 = T(0);
@@ -188,25 +343,62 @@ __device__ __forceinline__ void gs_visit(const Geom &g, const Mat24<T> &K, const
         for (int c = 0; c < 3; ++c) M[3 * r + c] += E * K.a[(3 * LN + r) * 24 + 3 * LN + c];
 }
 
+template <typename T, int A, int B, int C, typename KV>
+__device__ __forceinline__ void gs_visit_planes(const KV &K, const T (&Plo)[9][3], const T (&Phi)[9][3],
+                                                const T (&E)[8], T &s0, T &s1, T &s2, T *M) {
+    constexpr int LN = 4 * A + 2 * B + C;
+    const T e = E[LN];
+    T c0, c1, c2;
+    elem_rows_planes<T, A, B, C>(K, Plo, Phi, c0, c1, c2);
+    s0 -= e * c0;
+    s1 -= e * c1;
+    s2 -= e * c2;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) M[3 * r + c] += e * K(3 * LN + r, 3 * LN + c);
+}
+
 // One colour (x%2, y%2, z%2) = (cx, cy, cz) of multicoloured block Gauss-Seidel
 // (MultigridSolver.hh:409-458); incident elements in elementsAdjacentNode order
 // (TPSStencils.hh:47-73).
-template <typename T>
-__global__ void __launch_bounds__(BS) gs_fine_color_kernel(Geom g, const T *__restrict__ Y, T *u,
+template <typename T, bool Cube>
+__global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kernel(Geom g, const T *__restrict__ Y, T *u,
                                                            const T *__restrict__ b, const uint8_t *__restrict__ dmask,
                                                            int cx, int cy, int cz, int forward, const Mat24<T> K) {
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
-    const int kk = (int)(t % n2);
-    const int64_t q = t / n2;
-    const int jj = (int)(q % n1), ii = (int)(q / n1);
+    int ii, jj, kk;
+    decode3(t, n1, n2, ii, jj, kk);
     const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const uint8_t dm = dmask[n];
     if (dm == 7) return;
     T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
     T M[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+    if constexpr (sizeof(T) == 4) {
+        const K0View<T, Cube> Kv(K);
+        T E[8], Pa[9][3], Pb[9][3];
+        load_elem_moduli<T>(g, Y, i, j, k, E);
+        load_plane<T>(g, u, n, 0, Pa);
+        load_plane<T>(g, u, n, 1, Pb);
+        gs_visit_planes<T, 1, 1, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+        gs_visit_planes<T, 1, 0, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+        gs_visit_planes<T, 1, 1, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+        gs_visit_planes<T, 1, 0, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+        T u0 = Pb[4][0], u1 = Pb[4][1], u2 = Pb[4][2];
+        load_plane<T>(g, u, n, 2, Pa);
+        gs_visit_planes<T, 0, 1, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+        gs_visit_planes<T, 0, 0, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+        gs_visit_planes<T, 0, 1, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+        gs_visit_planes<T, 0, 0, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+        smooth_node_solve<T>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
+        u[n] = u0;
+        u[ld + n] = u1;
+        u[2 * ld + n] = u2;
+        return;
+    }
     gs_visit<T, 1, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
     gs_visit<T, 0, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
     gs_visit<T, 1, 0, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
@@ -245,8 +437,8 @@ __device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float b
     sl += err + e;
 }
 
-template <int LN>
-__device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const float *__restrict__ uh_,
+template <int LN, typename KV>
+__device__ __forceinline__ void df_elem(const Geom &g, const KV &K, const float *__restrict__ uh_,
                                         const float *__restrict__ ul_, int64_t base, float *ch, float *cl) {
     const int64_t ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
@@ -260,21 +452,21 @@ __device__ __forceinline__ void df_elem(const Geom &g, const Mat24DF &K, const f
             const float uh = uh_[c * ld + nm], ul = ul_[c * ld + nm];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
-                df_fma_acc(K.hi[(3 * m + c) * 24 + 3 * LN + r], K.lo[(3 * m + c) * 24 + 3 * LN + r], uh, ul, ch[r],
-                           cl[r]);
+                df_fma_acc(K.hi(3 * m + c, 3 * LN + r), K.lo(3 * m + c, 3 * LN + r), uh, ul, ch[r], cl[r]);
         }
     }
 }
 
-template <int A, int B, int Cc>
-__device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const float *__restrict__ Yh,
+template <int A, int B, int Cc, typename KV>
+__device__ __forceinline__ void df_visit(const Geom &g, const KV &K, const float *__restrict__ Yh,
                                          const float *__restrict__ Yl, const float *__restrict__ uh,
                                          const float *__restrict__ ul, int i, int j, int k, float *fh, float *fl) {
+    // zero-padded moduli: an element outside the grid reads E = 0; its node block is clamped
+    // onto a valid element (keeps the loads predicated and the register count low)
     const int ei = i - A, ej = j - B, ek = k - Cc;
-    const bool inb = ei >= 0 && ej >= 0 && ek >= 0 && ei < g.ne[0] && ej < g.ne[1] && ek < g.ne[2];
+    const int64_t e = g.padElem(ei, ej, ek);
+    const float eh = Yh[e], el = Yl[e];
     const int ci = min(max(ei, 0), g.ne[0] - 1), cj = min(max(ej, 0), g.ne[1] - 1), ck = min(max(ek, 0), g.ne[2] - 1);
-    const int64_t e = g.elem(ci, cj, ck);
-    const float eh = inb ? Yh[e] : 0.f, el = inb ? Yl[e] : 0.f;
     float ch[3], cl[3];
     df_elem<4 * A + 2 * B + Cc>(g, K, uh, ul, g.node(ci, cj, ck), ch, cl);
 #pragma unroll
@@ -288,6 +480,8 @@ __device__ __forceinline__ void df_visit(const Geom &g, const Mat24DF &K, const 
 
 // out = K u with u given as its double-float split (uh + ul) and E as (Yh + Yl); out and the
 // optional partial dot products u.out are FP64. No FP64 arithmetic in the inner loops.
+// Yh, Yl are zero-padded element arrays (Geom::padElem) and uh, ul guarded vectors.
+template <bool Cube>
 __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float *__restrict__ Yh,
                                                             const float *__restrict__ Yl,
                                                             const float *__restrict__ uh,
@@ -305,14 +499,15 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float 
         double f[3] = {0.0, 0.0, 0.0};
         if (j < g.nyv()) {
             float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
-            df_visit<0, 0, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<0, 0, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<0, 1, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<0, 1, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<1, 0, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<1, 0, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<1, 1, 0>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
-            df_visit<1, 1, 1>(g, K, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            const K0DFView<Cube> Kv(K);
+            df_visit<0, 0, 0>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 0, 1>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 1, 0>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<0, 1, 1>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 0, 0>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 0, 1>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 1, 0>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
+            df_visit<1, 1, 1>(g, Kv, Yh, Yl, uh, ul, i, j, k, fh, fl);
             const uint8_t dm = zeroDir ? dmask[n] : 0;
 #pragma unroll
             for (int r = 0; r < 3; ++r) f[r] = ((dm >> r) & 1) ? 0.0 : (double)fh[r] + (double)fl[r];
@@ -334,6 +529,21 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float 
     }
 }
 
+// Zero-padded FP32 copies of the moduli: hi = fl(Y) and, if lo is given, lo = fl(Y - hi).
+__global__ void pad_young_kernel(Geom g, const double *__restrict__ Y, float *__restrict__ hi,
+                                 float *__restrict__ lo) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= g.padNE()) return;
+    int pi, pj, pk;
+    decode3(t, g.ne[1] + 2, g.ne[2] + 2, pi, pj, pk);
+    const int i = pi - 1, j = pj - 1, k = pk - 1;
+    const bool in = i >= 0 && j >= 0 && k >= 0 && i < g.ne[0] && j < g.ne[1] && k < g.ne[2];
+    const double v = in ? Y[g.elem(i, j, k)] : 0.0;
+    const float h = __double2float_rn(v);
+    hi[t] = h;
+    if (lo) lo[t] = __double2float_rn(v - (double)h);
+}
+
 __global__ void split_df_kernel(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo,
                                 int64_t n) {
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
@@ -350,7 +560,7 @@ __global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restri
                              double gamma, double q, int law, int masking, int ipow) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= g.NE) return;
-    const int ej = (int)((e / g.ne[2]) % g.ne[1]);
+    const int ej = (int)(((uint32_t)e / (uint32_t)g.ne[2]) % (uint32_t)g.ne[1]);
     double v;
     if (masking && ej >= g.firstMaskedE) {
         v = 0.0;
@@ -379,9 +589,8 @@ __global__ void __launch_bounds__(BS) compliance_grad_kernel(Geom g, const doubl
                                                              const Mat24<double> K) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= g.NE) return;
-    const int ek = (int)(e % g.ne[2]);
-    const int64_t t = e / g.ne[2];
-    const int ej = (int)(t % g.ne[1]), ei = (int)(t / g.ne[1]);
+    int ei, ej, ek;
+    decode3(e, g.ne[1], g.ne[2], ei, ej, ek);
     if (ej >= g.firstMaskedE) { grad[e] = 0.0; return; }
     const int64_t base = g.node(ei, ej, ek), ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
@@ -417,9 +626,8 @@ __global__ void __launch_bounds__(BS) element_energy_kernel(Geom g, const double
                                                             const Mat24<double> K) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= g.NE) return;
-    const int ek = (int)(e % g.ne[2]);
-    const int64_t t = e / g.ne[2];
-    const int ej = (int)(t % g.ne[1]), ei = (int)(t / g.ne[1]);
+    int ei, ej, ek;
+    decode3(e, g.ne[1], g.ne[2], ei, ej, ek);
     const int64_t base = g.node(ei, ej, ek), ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
     double ue[24];
@@ -494,23 +702,30 @@ void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat
                         cudaStream_t st) {
     const unsigned grid = gridFor(g.NN, BS);
     const int zd = zeroDirichlet ? 1 : 0;
-    if (partialDot) {
-        if ((int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
-        applyk_fine_kernel<T, true, false, true><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, partialDot, K0);
-    } else if (zeroInit) {
-        if (negate) applyk_fine_kernel<T, true, true, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
-        else applyk_fine_kernel<T, true, false, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
-    } else {
-        if (negate) applyk_fine_kernel<T, false, true, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
-        else applyk_fine_kernel<T, false, false, false><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
-    }
+    if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
+    auto go = [&](auto cube) {
+        constexpr bool C = decltype(cube)::value;
+        if (partialDot)
+            applyk_fine_kernel<T, true, false, true, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, partialDot, K0);
+        else if (zeroInit && negate)
+            applyk_fine_kernel<T, true, true, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+        else if (zeroInit)
+            applyk_fine_kernel<T, true, false, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+        else if (negate)
+            applyk_fine_kernel<T, false, true, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+        else
+            applyk_fine_kernel<T, false, false, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+    };
+    if (sizeof(T) == 4 && K0.isCube) go(std::true_type{});
+    else go(std::false_type{});
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
                           const uint8_t *dmask, cudaStream_t st) {
-    residual_fine_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
+    if (sizeof(T) == 4 && K0.isCube) residual_fine_kernel<T, true><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
+    else residual_fine_kernel<T, false><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -520,8 +735,12 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
     const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
     const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
-    gs_fine_color_kernel<T><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz, forward ? 1 : 0,
-                                                                       K0);
+    if (sizeof(T) == 4 && K0.isCube)
+        gs_fine_color_kernel<T, true><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz,
+                                                                               forward ? 1 : 0, K0);
+    else
+        gs_fine_color_kernel<T, false><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz,
+                                                                                forward ? 1 : 0, K0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -530,8 +749,17 @@ void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, cons
                            double *partialDot, int partialBlocks, cudaStream_t st, const double *rhs) {
     const unsigned grid = gridFor(g.NN, BS);
     if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
-    applyk_fine_df_kernel<<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0, partialDot,
-                                               partialDot ? 1 : 0, rhs, K0);
+    if (K0.isCube)
+        applyk_fine_df_kernel<true><<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
+                                                         partialDot, partialDot ? 1 : 0, rhs, K0);
+    else
+        applyk_fine_df_kernel<false><<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
+                                                          partialDot, partialDot ? 1 : 0, rhs, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch_pad_young(const Geom &g, const double *Y, float *hi, float *lo, cudaStream_t st) {
+    pad_young_kernel<<<gridFor(g.padNE(), BS), BS, 0, st>>>(g, Y, hi, lo);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -23,9 +23,8 @@ __global__ void dense_from_stencil_kernel(Geom g, const T *__restrict__ S, const
     const int64_t n = t / 243;
     const int q = (int)(t % 243);  // row entry of the node-contiguous stencil
     const int o = q / 9, r = (q % 9) / 3, c = q % 3;
-    const int k = (int)(n % g.nn[2]);
-    const int64_t tt = n / g.nn[2];
-    const int j = (int)(tt % g.nn[1]), i = (int)(tt / g.nn[1]);
+    int i, j, k;
+    stencil::decode(n, g.nn[1], g.nn[2], i, j, k);
     const int ni = i + o / 9 - 1, nj = j + (o / 3) % 3 - 1, nk = k + o % 3 - 1;
     if (ni < 0 || nj < 0 || nk < 0 || ni >= g.nn[0] || nj >= g.nn[1] || nk >= g.nn[2]) return;
     const int64_t m = g.node(ni, nj, nk);
@@ -342,7 +341,7 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
         s[n] = s0;
         s[g.ld + n] = s1;
         s[2 * g.ld + n] = s2;
-        const int j = (int)((n / g.nn[2]) % g.nn[1]);
+        const int j = (int)(((uint32_t)n / (uint32_t)g.nn[2]) % (uint32_t)g.nn[1]);
         if (j < rows) acc += r[n] * s0 + r[g.ld + n] * s1 + r[2 * g.ld + n] * s2;
     }
     const double t = block_sum<BS>(acc);

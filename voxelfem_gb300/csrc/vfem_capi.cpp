@@ -85,6 +85,9 @@ int vfem_grid_get_etensor(const vfem_grid *g, double *young, double *poisson) {
 int vfem_grid_get_k0(const vfem_grid *g, double *out576) {
     return guarded([&] { need(g, "grid"); need(out576, "out"); std::memcpy(out576, g->g.K0.a, 576 * sizeof(double)); });
 }
+int vfem_grid_k0_is_cube(const vfem_grid *g, int *cube) {
+    return guarded([&] { need(g, "grid"); need(cube, "out"); *cube = g->g.K0.isCube; });
+}
 int vfem_grid_set_material_params(vfem_grid *g, double E0, double Emin, double gamma, double q, int law) {
     return guarded([&] {
         need(g, "grid");

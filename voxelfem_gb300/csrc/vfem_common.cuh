@@ -47,6 +47,15 @@ struct Geom {
     __host__ __device__ int nev() const { return firstMaskedE < ne[1] ? firstMaskedE : ne[1]; }
     __host__ __device__ int64_t node(int i, int j, int k) const { return ((int64_t)i * nn[1] + j) * nn[2] + k; }
     __host__ __device__ int64_t elem(int i, int j, int k) const { return ((int64_t)i * ne[1] + j) * ne[2] + k; }
+    // Zero-padded element arrays carry one ghost layer on every side: element (i, j, k),
+    // -1 <= i <= ne[0], sits at padElem(i, j, k); padNE() elements in all.
+    __host__ __device__ int64_t padElem(int i, int j, int k) const {
+        return ((int64_t)(i + 1) * (ne[1] + 2) + (j + 1)) * (ne[2] + 2) + (k + 1);
+    }
+    __host__ __device__ int64_t padNE() const { return (int64_t)(ne[0] + 2) * (ne[1] + 2) * (ne[2] + 2); }
+    // Guard (in elements) that a nodal gather reaching one node past the grid in every
+    // direction needs before and after a 3 x NN vector.
+    __host__ __device__ int64_t nodeGuard() const { return (int64_t)nn[1] * nn[2] + nn[2] + 1; }
 };
 
 inline int64_t padTo(int64_t n, int64_t a) { return (n + a - 1) / a * a; }
@@ -74,26 +83,43 @@ template <typename T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    size_t guard = 0;  // zeroed elements before p[0] and after p[n - 1]
     DevBuf() = default;
     explicit DevBuf(size_t count) { alloc(count); }
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), guard(o.guard) { o.p = nullptr; o.n = 0; o.guard = 0; }
     DevBuf &operator=(DevBuf &&o) noexcept {
-        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; guard = o.guard;
+            o.p = nullptr; o.n = 0; o.guard = 0;
+        }
         return *this;
     }
     ~DevBuf() { release(); }
-    void alloc(size_t count) {
-        if (count == n && p) return;
+    // count elements addressed from p, plus `guard` zeroed elements on either side (gathers that
+    // read past the ends of the array without bounds checks stay inside the allocation)
+    void alloc(size_t count, size_t guard_ = 0) {
+        if (count == n && guard_ == guard && p) return;
         release();
-        if (count) VFEM_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        if (count) {
+            T *base = nullptr;
+            VFEM_CUDA(cudaMalloc(&base, (count + 2 * guard_) * sizeof(T)));
+            if (guard_) {
+                VFEM_CUDA(cudaMemset(base, 0, guard_ * sizeof(T)));
+                VFEM_CUDA(cudaMemset(base + guard_ + count, 0, guard_ * sizeof(T)));
+            }
+            p = base + guard_;
+            guard = guard_;
+        }
         n = count;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFree(p - guard);
         p = nullptr;
         n = 0;
+        guard = 0;
     }
     size_t bytes() const { return n * sizeof(T); }
 };

@@ -9,7 +9,10 @@
 //  * the coarsened fine stiffness Kc_fi = I_fi^T K0 I_fi (MultigridSolver.hh:712-722).
 #include "vfem_element.hpp"
 
+#include <algorithm>
 #include <cmath>
+
+#include "vfem_kernels.hpp"
 
 namespace vfem {
 
@@ -85,6 +88,25 @@ void coarsen_element(const double phi[64], const double Kf[576], double Kc[576])
                 for (int fm = 0; fm < 8; ++fm) s += phi[fm * 8 + cm] * T[(3 * fm + d) * 24 + c];
                 Kc[(3 * cm + d) * 24 + c] += s;
             }
+}
+
+bool k0_cube_values(const double *K, double kv[10]) {
+    double amax = 0.0;
+    for (int t = 0; t < 576; ++t) amax = std::max(amax, std::fabs(K[t]));
+    bool set[10] = {false};
+    for (int row = 0; row < 24; ++row)
+        for (int col = 0; col < 24; ++col) {
+            const int c = k0_cube_class(row, col);
+            const double v = (c & 16) ? -K[row * 24 + col] : K[row * 24 + col];
+            const int k = c & 15;
+            if (!set[k]) {
+                kv[k] = v;
+                set[k] = true;
+            } else if (std::fabs(kv[k] - v) > 1e-13 * amax) {
+                return false;
+            }
+        }
+    return true;
 }
 
 }  // namespace vfem

@@ -79,6 +79,8 @@ Grid::Grid(const int ne[3], const double bmin_[3], const double bmax_[3]) {
         h[d] = (bmax[d] - bmin[d]) / ne[d];
     }
     g = makeGeom(ne);
+    // device index decodes are 32-bit
+    if (3 * g.NN >= (int64_t(1) << 31) || g.NE >= (int64_t(1) << 31)) throw Error(ERR_ARG, "grid too large");
     VFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     rho.alloc(g.NE);
     Y.alloc(g.NE);
@@ -108,6 +110,15 @@ void Grid::setETensor(double E, double nu_) {
         K0df.hi[t] = (float)K0.a[t];
         K0df.lo[t] = (float)(K0.a[t] - (double)K0df.hi[t]);
     }
+    double kv[10];
+    const bool cube = k0_cube_values(K0.a, kv);
+    K0.isCube = K0f.isCube = K0df.isCube = cube ? 1 : 0;
+    for (int c = 0; c < 10; ++c) {
+        K0.cube[c] = cube ? kv[c] : 0.0;
+        K0f.cube[c] = (float)K0.cube[c];
+        K0df.cubeHi[c] = (float)K0.cube[c];
+        K0df.cubeLo[c] = (float)(K0.cube[c] - (double)K0df.cubeHi[c]);
+    }
     ++densVersion;  // stiffness depends on K0
 }
 
@@ -124,19 +135,29 @@ void Grid::updateYoungModuli() {
     const bool masking = maskH < bmax[BUILD_DIR];
     launch_young_moduli<double>(g, rho.p, Y.p, E0, Emin, gamma, q, law, masking, stream);
     YfValid = false;
+    YfpValid = false;
     YdfValid = false;
     ++densVersion;
 }
 
 void Grid::youngDF(const float **hi, const float **lo) {
     if (!YdfValid) {
-        Yhi.alloc(g.NE);
-        Ylo.alloc(g.NE);
-        launch_split_df(Y.p, Yhi.p, Ylo.p, g.NE, stream);
+        Yhi.alloc(g.padNE());
+        Ylo.alloc(g.padNE());
+        launch_pad_young(g, Y.p, Yhi.p, Ylo.p, stream);
         YdfValid = true;
     }
     *hi = Yhi.p;
     *lo = Ylo.p;
+}
+
+const float *Grid::youngFPad() {
+    if (!YfpValid) {
+        Yfp.alloc(g.padNE());
+        launch_pad_young(g, Y.p, Yfp.p, nullptr, stream);
+        YfpValid = true;
+    }
+    return Yfp.p;
 }
 
 const float *Grid::youngF() {
@@ -349,8 +370,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     s.alloc(3 * NN);
     dvec.alloc(3 * NN);
     Ad.alloc(3 * NN);
-    dhi.alloc(3 * NN);
-    dlo.alloc(3 * NN);
+    dhi.alloc(3 * NN, fine->g.nodeGuard());  // read by the unchecked double-float gather
+    dlo.alloc(3 * NN, fine->g.nodeGuard());
     partialCount = std::max<int>(REDUCE_BLOCKS, (int)gridFor(NN, 256));
     partials.alloc(partialCount);
     sc.alloc(16);
@@ -470,7 +491,8 @@ void MG::allocLevels() {
             D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
         } else {
             auto &D = lv[l].d32;
-            D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3);
+            // the fine FP32 iterate is read by the unchecked neighbourhood gathers
+            D.x.alloc(n3, l == 0 ? lv[0].g.nodeGuard() : 0); D.b.alloc(n3); D.r.alloc(n3);
         }
     }
 }
@@ -485,6 +507,7 @@ struct Tr;
 template <>
 struct Tr<double> {
     static const double *Y(Grid &g) { return g.Y.p; }
+    static const double *Yfine(Grid &g) { return g.Y.p; }
     static const Mat24<double> &K0(Grid &g) { return g.K0; }
     static DevBuf<double> &Kc(MG &m) { return m.Kc64; }
     static DevBuf<double> &K2(MG &m) { return m.K2_64; }
@@ -493,6 +516,7 @@ struct Tr<double> {
 template <>
 struct Tr<float> {
     static const float *Y(Grid &g) { return g.youngF(); }
+    static const float *Yfine(Grid &g) { return g.youngFPad(); }
     static const Mat24<float> &K0(Grid &g) { return g.K0f; }
     static DevBuf<float> &Kc(MG &m) { return m.Kc32; }
     static DevBuf<float> &K2(MG &m) { return m.K2_32; }
@@ -610,7 +634,7 @@ void MG::smoothT(int l, bool forward) {
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
     for (int c = 0; c < 8; ++c) {
         const int color = forward ? c : 7 - c;
-        if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);
+        if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);
         else launch_gs_stencil_color<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, color, forward, lv[l].rows, st);
     }
 }
@@ -619,7 +643,7 @@ template <typename T>
 void MG::residualT(int l) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
-    if (l == 0) launch_residual_fine<T>(lv[0].g, Tr<T>::Y(*fine), D.x.p, D.b.p, D.r.p, Tr<T>::K0(*fine), fine->dmask.p, st);
+    if (l == 0) launch_residual_fine<T>(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, D.r.p, Tr<T>::K0(*fine), fine->dmask.p, st);
     else launch_stencil_residual<T>(lv[l].g, D.S.p, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, lv[l].rows, st);
 }
 
@@ -801,6 +825,7 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
     // everything the iteration reads must exist before a graph is captured (no allocation while capturing)
     if (precision == PREC_MIXED) {
         fine->youngF();
+        fine->youngFPad();
         const float *yh, *yl;
         if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
         allocLevels();
@@ -903,7 +928,7 @@ template <typename T>
 void MG::applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate) {
     cudaStream_t st = fine->stream;
     if (l == 0)
-        launch_applyk_fine<T>(lv[0].g, Tr<T>::Y(*fine), u, out, Tr<T>::K0(*fine), zeroInit, negate, fine->dmask.p, false,
+        launch_applyk_fine<T>(lv[0].g, Tr<T>::Yfine(*fine), u, out, Tr<T>::K0(*fine), zeroInit, negate, fine->dmask.p, false,
                               nullptr, 0, st);
     else launch_stencil_apply<T>(lv[l].g, lv[l].data<T>().S.p, u, out, zeroInit, negate, lv[l].rows, st);
 }
@@ -1264,8 +1289,12 @@ double MG::kernelBytes(int which) const {
     case 3: return 4.0 * (9 * nn + ne);
     case 4: return 8.0 * (9 * nn + ne);
     case 5: return 4.0 * (9 * nn + ne);
-    case 6: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 256 * n1); }
-    case 7: { const double n1 = (double)lv[1].g.NN; return 4.0 * (9 * n1 + 256 * n1); }
+    case 6: case 7: case 8: case 9: {
+        // one pass over the level's stencil plus x, b, r (or x read and written)
+        const Level &lvl = lv[which >= 8 ? 2 : 1];
+        const double n1 = (double)lvl.g.NN;
+        return 4.0 * (9 * n1 + (lvl.rows ? 256 : 243) * n1);
+    }
     }
     return 0;
 }
@@ -1273,22 +1302,23 @@ double MG::kernelBytes(int which) const {
 double MG::timeKernel(int which, int reps) {
     if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
     if ((which == 6 || which == 7) && L() < 3) throw Error(ERR_ARG, "level-1 kernels need at least two coarsenings");
+    if ((which == 8 || which == 9) && L() < 4) throw Error(ERR_ARG, "level-2 kernels need at least three coarsenings");
     syncFineGeom(*this);
     cudaStream_t st = fine->stream;
     const Geom &g = lv[0].g;
     const int64_t n3 = 3 * g.NN;
     auto &F = lv[0].d32;
     auto &D = lv[0].d64;
-    const bool need32 = which == 1 || which == 3 || which == 5 || which == 6 || which == 7;
+    const bool need32 = which == 1 || which == 3 || which == 5 || (which >= 6 && which <= 9);
     if (need32) {
         if (which >= 6) {
             if (precision != PREC_MIXED) throw Error(ERR_ARG, "level-1 FP32 kernels need mixed precision");
             ensureStiffness();
         }
-        for (int l = 0; l < (which >= 6 ? 2 : 1); ++l) {
+        for (int l = 0; l < (which >= 8 ? 3 : which >= 6 ? 2 : 1); ++l) {
             auto &Q = lv[l].d32;
             const int64_t m3 = 3 * lv[l].g.NN;
-            Q.x.alloc(m3); Q.b.alloc(m3); Q.r.alloc(m3);
+            Q.x.alloc(m3, l == 0 ? lv[0].g.nodeGuard() : 0); Q.b.alloc(m3); Q.r.alloc(m3);
             launch_fill<float>(Q.x.p, 0.5f, m3, st);
             launch_fill<float>(Q.b.p, 1.0f, m3, st);
         }
@@ -1301,7 +1331,7 @@ double MG::timeKernel(int which, int reps) {
     auto run = [&]() {
         switch (which) {
         case 0: launch_applyk_fine<double>(g, fine->Y.p, D.x.p, D.r.p, fine->K0, true, false, fine->dmask.p, false, nullptr, 0, st); break;
-        case 1: launch_applyk_fine<float>(g, fine->youngF(), F.x.p, F.r.p, fine->K0f, true, false, fine->dmask.p, false, nullptr, 0, st); break;
+        case 1: launch_applyk_fine<float>(g, fine->youngFPad(), F.x.p, F.r.p, fine->K0f, true, false, fine->dmask.p, false, nullptr, 0, st); break;
         case 2: {
             const float *yh, *yl;
             fine->youngDF(&yh, &yl);
@@ -1313,6 +1343,8 @@ double MG::timeKernel(int which, int reps) {
         case 5: residualT<float>(0); break;
         case 6: smoothT<float>(1, true); break;
         case 7: residualT<float>(1); break;
+        case 8: smoothT<float>(2, true); break;
+        case 9: residualT<float>(2); break;
         default: throw Error(ERR_ARG, "unknown kernel id");
         }
     };
@@ -1377,6 +1409,7 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
     }
     if (precision == PREC_MIXED) {
         fine->youngF();
+        fine->youngFPad();
         const float *yh, *yl;
         fine->youngDF(&yh, &yl);
     }

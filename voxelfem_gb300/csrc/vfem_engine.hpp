@@ -54,8 +54,8 @@ public:
     double grav[3] = {0, 0, 0};
 
     DevBuf<double> rho, Y;
-    DevBuf<float> Yf, Yhi, Ylo;
-    bool YfValid = false, YdfValid = false;
+    DevBuf<float> Yf, Yfp, Yhi, Ylo;  // FP32 moduli; zero-padded FP32; zero-padded double-float pair
+    bool YfValid = false, YfpValid = false, YdfValid = false;
     std::vector<uint8_t> dmask_h;
     std::vector<double> dval_h;   // SoA, stride NN
     std::vector<double> force_h;  // dense nodal forces, SoA
@@ -72,6 +72,7 @@ public:
     void getDensities(double *out);
     void getYoungModuli(double *out);
     void updateYoungModuli();
+    const float *youngFPad();  // zero-padded FP32 moduli (Geom::padElem layout)
     const float *youngF();
     void youngDF(const float **hi, const float **lo);  // double-float split of Y
     void addDirichlet(const double u[3], const double mn[3], const double mx[3], unsigned cmask);
@@ -139,7 +140,7 @@ public:
     // L() when no level is small enough).
     int tailStart() const;
     int64_t tailMaxNodes = 0;
-    int64_t rowsMaxNodes = 200000;  // levels up to this size store node-contiguous stencil rows
+    int64_t rowsMaxNodes = 0;  // levels up to this size store node-contiguous stencil rows (default: none)
     // When set, the stiffness update records a CUDA event after each of its steps (profiling).
     std::vector<std::pair<std::string, cudaEvent_t>> *stiffMarks = nullptr;
 

@@ -13,13 +13,44 @@ namespace vfem {
 template <typename T>
 struct Mat24 {
     T a[576];
+    // Equal element sizes (isotropic material): a[row * 24 + col] = +-cube[class], with
+    // k0_cube_class(row, col) = class | 16 * negative. Kernels then hold the 10 values in
+    // registers instead of reading 576 constants.
+    T cube[10];
+    int isCube = 0;
 };
 
 // Double-float copy of K0 for the FP64-accurate FP32 matvec.
 struct Mat24DF {
     float hi[576];
     float lo[576];
+    float cubeHi[10], cubeLo[10];
+    int isCube = 0;
 };
+
+// Entry (3m+d, 3n+r) of the stiffness matrix of a cube element (nodes l = 4x+2y+z, isotropic
+// material) depends only on which axes separate nodes m and n: for d == r on whether axis d
+// does and on how many of the other two do (6 classes); for d != r on whether axes d and r
+// both or neither separate them and on whether the third axis does (4 classes), with sign
+// xi_m[d] xi_n[r] (xi = +-1 the node's side along the axis). Returns class | 16 * negative.
+__host__ __device__ constexpr int k0_cube_class(int row, int col) {
+    const int m = row / 3, d = row % 3, n = col / 3, r = col % 3;
+    const int dd = ((m >> (2 - d)) ^ (n >> (2 - d))) & 1;
+    if (d == r) {
+        int others = 0;
+        for (int a = 0; a < 3; ++a)
+            if (a != d) others += ((m >> (2 - a)) ^ (n >> (2 - a))) & 1;
+        return 3 * dd + others;
+    }
+    const int t = 3 - d - r;
+    const int dr = ((m >> (2 - r)) ^ (n >> (2 - r))) & 1;
+    const int dt = ((m >> (2 - t)) ^ (n >> (2 - t))) & 1;
+    const int xm = 2 * ((m >> (2 - d)) & 1) - 1, xn = 2 * ((n >> (2 - r)) & 1) - 1;
+    return (6 + 2 * (dd == dr ? 1 : 0) + dt) | (xm * xn < 0 ? 16 : 0);
+}
+
+// kv[c] from K (24 x 24, row-major) if every entry matches the cube pattern to round-off.
+bool k0_cube_values(const double *K, double kv[10]);
 
 // ---------------- fine level (k_fine.cu) ----------------
 template <typename T>
@@ -28,6 +59,9 @@ void launch_young_moduli(const Geom &g, const double *rho, T *Y, double E0, doub
 template <typename T>
 void launch_convert(const void *src, bool srcDouble, T *dst, int64_t n, cudaStream_t st);
 
+// Fine-level gathers. T = double: Y is the plain moduli array. T = float: Y is the zero-padded
+// FP32 copy (launch_pad_young) and u a vector with a zeroed guard of Geom::nodeGuard() elements
+// on either side (DevBuf::alloc(n, guard)).
 // out = +-K u (+ out if !zeroInit). zeroDirichlet zeroes constrained components of out.
 // partialDot (optional, FP64 path only) receives per-block partials of sum(u . out) over nondetached rows.
 template <typename T>
@@ -48,6 +82,8 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
 void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, const float *uh, const float *ul,
                            const double *u, double *out, const Mat24DF &K0, const uint8_t *dmask, bool zeroDirichlet,
                            double *partialDot, int partialBlocks, cudaStream_t st, const double *rhs = nullptr);
+// Zero-padded (Geom::padElem) FP32 moduli: hi = fl(Y), and lo = fl(Y - hi) when lo is given.
+void launch_pad_young(const Geom &g, const double *Y, float *hi, float *lo, cudaStream_t st);
 // hi = fl(v), lo = fl(v - hi)
 void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStream_t st);
 

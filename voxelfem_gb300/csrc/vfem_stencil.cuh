@@ -6,11 +6,14 @@
 namespace vfem {
 namespace stencil {
 
+// Node and element counts stay below 2^31 (checked when a grid is created), so index
+// decodes use 32-bit unsigned division; a 64-bit division is a long software sequence.
 __device__ __forceinline__ void decode(const int64_t n, const int nn1, const int nn2, int &i, int &j, int &k) {
-    k = (int)(n % nn2);
-    const int64_t t = n / nn2;
-    j = (int)(t % nn1);
-    i = (int)(t / nn1);
+    const uint32_t u = (uint32_t)n, t = u / (uint32_t)nn2;
+    k = (int)(u - t * (uint32_t)nn2);
+    const uint32_t q = t / (uint32_t)nn1;
+    j = (int)(t - q * (uint32_t)nn1);
+    i = (int)q;
 }
 
 // Assembled stencil rows are stored node-contiguous: the 27 blocks of node n occupy
@@ -63,24 +66,34 @@ __device__ __forceinline__ T warp_reduce(T v) {
     return v;
 }
 
-// Lane-partial products of row n with u; v receives the lane's 8 row entries. After the
-// call every lane holds the full sums (butterfly reduction).
+// Lane-partial products of row n with u; v receives the lane's 8 row entries. The 8
+// entries of a lane span at most two neighbour blocks (o_a and o_a + 1), so the lane forms
+// two neighbour indices and walks its entries with a running (row, component) counter.
+// After the call every lane holds the full sums (butterfly reduction).
 template <typename T>
 __device__ __forceinline__ void row_times_u(const Geom &g, const T *__restrict__ S, const T *__restrict__ u, int64_t n,
                                             int i, int j, int k, int lane, T *v, T &f0, T &f1, T &f2) {
     RowVec<T>::load(S + n * ROW + lane * 8, v);
     const int64_t ld = g.ld;
+    const int e0 = lane * 8;
+    const int oa = e0 / 9;
+    const int64_t ma = neighbour(g, n, i, j, k, oa);
+    const int64_t mb = oa < 26 ? neighbour(g, n, i, j, k, oa + 1) : ma;
+    int rc = e0 - 9 * oa;  // position of the first entry inside its 3x3 block
     T p0 = T(0), p1 = T(0), p2 = T(0);
+    bool second = false;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const int e = lane * 8 + q;
-        if (e < ROW_USED) {
-            const int o = e / 9, rc = e % 9, r = rc / 3;
-            const int64_t m = neighbour(g, n, i, j, k, o);
-            const T prod = v[q] * u[(rc % 3) * ld + m];
+        if (e0 + q < ROW_USED) {
+            const int r = rc / 3, c = rc - 3 * r;
+            const T prod = v[q] * u[c * ld + (second ? mb : ma)];
             p0 += (r == 0) ? prod : T(0);
             p1 += (r == 1) ? prod : T(0);
             p2 += (r == 2) ? prod : T(0);
+        }
+        if (++rc == 9) {
+            rc = 0;
+            second = true;
         }
     }
     f0 = warp_reduce(p0);
@@ -195,78 +208,67 @@ __device__ __forceinline__ void colour_node(const Geom &g, int64_t p, int &i, in
     const int cz = p >= C;
     if (cz) p -= C;
     const int c2 = half_count(g.nn[2], cz);
-    const int kk = (int)(p % c2);
-    const int64_t q = p / c2;
-    i = 2 * (int)(q / c1) + cx;
-    j = 2 * (int)(q % c1) + cy;
+    int ii, jj, kk;
+    decode(p, c1, c2, ii, jj, kk);
+    i = 2 * ii + cx;
+    j = 2 * jj + cy;
     k = 2 * kk + cz;
 }
 
-// The 27 blocks are consumed in three batches of nine; each batch issues its 27 u loads and
-// 81 stencil loads before any arithmetic, so a thread waits on three memory round trips
-// instead of twenty-seven.
-template <typename T, bool Negate>
-__device__ __forceinline__ void stencil_row_soa(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
-                                                int64_t n, int64_t p, int i, int j, int k, T &f0, T &f1, T &f2) {
+// Split form for the plane layout: a block of SPLIT_SUB warps works on 32 nodes (lane =
+// node); warp w sums the neighbour blocks o = w, w + 8, w + 16, w + 24 of its lane's node,
+// issuing all of their loads before any arithmetic. The partial sums are combined in a
+// fixed order in shared memory. Eight times as many threads as nodes keep enough loads in
+// flight for a colour pass over a few tens of thousands of nodes.
+constexpr int SPLIT_SUB = 8;
+constexpr int SPLIT_NODES = 32;
+
+template <typename T>
+__device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+                                                 int64_t n, int64_t p, int i, int j, int k, int sub, T &f0, T &f1,
+                                                 T &f2) {
     const int64_t ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
-    const int64_t dx[3] = {i > 0 ? -sx : 0, 0, i + 1 < g.nn[0] ? sx : 0};
-    const int64_t dy[3] = {j > 0 ? -sy : 0, 0, j + 1 < g.nn[1] ? sy : 0};
-    const int64_t dz[3] = {k > 0 ? -1 : 0, 0, k + 1 < g.nn[2] ? 1 : 0};
+    T uu[4][3], ss[4][9];
 #pragma unroll
-    for (int bx = 0; bx < 3; ++bx) {
-        T uu[9][3], ss[9][9];
-#pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const int64_t m = n + dx[bx] + dy[t / 3] + dz[t % 3];
+    for (int t = 0; t < 4; ++t) {
+        const int o = sub + SPLIT_SUB * t;
+        if (o < 27) {
+            const int ox = o / 9 - 1, oy = (o / 3) % 3 - 1, oz = o % 3 - 1;
+            // a neighbour outside the grid has a zero block; read the node itself instead
+            const bool in = (unsigned)(i + ox) < (unsigned)g.nn[0] && (unsigned)(j + oy) < (unsigned)g.nn[1] &&
+                            (unsigned)(k + oz) < (unsigned)g.nn[2];
+            const int64_t m = in ? n + ox * sx + oy * sy + oz : n;
 #pragma unroll
             for (int c = 0; c < 3; ++c) uu[t][c] = u[c * ld + m];
-            const T *blk = S + (int64_t)((bx * 9 + t) * 9) * ld + p;
+            const T *blk = S + (int64_t)(o * 9) * ld + p;
 #pragma unroll
             for (int e = 0; e < 9; ++e) ss[t][e] = blk[e * ld];
-        }
+        } else {
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const T v0 = ss[t][0] * uu[t][0] + ss[t][1] * uu[t][1] + ss[t][2] * uu[t][2];
-            const T v1 = ss[t][3] * uu[t][0] + ss[t][4] * uu[t][1] + ss[t][5] * uu[t][2];
-            const T v2 = ss[t][6] * uu[t][0] + ss[t][7] * uu[t][1] + ss[t][8] * uu[t][2];
-            if (Negate) { f0 -= v0; f1 -= v1; f2 -= v2; }
-            else        { f0 += v0; f1 += v1; f2 += v2; }
+            for (int c = 0; c < 3; ++c) uu[t][c] = T(0);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) ss[t][e] = T(0);
         }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        f0 += ss[t][0] * uu[t][0] + ss[t][1] * uu[t][1] + ss[t][2] * uu[t][2];
+        f1 += ss[t][3] * uu[t][0] + ss[t][4] * uu[t][1] + ss[t][5] * uu[t][2];
+        f2 += ss[t][6] * uu[t][0] + ss[t][7] * uu[t][1] + ss[t][8] * uu[t][2];
     }
 }
 
+// Sum of the SPLIT_SUB partials of lane `lane` (fixed order); part is [3][SPLIT_SUB][32].
 template <typename T>
-__device__ __forceinline__ void gs_node_soa(const Geom &g, const T *__restrict__ S, T *u, const T *__restrict__ b,
-                                            const uint8_t *__restrict__ dmask, int i, int j, int k, int64_t p,
-                                            bool forward) {
-    const int64_t n = g.node(i, j, k), ld = g.ld;
-    const uint8_t dm = dmask[n];
-    if (dm == 7) return;
-    T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
-    stencil_row_soa<T, true>(g, S, u, n, p, i, j, k, s0, s1, s2);
-    T M[9];
+__device__ __forceinline__ void split_sum(const T (*part)[SPLIT_SUB][SPLIT_NODES], int lane, T &f0, T &f1, T &f2) {
+    f0 = f1 = f2 = T(0);
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
-    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
-    node_solve<T>(dm, s0, s1, s2, M, forward, u0, u1, u2);
-    u[n] = u0;
-    u[ld + n] = u1;
-    u[2 * ld + n] = u2;
-}
-
-template <typename T>
-__device__ __forceinline__ void residual_node_soa(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
-                                                  const T *__restrict__ b, T *__restrict__ r,
-                                                  const uint8_t *__restrict__ dmask, int64_t n, int64_t p, int i, int j,
-                                                  int k) {
-    const int64_t ld = g.ld;
-    T f0 = b[n], f1 = b[ld + n], f2 = b[2 * ld + n];
-    if (j < g.nyv()) stencil_row_soa<T, true>(g, S, u, n, p, i, j, k, f0, f1, f2);
-    const uint8_t dm = dmask[n];
-    r[n] = (dm & 1) ? T(0) : f0;
-    r[ld + n] = (dm & 2) ? T(0) : f1;
-    r[2 * ld + n] = (dm & 4) ? T(0) : f2;
+    for (int w = 0; w < SPLIT_SUB; ++w) {
+        f0 += part[0][w][lane];
+        f1 += part[1][w][lane];
+        f2 += part[2][w][lane];
+    }
 }
 
 // Full-weighting restriction onto coarse node (i, j, k) (MultigridSolver.hh:217-275); rows at or

@@ -211,6 +211,12 @@ class TensorProductSimulator_3D:
         check(_lib().vfem_grid_get_k0(self._h, _capi.dptr(K)))
         return K.reshape(24, 24)
 
+    def k0IsCube(self):
+        """Whether K0 has the cube structure the fast fine-level kernels use (diagnostic)."""
+        v = C.c_int32()
+        check(_lib().vfem_grid_k0_is_cube(self._h, C.byref(v)))
+        return bool(v.value)
+
     def elementStiffnessMatrix(self, ei):
         return self.elementYoungModulusScaleFactor(ei) * self.fullDensityElementStiffnessMatrix()
 
