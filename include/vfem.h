@@ -105,6 +105,13 @@ int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out);
 int vfem_grid_build_load(vfem_grid *g, double *out);
 /* complianceGradient(u) (TensorProductSimulator.hh:973-1005) */
 int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_out);
+/* Adjoint-method sensitivity (no reference counterpart; generalises complianceGradient,
+ * TensorProductSimulator.hh:973-1005): grad_e = load_weight * lambda^T df/drho_e
+ * - stiffness_weight * dE/drho_e * lambda_e^T K0 u_e, df/drho_e the self-weight load of element e.
+ * lambda = u, weights (1, 1/2) reproduce complianceGradient; (1, 1) is the backward of a solve whose
+ * adjoint state is lambda. */
+int vfem_grid_adjoint_sensitivity(vfem_grid *g, const double *lambda, const double *u, double load_weight,
+                                  double stiffness_weight, double *grad_out);
 /* elementEnergyDensity(u) (TensorProductSimulator.hh:638-654) */
 int vfem_grid_element_energy(vfem_grid *g, const double *u, double *out);
 

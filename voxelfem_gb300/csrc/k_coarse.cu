@@ -73,69 +73,93 @@ __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *_
 
 // Plane-layout kernels: blocks of SPLIT_SUB warps x 32 nodes (stencil::stencil_row_part).
 // Apply / residual walk the colour-ordered positions p; a Gauss-Seidel colour pass walks the
-// nodes of one colour, whose positions are contiguous.
+// nodes of one colour, whose positions are contiguous. Warp 0 and the row warps take separate
+// branches that meet at one named barrier (bar.sync counts arrivals from either site), so
+// the registers warp 0 holds across the barrier do not add to the row warps' live set.
 using stencil::SPLIT_NODES;
+using stencil::SPLIT_ROWS;
 using stencil::SPLIT_SUB;
 constexpr int SPLIT_BS = SPLIT_SUB * SPLIT_NODES;
 
+__device__ __forceinline__ void split_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(SPLIT_BS) : "memory"); }
+
+template <typename T>
+__device__ __forceinline__ void split_rows(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+                                           int64_t n, int64_t p, int i, int j, int k, bool active, int sub, int lane,
+                                           T (*part)[SPLIT_ROWS][SPLIT_NODES]) {
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    if (active) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
+    part[0][sub - 1][lane] = f0;
+    part[1][sub - 1][lane] = f1;
+    part[2][sub - 1][lane] = f2;
+    split_barrier();
+}
+
 template <typename T, bool ZeroInit, bool Negate>
-__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) stencil_apply_soa_kernel(Geom g, const T *__restrict__ S,
-                                                                     const T *__restrict__ u, T *__restrict__ out) {
-    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
+    stencil_apply_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, T *__restrict__ out) {
+    __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
     const bool valid = p < g.NN;
     int i = 0, j = 0, k = 0;
     if (valid) stencil::colour_node(g, p, i, j, k);
     const int64_t n = g.node(i, j, k), ld = g.ld;
-    T f0 = T(0), f1 = T(0), f2 = T(0);
-    if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
-    part[0][sub][lane] = f0;
-    part[1][sub][lane] = f1;
-    part[2][sub][lane] = f2;
-    __syncthreads();
-    if (sub != 0 || !valid) return;
+    if (sub > 0) {
+        split_rows<T>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
+        return;
+    }
+    T o[3] = {T(0), T(0), T(0)};
+    if (valid && !ZeroInit) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = out[c * ld + n];
+    }
+    split_barrier();
+    if (!valid) return;
+    T f0, f1, f2;
     stencil::split_sum<T>(part, lane, f0, f1, f2);
     if (Negate) { f0 = -f0; f1 = -f1; f2 = -f2; }
-    if (!ZeroInit) { f0 += out[n]; f1 += out[ld + n]; f2 += out[2 * ld + n]; }
-    out[n] = f0;
-    out[ld + n] = f1;
-    out[2 * ld + n] = f2;
+    out[n] = o[0] + f0;
+    out[ld + n] = o[1] + f1;
+    out[2 * ld + n] = o[2] + f2;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) stencil_residual_soa_kernel(Geom g, const T *__restrict__ S,
-                                                                        const T *__restrict__ u,
-                                                                        const T *__restrict__ b, T *__restrict__ r,
-                                                                        const uint8_t *__restrict__ dmask) {
-    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
+    stencil_residual_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, const T *__restrict__ b,
+                                T *__restrict__ r, const uint8_t *__restrict__ dmask) {
+    __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
     const bool valid = p < g.NN;
     int i = 0, j = 0, k = 0;
     if (valid) stencil::colour_node(g, p, i, j, k);
     const int64_t n = g.node(i, j, k), ld = g.ld;
-    const bool active = valid && j < g.nyv();
-    T f0 = T(0), f1 = T(0), f2 = T(0);
-    if (active) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
-    part[0][sub][lane] = f0;
-    part[1][sub][lane] = f1;
-    part[2][sub][lane] = f2;
-    __syncthreads();
-    if (sub != 0 || !valid) return;
+    if (sub > 0) {
+        split_rows<T>(g, S, u, n, p, i, j, k, valid && j < g.nyv(), sub, lane, part);
+        return;
+    }
+    T bb[3] = {T(0), T(0), T(0)};
+    uint8_t dm = 7;
+    if (valid) {
+        dm = dmask[n];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bb[c] = b[c * ld + n];
+    }
+    split_barrier();
+    if (!valid) return;
+    T f0, f1, f2;
     stencil::split_sum<T>(part, lane, f0, f1, f2);
-    const uint8_t dm = dmask[n];
-    r[n] = (dm & 1) ? T(0) : b[n] - f0;
-    r[ld + n] = (dm & 2) ? T(0) : b[ld + n] - f1;
-    r[2 * ld + n] = (dm & 4) ? T(0) : b[2 * ld + n] - f2;
+    r[n] = (dm & 1) ? T(0) : bb[0] - f0;
+    r[ld + n] = (dm & 2) ? T(0) : bb[1] - f1;
+    r[2 * ld + n] = (dm & 4) ? T(0) : bb[2] - f2;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u,
-                                                                        const T *__restrict__ b,
-                                                                        const uint8_t *__restrict__ dmask, int cx,
-                                                                        int cy, int cz, int forward) {
-    __shared__ T part[3][SPLIT_SUB][SPLIT_NODES];
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
+    gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+                                const uint8_t *__restrict__ dmask, int cx, int cy, int cz, int forward) {
+    __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t t = blockIdx.x * (int64_t)SPLIT_NODES + lane;
@@ -150,24 +174,30 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2) gs_stencil_c
     }
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const int64_t p = stencil::colour_pos(g, i, j, k);
-    T f0 = T(0), f1 = T(0), f2 = T(0);
-    if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub, f0, f1, f2);
-    part[0][sub][lane] = f0;
-    part[1][sub][lane] = f1;
-    part[2][sub][lane] = f2;
-    __syncthreads();
-    if (sub != 0 || !valid) return;
-    const uint8_t dm = dmask[n];
-    if (dm == 7) return;
-    stencil::split_sum<T>(part, lane, f0, f1, f2);
-    T M[9];
+    if (sub > 0) {
+        split_rows<T>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
+        return;
+    }
+    T M[9], bb[3], uu[3];
+    uint8_t dm = 7;
+    if (valid) {
+        dm = dmask[n];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
-    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
-    stencil::node_solve<T>(dm, b[n] - f0, b[ld + n] - f1, b[2 * ld + n] - f2, M, forward != 0, u0, u1, u2);
-    u[n] = u0;
-    u[ld + n] = u1;
-    u[2 * ld + n] = u2;
+        for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            bb[c] = b[c * ld + n];
+            uu[c] = u[c * ld + n];
+        }
+    }
+    split_barrier();
+    if (!valid || dm == 7) return;
+    T f0, f1, f2;
+    stencil::split_sum<T>(part, lane, f0, f1, f2);
+    stencil::node_solve<T>(dm, bb[0] - f0, bb[1] - f1, bb[2] - f2, M, forward != 0, uu[0], uu[1], uu[2]);
+    u[n] = uu[0];
+    u[ld + n] = uu[1];
+    u[2 * ld + n] = uu[2];
 }
 
 // Full-weighting restriction (MultigridSolver.hh:217-275): coarse node gathers the

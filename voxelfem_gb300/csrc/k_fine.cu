@@ -582,11 +582,16 @@ __global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restri
 }
 
 // TensorProductSimulator.hh:973-1005
+// grad_e = wF * lam^T df/drho_e - wK * dE/drho_e * lam_e^T K0 u_e, df/drho_e the self-weight load
+// of element e (g vol / 8 on each of its nodes). lam = u, wF = 1, wK = 1/2 is the compliance
+// gradient (TensorProductSimulator.hh:973-1005); wF = wK = 1 is the adjoint-method gradient
+// lam^T (df/drho - dK/drho u) of an objective whose adjoint state is lam.
 __global__ void __launch_bounds__(BS) compliance_grad_kernel(Geom g, const double *__restrict__ rho,
+                                                             const double *__restrict__ lam,
                                                              const double *__restrict__ u, double *__restrict__ grad,
                                                              double E0, double Emin, double gamma, double q, int law,
-                                                             double gx, double gy, double gz, double vol,
-                                                             const Mat24<double> K) {
+                                                             double gx, double gy, double gz, double vol, double wF,
+                                                             double wK, const Mat24<double> K) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= g.NE) return;
     int ei, ej, ek;
@@ -594,29 +599,32 @@ __global__ void __launch_bounds__(BS) compliance_grad_kernel(Geom g, const doubl
     if (ej >= g.firstMaskedE) { grad[e] = 0.0; return; }
     const int64_t base = g.node(ei, ej, ek), ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
-    double ue[24];
+    double ue[24], le[24];
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
         const int64_t nm = base + ((m >> 2) & 1) * sx + ((m >> 1) & 1) * sy + (m & 1);
-        ue[3 * m] = u[nm];
-        ue[3 * m + 1] = u[ld + nm];
-        ue[3 * m + 2] = u[2 * ld + nm];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ue[3 * m + c] = u[c * ld + nm];
+            le[3 * m + c] = lam[c * ld + nm];
+        }
     }
-    double uKu = 0.0;
+    double lKu = 0.0;
 #pragma unroll
     for (int r = 0; r < 24; ++r) {
         double acc = 0.0;
 #pragma unroll
         for (int c = 0; c < 24; ++c) acc += K.a[r * 24 + c] * ue[c];
-        uKu += ue[r] * acc;
+        lKu += le[r] * acc;
     }
     const double rh = rho[e];
-    double val;
-    if (law == 0) val = -0.5 * gamma * pow(rh, gamma - 1.0) * (E0 - Emin) * uKu;
-    else val = -0.5 * (1 + q) * (E0 - Emin) / ((1 + q * (1 - rh)) * (1 + q * (1 - rh))) * uKu;
+    double dE;
+    if (law == 0) dE = gamma * pow(rh, gamma - 1.0) * (E0 - Emin);
+    else dE = (1 + q) * (E0 - Emin) / ((1 + q * (1 - rh)) * (1 + q * (1 - rh)));
+    double val = -wK * dE * lKu;
     if (gx != 0.0 || gy != 0.0 || gz != 0.0) {
 #pragma unroll
-        for (int l = 0; l < 8; ++l) val += 0.125 * (gx * ue[3 * l] + gy * ue[3 * l + 1] + gz * ue[3 * l + 2]) * vol;
+        for (int l = 0; l < 8; ++l) val += wF * 0.125 * (gx * le[3 * l] + gy * le[3 * l + 1] + gz * le[3 * l + 2]) * vol;
     }
     grad[e] = val;
 }
@@ -771,8 +779,14 @@ void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStr
 void launch_compliance_gradient(const Geom &g, const double *rho, const double *u, double *grad,
                                 const Mat24<double> &K0, double E0, double Emin, double gamma, double q, int law,
                                 const double *grav, double vol, cudaStream_t st) {
-    compliance_grad_kernel<<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, u, grad, E0, Emin, gamma, q, law, grav[0],
-                                                             grav[1], grav[2], vol, K0);
+    launch_adjoint_sensitivity(g, rho, u, u, grad, K0, E0, Emin, gamma, q, law, grav, vol, 1.0, 0.5, st);
+}
+
+void launch_adjoint_sensitivity(const Geom &g, const double *rho, const double *lam, const double *u, double *grad,
+                                const Mat24<double> &K0, double E0, double Emin, double gamma, double q, int law,
+                                const double *grav, double vol, double wF, double wK, cudaStream_t st) {
+    compliance_grad_kernel<<<gridFor(g.NE, BS), BS, 0, st>>>(g, rho, lam, u, grad, E0, Emin, gamma, q, law, grav[0],
+                                                             grav[1], grav[2], vol, wF, wK, K0);
     VFEM_LAUNCH_CHECK();
 }
 

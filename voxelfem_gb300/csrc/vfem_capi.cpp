@@ -153,6 +153,16 @@ int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out) {
 int vfem_grid_build_load(vfem_grid *g, double *out) {
     return guarded([&] { need(g, "grid"); g->g.buildLoad(out); });
 }
+int vfem_grid_adjoint_sensitivity(vfem_grid *g, const double *lambda, const double *u, double load_weight,
+                                  double stiffness_weight, double *grad_out) {
+    return guarded([&] {
+        need(g, "grid");
+        need(lambda, "lambda");
+        need(u, "u");
+        need(grad_out, "grad_out");
+        g->g.adjointSensitivity(lambda, u, load_weight, stiffness_weight, grad_out);
+    });
+}
 int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_out) {
     return guarded([&] { need(g, "grid"); g->g.complianceGradient(u, grad_out); });
 }

@@ -320,6 +320,16 @@ void Grid::complianceGradient(const double *u, double *out) {
     finishOut(vo, stream);
 }
 
+void Grid::adjointSensitivity(const double *lam, const double *u, double wF, double wK, double *out) {
+    View vl, vu, vo;
+    viewIn(vl, lam, 3 * g.NN * sizeof(double), stream);
+    viewIn(vu, u, 3 * g.NN * sizeof(double), stream);
+    viewOut(vo, out, g.NE * sizeof(double));
+    launch_adjoint_sensitivity(g, rho.p, (const double *)vl.d, (const double *)vu.d, (double *)vo.d, K0, E0, Emin,
+                               gamma, q, law, grav, vol(), wF, wK, stream);
+    finishOut(vo, stream);
+}
+
 void Grid::elementEnergy(const double *u, double *out) {
     View vu, vo;
     viewIn(vu, u, 3 * g.NN * sizeof(double), stream);
@@ -334,7 +344,8 @@ void Grid::elementEnergy(const double *u, double *out) {
 MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     if (coarsenings < 0) throw Error(ERR_ARG, "numCoarseningLevels must be >= 0");
     // Stencil layout switch-over (node count up to which a level keeps node-contiguous rows);
-    // VFEM_STENCIL_ROWS_MAX_NODES overrides it, e.g. 0 puts every assembled level in planes.
+    // VFEM_STENCIL_ROWS_MAX_NODES overrides it (planes measured faster at every level of the
+    // 256x128x128 hierarchy, so the default is 0).
     if (const char *env = std::getenv("VFEM_STENCIL_ROWS_MAX_NODES")) rowsMaxNodes = std::atoll(env);
     lv.resize(coarsenings + 1);
     lv[0].g = fine->g;

@@ -85,6 +85,7 @@ public:
     void applyK(const double *u, double *out);
     void buildLoad(double *out);
     void complianceGradient(const double *u, double *out);
+    void adjointSensitivity(const double *lam, const double *u, double wF, double wK, double *out);
     void elementEnergy(const double *u, double *out);
     double vol() const { return h[0] * h[1] * h[2]; }
 

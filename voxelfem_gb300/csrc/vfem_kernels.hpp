@@ -90,6 +90,10 @@ void launch_split_df(const double *src, float *hi, float *lo, int64_t n, cudaStr
 void launch_compliance_gradient(const Geom &g, const double *rho, const double *u, double *grad, const Mat24<double> &K0,
                                 double E0, double Emin, double gamma, double q, int law, const double *grav,
                                 double vol, cudaStream_t st);
+// grad_e = wF lam^T df/drho_e - wK dE/drho_e lam_e^T K0 u_e (self-weight load term only with gravity).
+void launch_adjoint_sensitivity(const Geom &g, const double *rho, const double *lam, const double *u, double *grad,
+                                const Mat24<double> &K0, double E0, double Emin, double gamma, double q, int law,
+                                const double *grav, double vol, double wF, double wK, cudaStream_t st);
 void launch_element_energy(const Geom &g, const double *Y, const double *u, double *out, const Mat24<double> &K0,
                            cudaStream_t st);
 void launch_build_gravity_load(const Geom &g, const double *rho, double *f, const double *grav, double vol,

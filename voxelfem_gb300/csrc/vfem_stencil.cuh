@@ -216,23 +216,26 @@ __device__ __forceinline__ void colour_node(const Geom &g, int64_t p, int &i, in
 }
 
 // Split form for the plane layout: a block of SPLIT_SUB warps works on 32 nodes (lane =
-// node); warp w sums the neighbour blocks o = w, w + 8, w + 16, w + 24 of its lane's node,
-// issuing all of their loads before any arithmetic. The partial sums are combined in a
-// fixed order in shared memory. Eight times as many threads as nodes keep enough loads in
-// flight for a colour pass over a few tens of thousands of nodes.
+// node). Row warps w = 1..SPLIT_ROWS sum the neighbour blocks o = w-1, w-1+7, w-1+14, w-1+21
+// of their lane's node, issuing all of their loads before any arithmetic; warp 0 meanwhile
+// loads the node's own data (right-hand side, iterate, diagonal block) and, after the
+// barrier, combines the partial sums in a fixed order and finishes the node. Eight times as
+// many threads as nodes keep enough loads in flight for a colour pass over a few tens of
+// thousands of nodes.
 constexpr int SPLIT_SUB = 8;
+constexpr int SPLIT_ROWS = SPLIT_SUB - 1;
 constexpr int SPLIT_NODES = 32;
 
 template <typename T>
 __device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
                                                  int64_t n, int64_t p, int i, int j, int k, int sub, T &f0, T &f1,
-                                                 T &f2) {
+                                                 T &f2) {  // sub in [0, SPLIT_ROWS)
     const int64_t ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
     T uu[4][3], ss[4][9];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-        const int o = sub + SPLIT_SUB * t;
+        const int o = sub + SPLIT_ROWS * t;
         if (o < 27) {
             const int ox = o / 9 - 1, oy = (o / 3) % 3 - 1, oz = o % 3 - 1;
             // a neighbour outside the grid has a zero block; read the node itself instead
@@ -259,12 +262,12 @@ __device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restr
     }
 }
 
-// Sum of the SPLIT_SUB partials of lane `lane` (fixed order); part is [3][SPLIT_SUB][32].
+// Sum of the SPLIT_ROWS partials of lane `lane` (fixed order); part is [3][SPLIT_ROWS][32].
 template <typename T>
-__device__ __forceinline__ void split_sum(const T (*part)[SPLIT_SUB][SPLIT_NODES], int lane, T &f0, T &f1, T &f2) {
+__device__ __forceinline__ void split_sum(const T (*part)[SPLIT_ROWS][SPLIT_NODES], int lane, T &f0, T &f1, T &f2) {
     f0 = f1 = f2 = T(0);
 #pragma unroll
-    for (int w = 0; w < SPLIT_SUB; ++w) {
+    for (int w = 0; w < SPLIT_ROWS; ++w) {
         f0 += part[0][w][lane];
         f1 += part[1][w][lane];
         f2 += part[2][w][lane];

@@ -312,6 +312,15 @@ class TensorProductSimulator_3D:
         check(_lib().vfem_grid_compliance_gradient(self._h, ptr(u), ptr(out)))
         return out
 
+    def adjointSensitivity(self, lam, u, loadWeight=1.0, stiffnessWeight=1.0):
+        """lam^T (loadWeight df/drho - stiffnessWeight dK/drho u) per element (fused kernel)."""
+        lam = _as_vfield(lam, self._nn)
+        u = _as_vfield(u, self._nn)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid_adjoint_sensitivity(self._h, ptr(lam), ptr(u), float(loadWeight),
+                                                   float(stiffnessWeight), ptr(out)))
+        return out
+
     def elementEnergyDensity(self, u):
         u = _as_vfield(u, self._nn)
         out = np.empty(self._nel)
