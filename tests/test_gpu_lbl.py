@@ -1,0 +1,113 @@
+"""Layer-by-layer evaluation (LayerByLayerEvaluator) against per-height oracle solves, and the
+concurrent-slot schedule against one-at-a-time: per-height compliance to 1e-8, the same PCG
+iteration counts, the averaged gradient to 1e-6 (FP64), bit-identical compliances for any
+slot count (the gradient sum differs only in its summation order), and mixed precision within
+1e-6 of FP64."""
+import numpy as np
+import pytest
+
+from voxelfem_gb300 import pyVoxelFEM as pv
+
+pytestmark = pytest.mark.gpu
+
+NE = (16, 16, 8)
+LEVELS = 3  # numLevels: two coarsenings
+INC = 3
+TOL = 1e-10
+
+
+def _configure(sim, rho):
+    if hasattr(sim, "ETensor"):
+        sim.ETensor = (1.0, 0.3)
+        sim.E_0 = 1.0
+        sim.E_min = 1e-9
+        sim.gamma = 3.0
+        sim.gravity = [0.0, -1.0, 0.0]
+    else:
+        sim.setMaterial(1.0, 0.3)
+        sim.setParams(E0=1.0, Emin=1e-9, gamma=3.0)
+        sim.setGravity([0.0, -1.0, 0.0])
+    # base plate fixed (build direction y)
+    sim.addDirichletCondition([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [float(NE[0]), 0.0, float(NE[2])], "xyz")
+    sim.setDensities(rho)
+
+
+def _gpu_sim():
+    rho = np.random.default_rng(3).uniform(0.3, 1.0, int(np.prod(NE)))
+    sim = pv.TensorProductSimulator([1, 1, 1], [[0.0, 0.0, 0.0], [float(v) for v in NE]], NE)
+    _configure(sim, rho)
+    return sim, rho
+
+
+def _oracle_lbl(oracle, rho, layers):
+    comp, its, grad = [], [], np.zeros(rho.size)
+    for lay in layers:
+        o = oracle.Sim(NE)
+        _configure(o, rho)
+        o.setFabricationMaskHeightByLayer(int(lay))
+        om = oracle.MG(o, LEVELS - 1)
+        om.setFabricationMaskHeightByLayer(int(lay))
+        f = o.buildLoadVector()
+        u = om.preconditionedConjugateGradient(np.zeros_like(f), f, 500, TOL, None, 1, 2, False)
+        comp.append(float(np.sum(f * u)))
+        its.append(om.lastIterations)
+        grad += o.complianceGradient(u)
+    return np.array(comp), np.array(its), grad
+
+
+def test_lbl_matches_oracle_and_slot_schedules_agree(gpu, oracle):
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    runs = {}
+    for slots in (1, 3):
+        ev = pv.LayerByLayerEvaluator(sim)
+        ev.run(mg, True, INC, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=slots)
+        runs[slots] = ev
+    ev1, ev3 = runs[1], runs[3]
+    np.testing.assert_array_equal(ev1.layers, [16, 13, 10, 7, 4, 1])
+    np.testing.assert_array_equal(ev1.compliances, ev3.compliances)
+    np.testing.assert_array_equal(ev1.iterations, ev3.iterations)
+    g1, g3 = ev1.gradient(), ev3.gradient()
+    assert np.max(np.abs(g1 - g3)) <= 1e-13 * np.max(np.abs(g1))
+
+    comp, its, grad = _oracle_lbl(oracle, rho, ev1.layers)
+    assert np.max(np.abs(ev1.compliances - comp) / np.abs(comp)) < 1e-8
+    np.testing.assert_array_equal(ev1.iterations, its)
+    assert abs(ev1.objective() - 0.5 * comp.sum() / len(comp)) / abs(ev1.objective()) < 1e-8
+    g = grad / len(comp)
+    assert np.max(np.abs(ev1.gradient() - g)) / np.max(np.abs(g)) < 1e-6
+    # the source simulator is untouched
+    assert sim.getFabricationMaskHeight() >= NE[1]
+
+
+def test_lbl_mixed_precision(gpu, oracle):
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    ev64 = pv.LayerByLayerEvaluator(sim)
+    ev64.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=4)
+    mg.setPrecision("mixed")
+    evm = pv.LayerByLayerEvaluator(sim)
+    evm.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=4)
+    assert np.max(np.abs(evm.compliances - ev64.compliances) / np.abs(ev64.compliances)) < 1e-6
+    assert np.max(np.abs(evm.gradient() - ev64.gradient())) / np.max(np.abs(ev64.gradient())) < 1e-5
+
+
+def test_graphs_survive_mask_changes(gpu, oracle):
+    """Captured solve graphs read the fabrication mask from device memory: solving at several
+    mask heights with one solver reproduces fresh oracle solves at each height."""
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    for lay in (16, 9, 5, 12):
+        mg.setFabricationMaskHeightByLayer(lay)
+        f = sim.buildLoadVector()
+        u = mg.preconditionedConjugateGradient(np.zeros_like(f), f, 500, TOL, None, 1, 2, False)
+        o = oracle.Sim(NE)
+        _configure(o, rho)
+        o.setFabricationMaskHeightByLayer(lay)
+        om = oracle.MG(o, LEVELS - 1)
+        om.setFabricationMaskHeightByLayer(lay)
+        fo = o.buildLoadVector()
+        np.testing.assert_allclose(f, fo, rtol=0, atol=1e-14)
+        uo = om.preconditionedConjugateGradient(np.zeros_like(fo), fo, 500, TOL, None, 1, 2, False)
+        assert mg.lastStats.iterations == om.lastIterations, lay
+        assert np.max(np.abs(u - uo)) / np.max(np.abs(uo)) < 1e-8, lay

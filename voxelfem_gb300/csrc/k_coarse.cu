@@ -62,12 +62,14 @@ __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *_
                                                               const T *__restrict__ b,
                                                               const uint8_t *__restrict__ dmask, int cx, int cy,
                                                               int cz, int forward) {
-    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    // colour nodes over the full grid; detached rows (j >= nyv) are skipped
+    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int lane = threadIdx.x & 31;
     const int64_t t = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
     int ii, jj, kk;
     decode(t, n1, n2, ii, jj, kk);
+    if (cy + 2 * jj >= g.nyv()) return;
     stencil::gs_node_warp<T>(g, S, u, b, dmask, cx + 2 * ii, cy + 2 * jj, cz + 2 * kk, forward != 0, lane);
 }
 
@@ -160,10 +162,11 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
                                 const uint8_t *__restrict__ dmask, int cx, int cy, int cz, int forward) {
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
-    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    // colour nodes over the full grid; detached rows (j >= nyv) are skipped
+    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t t = blockIdx.x * (int64_t)SPLIT_NODES + lane;
-    const bool valid = n1 > 0 && t < (int64_t)n0 * n1 * n2;
+    bool valid = n1 > 0 && t < (int64_t)n0 * n1 * n2;
     int i = cx, j = cy, k = cz;
     if (valid) {
         int ii, jj, kk;
@@ -171,6 +174,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
         i = cx + 2 * ii;
         j = cy + 2 * jj;
         k = cz + 2 * kk;
+        valid = j < g.nyv();
     }
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const int64_t p = stencil::colour_pos(g, i, j, k);
@@ -209,9 +213,10 @@ __global__ void __launch_bounds__(BS) restrict_kernel(Geom gf, Geom gc, const T 
     const int cyv = gc.nyv();
     const int rows = cyv < gc.nn[1] ? cyv + 1 : cyv;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (t >= (int64_t)gc.nn[0] * rows * gc.nn[2]) return;
+    if (t >= gc.NN) return;
     int i, j, k;
-    decode(t, rows, gc.nn[2], i, j, k);
+    decode(t, gc.nn[1], gc.nn[2], i, j, k);
+    if (j >= rows) return;
     stencil::restrict_node<T>(gf, gc, fine, coarse, i, j, k);
 }
 
@@ -221,9 +226,10 @@ __global__ void __launch_bounds__(BS) interp_kernel(Geom gf, Geom gc, const T *_
                                                     T *__restrict__ fine) {
     const int rows = Accumulate ? gf.nyv() : gf.nn[1];
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (t >= (int64_t)gf.nn[0] * rows * gf.nn[2]) return;
+    if (t >= gf.NN) return;
     int f[3];
-    decode(t, rows, gf.nn[2], f[0], f[1], f[2]);
+    decode(t, gf.nn[1], gf.nn[2], f[0], f[1], f[2]);
+    if (f[1] >= rows) return;
     stencil::interp_node<T, Accumulate>(gf, gc, coarse, fine, f);
 }
 
@@ -239,11 +245,12 @@ __global__ void zero_dirichlet_kernel(Geom g, T *__restrict__ u, const uint8_t *
 }
 
 template <typename T>
-__global__ void masked_zero_kernel(Geom g, T *__restrict__ u, int rows) {
+__global__ void masked_zero_kernel(Geom g, T *__restrict__ u, int margin) {
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
-    if (t >= (int64_t)g.nn[0] * rows * g.nn[2]) return;
+    if (t >= g.NN) return;
     int i, j, k;
-    decode(t, rows, g.nn[2], i, j, k);
+    decode(t, g.nn[1], g.nn[2], i, j, k);
+    if (j >= g.nyv() + margin) return;
     const int64_t n = g.node(i, j, k);
     u[n] = T(0);
     u[g.ld + n] = T(0);
@@ -276,7 +283,7 @@ __global__ void __launch_bounds__(576) ke_level1_kernel(Geom g1, Geom g0, const 
     if (t < 8) sE[t] = Y0[g0.elem(2 * ei + ((t >> 2) & 1), 2 * ej + ((t >> 1) & 1), 2 * ek + (t & 1))];
     __syncthreads();
     T acc = T(0);
-    if (ej < g1.firstMaskedE) {
+    if (ej < g1.maskedE()) {
 #pragma unroll
         for (int fi = 0; fi < 8; ++fi) acc += sE[fi] * Kc[fi * 576 + t];
     }
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(ROW) stencil_level1_kernel(Geom g1, Geom g0, c
         const int a = (slot >> 2) & 1, b = (slot >> 1) & 1, cc = slot & 1;
         const int ei = i - a, ej = j - b, ek = k - cc;
         T E = T(0);
-        if (ei >= 0 && ej >= 0 && ek >= 0 && ei < g1.ne[0] && ej < g1.ne[1] && ek < g1.ne[2] && ej < g1.firstMaskedE)
+        if (ei >= 0 && ej >= 0 && ek >= 0 && ei < g1.ne[0] && ej < g1.ne[1] && ek < g1.ne[2] && ej < g1.maskedE())
             E = Y0[g0.elem(2 * ei + ((fi >> 2) & 1), 2 * ej + ((fi >> 1) & 1), 2 * ek + (fi & 1))];
         sE[slot][fi] = E;
     }
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0
                 if (ma < 0 || ma > 1 || mb < 0 || mb > 1 || mc < 0 || mc > 1) continue;
                 const int ei = i - a, ej = j - b, ek = k - cc;
                 if (ei < 0 || ej < 0 || ek < 0 || ei >= g1.ne[0] || ej >= g1.ne[1] || ek >= g1.ne[2]) continue;
-                if (ej >= g1.firstMaskedE) continue;
+                if (ej >= g1.maskedE()) continue;
                 T E[8];
 #pragma unroll
                 for (int fi = 0; fi < 8; ++fi)
@@ -392,7 +399,7 @@ __global__ void __launch_bounds__(576) ke_level2_kernel(Geom g2, Geom g1, Geom g
             const int ej = (int)(r % g2.ne[1]), ei = (int)(r / g2.ne[1]);
             const int c = f >> 3, fi = f & 7;
             const int i1 = 2 * ei + ((c >> 2) & 1), j1 = 2 * ej + ((c >> 1) & 1), k1 = 2 * ek + (c & 1);
-            if (ej < g2.firstMaskedE && j1 < g1.firstMaskedE)
+            if (ej < g2.maskedE() && j1 < g1.maskedE())
                 v = Y0[g0.elem(2 * i1 + ((fi >> 2) & 1), 2 * j1 + ((fi >> 1) & 1), 2 * k1 + (fi & 1))];
         }
         sY[eb][f] = v;
@@ -426,7 +433,7 @@ __global__ void __launch_bounds__(576) ke_coarsen_kernel(Geom gc, Geom gf, const
     const int ek = (int)(e % gc.ne[2]);
     const int64_t q = e / gc.ne[2];
     const int ej = (int)(q % gc.ne[1]), ei = (int)(q / gc.ne[1]);
-    const bool masked = ej >= gc.firstMaskedE;
+    const bool masked = ej >= gc.maskedE();
     T acc = T(0);
     const int row = t / 24, col = t % 24;
     for (int fi = 0; fi < 8; ++fi) {
@@ -567,7 +574,7 @@ template <typename T>
 void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                              bool rows, cudaStream_t st) {
     const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
-    const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
+    const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
     if (rows)
         gs_stencil_color_kernel<T><<<gridFor(n0 * n1 * n2, WPB), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
@@ -580,16 +587,13 @@ void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const 
 
 template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st) {
-    const int cyv = gc.nyv();
-    const int rows = cyv < gc.nn[1] ? cyv + 1 : cyv;
-    restrict_kernel<T><<<gridFor((int64_t)gc.nn[0] * rows * gc.nn[2], BS), BS, 0, st>>>(gf, gc, fine, coarse);
+    restrict_kernel<T><<<gridFor(gc.NN, BS), BS, 0, st>>>(gf, gc, fine, coarse);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_interpolate(const Geom &gf, const Geom &gc, const T *coarse, T *fine, bool accumulate, cudaStream_t st) {
-    const int rows = accumulate ? gf.nyv() : gf.nn[1];
-    const unsigned grid = gridFor((int64_t)gf.nn[0] * rows * gf.nn[2], BS);
+    const unsigned grid = gridFor(gf.NN, BS);
     if (accumulate) interp_kernel<T, true><<<grid, BS, 0, st>>>(gf, gc, coarse, fine);
     else interp_kernel<T, false><<<grid, BS, 0, st>>>(gf, gc, coarse, fine);
     VFEM_LAUNCH_CHECK();
@@ -603,9 +607,7 @@ void launch_zero_dirichlet(const Geom &g, T *u, const uint8_t *dmask, cudaStream
 
 template <typename T>
 void launch_masked_zero(const Geom &g, T *u, int margin, cudaStream_t st) {
-    int rows = g.nyv() + margin;
-    if (rows > g.nn[1]) rows = g.nn[1];
-    masked_zero_kernel<T><<<gridFor((int64_t)g.nn[0] * rows * g.nn[2], BS), BS, 0, st>>>(g, u, rows);
+    masked_zero_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, u, margin);
     VFEM_LAUNCH_CHECK();
 }
 

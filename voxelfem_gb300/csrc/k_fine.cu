@@ -366,12 +366,14 @@ template <typename T, bool Cube>
 __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kernel(Geom g, const T *__restrict__ Y, T *u,
                                                            const T *__restrict__ b, const uint8_t *__restrict__ dmask,
                                                            int cx, int cy, int cz, int forward, const Mat24<T> K) {
-    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    // colour nodes over the full grid; detached rows (j >= nyv) are skipped
+    const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n1 <= 0 || t >= (int64_t)n0 * n1 * n2) return;
     int ii, jj, kk;
     decode3(t, n1, n2, ii, jj, kk);
     const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
+    if (j >= g.nyv()) return;
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const uint8_t dm = dmask[n];
     if (dm == 7) return;
@@ -562,7 +564,7 @@ __global__ void young_kernel(Geom g, const double *__restrict__ rho, T *__restri
     if (e >= g.NE) return;
     const int ej = (int)(((uint32_t)e / (uint32_t)g.ne[2]) % (uint32_t)g.ne[1]);
     double v;
-    if (masking && ej >= g.firstMaskedE) {
+    if (masking && ej >= g.maskedE()) {
         v = 0.0;
     } else {
         const double r = rho[e];
@@ -596,7 +598,7 @@ __global__ void __launch_bounds__(BS) compliance_grad_kernel(Geom g, const doubl
     if (e >= g.NE) return;
     int ei, ej, ek;
     decode3(e, g.ne[1], g.ne[2], ei, ej, ek);
-    if (ej >= g.firstMaskedE) { grad[e] = 0.0; return; }
+    if (ej >= g.maskedE()) { grad[e] = 0.0; return; }
     const int64_t base = g.node(ei, ej, ek), ld = g.ld;
     const int64_t sx = (int64_t)g.nn[1] * g.nn[2], sy = g.nn[2];
     double ue[24], le[24];
@@ -670,7 +672,7 @@ __global__ void gravity_load_kernel(Geom g, const double *__restrict__ rho, doub
             for (int c = 1; c >= 0; --c) {
                 const int ei = i - a, ej = j - b, ek = k - c;
                 if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ne[0] || ej >= g.ne[1] || ek >= g.ne[2]) continue;
-                if (ej >= g.firstMaskedE) continue;
+                if (ej >= g.maskedE()) continue;
                 const double w = 0.125 * rho[g.elem(ei, ej, ek)] * vol;
                 acc0 += gx * w;
                 acc1 += gy * w;
@@ -741,7 +743,7 @@ template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                           const Mat24<T> &K0, cudaStream_t st) {
     const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
-    const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nyv() - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
+    const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
     if (sizeof(T) == 4 && K0.isCube)
         gs_fine_color_kernel<T, true><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz,

@@ -241,9 +241,11 @@ __global__ void zero_upper_kernel(double *A, int n) {
 }
 
 // ---------------- coarse solve ----------------
+// nfree is read from device memory (it changes with the fabrication mask under captured graphs)
 template <typename T>
-__global__ void gather_free_kernel(const Geom g, const int *__restrict__ freeIdx, int nfree, const T *__restrict__ b,
-                                   double *__restrict__ out) {
+__global__ void gather_free_kernel(const Geom g, const int *__restrict__ freeIdx, const int *__restrict__ nfreeDev,
+                                   const T *__restrict__ b, double *__restrict__ out) {
+    const int nfree = *nfreeDev;
     const int t = blockIdx.x * BS + threadIdx.x;
     if (t >= nfree) return;
     const int d = freeIdx[t];
@@ -252,7 +254,8 @@ __global__ void gather_free_kernel(const Geom g, const int *__restrict__ freeIdx
 
 template <typename T>
 __global__ void symv_scatter_kernel(const Geom g, const double *__restrict__ Ainv, const int *__restrict__ freeIdx,
-                                    int nfree, const double *__restrict__ bf, T *__restrict__ x) {
+                                    const int *__restrict__ nfreeDev, const double *__restrict__ bf, T *__restrict__ x) {
+    const int nfree = *nfreeDev;
     const int row = blockIdx.x * (BS / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= nfree) return;
@@ -267,10 +270,11 @@ __global__ void symv_scatter_kernel(const Geom g, const double *__restrict__ Ain
 }
 
 // ---------------- reductions and CG vector kernels ----------------
+// m-th node of the nondetached rows (rows < nn[1]) in node order; 32-bit division (counts < 2^31)
 __device__ __forceinline__ int64_t masked_node(const Geom &g, int64_t m, int rows) {
-    const int64_t per = (int64_t)rows * g.nn[2];
-    const int64_t i = m / per, rem = m % per;
-    return i * ((int64_t)g.nn[1] * g.nn[2]) + rem;
+    const uint32_t per = (uint32_t)rows * (uint32_t)g.nn[2];
+    const uint32_t i = (uint32_t)m / per, rem = (uint32_t)m - i * per;
+    return (int64_t)i * ((int64_t)g.nn[1] * g.nn[2]) + rem;
 }
 
 template <typename Ta, typename Tb>
@@ -458,13 +462,74 @@ void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t
 }
 
 template <typename T>
-void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, int nfree, const T *b, T *x,
-                         double *scratch, cudaStream_t st) {
+void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, const int *nfreeDev, int nfreeCap,
+                         const T *b, T *x, double *scratch, cudaStream_t st) {
     launch_fill<T>(x, T(0), 3 * g.ld, st);
-    if (nfree <= 0) return;
-    gather_free_kernel<T><<<gridFor(nfree, BS), BS, 0, st>>>(g, freeIdx, nfree, b, scratch);
+    if (nfreeCap <= 0) return;
+    gather_free_kernel<T><<<gridFor(nfreeCap, BS), BS, 0, st>>>(g, freeIdx, nfreeDev, b, scratch);
     VFEM_LAUNCH_CHECK();
-    symv_scatter_kernel<T><<<gridFor(nfree, BS / 32), BS, 0, st>>>(g, Ainv, freeIdx, nfree, scratch, x);
+    symv_scatter_kernel<T><<<gridFor(nfreeCap, BS / 32), BS, 0, st>>>(g, Ainv, freeIdx, nfreeDev, scratch, x);
+    VFEM_LAUNCH_CHECK();
+}
+
+// Loop control of the device-resident PCG (a conditional WHILE node of a CUDA graph):
+// sc[5] |r|^2, sc[7] |b|^2, sc[8] tol^2, sc[9] iterations done, sc[10] iteration limit,
+// sc[11] iteration at which the residual became NaN (-1: the initial one). The loop continues
+// while |r|^2 > tol^2 |b|^2 and the limit is not reached (MultigridSolver.hh:1068-1070).
+__global__ void cg_loop_control_kernel(cudaGraphConditionalHandle h, double *sc, int initial) {
+    const double rsq = sc[5];
+    double it = sc[9];
+    if (!initial) {
+        it += 1.0;
+        sc[9] = it;
+    }
+    unsigned cont = 1;
+    if (isnan(rsq)) {
+        sc[11] = initial ? -1.0 : it;
+        cont = 0;
+    } else if (!(rsq > sc[8] * sc[7]) || it >= sc[10]) {
+        cont = 0;
+    }
+    cudaGraphSetConditional(h, cont);
+}
+
+void launch_cg_loop_control(cudaGraphConditionalHandle h, double *sc, bool initial, cudaStream_t st) {
+    cg_loop_control_kernel<<<1, 1, 0, st>>>(h, sc, initial ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+// CG scalars before the first iteration; |r|^2 (sc[5]) and |b|^2 (sc[7]) are already in place
+__global__ void cg_init_kernel(double *sc, double tol2, double maxIter) {
+    sc[0] = 0.0;
+    sc[6] = 1.0;
+    sc[8] = tol2;
+    sc[9] = 0.0;
+    sc[10] = maxIter;
+    sc[11] = 0.0;
+}
+
+void launch_cg_init(double *sc, double tol2, double maxIter, cudaStream_t st) {
+    cg_init_kernel<<<1, 1, 0, st>>>(sc, tol2, maxIter);
+    VFEM_LAUNCH_CHECK();
+}
+
+__global__ void axpy_kernel(int64_t n, double a, const double *__restrict__ xv, double *__restrict__ yv) {
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) yv[t] += a * xv[t];
+}
+
+void launch_axpy(int64_t n, double a, const double *x, double *y, cudaStream_t st) {
+    if (n <= 0) return;
+    axpy_kernel<<<std::min<unsigned>(gridFor(n, BS), 4 * 152), BS, 0, st>>>(n, a, x, y);
+    VFEM_LAUNCH_CHECK();
+}
+
+__global__ void set_pair_kernel(int *p, int a, int b) {
+    p[0] = a;
+    p[1] = b;
+}
+
+void launch_set_pair(int *p, int a, int b, cudaStream_t st) {
+    set_pair_kernel<<<1, 1, 0, st>>>(p, a, b);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -525,10 +590,10 @@ template void launch_dense_from_stencil<double>(const Geom &, const double *, co
                                                cudaStream_t);
 template void launch_dense_from_stencil<float>(const Geom &, const float *, const int *, double *, int, bool,
                                               cudaStream_t);
-template void launch_coarse_solve<double>(const Geom &, const double *, const int *, int, const double *, double *,
-                                          double *, cudaStream_t);
-template void launch_coarse_solve<float>(const Geom &, const double *, const int *, int, const float *, float *,
-                                         double *, cudaStream_t);
+template void launch_coarse_solve<double>(const Geom &, const double *, const int *, const int *, int, const double *,
+                                          double *, double *, cudaStream_t);
+template void launch_coarse_solve<float>(const Geom &, const double *, const int *, const int *, int, const float *,
+                                         float *, double *, cudaStream_t);
 template void launch_masked_dot_partials<double, double>(const Geom &, const double *, const double *, double *,
                                                          cudaStream_t);
 template void launch_masked_dot_partials<float, float>(const Geom &, const float *, const float *, double *,

@@ -43,8 +43,24 @@ struct Geom {
     int64_t ld;      // leading dimension of a nodal SoA vector (component stride), padded
     int firstMaskedE;  // first masked element layer along y (or LAYER_MASK_NONE)
     int firstDetN;     // first detached node layer along y
-    __host__ __device__ int nyv() const { return firstDetN < nn[1] ? firstDetN : nn[1]; }  // nondetached node rows
-    __host__ __device__ int nev() const { return firstMaskedE < ne[1] ? firstMaskedE : ne[1]; }
+    // Device copy {firstMaskedE, firstDetN} of the level's mask. When set, kernels read the
+    // mask from it, launch over the full grid and skip the detached rows, so a captured CUDA
+    // graph stays valid when the fabrication mask height changes.
+    const int *dyn = nullptr;
+    __host__ __device__ int detN() const {
+#if defined(__CUDA_ARCH__)
+        if (dyn) return dyn[1];
+#endif
+        return firstDetN;
+    }
+    __host__ __device__ int maskedE() const {
+#if defined(__CUDA_ARCH__)
+        if (dyn) return dyn[0];
+#endif
+        return firstMaskedE;
+    }
+    __host__ __device__ int nyv() const { const int d = detN(); return d < nn[1] ? d : nn[1]; }  // nondetached node rows
+    __host__ __device__ int nev() const { const int m = maskedE(); return m < ne[1] ? m : ne[1]; }
     __host__ __device__ int64_t node(int i, int j, int k) const { return ((int64_t)i * nn[1] + j) * nn[2] + k; }
     __host__ __device__ int64_t elem(int i, int j, int k) const { return ((int64_t)i * ne[1] + j) * ne[2] + k; }
     // Zero-padded element arrays carry one ghost layer on every side: element (i, j, k),

@@ -90,6 +90,9 @@ Grid::Grid(const int ne[3], const double bmin_[3], const double bmax_[3]) {
     force_h.assign(3 * g.NN, 0.0);
     dmask.alloc(g.NN);
     dval.alloc(3 * g.NN);
+    dynMask.alloc(2);
+    g.dyn = dynMask.p;
+    uploadMask();
     uploadBC();
     setETensor(1.0, 0.0);
     updateYoungModuli();
@@ -261,6 +264,7 @@ void Grid::applySymmetry(const int axes[3], const int maxFace[3]) {
 }
 
 void Grid::setForces(const double *f) {
+    forceDevValid = false;
     if (isDevicePtr(f)) VFEM_CUDA(cudaMemcpy(force_h.data(), f, 3 * g.NN * sizeof(double), cudaMemcpyDeviceToHost));
     else std::memcpy(force_h.data(), f, 3 * g.NN * sizeof(double));
 }
@@ -282,9 +286,12 @@ void Grid::setMaskHeight(double hgt, bool update) {
     const double fl = std::ceil(hgt / h[BUILD_DIR] - 1e-10);
     g.firstMaskedE = (int)fl;
     g.firstDetN = g.firstMaskedE + 1;
+    uploadMask();
     ++maskVersion;
     if (update) updateYoungModuli();
 }
+
+void Grid::uploadMask() { launch_set_pair(dynMask.p, g.firstMaskedE, g.firstDetN, stream); }
 
 void Grid::setMaskLayer(int64_t l) { setMaskHeight(h[BUILD_DIR] * (double)l, true); }
 
@@ -302,6 +309,38 @@ void Grid::buildLoadDev(double *f) {
     if (grav[0] * grav[0] + grav[1] * grav[1] + grav[2] * grav[2] != 0)
         launch_build_gravity_load(g, rho.p, f, grav, vol(), stream);
     VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::buildLoadAsync(double *f) {
+    if (!forceDevValid) {
+        forceDev.alloc(3 * g.NN);
+        VFEM_CUDA(cudaMemcpy(forceDev.p, force_h.data(), 3 * g.NN * sizeof(double), cudaMemcpyHostToDevice));
+        forceDevValid = true;
+    }
+    VFEM_CUDA(cudaMemcpyAsync(f, forceDev.p, 3 * g.NN * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    if (grav[0] * grav[0] + grav[1] * grav[1] + grav[2] * grav[2] != 0)
+        launch_build_gravity_load(g, rho.p, f, grav, vol(), stream);
+}
+
+std::unique_ptr<Grid> Grid::clone() const {
+    auto c = std::make_unique<Grid>(g.ne, bmin, bmax);
+    c->setETensor(Eyoung, nu);
+    c->E0 = E0;
+    c->Emin = Emin;
+    c->gamma = gamma;
+    c->q = q;
+    c->law = law;
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+    VFEM_CUDA(cudaMemcpy(c->rho.p, rho.p, g.NE * sizeof(double), cudaMemcpyDeviceToDevice));
+    c->dmask_h = dmask_h;
+    c->dval_h = dval_h;
+    c->force_h = force_h;
+    c->uploadBC();
+    for (int d = 0; d < 3; ++d) c->grav[d] = grav[d];
+    if (maskH < std::numeric_limits<double>::infinity()) c->setMaskHeight(maskH, false);
+    c->updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(c->stream));
+    return c;
 }
 
 void Grid::buildLoad(double *out) {
@@ -367,6 +406,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     for (int l = 1; l < L(); ++l) {
         lv[l].dmask.alloc(lv[l].g.NN);
         VFEM_CUDA(cudaMemcpy(lv[l].dmask.p, lv[l].dmask_h.data(), lv[l].g.NN, cudaMemcpyHostToDevice));
+        lv[l].dyn.alloc(2);
+        lv[l].g.dyn = lv[l].dyn.p;
     }
     // propagate an existing fabrication mask (MultigridSolver.hh:1022-1028)
     if (fine->maskH < std::numeric_limits<double>::infinity()) {
@@ -376,6 +417,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
             lv[l].g.firstDetN = lv[l].g.firstMaskedE + 1;
         }
     }
+    for (int l = 1; l < L(); ++l) launch_set_pair(lv[l].dyn.p, lv[l].g.firstMaskedE, lv[l].g.firstDetN, fine->stream);
+    nfreeDev.alloc(1);
     const int64_t NN = fine->g.NN;
     rbuf.alloc(3 * NN);
     s.alloc(3 * NN);
@@ -400,6 +443,9 @@ void MG::clearGraphs() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
     graphKernels.clear();
+    for (auto &kv : loopGraphs) cudaGraphExecDestroy(kv.second);
+    loopGraphs.clear();
+    loopKernels.clear();
     graphX = nullptr;
 }
 
@@ -458,18 +504,22 @@ void MG::setupCoarsestIndex() {
     if (L() == 1 && fine->dvalNonzero) throw Error(ERR_ARG, "Nonzero Dirichlet constraints currently unsupported");
     if (fr.size() > 30000) throw Error(ERR_ARG, "coarsest level too large for the dense direct solve; use more coarsening levels");
     const int nf = (int)fr.size();
-    if (nf != nfree || !freeIdx.p) {
-        clearGraphs();
-        nfree = nf;
-        freeIdx.alloc(std::max(nf, 1));
-        Ainv.alloc(std::max<size_t>((size_t)nf * nf, 1));
-        work.alloc(std::max<size_t>(dense_inverse_work_size(nf), 1));
-        cscratch.alloc(std::max(nf, 1));
+    if (nf > nfreeCap || !freeIdx.p) {
+        clearGraphs();  // buffers baked into graphs move
+        nfreeCap = std::max(nf, 1);
+        freeIdx.alloc(nfreeCap);
+        Ainv.alloc((size_t)nfreeCap * nfreeCap);
+        work.alloc(dense_inverse_work_size(nfreeCap));
+        cscratch.alloc(nfreeCap);
         status.alloc(1);
     }
+    nfree = nf;
     redIdx.alloc(red.size());
-    VFEM_CUDA(cudaMemcpy(redIdx.p, red.data(), red.size() * sizeof(int), cudaMemcpyHostToDevice));
-    if (nf) VFEM_CUDA(cudaMemcpy(freeIdx.p, fr.data(), fr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    cudaStream_t st = fine->stream;
+    VFEM_CUDA(cudaMemcpyAsync(redIdx.p, red.data(), red.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (nf) VFEM_CUDA(cudaMemcpyAsync(freeIdx.p, fr.data(), fr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_set_pair(nfreeDev.p, nf, 0, st);
+    VFEM_CUDA(cudaStreamSynchronize(st));  // host vectors red / fr go out of scope
     stiffnessValid = false;
 }
 
@@ -489,8 +539,10 @@ void MG::setMaskLayer(int64_t layer) {
         const double fl = std::ceil(fine->maskH / lv[l].h[BUILD_DIR] - 1e-10);
         lv[l].g.firstMaskedE = (int)fl;
         lv[l].g.firstDetN = lv[l].g.firstMaskedE + 1;
+        launch_set_pair(lv[l].dyn.p, lv[l].g.firstMaskedE, lv[l].g.firstDetN, fine->stream);
     }
-    clearGraphs();
+    // captured graphs read the mask, the free-DOF count and the free-DOF list from device
+    // memory, so they stay valid; only a larger coarsest system reallocates
     setupCoarsestIndex();
 }
 
@@ -683,12 +735,12 @@ void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
         }
         launch_tail_down<T>(P, st);
         auto &Dc = lv.back().data<T>();
-        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
         launch_tail_up<T>(P, st);
         return;
     }
     if (l == L() - 1) {
-        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfree, D.b.p, D.x.p, cscratch.p, st);
+        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
@@ -710,7 +762,7 @@ void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (l == L() - 1) {
-        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfree, D.b.p, D.x.p, cscratch.p, st);
+        launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
     auto &Dc = lv[l + 1].data<T>();
@@ -741,7 +793,7 @@ void MG::preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg
 }
 
 // One PCG iteration (MultigridSolver.hh:1108-1144), enqueued without host synchronisation.
-void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
+void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror) {
     cudaStream_t st = fine->stream;
     const Geom &g = lv[0].g;
     if (mgIter > 0) {
@@ -770,7 +822,69 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
     launch_cg_alpha(partials.p, nb, sc.p, st);
     launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
     launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
-    VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (hostMirror) VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+}
+
+static uint64_t countKernelNodes(cudaGraph_t graph) {
+    size_t n = 0;
+    VFEM_CUDA(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    VFEM_CUDA(cudaGraphGetNodes(graph, nodes.data(), &n));
+    uint64_t k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType ty;
+        VFEM_CUDA(cudaGraphNodeGetType(nd, &ty));
+        if (ty == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+// [loop control (initial)] -> WHILE( [one PCG iteration] -> [loop control] )
+cudaGraphExec_t MG::loopGraph(const GraphKey &key, double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
+    if (graphX != x) clearGraphs();
+    auto it = loopGraphs.find(key);
+    if (it != loopGraphs.end()) return it->second;
+    cudaStream_t st = fine->stream;
+    cudaGraph_t top;
+    VFEM_CUDA(cudaGraphCreate(&top, 0));
+    cudaGraphExec_t exec = nullptr;
+    try {
+        cudaGraphConditionalHandle h;
+        VFEM_CUDA(cudaGraphConditionalHandleCreate(&h, top, 0, cudaGraphCondAssignDefault));
+        VFEM_CUDA(cudaStreamBeginCaptureToGraph(st, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launch_cg_loop_control(h, sc.p, true, st);
+        VFEM_CUDA(cudaStreamEndCapture(st, &top));
+        cudaGraphNode_t init;
+        size_t n = 1;
+        VFEM_CUDA(cudaGraphGetNodes(top, &init, &n));
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t loop;
+        VFEM_CUDA(cudaGraphAddNode(&loop, top, &init, nullptr, 1, &p));
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        VFEM_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+            cgIteration(x, mgIter, sweeps, fmg, false);
+            launch_cg_loop_control(h, sc.p, false, st);
+        } catch (...) {
+            cudaStreamEndCapture(st, &body);
+            throw;
+        }
+        VFEM_CUDA(cudaStreamEndCapture(st, &body));
+        const uint64_t k = countKernelNodes(body);
+        VFEM_CUDA(cudaGraphInstantiate(&exec, top, 0));
+        launchCounter() -= k + 1;  // the captures launched nothing
+        loopKernels[key] = k;
+    } catch (...) {
+        cudaGraphDestroy(top);
+        throw;
+    }
+    cudaGraphDestroy(top);
+    graphX = x;
+    return loopGraphs.emplace(key, exec).first->second;
 }
 
 static double readScalar(double *dev, cudaStream_t st) {
@@ -780,10 +894,67 @@ static double readScalar(double *dev, cudaStream_t st) {
     return v;
 }
 
+void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                  bool dirichletSatisfied) {
+    syncFineGeom(*this);
+    if (L() == 1) throw Error(ERR_ARG, "the asynchronous solve needs at least one coarsening level");
+    if (pending) throw Error(ERR_STATE, "a solve is already in flight on this solver");
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
+    if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
+    launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
+    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF) {
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+        launch_split_df(x, dhi.p, dlo.p, 3 * g.ld, st);
+        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, x, rbuf.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st, b);
+    } else {
+        launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
+    }
+    launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
+    launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
+    launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
+    if (precision == PREC_MIXED) {
+        fine->youngF();
+        fine->youngFPad();
+        const float *yh, *yl;
+        if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
+    }
+    allocLevels();
+    if (mgIter > 0) ensureStiffness();
+    pendingKey = GraphKey{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
+    VFEM_CUDA(cudaGraphLaunch(loopGraph(pendingKey, x, mgIter, sweeps, fmg), st));
+    pending = true;
+}
+
+PcgStats MG::pcgFinish() {
+    if (!pending) throw Error(ERR_STATE, "no solve in flight");
+    pending = false;
+    cudaStream_t st = fine->stream;
+    VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    PcgStats stats;
+    stats.iterations = (int64_t)hostSc[9];
+    stats.rsq = hostSc[5];
+    stats.bnorm2 = hostSc[7];
+    launchCounter() += 1 + (loopKernels[pendingKey] + 1) * (uint64_t)stats.iterations;
+    if (hostSc[11] < 0.0) throw Error(ERR_NAN, "NaN encountered");
+    if (hostSc[11] > 0.0) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string((int64_t)hostSc[11]));
+    stats.relres = stats.bnorm2 > 0 ? std::sqrt(stats.rsq / stats.bnorm2) : std::sqrt(stats.rsq);
+    return stats;
+}
+
 // MultigridSolver.hh:1047-1152
 PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
                        bool fmg, bool dirichletSatisfied, PcgCallback cb, void *user) {
     syncFineGeom(*this);
+    if (useGraphs && deviceLoop && !cb && L() > 1) {
+        // one graph launch runs every iteration (conditional WHILE node)
+        pcgStart(x, b, maxIter, tol, mgIter, sweeps, fmg, dirichletSatisfied);
+        return pcgFinish();
+    }
     cudaStream_t st = fine->stream;
     const Geom &g = lv[0].g;
     PcgStats stats;
@@ -810,7 +981,7 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
         // direct solve branch (MultigridSolver.hh:1056-1064)
         if (!(rsq < tol * tol * bnorm2)) {
             ensureStiffness();
-            if (precision == PREC_FP64) launch_coarse_solve<double>(g, Ainv.p, freeIdx.p, nfree, b, x, cscratch.p, st);
+            if (precision == PREC_FP64) launch_coarse_solve<double>(g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, b, x, cscratch.p, st);
             else throw Error(ERR_ARG, "numCoarseningLevels == 0 requires FP64 precision");
             launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
             launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
@@ -841,8 +1012,7 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
         if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
         allocLevels();
     }
-    const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec, fine->maskVersion,
-                       nfree};
+    const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
     bool updated = false;
     int64_t i = 0;
     while ((i++ < maxIter) && (rsq > tol * tol * bnorm2)) {
@@ -997,7 +1167,7 @@ void MG::levelOp(int l, int op, const double *a, const double *b, double *out, b
         auto &Dc = lv.back().data<T>();
         const int64_t nc = 3 * lv.back().g.NN;
         toT<T>(a, Dc.b.p, nc, st);
-        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+        launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
         fromT<T>(Dc.x.p, out, nc, st);
         break;
     }
@@ -1181,6 +1351,7 @@ double Problem::objective() {
     cudaStream_t st = grid->stream;
     Geom gall = grid->g;
     gall.firstDetN = (int)LAYER_MASK_NONE;  // 0.5 f.u over all nodes (TopologyOptimizationObjective.hh:41-43)
+    gall.dyn = nullptr;                      // use the override above, not the grid's device mask
     launch_masked_dot_partials<double, double>(gall, f.p, u.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, partials.p + REDUCE_BLOCKS, st);
     double v = 0;
@@ -1460,7 +1631,7 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
         } else {
             auto &Dc = lv.back().data<T>();
             timed("coarsest:solve", [&] {
-                launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfree, Dc.b.p, Dc.x.p, cscratch.p, st);
+                launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
             });
         }
         for (int l = ts - 1; l >= 0; --l) {

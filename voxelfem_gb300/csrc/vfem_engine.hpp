@@ -59,6 +59,8 @@ public:
     std::vector<uint8_t> dmask_h;
     std::vector<double> dval_h;   // SoA, stride NN
     std::vector<double> force_h;  // dense nodal forces, SoA
+    DevBuf<int> dynMask;  // device {firstMaskedE, firstDetN} (Geom::dyn)
+    void uploadMask();
     DevBuf<uint8_t> dmask;
     DevBuf<double> dval;
     bool dvalNonzero = false;
@@ -91,7 +93,12 @@ public:
 
     // device-side helpers
     void buildLoadDev(double *f_dev);
+    void buildLoadAsync(double *f_dev);  // stream-ordered, no host synchronisation
     void uploadBC();
+    DevBuf<double> forceDev;  // device copy of force_h (refreshed by setForces)
+    bool forceDevValid = false;
+    // a new grid with the same geometry, material, densities, boundary conditions, loads and mask
+    std::unique_ptr<Grid> clone() const;
 };
 
 template <typename T>
@@ -105,6 +112,7 @@ struct Level {
     bool rows = true;  // stencil layout: node-contiguous rows (small levels) or planes (large)
     std::vector<uint8_t> dmask_h;
     DevBuf<uint8_t> dmask;
+    DevBuf<int> dyn;  // device {firstMaskedE, firstDetN} (Geom::dyn)
     LevelData<double> d64;
     LevelData<float> d32;
     template <typename T>
@@ -163,6 +171,13 @@ public:
     PcgStats pcg(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
                  bool dirichletSatisfied, PcgCallback cb, void *user);
     // PCG on device-resident FP64 buffers (no staging); used by pcg() and by the problem layer.
+    // Asynchronous device-resident PCG (at least one coarsening): pcgStart enqueues the whole
+    // solve on the grid's stream (host synchronisation only inside a stiffness update);
+    // pcgFinish waits for it and returns the statistics.
+    void pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                  bool dirichletSatisfied);
+    PcgStats pcgFinish();
+    bool pending = false;
     PcgStats pcgDevice(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
                        bool fmg, bool dirichletSatisfied, PcgCallback cb, void *user);
     double lastTrueRelres = -1;
@@ -176,7 +191,8 @@ public:
     std::vector<std::pair<std::string, double>> profile(int64_t mgIter, int64_t sweeps, int reps);
 
     // coarsest level
-    int nfree = 0;
+    int nfree = 0, nfreeCap = 0;  // free coarsest DOFs now / allocated for
+    DevBuf<int> nfreeDev;          // device copy of nfree (read by the coarse solve)
     DevBuf<int> freeIdx, redIdx;
     DevBuf<double> Ainv, work, cscratch;
     DevBuf<int> status;
@@ -198,15 +214,20 @@ public:
     struct GraphKey {
         int64_t mgIter, sweeps;
         int fmg, sym, prec, matvec;
-        uint64_t maskVersion;
-        int nfree;
         bool operator<(const GraphKey &o) const {
-            return std::tie(mgIter, sweeps, fmg, sym, prec, matvec, maskVersion, nfree) <
-                   std::tie(o.mgIter, o.sweeps, o.fmg, o.sym, o.prec, o.matvec, o.maskVersion, o.nfree);
+            return std::tie(mgIter, sweeps, fmg, sym, prec, matvec) <
+                   std::tie(o.mgIter, o.sweeps, o.fmg, o.sym, o.prec, o.matvec);
         }
     };
+    GraphKey pendingKey{};  // graph of the solve in flight
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::map<GraphKey, uint64_t> graphKernels;  // kernel nodes per captured graph
+    // device-resident PCG: a graph whose conditional WHILE node repeats one iteration until
+    // convergence, so a solve is one graph launch with no host round trip per iteration
+    std::map<GraphKey, cudaGraphExec_t> loopGraphs;
+    std::map<GraphKey, uint64_t> loopKernels;  // kernel nodes per loop body
+    bool deviceLoop = true;
+    cudaGraphExec_t loopGraph(const GraphKey &key, double *x, int64_t mgIter, int64_t sweeps, bool fmg);
     const double *graphX = nullptr;  // buffers baked into captured graphs
     void clearGraphs();
 
@@ -228,7 +249,7 @@ private:
     void preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg);
     template <typename T>
     void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
-    void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg);
+    void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror = true);
     void ensureStiffness();
     template <typename T>
     void levelOp(int l, int op, const double *a, const double *b, double *out, bool flag);
@@ -278,5 +299,11 @@ private:
     void gradientDev(double *out);
     void jacobianDev(double *out);
 };
+
+// Layer-by-layer solves of `count` partial-build heights (layers[t] element layers built)
+// over `slots` concurrent solver instances cloned from `src` (vfem_lbl.cpp).
+void lblRun(Grid &src, int coarsenings, const int64_t *layers, int64_t count, int64_t slots, int precision,
+            int outerMatvec, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+            double *compliance, int64_t *iterations, double *gradSum);
 
 }  // namespace vfem

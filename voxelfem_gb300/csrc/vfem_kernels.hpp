@@ -171,9 +171,19 @@ void launch_symmetrize(double *A, int n, cudaStream_t st);
 inline size_t dense_inverse_work_size(int n) { return (size_t)n * n + (size_t)32 * 32 * ((n + 31) / 32); }
 void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
                        const std::function<void(const std::string &)> &mark = nullptr);
+// x = A^{-1} b on the free DOFs (nfreeDev[0] of them, at most nfreeCap), zero elsewhere.
 template <typename T>
-void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, int nfree, const T *b, T *x,
-                         double *scratch, cudaStream_t st);
+void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, const int *nfreeDev, int nfreeCap,
+                         const T *b, T *x, double *scratch, cudaStream_t st);
+// Sets the WHILE condition of a device-resident PCG loop from the CG scalars (initial: before
+// the first iteration, else after one; counts iterations, flags a NaN residual).
+void launch_cg_loop_control(cudaGraphConditionalHandle h, double *sc, bool initial, cudaStream_t st);
+// sc[0] = 0, first-iteration flag, tolerance, iteration counter and limit, NaN flag
+void launch_cg_init(double *sc, double tol2, double maxIter, cudaStream_t st);
+// y += a x
+void launch_axpy(int64_t n, double a, const double *x, double *y, cudaStream_t st);
+// p[0] = a, p[1] = b, ordered on the stream
+void launch_set_pair(int *p, int a, int b, cudaStream_t st);
 
 // Deterministic masked reductions: fixed grid of REDUCE_BLOCKS partials, then one block.
 constexpr int REDUCE_BLOCKS = 4 * NUM_SMS;

@@ -853,3 +853,62 @@ class OCOptimizer:
         check(_lib().vfem_problem_oc_step(self.problem._h, float(m), float(p), float(ctol), C.byref(probes)))
         self.lastProbes = probes.value
         self.problem.filterChain.setDesignVars(self.problem.getVars())
+
+
+class LayerByLayerEvaluator:
+    """LayerByLayerEvaluator(lblSim) (LayerByLayer.hh:223-296): compliance of every partial build
+    height, averaged, with its gradient.
+
+    ``run(solver, zeroInit, layerIncrement, maxIter, tol, ...)`` visits the heights
+    ny, ny - layerIncrement, ..., > 0 like the reference. Every height starts from a zero initial
+    guess (the reference's ``"zero"`` initialisation); the solves are independent and run
+    ``slots`` at a time on concurrent solver instances (``slots=1``: one at a time). ``solver``
+    supplies the number of coarsening levels and the precision.
+    """
+
+    def __init__(self, lblSim):
+        self.sim = lblSim
+        self.layers = np.zeros(0, dtype=np.int64)
+        self.compliances = np.zeros(0)
+        self.iterations = np.zeros(0, dtype=np.int64)
+        self._grad = np.zeros(lblSim.numElements())
+        self.initMethod = "zero"
+
+    def selectInitMethod(self, method):
+        if method != "zero":
+            raise RuntimeError("Unrecognized method " + str(method) + " (independent batched solves use 'zero')")
+        self.initMethod = method
+
+    def run(self, solver, zeroInit=True, layerIncrement=1, maxIter=500, tol=1e-8, it_callback=None,
+            mgIterations=1, mgSmoothingIterations=1, fmg=False, verbose=False, lblCallback=None, slots=8):
+        if it_callback is not None:
+            raise RuntimeError("per-iteration callbacks are not available for device-resident solves")
+        ny = int(self.sim.NbElementsPerDimension[1])
+        inc = int(layerIncrement)
+        if inc < 1:
+            raise RuntimeError("layerIncrement must be positive")
+        layers = []
+        l = ny
+        while l > 0:
+            layers.append(l)
+            l -= min(inc, l)
+        self.layers = np.array(layers, dtype=np.int64)
+        n = len(layers)
+        self.compliances = np.zeros(n)
+        self.iterations = np.zeros(n, dtype=np.int64)
+        self._grad = np.zeros(self.sim.numElements())
+        precision = 1 if getattr(solver, "_prec", "fp64") == "mixed" else 0
+        check(_lib().vfem_lbl_run(self.sim._h, int(solver.numLevels - 1), ptr(self.layers), n, int(slots), precision,
+                                  int(maxIter), float(tol), int(mgIterations), int(mgSmoothingIterations),
+                                  int(bool(fmg)), ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
+        for t, lay in enumerate(layers):
+            if verbose:
+                print("Layer %d: %g" % (lay, self.compliances[t]))
+            if lblCallback is not None:
+                lblCallback(lay, self.compliances[t], None, None)
+
+    def objective(self):
+        return 0.5 * float(np.sum(self.compliances)) / max(len(self.compliances), 1)
+
+    def gradient(self):
+        return self._grad / max(len(self.compliances), 1)
