@@ -361,12 +361,61 @@ def run_ours(args):
                            "df": kernels["applyk_fine_df"]["gbs"]},
             "kernels": kernels,
             "breakdown_ms": {"mixed_per_iteration": breakdown_mixed, "fp64_per_iteration": breakdown_fp64}}
+    if rank == 0 and ws == 1 and not args.no_lbl:
+        line["lbl"] = run_lbl()
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+LBL_NE = (128, 128, 128)
+LBL_COARSENINGS = 4
+
+
+def run_lbl(slots_list=(1, 8, 16)):
+    """Layer-by-layer workload: 128^3 Q1, rho U[0.1, 1] seed 0, base fixed, gravity (0, -1, 0),
+    heights 1..128 each solved from a zero guess (mixed precision, tol 1e-8, 2+2 sweeps, 4
+    coarsenings). Wall time of the 128 solves one height at a time (1 slot) and spread over
+    concurrent solver slots; each evaluator warmed up once (graph capture) before its timed run."""
+    import torch
+
+    from voxelfem_gb300 import pyVoxelFEM as pv
+    from voxelfem_gb300 import workloads as wl
+
+    ne = LBL_NE
+    sim = pv.TensorProductSimulator([1, 1, 1], [[0.0, 0.0, 0.0], [float(v) for v in ne]], ne)
+    wl.setup_layer_by_layer(sim, ne, 0.1, 0)
+    mg = sim.multigridSolver(LBL_COARSENINGS)
+    mg.setPrecision("mixed")
+    out = {"workload": "layer-by-layer 128^3 Q1, rho U[0.1,1] seed 0, base fixed, gravity -y, heights 1..128, "
+                       "zero initial guesses, mixed precision, tol 1e-8, 2+2 sweeps, 4 coarsenings",
+           "heights": ne[1]}
+    ref = None
+    for slots in slots_list:
+        ev = pv.LayerByLayerEvaluator(sim)
+        ev.run(mg, True, 1, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=slots)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev.run(mg, True, 1, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=slots)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        key = "one_at_a_time_s" if slots == 1 else "slots_%d_s" % slots
+        out[key] = dt
+        if ref is None:
+            ref = ev.compliances.copy()
+            out["iterations_total"] = int(ev.iterations.sum())
+            out["objective"] = ev.objective()
+        else:
+            out["max_rel_diff_vs_one_at_a_time_%d" % slots] = float(np.max(np.abs(ev.compliances - ref) / np.abs(ref)))
+        ev._release()
+    best = min((k for k in out if k.startswith("slots_")), key=lambda k: out[k], default=None)
+    if best is not None:
+        out["batched_speedup"] = out["one_at_a_time_s"] / out[best]
+        out["best"] = best
+    return out
 
 
 def run_kernel_case(args):
@@ -400,6 +449,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-lbl", action="store_true", help="skip the layer-by-layer batching measurement")
     ap.add_argument("--kernel-case", type=int, default=None,
                     help="only set up the workload and launch one hot kernel (id of vfem_mg_time_kernel) twice")
     args = ap.parse_args()

@@ -57,8 +57,10 @@ _SIGS = {
     "vfem_grid_build_load": (C.c_int, [_vp, _vp]),
     "vfem_grid_compliance_gradient": (C.c_int, [_vp, _vp, _vp]),
     "vfem_grid_adjoint_sensitivity": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, _vp]),
-    "vfem_lbl_run": (C.c_int, [_vp, C.c_int64, _vp, C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_double, C.c_int64,
-                               C.c_int64, C.c_int, _vp, _vp, _vp]),
+    "vfem_lbl_create": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "vfem_lbl_destroy": (C.c_int, [_vp]),
+    "vfem_lbl_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, _vp, _vp,
+                               _vp]),
     "vfem_grid_element_energy": (C.c_int, [_vp, _vp, _vp]),
     "vfem_mg_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "vfem_mg_destroy": (C.c_int, [_vp]),

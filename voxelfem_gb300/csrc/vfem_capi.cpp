@@ -153,17 +153,29 @@ int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out) {
 int vfem_grid_build_load(vfem_grid *g, double *out) {
     return guarded([&] { need(g, "grid"); g->g.buildLoad(out); });
 }
-int vfem_lbl_run(vfem_grid *g, int64_t coarsenings, const int64_t *layers, int64_t count, int64_t slots,
-                 int precision, int64_t max_iter, double tol, int64_t mg_iterations, int64_t mg_smoothing_iterations,
-                 int full_multigrid, double *compliance_out, int64_t *iterations_out, double *gradient_sum_out) {
+struct vfem_lbl {
+    vfem::LBL e;
+    vfem_lbl(vfem::Grid *g, int c, int64_t s, int p) : e(g, c, s, p) {}
+};
+int vfem_lbl_create(vfem_grid *g, int64_t coarsenings, int64_t slots, int precision, vfem_lbl **out) {
     return guarded([&] {
         need(g, "grid");
+        need(out, "out");
+        *out = new vfem_lbl(&g->g, (int)coarsenings, slots, precision);
+    });
+}
+int vfem_lbl_destroy(vfem_lbl *e) {
+    return guarded([&] { delete e; });
+}
+int vfem_lbl_run(vfem_lbl *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
+                 int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, double *compliance_out,
+                 int64_t *iterations_out, double *gradient_sum_out) {
+    return guarded([&] {
+        need(e, "evaluator");
         need(layers, "layers");
         need(compliance_out, "compliance_out");
-        if (coarsenings < 1) throw Error(ERR_ARG, "layer-by-layer solves need at least one coarsening level");
-        if (precision != PREC_FP64 && precision != PREC_MIXED) throw Error(ERR_ARG, "unknown precision");
-        lblRun(g->g, (int)coarsenings, layers, count, slots, precision, MATVEC_DF, max_iter, tol, mg_iterations,
-               mg_smoothing_iterations, full_multigrid != 0, compliance_out, iterations_out, gradient_sum_out);
+        e->e.run(layers, count, max_iter, tol, mg_iterations, mg_smoothing_iterations, full_multigrid != 0,
+                 compliance_out, iterations_out, gradient_sum_out);
     });
 }
 int vfem_grid_adjoint_sensitivity(vfem_grid *g, const double *lambda, const double *u, double load_weight,

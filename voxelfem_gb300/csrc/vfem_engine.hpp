@@ -300,10 +300,31 @@ private:
     void jacobianDev(double *out);
 };
 
-// Layer-by-layer solves of `count` partial-build heights (layers[t] element layers built)
-// over `slots` concurrent solver instances cloned from `src` (vfem_lbl.cpp).
-void lblRun(Grid &src, int coarsenings, const int64_t *layers, int64_t count, int64_t slots, int precision,
-            int outerMatvec, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
-            double *compliance, int64_t *iterations, double *gradSum);
+// Layer-by-layer solves of partial-build heights (layers[t] element layers built) over
+// persistent concurrent solver instances cloned from `src` (vfem_lbl.cpp).
+class LBL {
+public:
+    LBL(Grid *src, int coarsenings, int64_t slots, int precision);
+    ~LBL();
+    LBL(const LBL &) = delete;
+    LBL &operator=(const LBL &) = delete;
+    void run(const int64_t *layers, int64_t count, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
+             bool fmg, double *compliance, int64_t *iterations, double *gradSum);
+    Grid *src;
+    int coarsenings, precision;
+
+private:
+    struct Slot {
+        std::unique_ptr<Grid> grid;
+        std::unique_ptr<MG> mg;
+        DevBuf<double> x, f, gtmp, gacc, cpl;
+        cudaEvent_t done = nullptr;
+        int64_t idx = -1;
+        ~Slot();
+    };
+    std::vector<std::unique_ptr<Slot>> S;
+    double *cplHost = nullptr;
+    void syncSource();
+};
 
 }  // namespace vfem

@@ -873,6 +873,28 @@ class LayerByLayerEvaluator:
         self.iterations = np.zeros(0, dtype=np.int64)
         self._grad = np.zeros(lblSim.numElements())
         self.initMethod = "zero"
+        self._h = None
+        self._key = None
+
+    def __del__(self):
+        self._release()
+
+    def _release(self):
+        if getattr(self, "_h", None) is not None:
+            try:
+                _lib().vfem_lbl_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _handle(self, coarsenings, slots, precision):
+        key = (coarsenings, slots, precision)
+        if self._h is None or self._key != key:
+            self._release()
+            h = C.c_void_p()
+            check(_lib().vfem_lbl_create(self.sim._h, coarsenings, slots, precision, C.byref(h)))
+            self._h, self._key = h, key
+        return self._h
 
     def selectInitMethod(self, method):
         if method != "zero":
@@ -898,9 +920,10 @@ class LayerByLayerEvaluator:
         self.iterations = np.zeros(n, dtype=np.int64)
         self._grad = np.zeros(self.sim.numElements())
         precision = 1 if getattr(solver, "_prec", "fp64") == "mixed" else 0
-        check(_lib().vfem_lbl_run(self.sim._h, int(solver.numLevels - 1), ptr(self.layers), n, int(slots), precision,
-                                  int(maxIter), float(tol), int(mgIterations), int(mgSmoothingIterations),
-                                  int(bool(fmg)), ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
+        h = self._handle(int(solver.numLevels - 1), int(slots), precision)
+        check(_lib().vfem_lbl_run(h, ptr(self.layers), n, int(maxIter), float(tol), int(mgIterations),
+                                  int(mgSmoothingIterations), int(bool(fmg)), ptr(self.compliances),
+                                  ptr(self.iterations), ptr(self._grad)))
         for t, lay in enumerate(layers):
             if verbose:
                 print("Layer %d: %g" % (lay, self.compliances[t]))
