@@ -144,6 +144,10 @@ int vfem_mg_level_dirichlet_mask(const vfem_mg *mg, int level, uint8_t *mask_out
 int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec);
 /* CUDA-graph capture of the CG iteration (default on); no reference counterpart */
 int vfem_mg_set_use_graphs(vfem_mg *mg, int use);
+/* Execution option (no reference counterpart): with graphs on, a solve without a callback runs as
+ * one graph whose conditional WHILE node repeats the iteration on the device (default, 1); 0
+ * launches one graph per iteration from a host loop. Results are identical. */
+int vfem_mg_set_device_loop(vfem_mg *mg, int on);
 /* setSymmetricGaussSeidel (MultigridSolver.hh:123-125) */
 int vfem_mg_set_symmetric_gs(vfem_mg *mg, int symmetric);
 /* setFabricationMaskHeightByLayer (MultigridSolver.hh:1022-1028) */

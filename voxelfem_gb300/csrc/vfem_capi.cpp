@@ -228,6 +228,12 @@ int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec) {
         mg->m.outerMatvec = outer_matvec;
     });
 }
+int vfem_mg_set_device_loop(vfem_mg *mg, int on) {
+    return guarded([&] {
+        need(mg, "mg");
+        mg->m.deviceLoop = on != 0;
+    });
+}
 int vfem_mg_set_use_graphs(vfem_mg *mg, int use) {
     return guarded([&] { need(mg, "mg"); mg->m.useGraphs = use != 0; mg->m.clearGraphs(); });
 }

@@ -449,6 +449,10 @@ class MultigridSolver:
         check(_lib().vfem_mg_set_precision(self._h, p, m))
         self._prec = precision
 
+    def setDeviceLoop(self, on):
+        """Run a solve as one device-resident graph loop (default) or one graph per iteration."""
+        check(_lib().vfem_mg_set_device_loop(self._h, int(bool(on))))
+
     def setUseGraphs(self, use):
         check(_lib().vfem_mg_set_use_graphs(self._h, int(bool(use))))
 
