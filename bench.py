@@ -396,6 +396,8 @@ def run_ours(args):
             "breakdown_ms": {"mixed_per_iteration": breakdown_mixed, "fp64_per_iteration": breakdown_fp64}}
     if rank == 0 and ws == 1 and not args.no_lbl:
         line["lbl"] = run_lbl()
+    if rank == 0 and ws == 1 and not args.no_q2:
+        line["q2"] = run_q2(hbm)
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
     if rank == 0:
@@ -451,6 +453,35 @@ def run_lbl(slots_list=(1, 8, 16)):
     return out
 
 
+Q2_NE = (128, 128, 128)
+
+
+def run_q2(hbm):
+    """Triquadratic applyK at 128^3 Q2 elements (16.97M nodes, 50.9M DOF), rho U[0.01, 1] seed 0:
+    device time per launch on resident data (FP64 and FP32), algorithmic bytes s (6 nn + ne) and
+    FLOPs 2 * 81^2 * ne."""
+    import ctypes as C
+
+    from voxelfem_gb300 import _capi
+    from voxelfem_gb300 import pyVoxelFEM as pv
+
+    lib = _capi.load()
+    ne = Q2_NE
+    g = pv.TensorProductSimulator([2, 2, 2], [[0.0, 0.0, 0.0], [float(v) for v in ne]], ne)
+    g.ETensor = (1.0, 0.3)
+    g.E_0, g.E_min, g.gamma = 1.0, 1e-9, 3.0
+    g.setDensities(np.random.default_rng(0).uniform(0.01, 1.0, int(np.prod(ne))))
+    flops = 2.0 * 81 * 81 * g.numElements()
+    out = {"workload": "128^3 Q2 applyK (%d nodes), rho U[0.01,1] seed 0" % g.numNodes()}
+    for name, prec, reps in (("fp64", 0, 2), ("fp32", 1, 10)):
+        ms, nbytes = C.c_double(), C.c_double()
+        _capi.check(lib.vfem_q2_time_apply_k(g._h, prec, reps, C.byref(ms), C.byref(nbytes)))
+        gbs = nbytes.value / (ms.value * 1e-3) / 1e9
+        out[name] = {"ms": ms.value, "bytes": nbytes.value, "gbs": gbs, "hbm_frac": gbs / hbm,
+                     "tflops": flops / (ms.value * 1e-3) / 1e12}
+    return out
+
+
 def run_kernel_case(args):
     """One hot kernel of the workload, launched a handful of times (profiler captures)."""
     import ctypes as C
@@ -483,6 +514,7 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-lbl", action="store_true", help="skip the layer-by-layer batching measurement")
+    ap.add_argument("--no-q2", action="store_true", help="skip the triquadratic applyK measurement")
     ap.add_argument("--host-loop", action="store_true",
                     help="iterate PCG from the host (one graph per iteration) instead of the device-resident loop")
     ap.add_argument("--kernel-case", type=int, default=None,

@@ -238,6 +238,34 @@ int vfem_problem_last_solve(vfem_problem *p, vfem_pcg_stats *stats);
 /* OCOptimizer::step(m, p, ctol) (OptimalityCriterion.hh:51-138); probes = constraint evaluations */
 int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, int64_t *probes);
 
+/* ---- triquadratic voxels (TensorProductSimulator<double, 2, 2, 2>, TPSStencils.hh:135-186) ----
+ * Nodes (2 nx + 1)(2 ny + 1)(2 nz + 1), index (I ny' + J) nz' + K; nodal fields (nn, 3)
+ * column-major as for trilinear grids. precision 0 = FP64, 1 = FP32. */
+typedef struct vfem_q2 vfem_q2;
+int vfem_q2_create(const int64_t elems[3], const double bbox_min[3], const double bbox_max[3], vfem_q2 **out);
+int vfem_q2_destroy(vfem_q2 *g);
+int vfem_q2_dims(const vfem_q2 *g, int64_t *num_nodes, int64_t *num_elements);
+/* setETensor (isotropic E, nu) and E_0, E_min, gamma, q, interpolationLaw, as for vfem_grid_* */
+int vfem_q2_set_etensor(vfem_q2 *g, double young, double poisson);
+int vfem_q2_set_material_params(vfem_q2 *g, double E0, double Emin, double gamma, double q, int law);
+int vfem_q2_set_densities(vfem_q2 *g, const double *rho);
+/* fullDensityElementStiffnessMatrix: 81 x 81 row-major, DOF 3l + c, l = 9a + 3b + c, 3^3 Gauss points */
+int vfem_q2_get_k0(const vfem_q2 *g, double *out6561);
+/* zero-displacement supports on the nodes inside [min, max], components in cmask (bit c = component c) */
+int vfem_q2_add_dirichlet(vfem_q2 *g, const double min_corner[3], const double max_corner[3], int cmask);
+int vfem_q2_get_dirichlet_mask(const vfem_q2 *g, uint8_t *mask_out);
+/* applyK (TPSStencils.hh:135-186); zero_dirichlet zeroes the constrained components of the result */
+int vfem_q2_apply_k(vfem_q2 *g, const double *u, double *out, int precision, int zero_dirichlet);
+/* one 27-colour block Gauss-Seidel sweep on K u = b (MultigridSolver.hh:277-321, 409-442); u in/out */
+int vfem_q2_smooth(vfem_q2 *g, double *u_inout, const double *b, int forward, int precision);
+/* Q2 restriction (P^T) and prolongation (P) between a grid of elems_fine elements per axis and its
+ * 2x coarsening (MultigridSolver.hh:137-275) */
+int vfem_q2_restrict(const int64_t elems_fine[3], const double *fine, double *coarse);
+int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, double *fine, int accumulate);
+/* Benchmark hook (no reference counterpart): average device time of one applyK on resident data and
+ * its algorithmic bytes s (6 nn + ne). */
+int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes);
+
 #ifdef __cplusplus
 }
 #endif

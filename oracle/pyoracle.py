@@ -79,6 +79,11 @@ def lib():
             "ovf_top_get_design": (None, [C.c_void_p, _d]),
             "ovf_top_last_iters": (C.c_long, [C.c_void_p]),
             "ovf_top_oc_step": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, _l]),
+            "ovf_q2_k0": (None, [C.c_double, C.c_double, _d, C.c_int, _d]),
+            "ovf_q2_apply_k": (None, [_l, _d, _d, _d, _d]),
+            "ovf_q2_smooth": (None, [_l, _d, _d, _u8, _d, _d, C.c_int]),
+            "ovf_q2_interp": (None, [_l, _d, _d, C.c_int]),
+            "ovf_q2_restrict": (None, [_l, _d, _d]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -402,3 +407,58 @@ class TOP:
         probes = C.c_long(0)
         _check(lib().ovf_top_oc_step(self.h, m, p, ctol, C.byref(probes)))
         return probes.value
+
+
+# ---- triquadratic voxels ----
+def q2_num_nodes(ne):
+    return int(np.prod([2 * int(v) + 1 for v in ne]))
+
+
+def q2_k0(E=1.0, nu=0.3, h=(1.0, 1.0, 1.0), npts=3):
+    """81 x 81 triquadratic element stiffness with npts Gauss points per axis."""
+    out = np.empty(6561)
+    lib().ovf_q2_k0(float(E), float(nu), _dp(np.ascontiguousarray(h, dtype=np.float64)), int(npts), _dp(out))
+    return out.reshape(81, 81)
+
+
+def _ne(ne):
+    return (C.c_long * 3)(*[int(v) for v in ne])
+
+
+def q2_apply_k(ne, K0, Y, u):
+    nn = q2_num_nodes(ne)
+    u = vfield(u, nn)
+    out = np.zeros((nn, 3), order="F")
+    lib().ovf_q2_apply_k(_ne(ne), _dp(np.ascontiguousarray(K0, dtype=np.float64)),
+                         _dp(np.ascontiguousarray(Y, dtype=np.float64)), _dp(u), _dp(out))
+    return out
+
+
+def q2_smooth(ne, K0, Y, dmask_bits, u, b, forward=True):
+    nn = q2_num_nodes(ne)
+    x = vfield(u, nn).copy(order="F")
+    b = vfield(b, nn)
+    m = np.ascontiguousarray(dmask_bits, dtype=np.uint8)
+    lib().ovf_q2_smooth(_ne(ne), _dp(np.ascontiguousarray(K0, dtype=np.float64)),
+                        _dp(np.ascontiguousarray(Y, dtype=np.float64)), m.ctypes.data_as(_u8), _dp(x), _dp(b),
+                        int(bool(forward)))
+    return x
+
+
+def q2_interp(ne_fine, coarse, fine=None, accumulate=False):
+    nf = q2_num_nodes(ne_fine)
+    nc = q2_num_nodes([int(v) // 2 for v in ne_fine])
+    c = vfield(coarse, nc)
+    out = np.zeros((nf, 3), order="F") if fine is None else vfield(fine, nf).copy(order="F")
+    lib().ovf_q2_interp(_ne(ne_fine), _dp(c), _dp(out), int(bool(accumulate)))
+    return out
+
+
+def q2_restrict(ne_fine, fine):
+    nf = q2_num_nodes(ne_fine)
+    nc = q2_num_nodes([int(v) // 2 for v in ne_fine])
+    f = vfield(fine, nf)
+    out = np.zeros((nc, 3), order="F")
+    lib().ovf_q2_restrict(_ne(ne_fine), _dp(f), _dp(out))
+    return out
+

@@ -1310,6 +1310,241 @@ int guarded(F &&f) {
 // ---------------------------------------------------------------------------
 // C interface used by the tests and by the benchmark's CPU baseline leg.
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Triquadratic voxels (TensorProductSimulator<double, 2, 2, 2>).
+// K0: TensorProductSimulator.hh:54-80 with TensorProductQuadrature<(2 * 2)...> (3 Gauss points
+// per axis); local node l = 9a + 3b + c (NDArrayIndexer flattening, last index fastest).
+// applyK: element loop (TPSStencils.hh:135-186 gathers per node; summing element products is
+// the same operator). Smoother: visitNodesMulticolored with 27 colours (MultigridSolver.hh:
+// 409-442) and the Finest node stencil (:277-292). Transfers: phis / interpolation /
+// restriction (MultigridSolver.hh:137-275) as tensor products of 1-D Q2 interpolation matrices.
+// ---------------------------------------------------------------------------
+struct Q2Grid {
+    long ne[3], nn[3];
+    size_t NN, NE;
+    size_t node(long I, long J, long K) const { return ((size_t)I * nn[1] + J) * nn[2] + K; }
+    size_t elem(long i, long j, long k) const { return ((size_t)i * ne[1] + j) * ne[2] + k; }
+};
+
+Q2Grid q2grid(const long ne[3]) {
+    Q2Grid g;
+    for (int d = 0; d < 3; ++d) {
+        g.ne[d] = ne[d];
+        g.nn[d] = 2 * ne[d] + 1;
+    }
+    g.NN = (size_t)g.nn[0] * g.nn[1] * g.nn[2];
+    g.NE = (size_t)ne[0] * ne[1] * ne[2];
+    return g;
+}
+
+// Lagrange basis on the equispaced nodes {0, 1/2, 1}: value and derivative of basis a at x
+double lag2(int a, double x) {
+    const double xs[3] = {0.0, 0.5, 1.0};
+    double v = 1.0;
+    for (int m = 0; m < 3; ++m)
+        if (m != a) v *= (x - xs[m]) / (xs[a] - xs[m]);
+    return v;
+}
+double lag2d(int a, double x) {
+    const double xs[3] = {0.0, 0.5, 1.0};
+    double acc = 0.0;
+    for (int m = 0; m < 3; ++m) {
+        if (m == a) continue;
+        double t = 1.0 / (xs[a] - xs[m]);
+        for (int p = 0; p < 3; ++p)
+            if (p != a && p != m) t *= (x - xs[p]) / (xs[a] - xs[p]);
+        acc += t;
+    }
+    return acc;
+}
+
+// Gauss-Legendre points and weights on [0, 1] (n = 3 or 4)
+void gauss01(int n, double *x, double *w) {
+    if (n == 3) {
+        const double r = std::sqrt(0.6);
+        const double xm[3] = {-r, 0.0, r}, wm[3] = {5.0 / 9, 8.0 / 9, 5.0 / 9};
+        for (int i = 0; i < 3; ++i) { x[i] = 0.5 * (xm[i] + 1); w[i] = 0.5 * wm[i]; }
+    } else if (n == 4) {
+        const double a = std::sqrt(3.0 / 7 - 2.0 / 7 * std::sqrt(6.0 / 5)), b = std::sqrt(3.0 / 7 + 2.0 / 7 * std::sqrt(6.0 / 5));
+        const double wa = (18 + std::sqrt(30.0)) / 36, wb = (18 - std::sqrt(30.0)) / 36;
+        const double xm[4] = {-b, -a, a, b}, wm[4] = {wb, wa, wa, wb};
+        for (int i = 0; i < 4; ++i) { x[i] = 0.5 * (xm[i] + 1); w[i] = 0.5 * wm[i]; }
+    } else {
+        throw std::runtime_error("unsupported quadrature order");
+    }
+}
+
+void q2K0(double E, double nu, const double h[3], int npts, double *K) {
+    const double lam = E * nu / ((1 + nu) * (1 - 2 * nu)), mu = E / (2 * (1 + nu));
+    double gx[4], gw[4];
+    gauss01(npts, gx, gw);
+    std::fill(K, K + 6561, 0.0);
+    for (int qa = 0; qa < npts; ++qa)
+        for (int qb = 0; qb < npts; ++qb)
+            for (int qc = 0; qc < npts; ++qc) {
+                const double p[3] = {gx[qa], gx[qb], gx[qc]};
+                const double w = gw[qa] * gw[qb] * gw[qc] * h[0] * h[1] * h[2];
+                double G[27][3];
+                for (int l = 0; l < 27; ++l) {
+                    const int id[3] = {l / 9, (l / 3) % 3, l % 3};
+                    for (int d = 0; d < 3; ++d) {
+                        double g = 1.0;
+                        for (int e = 0; e < 3; ++e) g *= (e == d) ? lag2d(id[e], p[e]) / h[e] : lag2(id[e], p[e]);
+                        G[l][d] = g;
+                    }
+                }
+                // eps(phi_{l,c}) = sym(e_c (x) grad N_l); sigma = lam tr(eps) I + 2 mu eps
+                for (int i = 0; i < 81; ++i) {
+                    const int li = i / 3, ci = i % 3;
+                    for (int j = 0; j < 81; ++j) {
+                        const int lj = j / 3, cj = j % 3;
+                        double epsIepsJ = 0.5 * G[li][cj] * G[lj][ci];
+                        if (ci == cj) epsIepsJ += 0.5 * (G[li][0] * G[lj][0] + G[li][1] * G[lj][1] + G[li][2] * G[lj][2]);
+                        K[i * 81 + j] += w * (lam * G[li][ci] * G[lj][cj] + 2 * mu * epsIepsJ);
+                    }
+                }
+            }
+}
+
+void q2ApplyK(const Q2Grid &g, const double *K, const double *Y, const double *u, double *out) {
+    std::fill(out, out + 3 * g.NN, 0.0);
+    for (long i = 0; i < g.ne[0]; ++i)
+        for (long j = 0; j < g.ne[1]; ++j)
+            for (long k = 0; k < g.ne[2]; ++k) {
+                size_t nodes[27];
+                double ue[81], fe[81];
+                for (int l = 0; l < 27; ++l) {
+                    nodes[l] = g.node(2 * i + l / 9, 2 * j + (l / 3) % 3, 2 * k + l % 3);
+                    for (int c = 0; c < 3; ++c) ue[3 * l + c] = u[c * g.NN + nodes[l]];
+                }
+                const double E = Y[g.elem(i, j, k)];
+                for (int r = 0; r < 81; ++r) {
+                    double acc = 0.0;
+                    for (int t = 0; t < 81; ++t) acc += K[r * 81 + t] * ue[t];
+                    fe[r] = E * acc;
+                }
+                for (int l = 0; l < 27; ++l)
+                    for (int c = 0; c < 3; ++c) out[c * g.NN + nodes[l]] += fe[3 * l + c];
+            }
+}
+
+void q2Smooth(const Q2Grid &g, const double *K, const double *Y, const uint8_t *dmask, double *u, const double *b,
+              bool forward) {
+    for (int ci = 0; ci < 27; ++ci) {
+        const int col = forward ? ci : 26 - ci;
+        const long lo[3] = {col / 9, (col / 3) % 3, col % 3};
+        long inc[3];
+        for (int d = 0; d < 3; ++d) inc[d] = (lo[d] == 1) ? 2 : 4;
+        for (long I = lo[0]; I < g.nn[0]; I += inc[0])
+            for (long J = lo[1]; J < g.nn[1]; J += inc[1])
+                for (long Kk = lo[2]; Kk < g.nn[2]; Kk += inc[2]) {
+                    const size_t n = g.node(I, J, Kk);
+                    const uint8_t dm = dmask[n];
+                    if (dm == 7) continue;
+                    double bms[3] = {b[n], b[g.NN + n], b[2 * g.NN + n]};
+                    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    // incident elements: per axis, corner nodes (even) lie in elements I/2 - 1 and I/2
+                    const long P[3] = {I, J, Kk};
+                    long el[3][2], ll[3][2];
+                    int cnt[3];
+                    for (int d = 0; d < 3; ++d) {
+                        cnt[d] = 0;
+                        if (P[d] % 2) { el[d][0] = (P[d] - 1) / 2; ll[d][0] = 1; cnt[d] = 1; }
+                        else {
+                            if (P[d] / 2 - 1 >= 0) { el[d][cnt[d]] = P[d] / 2 - 1; ll[d][cnt[d]] = 2; ++cnt[d]; }
+                            if (P[d] / 2 < g.ne[d]) { el[d][cnt[d]] = P[d] / 2; ll[d][cnt[d]] = 0; ++cnt[d]; }
+                        }
+                    }
+                    for (int a = 0; a < cnt[0]; ++a)
+                        for (int bb = 0; bb < cnt[1]; ++bb)
+                            for (int c = 0; c < cnt[2]; ++c) {
+                                const long ei = el[0][a], ej = el[1][bb], ek = el[2][c];
+                                const int ln = 9 * ll[0][a] + 3 * ll[1][bb] + ll[2][c];
+                                const double E = Y[g.elem(ei, ej, ek)];
+                                for (int r = 0; r < 3; ++r) {
+                                    double acc = 0.0;
+                                    for (int m = 0; m < 27; ++m) {
+                                        const size_t nm = g.node(2 * ei + m / 9, 2 * ej + (m / 3) % 3, 2 * ek + m % 3);
+                                        for (int cc = 0; cc < 3; ++cc) acc += K[(3 * ln + r) * 81 + 3 * m + cc] * u[cc * g.NN + nm];
+                                    }
+                                    bms[r] -= E * acc;
+                                    for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] += E * K[(3 * ln + r) * 81 + 3 * ln + cc];
+                                }
+                            }
+                    double un[3] = {u[n], u[g.NN + n], u[2 * g.NN + n]};
+                    smoothNodeSolve(dm, bms, M, un, forward);
+                    for (int c = 0; c < 3; ++c) u[c * g.NN + n] = un[c];
+                }
+    }
+}
+
+// 1-D Q2 prolongation (fine nodes 0..4 nec) x (coarse nodes 0..2 nec), dense
+std::vector<double> q2P1d(long nec) {
+    const long nf = 4 * nec + 1, nc = 2 * nec + 1;
+    std::vector<double> P((size_t)nf * nc, 0.0);
+    for (long f = 0; f < nf; ++f) {
+        const long e = std::min(f / 4, nec - 1);
+        const double x = (f - 4.0 * e) / 4.0;
+        for (int a = 0; a < 3; ++a) P[(size_t)f * nc + 2 * e + a] = lag2(a, x);
+    }
+    return P;
+}
+
+void q2Interp(const long neF[3], const double *coarse, double *fine, bool accumulate) {
+    const long nec[3] = {neF[0] / 2, neF[1] / 2, neF[2] / 2};
+    std::vector<double> P[3] = {q2P1d(nec[0]), q2P1d(nec[1]), q2P1d(nec[2])};
+    const long nf[3] = {2 * neF[0] + 1, 2 * neF[1] + 1, 2 * neF[2] + 1}, nc[3] = {2 * nec[0] + 1, 2 * nec[1] + 1, 2 * nec[2] + 1};
+    const size_t NF = (size_t)nf[0] * nf[1] * nf[2], NC = (size_t)nc[0] * nc[1] * nc[2];
+    for (long I = 0; I < nf[0]; ++I)
+        for (long J = 0; J < nf[1]; ++J)
+            for (long K = 0; K < nf[2]; ++K) {
+                double acc[3] = {0, 0, 0};
+                for (long a = 0; a < nc[0]; ++a) {
+                    const double wa = P[0][(size_t)I * nc[0] + a];
+                    if (wa == 0.0) continue;
+                    for (long b = 0; b < nc[1]; ++b) {
+                        const double wb = P[1][(size_t)J * nc[1] + b];
+                        if (wb == 0.0) continue;
+                        for (long c = 0; c < nc[2]; ++c) {
+                            const double wc = P[2][(size_t)K * nc[2] + c];
+                            if (wc == 0.0) continue;
+                            const size_t cn = ((size_t)a * nc[1] + b) * nc[2] + c;
+                            for (int r = 0; r < 3; ++r) acc[r] += wa * wb * wc * coarse[r * NC + cn];
+                        }
+                    }
+                }
+                const size_t fn = ((size_t)I * nf[1] + J) * nf[2] + K;
+                for (int r = 0; r < 3; ++r) fine[r * NF + fn] = (accumulate ? fine[r * NF + fn] : 0.0) + acc[r];
+            }
+}
+
+void q2Restrict(const long neF[3], const double *fine, double *coarse) {
+    const long nec[3] = {neF[0] / 2, neF[1] / 2, neF[2] / 2};
+    std::vector<double> P[3] = {q2P1d(nec[0]), q2P1d(nec[1]), q2P1d(nec[2])};
+    const long nf[3] = {2 * neF[0] + 1, 2 * neF[1] + 1, 2 * neF[2] + 1}, nc[3] = {2 * nec[0] + 1, 2 * nec[1] + 1, 2 * nec[2] + 1};
+    const size_t NF = (size_t)nf[0] * nf[1] * nf[2], NC = (size_t)nc[0] * nc[1] * nc[2];
+    std::fill(coarse, coarse + 3 * NC, 0.0);
+    for (long I = 0; I < nf[0]; ++I)
+        for (long J = 0; J < nf[1]; ++J)
+            for (long K = 0; K < nf[2]; ++K) {
+                const size_t fn = ((size_t)I * nf[1] + J) * nf[2] + K;
+                for (long a = 0; a < nc[0]; ++a) {
+                    const double wa = P[0][(size_t)I * nc[0] + a];
+                    if (wa == 0.0) continue;
+                    for (long b = 0; b < nc[1]; ++b) {
+                        const double wb = P[1][(size_t)J * nc[1] + b];
+                        if (wb == 0.0) continue;
+                        for (long c = 0; c < nc[2]; ++c) {
+                            const double wc = P[2][(size_t)K * nc[2] + c];
+                            if (wc == 0.0) continue;
+                            const size_t cn = ((size_t)a * nc[1] + b) * nc[2] + c;
+                            for (int r = 0; r < 3; ++r) coarse[r * NC + cn] += wa * wb * wc * fine[r * NF + fn];
+                        }
+                    }
+                }
+            }
+}
+
 extern "C" {
 
 const char *ovf_last_error() { return g_err.c_str(); }
@@ -1479,4 +1714,18 @@ int ovf_top_oc_step(void *t, double m, double p, double ctol, long *probes) {
     return guarded([&] { ocStep(*(TOP *)t, m, p, ctol, probes); });
 }
 
+
+// ---- triquadratic voxels ----
+void ovf_q2_k0(double E, double nu, const double h[3], int npts, double *out) { q2K0(E, nu, h, npts, out); }
+void ovf_q2_apply_k(const long ne[3], const double *K, const double *Y, const double *u, double *out) {
+    q2ApplyK(q2grid(ne), K, Y, u, out);
+}
+void ovf_q2_smooth(const long ne[3], const double *K, const double *Y, const uint8_t *dmask, double *u,
+                   const double *b, int forward) {
+    q2Smooth(q2grid(ne), K, Y, dmask, u, b, forward != 0);
+}
+void ovf_q2_interp(const long neF[3], const double *coarse, double *fine, int accumulate) {
+    q2Interp(neF, coarse, fine, accumulate != 0);
+}
+void ovf_q2_restrict(const long neF[3], const double *fine, double *coarse) { q2Restrict(neF, fine, coarse); }
 }  // extern "C"

@@ -58,6 +58,20 @@ _SIGS = {
     "vfem_grid_compliance_gradient": (C.c_int, [_vp, _vp, _vp]),
     "vfem_grid_adjoint_sensitivity": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, _vp]),
     "vfem_lbl_create": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "vfem_q2_create": (C.c_int, [_vp, _vp, _vp, C.POINTER(C.c_void_p)]),
+    "vfem_q2_destroy": (C.c_int, [_vp]),
+    "vfem_q2_dims": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "vfem_q2_set_etensor": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "vfem_q2_set_material_params": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),
+    "vfem_q2_set_densities": (C.c_int, [_vp, _vp]),
+    "vfem_q2_get_k0": (C.c_int, [_vp, _vp]),
+    "vfem_q2_add_dirichlet": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "vfem_q2_get_dirichlet_mask": (C.c_int, [_vp, _vp]),
+    "vfem_q2_apply_k": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
+    "vfem_q2_smooth": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
+    "vfem_q2_restrict": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_q2_interpolate": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "vfem_q2_time_apply_k": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "vfem_lbl_destroy": (C.c_int, [_vp]),
     "vfem_lbl_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, _vp, _vp,
                                _vp]),

@@ -1,0 +1,323 @@
+// Triquadratic (Q2) voxel kernels (TPSStencils.hh:135-186, MultigridSolver.hh:277-321,
+// 409-442): matrix-free SIMP applyK, the 27-colour block Gauss-Seidel sweep and the Q2
+// restriction / prolongation between a grid and its 2x coarsening.
+//
+// Nodes: (2 nx + 1)(2 ny + 1)(2 nz + 1), index (I * NY + J) * NZ + K. Element (i, j, k) owns
+// nodes (2i + a, 2j + b, 2k + c), local index l = 9a + 3b + c; K0 is 81 x 81 with DOF 3l + r.
+// A node's parity (I&1, J&1, K&1) fixes where it sits in its incident elements: an even
+// coordinate is a corner (local 0 of element I/2, local 2 of element I/2 - 1), an odd one is
+// the middle (local 1 of element (I-1)/2). The kernels run one node parity (applyK) or one
+// colour (smoother) per launch, so every warp reads the same K0 rows: K0 lives in constant
+// memory (FP32, 26 KB) or in global memory (FP64, 52 KB) and its reads are broadcasts.
+#include "vfem_kernels.hpp"
+
+namespace vfem {
+
+__constant__ float c_K0q2f[81 * 81];
+
+namespace {
+
+constexpr int BS = 256;
+
+struct Q2Dims {
+    int ne[3], nn[3];
+    int64_t NN, NE;
+};
+
+__device__ __forceinline__ int64_t q2node(const Q2Dims &d, int I, int J, int K) {
+    return ((int64_t)I * d.nn[1] + J) * d.nn[2] + K;
+}
+
+template <typename T>
+struct Q2K;
+template <>
+struct Q2K<float> {
+    static __device__ __forceinline__ float at(const float *, int r, int c) { return c_K0q2f[r * 81 + c]; }
+};
+template <>
+struct Q2K<double> {
+    static __device__ __forceinline__ double at(const double *K, int r, int c) { return __ldg(K + r * 81 + c); }
+};
+
+// Incident elements of a node along one axis: count, element index and local coordinate.
+__device__ __forceinline__ int axis_elems(int I, int ne, int *ei, int *la) {
+    if (I & 1) {
+        ei[0] = (I - 1) >> 1;
+        la[0] = 1;
+        return 1;
+    }
+    int n = 0;
+    if ((I >> 1) < ne) { ei[n] = I >> 1; la[n] = 0; ++n; }
+    if ((I >> 1) - 1 >= 0) { ei[n] = (I >> 1) - 1; la[n] = 2; ++n; }
+    return n;
+}
+
+// s -= E_e K0[3ln + r, :] u_e over the node's incident elements (and M += E_e K0 diagonal block)
+template <typename T, bool WithM>
+__device__ __forceinline__ void q2_gather(const Q2Dims &d, const T *Kg, const T *__restrict__ Y,
+                                          const T *__restrict__ u, int I, int J, int K, T &s0, T &s1, T &s2, T *M) {
+    int ex[2], ey[2], ez[2], ax[2], ay[2], az[2];
+    const int nx = axis_elems(I, d.ne[0], ex, ax), ny = axis_elems(J, d.ne[1], ey, ay), nz = axis_elems(K, d.ne[2], ez, az);
+    const int64_t ld = d.NN;
+    for (int p = 0; p < nx; ++p)
+        for (int q = 0; q < ny; ++q)
+            for (int w = 0; w < nz; ++w) {
+                const int ei = ex[p], ej = ey[q], ek = ez[w];
+                const int ln = 9 * ax[p] + 3 * ay[q] + az[w];
+                const T E = Y[((int64_t)ei * d.ne[1] + ej) * d.ne[2] + ek];
+                T c0 = T(0), c1 = T(0), c2 = T(0);
+#pragma unroll 3
+                for (int m = 0; m < 27; ++m) {
+                    const int64_t nm = q2node(d, 2 * ei + m / 9, 2 * ej + (m / 3) % 3, 2 * ek + m % 3);
+                    const T u0 = u[nm], u1 = u[ld + nm], u2 = u[2 * ld + nm];
+                    // symmetric K0: column 3ln + r read as row (3m + c)
+                    c0 += Q2K<T>::at(Kg, 3 * m, 3 * ln) * u0 + Q2K<T>::at(Kg, 3 * m + 1, 3 * ln) * u1 +
+                          Q2K<T>::at(Kg, 3 * m + 2, 3 * ln) * u2;
+                    c1 += Q2K<T>::at(Kg, 3 * m, 3 * ln + 1) * u0 + Q2K<T>::at(Kg, 3 * m + 1, 3 * ln + 1) * u1 +
+                          Q2K<T>::at(Kg, 3 * m + 2, 3 * ln + 1) * u2;
+                    c2 += Q2K<T>::at(Kg, 3 * m, 3 * ln + 2) * u0 + Q2K<T>::at(Kg, 3 * m + 1, 3 * ln + 2) * u1 +
+                          Q2K<T>::at(Kg, 3 * m + 2, 3 * ln + 2) * u2;
+                }
+                s0 -= E * c0;
+                s1 -= E * c1;
+                s2 -= E * c2;
+                if (WithM) {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) M[3 * r + c] += E * Q2K<T>::at(Kg, 3 * ln + r, 3 * ln + c);
+                }
+            }
+}
+
+// out = K u at the nodes of one parity class (px, py, pz); constrained components zeroed when asked
+template <typename T>
+__global__ void __launch_bounds__(BS) applyk_q2_kernel(Q2Dims d, const T *Kg, const T *__restrict__ Y,
+                                                       const T *__restrict__ u, T *__restrict__ out,
+                                                       const uint8_t *__restrict__ dmask, int zeroDir) {
+    const int par = blockIdx.y;
+    const int px = (par >> 2) & 1, py = (par >> 1) & 1, pz = par & 1;
+    const int n0 = (d.nn[0] - px + 1) / 2, n1 = (d.nn[1] - py + 1) / 2, n2 = (d.nn[2] - pz + 1) / 2;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= (int64_t)n0 * n1 * n2) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n2;
+    const int K = 2 * (int)(tt - q * (uint32_t)n2) + pz;
+    const int J = 2 * (int)(q % (uint32_t)n1) + py, I = 2 * (int)(q / (uint32_t)n1) + px;
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+    q2_gather<T, false>(d, Kg, Y, u, I, J, K, s0, s1, s2, nullptr);
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = zeroDir ? dmask[n] : 0;
+    out[n] = (dm & 1) ? T(0) : -s0;
+    out[ld + n] = (dm & 2) ? T(0) : -s1;
+    out[2 * ld + n] = (dm & 4) ? T(0) : -s2;
+}
+
+// One colour (a, b, c) of the 27-colour block Gauss-Seidel sweep: nodes a + inc_a * s along x
+// (inc 4 for corner-type a in {0, 2}, 2 for the middle a = 1), likewise in y and z.
+template <typename T>
+__global__ void __launch_bounds__(BS) gs_q2_color_kernel(Q2Dims d, const T *Kg, const T *__restrict__ Y, T *u,
+                                                         const T *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                         int ca, int cb, int cc, int forward) {
+    const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
+    const int n0 = (d.nn[0] - 1 - ca) / ia + 1, n1 = (d.nn[1] - 1 - cb) / ib + 1, n2 = (d.nn[2] - 1 - cc) / ic + 1;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2] || t >= (int64_t)n0 * n1 * n2) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n2;
+    const int K = cc + ic * (int)(tt - q * (uint32_t)n2);
+    const int J = cb + ib * (int)(q % (uint32_t)n1), I = ca + ia * (int)(q / (uint32_t)n1);
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    T M[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+    q2_gather<T, true>(d, Kg, Y, u, I, J, K, s0, s1, s2, M);
+    T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    if (dm) {
+        // pointwise Gauss-Seidel on the free components (MultigridSolver.hh:352-366)
+        T dd[3] = {T(0), T(0), T(0)};
+        const T bs[3] = {s0, s1, s2};
+        if (forward) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                dd[r] = (bs[r] - (M[3 * r] * dd[0] + M[3 * r + 1] * dd[1] + M[3 * r + 2] * dd[2])) *
+                        (T(!((dm >> r) & 1)) / M[4 * r]);
+        } else {
+#pragma unroll
+            for (int r = 2; r >= 0; --r)
+                dd[r] = (bs[r] - (M[3 * r] * dd[0] + M[3 * r + 1] * dd[1] + M[3 * r + 2] * dd[2])) *
+                        (T(!((dm >> r) & 1)) / M[4 * r]);
+        }
+        u0 += dd[0];
+        u1 += dd[1];
+        u2 += dd[2];
+    } else {
+        const T c00 = M[4] * M[8] - M[5] * M[7], c01 = M[5] * M[6] - M[3] * M[8], c02 = M[3] * M[7] - M[4] * M[6];
+        const T id = T(1) / (M[0] * c00 + M[1] * c01 + M[2] * c02);
+        u0 += (c00 * s0 + (M[2] * M[7] - M[1] * M[8]) * s1 + (M[1] * M[5] - M[2] * M[4]) * s2) * id;
+        u1 += (c01 * s0 + (M[0] * M[8] - M[2] * M[6]) * s1 + (M[2] * M[3] - M[0] * M[5]) * s2) * id;
+        u2 += (c02 * s0 + (M[1] * M[6] - M[0] * M[7]) * s1 + (M[0] * M[4] - M[1] * M[3]) * s2) * id;
+    }
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
+// Coarse Q2 shape functions along one axis at fine node f (0 <= f <= 4 nec): the coarse element
+// e = min(f / 4, nec - 1), reference coordinate x = (f - 4e) / 4, equispaced quadratic Lagrange
+// basis N0 = 2 (x - 1/2)(x - 1), N1 = -4 x (x - 1), N2 = 2 x (x - 1/2) on coarse nodes 2e + lc.
+__device__ __forceinline__ double q2_basis(int lc, double x) {
+    return lc == 0 ? 2 * (x - 0.5) * (x - 1.0) : (lc == 1 ? -4 * x * (x - 1.0) : 2 * x * (x - 0.5));
+}
+
+__device__ __forceinline__ void q2_axis(int f, int nec, int &base, double w[3]) {
+    int e = f >> 2;
+    if (e >= nec) e = nec - 1;
+    base = 2 * e;
+    const double x = 0.25 * (f - 4 * e);
+#pragma unroll
+    for (int lc = 0; lc < 3; ++lc) w[lc] = q2_basis(lc, x);
+}
+
+// fine (=|+=) P coarse: the coarse Q2 interpolant evaluated at the fine nodes (MultigridSolver.hh:137-212)
+template <typename T>
+__global__ void __launch_bounds__(BS) interp_q2_kernel(Q2Dims df, Q2Dims dc, const T *__restrict__ coarse,
+                                                       T *__restrict__ fine, int accumulate) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= df.NN) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)df.nn[2];
+    const int F[3] = {(int)(q / (uint32_t)df.nn[1]), (int)(q % (uint32_t)df.nn[1]), (int)(tt - q * (uint32_t)df.nn[2])};
+    int base[3];
+    double w[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) q2_axis(F[a], dc.ne[a], base[a], w[a]);
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < 3; ++a) {
+        if (w[0][a] == 0.0) continue;
+        for (int b = 0; b < 3; ++b) {
+            if (w[1][b] == 0.0) continue;
+            for (int c = 0; c < 3; ++c) {
+                const double wt = w[0][a] * w[1][b] * w[2][c];
+                if (wt == 0.0) continue;
+                const int64_t cn = q2node(dc, base[0] + a, base[1] + b, base[2] + c);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += wt * (double)coarse[r * dc.NN + cn];
+            }
+        }
+    }
+    const int64_t n = q2node(df, F[0], F[1], F[2]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) fine[r * df.NN + n] = (accumulate ? fine[r * df.NN + n] : T(0)) + (T)acc[r];
+}
+
+// coarse = P^T fine: coarse node C gathers the fine nodes [2C - 3, 2C + 3] (per axis) whose
+// interpolation stencil contains it, with the same weights (MultigridSolver.hh:217-275)
+template <typename T>
+__global__ void __launch_bounds__(BS) restrict_q2_kernel(Q2Dims df, Q2Dims dc, const T *__restrict__ fine,
+                                                         T *__restrict__ coarse) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= dc.NN) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)dc.nn[2];
+    const int C[3] = {(int)(q / (uint32_t)dc.nn[1]), (int)(q % (uint32_t)dc.nn[1]), (int)(tt - q * (uint32_t)dc.nn[2])};
+    double wt[3][7];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int s = 0; s < 7; ++s) {
+            const int f = 2 * C[a] - 3 + s;
+            double wv = 0.0;
+            if (f >= 0 && f < df.nn[a]) {
+                int e = f >> 2;
+                if (e >= dc.ne[a]) e = dc.ne[a] - 1;
+                const int lc = C[a] - 2 * e;
+                if (lc >= 0 && lc <= 2) wv = q2_basis(lc, 0.25 * (f - 4 * e));
+            }
+            wt[a][s] = wv;
+        }
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int s = 0; s < 7; ++s) {
+        if (wt[0][s] == 0.0) continue;
+        for (int v = 0; v < 7; ++v) {
+            if (wt[1][v] == 0.0) continue;
+            for (int z = 0; z < 7; ++z) {
+                const double w = wt[0][s] * wt[1][v] * wt[2][z];
+                if (w == 0.0) continue;
+                const int64_t fn = q2node(df, 2 * C[0] - 3 + s, 2 * C[1] - 3 + v, 2 * C[2] - 3 + z);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += w * (double)fine[r * df.NN + fn];
+            }
+        }
+    }
+    const int64_t cn = q2node(dc, C[0], C[1], C[2]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) coarse[r * dc.NN + cn] = (T)acc[r];
+}
+
+Q2Dims dims_of(const int ne[3]) {
+    Q2Dims d;
+    for (int a = 0; a < 3; ++a) {
+        d.ne[a] = ne[a];
+        d.nn[a] = 2 * ne[a] + 1;
+    }
+    d.NN = (int64_t)d.nn[0] * d.nn[1] * d.nn[2];
+    d.NE = (int64_t)ne[0] * ne[1] * ne[2];
+    return d;
+}
+
+}  // namespace
+
+void q2_upload_k0f(const float *K0f, cudaStream_t st) {
+    VFEM_CUDA(cudaMemcpyToSymbolAsync(c_K0q2f, K0f, sizeof(float) * 81 * 81, 0, cudaMemcpyHostToDevice, st));
+}
+
+template <typename T>
+void launch_applyk_q2(const int ne[3], const T *K0, const T *Y, const T *u, T *out, const uint8_t *dmask,
+                      bool zeroDirichlet, cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    const int64_t per = (int64_t)(ne[0] + 1) * (ne[1] + 1) * (ne[2] + 1);  // largest parity class
+    applyk_q2_kernel<T><<<dim3(gridFor(per, BS), 8), BS, 0, st>>>(d, K0, Y, u, out, dmask, zeroDirichlet ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_gs_q2_sweep(const int ne[3], const T *K0, const T *Y, T *u, const T *b, const uint8_t *dmask, bool forward,
+                        cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    for (int s = 0; s < 27; ++s) {
+        const int col = forward ? s : 26 - s;
+        const int ca = col / 9, cb = (col / 3) % 3, cc = col % 3;
+        const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
+        if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2]) continue;
+        const int64_t cnt = (int64_t)((d.nn[0] - 1 - ca) / ia + 1) * ((d.nn[1] - 1 - cb) / ib + 1) *
+                            ((d.nn[2] - 1 - cc) / ic + 1);
+        gs_q2_color_kernel<T><<<gridFor(cnt, BS), BS, 0, st>>>(d, K0, Y, u, b, dmask, ca, cb, cc, forward ? 1 : 0);
+        VFEM_LAUNCH_CHECK();
+    }
+}
+
+template <typename T>
+void launch_restrict_q2(const int neFine[3], const T *fine, T *coarse, cudaStream_t st) {
+    const int nec[3] = {neFine[0] / 2, neFine[1] / 2, neFine[2] / 2};
+    const Q2Dims df = dims_of(neFine), dc = dims_of(nec);
+    restrict_q2_kernel<T><<<gridFor(dc.NN, BS), BS, 0, st>>>(df, dc, fine, coarse);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_interp_q2(const int neFine[3], const T *coarse, T *fine, bool accumulate, cudaStream_t st) {
+    const int nec[3] = {neFine[0] / 2, neFine[1] / 2, neFine[2] / 2};
+    const Q2Dims df = dims_of(neFine), dc = dims_of(nec);
+    interp_q2_kernel<T><<<gridFor(df.NN, BS), BS, 0, st>>>(df, dc, coarse, fine, accumulate ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+#define VFEM_INST_Q2(T)                                                                                               \
+    template void launch_applyk_q2<T>(const int[3], const T *, const T *, const T *, T *, const uint8_t *, bool,      \
+                                      cudaStream_t);                                                                  \
+    template void launch_gs_q2_sweep<T>(const int[3], const T *, const T *, T *, const T *, const uint8_t *, bool,    \
+                                        cudaStream_t);                                                                \
+    template void launch_restrict_q2<T>(const int[3], const T *, T *, cudaStream_t);                                  \
+    template void launch_interp_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);
+VFEM_INST_Q2(double)
+VFEM_INST_Q2(float)
+
+}  // namespace vfem

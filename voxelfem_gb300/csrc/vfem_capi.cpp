@@ -446,4 +446,106 @@ int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, in
     });
 }
 
+// ---- triquadratic voxels ----
+struct vfem_q2 {
+    GridQ2 g;
+    vfem_q2(const int ne[3], const double mn[3], const double mx[3]) : g(ne, mn, mx) {}
+};
+int vfem_q2_create(const int64_t elems[3], const double bbox_min[3], const double bbox_max[3], vfem_q2 **out) {
+    return guarded([&] {
+        need(elems, "elems");
+        need(out, "out");
+        int ne[3];
+        for (int d = 0; d < 3; ++d) {
+            if (elems[d] <= 0 || elems[d] > (1 << 20)) throw Error(ERR_ARG, "elementsPerDimension out of range");
+            ne[d] = (int)elems[d];
+        }
+        *out = new vfem_q2(ne, bbox_min, bbox_max);
+    });
+}
+int vfem_q2_destroy(vfem_q2 *g) {
+    return guarded([&] { delete g; });
+}
+int vfem_q2_dims(const vfem_q2 *g, int64_t *num_nodes, int64_t *num_elements) {
+    return guarded([&] {
+        need(g, "grid");
+        if (num_nodes) *num_nodes = g->g.NN;
+        if (num_elements) *num_elements = g->g.NE;
+    });
+}
+int vfem_q2_set_etensor(vfem_q2 *g, double young, double poisson) {
+    return guarded([&] { need(g, "grid"); g->g.setETensor(young, poisson); });
+}
+int vfem_q2_set_material_params(vfem_q2 *g, double E0, double Emin, double gamma, double q, int law) {
+    return guarded([&] {
+        need(g, "grid");
+        if (law != 0 && law != 1) throw Error(ERR_ARG, "unknown interpolation law");
+        g->g.setParams(E0, Emin, gamma, q, law);
+    });
+}
+int vfem_q2_set_densities(vfem_q2 *g, const double *rho) {
+    return guarded([&] { need(g, "grid"); need(rho, "rho"); g->g.setDensities(rho); });
+}
+int vfem_q2_get_k0(const vfem_q2 *g, double *out6561) {
+    return guarded([&] { need(g, "grid"); need(out6561, "out"); std::memcpy(out6561, g->g.K0.data(), 6561 * sizeof(double)); });
+}
+int vfem_q2_add_dirichlet(vfem_q2 *g, const double min_corner[3], const double max_corner[3], int cmask) {
+    return guarded([&] {
+        need(g, "grid");
+        need(min_corner, "min_corner");
+        need(max_corner, "max_corner");
+        g->g.addDirichlet(min_corner, max_corner, (unsigned)cmask);
+    });
+}
+int vfem_q2_get_dirichlet_mask(const vfem_q2 *g, uint8_t *mask_out) {
+    return guarded([&] {
+        need(g, "grid");
+        need(mask_out, "out");
+        if (isDevicePtr(mask_out)) VFEM_CUDA(cudaMemcpy(mask_out, g->g.dmask_h.data(), g->g.NN, cudaMemcpyHostToDevice));
+        else std::memcpy(mask_out, g->g.dmask_h.data(), g->g.NN);
+    });
+}
+int vfem_q2_apply_k(vfem_q2 *g, const double *u, double *out, int precision, int zero_dirichlet) {
+    return guarded([&] {
+        need(g, "grid");
+        need(u, "u");
+        need(out, "out");
+        g->g.applyK(u, out, precision, zero_dirichlet != 0);
+    });
+}
+int vfem_q2_smooth(vfem_q2 *g, double *u_inout, const double *b, int forward, int precision) {
+    return guarded([&] {
+        need(g, "grid");
+        need(u_inout, "u");
+        need(b, "b");
+        g->g.smooth(u_inout, b, forward != 0, precision);
+    });
+}
+int vfem_q2_restrict(const int64_t elems_fine[3], const double *fine, double *coarse) {
+    return guarded([&] {
+        need(elems_fine, "elems");
+        need(fine, "fine");
+        need(coarse, "coarse");
+        const int ne[3] = {(int)elems_fine[0], (int)elems_fine[1], (int)elems_fine[2]};
+        q2Restrict(ne, fine, coarse);
+    });
+}
+int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, double *fine, int accumulate) {
+    return guarded([&] {
+        need(elems_fine, "elems");
+        need(fine, "fine");
+        need(coarse, "coarse");
+        const int ne[3] = {(int)elems_fine[0], (int)elems_fine[1], (int)elems_fine[2]};
+        q2Interpolate(ne, coarse, fine, accumulate != 0);
+    });
+}
+int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes) {
+    return guarded([&] {
+        need(g, "grid");
+        need(ms, "ms");
+        need(bytes, "bytes");
+        *ms = g->g.timeApplyK(precision, reps, bytes);
+    });
+}
+
 }  // extern "C"

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "vfem_kernels.hpp"
 
@@ -88,6 +89,54 @@ void coarsen_element(const double phi[64], const double Kf[576], double Kc[576])
                 for (int fm = 0; fm < 8; ++fm) s += phi[fm * 8 + cm] * T[(3 * fm + d) * 24 + c];
                 Kc[(3 * cm + d) * 24 + c] += s;
             }
+}
+
+// Equispaced quadratic Lagrange basis on [0, 1] (nodes 0, 1/2, 1) and its derivative.
+static void q2_basis1d(double x, double v[3], double dv[3]) {
+    v[0] = 2 * (x - 0.5) * (x - 1.0);
+    v[1] = -4 * x * (x - 1.0);
+    v[2] = 2 * x * (x - 0.5);
+    dv[0] = 4 * x - 3;
+    dv[1] = -8 * x + 4;
+    dv[2] = 4 * x - 1;
+}
+
+void element_stiffness_q2(double E, double nu, const double h[3], double K0[6561]) {
+    const double lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+    const double mu = E / (2 * (1 + nu));
+    const double r = 0.5 * std::sqrt(0.6);
+    const double qp[3] = {0.5 - r, 0.5, 0.5 + r}, qw[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
+    std::vector<double> acc(6561, 0.0);
+    for (int qa = 0; qa < 3; ++qa)
+        for (int qb = 0; qb < 3; ++qb)
+            for (int qc = 0; qc < 3; ++qc) {
+                const double w = qw[qa] * qw[qb] * qw[qc];
+                double v[3][3], dv[3][3];
+                q2_basis1d(qp[qa], v[0], dv[0]);
+                q2_basis1d(qp[qb], v[1], dv[1]);
+                q2_basis1d(qp[qc], v[2], dv[2]);
+                double G[27][3];
+                for (int l = 0; l < 27; ++l) {
+                    const int a = l / 9, b = (l / 3) % 3, c = l % 3;
+                    G[l][0] = dv[0][a] * v[1][b] * v[2][c] / h[0];
+                    G[l][1] = v[0][a] * dv[1][b] * v[2][c] / h[1];
+                    G[l][2] = v[0][a] * v[1][b] * dv[2][c] / h[2];
+                }
+                for (int a = 0; a < 27; ++a)
+                    for (int c = 0; c < 3; ++c)
+                        for (int b = 0; b < 27; ++b)
+                            for (int d = 0; d < 3; ++d) {
+                                const double dot = G[a][0] * G[b][0] + G[a][1] * G[b][1] + G[a][2] * G[b][2];
+                                const double ee = 0.5 * ((c == d ? dot : 0.0) + G[a][d] * G[b][c]);
+                                acc[(3 * a + c) * 81 + 3 * b + d] += w * (lam * G[a][c] * G[b][d] + 2 * mu * ee);
+                            }
+            }
+    const double vol = h[0] * h[1] * h[2];
+    for (int i = 0; i < 81; ++i)
+        for (int j = i; j < 81; ++j) {
+            K0[i * 81 + j] = acc[i * 81 + j] * vol;
+            K0[j * 81 + i] = K0[i * 81 + j];
+        }
 }
 
 bool k0_cube_values(const double *K, double kv[10]) {

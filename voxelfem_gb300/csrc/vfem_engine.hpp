@@ -300,6 +300,54 @@ private:
     void jacobianDev(double *out);
 };
 
+// Triquadratic voxel grid (vfem_q2.cpp): K0, moduli, supports, applyK and the 27-colour
+// block Gauss-Seidel sweep.
+class GridQ2 {
+public:
+    GridQ2(const int ne[3], const double bmin[3], const double bmax[3]);
+    ~GridQ2();
+    GridQ2(const GridQ2 &) = delete;
+    GridQ2 &operator=(const GridQ2 &) = delete;
+    int ne[3], nn[3];
+    int64_t NN, NE;
+    double bmin[3], bmax[3], h[3];
+    double Eyoung = 1.0, nu = 0.0, E0 = 1.0, Emin = 1e-4, gamma = 3.0, q = 3.0;
+    int law = 0;
+    Geom egeom;  // element grid (for the moduli kernel)
+    std::vector<double> K0;
+    std::vector<float> K0f;
+    DevBuf<double> K0d, rho, Y;
+    DevBuf<float> Yf;
+    std::vector<uint8_t> dmask_h;
+    DevBuf<uint8_t> dmask;
+    LevelData<double> w64;
+    LevelData<float> w32;
+    cudaStream_t stream = nullptr;
+
+    void setETensor(double E, double nu);
+    void setParams(double E0_, double Emin_, double gamma_, double q_, int law_);
+    void setDensities(const double *rho);
+    void addDirichlet(const double mn[3], const double mx[3], unsigned cmask);
+    void applyK(const double *u, double *out, int precision, bool zeroDirichlet);
+    void smooth(double *u, const double *b, bool forward, int precision);
+    double timeApplyK(int precision, int reps, double *bytes);
+
+private:
+    void updateYoungModuli();
+    void uploadMask();
+    template <typename T>
+    LevelData<T> &work();
+    template <typename T>
+    const T *kernelK0();
+    template <typename T>
+    void applyKT(const double *u, double *out, bool zeroDirichlet);
+    template <typename T>
+    void smoothT(double *u, const double *b, bool forward);
+};
+// Q2 restriction / prolongation between a grid with neFine elements per axis and its 2x coarsening.
+void q2Restrict(const int neFine[3], const double *fine, double *coarse);
+void q2Interpolate(const int neFine[3], const double *coarse, double *fine, bool accumulate);
+
 // Layer-by-layer solves of partial-build heights (layers[t] element layers built) over
 // persistent concurrent solver instances cloned from `src` (vfem_lbl.cpp).
 class LBL {

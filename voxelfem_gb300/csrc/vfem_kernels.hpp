@@ -221,4 +221,20 @@ void launch_oc_update(int64_t n, const double *x0, const double *dJ, const doubl
                       double p, double *out, cudaStream_t st);
 void launch_sum_partials(const double *x, int64_t n, double *partials, cudaStream_t st);
 
+// ---------------- triquadratic voxels (k_q2.cu) ----------------
+// K0 is 81 x 81 (device pointer, FP64 kernels); the FP32 kernels read the copy uploaded with
+// q2_upload_k0f. ne = elements per axis; vectors are (3, (2ne+1)^3) SoA.
+void q2_upload_k0f(const float *K0f, cudaStream_t st);
+template <typename T>
+void launch_applyk_q2(const int ne[3], const T *K0, const T *Y, const T *u, T *out, const uint8_t *dmask,
+                      bool zeroDirichlet, cudaStream_t st);
+// one block Gauss-Seidel sweep over the 27 colours (forward 0..26, backward 26..0)
+template <typename T>
+void launch_gs_q2_sweep(const int ne[3], const T *K0, const T *Y, T *u, const T *b, const uint8_t *dmask, bool forward,
+                        cudaStream_t st);
+template <typename T>
+void launch_restrict_q2(const int neFine[3], const T *fine, T *coarse, cudaStream_t st);
+template <typename T>
+void launch_interp_q2(const int neFine[3], const T *coarse, T *fine, bool accumulate, cudaStream_t st);
+
 }  // namespace vfem

@@ -1,0 +1,228 @@
+// Triquadratic voxel grid (TensorProductSimulator<Real, 2, 2, 2>, TPSStencils.hh:135-186): the
+// element stiffness, SIMP moduli, zero-displacement supports, the matrix-free applyK and the
+// 27-colour block Gauss-Seidel sweep of the reference's generic (Q2) multigrid smoother
+// (MultigridSolver.hh:277-321, 409-442), in FP64 or FP32, and timing hooks.
+#include "vfem_engine.hpp"
+
+#include <cstring>
+#include <type_traits>
+
+#include "vfem_element.hpp"
+
+namespace vfem {
+
+GridQ2::GridQ2(const int ne_[3], const double bmin_[3], const double bmax_[3]) {
+    for (int d = 0; d < 3; ++d) {
+        if (ne_[d] <= 0) throw Error(ERR_ARG, "elementsPerDimension must be positive");
+        if (!(bmax_[d] > bmin_[d])) throw Error(ERR_ARG, "invalid domain bounding box");
+        ne[d] = ne_[d];
+        nn[d] = 2 * ne_[d] + 1;
+        bmin[d] = bmin_[d];
+        bmax[d] = bmax_[d];
+        h[d] = (bmax[d] - bmin[d]) / ne[d];
+    }
+    NN = (int64_t)nn[0] * nn[1] * nn[2];
+    NE = (int64_t)ne[0] * ne[1] * ne[2];
+    if (3 * NN >= (int64_t(1) << 31)) throw Error(ERR_ARG, "grid too large");
+    VFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    egeom = makeGeom(ne);
+    rho.alloc(NE);
+    Y.alloc(NE);
+    Yf.alloc(NE);
+    VFEM_CUDA(cudaMemsetAsync(rho.p, 0, NE * sizeof(double), stream));
+    dmask_h.assign(NN, 0);
+    dmask.alloc(NN);
+    K0.assign(6561, 0.0);
+    K0f.assign(6561, 0.f);
+    K0d.alloc(6561);
+    uploadMask();
+    setETensor(1.0, 0.0);
+    updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+GridQ2::~GridQ2() {
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void GridQ2::setETensor(double E, double nu_) {
+    if (!(nu_ < 0.5) || !(nu_ > -1.0)) throw Error(ERR_ARG, "Poisson ratio must lie in (-1, 0.5)");
+    Eyoung = E;
+    nu = nu_;
+    element_stiffness_q2(E, nu, h, K0.data());
+    for (int t = 0; t < 6561; ++t) K0f[t] = (float)K0[t];
+    VFEM_CUDA(cudaMemcpy(K0d.p, K0.data(), 6561 * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+void GridQ2::setParams(double E0_, double Emin_, double gamma_, double q_, int law_) {
+    E0 = E0_;
+    Emin = Emin_;
+    gamma = gamma_;
+    q = q_;
+    law = law_;
+    updateYoungModuli();
+}
+
+void GridQ2::updateYoungModuli() {
+    launch_young_moduli<double>(egeom, rho.p, Y.p, E0, Emin, gamma, q, law, false, stream);
+    launch_cast<float, double>(Y.p, Yf.p, NE, stream);
+}
+
+void GridQ2::setDensities(const double *r) {
+    VFEM_CUDA(cudaMemcpyAsync(rho.p, r, NE * sizeof(double), cudaMemcpyDefault, stream));
+    updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+void GridQ2::uploadMask() {
+    VFEM_CUDA(cudaMemcpyAsync(dmask.p, dmask_h.data(), NN, cudaMemcpyHostToDevice, stream));
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+}
+
+// Zero-displacement supports on the nodes inside the box [mn, mx] (node (I, J, K) at
+// bmin + (I, J, K) h / 2), components in cmask.
+void GridQ2::addDirichlet(const double mn[3], const double mx[3], unsigned cmask) {
+    for (int I = 0; I < nn[0]; ++I) {
+        const double px = bmin[0] + 0.5 * I * h[0];
+        if (px < mn[0] || px > mx[0]) continue;
+        for (int J = 0; J < nn[1]; ++J) {
+            const double py = bmin[1] + 0.5 * J * h[1];
+            if (py < mn[1] || py > mx[1]) continue;
+            for (int K = 0; K < nn[2]; ++K) {
+                const double pz = bmin[2] + 0.5 * K * h[2];
+                if (pz < mn[2] || pz > mx[2]) continue;
+                dmask_h[((int64_t)I * nn[1] + J) * nn[2] + K] |= (uint8_t)(cmask & 7u);
+            }
+        }
+    }
+    uploadMask();
+}
+
+static void allocWork(LevelData<double> &D, int64_t n3) { D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3); }
+static void allocWork(LevelData<float> &D, int64_t n3) { D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3); }
+
+template <>
+LevelData<double> &GridQ2::work<double>() {
+    allocWork(w64, 3 * NN);
+    return w64;
+}
+template <>
+LevelData<float> &GridQ2::work<float>() {
+    allocWork(w32, 3 * NN);
+    return w32;
+}
+
+template <typename T>
+static void toT(const double *src, T *dst, int64_t n, cudaStream_t st) {
+    if (std::is_same<T, double>::value) VFEM_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else launch_cast<float, double>(src, (float *)dst, n, st);
+}
+template <typename T>
+static void fromT(const T *src, double *dst, int64_t n, cudaStream_t st) {
+    if (std::is_same<T, double>::value) VFEM_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else launch_cast<double, float>((const float *)src, dst, n, st);
+}
+
+template <typename T>
+const T *GridQ2::kernelK0() {
+    if (std::is_same<T, float>::value) {
+        q2_upload_k0f(K0f.data(), stream);  // constant memory is shared by every Q2 grid
+        return nullptr;
+    }
+    return (const T *)K0d.p;
+}
+
+template <typename T>
+void GridQ2::applyKT(const double *u, double *out, bool zeroDirichlet) {
+    auto &D = work<T>();
+    const int64_t n3 = 3 * NN;
+    toT<T>(u, D.x.p, n3, stream);
+    const T *Yt = std::is_same<T, double>::value ? (const T *)Y.p : (const T *)Yf.p;
+    launch_applyk_q2<T>(ne, kernelK0<T>(), Yt, D.x.p, D.r.p, dmask.p, zeroDirichlet, stream);
+    fromT<T>(D.r.p, out, n3, stream);
+}
+
+template <typename T>
+void GridQ2::smoothT(double *u, const double *b, bool forward) {
+    auto &D = work<T>();
+    const int64_t n3 = 3 * NN;
+    toT<T>(u, D.x.p, n3, stream);
+    toT<T>(b, D.b.p, n3, stream);
+    const T *Yt = std::is_same<T, double>::value ? (const T *)Y.p : (const T *)Yf.p;
+    launch_gs_q2_sweep<T>(ne, kernelK0<T>(), Yt, D.x.p, D.b.p, dmask.p, forward, stream);
+    fromT<T>(D.x.p, u, n3, stream);
+}
+
+void GridQ2::applyK(const double *u, double *out, int precision, bool zeroDirichlet) {
+    View vu, vo;
+    viewIn(vu, u, 3 * NN * sizeof(double), stream);
+    viewOut(vo, out, 3 * NN * sizeof(double));
+    if (precision == PREC_FP64) applyKT<double>((const double *)vu.d, (double *)vo.d, zeroDirichlet);
+    else applyKT<float>((const double *)vu.d, (double *)vo.d, zeroDirichlet);
+    finishOut(vo, stream);
+}
+
+void GridQ2::smooth(double *u, const double *b, bool forward, int precision) {
+    View vu, vb;
+    viewInOut(vu, u, 3 * NN * sizeof(double), stream);
+    viewIn(vb, b, 3 * NN * sizeof(double), stream);
+    if (precision == PREC_FP64) smoothT<double>((double *)vu.d, (const double *)vb.d, forward);
+    else smoothT<float>((double *)vu.d, (const double *)vb.d, forward);
+    finishOut(vu, stream);
+}
+
+// Average device time of one applyK launch on resident data, with its algorithmic bytes
+// s * (6 NN + NE) (read u, write K u, read E).
+double GridQ2::timeApplyK(int precision, int reps, double *bytes) {
+    if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        auto &D = work<T>();
+        const T *Yt = std::is_same<T, double>::value ? (const T *)Y.p : (const T *)Yf.p;
+        launch_fill<T>(D.x.p, T(0.5), 3 * NN, stream);
+        const T *K = kernelK0<T>();
+        launch_applyk_q2<T>(ne, K, Yt, D.x.p, D.r.p, dmask.p, false, stream);
+        cudaEvent_t e0, e1;
+        VFEM_CUDA(cudaEventCreate(&e0));
+        VFEM_CUDA(cudaEventCreate(&e1));
+        VFEM_CUDA(cudaEventRecord(e0, stream));
+        for (int r = 0; r < reps; ++r) launch_applyk_q2<T>(ne, K, Yt, D.x.p, D.r.p, dmask.p, false, stream);
+        VFEM_CUDA(cudaEventRecord(e1, stream));
+        VFEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        VFEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *bytes = (double)sizeof(T) * (6.0 * NN + NE);
+        return (double)ms / reps;
+    };
+    return precision == PREC_FP64 ? run(double()) : run(float());
+}
+
+void q2Restrict(const int neFine[3], const double *fine, double *coarse) {
+    for (int d = 0; d < 3; ++d)
+        if (neFine[d] % 2) throw Error(ERR_ARG, "Grid size must be divisible by 2 for a coarsening");
+    const int64_t nf = (int64_t)(2 * neFine[0] + 1) * (2 * neFine[1] + 1) * (2 * neFine[2] + 1);
+    const int64_t nc = (int64_t)(neFine[0] + 1) * (neFine[1] + 1) * (neFine[2] + 1);
+    View vf, vc;
+    viewIn(vf, fine, 3 * nf * sizeof(double), 0);
+    viewOut(vc, coarse, 3 * nc * sizeof(double));
+    launch_restrict_q2<double>(neFine, (const double *)vf.d, (double *)vc.d, 0);
+    finishOut(vc, 0);
+    VFEM_CUDA(cudaDeviceSynchronize());
+}
+
+void q2Interpolate(const int neFine[3], const double *coarse, double *fine, bool accumulate) {
+    for (int d = 0; d < 3; ++d)
+        if (neFine[d] % 2) throw Error(ERR_ARG, "Grid size must be divisible by 2 for a coarsening");
+    const int64_t nf = (int64_t)(2 * neFine[0] + 1) * (2 * neFine[1] + 1) * (2 * neFine[2] + 1);
+    const int64_t nc = (int64_t)(neFine[0] + 1) * (neFine[1] + 1) * (neFine[2] + 1);
+    View vc, vf;
+    viewIn(vc, coarse, 3 * nc * sizeof(double), 0);
+    viewInOut(vf, fine, 3 * nf * sizeof(double), 0);
+    launch_interp_q2<double>(neFine, (const double *)vc.d, (double *)vf.d, accumulate, 0);
+    finishOut(vf, 0);
+    VFEM_CUDA(cudaDeviceSynchronize());
+}
+
+}  // namespace vfem

@@ -79,8 +79,10 @@ def _arr3(v):
 def TensorProductSimulator(degreesPerDimension, domainBBox, elementsPerDimension, numberType=NumberType.DOUBLE):
     """Factory of pyVoxelFEM.TensorProductSimulator (VoxelFEM.cc:423-430)."""
     degs = [int(d) for d in degreesPerDimension]
-    if degs != [1, 1, 1] or int(numberType) != int(NumberType.DOUBLE):
+    if int(numberType) != int(NumberType.DOUBLE) or degs not in ([1, 1, 1], [2, 2, 2]):
         raise RuntimeError("No template instantiation matching degreesPerDimension/number type!")
+    if degs == [2, 2, 2]:
+        return TensorProductSimulator_3D_Q2(domainBBox, elementsPerDimension)
     return TensorProductSimulator_3D(domainBBox, elementsPerDimension)
 
 
@@ -857,6 +859,131 @@ class OCOptimizer:
         check(_lib().vfem_problem_oc_step(self.problem._h, float(m), float(p), float(ctol), C.byref(probes)))
         self.lastProbes = probes.value
         self.problem.filterChain.setDesignVars(self.problem.getVars())
+
+
+class TensorProductSimulator_3D_Q2:
+    """TensorProductSimulator<double, 2, 2, 2>: triquadratic voxels (27 nodes per element).
+
+    Provides the element stiffness (81 x 81), SIMP moduli, zero-displacement supports, ``applyK``
+    and the 27-colour block Gauss-Seidel sweep of the reference's generic multigrid smoother
+    (``smoothingMulticoloredGS``), in FP64 or FP32 (``precision="fp32"``). Nodal fields are
+    (numNodes, 3) with node (I, J, K) at index (I * NY + J) * NZ + K, NY = 2 ny + 1.
+    """
+
+    def __init__(self, domainBBox, elementsPerDimension):
+        bb = [np.asarray(domainBBox[0], dtype=np.float64).reshape(3), np.asarray(domainBBox[1], dtype=np.float64).reshape(3)]
+        ne = np.ascontiguousarray(np.asarray(elementsPerDimension, dtype=np.int64).reshape(3))
+        h = C.c_void_p()
+        check(_lib().vfem_q2_create(ne.ctypes.data_as(_capi._i64), _capi.dptr(np.ascontiguousarray(bb[0])),
+                                    _capi.dptr(np.ascontiguousarray(bb[1])), C.byref(h)))
+        self._h = h
+        self._ne = tuple(int(v) for v in ne)
+        self._nn = (2 * self._ne[0] + 1) * (2 * self._ne[1] + 1) * (2 * self._ne[2] + 1)
+        self._nel = self._ne[0] * self._ne[1] * self._ne[2]
+        self._E = (1.0, 0.0)
+        self._params = [1.0, 1e-4, 3.0, 3.0, 0]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_q2_destroy(h)
+            self._h = None
+
+    def numNodes(self):
+        return self._nn
+
+    def numElements(self):
+        return self._nel
+
+    @property
+    def NbElementsPerDimension(self):
+        return np.array(self._ne)
+
+    @property
+    def NbNodesPerDimension(self):
+        return np.array([2 * v + 1 for v in self._ne])
+
+    @property
+    def ETensor(self):
+        return self._E
+
+    @ETensor.setter
+    def ETensor(self, value):
+        E, nu = value
+        check(_lib().vfem_q2_set_etensor(self._h, float(E), float(nu)))
+        self._E = (float(E), float(nu))
+
+    def _set_param(self, idx, value):
+        self._params[idx] = value
+        p = self._params
+        check(_lib().vfem_q2_set_material_params(self._h, float(p[0]), float(p[1]), float(p[2]), float(p[3]),
+                                                 int(p[4])))
+
+    E_0 = property(lambda self: self._params[0], lambda self, v: self._set_param(0, float(v)))
+    E_min = property(lambda self: self._params[1], lambda self, v: self._set_param(1, float(v)))
+    gamma = property(lambda self: self._params[2], lambda self, v: self._set_param(2, float(v)))
+    q = property(lambda self: self._params[3], lambda self, v: self._set_param(3, float(v)))
+
+    def fullDensityElementStiffnessMatrix(self):
+        K = np.empty(6561)
+        check(_lib().vfem_q2_get_k0(self._h, _capi.dptr(K)))
+        return K.reshape(81, 81)
+
+    def setDensities(self, rho):
+        a = _as_elems(rho, self._nel)
+        if np.any(a > 1.0) or np.any(a < 0.0):
+            raise RuntimeError("Density value has to be in between 0 and 1")
+        check(_lib().vfem_q2_set_densities(self._h, ptr(a)))
+
+    def addDirichletCondition(self, minCorner, maxCorner, componentMask="xyz"):
+        """Zero-displacement supports on the nodes inside the box."""
+        check(_lib().vfem_q2_add_dirichlet(self._h, _capi.dptr(_arr3(minCorner)), _capi.dptr(_arr3(maxCorner)),
+                                           _cmask(componentMask)))
+
+    def getDirichletMask(self):
+        m = np.empty(self._nn, dtype=np.uint8)
+        check(_lib().vfem_q2_get_dirichlet_mask(self._h, m.ctypes.data_as(C.c_void_p)))
+        return np.stack([(m >> c) & 1 for c in range(3)], axis=1).astype(bool)
+
+    def applyK(self, u, precision="fp64", zeroDirichlet=False):
+        u = _as_vfield(u, self._nn)
+        out = _new_vfield(self._nn)
+        p = {"fp64": 0, "fp32": 1}[precision]
+        check(_lib().vfem_q2_apply_k(self._h, ptr(u), ptr(out), p, int(bool(zeroDirichlet))))
+        return out
+
+    def smoothingMulticoloredGS(self, u, b, forwardSweep=True, precision="fp64"):
+        x = _as_vfield(u, self._nn).copy(order="F")
+        b = _as_vfield(b, self._nn)
+        p = {"fp64": 0, "fp32": 1}[precision]
+        check(_lib().vfem_q2_smooth(self._h, ptr(x), ptr(b), int(bool(forwardSweep)), p))
+        return x
+
+    def multigridSolver(self, numCoarseningLevels):
+        raise RuntimeError("Multigrid solves on triquadratic grids are not available (applyK, smoothing and "
+                           "transfers are)")
+
+
+def q2_restriction(elementsPerDimensionFine, fine):
+    """Q2 restriction P^T from a grid with the given elements per axis to its 2x coarsening."""
+    ne = np.ascontiguousarray(np.asarray(elementsPerDimensionFine, dtype=np.int64).reshape(3))
+    nf = int(np.prod(2 * ne + 1))
+    nc = int(np.prod(ne + 1))
+    fine = _as_vfield(fine, nf)
+    out = _new_vfield(nc)
+    check(_lib().vfem_q2_restrict(ne.ctypes.data_as(C.c_void_p), ptr(fine), ptr(out)))
+    return out
+
+
+def q2_interpolation(elementsPerDimensionFine, coarse, fine=None, accumulate=False):
+    """Q2 prolongation P (coarse quadratic interpolant at the fine nodes)."""
+    ne = np.ascontiguousarray(np.asarray(elementsPerDimensionFine, dtype=np.int64).reshape(3))
+    nf = int(np.prod(2 * ne + 1))
+    nc = int(np.prod(ne + 1))
+    coarse = _as_vfield(coarse, nc)
+    out = _new_vfield(nf) if fine is None else _as_vfield(fine, nf).copy(order="F")
+    check(_lib().vfem_q2_interpolate(ne.ctypes.data_as(C.c_void_p), ptr(coarse), ptr(out), int(bool(accumulate))))
+    return out
 
 
 class LayerByLayerEvaluator:
