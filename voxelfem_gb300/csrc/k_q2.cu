@@ -11,6 +11,8 @@
 // memory (FP32, 26 KB) or in global memory (FP64, 52 KB) and its reads are broadcasts.
 #include "vfem_kernels.hpp"
 
+#include <type_traits>
+
 namespace vfem {
 
 __constant__ float c_K0q2f[81 * 81];
@@ -90,6 +92,100 @@ __device__ __forceinline__ void q2_gather(const Q2Dims &d, const T *Kg, const T 
             }
 }
 
+// FP32 form with the node parity (PX, PY, PZ) as template parameters: every incident-element
+// slot has a compile-time local index, so each K0 entry is a constant-bank operand of its FFMA
+// (no load instruction). Even axes have two slots (local 0 of element I/2, local 2 of element
+// I/2 - 1, either may fall outside the grid), odd axes one (local 1 of element (I-1)/2).
+template <int P>
+__device__ __forceinline__ bool q2_slot(int I, int ne, int s, int &e) {
+    if (P) {
+        e = (I - 1) >> 1;
+        return true;
+    }
+    e = s == 0 ? (I >> 1) : (I >> 1) - 1;
+    return e >= 0 && e < ne;
+}
+
+template <int P, int S>
+struct Q2Local {
+    static constexpr int value = P ? 1 : (S == 0 ? 0 : 2);
+};
+
+template <int PX, int PY, int PZ, bool WithM>
+__device__ __forceinline__ void q2_gather_f32(const Q2Dims &d, const float *__restrict__ Y, const float *__restrict__ u,
+                                              int I, int J, int K, float &s0, float &s1, float &s2, float *M);
+
+template <int PX, int PY, int PZ, bool WithM, int SA, int SB, int SC>
+__device__ __forceinline__ void q2_slot_f32(const Q2Dims &d, const float *__restrict__ Y, const float *__restrict__ u,
+                                            int I, int J, int K, float &s0, float &s1, float &s2, float *M) {
+    int ei, ej, ek;
+    if (!q2_slot<PX>(I, d.ne[0], SA, ei) || !q2_slot<PY>(J, d.ne[1], SB, ej) || !q2_slot<PZ>(K, d.ne[2], SC, ek)) return;
+    constexpr int LN = 9 * Q2Local<PX, SA>::value + 3 * Q2Local<PY, SB>::value + Q2Local<PZ, SC>::value;
+    const float E = Y[((int64_t)ei * d.ne[1] + ej) * d.ne[2] + ek];
+    const int64_t ld = d.NN;
+    const int64_t base = q2node(d, 2 * ei, 2 * ej, 2 * ek);
+    const int64_t sx = (int64_t)d.nn[1] * d.nn[2], sy = d.nn[2];
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+#pragma unroll
+    for (int m = 0; m < 27; ++m) {
+        const int64_t nm = base + (m / 9) * sx + ((m / 3) % 3) * sy + (m % 3);
+        const float u0 = u[nm], u1 = u[ld + nm], u2 = u[2 * ld + nm];
+        c0 += c_K0q2f[(3 * m) * 81 + 3 * LN] * u0 + c_K0q2f[(3 * m + 1) * 81 + 3 * LN] * u1 +
+              c_K0q2f[(3 * m + 2) * 81 + 3 * LN] * u2;
+        c1 += c_K0q2f[(3 * m) * 81 + 3 * LN + 1] * u0 + c_K0q2f[(3 * m + 1) * 81 + 3 * LN + 1] * u1 +
+              c_K0q2f[(3 * m + 2) * 81 + 3 * LN + 1] * u2;
+        c2 += c_K0q2f[(3 * m) * 81 + 3 * LN + 2] * u0 + c_K0q2f[(3 * m + 1) * 81 + 3 * LN + 2] * u1 +
+              c_K0q2f[(3 * m + 2) * 81 + 3 * LN + 2] * u2;
+    }
+    s0 -= E * c0;
+    s1 -= E * c1;
+    s2 -= E * c2;
+    if (WithM) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) M[3 * r + c] += E * c_K0q2f[(3 * LN + r) * 81 + 3 * LN + c];
+    }
+}
+
+template <int PX, int PY, int PZ, bool WithM>
+__device__ __forceinline__ void q2_gather_f32(const Q2Dims &d, const float *__restrict__ Y, const float *__restrict__ u,
+                                              int I, int J, int K, float &s0, float &s1, float &s2, float *M) {
+    q2_slot_f32<PX, PY, PZ, WithM, 0, 0, 0>(d, Y, u, I, J, K, s0, s1, s2, M);
+    if (!PZ) q2_slot_f32<PX, PY, PZ, WithM, 0, 0, 1>(d, Y, u, I, J, K, s0, s1, s2, M);
+    if (!PY) {
+        q2_slot_f32<PX, PY, PZ, WithM, 0, 1, 0>(d, Y, u, I, J, K, s0, s1, s2, M);
+        if (!PZ) q2_slot_f32<PX, PY, PZ, WithM, 0, 1, 1>(d, Y, u, I, J, K, s0, s1, s2, M);
+    }
+    if (!PX) {
+        q2_slot_f32<PX, PY, PZ, WithM, 1, 0, 0>(d, Y, u, I, J, K, s0, s1, s2, M);
+        if (!PZ) q2_slot_f32<PX, PY, PZ, WithM, 1, 0, 1>(d, Y, u, I, J, K, s0, s1, s2, M);
+        if (!PY) {
+            q2_slot_f32<PX, PY, PZ, WithM, 1, 1, 0>(d, Y, u, I, J, K, s0, s1, s2, M);
+            if (!PZ) q2_slot_f32<PX, PY, PZ, WithM, 1, 1, 1>(d, Y, u, I, J, K, s0, s1, s2, M);
+        }
+    }
+}
+
+template <int PX, int PY, int PZ>
+__global__ void __launch_bounds__(BS) applyk_q2_f32_kernel(Q2Dims d, const float *__restrict__ Y,
+                                                           const float *__restrict__ u, float *__restrict__ out,
+                                                           const uint8_t *__restrict__ dmask, int zeroDir) {
+    const int n0 = (d.nn[0] - PX + 1) / 2, n1 = (d.nn[1] - PY + 1) / 2, n2 = (d.nn[2] - PZ + 1) / 2;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= (int64_t)n0 * n1 * n2) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n2;
+    const int K = 2 * (int)(tt - q * (uint32_t)n2) + PZ;
+    const int J = 2 * (int)(q % (uint32_t)n1) + PY, I = 2 * (int)(q / (uint32_t)n1) + PX;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    q2_gather_f32<PX, PY, PZ, false>(d, Y, u, I, J, K, s0, s1, s2, nullptr);
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = zeroDir ? dmask[n] : 0;
+    out[n] = (dm & 1) ? 0.f : -s0;
+    out[ld + n] = (dm & 2) ? 0.f : -s1;
+    out[2 * ld + n] = (dm & 4) ? 0.f : -s2;
+}
+
 // out = K u at the nodes of one parity class (px, py, pz); constrained components zeroed when asked
 template <typename T>
 __global__ void __launch_bounds__(BS) applyk_q2_kernel(Q2Dims d, const T *Kg, const T *__restrict__ Y,
@@ -110,6 +206,60 @@ __global__ void __launch_bounds__(BS) applyk_q2_kernel(Q2Dims d, const T *Kg, co
     out[n] = (dm & 1) ? T(0) : -s0;
     out[ld + n] = (dm & 2) ? T(0) : -s1;
     out[2 * ld + n] = (dm & 4) ? T(0) : -s2;
+}
+
+template <typename T>
+__device__ __forceinline__ void q2_node_update(uint8_t dm, T s0, T s1, T s2, const T *M, bool forward, T &u0, T &u1,
+                                               T &u2) {
+    if (dm) {
+        // pointwise Gauss-Seidel on the free components (MultigridSolver.hh:352-366)
+        T dd[3] = {T(0), T(0), T(0)};
+        const T bs[3] = {s0, s1, s2};
+        if (forward) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                dd[r] = (bs[r] - (M[3 * r] * dd[0] + M[3 * r + 1] * dd[1] + M[3 * r + 2] * dd[2])) *
+                        (T(!((dm >> r) & 1)) / M[4 * r]);
+        } else {
+#pragma unroll
+            for (int r = 2; r >= 0; --r)
+                dd[r] = (bs[r] - (M[3 * r] * dd[0] + M[3 * r + 1] * dd[1] + M[3 * r + 2] * dd[2])) *
+                        (T(!((dm >> r) & 1)) / M[4 * r]);
+        }
+        u0 += dd[0];
+        u1 += dd[1];
+        u2 += dd[2];
+    } else {
+        const T c00 = M[4] * M[8] - M[5] * M[7], c01 = M[5] * M[6] - M[3] * M[8], c02 = M[3] * M[7] - M[4] * M[6];
+        const T id = T(1) / (M[0] * c00 + M[1] * c01 + M[2] * c02);
+        u0 += (c00 * s0 + (M[2] * M[7] - M[1] * M[8]) * s1 + (M[1] * M[5] - M[2] * M[4]) * s2) * id;
+        u1 += (c01 * s0 + (M[0] * M[8] - M[2] * M[6]) * s1 + (M[2] * M[3] - M[0] * M[5]) * s2) * id;
+        u2 += (c02 * s0 + (M[1] * M[6] - M[0] * M[7]) * s1 + (M[0] * M[4] - M[1] * M[3]) * s2) * id;
+    }
+}
+
+template <int PX, int PY, int PZ>
+__global__ void __launch_bounds__(BS) gs_q2_f32_kernel(Q2Dims d, const float *__restrict__ Y, float *u,
+                                                       const float *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                       int ca, int cb, int cc, int forward) {
+    const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
+    const int n0 = (d.nn[0] - 1 - ca) / ia + 1, n1 = (d.nn[1] - 1 - cb) / ib + 1, n2 = (d.nn[2] - 1 - cc) / ic + 1;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2] || t >= (int64_t)n0 * n1 * n2) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n2;
+    const int K = cc + ic * (int)(tt - q * (uint32_t)n2);
+    const int J = cb + ib * (int)(q % (uint32_t)n1), I = ca + ia * (int)(q / (uint32_t)n1);
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    float s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    float M[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    q2_gather_f32<PX, PY, PZ, true>(d, Y, u, I, J, K, s0, s1, s2, M);
+    float u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    q2_node_update<float>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
 }
 
 // One colour (a, b, c) of the 27-colour block Gauss-Seidel sweep: nodes a + inc_a * s along x
@@ -274,7 +424,20 @@ void launch_applyk_q2(const int ne[3], const T *K0, const T *Y, const T *u, T *o
                       bool zeroDirichlet, cudaStream_t st) {
     const Q2Dims d = dims_of(ne);
     const int64_t per = (int64_t)(ne[0] + 1) * (ne[1] + 1) * (ne[2] + 1);  // largest parity class
-    applyk_q2_kernel<T><<<dim3(gridFor(per, BS), 8), BS, 0, st>>>(d, K0, Y, u, out, dmask, zeroDirichlet ? 1 : 0);
+    if constexpr (std::is_same<T, float>::value) {
+        const unsigned gs = gridFor(per, BS);
+        const int zd = zeroDirichlet ? 1 : 0;
+        applyk_q2_f32_kernel<0, 0, 0><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<0, 0, 1><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<0, 1, 0><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<0, 1, 1><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<1, 0, 0><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<1, 0, 1><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<1, 1, 0><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+        applyk_q2_f32_kernel<1, 1, 1><<<gs, BS, 0, st>>>(d, Y, u, out, dmask, zd);
+    } else {
+        applyk_q2_kernel<T><<<dim3(gridFor(per, BS), 8), BS, 0, st>>>(d, K0, Y, u, out, dmask, zeroDirichlet ? 1 : 0);
+    }
     VFEM_LAUNCH_CHECK();
 }
 
@@ -289,7 +452,23 @@ void launch_gs_q2_sweep(const int ne[3], const T *K0, const T *Y, T *u, const T 
         if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2]) continue;
         const int64_t cnt = (int64_t)((d.nn[0] - 1 - ca) / ia + 1) * ((d.nn[1] - 1 - cb) / ib + 1) *
                             ((d.nn[2] - 1 - cc) / ic + 1);
-        gs_q2_color_kernel<T><<<gridFor(cnt, BS), BS, 0, st>>>(d, K0, Y, u, b, dmask, ca, cb, cc, forward ? 1 : 0);
+        const unsigned gs = gridFor(cnt, BS);
+        const int fw = forward ? 1 : 0;
+        if constexpr (std::is_same<T, float>::value) {
+            const int px = ca == 1, py = cb == 1, pz = cc == 1;
+            switch (4 * px + 2 * py + pz) {
+            case 0: gs_q2_f32_kernel<0, 0, 0><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 1: gs_q2_f32_kernel<0, 0, 1><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 2: gs_q2_f32_kernel<0, 1, 0><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 3: gs_q2_f32_kernel<0, 1, 1><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 4: gs_q2_f32_kernel<1, 0, 0><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 5: gs_q2_f32_kernel<1, 0, 1><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            case 6: gs_q2_f32_kernel<1, 1, 0><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            default: gs_q2_f32_kernel<1, 1, 1><<<gs, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, cc, fw); break;
+            }
+        } else {
+            gs_q2_color_kernel<T><<<gs, BS, 0, st>>>(d, K0, Y, u, b, dmask, ca, cb, cc, fw);
+        }
         VFEM_LAUNCH_CHECK();
     }
 }

@@ -108,6 +108,7 @@ void Grid::setETensor(double E, double nu_) {
     Eyoung = E;
     nu = nu_;
     element_stiffness(E, nu, h, K0.a);
+    ++k0Version;
     for (int t = 0; t < 576; ++t) {
         K0f.a[t] = (float)K0.a[t];
         K0df.hi[t] = (float)K0.a[t];
@@ -429,8 +430,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     partialCount = std::max<int>(REDUCE_BLOCKS, (int)gridFor(NN, 256));
     partials.alloc(partialCount);
     sc.alloc(16);
-    VFEM_CUDA(cudaMallocHost(&hostSc, 16 * sizeof(double)));
-    std::memset(hostSc, 0, 16 * sizeof(double));
+    VFEM_CUDA(cudaMallocHost(&hostSc, 17 * sizeof(double)));  // [16]: coarse SPD flag
+    std::memset(hostSc, 0, 17 * sizeof(double));
     setupCoarsestIndex();
 }
 
@@ -518,8 +519,8 @@ void MG::setupCoarsestIndex() {
     cudaStream_t st = fine->stream;
     VFEM_CUDA(cudaMemcpyAsync(redIdx.p, red.data(), red.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (nf) VFEM_CUDA(cudaMemcpyAsync(freeIdx.p, fr.data(), fr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    // pageable-memory copies return once staged, so red / fr may go out of scope
     launch_set_pair(nfreeDev.p, nf, 0, st);
-    VFEM_CUDA(cudaStreamSynchronize(st));  // host vectors red / fr go out of scope
     stiffnessValid = false;
 }
 
@@ -602,16 +603,21 @@ void MG::updateStiffnessT() {
     cudaStream_t st = fine->stream;
     double phis[8][64];
     interpolation_phis(phis);
-    std::vector<double> Kc(8 * 576, 0.0);
-    for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[fi], fine->K0.a, &Kc[fi * 576]);
-    uploadConst(Tr<T>::Kc(*this), Kc.data(), Kc.size());
-    uploadConst(Tr<T>::phis(*this), &phis[0][0], 512);
-    if (L() > 2) {
-        // K2[8c + fi] = Phi_c^T Kc[fi] Phi_c: the fine element at position fi of level-1 child c
-        std::vector<double> K2(64 * 576, 0.0);
-        for (int c = 0; c < 8; ++c)
-            for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[c], &Kc[fi * 576], &K2[(8 * c + fi) * 576]);
-        uploadConst(Tr<T>::K2(*this), K2.data(), K2.size());
+    // coarsening tables depend only on K0: rebuilt when the element stiffness changes
+    const uint64_t constKey = fine->k0Version * 2 + (std::is_same<T, double>::value ? 1 : 0);
+    if (constVersion[std::is_same<T, double>::value ? 1 : 0] != constKey) {
+        std::vector<double> Kc(8 * 576, 0.0);
+        for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[fi], fine->K0.a, &Kc[fi * 576]);
+        uploadConst(Tr<T>::Kc(*this), Kc.data(), Kc.size());
+        uploadConst(Tr<T>::phis(*this), &phis[0][0], 512);
+        if (L() > 2) {
+            // K2[8c + fi] = Phi_c^T Kc[fi] Phi_c: the fine element at position fi of level-1 child c
+            std::vector<double> K2(64 * 576, 0.0);
+            for (int c = 0; c < 8; ++c)
+                for (int fi = 0; fi < 8; ++fi) coarsen_element(phis[c], &Kc[fi * 576], &K2[(8 * c + fi) * 576]);
+            uploadConst(Tr<T>::K2(*this), K2.data(), K2.size());
+        }
+        constVersion[std::is_same<T, double>::value ? 1 : 0] = constKey;
     }
     const T *Y0 = Tr<T>::Y(*fine);
     auto mark = [&](const std::string &name) {
@@ -666,12 +672,10 @@ void MG::updateStiffnessT() {
         mark("coarsest:dense assembly");
         if (stiffMarks) dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st, mark);
         else dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st);
-        int hs = 0;
-        VFEM_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        VFEM_CUDA(cudaStreamSynchronize(st));
-        if (hs) throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
+        // the positive-definiteness flag is read back once the stream reaches it
+        VFEM_CUDA(cudaMemcpyAsync(&hostSc[16], status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        spdCheckPending = true;
     }
-    VFEM_CUDA(cudaStreamSynchronize(st));
     stiffnessValid = true;
     stiffnessPrecision = precision;
     stiffnessDensVersion = fine->densVersion;
@@ -683,11 +687,25 @@ void MG::updateStiffness() {
     else updateStiffnessT<float>();
 }
 
-void MG::ensureStiffness() {
+void MG::ensureStiffness(bool deferCheck) {
     syncFineGeom(*this);
     if (!stiffnessValid || stiffnessPrecision != precision || stiffnessDensVersion != fine->densVersion ||
         stiffnessMaskVersion != fine->maskVersion)
         updateStiffness();
+    if (!deferCheck) checkStiffness();
+}
+
+// Raise the coarsest factorisation's positive-definiteness failure, if one is pending.
+void MG::checkStiffness() {
+    if (!spdCheckPending) return;
+    VFEM_CUDA(cudaStreamSynchronize(fine->stream));
+    spdCheckPending = false;
+    int hs = 0;
+    std::memcpy(&hs, &hostSc[16], sizeof(int));
+    if (hs) {
+        stiffnessValid = false;
+        throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
+    }
 }
 
 template <typename T>
@@ -923,7 +941,7 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
         if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
     }
     allocLevels();
-    if (mgIter > 0) ensureStiffness();
+    if (mgIter > 0) ensureStiffness(true);  // positive definiteness checked in pcgFinish
     pendingKey = GraphKey{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
     VFEM_CUDA(cudaGraphLaunch(loopGraph(pendingKey, x, mgIter, sweeps, fmg), st));
     pending = true;
@@ -934,6 +952,7 @@ PcgStats MG::pcgFinish() {
     pending = false;
     cudaStream_t st = fine->stream;
     VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    checkStiffness();  // synchronises the stream
     VFEM_CUDA(cudaStreamSynchronize(st));
     PcgStats stats;
     stats.iterations = (int64_t)hostSc[9];

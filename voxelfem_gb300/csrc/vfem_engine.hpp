@@ -64,7 +64,7 @@ public:
     DevBuf<uint8_t> dmask;
     DevBuf<double> dval;
     bool dvalNonzero = false;
-    uint64_t densVersion = 1, bcVersion = 1, maskVersion = 1;
+    uint64_t densVersion = 1, bcVersion = 1, maskVersion = 1, k0Version = 1;
     cudaStream_t stream = nullptr;
 
     void setETensor(double E, double nu);
@@ -250,7 +250,10 @@ private:
     template <typename T>
     void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
     void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror = true);
-    void ensureStiffness();
+    void ensureStiffness(bool deferCheck = false);
+    void checkStiffness();
+    bool spdCheckPending = false;
+    uint64_t constVersion[2] = {0, 0};  // K0 version of the uploaded coarsening tables (FP32, FP64)
     template <typename T>
     void levelOp(int l, int op, const double *a, const double *b, double *out, bool flag);
 };
