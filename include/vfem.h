@@ -265,6 +265,12 @@ int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, doubl
 /* Benchmark hook (no reference counterpart): average device time of one applyK on resident data and
  * its algorithmic bytes s (6 nn + ne). */
 int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes);
+/* preconditionedConjugateGradient on a triquadratic grid (MultigridSolver.hh:1047-1152 recurrences,
+ * FP64 outer iteration). The preconditioner is this library's p-multigrid cycle: Q2 block
+ * Gauss-Seidel sweeps (mg_smoothing_iterations before and after) around one FP32 V-cycle of the
+ * trilinear problem on the same mesh with `coarsenings` coarsenings. x in/out. */
+int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
+                int64_t mg_smoothing_iterations, vfem_pcg_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -23,8 +23,8 @@ def make(ne, seed=0, clamp=True):
     g.setDensities(rho)
     Y = 1e-9 + rho ** 3 * (1.0 - 1e-9)
     if clamp:
-        g.addDirichletCondition([0.0, 0.0, 0.0], [0.0, float(ne[1]), float(ne[2])], "xyz")
-        g.addDirichletCondition([float(ne[0]), 0.0, 0.0], [float(ne[0]), 0.0, float(ne[2])], "y")
+        g.addDirichletCondition([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, float(ne[1]), float(ne[2])], "xyz")
+        g.addDirichletCondition([0.0, 0.0, 0.0], [float(ne[0]), 0.0, 0.0], [float(ne[0]), 0.0, float(ne[2])], "y")
     m = g.getDirichletMask()
     bits = (m[:, 0] * 1 + m[:, 1] * 2 + m[:, 2] * 4).astype(np.uint8)
     return g, Y, bits
@@ -68,8 +68,40 @@ def test_q2_transfers(gpu, oracle):
     assert rel(pv.q2_interpolation(ne, c, f, accumulate=True), po.q2_interp(ne, c, f, True)) < 1e-13
 
 
-def test_q2_factory_rejects_multigrid(gpu):
+def test_q2_factory(gpu):
     g = pv.TensorProductSimulator([2, 2, 2], [[0, 0, 0], [2, 2, 2]], [2, 2, 2])
     assert g.numNodes() == 125 and g.numElements() == 8
     with pytest.raises(RuntimeError):
-        g.multigridSolver(1)
+        g.multigridSolver(0)
+
+
+@pytest.mark.parametrize("coarsenings", [1, 2])
+def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings):
+    """The PCG solution equals a dense direct solve of the oracle's Q2 operator on the free DOFs."""
+    ne = (8, 4, 4)
+    g, Y, bits = make(ne, seed=5)
+    K0 = g.fullDensityElementStiffnessMatrix()
+    nn = g.numNodes()
+    f = np.zeros((nn, 3))
+    nnd = [2 * v + 1 for v in ne]
+    tip = [(nnd[0] - 1) * nnd[1] * nnd[2] + j * nnd[2] + nnd[2] // 2 for j in range(nnd[1])]
+    f[tip, 1] = -1.0 / len(tip)
+    # dense oracle operator
+    Kd = np.zeros((3 * nn, 3 * nn))
+    for t in range(3 * nn):
+        e = np.zeros(3 * nn)
+        e[t] = 1.0
+        Kd[:, t] = po.q2_apply_k(ne, K0, Y, e.reshape(3, nn).T).T.ravel()
+    fixed = np.array([(bits[n] >> c) & 1 for c in range(3) for n in range(nn)], dtype=bool)
+    bvec = f.T.ravel().copy()
+    bvec[fixed] = 0
+    xs = np.zeros(3 * nn)
+    xs[~fixed] = np.linalg.solve(Kd[np.ix_(~fixed, ~fixed)], bvec[~fixed])
+    xref = xs.reshape(3, nn).T
+    mg = g.multigridSolver(coarsenings)
+    x = mg.preconditionedConjugateGradient(np.zeros((nn, 3)), f, 200, 1e-11, None, 1, 2, False)
+    assert mg.lastStats.relres <= 1e-11
+    assert rel(x, xref) < 1e-8
+    assert mg.lastStats.iterations < 60
+    c, cref = np.sum(f * x), np.sum(f * xref)
+    assert abs(c - cref) / abs(cref) < 1e-9

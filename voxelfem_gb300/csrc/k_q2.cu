@@ -402,6 +402,81 @@ __global__ void __launch_bounds__(BS) restrict_q2_kernel(Q2Dims df, Q2Dims dc, c
     for (int r = 0; r < 3; ++r) coarse[r * dc.NN + cn] = (T)acc[r];
 }
 
+// ---- Q2 <-> Q1 on the same mesh (the p-multigrid step of the Q2 preconditioner) ----
+// Q1 nodes are the even-indexed Q2 nodes; the trilinear interpolant at a Q2 node is the
+// tensor product of weight 1 (even index 2i -> i) and 1/2, 1/2 (odd index 2i+1 -> i, i+1).
+template <typename T>
+__global__ void __launch_bounds__(BS) interp_q1_q2_kernel(Q2Dims d, const T *__restrict__ q1, T *__restrict__ q2,
+                                                          int accumulate) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= d.NN) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)d.nn[2];
+    const int F[3] = {(int)(q / (uint32_t)d.nn[1]), (int)(q % (uint32_t)d.nn[1]), (int)(tt - q * (uint32_t)d.nn[2])};
+    const int n1[3] = {d.ne[0] + 1, d.ne[1] + 1, d.ne[2] + 1};
+    const int64_t N1 = (int64_t)n1[0] * n1[1] * n1[2];
+    int lo[3], cnt[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = F[a] >> 1;
+        cnt[a] = (F[a] & 1) ? 2 : 1;
+    }
+    T acc[3] = {T(0), T(0), T(0)};
+    const T w = T(1) / T(cnt[0] * cnt[1] * cnt[2]);
+    for (int a = 0; a < cnt[0]; ++a)
+        for (int b = 0; b < cnt[1]; ++b)
+            for (int c = 0; c < cnt[2]; ++c) {
+                const int64_t m = ((int64_t)(lo[0] + a) * n1[1] + lo[1] + b) * n1[2] + lo[2] + c;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += q1[r * N1 + m];
+            }
+    const int64_t n = q2node(d, F[0], F[1], F[2]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) q2[r * d.NN + n] = (accumulate ? q2[r * d.NN + n] : T(0)) + w * acc[r];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BS) restrict_q2_q1_kernel(Q2Dims d, const T *__restrict__ q2, T *__restrict__ q1) {
+    const int n1[3] = {d.ne[0] + 1, d.ne[1] + 1, d.ne[2] + 1};
+    const int64_t N1 = (int64_t)n1[0] * n1[1] * n1[2];
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= N1) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n1[2];
+    const int C[3] = {(int)(q / (uint32_t)n1[1]), (int)(q % (uint32_t)n1[1]), (int)(tt - q * (uint32_t)n1[2])};
+    T acc[3] = {T(0), T(0), T(0)};
+    for (int a = -1; a <= 1; ++a) {
+        const int I = 2 * C[0] + a;
+        if (I < 0 || I >= d.nn[0]) continue;
+        const T wa = a ? T(0.5) : T(1);
+        for (int b = -1; b <= 1; ++b) {
+            const int J = 2 * C[1] + b;
+            if (J < 0 || J >= d.nn[1]) continue;
+            const T wb = b ? T(0.5) : T(1);
+            for (int c = -1; c <= 1; ++c) {
+                const int K = 2 * C[2] + c;
+                if (K < 0 || K >= d.nn[2]) continue;
+                const T w = wa * wb * (c ? T(0.5) : T(1));
+                const int64_t n = q2node(d, I, J, K);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += w * q2[r * d.NN + n];
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) q1[r * N1 + t] = acc[r];
+}
+
+// r = b - Ku on the free components (Ku already masked to zero on constrained ones)
+template <typename T>
+__global__ void __launch_bounds__(BS) q2_residual_combine_kernel(int64_t NN, const T *__restrict__ b,
+                                                                 const T *__restrict__ Ku, T *__restrict__ r,
+                                                                 const uint8_t *__restrict__ dmask) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (n >= NN) return;
+    const uint8_t dm = dmask[n];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c * NN + n] = ((dm >> c) & 1) ? T(0) : b[c * NN + n] - Ku[c * NN + n];
+}
+
 Q2Dims dims_of(const int ne[3]) {
     Q2Dims d;
     for (int a = 0; a < 3; ++a) {
@@ -489,13 +564,36 @@ void launch_interp_q2(const int neFine[3], const T *coarse, T *fine, bool accumu
     VFEM_LAUNCH_CHECK();
 }
 
+template <typename T>
+void launch_interp_q1_q2(const int ne[3], const T *q1, T *q2, bool accumulate, cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    interp_q1_q2_kernel<T><<<gridFor(d.NN, BS), BS, 0, st>>>(d, q1, q2, accumulate ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_restrict_q2_q1(const int ne[3], const T *q2, T *q1, cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    restrict_q2_q1_kernel<T><<<gridFor((int64_t)(ne[0] + 1) * (ne[1] + 1) * (ne[2] + 1), BS), BS, 0, st>>>(d, q2, q1);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_q2_residual_combine(int64_t NN, const T *b, const T *Ku, T *r, const uint8_t *dmask, cudaStream_t st) {
+    q2_residual_combine_kernel<T><<<gridFor(NN, BS), BS, 0, st>>>(NN, b, Ku, r, dmask);
+    VFEM_LAUNCH_CHECK();
+}
+
 #define VFEM_INST_Q2(T)                                                                                               \
     template void launch_applyk_q2<T>(const int[3], const T *, const T *, const T *, T *, const uint8_t *, bool,      \
                                       cudaStream_t);                                                                  \
     template void launch_gs_q2_sweep<T>(const int[3], const T *, const T *, T *, const T *, const uint8_t *, bool,    \
                                         cudaStream_t);                                                                \
     template void launch_restrict_q2<T>(const int[3], const T *, T *, cudaStream_t);                                  \
-    template void launch_interp_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);
+    template void launch_interp_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);                              \
+    template void launch_interp_q1_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);                           \
+    template void launch_restrict_q2_q1<T>(const int[3], const T *, T *, cudaStream_t);                               \
+    template void launch_q2_residual_combine<T>(int64_t, const T *, const T *, T *, const uint8_t *, cudaStream_t);
 VFEM_INST_Q2(double)
 VFEM_INST_Q2(float)
 

@@ -539,6 +539,21 @@ int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, doubl
         q2Interpolate(ne, coarse, fine, accumulate != 0);
     });
 }
+int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
+                int64_t mg_smoothing_iterations, vfem_pcg_stats *stats) {
+    return guarded([&] {
+        need(g, "grid");
+        need(x_inout, "x");
+        need(b, "b");
+        const PcgStats s = g->g.pcg(x_inout, b, max_iter, tol, (int)coarsenings, mg_smoothing_iterations);
+        if (stats) {
+            stats->iterations = s.iterations;
+            stats->relres = s.relres;
+            stats->rsq = s.rsq;
+            stats->bnorm2 = s.bnorm2;
+        }
+    });
+}
 int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes) {
     return guarded([&] {
         need(g, "grid");

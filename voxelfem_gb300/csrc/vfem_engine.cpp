@@ -450,6 +450,13 @@ void MG::clearGraphs() {
     graphX = nullptr;
 }
 
+void MG::vcycleOnFineRhs(int64_t sweeps) {
+    if (precision != PREC_MIXED) throw Error(ERR_STATE, "the fine-rhs V-cycle runs in mixed precision");
+    auto &D = lv[0].d32;
+    launch_fill<float>(D.x.p, 0.f, 3 * lv[0].g.NN, fine->stream);
+    vcycleT<float>(0, sweeps, true);
+}
+
 // Dirichlet coarsening (MultigridSolver.hh:58-103): a fine constrained node on a coarse
 // element's vertex/edge/face constrains every coarse node of that vertex/edge/face.
 void MG::coarsenDirichlet() {

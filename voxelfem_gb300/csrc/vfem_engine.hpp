@@ -250,6 +250,11 @@ private:
     template <typename T>
     void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
     void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror = true);
+
+public:
+    // One FP32 V-cycle on the fine level's right-hand side lv[0].d32.b (zero initial guess),
+    // result in lv[0].d32.x (mixed precision; stiffness must be current).
+    void vcycleOnFineRhs(int64_t sweeps);
     void ensureStiffness(bool deferCheck = false);
     void checkStiffness();
     bool spdCheckPending = false;
@@ -334,8 +339,24 @@ public:
     void applyK(const double *u, double *out, int precision, bool zeroDirichlet);
     void smooth(double *u, const double *b, bool forward, int precision);
     double timeApplyK(int precision, int reps, double *bytes);
+    // PCG on K u = b (zero-displacement supports) with an FP64 outer iteration and a p-multigrid
+    // preconditioner: Q2 block Gauss-Seidel smoothing around one FP32 V-cycle of the trilinear
+    // problem on the same mesh (`coarsenings` coarsenings); x in/out.
+    PcgStats pcg(double *x, const double *b, int64_t maxIter, double tol, int coarsenings, int64_t sweeps);
 
 private:
+    struct Box {
+        double mn[3], mx[3];
+        unsigned cmask;
+    };
+    std::vector<Box> boxes;              // supports, replayed on the trilinear grid
+    std::unique_ptr<Grid> q1;            // trilinear grid on the same mesh
+    std::unique_ptr<MG> mg1;
+    int q1Coarsenings = -1;
+    DevBuf<double> cgX, cgR, cgS, cgD, cgAd, cgPart, cgSc;
+    double *cgHost = nullptr;
+    void prepareQ1(int coarsenings);
+    void precondition(const double *r, int64_t sweeps);
     void updateYoungModuli();
     void uploadMask();
     template <typename T>

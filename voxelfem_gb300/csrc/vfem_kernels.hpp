@@ -236,5 +236,13 @@ template <typename T>
 void launch_restrict_q2(const int neFine[3], const T *fine, T *coarse, cudaStream_t st);
 template <typename T>
 void launch_interp_q2(const int neFine[3], const T *coarse, T *fine, bool accumulate, cudaStream_t st);
+// Q1 (even-indexed nodes) <-> Q2 on the same mesh: trilinear prolongation and its transpose
+template <typename T>
+void launch_interp_q1_q2(const int ne[3], const T *q1, T *q2, bool accumulate, cudaStream_t st);
+template <typename T>
+void launch_restrict_q2_q1(const int ne[3], const T *q2, T *q1, cudaStream_t st);
+// r = b - Ku on the free components
+template <typename T>
+void launch_q2_residual_combine(int64_t NN, const T *b, const T *Ku, T *r, const uint8_t *dmask, cudaStream_t st);
 
 }  // namespace vfem

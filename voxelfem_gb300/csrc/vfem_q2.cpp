@@ -42,6 +42,9 @@ GridQ2::GridQ2(const int ne_[3], const double bmin_[3], const double bmax_[3]) {
 }
 
 GridQ2::~GridQ2() {
+    mg1.reset();
+    q1.reset();
+    if (cgHost) cudaFreeHost(cgHost);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -96,6 +99,10 @@ void GridQ2::addDirichlet(const double mn[3], const double mx[3], unsigned cmask
         }
     }
     uploadMask();
+    boxes.push_back(Box{{mn[0], mn[1], mn[2]}, {mx[0], mx[1], mx[2]}, cmask & 7u});
+    mg1.reset();
+    q1.reset();
+    q1Coarsenings = -1;
 }
 
 static void allocWork(LevelData<double> &D, int64_t n3) { D.x.alloc(n3); D.b.alloc(n3); D.r.alloc(n3); }
@@ -197,6 +204,117 @@ double GridQ2::timeApplyK(int precision, int reps, double *bytes) {
         return (double)ms / reps;
     };
     return precision == PREC_FP64 ? run(double()) : run(float());
+}
+
+// The trilinear grid on the same mesh carries the same material, densities and supports; its
+// FP32 multigrid hierarchy is the coarse correction of the Q2 preconditioner.
+void GridQ2::prepareQ1(int coarsenings) {
+    if (!q1 || q1Coarsenings != coarsenings) {
+        mg1.reset();
+        q1 = std::make_unique<Grid>(ne, bmin, bmax);
+        const double zero[3] = {0.0, 0.0, 0.0};
+        for (const Box &b : boxes) q1->addDirichlet(zero, b.mn, b.mx, b.cmask);
+        mg1 = std::make_unique<MG>(q1.get(), coarsenings);
+        mg1->setPrecision(PREC_MIXED);
+        mg1->symmetricGS = true;
+        q1Coarsenings = coarsenings;
+    }
+    if (q1->Eyoung != Eyoung || q1->nu != nu) q1->setETensor(Eyoung, nu);
+    q1->E0 = E0;
+    q1->Emin = Emin;
+    q1->gamma = gamma;
+    q1->q = q;
+    q1->law = law;
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+    VFEM_CUDA(cudaMemcpy(q1->rho.p, rho.p, NE * sizeof(double), cudaMemcpyDeviceToDevice));
+    q1->updateYoungModuli();
+    VFEM_CUDA(cudaStreamSynchronize(q1->stream));
+    mg1->ensureStiffness();
+}
+
+// z = M r: Q2 forward sweeps from zero, the residual restricted to the trilinear mesh, one V-cycle
+// there, the prolongated correction, Q2 backward sweeps (a symmetric preconditioner). The result
+// stays in the FP32 work vector w32.x. Runs on the trilinear grid's stream (the Q2 stream is
+// idle whenever this is called).
+void GridQ2::precondition(const double *r, int64_t sweeps) {
+    cudaStream_t st = q1->stream;
+    auto &W = work<float>();
+    const int64_t n3 = 3 * NN;
+    launch_cast<float, double>(r, W.b.p, n3, st);
+    launch_fill<float>(W.x.p, 0.f, n3, st);
+    q2_upload_k0f(K0f.data(), st);
+    for (int64_t s = 0; s < sweeps; ++s) launch_gs_q2_sweep<float>(ne, nullptr, Yf.p, W.x.p, W.b.p, dmask.p, true, st);
+    launch_applyk_q2<float>(ne, nullptr, Yf.p, W.x.p, W.r.p, dmask.p, true, st);
+    launch_q2_residual_combine<float>(NN, W.b.p, W.r.p, W.r.p, dmask.p, st);
+    auto &F = mg1->lv[0].d32;
+    launch_restrict_q2_q1<float>(ne, W.r.p, F.b.p, st);
+    mg1->vcycleOnFineRhs(sweeps);
+    launch_interp_q1_q2<float>(ne, F.x.p, W.x.p, true, st);
+    for (int64_t s = 0; s < sweeps; ++s) launch_gs_q2_sweep<float>(ne, nullptr, Yf.p, W.x.p, W.b.p, dmask.p, false, st);
+}
+
+// MultigridSolver.hh:1047-1152 recurrences (masked dot products over all nodes, deferred first
+// direction) with the Q2 operator and the preconditioner above.
+PcgStats GridQ2::pcg(double *x, const double *b, int64_t maxIter, double tol, int coarsenings, int64_t sweeps) {
+    if (coarsenings < 1) throw Error(ERR_ARG, "the Q2 preconditioner needs at least one coarsening of the trilinear mesh");
+    VFEM_CUDA(cudaStreamSynchronize(stream));
+    prepareQ1(coarsenings);
+    cudaStream_t st = q1->stream;
+    const int64_t n3 = 3 * NN;
+    cgX.alloc(n3);
+    cgR.alloc(n3);
+    cgS.alloc(n3);
+    cgD.alloc(n3);
+    cgAd.alloc(n3);
+    cgPart.alloc(REDUCE_BLOCKS + 1);
+    cgSc.alloc(16);
+    if (!cgHost) VFEM_CUDA(cudaMallocHost(&cgHost, 16 * sizeof(double)));
+    const int n2[3] = {2 * ne[0], 2 * ne[1], 2 * ne[2]};
+    const Geom gq = makeGeom(n2);  // the Q2 nodes as the nodes of a trilinear grid: reductions and updates
+    View vx, vb;
+    viewInOut(vx, x, n3 * sizeof(double), st);
+    viewIn(vb, b, n3 * sizeof(double), st);
+    VFEM_CUDA(cudaMemcpyAsync(cgX.p, vx.d, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    launch_zero_dirichlet<double>(gq, cgX.p, dmask.p, st);
+    const double *B = (const double *)vb.d;
+    launch_masked_dot_partials<double, double>(gq, B, B, cgPart.p, st);
+    launch_finalize(cgPart.p, REDUCE_BLOCKS, cgSc.p + 7, st);
+    launch_applyk_q2<double>(ne, K0d.p, Y.p, cgX.p, cgAd.p, dmask.p, true, st);
+    launch_q2_residual_combine<double>(NN, B, cgAd.p, cgR.p, dmask.p, st);
+    launch_masked_dot_partials<double, double>(gq, cgR.p, cgR.p, cgPart.p, st);
+    launch_finalize(cgPart.p, REDUCE_BLOCKS, cgSc.p + 5, st);
+    launch_cg_init(cgSc.p, tol * tol, (double)maxIter, st);
+    launch_fill<double>(cgD.p, 0.0, n3, st);
+    VFEM_CUDA(cudaMemcpyAsync(cgHost, cgSc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    PcgStats stats;
+    stats.bnorm2 = cgHost[7];
+    double rsq = cgHost[5];
+    if (std::isnan(rsq)) throw Error(ERR_NAN, "NaN encountered");
+    int64_t it = 0;
+    while (it < maxIter && rsq > tol * tol * stats.bnorm2) {
+        precondition(cgR.p, sweeps);
+        launch_cg_precond_out<float>(gq, work<float>().x.p, cgS.p, cgR.p, dmask.p, cgPart.p, st);
+        launch_cg_beta(cgPart.p, REDUCE_BLOCKS, cgSc.p, st);
+        launch_cg_direction(gq, cgS.p, cgD.p, cgSc.p, nullptr, nullptr, st);
+        launch_applyk_q2<double>(ne, K0d.p, Y.p, cgD.p, cgAd.p, dmask.p, true, st);
+        launch_masked_dot_partials<double, double>(gq, cgD.p, cgAd.p, cgPart.p, st);
+        launch_cg_alpha(cgPart.p, REDUCE_BLOCKS, cgSc.p, st);
+        launch_cg_update(gq, cgX.p, cgR.p, cgD.p, cgAd.p, cgSc.p, cgPart.p, st);
+        launch_cg_rsq(cgPart.p, REDUCE_BLOCKS, cgSc.p, nullptr, st);
+        VFEM_CUDA(cudaMemcpyAsync(cgHost, cgSc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        VFEM_CUDA(cudaStreamSynchronize(st));
+        rsq = cgHost[5];
+        ++it;
+        if (std::isnan(rsq)) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string(it));
+    }
+    VFEM_CUDA(cudaMemcpyAsync(vx.d, cgX.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    finishOut(vx, st);
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    stats.iterations = it;
+    stats.rsq = rsq;
+    stats.relres = stats.bnorm2 > 0 ? std::sqrt(rsq / stats.bnorm2) : std::sqrt(rsq);
+    return stats;
 }
 
 void q2Restrict(const int neFine[3], const double *fine, double *coarse) {

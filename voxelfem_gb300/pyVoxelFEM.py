@@ -935,8 +935,11 @@ class TensorProductSimulator_3D_Q2:
             raise RuntimeError("Density value has to be in between 0 and 1")
         check(_lib().vfem_q2_set_densities(self._h, ptr(a)))
 
-    def addDirichletCondition(self, minCorner, maxCorner, componentMask="xyz"):
-        """Zero-displacement supports on the nodes inside the box."""
+    def addDirichletCondition(self, u, minCorner, maxCorner, componentMask="xyz"):
+        """Supports on the nodes inside the box (TensorProductSimulator::addDirichletCondition).
+        Triquadratic grids take homogeneous supports only: u must be zero."""
+        if np.any(_arr3(u) != 0.0):
+            raise RuntimeError("triquadratic grids support zero prescribed displacements only")
         check(_lib().vfem_q2_add_dirichlet(self._h, _capi.dptr(_arr3(minCorner)), _capi.dptr(_arr3(maxCorner)),
                                            _cmask(componentMask)))
 
@@ -960,8 +963,31 @@ class TensorProductSimulator_3D_Q2:
         return x
 
     def multigridSolver(self, numCoarseningLevels):
-        raise RuntimeError("Multigrid solves on triquadratic grids are not available (applyK, smoothing and "
-                           "transfers are)")
+        """A PCG solver for this grid: FP64 outer iteration, p-multigrid preconditioner (Q2 block
+        Gauss-Seidel around a trilinear V-cycle with numCoarseningLevels coarsenings)."""
+        return _Q2MultigridSolver(self, int(numCoarseningLevels))
+
+
+class _Q2MultigridSolver:
+    def __init__(self, tps, numCoarseningLevels):
+        if numCoarseningLevels < 1:
+            raise RuntimeError("the triquadratic solver needs at least one coarsening of the trilinear mesh")
+        self.tps = tps
+        self.coarsenings = numCoarseningLevels
+        self.lastStats = None
+
+    def preconditionedConjugateGradient(self, u, b, maxIter, tol, it_callback=None, mgIterations=1,
+                                        mgSmoothingIterations=1, fullMultigrid=False):
+        if it_callback is not None or mgIterations != 1 or fullMultigrid:
+            raise RuntimeError("triquadratic solves support one cycle per iteration without callbacks")
+        nn = self.tps.numNodes()
+        x = _as_vfield(u, nn).copy(order="F")
+        b = _as_vfield(b, nn)
+        stats = _capi.PcgStats()
+        check(_lib().vfem_q2_pcg(self.tps._h, self.coarsenings, ptr(x), ptr(b), int(maxIter), float(tol),
+                                 int(mgSmoothingIterations), C.byref(stats)))
+        self.lastStats = stats
+        return x
 
 
 def q2_restriction(elementsPerDimensionFine, fine):
