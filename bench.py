@@ -46,7 +46,20 @@ FP64_ITERATIONS = {"c2": 16, "c1": 10}
 TOL = 1e-8
 KERNEL_NAMES = {0: "applyk_fine_fp64", 1: "applyk_fine_fp32", 2: "applyk_fine_df", 3: "gs_fine_sweep_fp32",
                 4: "gs_fine_sweep_fp64", 5: "residual_fine_fp32", 6: "gs_level1_sweep_fp32",
-                7: "residual_level1_fp32", 8: "gs_level2_sweep_fp32", 9: "residual_level2_fp32"}
+                7: "residual_level1_fp32", 8: "gs_level2_sweep_fp32", 9: "residual_level2_fp32",
+                10: "applyk_fine_tc"}
+
+
+def tc_mma_flops(ne):
+    """bf16 MMA flops one launch of the tensor-core matvec issues: per CTA step (one element layer
+    of an 8 x 16 element tile) 16 MMAs of 128 x 32 x 16; a CTA walks its x segment plus one layer."""
+    nn = [v + 1 for v in ne]
+    cols = -(-nn[1] // 7) * -(-nn[2] // 15)
+    seg = max(1, min(int(round(8.0 * 152 / cols)), nn[0]))
+    seg_len = -(-nn[0] // seg)
+    n_seg = -(-nn[0] // seg_len)
+    steps = cols * (nn[0] + n_seg)
+    return steps * 16 * 2.0 * 128 * 32 * 16
 
 
 def peaks():
@@ -56,6 +69,14 @@ def peaks():
             p = json.load(f)
         return float(p["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f).get("bf16_tflops", 1900.0))
+    return 1900.0
 
 
 def fp64_peak_tflops(n=4096, reps=5):
@@ -336,7 +357,9 @@ def run_ours(args):
     # ---------------- hot kernels: device time per launch (CUDA events on the solver stream) ----------------
     hbm, peak_kind = peaks()
     kernels = {}
-    for kid in (1, 2, 0, 3, 5, 6, 7, 8, 9):
+    outer_kind = mg.outerMatvecKind()
+    kids = (1, 2, 0, 3, 5, 6, 7, 8, 9) + ((10,) if outer_kind == "tensor" else ())
+    for kid in kids:
         ms = C.c_double()
         nbytes = C.c_double()
         reps = 3 if kid == 0 else 20
@@ -344,7 +367,8 @@ def run_ours(args):
         kernels[KERNEL_NAMES[kid]] = {"ms": ms.value, "bytes": nbytes.value,
                                       "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
     # launches per PCG iteration of the hot kernels of the mixed solve (2 pre + 2 post sweeps per level)
-    per_iter_launches = {"applyk_fine_df": 1, "gs_fine_sweep_fp32": 4, "residual_fine_fp32": 1,
+    outer_name = "applyk_fine_tc" if outer_kind == "tensor" else "applyk_fine_df"
+    per_iter_launches = {outer_name: 1, "gs_fine_sweep_fp32": 4, "residual_fine_fp32": 1,
                          "gs_level1_sweep_fp32": 4, "residual_level1_fp32": 1, "gs_level2_sweep_fp32": 4,
                          "residual_level2_fp32": 1}
     share = {k: n * kernels[k]["ms"] for k, n in per_iter_launches.items()}
@@ -360,24 +384,35 @@ def run_ours(args):
         rooflines[k] = {"bound": "hbm", "achieved": kd["gbs"], "peak": hbm, "unit": "GB/s", "frac": kd["gbs"] / hbm,
                         "traffic": traffic_tab.get(k), "algorithmic_bytes": kd["bytes"], "ms_per_launch": kd["ms"],
                         "ms_per_iteration": share[k]}
-    roofline = dict(rooflines[dom], kernel=dom, peak_kind=peak_kind)
-    if dom == "applyk_fine_df":
-        # the double-float matvec is bound by the FP32 pipe; its FP64-equivalent arithmetic
-        # (2 * 24^2 flops per element) against the measured FP64 rate of this GPU
+    p64 = fp64_peak_tflops()
+    for k in ("applyk_fine_df", "applyk_fine_tc"):
+        if k not in rooflines:
+            continue
+        # FP64-class matvecs: their FP64-equivalent arithmetic (2 * 24^2 flops per element)
+        # against the measured FP64 rate of this GPU
         flops = 2.0 * 24 * 24 * nel
-        p64 = fp64_peak_tflops()
-        achieved = flops / (kernels[dom]["ms"] * 1e-3) / 1e12
-        roofline["fp64_equivalent"] = {"flops": flops, "achieved": achieved, "unit": "TFLOP/s", "peak": p64,
-                                       "peak_kind": "measured (cuBLAS DGEMM 4096^3 in this run)",
-                                       "frac": achieved / p64 if p64 else None}
+        achieved = flops / (kernels[k]["ms"] * 1e-3) / 1e12
+        rooflines[k]["fp64_equivalent"] = {"flops": flops, "achieved": achieved, "unit": "TFLOP/s", "peak": p64,
+                                           "peak_kind": "measured (cuBLAS DGEMM 4096^3 in this run)",
+                                           "frac": achieved / p64 if p64 else None}
+    if "applyk_fine_tc" in rooflines:
+        tflops = tc_mma_flops(ne) / (kernels["applyk_fine_tc"]["ms"] * 1e-3) / 1e12
+        bf16 = bf16_peak()
+        rooflines["applyk_fine_tc"]["tensor"] = {"mma_flops": tc_mma_flops(ne), "achieved": tflops,
+                                                 "unit": "TFLOP/s", "peak": bf16,
+                                                 "peak_kind": "measured (MEASURED_PEAKS.json bf16 burst)",
+                                                 "frac": tflops / bf16 if bf16 else None}
+    roofline = dict(rooflines[dom], kernel=dom, peak_kind=peak_kind)
 
     line = {"metric": METRIC, "value": tmix_step if ws == 1 else tmix / (ws * args.steps), "unit": "s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmix_step * 1000,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": "cantilever %dx%dx%d Q1 (%d DOF), rho U[%g,1] seed 0, %d coarsenings, mixed FP32 "
-                                   "V-cycle (2+2 block-GS sweeps) in FP64 CG, double-float outer matvec, tol 1e-8"
-                                   % (ne[0], ne[1], ne[2], 3 * nn, rho_lo, levels),
+                                   "V-cycle (2+2 block-GS sweeps) in FP64 CG, %s outer matvec, tol 1e-8"
+                                   % (ne[0], ne[1], ne[2], 3 * nn, rho_lo, levels,
+                                      "tensor-core (integer-slice bf16)" if outer_kind == "tensor"
+                                      else "double-float"),
                        "l2": "no flush: working set of every step (> 2 GB) exceeds the 129 MB L2"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roofline,
@@ -391,7 +426,8 @@ def run_ours(args):
             "speedup_mixed_vs_fp64": t64 / tmix_step,
             "compliance_rel_err_mixed_vs_fp64": abs(compm - comp64) / abs(comp64),
             "applyk_gbs": {"fp32": kernels["applyk_fine_fp32"]["gbs"], "fp64": kernels["applyk_fine_fp64"]["gbs"],
-                           "df": kernels["applyk_fine_df"]["gbs"]},
+                           "df": kernels["applyk_fine_df"]["gbs"],
+                           "tc": kernels.get("applyk_fine_tc", {}).get("gbs")},
             "kernels": kernels,
             "breakdown_ms": {"mixed_per_iteration": breakdown_mixed, "fp64_per_iteration": breakdown_fp64}}
     if rank == 0 and ws == 1 and not args.no_lbl:
@@ -450,6 +486,20 @@ def run_lbl(slots_list=(1, 8, 16)):
     if best is not None:
         out["batched_speedup"] = out["one_at_a_time_s"] / out[best]
         out["best"] = best
+    # the plain method: 128 sequential FP64 solves on the same GPU
+    mg.setPrecision("fp64")
+    ev = pv.LayerByLayerEvaluator(sim)
+    ev.run(mg, True, 1, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=1)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev.run(mg, True, 1, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=1)
+    torch.cuda.synchronize()
+    out["sequential_fp64_s"] = time.perf_counter() - t0
+    out["sequential_fp64_iterations_total"] = int(ev.iterations.sum())
+    out["max_rel_diff_fp64_vs_mixed"] = float(np.max(np.abs(ev.compliances - ref) / np.abs(ref)))
+    ev._release()
+    if best is not None:
+        out["speedup_vs_sequential_fp64"] = out["sequential_fp64_s"] / out[best]
     return out
 
 

@@ -38,7 +38,10 @@ extern "C" {
 #define VFEM_PREC_MIXED 1   /* FP32 V-cycle inside FP64 outer CG */
 
 #define VFEM_MATVEC_FP64 0  /* outer CG matvec in native FP64 */
-#define VFEM_MATVEC_DF 1    /* outer CG matvec in double-float (FP64-class accuracy on FP32 units) */
+#define VFEM_MATVEC_DF 1    /* outer CG matvec with FP64-class accuracy without FP64 arithmetic: tensor cores
+                               when K0 is a scaled small-integer matrix (cube voxels, rational nu), else
+                               double-float on the FP32 units */
+#define VFEM_MATVEC_DF_SIMT 2 /* outer CG matvec in double-float on the FP32 units only */
 
 typedef struct vfem_grid vfem_grid; /* TensorProductSimulator<double, 1, 1, 1> */
 typedef struct vfem_mg vfem_mg;     /* MultigridSolver<double, 1, 1, 1> */
@@ -142,6 +145,16 @@ int vfem_mg_level_dims(const vfem_mg *mg, int level, int64_t elems[3]);
 int vfem_mg_level_dirichlet_mask(const vfem_mg *mg, int level, uint8_t *mask_out);
 /* precision of the V-cycle (VFEM_PREC_*) and kind of outer matvec (VFEM_MATVEC_*); no reference counterpart */
 int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec);
+/* outer matvec the mixed solve uses now: 0 FP64, 1 double-float (FP32 units), 2 tensor cores;
+ * no reference counterpart */
+int vfem_mg_outer_matvec_kind(const vfem_mg *mg, int *kind);
+/* out = K u with constrained components zeroed (rhs given: rhs - K u), through the outer matvec
+ * of the current precision setting (diagnostic; no reference counterpart) */
+int vfem_mg_outer_apply(vfem_mg *mg, const double *u, const double *rhs, double *out);
+/* Diagnostic (no reference counterpart, no GPU needed): whether K0 (24 x 24, row-major) is a
+ * scale times a small-integer matrix that keeps the tensor-core matvec exact, and its bf16 B
+ * tiles. */
+int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, int *ok);
 /* CUDA-graph capture of the CG iteration (default on); no reference counterpart */
 int vfem_mg_set_use_graphs(vfem_mg *mg, int use);
 /* Execution option (no reference counterpart): with graphs on, a solve without a callback runs as
@@ -181,7 +194,7 @@ int vfem_mg_pcg(vfem_mg *mg, double *x_inout, const double *b, int64_t max_iter,
  * average device time of one launch of a hot kernel (ids in vfem_mg_time_kernel's comment
  * in vfem_engine.cpp: 0 fine applyK FP64, 1 fine applyK FP32, 2 fine applyK double-float,
  * 3/4 fine GS sweep FP32/FP64, 5 fine residual FP32, 6/7 level-1 GS sweep / residual FP32,
- * 8/9 level-2 GS sweep / residual FP32) with its algorithmic bytes, and a counter of the library's
+ * 8/9 level-2 GS sweep / residual FP32, 10 fine applyK on the tensor cores) with its algorithmic bytes, and a counter of the library's
  * kernel launches (graph replays included). */
 int vfem_mg_get_stream(const vfem_mg *mg, void **stream);
 int vfem_mg_time_kernel(vfem_mg *mg, int kernel, int reps, double *ms, double *bytes);

@@ -353,9 +353,11 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
 }
 
 __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double *__restrict__ d,
-                                    const double *__restrict__ sc, float *__restrict__ dh, float *__restrict__ dl) {
+                                    const double *__restrict__ sc, float *__restrict__ dh, float *__restrict__ dl,
+                                    double *__restrict__ amax) {
     const double beta = sc[2];
     const int64_t N3 = 3 * g.ld;
+    double m = 0.0;
     for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS) {
         const double v = beta * d[t] + s[t];
         d[t] = v;
@@ -363,6 +365,23 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
             const float h = __double2float_rn(v);
             dh[t] = h;
             dl[t] = __double2float_rn(v - (double)h);
+        }
+        const double a = fabs(v);
+        m = (a > m || a != a) ? a : m;
+    }
+    if (amax) {
+        __shared__ double sh[BS / 32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double a = __shfl_xor_sync(0xffffffffu, m, o);
+            m = (a > m || a != a) ? a : m;
+        }
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double r = 0.0;
+            for (int w = 0; w < BS / 32; ++w) r = (sh[w] > r || sh[w] != sh[w]) ? sh[w] : r;
+            amax[blockIdx.x] = r;
         }
     }
 }
@@ -564,8 +583,8 @@ void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double
 }
 
 void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
-                         cudaStream_t st) {
-    cg_direction_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, s, d, sc, dh, dl);
+                         cudaStream_t st, double *amax) {
+    cg_direction_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, s, d, sc, dh, dl, amax);
     VFEM_LAUNCH_CHECK();
 }
 

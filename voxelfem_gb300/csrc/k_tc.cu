@@ -1,0 +1,511 @@
+// FP64-class outer matvec of the PCG iteration (MultigridSolver.hh:1108-1144, the product K d
+// with the Q1 operator of TPSStencils.hh:431-728) on the 5th-generation tensor cores.
+//
+// Idea. For cube voxels of an isotropic material with a rational lambda/mu, the element matrix
+// is K0 = c * C with C a small-integer matrix (|C| <= 88, row sums <= 472 at nu = 0.3). The
+// operand u is written in fixed point with one scale for the whole vector, F = round(u 2^(55-s)),
+// |u| < 2^s, and split into eight signed base-128 digits, paired into four 14-bit pieces
+// P_a = 128 D_2a + D_2a+1. Every digit and every C entry is exact in bf16, and
+// |sum_k C_nk P_ak| <= 472 * 8256 < 2^24, so the FP32 accumulator of a bf16 MMA holds C P_a
+// EXACTLY. Four accumulators give C F = acc0 2^42 + acc1 2^28 + acc2 2^14 + acc3; the epilogue
+// forms it in double-float, scales by E_e c per element and sums the eight element contributions
+// of every node in double-float. The result matches FP64 to ~3e-14 relative to |K| |u| (the
+// double-float kernel's accuracy); the FP64 units (1/64 of the FP32 rate here) only convert the
+// final sums.
+//
+// Mapping. A CTA owns a column of 7 (y) x 15 (z) nodes and a run of x planes. It walks x one
+// element layer at a time: the layer's 8 x 16 elements (own nodes plus a one-element halo) are
+// the 128 rows of an M = 128, N = 32 (24 DOFs + 8 zero), K = 16 tcgen05 MMA. The A operand is
+// the node digit table of the two node planes of the layer, read IN PLACE through the smem
+// descriptor: table rows are nodes (z-major, y fastest, 16 bytes = 3 hi digits, 3 lo digits,
+// 2 zeros), so element (y, z)'s local node (dx, dy, dz) is row (z + dz) 9 + (y + dy) of plane
+// x + dx. One MMA covers local nodes (dx, 0, dz) and (dx, 1, dz): its second K-chunk sits one
+// row (16 bytes, the descriptor's leading byte offset) after the first. Four MMAs cover the 8
+// local nodes, 16 the four digit pairs. B holds C (bf16) in the matching K order. The
+// accumulators live in TMEM (4 x 32 columns), the epilogue reads them with tcgen05.ld.
+// Every wait on the tensor core is bounded; a timeout is reported through a status word.
+#include "vfem_kernels.hpp"
+#include "vfem_reduce.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace vfem {
+
+namespace {
+
+constexpr int TCT = 128;                    // threads; thread i owns MMA row / TMEM lane i
+constexpr int TY = 8, TZ = 16;              // element tile (y, z): M = 128
+constexpr int NPY = TY + 1, NPZ = TZ + 1;   // node patch of the tile
+constexpr int OY = TY - 1, OZ = TZ - 1;     // nodes a tile owns
+constexpr int TROWS = NPZ * NPY;            // rows of a digit table
+constexpr int TAB = TROWS * 16;             // bytes of a digit table
+constexpr int NACC = 4;                     // digit pairs / accumulators
+constexpr int NCOL = 32;                    // MMA N
+constexpr uint32_t TMEM_COLS = 128;
+constexpr int SPITCH = TZ + 1;              // staging: [dof][y][z], z pitch padded
+constexpr int SDOF = TY * SPITCH;
+
+constexpr int OFF_B = 0;                                  // B tiles, 4 KB
+constexpr int OFF_TAB = OFF_B + 4096;                     // [2 planes][NACC] digit tables
+constexpr int OFF_STH = OFF_TAB + 2 * NACC * TAB;         // staging hi parts [24][SDOF]
+constexpr int OFF_STL = OFF_STH + 24 * SDOF * 4;          // staging lo parts
+constexpr int OFF_MISC = OFF_STL + 24 * SDOF * 4;         // mbarrier, TMEM address, scale
+constexpr int SMEM_USED = OFF_MISC + 64;
+// The allocation is padded so that at most four CTAs share an SM: 4 x 128 TMEM columns = 512.
+constexpr int SMEM_BYTES = 52 * 1024;
+static_assert(SMEM_USED <= SMEM_BYTES, "shared memory layout");
+static_assert(5 * (SMEM_BYTES + 1024) > 228 * 1024, "five CTAs must not fit on an SM");
+static_assert(OFF_TAB % 16 == 0 && TAB % 16 == 0 && OFF_MISC % 8 == 0, "alignment");
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
+// both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NCOL >> 3) << 17) |
+                           ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle: start address, leading byte offset (between the
+// two 8-element K chunks of a row), stride byte offset (between 8-row groups), version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Eight consecutive columns of this thread's TMEM lane from each of four column blocks; the
+// wait is part of the same asm statement, so no use of the values is scheduled before it.
+__device__ __forceinline__ void tmem_ld4x8(uint32_t t0, uint32_t t1, uint32_t t2, uint32_t t3, float *v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%33];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%34];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%35];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(t0), "r"(t1), "r"(t2), "r"(t3)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// round(v 2^(55 - s)) for |v| < 2^s from the bit pattern (integer unit only); sh0 = 1020 + s.
+// v = m 2^(e' - 1075), so F = m 2^-sh with sh = sh0 - e' >= -2.
+__device__ __forceinline__ long long fixed_point(double v, int sh0) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+    if (e == 0x7FF) return 0;  // Inf / NaN: the output scale carries the NaN
+    const int sh = sh0 - (e > 1 ? e : 1);
+    long long F;
+    if (sh <= 0) F = (long long)(m << (sh < -2 ? 2 : -sh));
+    else F = sh >= 60 ? 0ll : (long long)((m + (1ull << (sh - 1))) >> sh);
+    return (b >> 63) ? -F : F;
+}
+
+// Exact small integer (|d| < 2^22) as a float, then its bf16 bit pattern (exact for <= 8
+// significant bits).
+__device__ __forceinline__ uint32_t bf16_bits(int d) {
+    const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+    return __float_as_uint(f) >> 16;
+}
+
+// Digit-table entries of one node: for pair a, [128 D_2a (c = 0, 1, 2), D_2a+1 (c = 0, 1, 2), 0, 0].
+__device__ __forceinline__ void node_digits(const double u3[3], int sh0, uint4 out[NACC]) {
+    int D[3][2 * NACC];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        long long F = fixed_point(u3[c], sh0);
+#pragma unroll
+        for (int i = 2 * NACC - 1; i >= 1; --i) {
+            const int d = (int)((F + 64) & 127) - 64;
+            D[c][i] = d;
+            F = (F - d) >> 7;
+        }
+        D[c][0] = (int)F;
+    }
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) {
+        const uint32_t h0 = bf16_bits(128 * D[0][2 * a]), h1 = bf16_bits(128 * D[1][2 * a]),
+                       h2 = bf16_bits(128 * D[2][2 * a]);
+        const uint32_t l0 = bf16_bits(D[0][2 * a + 1]), l1 = bf16_bits(D[1][2 * a + 1]), l2 = bf16_bits(D[2][2 * a + 1]);
+        out[a] = make_uint4(h0 | (h1 << 16), h2 | (l0 << 16), l1 | (l2 << 16), 0u);
+    }
+}
+
+// Digit tables of node plane x for the patch whose first node is (ny0, nz0); zero outside the grid.
+__device__ __forceinline__ void build_tables(const Geom &g, const double *__restrict__ u, int x, int ny0, int nz0,
+                                             int sh0, uint8_t *tab) {
+    for (int t = threadIdx.x; t < TROWS; t += TCT) {
+        const int zn = t % NPZ, yn = t / NPZ;
+        const int y = ny0 + yn, z = nz0 + zn;
+        double u3[3] = {0.0, 0.0, 0.0};
+        if (x >= 0 && x < g.nn[0] && y >= 0 && y < g.nn[1] && z >= 0 && z < g.nn[2]) {
+            const int64_t n = g.node(x, y, z);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) u3[c] = u[c * g.ld + n];
+        }
+        uint4 e[NACC];
+        node_digits(u3, sh0, e);
+        const int row = zn * NPY + yn;
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) *reinterpret_cast<uint4 *>(tab + a * TAB + row * 16) = e[a];
+    }
+}
+
+__device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// out = K u (FP64-class), optionally the residual form rhs - K u and the partial dots u . out.
+// umax: REDUCE_BLOCKS partial maxima of |u|. Yh, Yl: zero-padded double-float moduli.
+__global__ void __launch_bounds__(TCT, 4)
+    applyk_fine_tc_kernel(Geom g, const float *__restrict__ Yh, const float *__restrict__ Yl,
+                          const double *__restrict__ u, const double *__restrict__ umax, double *__restrict__ out,
+                          const uint4 *__restrict__ bTiles, float scaleHi, float scaleLo,
+                          const uint8_t *__restrict__ dmask, int zeroDir, double *__restrict__ partials, int withDot,
+                          const double *__restrict__ rhs, int nTZ, int nTY, int segLen, int *status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *tabs = smem + OFF_TAB;
+    float *stH = reinterpret_cast<float *>(smem + OFF_STH);
+    float *stL = reinterpret_cast<float *>(smem + OFF_STL);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + OFF_MISC);
+    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + OFF_MISC + 8);
+    double *red = reinterpret_cast<double *>(smem + OFF_MISC + 16);  // 4 doubles
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int b = blockIdx.x;
+    const int tz = b % nTZ, ty = (b / nTZ) % nTY, sx = b / (nTZ * nTY);
+    const int Y0 = ty * OY, Z0 = tz * OZ;     // first owned node
+    const int ny0 = Y0 - 1, nz0 = Z0 - 1;     // first patch node / first tile element
+    const int X0 = sx * segLen, X1 = min(X0 + segLen, g.nn[0]);
+
+    // B tiles (4 KB) into shared memory
+    for (int t = tid; t < 256; t += TCT) reinterpret_cast<uint4 *>(smem + OFF_B)[t] = bTiles[t];
+    // global scale: |u| < 2^s
+    double m = 0.0;
+    for (int t = tid; t < REDUCE_BLOCKS; t += TCT) m = nanmax(m, umax[t]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((tid & 31) == 0) red[warp] = m;
+    if (tid == 0) mbar_init(smem_addr(mbar), 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmemSlot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmemSlot;
+    m = nanmax(nanmax(red[0], red[1]), nanmax(red[2], red[3]));
+    int s = 0;
+    const bool finite = isfinite(m);
+    if (finite && m > 0.0) {
+        int e;
+        frexp(m, &e);  // m < 2^e
+        s = e < -1000 ? -1000 : e;
+    }
+    const int sh0 = 1020 + s;
+    // a NaN or infinite operand makes every output NaN (the solver's NaN check sees it)
+    const double outScale = finite ? ldexp(1.0, s - 13) : __longlong_as_double(0x7FF8000000000000ll);
+
+    // this thread's element row of the MMA tile
+    const int ey = tid % TY, ez = tid / TY;
+    const int ej = ny0 + ey, ek = nz0 + ez;
+    const bool eIn = ej >= 0 && ej < g.ne[1] && ek >= 0 && ek < g.ne[2];
+    // this thread's owned node (threads >= OY * OZ own none)
+    const bool owner = tid < OY * OZ;
+    const int zo = tid % OZ, yo = tid / OZ;
+    const int yn = yo + 1, zn = zo + 1;
+    const int nj = Y0 + yo, nk = Z0 + zo;
+    const bool nIn = owner && nj < g.nn[1] && nk < g.nn[2];
+    float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};  // partial sums of the pending node plane
+
+    const uint32_t aBase = smem_addr(tabs), bBase = smem_addr(smem + OFF_B);
+    double dot = 0.0;
+    bool ok = true;
+    int phase = 0;
+    build_tables(g, u, X0 - 1, ny0, nz0, sh0, tabs + ((X0 - 1) & 1) * NACC * TAB);
+    for (int L = X0 - 1; L < X1 && ok; ++L) {
+        // tables of node plane L + 1 (plane L was built by the previous step)
+        build_tables(g, u, L + 1, ny0, nz0, sh0, tabs + ((L + 1) & 1) * NACC * TAB);
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int a = 0; a < NACC; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int dx = q >> 1, dz = q & 1;
+                    const uint32_t aAddr = aBase + (uint32_t)((((L + dx) & 1) * NACC + a) * TAB + dz * NPY * 16);
+                    mma_bf16(tmem + (uint32_t)(a * NCOL), sdesc(aAddr, 16, NPY * 16), sdesc(bBase + q * 1024, 512, 128),
+                             q > 0 ? 1u : 0u);
+                }
+            mma_commit(smem_addr(mbar));
+        }
+        // element scale E_e c (double-float) while the tensor core runs
+        float sh = 0.f, sl = 0.f;
+        if (eIn && L >= 0 && L < g.ne[0]) {
+            const int64_t e = g.padElem(L, ej, ek);
+            const float eh = Yh[e], el = Yl[e];
+            sh = eh * scaleHi;
+            sl = __fmaf_rn(eh, scaleHi, -sh);
+            sl = __fmaf_rn(eh, scaleLo, sl);
+            sl = __fmaf_rn(el, scaleHi, sl);
+        }
+        // one thread waits for the MMAs; the barrier passes completion (and a timeout) to all
+        int timedOut = 0;
+        if (tid == 0) timedOut = mbar_wait(smem_addr(mbar), (uint32_t)phase) ? 0 : 1;
+        phase ^= 1;
+        if (__syncthreads_or(timedOut)) {
+            if (tid == 0) atomicExch(status, 1);
+            ok = false;
+            break;
+        }
+        tc_fence_after();
+        const uint32_t lane = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int c0 = 0; c0 < 24; c0 += 8) {
+            float v[32];
+            const uint32_t t0 = tmem + lane + (uint32_t)c0;
+            tmem_ld4x8(t0, t0 + NCOL, t0 + 2 * NCOL, t0 + 3 * NCOL, v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float h, l;
+                two_sum(v[j], v[8 + j] * 0x1p-14f, h, l);
+                l += v[16 + j] * 0x1p-28f + v[24 + j] * 0x1p-42f;
+                const float p = h * sh;
+                float e = __fmaf_rn(h, sh, -p);
+                e = __fmaf_rn(h, sl, e);
+                e = __fmaf_rn(l, sh, e);
+                stH[(c0 + j) * SDOF + ey * SPITCH + ez] = p;
+                stL[(c0 + j) * SDOF + ey * SPITCH + ez] = e;
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (owner) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                // plane L: the pending sum plus this layer's lower-face contributions (dx = 0)
+                float h = ah[r], l = al[r];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int dy = q >> 1, dz = q & 1;
+                    const int idx = (3 * q + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                    float t, e;
+                    two_sum(h, stH[idx], t, e);
+                    h = t;
+                    l += e + stL[idx];
+                }
+                // plane L + 1 starts with the upper-face contributions (dx = 1)
+                float h2 = 0.f, l2 = 0.f;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int dy = q >> 1, dz = q & 1;
+                    const int idx = (3 * (4 + q) + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                    float t, e;
+                    two_sum(h2, stH[idx], t, e);
+                    h2 = t;
+                    l2 += e + stL[idx];
+                }
+                ah[r] = h2;
+                al[r] = l2;
+                if (L >= X0 && nIn) {
+                    const int64_t n = g.node(L, nj, nk);
+                    double f = 0.0;
+                    if (nj < g.nyv()) {
+                        const uint8_t dm = zeroDir ? dmask[n] : 0;
+                        f = ((dm >> r) & 1) ? 0.0 : ((double)h + (double)l) * outScale;
+                        if (withDot) dot += u[r * g.ld + n] * f;
+                    }
+                    if (rhs) {
+                        const uint8_t dm = dmask[n];
+                        f = ((dm >> r) & 1) ? 0.0 : rhs[r * g.ld + n] - f;
+                    }
+                    out[r * g.ld + n] = f;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (withDot) {
+        const double tot = block_sum<TCT>(dot);
+        if (tid == 0) partials[b] = tot;
+    }
+    if (!ok && tid == 0) mbar_wait(smem_addr(mbar), (uint32_t)phase ^ 1u);  // the MMAs in flight, bounded
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+__global__ void absmax_partials_kernel(const double *__restrict__ u, int64_t n, double *__restrict__ partials) {
+    double m = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        m = nanmax(m, fabs(u[t]));
+    __shared__ double sh[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = nanmax(r, sh[w]);
+        partials[blockIdx.x] = r;
+    }
+}
+
+struct TcGrid {
+    int nTY, nTZ, nSeg, segLen;
+};
+
+TcGrid tc_grid(const Geom &g, int maxBlocks) {
+    TcGrid t;
+    t.nTY = (g.nn[1] + OY - 1) / OY;
+    t.nTZ = (g.nn[2] + OZ - 1) / OZ;
+    const int cols = t.nTY * t.nTZ;
+    // about two waves of four CTAs per SM
+    int seg = (int)std::lround(8.0 * NUM_SMS / cols);
+    seg = std::max(1, std::min(seg, g.nn[0]));
+    if (maxBlocks > 0) seg = std::max(1, std::min(seg, maxBlocks / cols));
+    t.segLen = (g.nn[0] + seg - 1) / seg;
+    t.nSeg = (g.nn[0] + t.segLen - 1) / t.segLen;
+    return t;
+}
+
+}  // namespace
+
+bool tc_fit_k0(const double K0[576], double *scale, uint16_t bTiles[2048]) {
+    double kmax = 0.0;
+    for (int t = 0; t < 576; ++t) kmax = std::max(kmax, std::fabs(K0[t]));
+    if (!(kmax > 0.0)) return false;
+    double ref = kmax;
+    for (int t = 0; t < 576; ++t) {
+        const double v = std::fabs(K0[t]);
+        if (v > 1e-12 * kmax) ref = std::min(ref, v);
+    }
+    int C[576];
+    double c = 0.0;
+    bool found = false;
+    for (int q = 1; q <= 4096 && !found; ++q) {
+        const double cc = ref / q;
+        bool okq = true;
+        for (int t = 0; t < 576 && okq; ++t) {
+            const double v = K0[t] / cc;
+            const double r = std::nearbyint(v);
+            if (std::fabs(v - r) > 1e-7 || std::fabs(r) > 256.0) okq = false;
+            C[t] = (int)r;
+        }
+        if (okq) {
+            c = cc;
+            found = true;
+        }
+    }
+    if (!found) return false;
+    // exact fit to round-off, and the accumulator bound: row sum x max |P| < 2^24
+    for (int t = 0; t < 576; ++t)
+        if (std::fabs(K0[t] - c * C[t]) > 1e-13 * kmax) return false;
+    for (int n = 0; n < 24; ++n) {
+        long rs = 0;
+        for (int k = 0; k < 24; ++k) rs += std::labs((long)C[n * 24 + k]);
+        if (rs * 8256L >= (1L << 24)) return false;
+    }
+    // B tiles: MMA q = (dx, dz) at q * 1024 bytes; K chunk s = dy at s * 512; N group at g * 128;
+    // row n of the group at 16 bytes; K value v: C[n][3 m + v % 3] (v < 6, m = 4 dx + 2 dy + dz)
+    std::memset(bTiles, 0, 2048 * sizeof(uint16_t));
+    for (int q = 0; q < 4; ++q)
+        for (int s = 0; s < 2; ++s)
+            for (int n = 0; n < 24; ++n)
+                for (int v = 0; v < 6; ++v) {
+                    const int dx = q >> 1, dz = q & 1, m = 4 * dx + 2 * s + dz;
+                    const float f = (float)C[n * 24 + 3 * m + v % 3];
+                    uint32_t bits;
+                    std::memcpy(&bits, &f, 4);
+                    const int off = q * 1024 + s * 512 + (n / 8) * 128 + (n % 8) * 16 + v * 2;
+                    bTiles[off / 2] = (uint16_t)(bits >> 16);
+                }
+    *scale = c;
+    return true;
+}
+
+int tc_matvec_blocks(const Geom &g, int maxBlocks) {
+    const TcGrid t = tc_grid(g, maxBlocks);
+    return t.nTY * t.nTZ * t.nSeg;
+}
+
+void launch_absmax_partials(const double *u, int64_t n, double *partials, cudaStream_t st) {
+    absmax_partials_kernel<<<REDUCE_BLOCKS, 256, 0, st>>>(u, n, partials);
+    VFEM_LAUNCH_CHECK();
+}
+
+int launch_applyk_fine_tc(const Geom &g, const float *Yh, const float *Yl, const double *u, const double *umax,
+                          double *out, const uint16_t *bTiles, double scale, const uint8_t *dmask, bool zeroDirichlet,
+                          double *partialDot, int partialBlocks, int *status, cudaStream_t st, const double *rhs) {
+    static bool attr = false;
+    if (!attr) {
+        VFEM_CUDA(cudaFuncSetAttribute(applyk_fine_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        attr = true;
+    }
+    const TcGrid t = tc_grid(g, partialDot ? partialBlocks : 0);
+    const int blocks = t.nTY * t.nTZ * t.nSeg;
+    if (partialDot && blocks > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
+    const float sh = (float)scale, sl = (float)(scale - (double)sh);
+    applyk_fine_tc_kernel<<<blocks, TCT, SMEM_BYTES, st>>>(g, Yh, Yl, u, umax, out,
+                                                           reinterpret_cast<const uint4 *>(bTiles), sh, sl, dmask,
+                                                           zeroDirichlet ? 1 : 0, partialDot, partialDot ? 1 : 0, rhs,
+                                                           t.nTZ, t.nTY, t.segLen, status);
+    VFEM_LAUNCH_CHECK();
+    return blocks;
+}
+
+}  // namespace vfem

@@ -222,10 +222,35 @@ int vfem_mg_level_dirichlet_mask(const vfem_mg *mg, int level, uint8_t *mask_out
 int vfem_mg_set_precision(vfem_mg *mg, int precision, int outer_matvec) {
     return guarded([&] {
         need(mg, "mg");
-        if (outer_matvec != MATVEC_FP64 && outer_matvec != MATVEC_DF) throw Error(ERR_ARG, "unknown matvec kind");
+        if (outer_matvec != MATVEC_FP64 && outer_matvec != MATVEC_DF && outer_matvec != MATVEC_DF_SIMT)
+            throw Error(ERR_ARG, "unknown matvec kind");
         mg->m.setPrecision(precision);
         if (mg->m.outerMatvec != outer_matvec) mg->m.clearGraphs();
         mg->m.outerMatvec = outer_matvec;
+    });
+}
+int vfem_mg_outer_apply(vfem_mg *mg, const double *u, const double *rhs, double *out) {
+    return guarded([&] {
+        need(mg, "mg");
+        need(u, "u");
+        need(out, "out");
+        mg->m.outerApply(u, out, rhs);
+    });
+}
+int vfem_mg_outer_matvec_kind(const vfem_mg *mg, int *kind) {
+    return guarded([&] {
+        need(mg, "mg");
+        need(kind, "kind");
+        *kind = mg->m.outerKind();
+    });
+}
+int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, int *ok) {
+    return guarded([&] {
+        need(k0_576, "K0");
+        need(scale, "scale");
+        need(tiles_2048, "tiles");
+        need(ok, "ok");
+        *ok = tc_fit_k0(k0_576, scale, tiles_2048) ? 1 : 0;
     });
 }
 int vfem_mg_set_device_loop(vfem_mg *mg, int on) {

@@ -114,6 +114,16 @@ void Grid::setETensor(double E, double nu_) {
         K0df.hi[t] = (float)K0.a[t];
         K0df.lo[t] = (float)(K0.a[t] - (double)K0df.hi[t]);
     }
+    tcTiles.assign(2048, 0);
+    tcOk = tc_fit_k0(K0.a, &tcScale, tcTiles.data());
+    if (tcOk) {
+        tcB.alloc(2048);
+        VFEM_CUDA(cudaMemcpy(tcB.p, tcTiles.data(), 2048 * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    if (!tcStatus.p) {
+        tcStatus.alloc(1);
+        VFEM_CUDA(cudaMemset(tcStatus.p, 0, sizeof(int)));
+    }
     double kv[10];
     const bool cube = k0_cube_values(K0.a, kv);
     K0.isCube = K0f.isCube = K0df.isCube = cube ? 1 : 0;
@@ -571,6 +581,11 @@ void MG::allocLevels() {
 static void syncFineGeom(MG &mg) {
     // the fine level shares the grid's (possibly masked) geometry
     mg.lv[0].g = mg.fine->g;
+    // captured graphs hold K0 (kernel parameters) and the matvec kind chosen for it
+    if (mg.graphK0Version != mg.fine->k0Version) {
+        mg.clearGraphs();
+        mg.graphK0Version = mg.fine->k0Version;
+    }
 }
 
 template <typename T>
@@ -833,21 +848,79 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool h
         launch_cg_precond_out<double>(g, rbuf.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
     }
     launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
-    const bool df = precision == PREC_MIXED && outerMatvec == MATVEC_DF;
-    launch_cg_direction(g, s.p, dvec.p, sc.p, df ? dhi.p : nullptr, df ? dlo.p : nullptr, st);
-    const int nb = (int)gridFor(g.NN, 256);
-    if (df) {
-        const float *yh, *yl;
-        fine->youngDF(&yh, &yl);
-        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true, partials.p,
-                              partialCount, st);
-    } else
-        launch_applyk_fine<double>(g, fine->Y.p, dvec.p, Ad.p, fine->K0, true, false, fine->dmask.p, true, partials.p,
-                                   partialCount, st);
+    outerDirection();
+    const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
     launch_cg_alpha(partials.p, nb, sc.p, st);
     launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
     launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
     if (hostMirror) VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+}
+
+int MG::outerKind() const {
+    if (precision != PREC_MIXED || outerMatvec == MATVEC_FP64) return 0;
+    if (outerMatvec == MATVEC_DF && fine->tcOk) return 2;
+    return 1;
+}
+
+void MG::outerDirection() {
+    const int kind = outerKind();
+    if (kind == 2) umax.alloc(REDUCE_BLOCKS);
+    launch_cg_direction(lv[0].g, s.p, dvec.p, sc.p, kind == 1 ? dhi.p : nullptr, kind == 1 ? dlo.p : nullptr,
+                        fine->stream, kind == 2 ? umax.p : nullptr);
+}
+
+int MG::outerMatvecApply(const double *u, double *out, double *partialsOut, const double *rhs, bool uReady) {
+    const Geom &g = lv[0].g;
+    cudaStream_t st = fine->stream;
+    const int kind = outerKind();
+    if (kind == 2) {
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+        umax.alloc(REDUCE_BLOCKS);
+        if (!uReady) launch_absmax_partials(u, 3 * g.ld, umax.p, st);
+        return launch_applyk_fine_tc(g, yh, yl, u, umax.p, out, fine->tcB.p, fine->tcScale, fine->dmask.p, true,
+                                     partialsOut, partialCount, fine->tcStatus.p, st, rhs);
+    }
+    if (kind == 1) {
+        const float *yh, *yl;
+        fine->youngDF(&yh, &yl);
+        if (!uReady) launch_split_df(u, dhi.p, dlo.p, 3 * g.ld, st);
+        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, u, out, fine->K0df, fine->dmask.p, true, partialsOut,
+                              partialCount, st, rhs);
+        return (int)gridFor(g.NN, 256);
+    }
+    if (rhs) {
+        launch_residual_fine<double>(g, fine->Y.p, u, rhs, out, fine->K0, fine->dmask.p, st);
+        return 0;
+    }
+    launch_applyk_fine<double>(g, fine->Y.p, u, out, fine->K0, true, false, fine->dmask.p, true, partialsOut,
+                               partialCount, st);
+    return (int)gridFor(g.NN, 256);
+}
+
+void MG::outerApply(const double *u, double *out, const double *rhs) {
+    syncFineGeom(*this);
+    cudaStream_t st = fine->stream;
+    const size_t bytes = 3 * fine->g.NN * sizeof(double);
+    View vu, vo, vr;
+    viewIn(vu, u, bytes, st);
+    if (rhs) viewIn(vr, rhs, bytes, st);
+    viewOut(vo, out, bytes);
+    outerMatvecApply((const double *)vu.d, (double *)vo.d, nullptr, rhs ? (const double *)vr.d : nullptr, false);
+    finishOut(vo, st);
+    VFEM_CUDA(cudaStreamSynchronize(st));
+    checkTensorStatus();
+}
+
+void MG::checkTensorStatus() {
+    if (outerKind() != 2) return;
+    int v = 0;
+    VFEM_CUDA(cudaMemcpyAsync(&v, fine->tcStatus.p, sizeof(int), cudaMemcpyDeviceToHost, fine->stream));
+    VFEM_CUDA(cudaStreamSynchronize(fine->stream));
+    if (v) {
+        VFEM_CUDA(cudaMemsetAsync(fine->tcStatus.p, 0, sizeof(int), fine->stream));
+        throw Error(ERR_CUDA, "tensor-core matvec: a wait for the tensor core timed out");
+    }
 }
 
 static uint64_t countKernelNodes(cudaGraph_t graph) {
@@ -929,14 +1002,8 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
-    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF) {
-        const float *yh, *yl;
-        fine->youngDF(&yh, &yl);
-        launch_split_df(x, dhi.p, dlo.p, 3 * g.ld, st);
-        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, x, rbuf.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st, b);
-    } else {
-        launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
-    }
+    // initial residual through the outer operator, like every later product
+    outerMatvecApply(x, rbuf.p, nullptr, b, false);
     launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
     launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
@@ -945,7 +1012,8 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
         fine->youngF();
         fine->youngFPad();
         const float *yh, *yl;
-        if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
+        if (outerMatvec != MATVEC_FP64) fine->youngDF(&yh, &yl);
+        if (outerKind() == 2) umax.alloc(REDUCE_BLOCKS);
     }
     allocLevels();
     if (mgIter > 0) ensureStiffness(true);  // positive definiteness checked in pcgFinish
@@ -961,6 +1029,7 @@ PcgStats MG::pcgFinish() {
     VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
     checkStiffness();  // synchronises the stream
     VFEM_CUDA(cudaStreamSynchronize(st));
+    checkTensorStatus();
     PcgStats stats;
     stats.iterations = (int64_t)hostSc[9];
     stats.rsq = hostSc[5];
@@ -988,12 +1057,9 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
     const double bnorm2 = readScalar(sc.p + 7, st);
-    if (precision == PREC_MIXED && outerMatvec == MATVEC_DF && L() > 1) {
-        // initial residual through the double-float operator, like every later product
-        const float *yh, *yl;
-        fine->youngDF(&yh, &yl);
-        launch_split_df(x, dhi.p, dlo.p, 3 * g.ld, st);
-        launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, x, rbuf.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st, b);
+    if (L() > 1) {
+        // initial residual through the outer operator, like every later product
+        outerMatvecApply(x, rbuf.p, nullptr, b, false);
     } else {
         launch_residual_fine<double>(g, fine->Y.p, x, b, rbuf.p, fine->K0, fine->dmask.p, st);
     }
@@ -1035,7 +1101,8 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
         fine->youngF();
         fine->youngFPad();
         const float *yh, *yl;
-        if (outerMatvec == MATVEC_DF) fine->youngDF(&yh, &yl);
+        if (outerMatvec != MATVEC_FP64) fine->youngDF(&yh, &yl);
+        if (outerKind() == 2) umax.alloc(REDUCE_BLOCKS);
         allocLevels();
     }
     const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
@@ -1089,6 +1156,7 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
             if (cb(user, i, std::sqrt(rsq), x, rbuf.p)) break;
         }
     }
+    checkTensorStatus();
     stats.iterations = i - 1;
     stats.rsq = rsq;
     stats.relres = bnorm2 > 0 ? std::sqrt(rsq / bnorm2) : std::sqrt(rsq);
@@ -1493,7 +1561,7 @@ double MG::kernelBytes(int which) const {
     switch (which) {
     case 0: return 8.0 * (6 * nn + ne);
     case 1: return 4.0 * (6 * nn + ne);
-    case 2: return 8.0 * (6 * nn + ne);
+    case 2: case 10: return 8.0 * (6 * nn + ne);
     case 3: return 4.0 * (9 * nn + ne);
     case 4: return 8.0 * (9 * nn + ne);
     case 5: return 4.0 * (9 * nn + ne);
@@ -1535,6 +1603,11 @@ double MG::timeKernel(int which, int reps) {
         launch_fill<double>(D.x.p, 0.5, n3, st);
         launch_fill<double>(D.b.p, 1.0, n3, st);
         if (which == 2) launch_split_df(D.x.p, dhi.p, dlo.p, n3, st);
+        if (which == 10) {
+            if (!fine->tcOk) throw Error(ERR_ARG, "K0 has no scaled small-integer form for the tensor-core matvec");
+            umax.alloc(REDUCE_BLOCKS);
+            launch_absmax_partials(D.x.p, n3, umax.p, st);
+        }
     }
     auto run = [&]() {
         switch (which) {
@@ -1544,6 +1617,13 @@ double MG::timeKernel(int which, int reps) {
             const float *yh, *yl;
             fine->youngDF(&yh, &yl);
             launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, D.x.p, D.r.p, fine->K0df, fine->dmask.p, true, nullptr, 0, st);
+            break;
+        }
+        case 10: {
+            const float *yh, *yl;
+            fine->youngDF(&yh, &yl);
+            launch_applyk_fine_tc(g, yh, yl, D.x.p, umax.p, D.r.p, fine->tcB.p, fine->tcScale, fine->dmask.p, true,
+                                  nullptr, 0, fine->tcStatus.p, st);
             break;
         }
         case 3: smoothT<float>(0, true); break;
@@ -1678,21 +1758,9 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
     for (int r = 0; r < reps; ++r) {
         if (precision == PREC_FP64) body(double());
         else body(float());
-        const bool df = precision == PREC_MIXED && outerMatvec == MATVEC_DF;
-        timed("cg:direction", [&] {
-            launch_cg_direction(g, s.p, dvec.p, sc.p, df ? dhi.p : nullptr, df ? dlo.p : nullptr, st);
-        });
+        timed("cg:direction", [&] { outerDirection(); });
         timed("cg:matvec+alpha", [&] {
-            const int nb = (int)gridFor(g.NN, 256);
-            if (df) {
-                const float *yh, *yl;
-                fine->youngDF(&yh, &yl);
-                launch_applyk_fine_df(g, yh, yl, dhi.p, dlo.p, dvec.p, Ad.p, fine->K0df, fine->dmask.p, true,
-                                      partials.p, partialCount, st);
-            } else {
-                launch_applyk_fine<double>(g, fine->Y.p, dvec.p, Ad.p, fine->K0, true, false, fine->dmask.p, true,
-                                           partials.p, partialCount, st);
-            }
+            const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
             launch_cg_alpha(partials.p, nb, sc.p, st);
         });
         timed("cg:update+rsq", [&] {

@@ -18,7 +18,10 @@
 namespace vfem {
 
 enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
-enum OuterMatvec { MATVEC_FP64 = 0, MATVEC_DF = 1 };
+// Outer CG matvec of the mixed solve. MATVEC_DF: FP64-class accuracy without FP64 arithmetic,
+// on the tensor cores (integer-slice operands) when K0 is a scaled small-integer matrix, else in
+// double-float on the FP32 units; MATVEC_DF_SIMT forces the double-float kernel.
+enum OuterMatvec { MATVEC_FP64 = 0, MATVEC_DF = 1, MATVEC_DF_SIMT = 2 };
 
 bool isDevicePtr(const void *p);
 
@@ -48,6 +51,12 @@ public:
     Mat24<double> K0;
     Mat24<float> K0f;
     Mat24DF K0df;
+    // K0 = tcScale * C with C a small-integer matrix: bf16 B tiles of the tensor-core matvec
+    bool tcOk = false;
+    double tcScale = 0.0;
+    std::vector<uint16_t> tcTiles;
+    DevBuf<uint16_t> tcB;
+    DevBuf<int> tcStatus;  // nonzero: a tensor-core wait timed out
     double E0 = 1.0, Emin = 1e-4, gamma = 3.0, q = 3.0;  // TensorProductSimulator.hh:2137-2141
     int law = 0;                                          // 0 SIMP, 1 RAMP
     double maskH = std::numeric_limits<double>::infinity();
@@ -203,6 +212,18 @@ public:
     // CG workspace
     DevBuf<double> rbuf, s, dvec, Ad, partials, sc, xbuf;
     DevBuf<float> dhi, dlo;  // double-float split of the search direction
+    DevBuf<double> umax;     // partial maxima of |operand| of the tensor-core matvec
+    // kind of the mixed outer matvec in use: 0 FP64, 1 double-float (FP32 units), 2 tensor cores
+    int outerKind() const;
+    // d = beta d + s with the side outputs the outer matvec needs
+    void outerDirection();
+    // out = K u (rhs: rhs - K u) with the outer matvec; uReady: u's side data (split or maxima)
+    // are current. Returns the number of partial dots written when partialsOut is given.
+    int outerMatvecApply(const double *u, double *out, double *partialsOut, const double *rhs, bool uReady);
+    void checkTensorStatus();
+    // out = K u (rhs: rhs - K u) through the mixed solve's outer matvec on caller vectors
+    void outerApply(const double *u, double *out, const double *rhs);
+    uint64_t graphK0Version = 0;
     double *hostSc = nullptr;  // pinned mirror of sc
     int partialCount = 0;
 

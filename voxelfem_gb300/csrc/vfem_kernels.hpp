@@ -199,9 +199,26 @@ void launch_cg_rsq(const double *partials, int n, double *sc, double *hostMirror
 template <typename Ts>
 void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                            double *partials, cudaStream_t st);
-// d = beta d + s; when dh is given also writes the double-float split of d into (dh, dl).
+// d = beta d + s; when dh is given also writes the double-float split of d into (dh, dl), when
+// amax is given the REDUCE_BLOCKS partial maxima of |d| (NaN propagates).
 void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
-                         cudaStream_t st);
+                         cudaStream_t st, double *amax = nullptr);
+
+// ---------------- tensor-core outer matvec (k_tc.cu) ----------------
+// K0 = scale * C with C an integer matrix whose row sums keep the bf16 MMA accumulators exact;
+// fills the B tiles (2048 bf16). False when K0 has no such form.
+bool tc_fit_k0(const double K0[576], double *scale, uint16_t bTiles[2048]);
+int tc_matvec_blocks(const Geom &g, int maxBlocks);
+// REDUCE_BLOCKS partial maxima of |u[0..n)| (NaN propagates)
+void launch_absmax_partials(const double *u, int64_t n, double *partials, cudaStream_t st);
+// out = K u (or rhs - K u) to FP64-class accuracy on the tensor cores; umax holds the partial
+// maxima of |u|. Constrained components of out zeroed (zeroDirichlet), detached rows zero.
+// Returns the number of partial dots u . out written (one per CTA) when partialDot is given.
+// A bounded wait that expires sets *status.
+int launch_applyk_fine_tc(const Geom &g, const float *Yh, const float *Yl, const double *u, const double *umax,
+                          double *out, const uint16_t *bTiles, double scale, const uint8_t *dmask, bool zeroDirichlet,
+                          double *partialDot, int partialBlocks, int *status, cudaStream_t st,
+                          const double *rhs = nullptr);
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
                       double *partials, cudaStream_t st);
 void launch_copy(double *dst, const double *src, int64_t n, cudaStream_t st);

@@ -445,11 +445,29 @@ class MultigridSolver:
 
     def setPrecision(self, precision="fp64", outerMatvec="df"):
         """'fp64' (the reference's method) or 'mixed' (FP32 V-cycle in FP64 CG); the outer
-        matvec of the mixed mode is 'df' (double-float) or 'fp64'."""
+        matvec of the mixed mode is 'df' (FP64-class without FP64 arithmetic: tensor cores for
+        cube voxels with a rational Poisson ratio, else double-float), 'df-simt' (double-float
+        on the FP32 units) or 'fp64'."""
         p = {"fp64": 0, "mixed": 1}[precision]
-        m = {"fp64": 0, "df": 1}[outerMatvec]
+        m = {"fp64": 0, "df": 1, "df-simt": 2}[outerMatvec]
         check(_lib().vfem_mg_set_precision(self._h, p, m))
         self._prec = precision
+
+    def outerMatvecKind(self):
+        """'fp64', 'df-simt' or 'tensor': the outer matvec the mixed solve uses now."""
+        k = C.c_int()
+        check(_lib().vfem_mg_outer_matvec_kind(self._h, C.byref(k)))
+        return {0: "fp64", 1: "df-simt", 2: "tensor"}[k.value]
+
+    def outerApply(self, u, rhs=None):
+        """K u (rhs - K u when rhs is given), constrained components zeroed, through the outer
+        matvec of the mixed solve (diagnostic)."""
+        nn = self._nn(0)
+        u = _as_vfield(u, nn)
+        out = _new_vfield(nn)
+        r = None if rhs is None else _as_vfield(rhs, nn)
+        check(_lib().vfem_mg_outer_apply(self._h, ptr(u), None if r is None else ptr(r), ptr(out)))
+        return out
 
     def setDeviceLoop(self, on):
         """Run a solve as one device-resident graph loop (default) or one graph per iteration."""
