@@ -150,46 +150,54 @@ __device__ __forceinline__ uint32_t bf16_bits(int d) {
     return __float_as_uint(f) >> 16;
 }
 
-// Digit-table entries of one node: for pair a, [128 D_2a (c = 0, 1, 2), D_2a+1 (c = 0, 1, 2), 0, 0].
-__device__ __forceinline__ void node_digits(const double u3[3], int sh0, uint4 out[NACC]) {
-    int D[3][2 * NACC];
+// Signed base-128 digits of round(v 2^(55 - s)) written into the digit tables of one node row:
+// for pair a, 128 D_2a at value c and D_2a+1 at value 3 + c of the row's 8 (values 6, 7 stay 0).
+__device__ __forceinline__ void store_digits(double v, int sh0, uint8_t *row, int c) {
+    long long F = fixed_point(v, sh0);
+    int D[2 * NACC];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        long long F = fixed_point(u3[c], sh0);
-#pragma unroll
-        for (int i = 2 * NACC - 1; i >= 1; --i) {
-            const int d = (int)((F + 64) & 127) - 64;
-            D[c][i] = d;
-            F = (F - d) >> 7;
-        }
-        D[c][0] = (int)F;
+    for (int i = 2 * NACC - 1; i >= 1; --i) {
+        const int d = (int)((F + 64) & 127) - 64;
+        D[i] = d;
+        F = (F - d) >> 7;
     }
+    D[0] = (int)F;
 #pragma unroll
     for (int a = 0; a < NACC; ++a) {
-        const uint32_t h0 = bf16_bits(128 * D[0][2 * a]), h1 = bf16_bits(128 * D[1][2 * a]),
-                       h2 = bf16_bits(128 * D[2][2 * a]);
-        const uint32_t l0 = bf16_bits(D[0][2 * a + 1]), l1 = bf16_bits(D[1][2 * a + 1]), l2 = bf16_bits(D[2][2 * a + 1]);
-        out[a] = make_uint4(h0 | (h1 << 16), h2 | (l0 << 16), l1 | (l2 << 16), 0u);
+        *reinterpret_cast<uint16_t *>(row + a * TAB + 2 * c) = (uint16_t)bf16_bits(128 * D[2 * a]);
+        *reinterpret_cast<uint16_t *>(row + a * TAB + 2 * (3 + c)) = (uint16_t)bf16_bits(D[2 * a + 1]);
     }
 }
 
-// Digit tables of node plane x for the patch whose first node is (ny0, nz0); zero outside the grid.
-__device__ __forceinline__ void build_tables(const Geom &g, const double *__restrict__ u, int x, int ny0, int nz0,
-                                             int sh0, uint8_t *tab) {
-    for (int t = threadIdx.x; t < TROWS; t += TCT) {
-        const int zn = t % NPZ, yn = t / NPZ;
-        const int y = ny0 + yn, z = nz0 + zn;
-        double u3[3] = {0.0, 0.0, 0.0};
-        if (x >= 0 && x < g.nn[0] && y >= 0 && y < g.nn[1] && z >= 0 && z < g.nn[2]) {
-            const int64_t n = g.node(x, y, z);
+// The patch's node plane x as 3 x TROWS items (node-major: item = 3 node + c, node = yn NPZ + zn,
+// so consecutive threads read consecutive z); item tid + TCT k goes to pf[k]. Zero outside the grid.
+constexpr int PF = (3 * TROWS + TCT - 1) / TCT;
+
+__device__ __forceinline__ void load_plane(const Geom &g, const double *__restrict__ u, int x, int ny0, int nz0,
+                                           double pf[PF]) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) u3[c] = u[c * g.ld + n];
+    for (int k = 0; k < PF; ++k) {
+        const int item = threadIdx.x + TCT * k;
+        pf[k] = 0.0;
+        if (item < 3 * TROWS) {
+            const int node = item / 3, c = item - 3 * node;
+            const int yn = node / NPZ, zn = node - NPZ * yn;
+            const int y = ny0 + yn, z = nz0 + zn;
+            if (x >= 0 && x < g.nn[0] && y >= 0 && y < g.nn[1] && z >= 0 && z < g.nn[2])
+                pf[k] = __ldg(u + c * g.ld + g.node(x, y, z));
         }
-        uint4 e[NACC];
-        node_digits(u3, sh0, e);
-        const int row = zn * NPY + yn;
+    }
+}
+
+__device__ __forceinline__ void build_tables(const double pf[PF], int sh0, uint8_t *tab) {
 #pragma unroll
-        for (int a = 0; a < NACC; ++a) *reinterpret_cast<uint4 *>(tab + a * TAB + row * 16) = e[a];
+    for (int k = 0; k < PF; ++k) {
+        const int item = threadIdx.x + TCT * k;
+        if (item < 3 * TROWS) {
+            const int node = item / 3, c = item - 3 * node;
+            const int yn = node / NPZ, zn = node - NPZ * yn;
+            store_digits(pf[k], sh0, tab + (zn * NPY + yn) * 16, c);
+        }
     }
 }
 
@@ -271,11 +279,65 @@ __global__ void __launch_bounds__(TCT, 4)
     double dot = 0.0;
     bool ok = true;
     int phase = 0;
-    build_tables(g, u, X0 - 1, ny0, nz0, sh0, tabs + ((X0 - 1) & 1) * NACC * TAB);
-    for (int L = X0 - 1; L < X1 && ok; ++L) {
-        // tables of node plane L + 1 (plane L was built by the previous step)
-        build_tables(g, u, L + 1, ny0, nz0, sh0, tabs + ((L + 1) & 1) * NACC * TAB);
+
+    // node phase of element layer Lp (its staging is current): the pending plane Lp gets the
+    // layer's lower-face contributions and is written; plane Lp + 1 starts with its upper face
+    auto nodePhase = [&](int Lp) {
+        if (!owner) return;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            float h = ah[r], l = al[r];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int dy = q >> 1, dz = q & 1;
+                const int idx = (3 * q + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                float t, e;
+                two_sum(h, stH[idx], t, e);
+                h = t;
+                l += e + stL[idx];
+            }
+            float h2 = 0.f, l2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int dy = q >> 1, dz = q & 1;
+                const int idx = (3 * (4 + q) + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                float t, e;
+                two_sum(h2, stH[idx], t, e);
+                h2 = t;
+                l2 += e + stL[idx];
+            }
+            ah[r] = h2;
+            al[r] = l2;
+            if (Lp >= X0 && nIn) {
+                const int64_t n = g.node(Lp, nj, nk);
+                double f = 0.0;
+                if (nj < g.nyv()) {
+                    const uint8_t dm = zeroDir ? dmask[n] : 0;
+                    f = ((dm >> r) & 1) ? 0.0 : ((double)h + (double)l) * outScale;
+                    if (withDot) dot += u[r * g.ld + n] * f;
+                }
+                if (rhs) {
+                    const uint8_t dm = dmask[n];
+                    f = ((dm >> r) & 1) ? 0.0 : rhs[r * g.ld + n] - f;
+                }
+                out[r * g.ld + n] = f;
+            }
+        }
+    };
+
+    // the two zero values of every digit-table row
+    for (int t = tid; t < 2 * NACC * TROWS; t += TCT) *reinterpret_cast<uint32_t *>(tabs + t * 16 + 12) = 0u;
+    double pf[PF];
+    load_plane(g, u, X0 - 1, ny0, nz0, pf);
+    build_tables(pf, sh0, tabs + ((X0 - 1) & 1) * NACC * TAB);
+    load_plane(g, u, X0, ny0, nz0, pf);
+    for (int L = X0 - 1; L < X1; ++L) {
+        // tables of node plane L + 1 (plane L was built by the previous step); plane L + 2's
+        // operand loads stay in flight through the rest of the step
+        build_tables(pf, sh0, tabs + ((L + 1) & 1) * NACC * TAB);
+        load_plane(g, u, L + 2, ny0, nz0, pf);
         fence_async_smem();
+        tc_fence_before();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
@@ -290,7 +352,8 @@ __global__ void __launch_bounds__(TCT, 4)
                 }
             mma_commit(smem_addr(mbar));
         }
-        // element scale E_e c (double-float) while the tensor core runs
+        // while the tensor core runs: the previous layer's node phase and this layer's scales
+        if (L > X0 - 1) nodePhase(L - 1);
         float sh = 0.f, sl = 0.f;
         if (eIn && L >= 0 && L < g.ne[0]) {
             const int64_t e = g.padElem(L, ej, ek);
@@ -329,52 +392,10 @@ __global__ void __launch_bounds__(TCT, 4)
                 stL[(c0 + j) * SDOF + ey * SPITCH + ez] = e;
             }
         }
-        tc_fence_before();
+    }
+    if (ok) {
         __syncthreads();
-        if (owner) {
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                // plane L: the pending sum plus this layer's lower-face contributions (dx = 0)
-                float h = ah[r], l = al[r];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int dy = q >> 1, dz = q & 1;
-                    const int idx = (3 * q + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
-                    float t, e;
-                    two_sum(h, stH[idx], t, e);
-                    h = t;
-                    l += e + stL[idx];
-                }
-                // plane L + 1 starts with the upper-face contributions (dx = 1)
-                float h2 = 0.f, l2 = 0.f;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int dy = q >> 1, dz = q & 1;
-                    const int idx = (3 * (4 + q) + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
-                    float t, e;
-                    two_sum(h2, stH[idx], t, e);
-                    h2 = t;
-                    l2 += e + stL[idx];
-                }
-                ah[r] = h2;
-                al[r] = l2;
-                if (L >= X0 && nIn) {
-                    const int64_t n = g.node(L, nj, nk);
-                    double f = 0.0;
-                    if (nj < g.nyv()) {
-                        const uint8_t dm = zeroDir ? dmask[n] : 0;
-                        f = ((dm >> r) & 1) ? 0.0 : ((double)h + (double)l) * outScale;
-                        if (withDot) dot += u[r * g.ld + n] * f;
-                    }
-                    if (rhs) {
-                        const uint8_t dm = dmask[n];
-                        f = ((dm >> r) & 1) ? 0.0 : rhs[r * g.ld + n] - f;
-                    }
-                    out[r * g.ld + n] = f;
-                }
-            }
-        }
-        __syncthreads();
+        nodePhase(X1 - 1);
     }
     if (withDot) {
         const double tot = block_sum<TCT>(dot);
