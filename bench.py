@@ -523,7 +523,7 @@ def run_q2(hbm, solve=True):
     g.setDensities(np.random.default_rng(0).uniform(0.01, 1.0, int(np.prod(ne))))
     flops = 2.0 * 81 * 81 * g.numElements()
     out = {"workload": "128^3 Q2 applyK (%d nodes), rho U[0.01,1] seed 0" % g.numNodes()}
-    for name, prec, reps in (("fp64", 0, 2), ("fp32", 1, 10)):
+    for name, prec, reps in (("fp64", 0, 2), ("df", 2, 3), ("fp32", 1, 10)):
         ms, nbytes = C.c_double(), C.c_double()
         _capi.check(lib.vfem_q2_time_apply_k(g._h, prec, reps, C.byref(ms), C.byref(nbytes)))
         gbs = nbytes.value / (ms.value * 1e-3) / 1e9
@@ -536,9 +536,10 @@ def run_q2(hbm, solve=True):
 
 def run_q2_solve(g, ne):
     """Time to relative residual 1e-8 of the 128^3 Q2 cantilever (x = 0 face fixed, unit total -y
-    load spread over the nodes of the x = max, z = mid edge): FP64 CG, p-multigrid preconditioner
-    (Q2 block Gauss-Seidel around an FP32 trilinear V-cycle with 5 coarsenings). The accuracy check
-    is the true FP64 residual |f - K u| / |f| of the returned u."""
+    load spread over the nodes of the x = max, z = mid edge): FP64 CG with the double-float
+    matvec, p-multigrid preconditioner (Q2 block Gauss-Seidel around an FP32 trilinear V-cycle with
+    5 coarsenings). The accuracy check is the true FP64 residual |f - K u| / |f| of the returned
+    u."""
     import time
 
     nx, ny, nz = ne

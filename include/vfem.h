@@ -267,7 +267,9 @@ int vfem_q2_get_k0(const vfem_q2 *g, double *out6561);
 /* zero-displacement supports on the nodes inside [min, max], components in cmask (bit c = component c) */
 int vfem_q2_add_dirichlet(vfem_q2 *g, const double min_corner[3], const double max_corner[3], int cmask);
 int vfem_q2_get_dirichlet_mask(const vfem_q2 *g, uint8_t *mask_out);
-/* applyK (TPSStencils.hh:135-186); zero_dirichlet zeroes the constrained components of the result */
+/* applyK (TPSStencils.hh:135-186); precision VFEM_PREC_FP64, VFEM_PREC_MIXED (FP32 arithmetic) or
+ * 2 (double-float: FP64-class on the FP32 units); zero_dirichlet zeroes the constrained
+ * components of the result */
 int vfem_q2_apply_k(vfem_q2 *g, const double *u, double *out, int precision, int zero_dirichlet);
 /* one 27-colour block Gauss-Seidel sweep on K u = b (MultigridSolver.hh:277-321, 409-442); u in/out */
 int vfem_q2_smooth(vfem_q2 *g, double *u_inout, const double *b, int forward, int precision);
@@ -281,7 +283,10 @@ int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double
 /* preconditionedConjugateGradient on a triquadratic grid (MultigridSolver.hh:1047-1152 recurrences,
  * FP64 outer iteration). The preconditioner is this library's p-multigrid cycle: Q2 block
  * Gauss-Seidel sweeps (mg_smoothing_iterations before and after) around one FP32 V-cycle of the
- * trilinear problem on the same mesh with `coarsenings` coarsenings. x in/out. */
+ * trilinear problem on the same mesh with `coarsenings` coarsenings. x in/out. The CG matvec is
+ * double-float unless vfem_q2_set_outer_matvec chose FP64. */
+/* outer matvec of vfem_q2_pcg: VFEM_MATVEC_FP64 or VFEM_MATVEC_DF (default); no reference counterpart */
+int vfem_q2_set_outer_matvec(vfem_q2 *g, int outer_matvec);
 int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
                 int64_t mg_smoothing_iterations, vfem_pcg_stats *stats);
 

@@ -38,6 +38,7 @@ def test_q2_k0_and_apply_k(gpu, oracle, ne):
     u = np.random.default_rng(1).standard_normal((g.numNodes(), 3))
     ref = po.q2_apply_k(ne, K0, Y, u)
     assert rel(g.applyK(u), ref) < 1e-12
+    assert rel(g.applyK(u, precision="df"), ref) < 1e-12
     assert rel(g.applyK(u, precision="fp32"), ref) < 1e-5
     z = g.applyK(u, zeroDirichlet=True)
     ref[g.getDirichletMask()] = 0
@@ -75,8 +76,8 @@ def test_q2_factory(gpu):
         g.multigridSolver(0)
 
 
-@pytest.mark.parametrize("coarsenings", [1, 2])
-def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings):
+@pytest.mark.parametrize("coarsenings,matvec", [(1, "df"), (2, "df"), (2, "fp64")])
+def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings, matvec):
     """The PCG solution equals a dense direct solve of the oracle's Q2 operator on the free DOFs."""
     ne = (8, 4, 4)
     g, Y, bits = make(ne, seed=5)
@@ -99,6 +100,7 @@ def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings):
     xs[~fixed] = np.linalg.solve(Kd[np.ix_(~fixed, ~fixed)], bvec[~fixed])
     xref = xs.reshape(3, nn).T
     mg = g.multigridSolver(coarsenings)
+    mg.setOuterMatvec(matvec)
     x = mg.preconditionedConjugateGradient(np.zeros((nn, 3)), f, 200, 1e-11, None, 1, 2, False)
     assert mg.lastStats.relres <= 1e-11
     assert rel(x, xref) < 1e-8

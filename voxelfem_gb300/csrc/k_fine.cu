@@ -6,6 +6,7 @@
 // (TPSStencils.hh:577-659): element (i-a, j-b, k-c) for a, b, c in {0,1}, in which
 // the node has local index 4a+2b+c. K0 is a by-value kernel parameter (constant
 // bank); its symmetry lets every thread scan a column K0[:, row].
+#include "vfem_df.cuh"
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 
@@ -417,28 +418,6 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kern
 }
 
 // ---------------- double-float FP64-accurate matvec ----------------
-struct DF {
-    float hi, lo;
-};
-
-__device__ __forceinline__ void df_split(double v, float &hi, float &lo) {
-    hi = __double2float_rn(v);
-    lo = __double2float_rn(v - (double)hi);
-}
-
-// (sh, sl) += a*b with a = (ah, al), b = (bh, bl) (error-free product of the high parts)
-__device__ __forceinline__ void df_fma_acc(float ah, float al, float bh, float bl, float &sh, float &sl) {
-    const float p = ah * bh;
-    float e = __fmaf_rn(ah, bh, -p);
-    e = __fmaf_rn(ah, bl, e);
-    e = __fmaf_rn(al, bh, e);
-    const float t = sh + p;
-    const float bp = t - sh;
-    const float err = (sh - (t - bp)) + (p - bp);
-    sh = t;
-    sl += err + e;
-}
-
 template <int LN, typename KV>
 __device__ __forceinline__ void df_elem(const Geom &g, const KV &K, const float *__restrict__ uh_,
                                         const float *__restrict__ ul_, int64_t base, float *ch, float *cl) {

@@ -9,6 +9,7 @@
 // the middle (local 1 of element (I-1)/2). The kernels run one node parity (applyK) or one
 // colour (smoother) per launch, so every warp reads the same K0 rows: K0 lives in constant
 // memory (FP32, 26 KB) or in global memory (FP64, 52 KB) and its reads are broadcasts.
+#include "vfem_df.cuh"
 #include "vfem_kernels.hpp"
 
 #include <type_traits>
@@ -16,6 +17,7 @@
 namespace vfem {
 
 __constant__ float c_K0q2f[81 * 81];
+__constant__ float c_K0q2lo[81 * 81];  // K0 - c_K0q2f (double-float matvec)
 
 namespace {
 
@@ -165,6 +167,75 @@ __device__ __forceinline__ void q2_gather_f32(const Q2Dims &d, const float *__re
             if (!PZ) q2_slot_f32<PX, PY, PZ, WithM, 1, 1, 1>(d, Y, u, I, J, K, s0, s1, s2, M);
         }
     }
+}
+
+// Double-float form of q2_slot_f32: K0 = c_K0q2f + c_K0q2lo, u = uh + ul, E = Yh + Yl;
+// (fh, fl) += E_e K0[3 LN + r, :] u_e.
+template <int PX, int PY, int PZ, int SA, int SB, int SC>
+__device__ __forceinline__ void q2_slot_df(const Q2Dims &d, const float *__restrict__ Yh, const float *__restrict__ Yl,
+                                           const float *__restrict__ uh, const float *__restrict__ ul, int I, int J,
+                                           int K, float *fh, float *fl) {
+    int ei, ej, ek;
+    if (!q2_slot<PX>(I, d.ne[0], SA, ei) || !q2_slot<PY>(J, d.ne[1], SB, ej) || !q2_slot<PZ>(K, d.ne[2], SC, ek)) return;
+    constexpr int LN = 9 * Q2Local<PX, SA>::value + 3 * Q2Local<PY, SB>::value + Q2Local<PZ, SC>::value;
+    const int64_t e = ((int64_t)ei * d.ne[1] + ej) * d.ne[2] + ek;
+    const float eh = Yh[e], el = Yl[e];
+    const int64_t ld = d.NN;
+    const int64_t base = q2node(d, 2 * ei, 2 * ej, 2 * ek);
+    const int64_t sx = (int64_t)d.nn[1] * d.nn[2], sy = d.nn[2];
+    float ch[3] = {0.f, 0.f, 0.f}, cl[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < 27; ++m) {
+        const int64_t nm = base + (m / 9) * sx + ((m / 3) % 3) * sy + (m % 3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float vh = uh[c * ld + nm], vl = ul[c * ld + nm];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                df_fma_acc(c_K0q2f[(3 * m + c) * 81 + 3 * LN + r], c_K0q2lo[(3 * m + c) * 81 + 3 * LN + r], vh, vl,
+                           ch[r], cl[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float s = ch[r] + cl[r];
+        const float sl = cl[r] - (s - ch[r]);
+        df_fma_acc(eh, el, s, sl, fh[r], fl[r]);
+    }
+}
+
+// out = K u to FP64-class accuracy on the FP32 units, at the nodes of parity class (PX, PY, PZ);
+// constrained components zeroed when asked; optional partial dots u . out per block.
+template <int PX, int PY, int PZ>
+__global__ void __launch_bounds__(BS) applyk_q2_df_kernel(Q2Dims d, const float *__restrict__ Yh,
+                                                          const float *__restrict__ Yl, const float *__restrict__ uh,
+                                                          const float *__restrict__ ul, double *__restrict__ out,
+                                                          const uint8_t *__restrict__ dmask, int zeroDir) {
+    const int n0 = (d.nn[0] - PX + 1) / 2, n1 = (d.nn[1] - PY + 1) / 2, n2 = (d.nn[2] - PZ + 1) / 2;
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= (int64_t)n0 * n1 * n2) return;
+    const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)n2;
+    const int K = 2 * (int)(tt - q * (uint32_t)n2) + PZ;
+    const int J = 2 * (int)(q % (uint32_t)n1) + PY, I = 2 * (int)(q / (uint32_t)n1) + PX;
+    float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
+    q2_slot_df<PX, PY, PZ, 0, 0, 0>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+    if (!PZ) q2_slot_df<PX, PY, PZ, 0, 0, 1>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+    if (!PY) {
+        q2_slot_df<PX, PY, PZ, 0, 1, 0>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+        if (!PZ) q2_slot_df<PX, PY, PZ, 0, 1, 1>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+    }
+    if (!PX) {
+        q2_slot_df<PX, PY, PZ, 1, 0, 0>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+        if (!PZ) q2_slot_df<PX, PY, PZ, 1, 0, 1>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+        if (!PY) {
+            q2_slot_df<PX, PY, PZ, 1, 1, 0>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+            if (!PZ) q2_slot_df<PX, PY, PZ, 1, 1, 1>(d, Yh, Yl, uh, ul, I, J, K, fh, fl);
+        }
+    }
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = zeroDir ? dmask[n] : 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) out[r * ld + n] = ((dm >> r) & 1) ? 0.0 : (double)fh[r] + (double)fl[r];
 }
 
 template <int PX, int PY, int PZ>
@@ -492,6 +563,27 @@ Q2Dims dims_of(const int ne[3]) {
 
 void q2_upload_k0f(const float *K0f, cudaStream_t st) {
     VFEM_CUDA(cudaMemcpyToSymbolAsync(c_K0q2f, K0f, sizeof(float) * 81 * 81, 0, cudaMemcpyHostToDevice, st));
+}
+
+void q2_upload_k0lo(const float *K0lo, cudaStream_t st) {
+    VFEM_CUDA(cudaMemcpyToSymbolAsync(c_K0q2lo, K0lo, sizeof(float) * 81 * 81, 0, cudaMemcpyHostToDevice, st));
+}
+
+void launch_applyk_q2_df(const int ne[3], const float *Yh, const float *Yl, const float *uh, const float *ul,
+                         double *out, const uint8_t *dmask, bool zeroDirichlet, cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    const int64_t per = (int64_t)(ne[0] + 1) * (ne[1] + 1) * (ne[2] + 1);
+    const unsigned gs = gridFor(per, BS);
+    const int zd = zeroDirichlet ? 1 : 0;
+    applyk_q2_df_kernel<0, 0, 0><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<0, 0, 1><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<0, 1, 0><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<0, 1, 1><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<1, 0, 0><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<1, 0, 1><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<1, 1, 0><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    applyk_q2_df_kernel<1, 1, 1><<<gs, BS, 0, st>>>(d, Yh, Yl, uh, ul, out, dmask, zd);
+    VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>

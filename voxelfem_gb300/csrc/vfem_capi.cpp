@@ -564,6 +564,13 @@ int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, doubl
         q2Interpolate(ne, coarse, fine, accumulate != 0);
     });
 }
+int vfem_q2_set_outer_matvec(vfem_q2 *g, int outer_matvec) {
+    return guarded([&] {
+        need(g, "grid");
+        if (outer_matvec != MATVEC_FP64 && outer_matvec != MATVEC_DF) throw Error(ERR_ARG, "unknown matvec kind");
+        g->g.outerDF = outer_matvec == MATVEC_DF;
+    });
+}
 int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
                 int64_t mg_smoothing_iterations, vfem_pcg_stats *stats) {
     return guarded([&] {

@@ -344,9 +344,11 @@ public:
     int law = 0;
     Geom egeom;  // element grid (for the moduli kernel)
     std::vector<double> K0;
-    std::vector<float> K0f;
+    std::vector<float> K0f, K0lo;  // fl(K0) and K0 - fl(K0)
     DevBuf<double> K0d, rho, Y;
-    DevBuf<float> Yf;
+    DevBuf<float> Yf, Yhi, Ylo;   // FP32 moduli; double-float split of Y
+    DevBuf<float> uhi, ulo;       // double-float split of the outer matvec's operand
+    bool outerDF = true;          // PCG matvec in double-float (else FP64)
     std::vector<uint8_t> dmask_h;
     DevBuf<uint8_t> dmask;
     LevelData<double> w64;
@@ -357,6 +359,7 @@ public:
     void setParams(double E0_, double Emin_, double gamma_, double q_, int law_);
     void setDensities(const double *rho);
     void addDirichlet(const double mn[3], const double mx[3], unsigned cmask);
+    // precision: PREC_FP64, PREC_MIXED (FP32) or 2 (double-float, FP64-class on the FP32 units)
     void applyK(const double *u, double *out, int precision, bool zeroDirichlet);
     void smooth(double *u, const double *b, bool forward, int precision);
     double timeApplyK(int precision, int reps, double *bytes);
@@ -377,6 +380,7 @@ private:
     DevBuf<double> cgX, cgR, cgS, cgD, cgAd, cgPart, cgSc;
     double *cgHost = nullptr;
     void prepareQ1(int coarsenings);
+    void applyDF(const double *u, double *out, bool zeroDirichlet, cudaStream_t st);
     void precondition(const double *r, int64_t sweeps);
     void updateYoungModuli();
     void uploadMask();

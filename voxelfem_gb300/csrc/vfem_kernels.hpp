@@ -242,6 +242,10 @@ void launch_sum_partials(const double *x, int64_t n, double *partials, cudaStrea
 // K0 is 81 x 81 (device pointer, FP64 kernels); the FP32 kernels read the copy uploaded with
 // q2_upload_k0f. ne = elements per axis; vectors are (3, (2ne+1)^3) SoA.
 void q2_upload_k0f(const float *K0f, cudaStream_t st);
+void q2_upload_k0lo(const float *K0lo, cudaStream_t st);  // K0 - fl(K0), for the double-float matvec
+// out = K u in double-float arithmetic (u = uh + ul, Y = Yh + Yl; unpadded arrays), FP64 out
+void launch_applyk_q2_df(const int ne[3], const float *Yh, const float *Yl, const float *uh, const float *ul,
+                         double *out, const uint8_t *dmask, bool zeroDirichlet, cudaStream_t st);
 template <typename T>
 void launch_applyk_q2(const int ne[3], const T *K0, const T *Y, const T *u, T *out, const uint8_t *dmask,
                       bool zeroDirichlet, cudaStream_t st);

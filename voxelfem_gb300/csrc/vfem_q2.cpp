@@ -29,11 +29,14 @@ GridQ2::GridQ2(const int ne_[3], const double bmin_[3], const double bmax_[3]) {
     rho.alloc(NE);
     Y.alloc(NE);
     Yf.alloc(NE);
+    Yhi.alloc(NE);
+    Ylo.alloc(NE);
     VFEM_CUDA(cudaMemsetAsync(rho.p, 0, NE * sizeof(double), stream));
     dmask_h.assign(NN, 0);
     dmask.alloc(NN);
     K0.assign(6561, 0.0);
     K0f.assign(6561, 0.f);
+    K0lo.assign(6561, 0.f);
     K0d.alloc(6561);
     uploadMask();
     setETensor(1.0, 0.0);
@@ -53,7 +56,10 @@ void GridQ2::setETensor(double E, double nu_) {
     Eyoung = E;
     nu = nu_;
     element_stiffness_q2(E, nu, h, K0.data());
-    for (int t = 0; t < 6561; ++t) K0f[t] = (float)K0[t];
+    for (int t = 0; t < 6561; ++t) {
+        K0f[t] = (float)K0[t];
+        K0lo[t] = (float)(K0[t] - (double)K0f[t]);
+    }
     VFEM_CUDA(cudaMemcpy(K0d.p, K0.data(), 6561 * sizeof(double), cudaMemcpyHostToDevice));
 }
 
@@ -69,6 +75,17 @@ void GridQ2::setParams(double E0_, double Emin_, double gamma_, double q_, int l
 void GridQ2::updateYoungModuli() {
     launch_young_moduli<double>(egeom, rho.p, Y.p, E0, Emin, gamma, q, law, false, stream);
     launch_cast<float, double>(Y.p, Yf.p, NE, stream);
+    launch_split_df(Y.p, Yhi.p, Ylo.p, NE, stream);
+}
+
+// out = K u in double-float arithmetic (FP64-class result, no FP64 arithmetic in the sums)
+void GridQ2::applyDF(const double *u, double *out, bool zeroDirichlet, cudaStream_t st) {
+    uhi.alloc(3 * NN);
+    ulo.alloc(3 * NN);
+    launch_split_df(u, uhi.p, ulo.p, 3 * NN, st);
+    q2_upload_k0f(K0f.data(), st);  // constant memory is shared by every Q2 grid
+    q2_upload_k0lo(K0lo.data(), st);
+    launch_applyk_q2_df(ne, Yhi.p, Ylo.p, uhi.p, ulo.p, out, dmask.p, zeroDirichlet, st);
 }
 
 void GridQ2::setDensities(const double *r) {
@@ -165,6 +182,7 @@ void GridQ2::applyK(const double *u, double *out, int precision, bool zeroDirich
     viewIn(vu, u, 3 * NN * sizeof(double), stream);
     viewOut(vo, out, 3 * NN * sizeof(double));
     if (precision == PREC_FP64) applyKT<double>((const double *)vu.d, (double *)vo.d, zeroDirichlet);
+    else if (precision == 2) applyDF((const double *)vu.d, (double *)vo.d, zeroDirichlet, stream);
     else applyKT<float>((const double *)vu.d, (double *)vo.d, zeroDirichlet);
     finishOut(vo, stream);
 }
@@ -182,6 +200,24 @@ void GridQ2::smooth(double *u, const double *b, bool forward, int precision) {
 // s * (6 NN + NE) (read u, write K u, read E).
 double GridQ2::timeApplyK(int precision, int reps, double *bytes) {
     if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
+    if (precision == 2) {
+        auto &D = work<double>();
+        launch_fill<double>(D.x.p, 0.5, 3 * NN, stream);
+        applyDF(D.x.p, D.r.p, false, stream);
+        cudaEvent_t e0, e1;
+        VFEM_CUDA(cudaEventCreate(&e0));
+        VFEM_CUDA(cudaEventCreate(&e1));
+        VFEM_CUDA(cudaEventRecord(e0, stream));
+        for (int r = 0; r < reps; ++r) launch_applyk_q2_df(ne, Yhi.p, Ylo.p, uhi.p, ulo.p, D.r.p, dmask.p, false, stream);
+        VFEM_CUDA(cudaEventRecord(e1, stream));
+        VFEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        VFEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *bytes = 8.0 * (6.0 * NN + NE);
+        return (double)ms / reps;
+    }
     auto run = [&](auto tag) {
         using T = decltype(tag);
         auto &D = work<T>();
@@ -279,7 +315,8 @@ PcgStats GridQ2::pcg(double *x, const double *b, int64_t maxIter, double tol, in
     const double *B = (const double *)vb.d;
     launch_masked_dot_partials<double, double>(gq, B, B, cgPart.p, st);
     launch_finalize(cgPart.p, REDUCE_BLOCKS, cgSc.p + 7, st);
-    launch_applyk_q2<double>(ne, K0d.p, Y.p, cgX.p, cgAd.p, dmask.p, true, st);
+    if (outerDF) applyDF(cgX.p, cgAd.p, true, st);
+    else launch_applyk_q2<double>(ne, K0d.p, Y.p, cgX.p, cgAd.p, dmask.p, true, st);
     launch_q2_residual_combine<double>(NN, B, cgAd.p, cgR.p, dmask.p, st);
     launch_masked_dot_partials<double, double>(gq, cgR.p, cgR.p, cgPart.p, st);
     launch_finalize(cgPart.p, REDUCE_BLOCKS, cgSc.p + 5, st);
@@ -297,7 +334,8 @@ PcgStats GridQ2::pcg(double *x, const double *b, int64_t maxIter, double tol, in
         launch_cg_precond_out<float>(gq, work<float>().x.p, cgS.p, cgR.p, dmask.p, cgPart.p, st);
         launch_cg_beta(cgPart.p, REDUCE_BLOCKS, cgSc.p, st);
         launch_cg_direction(gq, cgS.p, cgD.p, cgSc.p, nullptr, nullptr, st);
-        launch_applyk_q2<double>(ne, K0d.p, Y.p, cgD.p, cgAd.p, dmask.p, true, st);
+        if (outerDF) applyDF(cgD.p, cgAd.p, true, st);
+        else launch_applyk_q2<double>(ne, K0d.p, Y.p, cgD.p, cgAd.p, dmask.p, true, st);
         launch_masked_dot_partials<double, double>(gq, cgD.p, cgAd.p, cgPart.p, st);
         launch_cg_alpha(cgPart.p, REDUCE_BLOCKS, cgSc.p, st);
         launch_cg_update(gq, cgX.p, cgR.p, cgD.p, cgAd.p, cgSc.p, cgPart.p, st);

@@ -969,7 +969,7 @@ class TensorProductSimulator_3D_Q2:
     def applyK(self, u, precision="fp64", zeroDirichlet=False):
         u = _as_vfield(u, self._nn)
         out = _new_vfield(self._nn)
-        p = {"fp64": 0, "fp32": 1}[precision]
+        p = {"fp64": 0, "fp32": 1, "df": 2}[precision]
         check(_lib().vfem_q2_apply_k(self._h, ptr(u), ptr(out), p, int(bool(zeroDirichlet))))
         return out
 
@@ -993,6 +993,10 @@ class _Q2MultigridSolver:
         self.tps = tps
         self.coarsenings = numCoarseningLevels
         self.lastStats = None
+
+    def setOuterMatvec(self, outerMatvec="df"):
+        """CG matvec in 'df' (double-float, default) or 'fp64'."""
+        check(_lib().vfem_q2_set_outer_matvec(self.tps._h, {"fp64": 0, "df": 1}[outerMatvec]))
 
     def preconditionedConjugateGradient(self, u, b, maxIter, tol, it_callback=None, mgIterations=1,
                                         mgSmoothingIterations=1, fullMultigrid=False):
