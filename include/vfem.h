@@ -108,10 +108,10 @@ int vfem_grid_apply_k(vfem_grid *g, const double *u, double *out);
 int vfem_grid_build_load(vfem_grid *g, double *out);
 /* complianceGradient(u) (TensorProductSimulator.hh:973-1005) */
 int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_out);
-/* Layer-by-layer evaluation (LayerByLayerEvaluator, LayerByLayer.hh:223-296) with zero initial
- * guesses. vfem_lbl_create clones g into `slots` persistent solver instances (numCoarseningLevels
- * = coarsenings; precision 0 = FP64, 1 = mixed FP32 V-cycle with double-float outer matvec) that
- * run concurrently, each on its own stream (1 slot = one height at a time). vfem_lbl_run takes
+/* Layer-by-layer evaluation (LayerByLayerEvaluator, LayerByLayer.hh:223-296). vfem_lbl_create
+ * clones g into `slots` persistent solver instances (numCoarseningLevels = coarsenings;
+ * precision 0 = FP64, 1 = mixed FP32 V-cycle with FP64-class outer matvec) that run
+ * concurrently, each on its own stream; the initial guesses follow vfem_lbl_set_init. vfem_lbl_run takes
  * g's current densities, material and loads (its supports must be unchanged) and, for each
  * t < count, solves the grid masked to layers[t] element layers (1..ny): compliance_out[t] = f.u
  * over the nondetached nodes, iterations_out[t] (may be NULL) the PCG iterations,
@@ -120,9 +120,16 @@ int vfem_grid_compliance_gradient(vfem_grid *g, const double *u, double *grad_ou
 typedef struct vfem_lbl vfem_lbl;
 int vfem_lbl_create(vfem_grid *g, int64_t coarsenings, int64_t slots, int precision, vfem_lbl **out);
 int vfem_lbl_destroy(vfem_lbl *e);
+/* Initial guesses (LayerByLayerEvaluator::selectInitMethod, LayerByLayer.hh:253-259): kind 0 "zero",
+ * 1 "constant", 2 "fd", 3 "N=<history>" (subspace of the last `history` solutions, 1..8; the
+ * default, N=3). With a warm-start kind the heights are solved as min(slots, count) contiguous
+ * chains, each in order on one slot (one slot: the reference's sequential algorithm); with
+ * "zero" the heights are independent and spread over the slots. */
+int vfem_lbl_set_init(vfem_lbl *e, int kind, int history);
+/* zero_init 0: the full-design height starts from the previous run's full-design solution */
 int vfem_lbl_run(vfem_lbl *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
-                 int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, double *compliance_out,
-                 int64_t *iterations_out, double *gradient_sum_out);
+                 int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, int zero_init,
+                 double *compliance_out, int64_t *iterations_out, double *gradient_sum_out);
 
 /* Adjoint-method sensitivity (no reference counterpart; generalises complianceGradient,
  * TensorProductSimulator.hh:973-1005): grad_e = load_weight * lambda^T df/drho_e

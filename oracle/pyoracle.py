@@ -462,3 +462,70 @@ def q2_restrict(ne_fine, fine):
     lib().ovf_q2_restrict(_ne(ne_fine), _dp(f), _dp(out))
     return out
 
+
+
+def _lbl_init(method):
+    if method == "zero":
+        return "zero", 0
+    if method == "constant":
+        return "fd", 1
+    if method == "fd":
+        return "fd", 2
+    if isinstance(method, str) and method.startswith("N="):
+        return "subspace", int(method[2:])
+    raise RuntimeError("Unrecognized method " + str(method))
+
+
+def layer_by_layer(sim, mg, method="N=3", zero_init=True, layer_increment=1, max_iter=500, tol=1e-8,
+                   mg_iterations=1, mg_smoothing_iterations=1, fmg=False, u_full=None):
+    """Restatement of LayerByLayerEvaluator::run (LayerByLayer.hh:223-296) with its initial-guess
+    generators (LayerByLayer.hh:55-209): heights ny, ny - inc, ..., each solved from a guess built
+    from the previous heights' solutions (newest first, at most N kept; pushed after every height
+    but the last). "fd": 0, u(0) or 2 u(0) - u(1); "constant": u(0); "N=<s>": the Galerkin
+    projection onto the last s solutions, A_ij = u_i . K u_j, b_i = u_i . f for the NEW mask
+    (formed directly: the reference maintains the same quantities by recurrences,
+    LayerByLayer.hh:162-204), c = JacobiSVD(A).solve(b), i.e. the minimum-norm least-squares
+    solution with singular values <= s eps sigma_max dropped. Guesses are zero on detached nodes.
+    Returns (layers, compliances f.u over nondetached nodes, PCG iterations, gradient sum,
+    full-design solution)."""
+    kind, nmax = _lbl_init(method)
+    ne = sim.ne
+    ny = ne[1]
+    nn1 = (ne[1] + 1, ne[2] + 1)
+    jrow = (np.arange(sim.nn) // nn1[1]) % nn1[0]
+    hist = []
+    layers, comps, iters = [], [], []
+    grad = np.zeros(sim.numElements)
+    l = ny
+    while l > 0:
+        sim.setFabricationMaskHeightByLayer(l)
+        mg.setFabricationMaskHeightByLayer(l)
+        live = jrow <= l  # nondetached node rows
+        f = sim.buildLoadVector()
+        s = len(hist)
+        if not zero_init and l == ny and u_full is not None:
+            g = u_full.copy()
+        elif kind == "zero" or s == 0:
+            g = np.zeros((sim.nn, 3))
+        elif kind == "fd":
+            g = hist[0].copy() if s == 1 else 2.0 * hist[0] - hist[1]
+        else:
+            Ku = [sim.applyK(u) for u in hist]
+            A = np.array([[float(np.sum((hist[i] * Ku[j])[live])) for j in range(s)] for i in range(s)])
+            A = 0.5 * (A + A.T)
+            b = np.array([float(np.sum((hist[i] * f)[live])) for i in range(s)])
+            c = np.linalg.lstsq(A, b, rcond=s * np.finfo(np.float64).eps)[0]
+            g = sum(c[i] * hist[i] for i in range(s))
+        g[~live] = 0.0
+        u = mg.preconditionedConjugateGradient(g, f, max_iter, tol, None, mg_iterations, mg_smoothing_iterations, fmg)
+        layers.append(l)
+        comps.append(float(np.sum((f * u)[live])))
+        iters.append(mg.lastIterations)
+        grad += sim.complianceGradient(u)
+        if l == ny:
+            u_full = u.copy()
+        if l >= layer_increment and nmax > 0:
+            hist.insert(0, u.copy())
+            del hist[nmax:]
+        l -= min(layer_increment, l)
+    return np.array(layers), np.array(comps), np.array(iters), grad, u_full

@@ -1,8 +1,10 @@
-"""Layer-by-layer evaluation (LayerByLayerEvaluator) against per-height oracle solves, and the
-concurrent-slot schedule against one-at-a-time: per-height compliance to 1e-8, the same PCG
-iteration counts, the averaged gradient to 1e-6 (FP64), bit-identical compliances for any
-slot count (the gradient sum differs only in its summation order), and mixed precision within
-1e-6 of FP64."""
+"""Layer-by-layer evaluation (LayerByLayerEvaluator) against the oracle. Zero guesses: per-height
+oracle solves and the concurrent-slot schedule against one-at-a-time: per-height compliance to
+1e-8, the same PCG iteration counts, the averaged gradient to 1e-6 (FP64), bit-identical
+compliances for any slot count (the gradient sum differs only in its summation order), and
+mixed precision within 1e-6 of FP64. Warm starts ("N=3", "fd", "constant"): one chain follows
+the oracle's sequential restatement with the same iteration count at every height; several
+chains converge to the same compliances; zeroInit=False restarts from the full-design solution."""
 import numpy as np
 import pytest
 
@@ -61,6 +63,7 @@ def test_lbl_matches_oracle_and_slot_schedules_agree(gpu, oracle):
     runs = {}
     for slots in (1, 3):
         ev = pv.LayerByLayerEvaluator(sim)
+        ev.selectInitMethod("zero")
         ev.run(mg, True, INC, 500, TOL, mgIterations=1, mgSmoothingIterations=2, slots=slots)
         runs[slots] = ev
     ev1, ev3 = runs[1], runs[3]
@@ -84,9 +87,11 @@ def test_lbl_mixed_precision(gpu, oracle):
     sim, rho = _gpu_sim()
     mg = sim.multigridSolver(LEVELS - 1)
     ev64 = pv.LayerByLayerEvaluator(sim)
+    ev64.selectInitMethod("zero")
     ev64.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=4)
     mg.setPrecision("mixed")
     evm = pv.LayerByLayerEvaluator(sim)
+    evm.selectInitMethod("zero")
     evm.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=4)
     assert np.max(np.abs(evm.compliances - ev64.compliances) / np.abs(ev64.compliances)) < 1e-6
     assert np.max(np.abs(evm.gradient() - ev64.gradient())) / np.max(np.abs(ev64.gradient())) < 1e-5
@@ -111,3 +116,44 @@ def test_graphs_survive_mask_changes(gpu, oracle):
         uo = om.preconditionedConjugateGradient(np.zeros_like(fo), fo, 500, TOL, None, 1, 2, False)
         assert mg.lastStats.iterations == om.lastIterations, lay
         assert np.max(np.abs(u - uo)) / np.max(np.abs(uo)) < 1e-8, lay
+
+
+@pytest.mark.parametrize("method", ["N=3", "fd", "constant", "N=1"])
+def test_lbl_warm_start_matches_sequential_oracle(gpu, oracle, method):
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    ev = pv.LayerByLayerEvaluator(sim)
+    ev.selectInitMethod(method)
+    ev.run(mg, True, INC, 500, TOL, mgIterations=1, mgSmoothingIterations=2)
+    o = oracle.Sim(NE)
+    _configure(o, rho)
+    om = oracle.MG(o, LEVELS - 1)
+    lay, comp, its, grad, _ = oracle.layer_by_layer(o, om, method, True, INC, 500, TOL, 1, 2, False)
+    np.testing.assert_array_equal(ev.layers, lay)
+    np.testing.assert_array_equal(ev.iterations, its)
+    assert np.max(np.abs(ev.compliances - comp) / np.abs(comp)) < 1e-8
+    g = grad / len(comp)
+    assert np.max(np.abs(ev.gradient() - g)) / np.max(np.abs(g)) < 1e-6
+    if method == "N=3":
+        # warm starts save iterations against zero guesses
+        ez = pv.LayerByLayerEvaluator(sim)
+        ez.selectInitMethod("zero")
+        ez.run(mg, True, INC, 500, TOL, mgIterations=1, mgSmoothingIterations=2)
+        assert ev.iterations.sum() < ez.iterations.sum()
+
+
+def test_lbl_warm_chains_and_restart(gpu, oracle):
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    ev1 = pv.LayerByLayerEvaluator(sim)
+    ev1.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=1)
+    ev3 = pv.LayerByLayerEvaluator(sim)
+    ev3.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2, slots=3)
+    assert np.max(np.abs(ev3.compliances - ev1.compliances) / np.abs(ev1.compliances)) < 1e-8
+    # a chain head starts from zero: with 3 chains of 2 heights, heights 0, 2, 4 match the
+    # zero-guess iteration counts of a single chain's first height pattern
+    assert ev3.iterations[0] == ev1.iterations[0]
+    # restart from the previous run's full-design solution
+    ev1.run(mg, False, INC, 500, TOL, mgSmoothingIterations=2, slots=1)
+    assert ev1.iterations[0] == 0
+    assert np.max(np.abs(ev3.compliances - ev1.compliances) / np.abs(ev1.compliances)) < 1e-8

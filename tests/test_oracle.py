@@ -266,3 +266,32 @@ def test_masked_layers_semantics(oracle):
     Ku = s.applyK(u).reshape(ne[0] + 1, ne[1] + 1, ne[2] + 1, 3, order="F")
     # nodes above the first detached layer (y >= 4) are not visited and read back as zero
     assert np.all(Ku[:, 4:, :, :] == 0)
+
+
+def test_oracle_layer_by_layer_warm_starts():
+    """The oracle's sequential layer-by-layer restatement: warm-started heights converge to the
+    zero-guess compliances with fewer iterations; N=1 equals the scaled previous solution."""
+    from oracle import pyoracle as po
+    ne = (8, 8, 4)
+    rho = np.random.default_rng(3).uniform(0.3, 1.0, int(np.prod(ne)))
+
+    def make():
+        s = po.Sim(ne)
+        s.setMaterial(1.0, 0.3)
+        s.setParams(E0=1.0, Emin=1e-9, gamma=3.0)
+        s.setGravity([0.0, -1.0, 0.0])
+        s.addDirichletCondition([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [float(ne[0]), 0.0, float(ne[2])], "xyz")
+        s.setDensities(rho)
+        return s, po.MG(s, 2)
+
+    res = {}
+    for method in ("zero", "N=3", "fd"):
+        s, m = make()
+        res[method] = po.layer_by_layer(s, m, method, True, 2, 500, 1e-10, 1, 2, False)
+    lz, cz, iz, gz, _ = res["zero"]
+    for method in ("N=3", "fd"):
+        l, c, i, g, _ = res[method]
+        np.testing.assert_array_equal(l, lz)
+        assert np.max(np.abs(c - cz) / np.abs(cz)) < 1e-8
+        assert np.max(np.abs(g - gz)) / np.max(np.abs(gz)) < 1e-6
+    assert res["N=3"][2].sum() < iz.sum()

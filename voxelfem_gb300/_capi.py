@@ -78,8 +78,9 @@ _SIGS = {
     "vfem_mg_outer_apply": (C.c_int, [_vp, _vp, _vp, _vp]),
     "vfem_tc_fit_k0": (C.c_int, [_vp, C.POINTER(C.c_double), _vp, C.POINTER(C.c_int)]),
     "vfem_lbl_destroy": (C.c_int, [_vp]),
-    "vfem_lbl_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, _vp, _vp,
-                               _vp]),
+    "vfem_lbl_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                               _vp, _vp, _vp]),
+    "vfem_lbl_set_init": (C.c_int, [_vp, C.c_int, C.c_int]),
     "vfem_grid_element_energy": (C.c_int, [_vp, _vp, _vp]),
     "vfem_mg_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "vfem_mg_destroy": (C.c_int, [_vp]),

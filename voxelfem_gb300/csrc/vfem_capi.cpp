@@ -167,15 +167,21 @@ int vfem_lbl_create(vfem_grid *g, int64_t coarsenings, int64_t slots, int precis
 int vfem_lbl_destroy(vfem_lbl *e) {
     return guarded([&] { delete e; });
 }
+int vfem_lbl_set_init(vfem_lbl *e, int kind, int history) {
+    return guarded([&] {
+        need(e, "evaluator");
+        e->e.setInit(kind, history);
+    });
+}
 int vfem_lbl_run(vfem_lbl *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
-                 int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, double *compliance_out,
-                 int64_t *iterations_out, double *gradient_sum_out) {
+                 int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, int zero_init,
+                 double *compliance_out, int64_t *iterations_out, double *gradient_sum_out) {
     return guarded([&] {
         need(e, "evaluator");
         need(layers, "layers");
         need(compliance_out, "compliance_out");
         e->e.run(layers, count, max_iter, tol, mg_iterations, mg_smoothing_iterations, full_multigrid != 0,
-                 compliance_out, iterations_out, gradient_sum_out);
+                 zero_init != 0, compliance_out, iterations_out, gradient_sum_out);
     });
 }
 int vfem_grid_adjoint_sensitivity(vfem_grid *g, const double *lambda, const double *u, double load_weight,

@@ -399,29 +399,50 @@ void q2Interpolate(const int neFine[3], const double *coarse, double *fine, bool
 
 // Layer-by-layer solves of partial-build heights (layers[t] element layers built) over
 // persistent concurrent solver instances cloned from `src` (vfem_lbl.cpp).
+// Initial guesses of the layer-by-layer solves (LayerByLayer.hh:55-209 generators)
+enum LblInit { LBL_INIT_ZERO = 0, LBL_INIT_CONSTANT = 1, LBL_INIT_FD = 2, LBL_INIT_SUBSPACE = 3 };
+
 class LBL {
 public:
     LBL(Grid *src, int coarsenings, int64_t slots, int precision);
     ~LBL();
     LBL(const LBL &) = delete;
     LBL &operator=(const LBL &) = delete;
+    // kind LblInit; history: the subspace size N of "N=<N>" (LBL_INIT_SUBSPACE)
+    void setInit(int kind, int history);
+    // Heights layers[0..count) in the given order (the reference runs them from the full design
+    // down). Zero guesses: every height is independent and the heights are spread over the
+    // slots. Warm starts: the heights are cut into min(slots, count) contiguous chains, each
+    // solved in order on its slot with the generator's history of that chain (one slot: the
+    // reference's sequential algorithm). zeroInit false: the full-design height starts from
+    // the previous run's full-design solution.
     void run(const int64_t *layers, int64_t count, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
-             bool fmg, double *compliance, int64_t *iterations, double *gradSum);
+             bool fmg, bool zeroInit, double *compliance, int64_t *iterations, double *gradSum);
     Grid *src;
     int coarsenings, precision;
+    int initKind = LBL_INIT_SUBSPACE, historySize = 3;
 
 private:
     struct Slot {
         std::unique_ptr<Grid> grid;
         std::unique_ptr<MG> mg;
         DevBuf<double> x, f, gtmp, gacc, cpl;
+        DevBuf<double> hist[LBL_MAX_HISTORY], Ku[LBL_MAX_HISTORY], subPart, subC;
+        int order[LBL_MAX_HISTORY] = {0};  // hist buffer of the i-th most recent solution
+        int hs = 0;                        // history size
+        std::vector<int64_t> queue;        // indices into layers, in solve order
+        size_t qpos = 0;
         cudaEvent_t done = nullptr;
         int64_t idx = -1;
         ~Slot();
     };
     std::vector<std::unique_ptr<Slot>> S;
     double *cplHost = nullptr;
+    DevBuf<double> uFull;  // full-design solution of the last run
+    bool haveFull = false;
     void syncSource();
+    void guess(Slot &sl, int64_t layer, int ny, bool zeroInit);
+    void pushHistory(Slot &sl);
 };
 
 }  // namespace vfem

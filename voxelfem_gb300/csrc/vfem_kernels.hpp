@@ -204,6 +204,20 @@ void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double
 void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
                          cudaStream_t st, double *amax = nullptr);
 
+// ---------------- warm starts of the layer-by-layer evaluation (k_lbl.cu) ----------------
+constexpr int LBL_MAX_HISTORY = 8;
+struct LblVectors {
+    const double *u[LBL_MAX_HISTORY];
+};
+struct LblCoeffs {
+    double c[LBL_MAX_HISTORY];
+};
+// c = pinv(A) b from the dot partials (pairs i <= j of u_i . K u_j, then u_i . f; nb each)
+void launch_subspace_solve(const double *partials, int nb, int s, double *c, cudaStream_t st);
+// x = sum_i c_i u_i on nondetached nodes (c from cDev if given, else cv), zero elsewhere
+void launch_subspace_combine(const Geom &g, const LblVectors &U, int s, const double *cDev, const LblCoeffs &cv,
+                             double *x, cudaStream_t st);
+
 // ---------------- tensor-core outer matvec (k_tc.cu) ----------------
 // K0 = scale * C with C an integer matrix whose row sums keep the bf16 MMA accumulators exact;
 // fills the B tiles (2048 bf16). False when K0 has no such form.

@@ -1039,10 +1039,13 @@ class LayerByLayerEvaluator:
     height, averaged, with its gradient.
 
     ``run(solver, zeroInit, layerIncrement, maxIter, tol, ...)`` visits the heights
-    ny, ny - layerIncrement, ..., > 0 like the reference. Every height starts from a zero initial
-    guess (the reference's ``"zero"`` initialisation); the solves are independent and run
-    ``slots`` at a time on concurrent solver instances (``slots=1``: one at a time). ``solver``
-    supplies the number of coarsening levels and the precision.
+    ny, ny - layerIncrement, ..., > 0 like the reference. ``selectInitMethod`` chooses the
+    initial guesses as the reference does: ``"N=3"`` (default; Galerkin projection onto the last
+    3 solutions), ``"N=<k>"``, ``"fd"``, ``"constant"`` or ``"zero"``. Warm-started heights form
+    chains: ``slots`` (default 1, the reference's sequential algorithm) contiguous runs of
+    heights solved concurrently, each in order. With ``"zero"`` every height is independent
+    and the solves run ``slots`` (default 8) at a time. ``solver`` supplies the number of
+    coarsening levels and the precision.
     """
 
     def __init__(self, lblSim):
@@ -1051,7 +1054,7 @@ class LayerByLayerEvaluator:
         self.compliances = np.zeros(0)
         self.iterations = np.zeros(0, dtype=np.int64)
         self._grad = np.zeros(lblSim.numElements())
-        self.initMethod = "zero"
+        self.initMethod = "N=3"
         self._h = None
         self._key = None
 
@@ -1076,12 +1079,25 @@ class LayerByLayerEvaluator:
         return self._h
 
     def selectInitMethod(self, method):
-        if method != "zero":
-            raise RuntimeError("Unrecognized method " + str(method) + " (independent batched solves use 'zero')")
+        self._init_kind(method)
         self.initMethod = method
 
+    @staticmethod
+    def _init_kind(method):
+        fixed = {"zero": (0, 0), "constant": (1, 1), "fd": (2, 2)}
+        if method in fixed:
+            return fixed[method]
+        if isinstance(method, str) and method.startswith("N="):
+            try:
+                n = int(method[2:])
+            except ValueError:
+                n = -1
+            if 1 <= n <= 8:
+                return 3, n
+        raise RuntimeError("Unrecognized method " + str(method))
+
     def run(self, solver, zeroInit=True, layerIncrement=1, maxIter=500, tol=1e-8, it_callback=None,
-            mgIterations=1, mgSmoothingIterations=1, fmg=False, verbose=False, lblCallback=None, slots=8):
+            mgIterations=1, mgSmoothingIterations=1, fmg=False, verbose=False, lblCallback=None, slots=None):
         if it_callback is not None:
             raise RuntimeError("per-iteration callbacks are not available for device-resident solves")
         ny = int(self.sim.NbElementsPerDimension[1])
@@ -1099,10 +1115,14 @@ class LayerByLayerEvaluator:
         self.iterations = np.zeros(n, dtype=np.int64)
         self._grad = np.zeros(self.sim.numElements())
         precision = 1 if getattr(solver, "_prec", "fp64") == "mixed" else 0
+        kind, hist = self._init_kind(self.initMethod)
+        if slots is None:
+            slots = 8 if kind == 0 else 1
         h = self._handle(int(solver.numLevels - 1), int(slots), precision)
+        check(_lib().vfem_lbl_set_init(h, kind, hist))
         check(_lib().vfem_lbl_run(h, ptr(self.layers), n, int(maxIter), float(tol), int(mgIterations),
-                                  int(mgSmoothingIterations), int(bool(fmg)), ptr(self.compliances),
-                                  ptr(self.iterations), ptr(self._grad)))
+                                  int(mgSmoothingIterations), int(bool(fmg)), int(bool(zeroInit)),
+                                  ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
         for t, lay in enumerate(layers):
             if verbose:
                 print("Layer %d: %g" % (lay, self.compliances[t]))
