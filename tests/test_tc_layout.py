@@ -1,5 +1,5 @@
 """Host side of the tensor-core outer matvec, without a GPU: the integer form of K0 and its
-bf16 B tiles (vfem_tc_fit_k0), the signed base-128 digit split of the fixed-point operand,
+bf16 B tiles (vfem_tc_fit_k0), the base-128 digit split of the fixed-point operand,
 and the operand addressing of the MMA descriptors (a digit table read in place, the second
 K chunk one node row after the first), checked by contracting one element tile on the CPU."""
 import ctypes as C
@@ -32,13 +32,8 @@ def k0(nu, h=(1.0, 1.0, 1.0)):
 
 
 def digits(F):
-    D = [0] * 8
-    for i in range(7, 0, -1):
-        d = ((F + 64) & 127) - 64
-        D[i] = d
-        F = (F - d) >> 7
-    D[0] = F
-    return D
+    """A signed top digit F >> 49 and seven unsigned 7-bit fields of the two's complement F."""
+    return [F >> 49] + [(F >> (7 * (7 - i))) & 127 for i in range(1, 8)]
 
 
 def test_integer_form_of_k0():
@@ -47,7 +42,7 @@ def test_integer_form_of_k0():
     assert ok
     C_ = np.rint(K / c)
     assert np.max(np.abs(K - c * C_)) <= 1e-13 * np.max(np.abs(K))
-    assert np.max(np.abs(C_).sum(1)) * 8256 < 2 ** 24  # FP32 accumulators stay exact
+    assert np.max(np.abs(C_).sum(1)) * 16383 < 2 ** 24  # FP32 accumulators stay exact
     assert not fit(k0(0.33))[0]                         # accumulator bound exceeded
     assert not fit(k0(0.3, (1.0, 1.5, 1.0)))[0]         # stretched voxels
 
@@ -57,9 +52,10 @@ def test_digit_split():
     for F in list(rng.integers(-2 ** 55, 2 ** 55, 2000)) + [2 ** 55, -2 ** 55, 0, 1, -1]:
         F = int(F)
         D = digits(F)
-        assert max(abs(d) for d in D) <= 64
+        assert -64 <= D[0] <= 64 and all(0 <= d <= 127 for d in D[1:])
         assert sum(d * 128 ** (7 - i) for i, d in enumerate(D)) == F
         P = [128 * D[2 * a] + D[2 * a + 1] for a in range(4)]
+        assert -8192 <= P[0] <= 8319 and all(0 <= p <= 16383 for p in P[1:])
         assert sum(p * 2 ** (14 * (3 - a)) for a, p in enumerate(P)) == F
 
 
@@ -71,7 +67,7 @@ def test_descriptor_addressing_contracts_elements():
     C_ = np.rint(K / c)
     rng = np.random.default_rng(1)
     # one digit pair per node component: table rows (z-major, y fastest), 8 values per row
-    planes = [rng.integers(-8256, 8257, (NPZ * NPY, 3)).astype(np.float64) for _ in range(2)]
+    planes = [rng.integers(-8192, 16384, (NPZ * NPY, 3)).astype(np.float64) for _ in range(2)]
     tabs = []
     for P in planes:
         t = np.zeros(NPZ * NPY * 8)

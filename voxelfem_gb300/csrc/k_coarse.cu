@@ -27,6 +27,7 @@ constexpr int WPB = BS / 32;  // warps (rows) per block
 template <typename T, bool ZeroInit, bool Negate>
 __global__ void __launch_bounds__(BS) stencil_apply_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u,
                                                            T *__restrict__ out) {
+    VFEM_PDL_ENTRY();
     const int lane = threadIdx.x & 31;
     const int64_t n = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n >= g.NN) return;
@@ -47,6 +48,7 @@ template <typename T>
 __global__ void __launch_bounds__(BS) stencil_residual_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u,
                                                               const T *__restrict__ b, T *__restrict__ r,
                                                               const uint8_t *__restrict__ dmask) {
+    VFEM_PDL_ENTRY();
     const int lane = threadIdx.x & 31;
     const int64_t n = blockIdx.x * (int64_t)WPB + (threadIdx.x >> 5);
     if (n >= g.NN) return;
@@ -62,6 +64,7 @@ __global__ void __launch_bounds__(BS) gs_stencil_color_kernel(Geom g, const T *_
                                                               const T *__restrict__ b,
                                                               const uint8_t *__restrict__ dmask, int cx, int cy,
                                                               int cz, int forward) {
+    VFEM_PDL_ENTRY();
     // colour nodes over the full grid; detached rows (j >= nyv) are skipped
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int lane = threadIdx.x & 31;
@@ -100,6 +103,7 @@ __device__ __forceinline__ void split_rows(const Geom &g, const T *__restrict__ 
 template <typename T, bool ZeroInit, bool Negate>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     stencil_apply_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, T *__restrict__ out) {
+    VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
@@ -130,6 +134,7 @@ template <typename T>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     stencil_residual_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, const T *__restrict__ b,
                                 T *__restrict__ r, const uint8_t *__restrict__ dmask) {
+    VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
     const int64_t p = blockIdx.x * (int64_t)SPLIT_NODES + lane;
@@ -161,6 +166,7 @@ template <typename T>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
                                 const uint8_t *__restrict__ dmask, int cx, int cy, int cz, int forward) {
+    VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     // colour nodes over the full grid; detached rows (j >= nyv) are skipped
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
@@ -210,6 +216,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
 template <typename T>
 __global__ void __launch_bounds__(BS) restrict_kernel(Geom gf, Geom gc, const T *__restrict__ fine,
                                                       T *__restrict__ coarse) {
+    VFEM_PDL_ENTRY();
     const int cyv = gc.nyv();
     const int rows = cyv < gc.nn[1] ? cyv + 1 : cyv;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
@@ -224,6 +231,7 @@ __global__ void __launch_bounds__(BS) restrict_kernel(Geom gf, Geom gc, const T 
 template <typename T, bool Accumulate>
 __global__ void __launch_bounds__(BS) interp_kernel(Geom gf, Geom gc, const T *__restrict__ coarse,
                                                     T *__restrict__ fine) {
+    VFEM_PDL_ENTRY();
     const int rows = Accumulate ? gf.nyv() : gf.nn[1];
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= gf.NN) return;
@@ -235,6 +243,7 @@ __global__ void __launch_bounds__(BS) interp_kernel(Geom gf, Geom gc, const T *_
 
 template <typename T>
 __global__ void zero_dirichlet_kernel(Geom g, T *__restrict__ u, const uint8_t *__restrict__ dmask) {
+    VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     const uint8_t dm = dmask[n];
@@ -246,6 +255,7 @@ __global__ void zero_dirichlet_kernel(Geom g, T *__restrict__ u, const uint8_t *
 
 template <typename T>
 __global__ void masked_zero_kernel(Geom g, T *__restrict__ u, int margin) {
+    VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= g.NN) return;
     int i, j, k;
@@ -259,12 +269,14 @@ __global__ void masked_zero_kernel(Geom g, T *__restrict__ u, int margin) {
 
 template <typename T>
 __global__ void fill_kernel(T *__restrict__ p, T v, int64_t n) {
+    VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t < n) p[t] = v;
 }
 
 template <typename Tdst, typename Tsrc>
 __global__ void cast_kernel(const Tsrc *__restrict__ s, Tdst *__restrict__ d, int64_t n) {
+    VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t < n) d[t] = (Tdst)s[t];
 }
@@ -542,22 +554,22 @@ void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool ze
     if (!rows) {
         const unsigned gs = gridFor(g.NN, SPLIT_NODES);
         if (zeroInit) {
-            if (negate) stencil_apply_soa_kernel<T, true, true><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
-            else stencil_apply_soa_kernel<T, true, false><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
+            if (negate) launch_pdl(stencil_apply_soa_kernel<T, true, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_soa_kernel<T, true, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
         } else {
-            if (negate) stencil_apply_soa_kernel<T, false, true><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
-            else stencil_apply_soa_kernel<T, false, false><<<gs, SPLIT_BS, 0, st>>>(g, S, u, out);
+            if (negate) launch_pdl(stencil_apply_soa_kernel<T, false, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_soa_kernel<T, false, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
         }
         VFEM_LAUNCH_CHECK();
         return;
     }
     const unsigned grid = gridFor(g.NN, WPB);
     if (zeroInit) {
-        if (negate) stencil_apply_kernel<T, true, true><<<grid, BS, 0, st>>>(g, S, u, out);
-        else stencil_apply_kernel<T, true, false><<<grid, BS, 0, st>>>(g, S, u, out);
+        if (negate) launch_pdl(stencil_apply_kernel<T, true, true>, grid, BS, 0, st, g, S, u, out);
+        else launch_pdl(stencil_apply_kernel<T, true, false>, grid, BS, 0, st, g, S, u, out);
     } else {
-        if (negate) stencil_apply_kernel<T, false, true><<<grid, BS, 0, st>>>(g, S, u, out);
-        else stencil_apply_kernel<T, false, false><<<grid, BS, 0, st>>>(g, S, u, out);
+        if (negate) launch_pdl(stencil_apply_kernel<T, false, true>, grid, BS, 0, st, g, S, u, out);
+        else launch_pdl(stencil_apply_kernel<T, false, false>, grid, BS, 0, st, g, S, u, out);
     }
     VFEM_LAUNCH_CHECK();
 }
@@ -565,8 +577,8 @@ void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool ze
 template <typename T>
 void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st) {
-    if (rows) stencil_residual_kernel<T><<<gridFor(g.NN, WPB), BS, 0, st>>>(g, S, u, b, r, dmask);
-    else stencil_residual_soa_kernel<T><<<gridFor(g.NN, SPLIT_NODES), SPLIT_BS, 0, st>>>(g, S, u, b, r, dmask);
+    if (rows) launch_pdl(stencil_residual_kernel<T>, gridFor(g.NN, WPB), BS, 0, st, g, S, u, b, r, dmask);
+    else launch_pdl(stencil_residual_soa_kernel<T>, gridFor(g.NN, SPLIT_NODES), SPLIT_BS, 0, st, g, S, u, b, r, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -577,51 +589,51 @@ void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const 
     const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
     if (rows)
-        gs_stencil_color_kernel<T><<<gridFor(n0 * n1 * n2, WPB), BS, 0, st>>>(g, S, u, b, dmask, cx, cy, cz,
+        launch_pdl(gs_stencil_color_kernel<T>, gridFor(n0 * n1 * n2, WPB), BS, 0, st, g, S, u, b, dmask, cx, cy, cz,
                                                                                forward ? 1 : 0);
     else
-        gs_stencil_color_soa_kernel<T><<<gridFor(n0 * n1 * n2, SPLIT_NODES), SPLIT_BS, 0, st>>>(
+        launch_pdl(gs_stencil_color_soa_kernel<T>, gridFor(n0 * n1 * n2, SPLIT_NODES), SPLIT_BS, 0, st, 
             g, S, u, b, dmask, cx, cy, cz, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st) {
-    restrict_kernel<T><<<gridFor(gc.NN, BS), BS, 0, st>>>(gf, gc, fine, coarse);
+    launch_pdl(restrict_kernel<T>, gridFor(gc.NN, BS), BS, 0, st, gf, gc, fine, coarse);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_interpolate(const Geom &gf, const Geom &gc, const T *coarse, T *fine, bool accumulate, cudaStream_t st) {
     const unsigned grid = gridFor(gf.NN, BS);
-    if (accumulate) interp_kernel<T, true><<<grid, BS, 0, st>>>(gf, gc, coarse, fine);
-    else interp_kernel<T, false><<<grid, BS, 0, st>>>(gf, gc, coarse, fine);
+    if (accumulate) launch_pdl(interp_kernel<T, true>, grid, BS, 0, st, gf, gc, coarse, fine);
+    else launch_pdl(interp_kernel<T, false>, grid, BS, 0, st, gf, gc, coarse, fine);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_zero_dirichlet(const Geom &g, T *u, const uint8_t *dmask, cudaStream_t st) {
-    zero_dirichlet_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, u, dmask);
+    launch_pdl(zero_dirichlet_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, u, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_masked_zero(const Geom &g, T *u, int margin, cudaStream_t st) {
-    masked_zero_kernel<T><<<gridFor(g.NN, BS), BS, 0, st>>>(g, u, margin);
+    launch_pdl(masked_zero_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, u, margin);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
 void launch_fill(T *p, T v, int64_t n, cudaStream_t st) {
     if (n <= 0) return;
-    fill_kernel<T><<<gridFor(n, BS), BS, 0, st>>>(p, v, n);
+    launch_pdl(fill_kernel<T>, gridFor(n, BS), BS, 0, st, p, v, n);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename Tdst, typename Tsrc>
 void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st) {
     if (n <= 0) return;
-    cast_kernel<Tdst, Tsrc><<<gridFor(n, BS), BS, 0, st>>>(src, dst, n);
+    launch_pdl(cast_kernel<Tdst, Tsrc>, gridFor(n, BS), BS, 0, st, src, dst, n);
     VFEM_LAUNCH_CHECK();
 }
 

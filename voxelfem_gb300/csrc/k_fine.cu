@@ -234,6 +234,7 @@ __global__ void __launch_bounds__(BS, 2) applyk_fine_kernel(Geom g, const T *__r
                                                          T *__restrict__ out, const uint8_t *__restrict__ dmask,
                                                          int zeroDir, double *__restrict__ partials,
                                                          const Mat24<T> K) {
+    VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     double dot = 0.0;
     if (n < g.NN) {
@@ -272,6 +273,7 @@ template <typename T, bool Cube>
 __global__ void __launch_bounds__(BS, 2) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
                                                            const T *__restrict__ b, T *__restrict__ r,
                                                            const uint8_t *__restrict__ dmask, const Mat24<T> K) {
+    VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     int i, j, k;
@@ -367,6 +369,7 @@ template <typename T, bool Cube>
 __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kernel(Geom g, const T *__restrict__ Y, T *u,
                                                            const T *__restrict__ b, const uint8_t *__restrict__ dmask,
                                                            int cx, int cy, int cz, int forward, const Mat24<T> K) {
+    VFEM_PDL_ENTRY();
     // colour nodes over the full grid; detached rows (j >= nyv) are skipped
     const int n2 = (g.nn[2] - cz + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
@@ -471,6 +474,7 @@ __global__ void __launch_bounds__(BS) applyk_fine_df_kernel(Geom g, const float 
                                                             const uint8_t *__restrict__ dmask, int zeroDir,
                                                             double *__restrict__ partials, int withDot,
                                                             const double *__restrict__ rhs, const Mat24DF K) {
+    VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     double dot = 0.0;
     if (n < g.NN) {
@@ -695,15 +699,15 @@ void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat
     auto go = [&](auto cube) {
         constexpr bool C = decltype(cube)::value;
         if (partialDot)
-            applyk_fine_kernel<T, true, false, true, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, partialDot, K0);
+            launch_pdl(applyk_fine_kernel<T, true, false, true, C>, grid, BS, 0, st, g, Y, u, out, dmask, zd, partialDot, K0);
         else if (zeroInit && negate)
-            applyk_fine_kernel<T, true, true, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+            launch_pdl(applyk_fine_kernel<T, true, true, false, C>, grid, BS, 0, st, g, Y, u, out, dmask, zd, nullptr, K0);
         else if (zeroInit)
-            applyk_fine_kernel<T, true, false, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+            launch_pdl(applyk_fine_kernel<T, true, false, false, C>, grid, BS, 0, st, g, Y, u, out, dmask, zd, nullptr, K0);
         else if (negate)
-            applyk_fine_kernel<T, false, true, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+            launch_pdl(applyk_fine_kernel<T, false, true, false, C>, grid, BS, 0, st, g, Y, u, out, dmask, zd, nullptr, K0);
         else
-            applyk_fine_kernel<T, false, false, false, C><<<grid, BS, 0, st>>>(g, Y, u, out, dmask, zd, nullptr, K0);
+            launch_pdl(applyk_fine_kernel<T, false, false, false, C>, grid, BS, 0, st, g, Y, u, out, dmask, zd, nullptr, K0);
     };
     if (sizeof(T) == 4 && K0.isCube) go(std::true_type{});
     else go(std::false_type{});
@@ -713,8 +717,8 @@ void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat
 template <typename T>
 void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
                           const uint8_t *dmask, cudaStream_t st) {
-    if (sizeof(T) == 4 && K0.isCube) residual_fine_kernel<T, true><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
-    else residual_fine_kernel<T, false><<<gridFor(g.NN, BS), BS, 0, st>>>(g, Y, u, b, r, dmask, K0);
+    if (sizeof(T) == 4 && K0.isCube) launch_pdl(residual_fine_kernel<T, true>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
+    else launch_pdl(residual_fine_kernel<T, false>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -725,10 +729,10 @@ void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uin
     const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
     if (sizeof(T) == 4 && K0.isCube)
-        gs_fine_color_kernel<T, true><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz,
+        launch_pdl(gs_fine_color_kernel<T, true>, gridFor(n0 * n1 * n2, BS), BS, 0, st, g, Y, u, b, dmask, cx, cy, cz,
                                                                                forward ? 1 : 0, K0);
     else
-        gs_fine_color_kernel<T, false><<<gridFor(n0 * n1 * n2, BS), BS, 0, st>>>(g, Y, u, b, dmask, cx, cy, cz,
+        launch_pdl(gs_fine_color_kernel<T, false>, gridFor(n0 * n1 * n2, BS), BS, 0, st, g, Y, u, b, dmask, cx, cy, cz,
                                                                                 forward ? 1 : 0, K0);
     VFEM_LAUNCH_CHECK();
 }
@@ -739,10 +743,10 @@ void launch_applyk_fine_df(const Geom &g, const float *Yh, const float *Yl, cons
     const unsigned grid = gridFor(g.NN, BS);
     if (partialDot && (int)grid > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
     if (K0.isCube)
-        applyk_fine_df_kernel<true><<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
+        launch_pdl(applyk_fine_df_kernel<true>, grid, BS, 0, st, g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
                                                          partialDot, partialDot ? 1 : 0, rhs, K0);
     else
-        applyk_fine_df_kernel<false><<<grid, BS, 0, st>>>(g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
+        launch_pdl(applyk_fine_df_kernel<false>, grid, BS, 0, st, g, Yh, Yl, uh, ul, u, out, dmask, zeroDirichlet ? 1 : 0,
                                                           partialDot, partialDot ? 1 : 0, rhs, K0);
     VFEM_LAUNCH_CHECK();
 }

@@ -245,6 +245,7 @@ __global__ void zero_upper_kernel(double *A, int n) {
 template <typename T>
 __global__ void gather_free_kernel(const Geom g, const int *__restrict__ freeIdx, const int *__restrict__ nfreeDev,
                                    const T *__restrict__ b, double *__restrict__ out) {
+    VFEM_PDL_ENTRY();
     const int nfree = *nfreeDev;
     const int t = blockIdx.x * BS + threadIdx.x;
     if (t >= nfree) return;
@@ -255,6 +256,7 @@ __global__ void gather_free_kernel(const Geom g, const int *__restrict__ freeIdx
 template <typename T>
 __global__ void symv_scatter_kernel(const Geom g, const double *__restrict__ Ainv, const int *__restrict__ freeIdx,
                                     const int *__restrict__ nfreeDev, const double *__restrict__ bf, T *__restrict__ x) {
+    VFEM_PDL_ENTRY();
     const int nfree = *nfreeDev;
     const int row = blockIdx.x * (BS / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -280,6 +282,7 @@ __device__ __forceinline__ int64_t masked_node(const Geom &g, int64_t m, int row
 template <typename Ta, typename Tb>
 __global__ void __launch_bounds__(BS) masked_dot_kernel(Geom g, const Ta *__restrict__ a, const Tb *__restrict__ b,
                                                         double *__restrict__ partials) {
+    VFEM_PDL_ENTRY();
     const int rows = g.nyv();
     const int64_t M = (int64_t)g.nn[0] * rows * g.nn[2];
     double acc = 0.0;
@@ -299,12 +302,14 @@ __device__ double sum_partials(const double *partials, int n) {
 }
 
 __global__ void finalize_kernel(const double *partials, int n, double *out) {
+    VFEM_PDL_ENTRY();
     const double s = sum_partials(partials, n);
     if (threadIdx.x == 0) *out = s;
 }
 
 // sc: 0 rMr, 1 rMr_old, 2 beta, 3 alpha, 4 dAd, 5 rsq, 6 first
 __global__ void cg_beta_kernel(const double *partials, int n, double *sc) {
+    VFEM_PDL_ENTRY();
     const double s = sum_partials(partials, n);
     if (threadIdx.x == 0) {
         sc[1] = sc[0];
@@ -315,6 +320,7 @@ __global__ void cg_beta_kernel(const double *partials, int n, double *sc) {
 }
 
 __global__ void cg_alpha_kernel(const double *partials, int n, double *sc) {
+    VFEM_PDL_ENTRY();
     const double s = sum_partials(partials, n);
     if (threadIdx.x == 0) {
         sc[4] = s;
@@ -323,6 +329,7 @@ __global__ void cg_alpha_kernel(const double *partials, int n, double *sc) {
 }
 
 __global__ void cg_rsq_kernel(const double *partials, int n, double *sc, double *mirror) {
+    VFEM_PDL_ENTRY();
     const double s = sum_partials(partials, n);
     if (threadIdx.x == 0) {
         sc[5] = s;
@@ -335,6 +342,7 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
                                                             const double *__restrict__ r,
                                                             const uint8_t *__restrict__ dmask,
                                                             double *__restrict__ partials) {
+    VFEM_PDL_ENTRY();
     const int rows = g.nyv();
     double acc = 0.0;
     for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
@@ -355,6 +363,7 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
 __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double *__restrict__ d,
                                     const double *__restrict__ sc, float *__restrict__ dh, float *__restrict__ dl,
                                     double *__restrict__ amax) {
+    VFEM_PDL_ENTRY();
     const double beta = sc[2];
     const int64_t N3 = 3 * g.ld;
     double m = 0.0;
@@ -389,6 +398,7 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
 __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restrict__ x, double *__restrict__ r,
                                                        const double *__restrict__ d, const double *__restrict__ Ad,
                                                        const double *__restrict__ sc, double *__restrict__ partials) {
+    VFEM_PDL_ENTRY();
     const double alpha = sc[3];
     const int rows = g.nyv();
     const int64_t M = (int64_t)g.nn[0] * rows * g.nn[2];
@@ -409,6 +419,7 @@ __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restric
 }
 
 __global__ void copy_kernel(double *__restrict__ dst, const double *__restrict__ src, int64_t n) {
+    VFEM_PDL_ENTRY();
     for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) dst[t] = src[t];
 }
 
@@ -485,9 +496,9 @@ void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, 
                          const T *b, T *x, double *scratch, cudaStream_t st) {
     launch_fill<T>(x, T(0), 3 * g.ld, st);
     if (nfreeCap <= 0) return;
-    gather_free_kernel<T><<<gridFor(nfreeCap, BS), BS, 0, st>>>(g, freeIdx, nfreeDev, b, scratch);
+    launch_pdl(gather_free_kernel<T>, gridFor(nfreeCap, BS), BS, 0, st, g, freeIdx, nfreeDev, b, scratch);
     VFEM_LAUNCH_CHECK();
-    symv_scatter_kernel<T><<<gridFor(nfreeCap, BS / 32), BS, 0, st>>>(g, Ainv, freeIdx, nfreeDev, scratch, x);
+    launch_pdl(symv_scatter_kernel<T>, gridFor(nfreeCap, BS / 32), BS, 0, st, g, Ainv, freeIdx, nfreeDev, scratch, x);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -533,12 +544,13 @@ void launch_cg_init(double *sc, double tol2, double maxIter, cudaStream_t st) {
 }
 
 __global__ void axpy_kernel(int64_t n, double a, const double *__restrict__ xv, double *__restrict__ yv) {
+    VFEM_PDL_ENTRY();
     for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) yv[t] += a * xv[t];
 }
 
 void launch_axpy(int64_t n, double a, const double *x, double *y, cudaStream_t st) {
     if (n <= 0) return;
-    axpy_kernel<<<std::min<unsigned>(gridFor(n, BS), 4 * 152), BS, 0, st>>>(n, a, x, y);
+    launch_pdl(axpy_kernel, std::min<unsigned>(gridFor(n, BS), 4 * 152), BS, 0, st, n, a, x, y);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -554,48 +566,48 @@ void launch_set_pair(int *p, int a, int b, cudaStream_t st) {
 
 template <typename Ta, typename Tb>
 void launch_masked_dot_partials(const Geom &g, const Ta *a, const Tb *b, double *partials, cudaStream_t st) {
-    masked_dot_kernel<Ta, Tb><<<REDUCE_BLOCKS, BS, 0, st>>>(g, a, b, partials);
+    launch_pdl(masked_dot_kernel<Ta, Tb>, REDUCE_BLOCKS, BS, 0, st, g, a, b, partials);
     VFEM_LAUNCH_CHECK();
 }
 
 void launch_finalize(const double *partials, int n, double *out, cudaStream_t st) {
-    finalize_kernel<<<1, BS, 0, st>>>(partials, n, out);
+    launch_pdl(finalize_kernel, 1, BS, 0, st, partials, n, out);
     VFEM_LAUNCH_CHECK();
 }
 void launch_cg_beta(const double *partials, int n, double *sc, cudaStream_t st) {
-    cg_beta_kernel<<<1, BS, 0, st>>>(partials, n, sc);
+    launch_pdl(cg_beta_kernel, 1, BS, 0, st, partials, n, sc);
     VFEM_LAUNCH_CHECK();
 }
 void launch_cg_alpha(const double *partials, int n, double *sc, cudaStream_t st) {
-    cg_alpha_kernel<<<1, BS, 0, st>>>(partials, n, sc);
+    launch_pdl(cg_alpha_kernel, 1, BS, 0, st, partials, n, sc);
     VFEM_LAUNCH_CHECK();
 }
 void launch_cg_rsq(const double *partials, int n, double *sc, double *mirror, cudaStream_t st) {
-    cg_rsq_kernel<<<1, BS, 0, st>>>(partials, n, sc, mirror);
+    launch_pdl(cg_rsq_kernel, 1, BS, 0, st, partials, n, sc, mirror);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename Ts>
 void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                            double *partials, cudaStream_t st) {
-    cg_precond_out_kernel<Ts><<<REDUCE_BLOCKS, BS, 0, st>>>(g, src, s, r, dmask, partials);
+    launch_pdl(cg_precond_out_kernel<Ts>, REDUCE_BLOCKS, BS, 0, st, g, src, s, r, dmask, partials);
     VFEM_LAUNCH_CHECK();
 }
 
 void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
                          cudaStream_t st, double *amax) {
-    cg_direction_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, s, d, sc, dh, dl, amax);
+    launch_pdl(cg_direction_kernel, REDUCE_BLOCKS, BS, 0, st, g, s, d, sc, dh, dl, amax);
     VFEM_LAUNCH_CHECK();
 }
 
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
                       double *partials, cudaStream_t st) {
-    cg_update_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(g, x, r, d, Ad, sc, partials);
+    launch_pdl(cg_update_kernel, REDUCE_BLOCKS, BS, 0, st, g, x, r, d, Ad, sc, partials);
     VFEM_LAUNCH_CHECK();
 }
 
 void launch_copy(double *dst, const double *src, int64_t n, cudaStream_t st) {
-    copy_kernel<<<REDUCE_BLOCKS, BS, 0, st>>>(dst, src, n);
+    launch_pdl(copy_kernel, REDUCE_BLOCKS, BS, 0, st, dst, src, n);
     VFEM_LAUNCH_CHECK();
 }
 

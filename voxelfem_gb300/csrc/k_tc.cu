@@ -4,10 +4,10 @@
 // Idea. For cube voxels of an isotropic material with a rational lambda/mu, the element matrix
 // is K0 = c * C with C a small-integer matrix (|C| <= 88, row sums <= 472 at nu = 0.3). The
 // operand u is written in fixed point with one scale for the whole vector, F = round(u 2^(55-s)),
-// |u| < 2^s, and split into eight signed base-128 digits, paired into four 14-bit pieces
-// P_a = 128 D_2a + D_2a+1. Every digit and every C entry is exact in bf16, and
-// |sum_k C_nk P_ak| <= 472 * 8256 < 2^24, so the FP32 accumulator of a bf16 MMA holds C P_a
-// EXACTLY. Four accumulators give C F = acc0 2^42 + acc1 2^28 + acc2 2^14 + acc3; the epilogue
+// |u| < 2^s, and split into eight base-128 digits (a signed top digit, seven 7-bit fields),
+// paired into four pieces P_a = 128 D_2a + D_2a+1. Every digit and every C entry is exact in
+// bf16, and |sum_k C_nk P_ak| <= 472 * 16383 < 2^24, so the FP32 accumulator of a bf16 MMA holds
+// C P_a EXACTLY. Four accumulators give C F = acc0 2^42 + acc1 2^28 + acc2 2^14 + acc3; the epilogue
 // forms it in double-float, scales by E_e c per element and sums the eight element contributions
 // of every node in double-float. The result matches FP64 to ~3e-14 relative to |K| |u| (the
 // double-float kernel's accuracy); the FP64 units (1/64 of the FP32 rate here) only convert the
@@ -48,9 +48,8 @@ constexpr int SDOF = TY * SPITCH;
 
 constexpr int OFF_B = 0;                                  // B tiles, 4 KB
 constexpr int OFF_TAB = OFF_B + 4096;                     // [2 planes][NACC] digit tables
-constexpr int OFF_STH = OFF_TAB + 2 * NACC * TAB;         // staging hi parts [24][SDOF]
-constexpr int OFF_STL = OFF_STH + 24 * SDOF * 4;          // staging lo parts
-constexpr int OFF_MISC = OFF_STL + 24 * SDOF * 4;         // mbarrier, TMEM address, scale
+constexpr int OFF_STH = OFF_TAB + 2 * NACC * TAB;         // staging (hi, lo) pairs [24][SDOF]
+constexpr int OFF_MISC = OFF_STH + 24 * SDOF * 8;         // mbarrier, TMEM address, scale
 constexpr int SMEM_USED = OFF_MISC + 64;
 // The allocation is padded so that at most four CTAs share an SM: 4 x 128 TMEM columns = 512.
 constexpr int SMEM_BYTES = 52 * 1024;
@@ -143,60 +142,77 @@ __device__ __forceinline__ long long fixed_point(double v, int sh0) {
     return (b >> 63) ? -F : F;
 }
 
-// Exact small integer (|d| < 2^22) as a float, then its bf16 bit pattern (exact for <= 8
-// significant bits).
-__device__ __forceinline__ uint32_t bf16_bits(int d) {
-    const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
-    return __float_as_uint(f) >> 16;
-}
+// The float of a small integer d (|d| < 2^22), exact.
+__device__ __forceinline__ float int_float(int d) { return __int_as_float(0x4B400000 + d) - 12582912.0f; }
 
-// Signed base-128 digits of round(v 2^(55 - s)) written into the digit tables of one node row:
-// for pair a, 128 D_2a at value c and D_2a+1 at value 3 + c of the row's 8 (values 6, 7 stay 0).
-__device__ __forceinline__ void store_digits(double v, int sh0, uint8_t *row, int c) {
-    long long F = fixed_point(v, sh0);
-    int D[2 * NACC];
+// Digit-table rows of one node: the three components' fixed-point values F (two's complement,
+// |F| <= 2^55) as D0 = F >> 49 (signed) and seven unsigned 7-bit fields D1..D7, so that
+// F = sum_a P_a 2^(14 (3 - a)) with P_a = 128 D_2a + D_2a+1 (P_0 in [-8192, 8319], P_a in
+// [0, 16383] otherwise). Pair a's row holds bf16 [128 D_2a (c = 0, 1, 2), D_2a+1 (c = 0, 1, 2),
+// 0, 0]; every value has at most 7 significant bits, so bf16 holds it exactly.
+__device__ __forceinline__ void node_rows(const double u3[3], int sh0, uint4 rows[NACC]) {
+    float hi[3][NACC], lo[3][NACC];
 #pragma unroll
-    for (int i = 2 * NACC - 1; i >= 1; --i) {
-        const int d = (int)((F + 64) & 127) - 64;
-        D[i] = d;
-        F = (F - d) >> 7;
+    for (int c = 0; c < 3; ++c) {
+        const long long F = fixed_point(u3[c], sh0);
+        const uint32_t l32 = (uint32_t)F, h32 = (uint32_t)(F >> 32);
+        const int D0 = (int)h32 >> 17;
+        const int D1 = (int)((h32 >> 10) & 127u), D2 = (int)((h32 >> 3) & 127u);
+        const int D3 = (int)(__funnelshift_r(l32, h32, 28) & 127u);
+        const int D4 = (int)((l32 >> 21) & 127u), D5 = (int)((l32 >> 14) & 127u);
+        const int D6 = (int)((l32 >> 7) & 127u), D7 = (int)(l32 & 127u);
+        hi[c][0] = int_float(D0) * 128.0f;
+        lo[c][0] = int_float(D1);
+        hi[c][1] = int_float(D2) * 128.0f;
+        lo[c][1] = int_float(D3);
+        hi[c][2] = int_float(D4) * 128.0f;
+        lo[c][2] = int_float(D5);
+        hi[c][3] = int_float(D6) * 128.0f;
+        lo[c][3] = int_float(D7);
     }
-    D[0] = (int)F;
 #pragma unroll
     for (int a = 0; a < NACC; ++a) {
-        *reinterpret_cast<uint16_t *>(row + a * TAB + 2 * c) = (uint16_t)bf16_bits(128 * D[2 * a]);
-        *reinterpret_cast<uint16_t *>(row + a * TAB + 2 * (3 + c)) = (uint16_t)bf16_bits(D[2 * a + 1]);
+        // upper halves of two floats = two bf16 values (exact: at most 7 significant bits)
+        const uint32_t w0 = __byte_perm(__float_as_uint(hi[0][a]), __float_as_uint(hi[1][a]), 0x7632);
+        const uint32_t w1 = __byte_perm(__float_as_uint(hi[2][a]), __float_as_uint(lo[0][a]), 0x7632);
+        const uint32_t w2 = __byte_perm(__float_as_uint(lo[1][a]), __float_as_uint(lo[2][a]), 0x7632);
+        rows[a] = make_uint4(w0, w1, w2, 0u);
     }
 }
 
-// The patch's node plane x as 3 x TROWS items (node-major: item = 3 node + c, node = yn NPZ + zn,
-// so consecutive threads read consecutive z); item tid + TCT k goes to pf[k]. Zero outside the grid.
-constexpr int PF = (3 * TROWS + TCT - 1) / TCT;
+// The patch's node plane x, one node per item (node = yn NPZ + zn, consecutive threads read
+// consecutive z); item tid + TCT k goes to pf[k]. Zero outside the grid.
+constexpr int PF = (TROWS + TCT - 1) / TCT;
 
 __device__ __forceinline__ void load_plane(const Geom &g, const double *__restrict__ u, int x, int ny0, int nz0,
-                                           double pf[PF]) {
+                                           double pf[PF][3]) {
 #pragma unroll
     for (int k = 0; k < PF; ++k) {
-        const int item = threadIdx.x + TCT * k;
-        pf[k] = 0.0;
-        if (item < 3 * TROWS) {
-            const int node = item / 3, c = item - 3 * node;
+        const int node = threadIdx.x + TCT * k;
+        pf[k][0] = pf[k][1] = pf[k][2] = 0.0;
+        if (node < TROWS) {
             const int yn = node / NPZ, zn = node - NPZ * yn;
             const int y = ny0 + yn, z = nz0 + zn;
-            if (x >= 0 && x < g.nn[0] && y >= 0 && y < g.nn[1] && z >= 0 && z < g.nn[2])
-                pf[k] = __ldg(u + c * g.ld + g.node(x, y, z));
+            if (x >= 0 && x < g.nn[0] && y >= 0 && y < g.nn[1] && z >= 0 && z < g.nn[2]) {
+                const double *p = u + g.node(x, y, z);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) pf[k][c] = __ldg(p + c * g.ld);
+            }
         }
     }
 }
 
-__device__ __forceinline__ void build_tables(const double pf[PF], int sh0, uint8_t *tab) {
+__device__ __forceinline__ void build_tables(const double pf[PF][3], int sh0, uint8_t *tab) {
 #pragma unroll
     for (int k = 0; k < PF; ++k) {
-        const int item = threadIdx.x + TCT * k;
-        if (item < 3 * TROWS) {
-            const int node = item / 3, c = item - 3 * node;
+        const int node = threadIdx.x + TCT * k;
+        if (node < TROWS) {
             const int yn = node / NPZ, zn = node - NPZ * yn;
-            store_digits(pf[k], sh0, tab + (zn * NPY + yn) * 16, c);
+            uint4 rows[NACC];
+            node_rows(pf[k], sh0, rows);
+            uint8_t *row = tab + (zn * NPY + yn) * 16;
+#pragma unroll
+            for (int a = 0; a < NACC; ++a) *reinterpret_cast<uint4 *>(row + a * TAB) = rows[a];
         }
     }
 }
@@ -217,10 +233,10 @@ __global__ void __launch_bounds__(TCT, 4)
                           const uint4 *__restrict__ bTiles, float scaleHi, float scaleLo,
                           const uint8_t *__restrict__ dmask, int zeroDir, double *__restrict__ partials, int withDot,
                           const double *__restrict__ rhs, int nTZ, int nTY, int segLen, int *status) {
+    VFEM_PDL_ENTRY();
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *tabs = smem + OFF_TAB;
-    float *stH = reinterpret_cast<float *>(smem + OFF_STH);
-    float *stL = reinterpret_cast<float *>(smem + OFF_STL);
+    float2 *stg = reinterpret_cast<float2 *>(smem + OFF_STH);  // (hi, lo) of each element contribution
     uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + OFF_MISC);
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + OFF_MISC + 8);
     double *red = reinterpret_cast<double *>(smem + OFF_MISC + 16);  // 4 doubles
@@ -290,21 +306,21 @@ __global__ void __launch_bounds__(TCT, 4)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int dy = q >> 1, dz = q & 1;
-                const int idx = (3 * q + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                const float2 v = stg[(3 * q + r) * SDOF + (yn - dy) * SPITCH + (zn - dz)];
                 float t, e;
-                two_sum(h, stH[idx], t, e);
+                two_sum(h, v.x, t, e);
                 h = t;
-                l += e + stL[idx];
+                l += e + v.y;
             }
             float h2 = 0.f, l2 = 0.f;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int dy = q >> 1, dz = q & 1;
-                const int idx = (3 * (4 + q) + r) * SDOF + (yn - dy) * SPITCH + (zn - dz);
+                const float2 v = stg[(3 * (4 + q) + r) * SDOF + (yn - dy) * SPITCH + (zn - dz)];
                 float t, e;
-                two_sum(h2, stH[idx], t, e);
+                two_sum(h2, v.x, t, e);
                 h2 = t;
-                l2 += e + stL[idx];
+                l2 += e + v.y;
             }
             ah[r] = h2;
             al[r] = l2;
@@ -325,9 +341,7 @@ __global__ void __launch_bounds__(TCT, 4)
         }
     };
 
-    // the two zero values of every digit-table row
-    for (int t = tid; t < 2 * NACC * TROWS; t += TCT) *reinterpret_cast<uint32_t *>(tabs + t * 16 + 12) = 0u;
-    double pf[PF];
+    double pf[PF][3];
     load_plane(g, u, X0 - 1, ny0, nz0, pf);
     build_tables(pf, sh0, tabs + ((X0 - 1) & 1) * NACC * TAB);
     load_plane(g, u, X0, ny0, nz0, pf);
@@ -388,8 +402,7 @@ __global__ void __launch_bounds__(TCT, 4)
                 float e = __fmaf_rn(h, sh, -p);
                 e = __fmaf_rn(h, sl, e);
                 e = __fmaf_rn(l, sh, e);
-                stH[(c0 + j) * SDOF + ey * SPITCH + ez] = p;
-                stL[(c0 + j) * SDOF + ey * SPITCH + ez] = e;
+                stg[(c0 + j) * SDOF + ey * SPITCH + ez] = make_float2(p, e);
             }
         }
     }
@@ -411,6 +424,7 @@ __global__ void __launch_bounds__(TCT, 4)
 }
 
 __global__ void absmax_partials_kernel(const double *__restrict__ u, int64_t n, double *__restrict__ partials) {
+    VFEM_PDL_ENTRY();
     double m = 0.0;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
         m = nanmax(m, fabs(u[t]));
@@ -479,7 +493,7 @@ bool tc_fit_k0(const double K0[576], double *scale, uint16_t bTiles[2048]) {
     for (int n = 0; n < 24; ++n) {
         long rs = 0;
         for (int k = 0; k < 24; ++k) rs += std::labs((long)C[n * 24 + k]);
-        if (rs * 8256L >= (1L << 24)) return false;
+        if (rs * 16383L >= (1L << 24)) return false;
     }
     // B tiles: MMA q = (dx, dz) at q * 1024 bytes; K chunk s = dy at s * 512; N group at g * 128;
     // row n of the group at 16 bytes; K value v: C[n][3 m + v % 3] (v < 6, m = 4 dx + 2 dy + dz)
@@ -505,7 +519,7 @@ int tc_matvec_blocks(const Geom &g, int maxBlocks) {
 }
 
 void launch_absmax_partials(const double *u, int64_t n, double *partials, cudaStream_t st) {
-    absmax_partials_kernel<<<REDUCE_BLOCKS, 256, 0, st>>>(u, n, partials);
+    launch_pdl(absmax_partials_kernel, REDUCE_BLOCKS, 256, 0, st, u, n, partials);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -521,7 +535,7 @@ int launch_applyk_fine_tc(const Geom &g, const float *Yh, const float *Yl, const
     const int blocks = t.nTY * t.nTZ * t.nSeg;
     if (partialDot && blocks > partialBlocks) throw Error(ERR_ARG, "partial buffer too small");
     const float sh = (float)scale, sl = (float)(scale - (double)sh);
-    applyk_fine_tc_kernel<<<blocks, TCT, SMEM_BYTES, st>>>(g, Yh, Yl, u, umax, out,
+    launch_pdl(applyk_fine_tc_kernel, blocks, TCT, SMEM_BYTES, st, g, Yh, Yl, u, umax, out,
                                                            reinterpret_cast<const uint4 *>(bTiles), sh, sl, dmask,
                                                            zeroDirichlet ? 1 : 0, partialDot, partialDot ? 1 : 0, rhs,
                                                            t.nTZ, t.nTY, t.segLen, status);

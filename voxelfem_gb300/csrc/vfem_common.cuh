@@ -30,6 +30,43 @@ uint64_t &launchCounter();
         ++::vfem::launchCounter();                                       \
     } while (0)
 
+// Programmatic dependent launch. Kernels of the solve's inner loops start with
+// VFEM_PDL_ENTRY(): they wait for the previous kernel of the stream to complete (and its memory
+// to be visible), then allow the next kernel to be scheduled, so its launch overlaps this
+// kernel's execution. Launched without the attribute, the entry is a no-op.
+#if defined(__CUDA_ARCH__)
+#define VFEM_PDL_ENTRY()                                                    \
+    do {                                                                    \
+        asm volatile("griddepcontrol.wait;" ::: "memory");                  \
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");     \
+    } while (0)
+#else
+#define VFEM_PDL_ENTRY() \
+    do {                 \
+    } while (0)
+#endif
+
+// Process-wide switch of programmatic dependent launch (on unless VFEM_PDL=0).
+bool pdlEnabled();
+
+// kernel<<<grid, block, smem, st>>>(args...) with programmatic stream serialisation; the kernel
+// must begin with VFEM_PDL_ENTRY().
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdlEnabled() ? 1 : 0;
+    cudaCheck(cudaLaunchKernelEx(&cfg, kernel, args...), "kernel launch");
+}
+
 constexpr int BUILD_DIR = 1;         // layers are stacked along y (TensorProductSimulator.hh:1851)
 constexpr int64_t LAYER_MASK_NONE = 2147483647;
 constexpr int MARGIN = 4;            // detached-node margin copied with b (MultigridSolver.hh:532)

@@ -16,6 +16,14 @@ uint64_t &launchCounter() {
     return counter;
 }
 
+bool pdlEnabled() {
+    static const bool on = [] {
+        const char *env = std::getenv("VFEM_PDL");
+        return !(env && env[0] == '0');
+    }();
+    return on;
+}
+
 // ---------------------------------------------------------------------------
 // caller-memory views
 // ---------------------------------------------------------------------------
