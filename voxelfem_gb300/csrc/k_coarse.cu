@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     if (valid) {
         dm = dmask[n];
 #pragma unroll
-        for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)(13 * 9 + e) * ld + p];
+        for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)e * ld + p];  // diagonal block (offset 13)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             bb[c] = b[c * ld + n];
@@ -341,15 +341,15 @@ __global__ void __launch_bounds__(ROW) stencil_level1_kernel(Geom g1, Geom g0, c
     S[n * ROW + q] = acc;
 }
 
-// Plane-layout variant: thread per (position p, neighbour offset o), o = blockIdx.y, writing
-// the nine entries of block (n, n+o). The Kc indices are warp-uniform (constant-cache
+// Plane-layout variant: thread per (position p, neighbour offset o), o = 13 + blockIdx.y (the
+// stored half), writing the nine entries of block (n, n+o). The Kc indices are warp-uniform (constant-cache
 // broadcasts) and the eight fine moduli of each shared coarse element are loaded once for
 // all nine entries.
 template <typename T>
 __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
                                                                 const T *__restrict__ Kc, T *__restrict__ S) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
-    const int o = blockIdx.y;
+    const int o = 13 + blockIdx.y;
     if (p >= g1.NN) return;
     int i, j, k;
     stencil::colour_node(g1, p, i, j, k);
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0
                     }
             }
 #pragma unroll
-    for (int e = 0; e < 9; ++e) S[(int64_t)(o * 9 + e) * g1.ld + p] = acc[e];
+    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g1.ld + p] = acc[e];
 }
 
 // Level-2 element matrices straight from the fine moduli: Ke_2(e) = sum over the 64 fine
@@ -517,7 +517,7 @@ template <typename T>
 __global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T *__restrict__ Ke,
                                                                  T *__restrict__ S) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
-    const int o = blockIdx.y;
+    const int o = 13 + blockIdx.y;
     if (p >= g.NN) return;
     int i, j, k;
     stencil::colour_node(g, p, i, j, k);
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T
                     for (int c = 0; c < 3; ++c) acc[3 * r + c] += ke[(3 * ln + r) * 24 + 3 * lm + c];
             }
 #pragma unroll
-    for (int e = 0; e < 9; ++e) S[(int64_t)(o * 9 + e) * g.ld + p] = acc[e];
+    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g.ld + p] = acc[e];
 }
 
 }  // namespace
@@ -648,7 +648,7 @@ template <typename T>
 void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st) {
     if (g1.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
     if (rows) stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
-    else stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), 27), BS, 0, st>>>(g1, g0, Y0, Kc, S);
+    else stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g1, g0, Y0, Kc, S);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -675,7 +675,7 @@ template <typename T>
 void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st) {
     if (g.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
     if (rows) stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
-    else stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), 27), BS, 0, st>>>(g, Ke, S);
+    else stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g, Ke, S);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -30,7 +30,11 @@ __global__ void dense_from_stencil_kernel(Geom g, const T *__restrict__ S, const
     const int64_t m = g.node(ni, nj, nk);
     const int ra = red[3 * n + r], cb = red[3 * m + c];
     if (ra < 0 || cb < 0) return;
-    A[(int64_t)ra * nfree + cb] = (double)(rows ? S[n * 256 + q] : S[(int64_t)q * g.ld + stencil::colour_pos(g, i, j, k)]);
+    T v;
+    if (rows) v = S[n * 256 + q];
+    else if (o >= 13) v = S[(int64_t)((o - 13) * 9 + 3 * r + c) * g.ld + stencil::colour_pos(g, i, j, k)];
+    else v = S[(int64_t)((13 - o) * 9 + 3 * c + r) * g.ld + stencil::colour_pos(g, ni, nj, nk)];  // stored half
+    A[(int64_t)ra * nfree + cb] = (double)v;
 }
 
 __global__ void symmetrize_kernel(double *A, int n) {

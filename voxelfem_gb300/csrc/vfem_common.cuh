@@ -84,6 +84,10 @@ struct Geom {
     // mask from it, launch over the full grid and skip the detached rows, so a captured CUDA
     // graph stays valid when the fabrication mask height changes.
     const int *dyn = nullptr;
+    // Colour-ordered node positions (plane-layout stencils): colour c = 4(i&1) + 2(j&1) + (k&1)
+    // starts at coff[c]; hc1[b], hc2[b] = nodes with j&1 == b, k&1 == b along y, z.
+    int64_t coff[8];
+    int hc1[2], hc2[2];
     __host__ __device__ int detN() const {
 #if defined(__CUDA_ARCH__)
         if (dyn) return dyn[1];
@@ -121,6 +125,17 @@ inline Geom makeGeom(const int ne[3]) {
     g.ld = g.NN;  // SoA component stride: exactly the (nn, 3) column-major VField layout
     g.firstMaskedE = (int)LAYER_MASK_NONE;
     g.firstDetN = (int)LAYER_MASK_NONE;
+    auto half = [](int n, int b) { return (n + 1 - b) >> 1; };
+    for (int b = 0; b < 2; ++b) {
+        g.hc1[b] = half(g.nn[1], b);
+        g.hc2[b] = half(g.nn[2], b);
+    }
+    for (int c = 0; c < 8; ++c) {
+        const int cx = (c >> 2) & 1, cy = (c >> 1) & 1, cz = c & 1;
+        g.coff[c] = (cx ? (int64_t)half(g.nn[0], 0) * g.nn[1] * g.nn[2] : 0) +
+                    (int64_t)half(g.nn[0], cx) * ((cy ? (int64_t)half(g.nn[1], 0) * g.nn[2] : 0) +
+                                                  (int64_t)half(g.nn[1], cy) * (cz ? half(g.nn[2], 0) : 0));
+    }
     return g;
 }
 

@@ -663,7 +663,7 @@ void MG::updateStiffnessT() {
         auto &D = lv[0].data<T>();
         D.Ke.alloc((size_t)lv[0].g.NE * 576);
         lv[0].rows = lv[0].g.NN <= rowsMaxNodes;
-        D.S.alloc((size_t)(lv[0].rows ? 256 : 243) * lv[0].g.NN);
+        D.S.alloc((size_t)(lv[0].rows ? 256 : STENCIL_PLANES) * lv[0].g.NN);
         std::vector<double> k0(fine->K0.a, fine->K0.a + 576);
         DevBuf<T> K0d;
         uploadConst(K0d, k0.data(), 576);
@@ -674,7 +674,7 @@ void MG::updateStiffnessT() {
         for (int l = 1; l < L(); ++l) {
             auto &D = lv[l].data<T>();
             lv[l].rows = lv[l].g.NN <= rowsMaxNodes;
-            D.S.alloc((size_t)(lv[l].rows ? 256 : 243) * lv[l].g.NN);
+            D.S.alloc((size_t)(lv[l].rows ? 256 : STENCIL_PLANES) * lv[l].g.NN);
             if (l == 1) {
                 // the level-1 stencil comes straight from the fine moduli; no level-1 element
                 // matrices are stored
@@ -1577,7 +1577,7 @@ double MG::kernelBytes(int which) const {
         // one pass over the level's stencil plus x, b, r (or x read and written)
         const Level &lvl = lv[which >= 8 ? 2 : 1];
         const double n1 = (double)lvl.g.NN;
-        return 4.0 * (9 * n1 + (lvl.rows ? 256 : 243) * n1);
+        return 4.0 * (9 * n1 + (lvl.rows ? 256 : STENCIL_PLANES) * n1);
     }
     }
     return 0;

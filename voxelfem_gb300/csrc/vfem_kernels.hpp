@@ -52,6 +52,10 @@ __host__ __device__ constexpr int k0_cube_class(int row, int col) {
 // kv[c] from K (24 x 24, row-major) if every entry matches the cube pattern to round-off.
 bool k0_cube_values(const double *K, double kv[10]);
 
+// Stored entries per node of a plane-layout stencil: the diagonal and upper-half blocks
+// (offsets 13..26) of the symmetric Galerkin operator.
+constexpr int STENCIL_PLANES = 14 * 9;
+
 // ---------------- fine level (k_fine.cu) ----------------
 template <typename T>
 void launch_young_moduli(const Geom &g, const double *rho, T *Y, double E0, double Emin, double gamma, double q,

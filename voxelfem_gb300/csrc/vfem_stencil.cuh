@@ -181,19 +181,21 @@ __device__ __forceinline__ void residual_node_warp(const Geom &g, const T *__res
 }
 
 
-// ---- plane layout (large levels): S[(o*9 + 3r + c) * ld + p], one thread per node ----
+// ---- plane layout (large levels): S[((o - 13)*9 + 3r + c) * ld + p], one thread per node ----
 // p is the node's colour-ordered position: nodes grouped by colour (i&1, j&1, k&1), colours in
 // ascending order 4cx+2cy+cz, each colour's nodes in lexicographic (i>>1, j>>1, k>>1) order.
-// A Gauss-Seidel colour pass then streams a contiguous slice of every plane.
+// A Gauss-Seidel colour pass then streams a contiguous slice of every plane. The Galerkin
+// operator is symmetric, so only the blocks of offsets o = 13..26 (the diagonal and the upper
+// half) are stored: block (n, n + d_o) for o < 13 is the transpose of block (m, m + d_(26-o)) of
+// the neighbour m = n + d_o, read at m's position. The neighbours of a warp's consecutive
+// colour positions are consecutive positions of the neighbour colour, so those reads coalesce.
+constexpr int HALF_OFFSETS = 14;
+constexpr int PLANES = HALF_OFFSETS * 9;  // stored entries per node (STENCIL_PLANES)
 __device__ __forceinline__ int half_count(int nn, int b) { return (nn + 1 - b) >> 1; }
 
 __device__ __forceinline__ int64_t colour_pos(const Geom &g, int i, int j, int k) {
-    const int cx = i & 1, cy = j & 1, cz = k & 1;
-    const int c1 = half_count(g.nn[1], cy), c2 = half_count(g.nn[2], cz);
-    const int64_t off = (cx ? (int64_t)half_count(g.nn[0], 0) * g.nn[1] * g.nn[2] : 0) +
-                        (int64_t)half_count(g.nn[0], cx) *
-                            ((cy ? (int64_t)half_count(g.nn[1], 0) * g.nn[2] : 0) + (int64_t)c1 * (cz ? half_count(g.nn[2], 0) : 0));
-    return off + ((int64_t)(i >> 1) * c1 + (j >> 1)) * c2 + (k >> 1);
+    const int cy = j & 1, cz = k & 1;
+    return g.coff[4 * (i & 1) + 2 * cy + cz] + ((int64_t)(i >> 1) * g.hc1[cy] + (j >> 1)) * g.hc2[cz] + (k >> 1);
 }
 
 __device__ __forceinline__ void colour_node(const Geom &g, int64_t p, int &i, int &j, int &k) {
@@ -244,9 +246,21 @@ __device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restr
             const int64_t m = in ? n + ox * sx + oy * sy + oz : n;
 #pragma unroll
             for (int c = 0; c < 3; ++c) uu[t][c] = u[c * ld + m];
-            const T *blk = S + (int64_t)(o * 9) * ld + p;
+            if (o >= 13) {
+                const T *blk = S + (int64_t)((o - 13) * 9) * ld + p;
 #pragma unroll
-            for (int e = 0; e < 9; ++e) ss[t][e] = blk[e * ld];
+                for (int e = 0; e < 9; ++e) ss[t][e] = blk[e * ld];
+            } else if (in) {
+                // transpose of the neighbour's block towards this node (offset 26 - o)
+                const T *blk = S + (int64_t)((13 - o) * 9) * ld + colour_pos(g, i + ox, j + oy, k + oz);
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) ss[t][3 * r + c] = blk[(3 * c + r) * ld];
+            } else {
+#pragma unroll
+                for (int e = 0; e < 9; ++e) ss[t][e] = T(0);
+            }
         } else {
 #pragma unroll
             for (int c = 0; c < 3; ++c) uu[t][c] = T(0);
