@@ -370,7 +370,10 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
     VFEM_PDL_ENTRY();
     const double beta = sc[2];
     const int64_t N3 = 3 * g.ld;
-    double m = 0.0;
+    // |v| as the bit pattern with the sign cleared: for non-negative doubles the unsigned order
+    // of the patterns is the numeric order, and NaN patterns exceed every number, so an integer
+    // maximum (integer units; the FP64 units are the scarce ones here) propagates NaN
+    unsigned long long m = 0ull;
     for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS) {
         const double v = beta * d[t] + s[t];
         d[t] = v;
@@ -379,22 +382,22 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
             dh[t] = h;
             dl[t] = __double2float_rn(v - (double)h);
         }
-        const double a = fabs(v);
-        m = (a > m || a != a) ? a : m;
+        const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+        m = a > m ? a : m;
     }
     if (amax) {
-        __shared__ double sh[BS / 32];
+        __shared__ unsigned long long sh[BS / 32];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double a = __shfl_xor_sync(0xffffffffu, m, o);
-            m = (a > m || a != a) ? a : m;
+            const unsigned long long a = __shfl_xor_sync(0xffffffffu, m, o);
+            m = a > m ? a : m;
         }
         if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
         __syncthreads();
         if (threadIdx.x == 0) {
-            double r = 0.0;
-            for (int w = 0; w < BS / 32; ++w) r = (sh[w] > r || sh[w] != sh[w]) ? sh[w] : r;
-            amax[blockIdx.x] = r;
+            unsigned long long r = 0ull;
+            for (int w = 0; w < BS / 32; ++w) r = sh[w] > r ? sh[w] : r;
+            amax[blockIdx.x] = __longlong_as_double((long long)r);
         }
     }
 }
