@@ -404,7 +404,8 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
 
 __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restrict__ x, double *__restrict__ r,
                                                        const double *__restrict__ d, const double *__restrict__ Ad,
-                                                       const double *__restrict__ sc, double *__restrict__ partials) {
+                                                       const double *__restrict__ sc, double *__restrict__ partials,
+                                                       float *__restrict__ b32, float *__restrict__ x32) {
     VFEM_PDL_ENTRY();
     const double alpha = sc[3];
     const int rows = g.nyv();
@@ -419,6 +420,11 @@ __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restric
             const double rv = r[q] - alpha * Ad[q];
             r[q] = rv;
             acc += rv * rv;
+            if (b32) {
+                // the next FP32 V-cycle's right-hand side and zero initial iterate
+                b32[q] = (float)rv;
+                x32[q] = 0.f;
+            }
         }
     }
     const double s = block_sum<BS>(acc);
@@ -608,8 +614,8 @@ void launch_cg_direction(const Geom &g, const double *s, double *d, const double
 }
 
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
-                      double *partials, cudaStream_t st) {
-    launch_pdl(cg_update_kernel, REDUCE_BLOCKS, BS, 0, st, g, x, r, d, Ad, sc, partials);
+                      double *partials, cudaStream_t st, float *b32, float *x32) {
+    launch_pdl(cg_update_kernel, REDUCE_BLOCKS, BS, 0, st, g, x, r, d, Ad, sc, partials, b32, x32);
     VFEM_LAUNCH_CHECK();
 }
 

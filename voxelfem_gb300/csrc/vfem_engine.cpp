@@ -823,21 +823,33 @@ void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
 // Preconditioner s = M^{-1} r (MultigridSolver.hh:547-580): zero initial guess,
 // residual system, mgIter V-cycles (or FMG + mgIter-1 V-cycles).
 template <typename T>
-void MG::preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg) {
+void MG::preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg, bool prepared) {
     cudaStream_t st = fine->stream;
     if (sweeps == 0) return;  // applyPreconditionerInv returns without touching the MG iterate
     auto &D = lv[0].data<T>();
     const int64_t n3 = 3 * lv[0].g.NN;
-    launch_fill<T>(D.x.p, T(0), n3, st);
-    if (mgIter == 0) return;
-    if (std::is_same<T, double>::value) launch_copy((double *)D.b.p, r, n3, st);
-    else launch_cast<float, double>(r, (float *)D.b.p, n3, st);
+    if (!prepared) {
+        launch_fill<T>(D.x.p, T(0), n3, st);
+        if (mgIter == 0) return;
+        if (std::is_same<T, double>::value) launch_copy((double *)D.b.p, r, n3, st);
+        else launch_cast<float, double>(r, (float *)D.b.p, n3, st);
+    }
     if (fmg) {
         fmgT<T>(0, sweeps, true);
         for (int64_t i = 1; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
     } else {
         for (int64_t i = 0; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
     }
+}
+
+void MG::prepareFusedInit(int64_t mgIter, int64_t sweeps) {
+    fusedInitOn = precision == PREC_MIXED && mgIter > 0 && sweeps > 0;
+    if (!fusedInitOn) return;
+    allocLevels();
+    auto &D = lv[0].d32;
+    const int64_t n3 = 3 * lv[0].g.NN;
+    launch_fill<float>(D.x.p, 0.f, n3, fine->stream);
+    launch_cast<float, double>(rbuf.p, D.b.p, n3, fine->stream);
 }
 
 // One PCG iteration (MultigridSolver.hh:1108-1144), enqueued without host synchronisation.
@@ -849,7 +861,8 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool h
             preconditionT<double>(rbuf.p, mgIter, sweeps, fmg);
             launch_cg_precond_out<double>(g, lv[0].d64.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
         } else {
-            preconditionT<float>(rbuf.p, mgIter, sweeps, fmg);
+            // the previous cg_update (or the solve's start) left b32 = (float) r and x32 = 0
+            preconditionT<float>(rbuf.p, mgIter, sweeps, fmg, fusedInit());
             launch_cg_precond_out<float>(g, lv[0].d32.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
         }
     } else {
@@ -859,7 +872,10 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool h
     outerDirection();
     const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
     launch_cg_alpha(partials.p, nb, sc.p, st);
-    launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
+    if (fusedInit())
+        launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st, lv[0].d32.b.p, lv[0].d32.x.p);
+    else
+        launch_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
     launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
     if (hostMirror) VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
 }
@@ -1015,6 +1031,7 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     launch_masked_dot_partials<double, double>(g, rbuf.p, rbuf.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
     launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
+    prepareFusedInit(mgIter, sweeps);
     launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
     if (precision == PREC_MIXED) {
         fine->youngF();
@@ -1113,6 +1130,7 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
         if (outerKind() == 2) umax.alloc(REDUCE_BLOCKS);
         allocLevels();
     }
+    prepareFusedInit(mgIter, sweeps);
     const GraphKey key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
     bool updated = false;
     int64_t i = 0;

@@ -267,7 +267,12 @@ private:
     template <typename T>
     void fmgT(int l, int64_t sweeps, bool residualSystem);
     template <typename T>
-    void preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg);
+    void preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg, bool prepared = false);
+    // mixed solves: cg_update writes the FP32 V-cycle's b and zero x (set up once per solve by
+    // prepareFusedInit after the initial residual)
+    bool fusedInitOn = false;
+    bool fusedInit() const { return fusedInitOn; }
+    void prepareFusedInit(int64_t mgIter, int64_t sweeps);
     template <typename T>
     void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
     void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror = true);

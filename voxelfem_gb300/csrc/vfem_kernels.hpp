@@ -237,8 +237,11 @@ int launch_applyk_fine_tc(const Geom &g, const float *Yh, const float *Yl, const
                           double *out, const uint16_t *bTiles, double scale, const uint8_t *dmask, bool zeroDirichlet,
                           double *partialDot, int partialBlocks, int *status, cudaStream_t st,
                           const double *rhs = nullptr);
+// b32, x32 (optional): also write (float) r and 0 on the nondetached rows (the next FP32
+// V-cycle's right-hand side and initial iterate)
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
-                      double *partials, cudaStream_t st);
+                      double *partials, cudaStream_t st,
+                      float *b32 = nullptr, float *x32 = nullptr);
 void launch_copy(double *dst, const double *src, int64_t n, cudaStream_t st);
 template <typename T>
 void launch_enforce_dirichlet(const Geom &g, T *u, const uint8_t *dmask, const double *dval, cudaStream_t st);
