@@ -297,6 +297,24 @@ int vfem_q2_set_outer_matvec(vfem_q2 *g, int outer_matvec);
 int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
                 int64_t mg_smoothing_iterations, vfem_pcg_stats *stats);
 
+/* ---------------- Method of Moving Asymptotes (MethodOfMovingAsymptotes.hh; pyOptimizer.MMA,
+ * python_bindings/Optimizer.cc:16-22) ----------------
+ * MMA(numVars, numConstr, xmin, xmax, f, df_dx): the n-length work on the GPU, the (m+1)-sized
+ * dual system on the host. f writes the objective and the m constraint values at x (host
+ * memory); df_dx writes their gradients as an (m+1) x n row-major array. Nonzero returns abort
+ * the step. Device optimiser: 1 <= m <= 3. */
+typedef int (*vfem_mma_f)(void *user, const double *x, int64_t n, double *f_out);
+typedef int (*vfem_mma_df)(void *user, const double *x, int64_t n, double *df_out);
+typedef struct vfem_mma vfem_mma;
+int vfem_mma_create(int64_t num_vars, int num_constraints, const double *xmin, const double *xmax, vfem_mma_f f,
+                    vfem_mma_df df_dx, void *user, vfem_mma **out);
+int vfem_mma_destroy(vfem_mma *o);
+int vfem_mma_set_initial_var(vfem_mma *o, const double *x0);  /* MMA::setInitialVar */
+int vfem_mma_enable_gcmma(vfem_mma *o, int enable);           /* MMA::enableGCMMA */
+int vfem_mma_step(vfem_mma *o);                               /* MMA::step */
+/* MMA::getOptimalVar (not bound by the reference module; the current iterate) */
+int vfem_mma_get_optimal_var(vfem_mma *o, double *x_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -295,3 +295,26 @@ def test_oracle_layer_by_layer_warm_starts():
         assert np.max(np.abs(c - cz) / np.abs(cz)) < 1e-8
         assert np.max(np.abs(g - gz)) / np.max(np.abs(gz)) < 1e-6
     assert res["N=3"][2].sum() < iz.sum()
+
+
+def test_oracle_mma_reaches_analytic_optimum():
+    """The numpy restatement of the reference's MMA (and GCMMA) solves a box-constrained quadratic
+    with a volume constraint to its analytic optimum."""
+    from oracle import mma as omma
+    n = 300
+    t = np.random.default_rng(0).uniform(0.1, 0.9, n)
+    f = lambda x: np.array([np.sum((x - t) ** 2), np.mean(x) / 0.4 - 1.0])
+    df = lambda x: np.vstack([2 * (x - t), np.full(n, 1.0 / (0.4 * n))])
+    lo, hi = 0.0, 10.0
+    for _ in range(200):
+        lam = 0.5 * (lo + hi)
+        lo, hi = (lam, hi) if np.clip(t - lam, 0, 1).mean() > 0.4 else (lo, lam)
+    fs = f(np.clip(t - lam, 0, 1))[0]
+    for gc in (False, True):
+        o = omma.MMA(n, 1, np.zeros(n), np.ones(n), f, df)
+        o.enableGCMMA(gc)
+        o.setInitialVar(np.full(n, 0.5))
+        for _ in range(15):
+            o.step()
+        x = o.getOptimalVar()
+        assert abs(f(x)[0] - fs) < 1e-5 * fs and f(x)[1] < 1e-6

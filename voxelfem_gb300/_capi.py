@@ -81,6 +81,12 @@ _SIGS = {
     "vfem_lbl_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
                                _vp, _vp, _vp]),
     "vfem_lbl_set_init": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "vfem_mma_create": (C.c_int, [C.c_int64, C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(C.c_void_p)]),
+    "vfem_mma_destroy": (C.c_int, [_vp]),
+    "vfem_mma_set_initial_var": (C.c_int, [_vp, _vp]),
+    "vfem_mma_enable_gcmma": (C.c_int, [_vp, C.c_int]),
+    "vfem_mma_step": (C.c_int, [_vp]),
+    "vfem_mma_get_optimal_var": (C.c_int, [_vp, _vp]),
     "vfem_grid_element_energy": (C.c_int, [_vp, _vp, _vp]),
     "vfem_mg_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "vfem_mg_destroy": (C.c_int, [_vp]),

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "vfem_engine.hpp"
+#include "vfem_mma.hpp"
 
 using namespace vfem;
 
@@ -602,3 +603,49 @@ int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double
 }
 
 }  // extern "C"
+
+// ---------------- Method of Moving Asymptotes ----------------
+struct vfem_mma {
+    vfem::MMAOpt o;
+    vfem_mma(int64_t n, int m, const double *xmin, const double *xmax, vfem_mma_f f, vfem_mma_df df, void *user)
+        : o(n, m, xmin, xmax, f, df, user) {}
+};
+int vfem_mma_create(int64_t num_vars, int num_constraints, const double *xmin, const double *xmax, vfem_mma_f f,
+                    vfem_mma_df df_dx, void *user, vfem_mma **out) {
+    return guarded([&] {
+        need(xmin, "xmin");
+        need(xmax, "xmax");
+        if (!f || !df_dx) throw vfem::Error(vfem::ERR_ARG, "f and df_dx callbacks are required");
+        need(out, "out");
+        *out = new vfem_mma(num_vars, num_constraints, xmin, xmax, f, df_dx, user);
+    });
+}
+int vfem_mma_destroy(vfem_mma *o) {
+    return guarded([&] { delete o; });
+}
+int vfem_mma_set_initial_var(vfem_mma *o, const double *x0) {
+    return guarded([&] {
+        need(o, "optimizer");
+        need(x0, "x0");
+        o->o.setInitialVar(x0);
+    });
+}
+int vfem_mma_enable_gcmma(vfem_mma *o, int enable) {
+    return guarded([&] {
+        need(o, "optimizer");
+        o->o.gcmma = enable != 0;
+    });
+}
+int vfem_mma_step(vfem_mma *o) {
+    return guarded([&] {
+        need(o, "optimizer");
+        o->o.step();
+    });
+}
+int vfem_mma_get_optimal_var(vfem_mma *o, double *x_out) {
+    return guarded([&] {
+        need(o, "optimizer");
+        need(x_out, "x");
+        o->o.getOptimalVar(x_out);
+    });
+}

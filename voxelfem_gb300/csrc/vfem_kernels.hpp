@@ -222,6 +222,42 @@ void launch_subspace_solve(const double *partials, int nb, int s, double *c, cud
 void launch_subspace_combine(const Geom &g, const LblVectors &U, int s, const double *cDev, const LblCoeffs &cv,
                              double *x, cudaStream_t st);
 
+// ---------------- Method of Moving Asymptotes (k_mma.cu) ----------------
+// Row-major (m+1) x n arrays for df, p, q and m x n for G; partials are K rows of
+// mma_blocks(n) entries.
+constexpr int MMA_MAX_M = 3;      // constraints handled on the device
+constexpr int MMA_MAX_ROWS = 12;  // partial rows of one kernel (>= m(m+1)/2 + m + 3)
+struct MmaRows {
+    double v[MMA_MAX_ROWS];
+};
+unsigned mma_blocks(int64_t n);
+void launch_mma_bounds(int64_t n, int mode, const double *x0, const double *x1, const double *x2, const double *xmin,
+                       const double *xmax, double *l, double *u, double *alpha, double *beta, cudaStream_t st);
+void launch_mma_pq(int64_t n, int m1, const double *x, const double *u, const double *l, const double *xmin,
+                   const double *xmax, const double *df, bool gcmma, const MmaRows &rho, double *p, double *q,
+                   double *partials, cudaStream_t st);
+void launch_mma_absdf(int64_t n, int m1, const double *df, const double *xmin, const double *xmax, double *partials,
+                      cudaStream_t st);
+void launch_mma_eval(int64_t n, int m1, const double *x, const double *xk, const double *u, const double *l,
+                     const double *xmin, const double *xmax, const double *p, const double *q, double *partials,
+                     cudaStream_t st);
+void launch_mma_sub_init(int64_t n, int m, const double *alpha, const double *beta, const double *u, const double *l,
+                         const double *p, const double *q, double *x, double *xi, double *eta, double *partials,
+                         cudaStream_t st);
+void launch_mma_sub_dir1(int64_t n, int m, double eps, const MmaRows &lam, const double *x, const double *xi,
+                         const double *eta, const double *alpha, const double *beta, const double *u, const double *l,
+                         const double *p, const double *q, double *dx, double *Dx, double *G, double *partials,
+                         cudaStream_t st);
+void launch_mma_sub_dir2(int64_t n, int m, double eps, const MmaRows &dlam, const double *x, const double *xi,
+                         const double *eta, const double *alpha, const double *beta, const double *dx,
+                         const double *Dx, const double *G, double *ddx, double *dxi, double *deta, double *partials,
+                         cudaStream_t st);
+void launch_mma_sub_move(int64_t n, int m, double step, double eps, const MmaRows &lam, double *x, double *xi,
+                         double *eta, const double *ddx, const double *dxi, const double *deta, const double *alpha,
+                         const double *beta, const double *u, const double *l, const double *p, const double *q,
+                         double *partials, cudaStream_t st);
+void launch_mma_rows_reduce(const double *partials, int K, int nsum, int nb, double *out, cudaStream_t st);
+
 // ---------------- tensor-core outer matvec (k_tc.cu) ----------------
 // K0 = scale * C with C an integer matrix whose row sums keep the bf16 MMA accumulators exact;
 // fills the B tiles (2048 bf16). False when K0 has no such form.
