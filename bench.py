@@ -434,6 +434,8 @@ def run_ours(args):
         line["lbl"] = run_lbl()
     if rank == 0 and ws == 1 and not args.no_q2:
         line["q2"] = run_q2(hbm)
+    if rank == 0 and ws == 1 and not args.no_mma:
+        line["mma"] = run_mma(args.no_cpu)
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
     if rank == 0:
@@ -524,6 +526,51 @@ def run_lbl(slots_list=(1, 8, 16)):
 
 
 Q2_NE = (128, 128, 128)
+
+
+MMA_N = 192 * 96 * 96  # the 192x96x96 MBB design's element count
+
+
+def run_mma(no_cpu):
+    """One MMA step (and one GCMMA step) on 1,769,472 variables with one volume-type constraint:
+    a box-constrained quadratic objective, x0 = 0.5, callbacks evaluated in numpy on the host
+    (the reference's interface). Wall time per step from the second step on; the CPU leg runs
+    the oracle's numpy restatement of the same algorithm on one step."""
+    from voxelfem_gb300 import pyOptimizer
+
+    n = MMA_N
+    t = np.random.default_rng(0).uniform(0.1, 0.9, n)
+    calls = {"f": 0, "df": 0}
+
+    def f(x):
+        calls["f"] += 1
+        return np.array([np.sum((x - t) ** 2), np.mean(x) / 0.3 - 1.0])
+
+    def df(x):
+        calls["df"] += 1
+        return np.vstack([2 * (x - t), np.full(n, 1.0 / (0.3 * n))])
+
+    out = {"workload": "MMA, n = %d, m = 1, quadratic objective, host callbacks" % n}
+    for name, gc in (("mma", False), ("gcmma", True)):
+        g = pyOptimizer.MMA(n, 1, np.zeros(n), np.ones(n), f, df)
+        g.enableGCMMA(gc)
+        g.setInitialVar(np.full(n, 0.5))
+        g.step()
+        t0 = time.perf_counter()
+        steps = 3
+        for _ in range(steps):
+            g.step()
+        out[name + "_s_per_step"] = (time.perf_counter() - t0) / steps
+        out[name + "_objective"] = float(f(g.getOptimalVar())[0])
+    if not no_cpu:
+        from oracle import mma as omma
+        o = omma.MMA(n, 1, np.zeros(n), np.ones(n), f, df)
+        o.setInitialVar(np.full(n, 0.5))
+        o.step()
+        t0 = time.perf_counter()
+        o.step()
+        out["cpu_oracle_numpy_s_per_step"] = time.perf_counter() - t0
+    return out
 
 
 def run_q2(hbm, solve=True):
@@ -618,6 +665,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-lbl", action="store_true", help="skip the layer-by-layer batching measurement")
     ap.add_argument("--no-q2", action="store_true", help="skip the triquadratic applyK measurement")
+    ap.add_argument("--no-mma", action="store_true", help="skip the MMA optimiser measurement")
     ap.add_argument("--host-loop", action="store_true",
                     help="iterate PCG from the host (one graph per iteration) instead of the device-resident loop")
     ap.add_argument("--kernel-case", type=int, default=None,

@@ -315,6 +315,22 @@ int vfem_mma_step(vfem_mma *o);                               /* MMA::step */
 /* MMA::getOptimalVar (not bound by the reference module; the current iterate) */
 int vfem_mma_get_optimal_var(vfem_mma *o, double *x_out);
 
+/* ---------------- further filters (TopologyOptimizationFilter.hh:402-709) ----------------
+ * UpsampleFilter(factor): in_dims coarse nodes -> (in_dims - 1) * factor + 1 fine nodes,
+ * trilinear; VertexToCellFilter: vertex_dims -> vertex_dims - 1 cells, corner mean;
+ * LangelaarFilter: the overhang filter along y, stateful like the reference's (its output buffer
+ * enters the next application through the own-voxel term of the supporting region; backprop
+ * uses the smax and filtered values of the last application). Arrays host or device. */
+int vfem_upsample_filter(const int64_t in_dims[3], int64_t factor, const double *in, double *out);
+int vfem_upsample_filter_backprop(const int64_t in_dims[3], int64_t factor, const double *g, double *out);
+int vfem_vertex_to_cell_filter(const int64_t vertex_dims[3], const double *in, double *out);
+int vfem_vertex_to_cell_filter_backprop(const int64_t vertex_dims[3], const double *g, double *out);
+typedef struct vfem_langelaar vfem_langelaar;
+int vfem_langelaar_create(const int64_t dims[3], vfem_langelaar **out);
+int vfem_langelaar_destroy(vfem_langelaar *h);
+int vfem_langelaar_apply(vfem_langelaar *h, const double *in, double *out);
+int vfem_langelaar_backprop(vfem_langelaar *h, const double *g, const double *vars, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -318,3 +318,23 @@ def test_oracle_mma_reaches_analytic_optimum():
             o.step()
         x = o.getOptimalVar()
         assert abs(f(x)[0] - fs) < 1e-5 * fs and f(x)[1] < 1e-6
+
+
+def test_oracle_filters_adjoint():
+    """The oracle's upsample and vertex-to-cell restatements are adjoint to their backprops;
+    upsampling reproduces trilinear fields exactly."""
+    from oracle import filters as of
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0, 1, (3, 4, 3))
+    for F in (1, 2, 3):
+        y = of.upsample(x, F)
+        g = rng.standard_normal(y.shape)
+        assert abs(np.sum(y * g) - np.sum(x * of.upsample_backprop(g, x.shape, F))) < 1e-12
+    i, j, k = np.meshgrid(np.arange(3), np.arange(4), np.arange(3), indexing="ij")
+    lin = 0.3 * i - 0.2 * j + 0.7 * k + 0.1 * i * j * k
+    fi, fj, fk = np.meshgrid(np.arange(5) / 2, np.arange(7) / 2, np.arange(5) / 2, indexing="ij")
+    assert np.max(np.abs(of.upsample(lin, 2) - (0.3 * fi - 0.2 * fj + 0.7 * fk + 0.1 * fi * fj * fk))) < 1e-14
+    v = rng.uniform(0, 1, (4, 5, 3))
+    c = of.vertex_to_cell(v)
+    g = rng.standard_normal(c.shape)
+    assert abs(np.sum(c * g) - np.sum(v * of.vertex_to_cell_backprop(g))) < 1e-12

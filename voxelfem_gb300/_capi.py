@@ -87,6 +87,14 @@ _SIGS = {
     "vfem_mma_enable_gcmma": (C.c_int, [_vp, C.c_int]),
     "vfem_mma_step": (C.c_int, [_vp]),
     "vfem_mma_get_optimal_var": (C.c_int, [_vp, _vp]),
+    "vfem_upsample_filter": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
+    "vfem_upsample_filter_backprop": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
+    "vfem_vertex_to_cell_filter": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_vertex_to_cell_filter_backprop": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_langelaar_create": (C.c_int, [_vp, C.POINTER(C.c_void_p)]),
+    "vfem_langelaar_destroy": (C.c_int, [_vp]),
+    "vfem_langelaar_apply": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_langelaar_backprop": (C.c_int, [_vp, _vp, _vp, _vp]),
     "vfem_grid_element_energy": (C.c_int, [_vp, _vp, _vp]),
     "vfem_mg_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "vfem_mg_destroy": (C.c_int, [_vp]),

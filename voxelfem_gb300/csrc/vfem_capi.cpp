@@ -649,3 +649,115 @@ int vfem_mma_get_optimal_var(vfem_mma *o, double *x_out) {
         o->o.getOptimalVar(x_out);
     });
 }
+
+// ---------------- Upsample / VertexToCell / Langelaar filters ----------------
+namespace {
+void dims3(const int64_t d[3], int out[3], int minimum, const char *msg) {
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] < minimum || d[a] > (int64_t)1 << 30) throw vfem::Error(vfem::ERR_ARG, msg);
+        out[a] = (int)d[a];
+    }
+}
+// run a filter kernel on caller arrays (host or device) of nin and nout doubles
+template <typename F>
+void filter_call(const double *in, int64_t nin, double *out, int64_t nout, F launch) {
+    vfem::View vi, vo;
+    vfem::viewIn(vi, in, nin * sizeof(double), 0);
+    vfem::viewOut(vo, out, nout * sizeof(double));
+    launch((const double *)vi.d, (double *)vo.d);
+    vfem::finishOut(vo, 0);
+    VFEM_CUDA(cudaDeviceSynchronize());
+}
+int64_t prod3(const int d[3]) { return (int64_t)d[0] * d[1] * d[2]; }
+}  // namespace
+
+int vfem_upsample_filter(const int64_t in_dims[3], int64_t factor, const double *in, double *out) {
+    return guarded([&] {
+        need(in, "in");
+        need(out, "out");
+        int d[3];
+        dims3(in_dims, d, 2, "Interpolation can only be applied to a 2^d grid or larger");
+        if (factor < 1) throw vfem::Error(vfem::ERR_ARG, "factor must be positive");
+        const int F = (int)factor;
+        const int o[3] = {(d[0] - 1) * F + 1, (d[1] - 1) * F + 1, (d[2] - 1) * F + 1};
+        filter_call(in, prod3(d), out, prod3(o), [&](const double *a, double *b) { vfem::launch_upsample(d, F, a, b, 0); });
+    });
+}
+int vfem_upsample_filter_backprop(const int64_t in_dims[3], int64_t factor, const double *g, double *out) {
+    return guarded([&] {
+        need(g, "g");
+        need(out, "out");
+        int d[3];
+        dims3(in_dims, d, 2, "Interpolation can only be applied to a 2^d grid or larger");
+        if (factor < 1) throw vfem::Error(vfem::ERR_ARG, "factor must be positive");
+        const int F = (int)factor;
+        const int o[3] = {(d[0] - 1) * F + 1, (d[1] - 1) * F + 1, (d[2] - 1) * F + 1};
+        filter_call(g, prod3(o), out, prod3(d), [&](const double *a, double *b) { vfem::launch_upsample_backprop(d, F, a, b, 0); });
+    });
+}
+int vfem_vertex_to_cell_filter(const int64_t vertex_dims[3], const double *in, double *out) {
+    return guarded([&] {
+        need(in, "in");
+        need(out, "out");
+        int d[3];
+        dims3(vertex_dims, d, 2, "Input grid must be 2^d or larger.");
+        const int e[3] = {d[0] - 1, d[1] - 1, d[2] - 1};
+        filter_call(in, prod3(d), out, prod3(e), [&](const double *a, double *b) { vfem::launch_vertex_to_cell(d, a, b, 0); });
+    });
+}
+int vfem_vertex_to_cell_filter_backprop(const int64_t vertex_dims[3], const double *g, double *out) {
+    return guarded([&] {
+        need(g, "g");
+        need(out, "out");
+        int d[3];
+        dims3(vertex_dims, d, 2, "Input grid must be 2^d or larger.");
+        const int e[3] = {d[0] - 1, d[1] - 1, d[2] - 1};
+        filter_call(g, prod3(e), out, prod3(d), [&](const double *a, double *b) { vfem::launch_vertex_to_cell_backprop(d, a, b, 0); });
+    });
+}
+
+struct vfem_langelaar {
+    int d[3];
+    int64_t n;
+    vfem::DevBuf<double> out, smax, filt, lam, vars, g;
+};
+int vfem_langelaar_create(const int64_t dims[3], vfem_langelaar **h) {
+    return guarded([&] {
+        need(h, "handle");
+        auto f = std::make_unique<vfem_langelaar>();
+        dims3(dims, f->d, 1, "invalid grid dimensions");
+        f->n = prod3(f->d);
+        for (auto *b : {&f->out, &f->smax, &f->filt, &f->lam, &f->vars, &f->g}) b->alloc(f->n);
+        VFEM_CUDA(cudaMemset(f->out.p, 0, f->n * sizeof(double)));
+        VFEM_CUDA(cudaMemset(f->smax.p, 0, f->n * sizeof(double)));
+        VFEM_CUDA(cudaMemset(f->filt.p, 0, f->n * sizeof(double)));
+        *h = f.release();
+    });
+}
+int vfem_langelaar_destroy(vfem_langelaar *h) {
+    return guarded([&] { delete h; });
+}
+int vfem_langelaar_apply(vfem_langelaar *h, const double *in, double *out) {
+    return guarded([&] {
+        need(h, "handle");
+        need(in, "in");
+        need(out, "out");
+        VFEM_CUDA(cudaMemcpy(h->vars.p, in, h->n * sizeof(double), cudaMemcpyDefault));
+        vfem::launch_langelaar(h->d, h->vars.p, h->out.p, h->smax.p, 0);
+        VFEM_CUDA(cudaMemcpy(h->filt.p, h->out.p, h->n * sizeof(double), cudaMemcpyDeviceToDevice));
+        VFEM_CUDA(cudaMemcpy(out, h->out.p, h->n * sizeof(double), cudaMemcpyDefault));
+    });
+}
+int vfem_langelaar_backprop(vfem_langelaar *h, const double *g, const double *vars, double *out) {
+    return guarded([&] {
+        need(h, "handle");
+        need(g, "g");
+        need(vars, "vars");
+        need(out, "out");
+        VFEM_CUDA(cudaMemcpy(h->g.p, g, h->n * sizeof(double), cudaMemcpyDefault));
+        VFEM_CUDA(cudaMemcpy(h->vars.p, vars, h->n * sizeof(double), cudaMemcpyDefault));
+        vfem::DevBuf<double> res(h->n);
+        vfem::launch_langelaar_backprop(h->d, h->g.p, h->vars.p, h->filt.p, h->smax.p, h->lam.p, res.p, 0);
+        VFEM_CUDA(cudaMemcpy(out, res.p, h->n * sizeof(double), cudaMemcpyDefault));
+    });
+}

@@ -222,6 +222,17 @@ void launch_subspace_solve(const double *partials, int nb, int s, double *c, cud
 void launch_subspace_combine(const Geom &g, const LblVectors &U, int s, const double *cDev, const LblCoeffs &cv,
                              double *x, cudaStream_t st);
 
+// ---------------- further density filters (k_filters.cu) ----------------
+// dims: the input grid (Upsample: coarse nodes; VertexToCell: vertices; Langelaar: cells)
+void launch_upsample(const int dims[3], int factor, const double *in, double *out, cudaStream_t st);
+void launch_upsample_backprop(const int dims[3], int factor, const double *g, double *out, cudaStream_t st);
+void launch_vertex_to_cell(const int vdims[3], const double *in, double *out, cudaStream_t st);
+void launch_vertex_to_cell_backprop(const int vdims[3], const double *g, double *out, cudaStream_t st);
+// out: the previous output on entry (the own-voxel term of the supporting region); smax: cached
+void launch_langelaar(const int dims[3], const double *in, double *out, double *smax, cudaStream_t st);
+void launch_langelaar_backprop(const int dims[3], const double *g, const double *vars, const double *filt,
+                               const double *smax, double *lam, double *out, cudaStream_t st);
+
 // ---------------- Method of Moving Asymptotes (k_mma.cu) ----------------
 // Row-major (m+1) x n arrays for df, p, q and m x n for G; partials are K rows of
 // mma_blocks(n) entries.

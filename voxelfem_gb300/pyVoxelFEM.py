@@ -660,6 +660,12 @@ class ProjectionFilter(Filter):
 
     setOutputDimensions = setInputDimensions
 
+    @property
+    def inputDimensions(self):
+        return np.array(self._dims)
+
+    outputDimensions = inputDimensions
+
     def apply(self, x):
         a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
         out = np.empty_like(a)
@@ -679,25 +685,171 @@ class ProjectionFilter(Filter):
         return np.arctanh((2 * filteredValue - 1) * np.tanh(0.5 * self._beta)) / self._beta + 0.5
 
 
+class _ReshapingFilter(Filter):
+    """Dimension bookkeeping of the filters that change the grid size."""
+
+    def _set(self, inDims, outDims):
+        self._in = tuple(int(v) for v in inDims)
+        self._out = tuple(int(v) for v in outDims)
+
+    @property
+    def inputDimensions(self):
+        return np.array(self._in)
+
+    @property
+    def outputDimensions(self):
+        return np.array(self._out)
+
+    def _need(self):
+        if getattr(self, "_in", None) is None:
+            raise RuntimeError("Filter grid dimensions not set. Initialize a TopologyOptimizationProblem object "
+                               "with this filter before using it.")
+
+
+class UpsampleFilter(_ReshapingFilter):
+    """UpsampleFilter(factor=2) (TopologyOptimizationFilter.hh:402-505): trilinear upsampling of a
+    node-valued grid from s to (s - 1) * factor + 1 values per axis."""
+
+    def __init__(self, factor=2):
+        self.factor = int(factor)
+        self._in = None
+
+    def setInputDimensions(self, gridDims):
+        d = np.asarray(gridDims, dtype=np.int64)
+        if (d < 2).any():
+            raise RuntimeError("Interpolation can only be applied to a 2^d grid or larger")
+        self._set(d, (d - 1) * self.factor + 1)
+
+    def setOutputDimensions(self, gridDims):
+        d = np.asarray(gridDims, dtype=np.int64)
+        if (d < 2).any():
+            raise RuntimeError("Interpolation can only be applied to a 2^d grid or larger")
+        i = (d - 1) // self.factor + 1
+        if ((i - 1) * self.factor + 1 != d).any():
+            raise RuntimeError("Output size is not divisible by factor")
+        self._set(i, d)
+
+    def apply(self, x):
+        self._need()
+        a = _as_elems(x, int(np.prod(self._in)))
+        out = np.empty(int(np.prod(self._out)))
+        dims = np.array(self._in, dtype=np.int64)
+        check(_lib().vfem_upsample_filter(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
+        return out
+
+    def backprop(self, g, vars_=None):
+        self._need()
+        a = _as_elems(g, int(np.prod(self._out)))
+        out = np.empty(int(np.prod(self._in)))
+        dims = np.array(self._in, dtype=np.int64)
+        check(_lib().vfem_upsample_filter_backprop(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
+        return out
+
+
+class VertexToCellFilter(_ReshapingFilter):
+    """VertexToCellFilter (TopologyOptimizationFilter.hh:507-575): cell value = mean of its
+    corner values (vertex grid s -> cell grid s - 1)."""
+
+    def __init__(self):
+        self._in = None
+
+    def setInputDimensions(self, gridDims):
+        d = np.asarray(gridDims, dtype=np.int64)
+        if (d < 2).any():
+            raise RuntimeError("Input grid must be 2^d or larger.")
+        self._set(d, d - 1)
+
+    def setOutputDimensions(self, gridDims):
+        d = np.asarray(gridDims, dtype=np.int64)
+        self._set(d + 1, d)
+
+    def apply(self, x):
+        self._need()
+        a = _as_elems(x, int(np.prod(self._in)))
+        out = np.empty(int(np.prod(self._out)))
+        dims = np.array(self._in, dtype=np.int64)
+        check(_lib().vfem_vertex_to_cell_filter(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
+        return out
+
+    def backprop(self, g, vars_=None):
+        self._need()
+        a = _as_elems(g, int(np.prod(self._out)))
+        out = np.empty(int(np.prod(self._in)))
+        dims = np.array(self._in, dtype=np.int64)
+        check(_lib().vfem_vertex_to_cell_filter_backprop(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
+        return out
+
+
+class LangelaarFilter(_ReshapingFilter):
+    """LangelaarFilter (TopologyOptimizationFilter.hh:577-709): the additive-manufacturing
+    overhang filter along the build direction y. Stateful like the reference's: its previous
+    output enters the own-voxel term of each supporting region, and backprop uses the smax and
+    filtered values of the last apply."""
+
+    def __init__(self):
+        self._in = None
+        self._h = None
+
+    def setInputDimensions(self, gridDims):
+        self._set(gridDims, gridDims)
+        self._release()
+        h = C.c_void_p()
+        dims = np.array(self._in, dtype=np.int64)
+        check(_lib().vfem_langelaar_create(dims.ctypes.data_as(_capi._i64), C.byref(h)))
+        self._h = h
+
+    setOutputDimensions = setInputDimensions
+
+    def _release(self):
+        if getattr(self, "_h", None) is not None and _capi._lib is not None:
+            _capi._lib.vfem_langelaar_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        self._release()
+
+    def apply(self, x):
+        self._need()
+        a = _as_elems(x, int(np.prod(self._in)))
+        out = np.empty_like(a)
+        check(_lib().vfem_langelaar_apply(self._h, ptr(a), ptr(out)))
+        return out
+
+    def backprop(self, g, vars_):
+        self._need()
+        a = _as_elems(g, int(np.prod(self._in)))
+        v = _as_elems(vars_, int(np.prod(self._in)))
+        out = np.empty_like(a)
+        check(_lib().vfem_langelaar_backprop(self._h, ptr(a), ptr(v), ptr(out)))
+        return out
+
+
 class FilterChain:
-    """FilterChain (TopologyOptimizationFilter.hh:90-187), host-side composition of device filters."""
+    """FilterChain (TopologyOptimizationFilter.hh:90-187), host-side composition of device filters.
+    The chain produces a density grid of outGridDimensions; dimension-changing filters
+    (UpsampleFilter, VertexToCellFilter) are sized backwards from it, like the reference."""
 
     def __init__(self, filters, outGridDimensions):
         self.filters = list(filters)
-        for f in self.filters:
-            f.setInputDimensions(outGridDimensions)
-        self._dims = tuple(int(v) for v in outGridDimensions)
+        dims = tuple(int(v) for v in outGridDimensions)
+        self._out = dims
+        for f in reversed(self.filters):
+            f.setOutputDimensions(dims)
+            dims = tuple(int(v) for v in f.inputDimensions)
+        self._dims = dims
         self._vars = None
 
     def numVars(self):
         return int(np.prod(self._dims))
 
-    numPhysicalVars = numVars
+    def numPhysicalVars(self):
+        return int(np.prod(self._out))
 
     def gridDims(self):
         return np.array(self._dims)
 
-    physicalGridDims = gridDims
+    def physicalGridDims(self):
+        return np.array(self._out)
 
     def setDesignVars(self, xDesign):
         v = [_as_elems(xDesign, self.numVars())]
@@ -712,7 +864,7 @@ class FilterChain:
         return self._vars[-1].copy()
 
     def backprop(self, g):
-        g = _as_elems(g, self.numVars())
+        g = _as_elems(g, self.numPhysicalVars())
         for i in range(len(self.filters) - 1, -1, -1):
             g = self.filters[i].backprop(g, self._vars[i])
         return g
