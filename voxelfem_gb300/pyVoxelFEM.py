@@ -222,6 +222,173 @@ class TensorProductSimulator_3D:
     def elementStiffnessMatrix(self, ei):
         return self.elementYoungModulusScaleFactor(ei) * self.fullDensityElementStiffnessMatrix()
 
+    def clearCachedElementStiffness(self):
+        """No per-element stiffness cache exists here (elements are scaled copies of K0)."""
+
+    # --- mesh, sampling and BC fields (TensorProductSimulator.hh:689-712, 746-778, 1161-1179) ---
+    def mesh(self):
+        return self
+
+    def getMesh(self):
+        """(V, F): node positions (nn, 3) and hexahedra (ne, 8) in Gmsh node order."""
+        nn = self.NbNodesPerDimension
+        I, J, K = np.meshgrid(np.arange(nn[0]), np.arange(nn[1]), np.arange(nn[2]), indexing="ij")
+        V = self._bbox[0] + np.stack([I.ravel(), J.ravel(), K.ravel()], axis=1) * self.dx
+        ne = self._ne
+        i, j, k = np.meshgrid(np.arange(ne[0]), np.arange(ne[1]), np.arange(ne[2]), indexing="ij")
+        base = (i.ravel() * nn[1] + j.ravel()) * nn[2] + k.ravel()
+        off = [(l >> 2 & 1) * nn[1] * nn[2] + (l >> 1 & 1) * nn[2] + (l & 1) for l in range(8)]
+        order = [0, 1, 3, 2, 4, 5, 7, 6]  # pairs (0,1), (3,2), (4,5), (7,6)
+        F = np.stack([base + off[l] for l in order], axis=1)
+        return V, F
+
+    def sampleNodalField(self, u, p):
+        """Trilinear interpolation of the nodal field u (nn x c) at the rows of p, each point
+        clamped into the domain first."""
+        u = np.asarray(u, dtype=np.float64).reshape(self._nn, -1)
+        p = np.clip(np.atleast_2d(np.asarray(p, dtype=np.float64)), self._bbox[0], self._bbox[1])
+        t = (p - self._bbox[0]) / self.dx
+        e = np.minimum(np.floor(t).astype(np.int64), np.array(self._ne) - 1)
+        x = t - e
+        nn = self.NbNodesPerDimension
+        out = np.zeros((p.shape[0], u.shape[1]))
+        for l in range(8):
+            b = [(l >> 2) & 1, (l >> 1) & 1, l & 1]
+            w = np.prod([x[:, d] if b[d] else 1.0 - x[:, d] for d in range(3)], axis=0)
+            n = ((e[:, 0] + b[0]) * nn[1] + e[:, 1] + b[1]) * nn[2] + e[:, 2] + b[2]
+            out += w[:, None] * u[n]
+        return out
+
+    def getBCIndicatorField(self):
+        """Per node: Dirichlet component bits + 8 x force component bits."""
+        d = self.getDirichletMask()
+        f = self.getForceMask()
+        return (d[:, 0] * 1 + d[:, 1] * 2 + d[:, 2] * 4 + 8 * (f[:, 0] * 1 + f[:, 1] * 2 + f[:, 2] * 4)).astype(np.float64)
+
+    def getK(self):
+        """The assembled stiffness matrix (3 nn x 3 nn, DOF 3 n + c) as a scipy CSC matrix."""
+        import scipy.sparse as sp
+        K0 = self.fullDensityElementStiffnessMatrix()
+        Y = self.getYoungModulusScaleFactor()
+        ne = self._ne
+        nn = self.NbNodesPerDimension
+        i, j, k = np.meshgrid(np.arange(ne[0]), np.arange(ne[1]), np.arange(ne[2]), indexing="ij")
+        base = (i.ravel() * nn[1] + j.ravel()) * nn[2] + k.ravel()
+        nodes = np.stack([base + (l >> 2 & 1) * nn[1] * nn[2] + (l >> 1 & 1) * nn[2] + (l & 1) for l in range(8)], 1)
+        dofs = (3 * nodes[:, :, None] + np.arange(3)[None, None, :]).reshape(-1, 24)
+        rows = np.repeat(dofs, 24, axis=1).ravel()
+        cols = np.tile(dofs, (1, 24)).ravel()
+        vals = (Y[:, None] * K0.ravel()[None, :]).ravel()
+        return sp.csc_matrix((vals, (rows, cols)), shape=(3 * self._nn, 3 * self._nn))
+
+    def solveWithImposedLoads(self):
+        return self.solve(self.buildLoadVector())
+
+    # --- coarser and intermediate simulators (TensorProductSimulator.hh:793-803, 1852-1992, 1994-2035) ---
+    def _copy_material(self, other):
+        other.ETensor = self.ETensor
+        other.E_min = self.E_min
+        other.E_0 = self.E_0
+        other.gamma = self.gamma
+
+    def downsample(self, downsamplingLevels):
+        """A coarser simulator (elements / 2^levels, same domain and material), no BCs applied."""
+        f = 2 ** int(downsamplingLevels)
+        ne = np.array(self._ne)
+        if (ne % f).any():
+            raise RuntimeError("Grid size must be divisible by 2^downsamplingLevels")
+        c = TensorProductSimulator_3D([self._bbox[0], self._bbox[1]], ne // f)
+        self._copy_material(c)
+        return c
+
+    def _factor(self, coarse):
+        f = self._ne[0] // coarse._ne[0]
+        if any(f * coarse._ne[d] != self._ne[d] for d in range(3)):
+            raise RuntimeError("Invalid downsampled simulator")
+        return f
+
+    def downsampleDensityFieldTo(self, densities, coarseTPS):
+        f = self._factor(coarseTPS)
+        rho = np.asarray(densities, dtype=np.float64).reshape(-1)
+        if rho.size != self._nel:
+            raise RuntimeError("Invalid input densities size (%d vs %d)" % (rho.size, self._nel))
+        a = rho.reshape(self._ne)
+        c = a.reshape(self._ne[0] // f, f, self._ne[1] // f, f, self._ne[2] // f, f).sum(axis=(1, 3, 5)) / f ** 3
+        coarseTPS.setDensities(c.ravel())
+
+    def upsampleDensityGradientFrom(self, coarseTPS, g_coarse):
+        f = self._factor(coarseTPS)
+        g = np.asarray(g_coarse, dtype=np.float64).reshape(-1)
+        if g.size != coarseTPS._nel:
+            raise RuntimeError("Invalid coarse gradient size")
+        gc = g.reshape(coarseTPS._ne)
+        return (np.repeat(np.repeat(np.repeat(gc, f, 0), f, 1), f, 2) / f ** 3).ravel()
+
+    def setDensitiesFromCoarseGrid(self, upscalingFactor, rho):
+        f = int(upscalingFactor)
+        rho = np.asarray(rho, dtype=np.float64).reshape(-1)
+        if self._nel != f ** 3 * rho.size:
+            raise RuntimeError("Incorrect rho size")
+        rc = rho.reshape(tuple(v // f for v in self._ne))
+        self.setDensities(np.repeat(np.repeat(np.repeat(rc, f, 0), f, 1), f, 2).ravel())
+
+    def getIntermediateFabricationShape(self, yfrac, validateBoundaryConditions=True, law=None):
+        """The partial build up to height fraction yfrac along y: same material, the densities of
+        the lower layers, self-weight gravity and the build plate (y = min) fixed."""
+        if yfrac < 0 or yfrac > 1:
+            raise RuntimeError("hfrac is out of bounds")
+        full = self._ne[1]
+        h = int(round(yfrac * full))
+        if abs(yfrac * full - h) > 1e-10:
+            raise RuntimeError("hfrac chops off a noninteger number of element layers")
+        lo, hi = self._bbox[0].copy(), self._bbox[1].copy()
+        hi[1] = lo[1] + yfrac * (self._bbox[1][1] - lo[1])
+        ne = np.array(self._ne)
+        ne[1] = h
+        r = TensorProductSimulator_3D([lo, hi], ne)
+        if law is not None:
+            r.interpolationLaw = law
+        r.ETensor = self.ETensor
+        self.transferDensitiesToIntermediateFabricationShape(r)
+        r.E_min, r.E_0, r.gamma = self.E_min, self.E_0, self.gamma
+        g = self.gravity
+        if not np.any(g):
+            if validateBoundaryConditions:
+                raise RuntimeError("Original simulator has unexpected boundary conditions for layer-by-layer simulation")
+            g = np.array([0.0, -1.0, 0.0])
+        r.gravity = g
+        if validateBoundaryConditions:
+            bad = RuntimeError("Original simulator has unexpected boundary conditions for layer-by-layer simulation")
+            if self.getForceMask().any():
+                raise bad
+            m = self.getDirichletMask()
+            nn = self.NbNodesPerDimension
+            jrow = (np.arange(self._nn) // nn[2]) % nn[1]
+            if not m[jrow == 0].all() or m[jrow != 0].any():
+                raise bad
+        r.addDirichletCondition([0.0, 0.0, 0.0], [lo[0], lo[1], lo[2]], [hi[0], lo[1], hi[2]], "xyz")
+        return r
+
+    def _check_intermediate(self, itps):
+        if itps._ne[0] != self._ne[0] or itps._ne[2] != self._ne[2] or itps._ne[1] > self._ne[1]:
+            raise RuntimeError("Intermediate shape is of unexpected size")
+
+    def transferDensitiesToIntermediateFabricationShape(self, intermediateTPS):
+        rho = self.getDensities().reshape(self._ne)
+        intermediateTPS.setDensities(rho[:, :intermediateTPS._ne[1], :].ravel())
+
+    def transferVFieldToIntermediateFabricationShape(self, intermediateTPS, u):
+        self._check_intermediate(intermediateTPS)
+        nn = self.NbNodesPerDimension
+        u = np.asarray(u, dtype=np.float64).reshape(nn[0], nn[1], nn[2], -1)
+        ny = intermediateTPS._ne[1] + 1
+        return np.asfortranarray(u[:, :ny, :, :].reshape(-1, u.shape[-1]))
+
+    def accumElementScalarFieldFromIntermediateFabricationShape(self, intermediateTPS, rho_in, rho_accum):
+        """rho_accum (this grid's elements, modified in place) += rho_in on the partial build's cells."""
+        acc = rho_accum.reshape(self._ne)
+        acc[:, :intermediateTPS._ne[1], :] += np.asarray(rho_in, dtype=np.float64).reshape(intermediateTPS._ne)
+
     # --- densities ---
     def getDensities(self):
         out = np.empty(self._nel)
