@@ -596,6 +596,11 @@ def run_q2(hbm, solve=True):
         gbs = nbytes.value / (ms.value * 1e-3) / 1e9
         out[name] = {"ms": ms.value, "bytes": nbytes.value, "gbs": gbs, "hbm_frac": gbs / hbm,
                      "tflops": flops / (ms.value * 1e-3) / 1e12}
+    for name, prec, reps in (("smoother_fp32", 1, 3), ("smoother_fp64", 0, 1)):
+        ms, nbytes = C.c_double(), C.c_double()
+        _capi.check(lib.vfem_q2_time_smooth(g._h, prec, reps, C.byref(ms), C.byref(nbytes)))
+        gbs = nbytes.value / (ms.value * 1e-3) / 1e9
+        out[name] = {"ms": ms.value, "bytes": nbytes.value, "gbs": gbs, "hbm_frac": gbs / hbm}
     if solve:
         out["solve"] = run_q2_solve(g, ne)
     return out

@@ -287,6 +287,9 @@ int vfem_q2_interpolate(const int64_t elems_fine[3], const double *coarse, doubl
 /* Benchmark hook (no reference counterpart): average device time of one applyK on resident data and
  * its algorithmic bytes s (6 nn + ne). */
 int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes);
+/* Benchmark hook (no reference counterpart): one forward Gauss-Seidel sweep (27 colours) on
+ * resident data, with its algorithmic bytes s (9 nn + ne). */
+int vfem_q2_time_smooth(vfem_q2 *g, int precision, int reps, double *ms, double *bytes);
 /* preconditionedConjugateGradient on a triquadratic grid (MultigridSolver.hh:1047-1152 recurrences,
  * FP64 outer iteration). The preconditioner is this library's p-multigrid cycle: Q2 block
  * Gauss-Seidel sweeps (mg_smoothing_iterations before and after) around one FP32 V-cycle of the

@@ -593,6 +593,14 @@ int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *
         }
     });
 }
+int vfem_q2_time_smooth(vfem_q2 *g, int precision, int reps, double *ms, double *bytes) {
+    return guarded([&] {
+        need(g, "grid");
+        need(ms, "ms");
+        need(bytes, "bytes");
+        *ms = g->g.timeSmooth(precision, reps, bytes);
+    });
+}
 int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double *bytes) {
     return guarded([&] {
         need(g, "grid");

@@ -368,6 +368,8 @@ public:
     void applyK(const double *u, double *out, int precision, bool zeroDirichlet);
     void smooth(double *u, const double *b, bool forward, int precision);
     double timeApplyK(int precision, int reps, double *bytes);
+    // one forward block Gauss-Seidel sweep (27 colour passes) on resident data; bytes s (9 nn + ne)
+    double timeSmooth(int precision, int reps, double *bytes);
     // PCG on K u = b (zero-displacement supports) with an FP64 outer iteration and a p-multigrid
     // preconditioner: Q2 block Gauss-Seidel smoothing around one FP32 V-cycle of the trilinear
     // problem on the same mesh (`coarsenings` coarsenings); x in/out.

@@ -196,6 +196,33 @@ void GridQ2::smooth(double *u, const double *b, bool forward, int precision) {
     finishOut(vu, stream);
 }
 
+double GridQ2::timeSmooth(int precision, int reps, double *bytes) {
+    if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        auto &D = work<T>();
+        const T *Yt = std::is_same<T, double>::value ? (const T *)Y.p : (const T *)Yf.p;
+        launch_fill<T>(D.x.p, T(0.5), 3 * NN, stream);
+        launch_fill<T>(D.b.p, T(1), 3 * NN, stream);
+        const T *K = kernelK0<T>();
+        launch_gs_q2_sweep<T>(ne, K, Yt, D.x.p, D.b.p, dmask.p, true, stream);
+        cudaEvent_t e0, e1;
+        VFEM_CUDA(cudaEventCreate(&e0));
+        VFEM_CUDA(cudaEventCreate(&e1));
+        VFEM_CUDA(cudaEventRecord(e0, stream));
+        for (int r = 0; r < reps; ++r) launch_gs_q2_sweep<T>(ne, K, Yt, D.x.p, D.b.p, dmask.p, true, stream);
+        VFEM_CUDA(cudaEventRecord(e1, stream));
+        VFEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        VFEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *bytes = (double)sizeof(T) * (9.0 * NN + NE);
+        return (double)ms / reps;
+    };
+    return precision == PREC_FP64 ? run(double()) : run(float());
+}
+
 // Average device time of one applyK launch on resident data, with its algorithmic bytes
 // s * (6 NN + NE) (read u, write K u, read E).
 double GridQ2::timeApplyK(int precision, int reps, double *bytes) {
