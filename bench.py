@@ -44,6 +44,7 @@ CONFIGS = {
 # algorithm and reports its own count in every run.
 FP64_ITERATIONS = {"c2": 16, "c1": 10}
 TOL = 1e-8
+FP32_PEAK_TFLOPS = 74.0  # FFMA-loop probe on this machine's GB300 (dependent-free FMA chains, all SMs)
 KERNEL_NAMES = {0: "applyk_fine_fp64", 1: "applyk_fine_fp32", 2: "applyk_fine_df", 3: "gs_fine_sweep_fp32",
                 4: "gs_fine_sweep_fp64", 5: "residual_fine_fp32", 6: "gs_level1_sweep_fp32",
                 7: "residual_level1_fp32", 8: "gs_level2_sweep_fp32", 9: "residual_level2_fp32",
@@ -402,6 +403,16 @@ def run_ours(args):
                                                  "unit": "TFLOP/s", "peak": bf16,
                                                  "peak_kind": "measured (MEASURED_PEAKS.json bf16 burst)",
                                                  "frac": tflops / bf16 if bf16 else None}
+    # the matrix-free FP32 fine-level kernels are bound by the FP32 pipe: 2 * 24^2 flops per node
+    # (the 8 incident element rows of K0 times u) against the FFMA rate of this GPU
+    for k in ("gs_fine_sweep_fp32", "residual_fine_fp32"):
+        if k in rooflines:
+            flops = 2.0 * 24 * 24 * nn
+            achieved = flops / (kernels[k]["ms"] * 1e-3) / 1e12
+            rooflines[k]["fp32_compute"] = {"flops": flops, "achieved": achieved, "unit": "TFLOP/s",
+                                            "peak": FP32_PEAK_TFLOPS,
+                                            "peak_kind": "measured (FFMA-loop probe on this pool's GB300)",
+                                            "frac": achieved / FP32_PEAK_TFLOPS}
     roofline = dict(rooflines[dom], kernel=dom, peak_kind=peak_kind)
 
     line = {"metric": METRIC, "value": tmix_step if ws == 1 else tmix / (ws * args.steps), "unit": "s",
