@@ -334,6 +334,76 @@ int vfem_langelaar_destroy(vfem_langelaar *h);
 int vfem_langelaar_apply(vfem_langelaar *h, const double *in, double *out);
 int vfem_langelaar_backprop(vfem_langelaar *h, const double *g, const double *vars, double *out);
 
+/* ---------------- 2D: TensorProductSimulator<double, 1, 1> / MultigridSolver<double, 1, 1> ----------------
+ * The bilinear-quadrilateral instantiation the module registers beside the 3D one
+ * (VoxelFEM.cc:413-414, factory TensorProductSimulator([1, 1], bbox, dims)). Nodal fields are
+ * (numNodes, 2) column-major, node (i, j) -> i * ny1 + j; the isotropic elasticity tensor is the
+ * plane-stress one of MeshFEM's ElasticityTensor<Real, 2>::setIsotropic. Each entry point
+ * mirrors the 3D one of the same name (same reference line, same error behaviour). */
+typedef struct vfem_grid2 vfem_grid2; /* TensorProductSimulator<double, 1, 1> */
+typedef struct vfem_mg2 vfem_mg2;     /* MultigridSolver<double, 1, 1> */
+int vfem_grid2_create(const int64_t elems[2], const double bbox_min[2], const double bbox_max[2], vfem_grid2 **out);
+int vfem_grid2_destroy(vfem_grid2 *g);
+int vfem_grid2_dims(const vfem_grid2 *g, int64_t elems[2], int64_t *num_nodes, int64_t *num_elements);
+int vfem_grid2_set_etensor(vfem_grid2 *g, double young, double poisson);
+int vfem_grid2_get_etensor(const vfem_grid2 *g, double *young, double *poisson);
+/* fullDensityElementStiffnessMatrix, 8x8 row-major, DOF 2 l + c with local node l = 2 dx + dy */
+int vfem_grid2_get_k0(const vfem_grid2 *g, double *out64);
+int vfem_grid2_set_material_params(vfem_grid2 *g, double E0, double Emin, double gamma, double q, int law);
+int vfem_grid2_get_material_params(const vfem_grid2 *g, double *E0, double *Emin, double *gamma, double *q, int *law);
+int vfem_grid2_set_densities(vfem_grid2 *g, const double *rho);
+int vfem_grid2_get_densities(vfem_grid2 *g, double *rho_out);
+int vfem_grid2_set_uniform_densities(vfem_grid2 *g, double value);
+int vfem_grid2_get_young_moduli(vfem_grid2 *g, double *out);
+/* component_mask bit c constrains component c ("xy" = 3) */
+int vfem_grid2_add_dirichlet(vfem_grid2 *g, const double u[2], const double min_corner[2], const double max_corner[2],
+                             uint32_t component_mask);
+int vfem_grid2_apply_symmetry(vfem_grid2 *g, const int axes[2], const int max_face[2]);
+int vfem_grid2_set_nodal_forces(vfem_grid2 *g, const double *forces);
+int vfem_grid2_get_dirichlet_mask(const vfem_grid2 *g, uint8_t *mask_out);
+/* Dirichlet values as an (nn, 2) field (getDirichletVarsAndValues, VoxelFEM.cc:93) */
+int vfem_grid2_get_dirichlet_values(const vfem_grid2 *g, double *values_out);
+int vfem_grid2_set_gravity(vfem_grid2 *g, const double gravity[2]);
+int vfem_grid2_get_gravity(const vfem_grid2 *g, double gravity[2]);
+int vfem_grid2_set_mask_layer(vfem_grid2 *g, int64_t layer);
+int vfem_grid2_get_mask_height(const vfem_grid2 *g, double *height);
+int vfem_grid2_apply_k(vfem_grid2 *g, const double *u, double *out);
+int vfem_grid2_build_load(vfem_grid2 *g, double *out);
+int vfem_grid2_compliance_gradient(vfem_grid2 *g, const double *u, double *grad_out);
+int vfem_grid2_adjoint_sensitivity(vfem_grid2 *g, const double *lambda, const double *u, double load_weight,
+                                   double stiffness_weight, double *out);
+int vfem_grid2_element_energy(vfem_grid2 *g, const double *u, double *out);
+int vfem_mg2_create(vfem_grid2 *g, int num_coarsening_levels, vfem_mg2 **out);
+int vfem_mg2_destroy(vfem_mg2 *mg);
+int vfem_mg2_num_levels(const vfem_mg2 *mg, int *levels);
+int vfem_mg2_level_dims(const vfem_mg2 *mg, int level, int64_t elems[2]);
+int vfem_mg2_level_dirichlet_mask(const vfem_mg2 *mg, int level, uint8_t *mask_out);
+int vfem_mg2_set_use_graphs(vfem_mg2 *mg, int use);
+int vfem_mg2_set_symmetric_gs(vfem_mg2 *mg, int symmetric);
+int vfem_mg2_set_mask_layer(vfem_mg2 *mg, int64_t layer);
+int vfem_mg2_update_stiffness(vfem_mg2 *mg);
+int vfem_mg2_apply_k(vfem_mg2 *mg, int level, const double *u, double *out);
+int vfem_mg2_residual(vfem_mg2 *mg, int level, const double *u, const double *b, double *r_out);
+int vfem_mg2_smooth(vfem_mg2 *mg, int level, double *u_inout, const double *b, int forward);
+int vfem_mg2_restrict(vfem_mg2 *mg, int level, const double *fine, double *coarse_out);
+int vfem_mg2_interpolate(vfem_mg2 *mg, int level, const double *coarse, double *fine_inout, int accumulate);
+int vfem_mg2_coarse_solve(vfem_mg2 *mg, const double *b, double *x_out);
+int vfem_mg2_zero_dirichlet(vfem_mg2 *mg, int level, double *u_inout);
+int vfem_mg2_solve(vfem_mg2 *mg, const double *u, const double *f, int64_t num_steps, int64_t num_smoothing_steps,
+                   int zero_dirichlet, int full_multigrid, double *x_out);
+int vfem_mg2_pcg(vfem_mg2 *mg, double *x_inout, const double *b, int64_t max_iter, double tol, int64_t mg_iterations,
+                 int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
+                 vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats);
+/* Benchmark hook (no reference counterpart): average device time of one launch on resident data.
+ * kernel 0: fine applyK, 1: fine 4-colour Gauss-Seidel sweep, 2: one V-cycle, 3: one PCG iteration. */
+int vfem_mg2_time_kernel(vfem_mg2 *mg, int kernel, int reps, double *ms);
+/* TopologyOptimizationProblem + MultigridComplianceObjective over the 2D solver; the handle takes
+ * every vfem_problem_* call (filters as in vfem_problem_create, smoothing over the 2D neighbourhood). */
+/* SmoothingFilter::apply on a 2D (dims[0], dims[1]) grid (ApplyImpl<2>, TopologyOptimizationFilter.hh:329-397) */
+int vfem_smoothing_filter2(const int64_t dims[2], int radius, int type, const double *in, double *out);
+int vfem_problem2_create(vfem_mg2 *mg, int num_filters, const int *kinds, const int *radii, const int *types,
+                         const double *betas, double volume_fraction, vfem_problem **out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,6 +47,6 @@ def test_error_path_without_device_work():
 def test_api_rejects_unsupported_instantiations():
     from voxelfem_gb300 import pyVoxelFEM as pv
     with pytest.raises(RuntimeError, match="No template instantiation"):
-        pv.TensorProductSimulator([1, 1], [[0, 0], [1, 1]], [2, 2])
+        pv.TensorProductSimulator([2, 2], [[0, 0], [1, 1]], [2, 2])
     with pytest.raises(RuntimeError, match="No template instantiation"):
         pv.TensorProductSimulator([1, 1, 1], [[0, 0, 0], [1, 1, 1]], [2, 2, 2], pv.NumberType.FLOAT)

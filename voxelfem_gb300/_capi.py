@@ -139,6 +139,55 @@ _SIGS = {
     "vfem_problem_get_physical": (C.c_int, [_vp, _vp]),
     "vfem_problem_last_solve": (C.c_int, [_vp, C.POINTER(PcgStats)]),
     "vfem_problem_oc_step": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _i64]),
+    # ---- 2D (bilinear quadrilaterals) ----
+    "vfem_grid2_create": (C.c_int, [_i64, _d, _d, C.POINTER(_vp)]),
+    "vfem_grid2_destroy": (C.c_int, [_vp]),
+    "vfem_grid2_dims": (C.c_int, [_vp, _i64, _i64, _i64]),
+    "vfem_grid2_set_etensor": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "vfem_grid2_get_etensor": (C.c_int, [_vp, _d, _d]),
+    "vfem_grid2_get_k0": (C.c_int, [_vp, _d]),
+    "vfem_grid2_set_material_params": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),
+    "vfem_grid2_get_material_params": (C.c_int, [_vp, _d, _d, _d, _d, _i32]),
+    "vfem_grid2_set_densities": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_get_densities": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_set_uniform_densities": (C.c_int, [_vp, C.c_double]),
+    "vfem_grid2_get_young_moduli": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_add_dirichlet": (C.c_int, [_vp, _d, _d, _d, C.c_uint32]),
+    "vfem_grid2_apply_symmetry": (C.c_int, [_vp, _i32, _i32]),
+    "vfem_grid2_set_nodal_forces": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_get_dirichlet_mask": (C.c_int, [_vp, _u8]),
+    "vfem_grid2_get_dirichlet_values": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_set_gravity": (C.c_int, [_vp, _d]),
+    "vfem_grid2_get_gravity": (C.c_int, [_vp, _d]),
+    "vfem_grid2_set_mask_layer": (C.c_int, [_vp, C.c_int64]),
+    "vfem_grid2_get_mask_height": (C.c_int, [_vp, _d]),
+    "vfem_grid2_apply_k": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_grid2_build_load": (C.c_int, [_vp, _vp]),
+    "vfem_grid2_compliance_gradient": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_grid2_adjoint_sensitivity": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, _vp]),
+    "vfem_grid2_element_energy": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_mg2_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "vfem_mg2_destroy": (C.c_int, [_vp]),
+    "vfem_mg2_num_levels": (C.c_int, [_vp, _i32]),
+    "vfem_mg2_level_dims": (C.c_int, [_vp, C.c_int, _i64]),
+    "vfem_mg2_level_dirichlet_mask": (C.c_int, [_vp, C.c_int, _u8]),
+    "vfem_mg2_set_use_graphs": (C.c_int, [_vp, C.c_int]),
+    "vfem_mg2_set_symmetric_gs": (C.c_int, [_vp, C.c_int]),
+    "vfem_mg2_set_mask_layer": (C.c_int, [_vp, C.c_int64]),
+    "vfem_mg2_update_stiffness": (C.c_int, [_vp]),
+    "vfem_mg2_apply_k": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "vfem_mg2_residual": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "vfem_mg2_smooth": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int]),
+    "vfem_mg2_restrict": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "vfem_mg2_interpolate": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int]),
+    "vfem_mg2_coarse_solve": (C.c_int, [_vp, _vp, _vp]),
+    "vfem_mg2_zero_dirichlet": (C.c_int, [_vp, C.c_int, _vp]),
+    "vfem_mg2_solve": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int, C.c_int, _vp]),
+    "vfem_mg2_pcg": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                              PCG_CALLBACK, C.c_void_p, C.POINTER(PcgStats)]),
+    "vfem_mg2_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _d]),
+    "vfem_smoothing_filter2": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp]),
+    "vfem_problem2_create": (C.c_int, [_vp, C.c_int, _i32, _i32, _i32, _d, C.c_double, C.POINTER(_vp)]),
 }
 
 EXPORTED = sorted(_SIGS)

@@ -18,7 +18,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIB_DIR, "libvfem.so")
 
 SOURCES = ["k_fine.cu", "k_coarse.cu", "k_tail.cu", "k_linalg.cu", "k_topopt.cu", "vfem_element.cpp", "vfem_engine.cpp",
-           "vfem_lbl.cpp", "k_q2.cu", "vfem_q2.cpp", "k_tc.cu", "k_lbl.cu", "k_mma.cu", "vfem_mma.cpp", "k_filters.cu", "vfem_capi.cpp"]
+           "vfem_lbl.cpp", "k_q2.cu", "vfem_q2.cpp", "k_tc.cu", "k_lbl.cu", "k_mma.cu", "vfem_mma.cpp", "k_filters.cu", "k_2d.cu", "vfem_2d.cpp", "vfem_capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(BS) smoothing_filter_noalloc_kernel(int d0, in
 }
 
 struct TapCache {
-    int radius = -1, type = -1;
+    int radius = -1, type = -1, ndim = -1;
     DevBuf<int> offs;
     DevBuf<double> w;
     int ntaps = 0;
@@ -155,16 +155,20 @@ thread_local TapCache g_taps;
 
 }  // namespace
 
-void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st) {
+void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st,
+                             int ndim) {
     if (radius < 0) throw Error(ERR_ARG, "negative filter radius");
-    if (g_taps.radius != radius || g_taps.type != type) {
+    if (ndim != 2 && ndim != 3) throw Error(ERR_ARG, "smoothing filter: unsupported dimension");
+    if (ndim == 2 && dims[2] != 1) throw Error(ERR_ARG, "smoothing filter: a 2D grid has dims[2] == 1");
+    if (g_taps.radius != radius || g_taps.type != type || g_taps.ndim != ndim) {
+        const int rz = ndim == 2 ? 0 : radius;
         std::vector<int> offs;
         std::vector<double> ws;
         const double rp1 = 1.0 + radius;
         double W = 0;
         for (int a = -radius; a <= radius; ++a)
             for (int b = -radius; b <= radius; ++b)
-                for (int c = -radius; c <= radius; ++c) {
+                for (int c = -rz; c <= rz; ++c) {
                     const double w = type == 1 ? rp1 - std::sqrt((double)(a * a + b * b + c * c)) : 1.0;
                     if (w <= 0) continue;
                     offs.push_back(a);
@@ -181,6 +185,7 @@ void launch_smoothing_filter(const int dims[3], int radius, int type, const doub
         g_taps.W = W;
         g_taps.radius = radius;
         g_taps.type = type;
+        g_taps.ndim = ndim;
     }
     const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
     smoothing_filter_kernel<<<gridFor(n, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], in, out, g_taps.offs.p,

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <string>
 
+#include "vfem_2d.hpp"
 #include "vfem_engine.hpp"
 #include "vfem_mma.hpp"
 
@@ -20,6 +21,16 @@ struct vfem_mg {
 struct vfem_problem {
     Problem p;
     vfem_problem(MG *m, const std::vector<FilterSpec> &f, double v) : p(m, f, v) {}
+    vfem_problem(std::unique_ptr<ProblemBackend> b, const std::vector<FilterSpec> &f, double v)
+        : p(std::move(b), f, v) {}
+};
+struct vfem_grid2 {
+    Grid2 g;
+    vfem_grid2(const int ne[2], const double mn[2], const double mx[2]) : g(ne, mn, mx) {}
+};
+struct vfem_mg2 {
+    MG2 m;
+    vfem_mg2(Grid2 *g, int l) : m(g, l) {}
 };
 
 namespace {
@@ -359,6 +370,24 @@ int vfem_kernel_launch_count(uint64_t *count) {
     return guarded([&] { *count = launchCounter(); });
 }
 
+int vfem_smoothing_filter2(const int64_t dims[2], int radius, int type, const double *in, double *out) {
+    return guarded([&] {
+        need(dims, "dims");
+        int d[3] = {0, 0, 1};
+        for (int i = 0; i < 2; ++i) {
+            if (dims[i] <= 0) throw Error(ERR_ARG, "invalid dims");
+            d[i] = (int)dims[i];
+        }
+        if (type != 0 && type != 1) throw Error(ERR_ARG, "Unexpected smoothing kernel type");
+        const int64_t n = (int64_t)d[0] * d[1];
+        cudaStream_t st = nullptr;
+        View vi, vo;
+        viewIn(vi, in, n * sizeof(double), st);
+        viewOut(vo, out, n * sizeof(double));
+        launch_smoothing_filter(d, radius, type, (const double *)vi.d, (double *)vo.d, st, 2);
+        finishOut(vo, st);
+    });
+}
 int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out) {
     return guarded([&] {
         need(dims, "dims");
@@ -440,7 +469,7 @@ int vfem_problem_set_vars(vfem_problem *p, const double *x) {
 int vfem_problem_get_vars(vfem_problem *p, double *x_out) {
     return guarded([&] {
         need(p, "problem");
-        VFEM_CUDA(cudaMemcpy(x_out, p->p.vars[0].p, p->p.grid->g.NE * sizeof(double), cudaMemcpyDefault));
+        VFEM_CUDA(cudaMemcpy(x_out, p->p.vars[0].p, p->p.be->numElems() * sizeof(double), cudaMemcpyDefault));
     });
 }
 int vfem_problem_objective(vfem_problem *p, double *value) {
@@ -607,6 +636,242 @@ int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double
         need(ms, "ms");
         need(bytes, "bytes");
         *ms = g->g.timeApplyK(precision, reps, bytes);
+    });
+}
+
+
+// ---- 2D: TensorProductSimulator<double, 1, 1> / MultigridSolver<double, 1, 1> ----
+int vfem_grid2_create(const int64_t elems[2], const double bbox_min[2], const double bbox_max[2], vfem_grid2 **out) {
+    return guarded([&] {
+        need(elems, "elems"); need(bbox_min, "bbox"); need(bbox_max, "bbox"); need(out, "out");
+        int ne[2];
+        for (int d = 0; d < 2; ++d) {
+            if (elems[d] <= 0 || elems[d] > (1 << 24)) throw Error(ERR_ARG, "invalid elementsPerDimension");
+            ne[d] = (int)elems[d];
+        }
+        if ((int64_t)(ne[0] + 1) * (ne[1] + 1) > ((int64_t)1 << 31)) throw Error(ERR_ARG, "grid too large");
+        *out = new vfem_grid2(ne, bbox_min, bbox_max);
+    });
+}
+int vfem_grid2_destroy(vfem_grid2 *g) {
+    return guarded([&] { delete g; });
+}
+int vfem_grid2_dims(const vfem_grid2 *g, int64_t elems[2], int64_t *num_nodes, int64_t *num_elements) {
+    return guarded([&] {
+        need(g, "grid");
+        if (elems) for (int d = 0; d < 2; ++d) elems[d] = g->g.g.ne[d];
+        if (num_nodes) *num_nodes = g->g.g.NN;
+        if (num_elements) *num_elements = g->g.g.NE;
+    });
+}
+int vfem_grid2_set_etensor(vfem_grid2 *g, double young, double poisson) {
+    return guarded([&] {
+        need(g, "grid");
+        g->g.setETensor(young, poisson);
+    });
+}
+int vfem_grid2_get_etensor(const vfem_grid2 *g, double *young, double *poisson) {
+    return guarded([&] {
+        need(g, "grid");
+        *young = g->g.Eyoung;
+        *poisson = g->g.nu;
+    });
+}
+int vfem_grid2_get_k0(const vfem_grid2 *g, double *out64) {
+    return guarded([&] {
+        need(g, "grid"); need(out64, "out");
+        std::memcpy(out64, g->g.K0.a, 64 * sizeof(double));
+    });
+}
+int vfem_grid2_set_material_params(vfem_grid2 *g, double E0, double Emin, double gamma, double q, int law) {
+    return guarded([&] { need(g, "grid"); g->g.setParams(E0, Emin, gamma, q, law); });
+}
+int vfem_grid2_get_material_params(const vfem_grid2 *g, double *E0, double *Emin, double *gamma, double *q, int *law) {
+    return guarded([&] {
+        need(g, "grid");
+        *E0 = g->g.E0; *Emin = g->g.Emin; *gamma = g->g.gamma; *q = g->g.q; *law = g->g.law;
+    });
+}
+int vfem_grid2_set_densities(vfem_grid2 *g, const double *rho) {
+    return guarded([&] { need(g, "grid"); need(rho, "rho"); g->g.setDensities(rho, true); });
+}
+int vfem_grid2_get_densities(vfem_grid2 *g, double *rho_out) {
+    return guarded([&] {
+        need(g, "grid"); need(rho_out, "out");
+        VFEM_CUDA(cudaMemcpy(rho_out, g->g.rho.p, g->g.g.NE * sizeof(double), cudaMemcpyDefault));
+    });
+}
+int vfem_grid2_set_uniform_densities(vfem_grid2 *g, double value) {
+    return guarded([&] { need(g, "grid"); g->g.setUniformDensities(value); });
+}
+int vfem_grid2_get_young_moduli(vfem_grid2 *g, double *out) {
+    return guarded([&] {
+        need(g, "grid"); need(out, "out");
+        VFEM_CUDA(cudaMemcpy(out, g->g.Y.p, g->g.g.NE * sizeof(double), cudaMemcpyDefault));
+    });
+}
+int vfem_grid2_add_dirichlet(vfem_grid2 *g, const double u[2], const double min_corner[2], const double max_corner[2],
+                             uint32_t component_mask) {
+    return guarded([&] {
+        need(g, "grid"); need(u, "u"); need(min_corner, "minCorner"); need(max_corner, "maxCorner");
+        g->g.addDirichlet(u, min_corner, max_corner, component_mask);
+    });
+}
+int vfem_grid2_apply_symmetry(vfem_grid2 *g, const int axes[2], const int max_face[2]) {
+    return guarded([&] { need(g, "grid"); need(axes, "axes"); need(max_face, "max_face"); g->g.applySymmetry(axes, max_face); });
+}
+int vfem_grid2_set_nodal_forces(vfem_grid2 *g, const double *forces) {
+    return guarded([&] { need(g, "grid"); need(forces, "forces"); g->g.setForces(forces); });
+}
+int vfem_grid2_get_dirichlet_mask(const vfem_grid2 *g, uint8_t *mask_out) {
+    return guarded([&] {
+        need(g, "grid"); need(mask_out, "out");
+        VFEM_CUDA(cudaMemcpy(mask_out, g->g.hmask.data(), g->g.g.NN, cudaMemcpyDefault));
+    });
+}
+int vfem_grid2_get_dirichlet_values(const vfem_grid2 *g, double *values_out) {
+    return guarded([&] {
+        need(g, "grid"); need(values_out, "out");
+        VFEM_CUDA(cudaMemcpy(values_out, g->g.hval.data(), 2 * g->g.g.NN * sizeof(double), cudaMemcpyDefault));
+    });
+}
+int vfem_grid2_set_gravity(vfem_grid2 *g, const double gravity[2]) {
+    return guarded([&] { need(g, "grid"); need(gravity, "gravity"); g->g.setGravity(gravity); });
+}
+int vfem_grid2_get_gravity(const vfem_grid2 *g, double gravity[2]) {
+    return guarded([&] {
+        need(g, "grid"); need(gravity, "gravity");
+        gravity[0] = g->g.grav[0];
+        gravity[1] = g->g.grav[1];
+    });
+}
+int vfem_grid2_set_mask_layer(vfem_grid2 *g, int64_t layer) {
+    return guarded([&] { need(g, "grid"); g->g.setMaskLayer(layer); });
+}
+int vfem_grid2_get_mask_height(const vfem_grid2 *g, double *height) {
+    return guarded([&] { need(g, "grid"); need(height, "height"); *height = g->g.maskH; });
+}
+int vfem_grid2_apply_k(vfem_grid2 *g, const double *u, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.applyK(u, out); });
+}
+int vfem_grid2_build_load(vfem_grid2 *g, double *out) {
+    return guarded([&] {
+        need(g, "grid");
+        View vo;
+        viewOut(vo, out, 2 * g->g.g.NN * sizeof(double));
+        g->g.buildLoadDev((double *)vo.d);
+        finishOut(vo, g->g.stream);
+    });
+}
+int vfem_grid2_compliance_gradient(vfem_grid2 *g, const double *u, double *grad_out) {
+    return guarded([&] { need(g, "grid"); g->g.adjoint(u, u, 1.0, 0.5, grad_out); });
+}
+int vfem_grid2_adjoint_sensitivity(vfem_grid2 *g, const double *lambda, const double *u, double load_weight,
+                                   double stiffness_weight, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.adjoint(lambda, u, load_weight, stiffness_weight, out); });
+}
+int vfem_grid2_element_energy(vfem_grid2 *g, const double *u, double *out) {
+    return guarded([&] { need(g, "grid"); g->g.elementEnergy(u, out); });
+}
+int vfem_mg2_create(vfem_grid2 *g, int num_coarsening_levels, vfem_mg2 **out) {
+    return guarded([&] {
+        need(g, "grid"); need(out, "out");
+        *out = new vfem_mg2(&g->g, num_coarsening_levels);
+    });
+}
+int vfem_mg2_destroy(vfem_mg2 *mg) {
+    return guarded([&] { delete mg; });
+}
+int vfem_mg2_num_levels(const vfem_mg2 *mg, int *levels) {
+    return guarded([&] { need(mg, "mg"); *levels = mg->m.L(); });
+}
+int vfem_mg2_level_dims(const vfem_mg2 *mg, int level, int64_t elems[2]) {
+    return guarded([&] {
+        need(mg, "mg");
+        if (level < 0 || level >= mg->m.L()) throw Error(ERR_ARG, "level out of range");
+        elems[0] = mg->m.lv[level].g.ne[0];
+        elems[1] = mg->m.lv[level].g.ne[1];
+    });
+}
+int vfem_mg2_level_dirichlet_mask(const vfem_mg2 *mg, int level, uint8_t *mask_out) {
+    return guarded([&] {
+        need(mg, "mg"); need(mask_out, "out");
+        if (level < 0 || level >= mg->m.L()) throw Error(ERR_ARG, "level out of range");
+        const std::vector<uint8_t> &m = level == 0 ? mg->m.fine->hmask : mg->m.lv[level].hmask;
+        VFEM_CUDA(cudaMemcpy(mask_out, m.data(), m.size(), cudaMemcpyDefault));
+    });
+}
+int vfem_mg2_set_use_graphs(vfem_mg2 *mg, int use) {
+    return guarded([&] { need(mg, "mg"); mg->m.useGraphs = use != 0; });
+}
+int vfem_mg2_set_symmetric_gs(vfem_mg2 *mg, int symmetric) {
+    return guarded([&] { need(mg, "mg"); mg->m.symmetricGS = symmetric != 0; });
+}
+int vfem_mg2_set_mask_layer(vfem_mg2 *mg, int64_t layer) {
+    return guarded([&] { need(mg, "mg"); mg->m.setMaskLayer(layer); });
+}
+int vfem_mg2_update_stiffness(vfem_mg2 *mg) {
+    return guarded([&] { need(mg, "mg"); mg->m.updateStiffness(); });
+}
+int vfem_mg2_apply_k(vfem_mg2 *mg, int level, const double *u, double *out) {
+    return guarded([&] { need(mg, "mg"); mg->m.applyK(level, u, out); });
+}
+int vfem_mg2_residual(vfem_mg2 *mg, int level, const double *u, const double *b, double *r_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.residual(level, u, b, r_out); });
+}
+int vfem_mg2_smooth(vfem_mg2 *mg, int level, double *u_inout, const double *b, int forward) {
+    return guarded([&] { need(mg, "mg"); mg->m.smooth(level, u_inout, b, forward != 0); });
+}
+int vfem_mg2_restrict(vfem_mg2 *mg, int level, const double *fine, double *coarse_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.restrictTo(level, fine, coarse_out); });
+}
+int vfem_mg2_interpolate(vfem_mg2 *mg, int level, const double *coarse, double *fine_inout, int accumulate) {
+    return guarded([&] { need(mg, "mg"); mg->m.interpolate(level, coarse, fine_inout, accumulate != 0); });
+}
+int vfem_mg2_coarse_solve(vfem_mg2 *mg, const double *b, double *x_out) {
+    return guarded([&] { need(mg, "mg"); mg->m.coarseSolve(b, x_out); });
+}
+int vfem_mg2_zero_dirichlet(vfem_mg2 *mg, int level, double *u_inout) {
+    return guarded([&] { need(mg, "mg"); mg->m.zeroDirichlet(level, u_inout); });
+}
+int vfem_mg2_solve(vfem_mg2 *mg, const double *u, const double *f, int64_t num_steps, int64_t num_smoothing_steps,
+                   int zero_dirichlet, int full_multigrid, double *x_out) {
+    return guarded([&] {
+        need(mg, "mg");
+        if (num_steps < 0 || num_smoothing_steps < 0) throw Error(ERR_ARG, "negative count");
+        mg->m.solve(u, f, num_steps, num_smoothing_steps, zero_dirichlet != 0, full_multigrid != 0, x_out);
+    });
+}
+int vfem_mg2_pcg(vfem_mg2 *mg, double *x_inout, const double *b, int64_t max_iter, double tol, int64_t mg_iterations,
+                 int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
+                 vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats) {
+    return guarded([&] {
+        need(mg, "mg"); need(x_inout, "x"); need(b, "b");
+        if (max_iter < 0 || mg_iterations < 0 || mg_smoothing_iterations < 0) throw Error(ERR_ARG, "negative count");
+        PcgStats s = mg->m.pcg(x_inout, b, max_iter, tol, mg_iterations, mg_smoothing_iterations, full_multigrid != 0,
+                               dirichlet_already_satisfied != 0, cb, user);
+        if (stats) {
+            stats->iterations = s.iterations;
+            stats->relres = s.relres;
+            stats->rsq = s.rsq;
+            stats->bnorm2 = s.bnorm2;
+        }
+    });
+}
+int vfem_mg2_time_kernel(vfem_mg2 *mg, int kernel, int reps, double *ms) {
+    return guarded([&] {
+        need(mg, "mg"); need(ms, "ms");
+        if (reps <= 0) throw Error(ERR_ARG, "reps must be positive");
+        *ms = mg->m.timeKernel(kernel, reps);
+    });
+}
+int vfem_problem2_create(vfem_mg2 *mg, int num_filters, const int *kinds, const int *radii, const int *types,
+                         const double *betas, double volume_fraction, vfem_problem **out) {
+    return guarded([&] {
+        need(mg, "mg"); need(out, "out");
+        std::vector<FilterSpec> f;
+        for (int i = 0; i < num_filters; ++i) f.push_back({kinds[i], radii[i], types[i], betas[i]});
+        *out = new vfem_problem(makeBackend2D(&mg->m), f, volume_fraction);
     });
 }
 

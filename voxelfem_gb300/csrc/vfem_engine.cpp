@@ -1385,18 +1385,65 @@ void MG::solve(const double *u0, const double *f, int64_t steps, int64_t sweeps,
 // ---------------------------------------------------------------------------
 // Problem: MG compliance objective + filter chain + total volume constraint
 // ---------------------------------------------------------------------------
+namespace {
+struct Backend3D : ProblemBackend {
+    MG *mg;
+    Grid *grid;
+    explicit Backend3D(MG *m) : mg(m), grid(m->fine) {}
+    int64_t numElems() const override { return grid->g.NE; }
+    int64_t numDofs() const override { return 3 * grid->g.NN; }
+    void filterDims(int dims[3], int &ndim) const override {
+        for (int d = 0; d < 3; ++d) dims[d] = grid->g.ne[d];
+        ndim = 3;
+    }
+    cudaStream_t stream() const override { return grid->stream; }
+    void buildLoad(double *f) override { grid->buildLoadDev(f); }
+    void setPhysical(const double *rho) override {
+        VFEM_CUDA(cudaMemcpyAsync(grid->rho.p, rho, grid->g.NE * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  grid->stream));
+        grid->updateYoungModuli();
+    }
+    PcgStats solve(double *u, const double *f, int64_t cgIter, double tol, int64_t mgIter, int64_t sweeps,
+                   bool fmg) override {
+        VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+        return mg->pcgDevice(u, f, cgIter, tol, mgIter, sweeps, fmg, false, nullptr, nullptr);
+    }
+    double dotAll(const double *a, const double *b, double *partials) override {
+        cudaStream_t st = grid->stream;
+        Geom gall = grid->g;
+        gall.firstDetN = (int)LAYER_MASK_NONE;  // every node, whatever the fabrication mask
+        gall.dyn = nullptr;
+        launch_masked_dot_partials<double, double>(gall, a, b, partials, st);
+        launch_finalize(partials, REDUCE_BLOCKS, partials + REDUCE_BLOCKS, st);
+        double v = 0;
+        VFEM_CUDA(cudaMemcpyAsync(&v, partials + REDUCE_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
+        VFEM_CUDA(cudaStreamSynchronize(st));
+        return v;
+    }
+    void complianceGradient(const double *u, double *out) override {
+        launch_compliance_gradient(grid->g, grid->rho.p, u, out, grid->K0, grid->E0, grid->Emin, grid->gamma, grid->q,
+                                   grid->law, grid->grav, grid->vol(), grid->stream);
+    }
+};
+}  // namespace
+
+std::unique_ptr<ProblemBackend> makeBackend(MG *mg) { return std::unique_ptr<ProblemBackend>(new Backend3D(mg)); }
+
 Problem::Problem(MG *mg_, const std::vector<FilterSpec> &filters_, double volfrac_)
-    : mg(mg_), grid(mg_->fine), filters(filters_), volfrac(volfrac_) {
+    : Problem(makeBackend(mg_), filters_, volfrac_) {}
+
+Problem::Problem(std::unique_ptr<ProblemBackend> be_, const std::vector<FilterSpec> &filters_, double volfrac_)
+    : be(std::move(be_)), filters(filters_), volfrac(volfrac_) {
     for (const auto &f : filters) {
         if (f.kind == 0 && f.radius < 0) throw Error(ERR_ARG, "negative filter radius");
         if (f.kind == 1 && !(f.beta > 0)) throw Error(ERR_ARG, "Beta parameter has to be positive");
         if (f.kind != 0 && f.kind != 1) throw Error(ERR_ARG, "unknown filter kind");
     }
-    const int64_t ne = grid->g.NE, n3 = 3 * grid->g.NN;
+    const int64_t ne = be->numElems(), nd = be->numDofs();
     vars.resize(filters.size() + 1);
     for (auto &v : vars) v.alloc(ne);
-    f.alloc(n3);
-    u.alloc(n3);
+    f.alloc(nd);
+    u.alloc(nd);
     gradBuf.alloc(ne);
     scratch.alloc(ne);
     scratch2.alloc(ne);
@@ -1406,14 +1453,21 @@ Problem::Problem(MG *mg_, const std::vector<FilterSpec> &filters_, double volfra
     dc.alloc(ne);
     partials.alloc(REDUCE_BLOCKS + 8);
     // the load is fixed when the objective is built (TopologyOptimizationObjective.hh:34-37)
-    grid->buildLoadDev(f.p);
-    launch_fill<double>(u.p, 0.0, n3, grid->stream);
-    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+    be->buildLoad(f.p);
+    launch_fill<double>(u.p, 0.0, nd, be->stream());
+    VFEM_CUDA(cudaStreamSynchronize(be->stream()));
+}
+
+void Problem::applyFilter(const FilterSpec &fs, const double *in, double *out) {
+    int dims[3], nd;
+    be->filterDims(dims, nd);
+    if (fs.kind == 0) launch_smoothing_filter(dims, fs.radius, fs.type, in, out, be->stream(), nd);
+    else launch_projection(be->numElems(), fs.beta, in, out, be->stream());
 }
 
 void Problem::filterApply(const double *x, double *out) {
-    cudaStream_t st = grid->stream;
-    const int64_t ne = grid->g.NE;
+    cudaStream_t st = be->stream();
+    const int64_t ne = be->numElems();
     if (filters.empty()) {
         VFEM_CUDA(cudaMemcpyAsync(out, x, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
         return;
@@ -1421,77 +1475,62 @@ void Problem::filterApply(const double *x, double *out) {
     const double *src = x;
     for (size_t i = 0; i < filters.size(); ++i) {
         double *dst = (i + 1 == filters.size()) ? out : ((i % 2 == 0) ? scratch.p : scratch2.p);
-        if (filters[i].kind == 0) launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, src, dst, st);
-        else launch_projection(ne, filters[i].beta, src, dst, st);
+        applyFilter(filters[i], src, dst);
         src = dst;
     }
 }
 
 // FilterChain::backprop (TopologyOptimizationFilter.hh:162-175); g is overwritten.
 void Problem::backprop(double *g) {
-    cudaStream_t st = grid->stream;
-    const int64_t ne = grid->g.NE;
+    cudaStream_t st = be->stream();
+    const int64_t ne = be->numElems();
+    int dims[3], nd;
+    be->filterDims(dims, nd);
     for (size_t i = filters.size(); i-- > 0;) {
-        if (filters[i].kind == 0) launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, g, scratch.p, st);
+        if (filters[i].kind == 0) launch_smoothing_filter(dims, filters[i].radius, filters[i].type, g, scratch.p, st, nd);
         else launch_projection_backprop(ne, filters[i].beta, g, vars[i].p, scratch.p, st);
         VFEM_CUDA(cudaMemcpyAsync(g, scratch.p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
     }
 }
 
 double Problem::meanDev(const double *x) {
-    cudaStream_t st = grid->stream;
-    launch_sum_partials(x, grid->g.NE, partials.p, st);
+    cudaStream_t st = be->stream();
+    launch_sum_partials(x, be->numElems(), partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, partials.p + REDUCE_BLOCKS, st);
     double v = 0;
     VFEM_CUDA(cudaMemcpyAsync(&v, partials.p + REDUCE_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
     VFEM_CUDA(cudaStreamSynchronize(st));
-    return v / (double)grid->g.NE;
+    return v / (double)be->numElems();
 }
 
 // TopologyOptimizationProblem.hh:41-50 and MultigridComplianceObjective::updateCache
 void Problem::setVars(const double *x, bool /*device*/) {
-    cudaStream_t st = grid->stream;
-    const int64_t ne = grid->g.NE;
+    cudaStream_t st = be->stream();
+    const int64_t ne = be->numElems();
     VFEM_CUDA(cudaMemcpyAsync(vars[0].p, x, ne * sizeof(double), cudaMemcpyDefault, st));
-    for (size_t i = 0; i < filters.size(); ++i) {
-        if (filters[i].kind == 0)
-            launch_smoothing_filter(grid->g.ne, filters[i].radius, filters[i].type, vars[i].p, vars[i + 1].p, st);
-        else launch_projection(ne, filters[i].beta, vars[i].p, vars[i + 1].p, st);
-    }
-    VFEM_CUDA(cudaMemcpyAsync(grid->rho.p, vars.back().p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    grid->updateYoungModuli();
-    if (zeroInit) launch_fill<double>(u.p, 0.0, 3 * grid->g.NN, st);
-    VFEM_CUDA(cudaStreamSynchronize(st));
-    lastStats = mg->pcgDevice(u.p, f.p, cgIter, tol, mgIter, mgSweeps, fmg, false, nullptr, nullptr);
+    for (size_t i = 0; i < filters.size(); ++i) applyFilter(filters[i], vars[i].p, vars[i + 1].p);
+    be->setPhysical(vars.back().p);
+    if (zeroInit) launch_fill<double>(u.p, 0.0, be->numDofs(), st);
+    lastStats = be->solve(u.p, f.p, cgIter, tol, mgIter, mgSweeps, fmg);
     varsSet = true;
 }
 
 double Problem::objective() {
     if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
-    cudaStream_t st = grid->stream;
-    Geom gall = grid->g;
-    gall.firstDetN = (int)LAYER_MASK_NONE;  // 0.5 f.u over all nodes (TopologyOptimizationObjective.hh:41-43)
-    gall.dyn = nullptr;                      // use the override above, not the grid's device mask
-    launch_masked_dot_partials<double, double>(gall, f.p, u.p, partials.p, st);
-    launch_finalize(partials.p, REDUCE_BLOCKS, partials.p + REDUCE_BLOCKS, st);
-    double v = 0;
-    VFEM_CUDA(cudaMemcpyAsync(&v, partials.p + REDUCE_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
-    VFEM_CUDA(cudaStreamSynchronize(st));
-    return 0.5 * v;
+    // 0.5 f.u over all nodes (TopologyOptimizationObjective.hh:41-43)
+    return 0.5 * be->dotAll(f.p, u.p, partials.p);
 }
 
 void Problem::gradientDev(double *out) {
-    cudaStream_t st = grid->stream;
-    launch_compliance_gradient(grid->g, grid->rho.p, u.p, out, grid->K0, grid->E0, grid->Emin, grid->gamma, grid->q,
-                               grid->law, grid->grav, grid->vol(), st);
+    be->complianceGradient(u.p, out);
     backprop(out);
 }
 
 void Problem::gradient(double *out, bool /*device*/) {
     if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
     gradientDev(gradBuf.p);
-    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
-    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, be->numElems() * sizeof(double), cudaMemcpyDefault, be->stream()));
+    VFEM_CUDA(cudaStreamSynchronize(be->stream()));
 }
 
 double Problem::constraint() {
@@ -1500,15 +1539,15 @@ double Problem::constraint() {
 }
 
 void Problem::jacobianDev(double *out) {
-    launch_fill<double>(out, -1.0 / (volfrac * (double)grid->g.NE), grid->g.NE, grid->stream);
+    launch_fill<double>(out, -1.0 / (volfrac * (double)be->numElems()), be->numElems(), be->stream());
     backprop(out);
 }
 
 void Problem::jacobian(double *out, bool /*device*/) {
     if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
     jacobianDev(gradBuf.p);
-    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
-    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+    VFEM_CUDA(cudaMemcpyAsync(out, gradBuf.p, be->numElems() * sizeof(double), cudaMemcpyDefault, be->stream()));
+    VFEM_CUDA(cudaStreamSynchronize(be->stream()));
 }
 
 // TopologyOptimizationProblem::evaluateOCConstraintAtVars (TopologyOptimizationProblem.hh:58-66)
@@ -1520,8 +1559,8 @@ double Problem::constraintAtVars(const double *x) {
 // OptimalityCriterion.hh:51-138
 int64_t Problem::ocStep(double m, double p, double ctol) {
     if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
-    cudaStream_t st = grid->stream;
-    const int64_t ne = grid->g.NE;
+    cudaStream_t st = be->stream();
+    const int64_t ne = be->numElems();
     gradientDev(dJ.p);
     jacobianDev(dc.p);
     VFEM_CUDA(cudaMemcpyAsync(x0.p, vars[0].p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1566,13 +1605,13 @@ int64_t Problem::ocStep(double m, double p, double ctol) {
 }
 
 void Problem::getU(double *out, bool /*device*/) {
-    VFEM_CUDA(cudaMemcpyAsync(out, u.p, 3 * grid->g.NN * sizeof(double), cudaMemcpyDefault, grid->stream));
-    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+    VFEM_CUDA(cudaMemcpyAsync(out, u.p, be->numDofs() * sizeof(double), cudaMemcpyDefault, be->stream()));
+    VFEM_CUDA(cudaStreamSynchronize(be->stream()));
 }
 
 void Problem::getPhysical(double *out, bool /*device*/) {
-    VFEM_CUDA(cudaMemcpyAsync(out, vars.back().p, grid->g.NE * sizeof(double), cudaMemcpyDefault, grid->stream));
-    VFEM_CUDA(cudaStreamSynchronize(grid->stream));
+    VFEM_CUDA(cudaMemcpyAsync(out, vars.back().p, be->numElems() * sizeof(double), cudaMemcpyDefault, be->stream()));
+    VFEM_CUDA(cudaStreamSynchronize(be->stream()));
 }
 
 

@@ -6,10 +6,10 @@
 #include <cmath>
 #include <limits>
 #include <map>
-#include <string>
-#include <utility>
 #include <memory>
+#include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include "vfem_common.cuh"
@@ -299,11 +299,27 @@ struct FilterSpec {
     double beta;
 };
 
+// What the problem needs from a simulator and its multigrid solver (3D: Grid + MG, 2D: Grid2 + MG2).
+struct ProblemBackend {
+    virtual ~ProblemBackend() = default;
+    virtual int64_t numElems() const = 0;
+    virtual int64_t numDofs() const = 0;  // length of u and f
+    virtual void filterDims(int dims[3], int &ndim) const = 0;
+    virtual cudaStream_t stream() const = 0;
+    virtual void buildLoad(double *f) = 0;             // device
+    virtual void setPhysical(const double *rho) = 0;  // device densities -> simulator, moduli updated
+    virtual PcgStats solve(double *u, const double *f, int64_t cgIter, double tol, int64_t mgIter, int64_t sweeps,
+                           bool fmg) = 0;
+    virtual double dotAll(const double *a, const double *b, double *partials) = 0;  // over every node
+    virtual void complianceGradient(const double *u, double *out) = 0;              // device, per element
+};
+std::unique_ptr<ProblemBackend> makeBackend(MG *mg);
+
 class Problem {
 public:
     Problem(MG *mg, const std::vector<FilterSpec> &filters, double volfrac);
-    MG *mg;
-    Grid *grid;
+    Problem(std::unique_ptr<ProblemBackend> be, const std::vector<FilterSpec> &filters, double volfrac);
+    std::unique_ptr<ProblemBackend> be;
     std::vector<FilterSpec> filters;
     double volfrac;
     int64_t cgIter = 100;
@@ -328,6 +344,7 @@ public:
     void backprop(double *g_dev);
 
 private:
+    void applyFilter(const FilterSpec &fs, const double *in, double *out);
     double meanDev(const double *x);
     double constraintAtVars(const double *x_dev);
     void gradientDev(double *out);

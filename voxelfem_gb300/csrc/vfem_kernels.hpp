@@ -294,7 +294,10 @@ template <typename T>
 void launch_enforce_dirichlet(const Geom &g, T *u, const uint8_t *dmask, const double *dval, cudaStream_t st);
 
 // ---------------- topology optimisation (k_topopt.cu) ----------------
-void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st);
+// ndim 2: a (dims[0], dims[1]) grid with dims[2] == 1 and a 2D neighbourhood
+// (SmoothingFilter::ApplyImpl<2>, TopologyOptimizationFilter.hh:329-397).
+void launch_smoothing_filter(const int dims[3], int radius, int type, const double *in, double *out, cudaStream_t st,
+                             int ndim = 3);
 // Allocation-free density filter: taps in a file-scope device array (radius <= noalloc_filter_max_radius()).
 void launch_smoothing_filter_noalloc(const int dims[3], int radius, int type, const double *in, double *out,
                                      cudaStream_t st);

@@ -41,18 +41,18 @@ def _lib():
     return _capi.load()
 
 
-def _as_vfield(u, nn):
+def _as_vfield(u, nn, nc=3):
     a = np.asarray(u, dtype=np.float64)
-    if a.shape != (nn, 3):
-        if a.size == 3 * nn and a.ndim == 1:
-            a = a.reshape(nn, 3)
+    if a.shape != (nn, nc):
+        if a.size == nc * nn and a.ndim == 1:
+            a = a.reshape(nn, nc)
         else:
             raise RuntimeError("Invalid input size")
     return np.asfortranarray(a)
 
 
-def _new_vfield(nn):
-    return np.zeros((nn, 3), order="F")
+def _new_vfield(nn, nc=3):
+    return np.zeros((nn, nc), order="F")
 
 
 def _as_elems(x, ne):
@@ -62,13 +62,13 @@ def _as_elems(x, ne):
     return a
 
 
-def _cmask(mask):
+def _cmask(mask, dim=3):
     bits = 0
     for ch in mask:
         if ch not in "xyz":
             raise RuntimeError("Invalid component mask " + mask)
         bits |= 1 << "xyz".index(ch)
-    return bits
+    return bits & ((1 << dim) - 1)
 
 
 def _arr3(v):
@@ -79,15 +79,19 @@ def _arr3(v):
 def TensorProductSimulator(degreesPerDimension, domainBBox, elementsPerDimension, numberType=NumberType.DOUBLE):
     """Factory of pyVoxelFEM.TensorProductSimulator (VoxelFEM.cc:423-430)."""
     degs = [int(d) for d in degreesPerDimension]
-    if int(numberType) != int(NumberType.DOUBLE) or degs not in ([1, 1, 1], [2, 2, 2]):
+    if int(numberType) != int(NumberType.DOUBLE) or degs not in ([1, 1], [1, 1, 1], [2, 2, 2]):
         raise RuntimeError("No template instantiation matching degreesPerDimension/number type!")
     if degs == [2, 2, 2]:
         return TensorProductSimulator_3D_Q2(domainBBox, elementsPerDimension)
+    if degs == [1, 1]:
+        return TensorProductSimulator_2D(domainBBox, elementsPerDimension)
     return TensorProductSimulator_3D(domainBBox, elementsPerDimension)
 
 
 class TensorProductSimulator_3D:
     """TensorProductSimulator<double, 1, 1, 1> (TensorProductSimulator.hh:166-623)."""
+
+    _nc = 3
 
     def __init__(self, domainBBox, elementsPerDimension):
         bb = [np.asarray(domainBBox[0], dtype=np.float64).reshape(3), np.asarray(domainBBox[1], dtype=np.float64).reshape(3)]
@@ -508,29 +512,32 @@ class TensorProductSimulator_3D:
 def apply_bc_file(tps, path):
     """Minimal reader of the reference's `.bc` JSON regions ("box%" or "box"; types
     "dirichlet[x|y|z...]" and "force"; forces split equally over the region's nodes,
-    TensorProductSimulator.hh:600-652)."""
+    TensorProductSimulator.hh:600-652). A 2D simulator reads the first two entries of each
+    vector (the reference's 2D files carry a third, zero coordinate)."""
     with open(path) as f:
         spec = json.load(f)
+    dim = tps._nc
     lo, hi = tps.domain
     size = hi - lo
     nn = tps.NbNodesPerDimension
     dx = tps.dx
-    I, J, K = np.meshgrid(np.arange(nn[0]), np.arange(nn[1]), np.arange(nn[2]), indexing="ij")
-    pos = np.stack([lo[0] + I.ravel() * dx[0], lo[1] + J.ravel() * dx[1], lo[2] + K.ravel() * dx[2]], axis=1)
-    forces = np.zeros((tps.numNodes(), 3))
+    grids = np.meshgrid(*[np.arange(nn[d]) for d in range(dim)], indexing="ij")
+    pos = np.stack([lo[d] + grids[d].ravel() * dx[d] for d in range(dim)], axis=1)
+    forces = np.zeros((tps.numNodes(), dim))
     have_force = False
+    vec = lambda v: np.asarray(v, dtype=float).reshape(-1)[:dim]
     for reg in spec["regions"]:
         if "box%" in reg:
             b = reg["box%"]
-            mn = lo + np.asarray(b["minCorner"], dtype=float) * size
-            mx = lo + np.asarray(b["maxCorner"], dtype=float) * size
+            mn = lo + vec(b["minCorner"]) * size
+            mx = lo + vec(b["maxCorner"]) * size
         elif "box" in reg:
-            mn = np.asarray(reg["box"]["minCorner"], dtype=float)
-            mx = np.asarray(reg["box"]["maxCorner"], dtype=float)
+            mn = vec(reg["box"]["minCorner"])
+            mx = vec(reg["box"]["maxCorner"])
         else:
             raise RuntimeError("Unsupported boundary condition region")
         typ = reg["type"]
-        val = np.asarray(reg["value"], dtype=float)
+        val = vec(reg["value"])
         inside = np.all((pos >= mn) & (pos <= mx), axis=1)
         if typ.startswith("dirichlet"):
             comps = typ[len("dirichlet"):] or "xyz"
@@ -581,7 +588,13 @@ class _LevelSimulator:
 
 
 class MultigridSolver:
-    """MultigridSolver<double, 1, 1, 1> (MultigridSolver.hh); created by tps.multigridSolver(levels)."""
+    """MultigridSolver<double, 1, 1, 1> (MultigridSolver.hh); created by tps.multigridSolver(levels).
+    Constructed on a 2D simulator it is a MultigridSolver2D."""
+
+    def __new__(cls, tps=None, numCoarseningLevels=0):
+        if cls is MultigridSolver and isinstance(tps, TensorProductSimulator_2D):
+            return MultigridSolver2D(tps, numCoarseningLevels)
+        return super().__new__(cls)
 
     def __init__(self, tps, numCoarseningLevels):
         h = C.c_void_p()
@@ -739,8 +752,8 @@ class MultigridSolver:
 _cudart = None
 
 
-def _device_to_host(dev_ptr, nn):
-    """Copy a device FP64 (nn, 3) field to a new host array (used by per-iteration callbacks)."""
+def _device_to_host(dev_ptr, nn, nc=3):
+    """Copy a device FP64 (nn, nc) field to a new host array (used by per-iteration callbacks)."""
     global _cudart
     if _cudart is None:
         import ctypes.util
@@ -751,7 +764,7 @@ def _device_to_host(dev_ptr, nn):
             import glob
             cands = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
             _cudart = C.CDLL(cands[0])
-    out = np.empty((nn, 3), order="F")
+    out = np.empty((nn, nc), order="F")
     rc = _cudart.cudaMemcpy(C.c_void_p(out.ctypes.data), C.c_void_p(dev_ptr), C.c_size_t(out.nbytes), 4)
     if rc != 0:
         raise RuntimeError("cudaMemcpy failed in callback")
@@ -796,8 +809,8 @@ class SmoothingFilter(Filter):
         a = _as_elems(x, int(np.prod(self._dims)))
         out = np.empty_like(a)
         dims = np.array(self._dims, dtype=np.int64)
-        check(_lib().vfem_smoothing_filter(dims.ctypes.data_as(_capi._i64), self.radius, int(self.type), ptr(a),
-                                           ptr(out)))
+        fn = _lib().vfem_smoothing_filter2 if len(self._dims) == 2 else _lib().vfem_smoothing_filter
+        check(fn(dims.ctypes.data_as(_capi._i64), self.radius, int(self.type), ptr(a), ptr(out)))
         return out
 
     backprop = lambda self, g, vars_=None: self.apply(g)
@@ -1108,9 +1121,9 @@ class TopologyOptimizationProblem:
                 raise RuntimeError("Unsupported filter type " + type(f).__name__)
         n = max(len(kinds), 1)
         h = C.c_void_p()
-        check(_lib().vfem_problem_create(objective.mg._h, len(kinds), (C.c_int * n)(*kinds), (C.c_int * n)(*radii),
-                                         (C.c_int * n)(*types), (C.c_double * n)(*betas),
-                                         self.constraints[0].volumeFraction, C.byref(h)))
+        create = _lib().vfem_problem2_create if simulator._nc == 2 else _lib().vfem_problem_create
+        check(create(objective.mg._h, len(kinds), (C.c_int * n)(*kinds), (C.c_int * n)(*radii), (C.c_int * n)(*types),
+                     (C.c_double * n)(*betas), self.constraints[0].volumeFraction, C.byref(h)))
         self._h = h
         objective._problem = self
         self._ne = simulator.numElements()
@@ -1150,7 +1163,7 @@ class TopologyOptimizationProblem:
 
     def _get_u(self):
         nn = self._sim.numNodes()
-        out = _new_vfield(nn)
+        out = _new_vfield(nn, self._sim._nc)
         check(_lib().vfem_problem_get_u(self._h, ptr(out)))
         return out
 
@@ -1453,3 +1466,568 @@ class LayerByLayerEvaluator:
 
     def gradient(self):
         return self._grad / max(len(self.compliances), 1)
+
+
+# ---------------------------------------------------------------------------
+# 2D: bilinear quadrilaterals (TensorProductSimulator<double, 1, 1>, registered by
+# VoxelFEM.cc:413-414 beside the 3D instantiation)
+# ---------------------------------------------------------------------------
+def _arr2(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1)[:2])
+
+
+class TensorProductSimulator_2D:
+    """TensorProductSimulator<double, 1, 1>: nodal fields (numNodes, 2), node (i, j) -> i * ny1 + j,
+    plane-stress isotropic material (MeshFEM ElasticityTensor<Real, 2>::setIsotropic)."""
+
+    _nc = 2
+
+    def __init__(self, domainBBox, elementsPerDimension):
+        bb = [np.asarray(domainBBox[0], dtype=np.float64).reshape(2), np.asarray(domainBBox[1], dtype=np.float64).reshape(2)]
+        ne = np.ascontiguousarray(np.asarray(elementsPerDimension, dtype=np.int64).reshape(2))
+        h = C.c_void_p()
+        check(_lib().vfem_grid2_create(ne.ctypes.data_as(_capi._i64), _capi.dptr(np.ascontiguousarray(bb[0])),
+                                       _capi.dptr(np.ascontiguousarray(bb[1])), C.byref(h)))
+        self._h = h
+        self._bbox = (bb[0].copy(), bb[1].copy())
+        self._ne = tuple(int(v) for v in ne)
+        self._nn = (self._ne[0] + 1) * (self._ne[1] + 1)
+        self._nel = self._ne[0] * self._ne[1]
+        self._forces = np.zeros((self._nn, 2), order="F")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_grid2_destroy(h)
+            self._h = None
+
+    # --- sizes / geometry ---
+    def numNodes(self):
+        return self._nn
+
+    def numElements(self):
+        return self._nel
+
+    @property
+    def gridShape(self):
+        return np.array(self._ne)
+
+    NbElementsPerDimension = gridShape
+
+    @property
+    def NbNodesPerDimension(self):
+        return np.array([n + 1 for n in self._ne])
+
+    @property
+    def domain(self):
+        return (self._bbox[0].copy(), self._bbox[1].copy())
+
+    bbox = domain
+
+    @property
+    def dx(self):
+        return (self._bbox[1] - self._bbox[0]) / np.array(self._ne)
+
+    @property
+    def elementVolume(self):
+        return float(np.prod(self.dx))
+
+    def nodePosition(self, ni):
+        i, j = divmod(int(ni), self._ne[1] + 1)
+        return self._bbox[0] + np.array([i, j]) * self.dx
+
+    def elementNodes(self, ei):
+        i, j = divmod(int(ei), self._ne[1])
+        ny1 = self._ne[1] + 1
+        return np.array([(i + (l >> 1)) * ny1 + j + (l & 1) for l in range(4)])
+
+    def elemNodeGlobalIndex(self, ei, n):
+        return int(self.elementNodes(ei)[int(n)])
+
+    def elementIndexForGridCell(self, cellIdxs):
+        i, j = (int(v) for v in cellIdxs)
+        return i * self._ne[1] + j
+
+    # --- material ---
+    def readMaterial(self, materialPath):
+        with open(materialPath) as f:
+            mat = json.load(f)
+        if mat.get("type", "isotropic_material") not in ("isotropic_material", "isotropic"):
+            raise RuntimeError("Only isotropic materials are supported")
+        self.ETensor = (float(mat["young"]), float(mat["poisson"]))
+
+    @property
+    def ETensor(self):
+        E, nu = C.c_double(), C.c_double()
+        check(_lib().vfem_grid2_get_etensor(self._h, C.byref(E), C.byref(nu)))
+        return (E.value, nu.value)
+
+    @ETensor.setter
+    def ETensor(self, value):
+        E, nu = value
+        check(_lib().vfem_grid2_set_etensor(self._h, float(E), float(nu)))
+
+    def _params(self):
+        v = [C.c_double() for _ in range(4)]
+        law = C.c_int()
+        check(_lib().vfem_grid2_get_material_params(self._h, *[C.byref(x) for x in v], C.byref(law)))
+        return [x.value for x in v] + [law.value]
+
+    def _set_param(self, idx, value):
+        p = self._params()
+        p[idx] = value
+        check(_lib().vfem_grid2_set_material_params(self._h, p[0], p[1], p[2], p[3], int(p[4])))
+
+    E_0 = property(lambda self: self._params()[0], lambda self, v: self._set_param(0, float(v)))
+    E_min = property(lambda self: self._params()[1], lambda self, v: self._set_param(1, float(v)))
+    gamma = property(lambda self: self._params()[2], lambda self, v: self._set_param(2, float(v)))
+    q = property(lambda self: self._params()[3], lambda self, v: self._set_param(3, float(v)))
+    interpolationLaw = property(lambda self: InterpolationLaw(self._params()[4]),
+                                lambda self, v: self._set_param(4, int(v)))
+
+    @property
+    def gravity(self):
+        g = np.zeros(2)
+        check(_lib().vfem_grid2_get_gravity(self._h, _capi.dptr(g)))
+        return g
+
+    @gravity.setter
+    def gravity(self, g):
+        check(_lib().vfem_grid2_set_gravity(self._h, _capi.dptr(_arr2(g))))
+
+    def fullDensityElementStiffnessMatrix(self):
+        K = np.empty(64)
+        check(_lib().vfem_grid2_get_k0(self._h, _capi.dptr(K)))
+        return K.reshape(8, 8)
+
+    def elementStiffnessMatrix(self, ei):
+        return self.elementYoungModulusScaleFactor(ei) * self.fullDensityElementStiffnessMatrix()
+
+    def clearCachedElementStiffness(self):
+        """No per-element stiffness cache exists here (elements are scaled copies of K0)."""
+
+    # --- mesh, sampling and BC fields (TensorProductSimulator.hh:689-712, 746-778, 1161-1179) ---
+    def mesh(self):
+        return self
+
+    def getMesh(self):
+        """(V, F): node positions (nn, 3) with z = 0 and quadrilaterals (ne, 4) in Gmsh order."""
+        nn = self.NbNodesPerDimension
+        I, J = np.meshgrid(np.arange(nn[0]), np.arange(nn[1]), indexing="ij")
+        V = np.zeros((self._nn, 3))
+        V[:, :2] = self._bbox[0] + np.stack([I.ravel(), J.ravel()], axis=1) * self.dx
+        i, j = np.meshgrid(np.arange(self._ne[0]), np.arange(self._ne[1]), indexing="ij")
+        base = i.ravel() * nn[1] + j.ravel()
+        off = [(l >> 1) * nn[1] + (l & 1) for l in range(4)]
+        F = np.stack([base + off[l] for l in (0, 1, 3, 2)], axis=1)
+        return V, F
+
+    def sampleNodalField(self, u, p):
+        """Bilinear interpolation of the nodal field u (nn x c) at the rows of p (clamped into the domain)."""
+        u = np.asarray(u, dtype=np.float64).reshape(self._nn, -1)
+        p = np.atleast_2d(np.asarray(p, dtype=np.float64))[:, :2]
+        p = np.clip(p, self._bbox[0], self._bbox[1])
+        t = (p - self._bbox[0]) / self.dx
+        e = np.minimum(np.floor(t).astype(np.int64), np.array(self._ne) - 1)
+        x = t - e
+        ny1 = self._ne[1] + 1
+        out = np.zeros((p.shape[0], u.shape[1]))
+        for l in range(4):
+            b = [l >> 1, l & 1]
+            w = np.prod([x[:, d] if b[d] else 1.0 - x[:, d] for d in range(2)], axis=0)
+            out += w[:, None] * u[(e[:, 0] + b[0]) * ny1 + e[:, 1] + b[1]]
+        return out
+
+    def getBCIndicatorField(self):
+        d = self.getDirichletMask()
+        f = self.getForceMask()
+        return (d[:, 0] * 1 + d[:, 1] * 2 + 8 * (f[:, 0] * 1 + f[:, 1] * 2)).astype(np.float64)
+
+    def getK(self):
+        """The assembled stiffness matrix (2 nn x 2 nn, DOF 2 n + c) as a scipy CSC matrix."""
+        import scipy.sparse as sp
+        K0 = self.fullDensityElementStiffnessMatrix()
+        Y = self.getYoungModulusScaleFactor()
+        i, j = np.meshgrid(np.arange(self._ne[0]), np.arange(self._ne[1]), indexing="ij")
+        base = i.ravel() * (self._ne[1] + 1) + j.ravel()
+        nodes = np.stack([base + (l >> 1) * (self._ne[1] + 1) + (l & 1) for l in range(4)], 1)
+        dofs = (2 * nodes[:, :, None] + np.arange(2)[None, None, :]).reshape(-1, 8)
+        rows = np.repeat(dofs, 8, axis=1).ravel()
+        cols = np.tile(dofs, (1, 8)).ravel()
+        vals = (Y[:, None] * K0.ravel()[None, :]).ravel()
+        return sp.csc_matrix((vals, (rows, cols)), shape=(2 * self._nn, 2 * self._nn))
+
+    def solveWithImposedLoads(self):
+        return self.solve(self.buildLoadVector())
+
+    # --- coarser and intermediate simulators ---
+    def _copy_material(self, other):
+        other.ETensor = self.ETensor
+        other.E_min = self.E_min
+        other.E_0 = self.E_0
+        other.gamma = self.gamma
+
+    def downsample(self, downsamplingLevels):
+        f = 2 ** int(downsamplingLevels)
+        ne = np.array(self._ne)
+        if (ne % f).any():
+            raise RuntimeError("Grid size must be divisible by 2^downsamplingLevels")
+        c = TensorProductSimulator_2D([self._bbox[0], self._bbox[1]], ne // f)
+        self._copy_material(c)
+        return c
+
+    def _factor(self, coarse):
+        f = self._ne[0] // coarse._ne[0]
+        if any(f * coarse._ne[d] != self._ne[d] for d in range(2)):
+            raise RuntimeError("Invalid downsampled simulator")
+        return f
+
+    def downsampleDensityFieldTo(self, densities, coarseTPS):
+        f = self._factor(coarseTPS)
+        rho = np.asarray(densities, dtype=np.float64).reshape(-1)
+        if rho.size != self._nel:
+            raise RuntimeError("Invalid input densities size (%d vs %d)" % (rho.size, self._nel))
+        c = rho.reshape(self._ne[0] // f, f, self._ne[1] // f, f).sum(axis=(1, 3)) / f ** 2
+        coarseTPS.setDensities(c.ravel())
+
+    def upsampleDensityGradientFrom(self, coarseTPS, g_coarse):
+        f = self._factor(coarseTPS)
+        g = np.asarray(g_coarse, dtype=np.float64).reshape(coarseTPS._ne)
+        return (np.repeat(np.repeat(g, f, 0), f, 1) / f ** 2).ravel()
+
+    def setDensitiesFromCoarseGrid(self, upscalingFactor, rho):
+        f = int(upscalingFactor)
+        rho = np.asarray(rho, dtype=np.float64).reshape(-1)
+        if self._nel != f ** 2 * rho.size:
+            raise RuntimeError("Incorrect rho size")
+        rc = rho.reshape(tuple(v // f for v in self._ne))
+        self.setDensities(np.repeat(np.repeat(rc, f, 0), f, 1).ravel())
+
+    def getIntermediateFabricationShape(self, yfrac, validateBoundaryConditions=True, law=None):
+        if yfrac < 0 or yfrac > 1:
+            raise RuntimeError("hfrac is out of bounds")
+        full = self._ne[1]
+        h = int(round(yfrac * full))
+        if abs(yfrac * full - h) > 1e-10:
+            raise RuntimeError("hfrac chops off a noninteger number of element layers")
+        lo, hi = self._bbox[0].copy(), self._bbox[1].copy()
+        hi[1] = lo[1] + yfrac * (self._bbox[1][1] - lo[1])
+        r = TensorProductSimulator_2D([lo, hi], [self._ne[0], h])
+        if law is not None:
+            r.interpolationLaw = law
+        r.ETensor = self.ETensor
+        self.transferDensitiesToIntermediateFabricationShape(r)
+        r.E_min, r.E_0, r.gamma = self.E_min, self.E_0, self.gamma
+        g = self.gravity
+        bad = RuntimeError("Original simulator has unexpected boundary conditions for layer-by-layer simulation")
+        if not np.any(g):
+            if validateBoundaryConditions:
+                raise bad
+            g = np.array([0.0, -1.0])
+        r.gravity = g
+        if validateBoundaryConditions:
+            if self.getForceMask().any():
+                raise bad
+            m = self.getDirichletMask()
+            jrow = np.arange(self._nn) % (self._ne[1] + 1)
+            if not m[jrow == 0].all() or m[jrow != 0].any():
+                raise bad
+        r.addDirichletCondition([0.0, 0.0], [lo[0], lo[1]], [hi[0], lo[1]], "xy")
+        return r
+
+    def _check_intermediate(self, itps):
+        if itps._ne[0] != self._ne[0] or itps._ne[1] > self._ne[1]:
+            raise RuntimeError("Intermediate shape is of unexpected size")
+
+    def transferDensitiesToIntermediateFabricationShape(self, intermediateTPS):
+        rho = self.getDensities().reshape(self._ne)
+        intermediateTPS.setDensities(rho[:, :intermediateTPS._ne[1]].ravel())
+
+    def transferVFieldToIntermediateFabricationShape(self, intermediateTPS, u):
+        self._check_intermediate(intermediateTPS)
+        u = np.asarray(u, dtype=np.float64).reshape(self._ne[0] + 1, self._ne[1] + 1, -1)
+        return np.asfortranarray(u[:, :intermediateTPS._ne[1] + 1, :].reshape(-1, u.shape[-1]))
+
+    def accumElementScalarFieldFromIntermediateFabricationShape(self, intermediateTPS, rho_in, rho_accum):
+        acc = rho_accum.reshape(self._ne)
+        acc[:, :intermediateTPS._ne[1]] += np.asarray(rho_in, dtype=np.float64).reshape(intermediateTPS._ne)
+
+    # --- densities ---
+    def getDensities(self):
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid2_get_densities(self._h, ptr(out)))
+        return out
+
+    def setDensities(self, rho):
+        if np.asarray(rho).size != self._nel:
+            raise RuntimeError("Incorrect rho size")
+        check(_lib().vfem_grid2_set_densities(self._h, ptr(_as_elems(rho, self._nel))))
+
+    def setUniformDensities(self, density):
+        check(_lib().vfem_grid2_set_uniform_densities(self._h, float(density)))
+
+    def setDensity(self, ei, value):
+        if value > 1.0 or value < 0:
+            raise RuntimeError("Density value (%g) has to be in between 0 and 1" % value)
+        rho = self.getDensities()
+        rho[int(ei)] = value
+        self.setDensities(rho)
+
+    def elementDensity(self, ei):
+        return float(self.getDensities()[int(ei)])
+
+    def getYoungModulusScaleFactor(self):
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid2_get_young_moduli(self._h, ptr(out)))
+        return out
+
+    def elementYoungModulusScaleFactor(self, ei):
+        return float(self.getYoungModulusScaleFactor()[int(ei)])
+
+    # --- boundary conditions ---
+    def addDirichletCondition(self, u, minCorner, maxCorner, componentMask="xyz"):
+        check(_lib().vfem_grid2_add_dirichlet(self._h, _capi.dptr(_arr2(u)), _capi.dptr(_arr2(minCorner)),
+                                              _capi.dptr(_arr2(maxCorner)), _cmask(componentMask, 2)))
+
+    def applySymmetryConditions(self, symmetry_axes, minMaxFace=(False, False)):
+        ax = (C.c_int * 2)(*[int(bool(v)) for v in list(symmetry_axes)[:2]])
+        mf = (C.c_int * 2)(*[int(bool(v)) for v in list(minMaxFace)[:2]])
+        check(_lib().vfem_grid2_apply_symmetry(self._h, ax, mf))
+
+    def setNodalForces(self, forces):
+        f = _as_vfield(forces, self._nn, 2)
+        self._forces = f.copy(order="F")
+        check(_lib().vfem_grid2_set_nodal_forces(self._h, ptr(f)))
+
+    def applyDisplacementsAndLoadsFromFile(self, bcPath):
+        apply_bc_file(self, bcPath)
+
+    def getDirichletMask(self):
+        m = np.zeros(self._nn, dtype=np.uint8)
+        check(_lib().vfem_grid2_get_dirichlet_mask(self._h, m.ctypes.data_as(_capi._u8)))
+        return np.stack([(m >> c) & 1 for c in range(2)], axis=1).astype(bool)
+
+    def getForceMask(self):
+        return self._forces != 0
+
+    def getDirichletVarsAndValues(self):
+        m = self.getDirichletMask()
+        vals = np.zeros((self._nn, 2), order="F")
+        check(_lib().vfem_grid2_get_dirichlet_values(self._h, ptr(vals)))
+        nodes, comps = np.nonzero(m)
+        return (list(2 * nodes + comps), list(vals[nodes, comps]))
+
+    # --- layer-by-layer fabrication mask ---
+    def setFabricationMaskHeightByLayer(self, l):
+        check(_lib().vfem_grid2_set_mask_layer(self._h, int(l)))
+
+    def getFabricationMaskHeight(self):
+        h = C.c_double()
+        check(_lib().vfem_grid2_get_mask_height(self._h, C.byref(h)))
+        return h.value
+
+    # --- physics ---
+    def applyK(self, u):
+        u = _as_vfield(u, self._nn, 2)
+        out = _new_vfield(self._nn, 2)
+        check(_lib().vfem_grid2_apply_k(self._h, ptr(u), ptr(out)))
+        return out
+
+    def buildLoadVector(self):
+        out = _new_vfield(self._nn, 2)
+        check(_lib().vfem_grid2_build_load(self._h, ptr(out)))
+        return out
+
+    def complianceGradient(self, u):
+        u = _as_vfield(u, self._nn, 2)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid2_compliance_gradient(self._h, ptr(u), ptr(out)))
+        return out
+
+    def adjointSensitivity(self, lam, u, loadWeight=1.0, stiffnessWeight=1.0):
+        lam = _as_vfield(lam, self._nn, 2)
+        u = _as_vfield(u, self._nn, 2)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid2_adjoint_sensitivity(self._h, ptr(lam), ptr(u), float(loadWeight),
+                                                    float(stiffnessWeight), ptr(out)))
+        return out
+
+    def elementEnergyDensity(self, u):
+        u = _as_vfield(u, self._nn, 2)
+        out = np.empty(self._nel)
+        check(_lib().vfem_grid2_element_energy(self._h, ptr(u), ptr(out)))
+        return out
+
+    def solve(self, f):
+        """Direct solve (TensorProductSimulator::solve) through a zero-coarsening hierarchy."""
+        mg = self.multigridSolver(0)
+        return mg.preconditionedConjugateGradient(np.zeros((self._nn, 2)), f, 1, 0.0)
+
+    def multigridSolver(self, numCoarseningLevels):
+        return MultigridSolver2D(self, int(numCoarseningLevels))
+
+
+class _LevelSimulator2D:
+    """Read-only view of a coarse 2D level (MultigridSolver::getSimulator(l), l > 0)."""
+
+    _nc = 2
+
+    def __init__(self, mg, l):
+        self._mg, self._l = mg, l
+        ne = np.zeros(2, dtype=np.int64)
+        check(_lib().vfem_mg2_level_dims(mg._h, l, ne.ctypes.data_as(_capi._i64)))
+        self._ne = tuple(int(v) for v in ne)
+
+    def numNodes(self):
+        return (self._ne[0] + 1) * (self._ne[1] + 1)
+
+    def numElements(self):
+        return self._ne[0] * self._ne[1]
+
+    @property
+    def NbElementsPerDimension(self):
+        return np.array(self._ne)
+
+    gridShape = NbElementsPerDimension
+
+    @property
+    def NbNodesPerDimension(self):
+        return np.array([n + 1 for n in self._ne])
+
+    def getDirichletMask(self):
+        m = np.zeros(self.numNodes(), dtype=np.uint8)
+        check(_lib().vfem_mg2_level_dirichlet_mask(self._mg._h, self._l, m.ctypes.data_as(_capi._u8)))
+        return np.stack([(m >> c) & 1 for c in range(2)], axis=1).astype(bool)
+
+
+class MultigridSolver2D:
+    """MultigridSolver<double, 1, 1> (MultigridSolver.hh) over a TensorProductSimulator_2D."""
+
+    def __init__(self, tps, numCoarseningLevels):
+        h = C.c_void_p()
+        check(_lib().vfem_mg2_create(tps._h, int(numCoarseningLevels), C.byref(h)))
+        self._h = h
+        self._tps = tps
+        n = C.c_int()
+        check(_lib().vfem_mg2_num_levels(h, C.byref(n)))
+        self.numLevels = n.value
+        self.lastStats = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.vfem_mg2_destroy(h)
+            self._h = None
+
+    def _nn(self, l):
+        return self.getSimulator(l).numNodes()
+
+    def getSimulator(self, l):
+        if l == 0:
+            return self._tps
+        if l < 0 or l >= self.numLevels:
+            raise IndexError("level out of range")
+        return _LevelSimulator2D(self, l)
+
+    def setPrecision(self, precision="fp64", outerMatvec="df"):
+        """The 2D solver runs in FP64 only."""
+        if precision != "fp64":
+            raise RuntimeError("the 2D multigrid solver supports precision 'fp64' only")
+
+    def setUseGraphs(self, use):
+        check(_lib().vfem_mg2_set_use_graphs(self._h, int(bool(use))))
+
+    def setSymmetricGaussSeidel(self, symmetric):
+        check(_lib().vfem_mg2_set_symmetric_gs(self._h, int(bool(symmetric))))
+
+    def setFabricationMaskHeightByLayer(self, h):
+        check(_lib().vfem_mg2_set_mask_layer(self._h, int(h)))
+
+    def updateStiffnessMatrices(self):
+        check(_lib().vfem_mg2_update_stiffness(self._h))
+
+    def applyK(self, l, u):
+        nn = self._nn(l)
+        u = _as_vfield(u, nn, 2)
+        out = _new_vfield(nn, 2)
+        check(_lib().vfem_mg2_apply_k(self._h, int(l), ptr(u), ptr(out)))
+        return out
+
+    def computeResidual(self, l, u, b):
+        nn = self._nn(l)
+        u, b = _as_vfield(u, nn, 2), _as_vfield(b, nn, 2)
+        out = _new_vfield(nn, 2)
+        check(_lib().vfem_mg2_residual(self._h, int(l), ptr(u), ptr(b), ptr(out)))
+        return out
+
+    def zeroOutDirichletComponents(self, l, u):
+        u = _as_vfield(u, self._nn(l), 2).copy(order="F")
+        check(_lib().vfem_mg2_zero_dirichlet(self._h, int(l), ptr(u)))
+        return u
+
+    def smoothingMulticoloredGS(self, l, u, b, forwardSweep=True):
+        nn = self._nn(l)
+        u = _as_vfield(u, nn, 2).copy(order="F")
+        b = _as_vfield(b, nn, 2)
+        check(_lib().vfem_mg2_smooth(self._h, int(l), ptr(u), ptr(b), int(bool(forwardSweep))))
+        return u
+
+    def restriction(self, l, fine):
+        fine = _as_vfield(fine, self._nn(l), 2)
+        out = _new_vfield(self._nn(l + 1), 2)
+        check(_lib().vfem_mg2_restrict(self._h, int(l), ptr(fine), ptr(out)))
+        return out
+
+    def interpolation(self, l, coarse, fine=None, accumulate=False):
+        coarse = _as_vfield(coarse, self._nn(l + 1), 2)
+        out = _new_vfield(self._nn(l), 2) if fine is None else _as_vfield(fine, self._nn(l), 2).copy(order="F")
+        check(_lib().vfem_mg2_interpolate(self._h, int(l), ptr(coarse), ptr(out), int(bool(accumulate))))
+        return out
+
+    def coarseSolve(self, b):
+        nn = self._nn(self.numLevels - 1)
+        b = _as_vfield(b, nn, 2)
+        out = _new_vfield(nn, 2)
+        check(_lib().vfem_mg2_coarse_solve(self._h, ptr(b), ptr(out)))
+        return out
+
+    def solve(self, u, f, numSteps, numSmoothingSteps, stiffnessUpdated=False, zeroDirichlet=False,
+              it_callback=None, fullMultigrid=False):
+        nn = self._nn(0)
+        u, f = _as_vfield(u, nn, 2), _as_vfield(f, nn, 2)
+        if it_callback is None:
+            out = _new_vfield(nn, 2)
+            check(_lib().vfem_mg2_solve(self._h, ptr(u), ptr(f), int(numSteps), int(numSmoothingSteps),
+                                        int(bool(zeroDirichlet)), int(bool(fullMultigrid)), ptr(out)))
+            return out
+        x = u
+        for i in range(int(numSteps)):
+            out = _new_vfield(nn, 2)
+            check(_lib().vfem_mg2_solve(self._h, ptr(x), ptr(f), 1, int(numSmoothingSteps), int(bool(zeroDirichlet)),
+                                        int(bool(fullMultigrid) and i == 0), ptr(out)))
+            it_callback(i, out)
+            x = out
+        return x
+
+    def preconditionedConjugateGradient(self, u, b, maxIter, tol, it_callback=None, mgIterations=1,
+                                        mgSmoothingIterations=1, fullMultigrid=False):
+        nn = self._nn(0)
+        x = _as_vfield(u, nn, 2).copy(order="F")
+        b = _as_vfield(b, nn, 2)
+        stats = _capi.PcgStats()
+        cb = _capi.PCG_CALLBACK()
+        if it_callback is not None:
+            def _cb(user, it, rnorm, xdev, rdev):
+                it_callback(int(it), _device_to_host(xdev, nn, 2), _device_to_host(rdev, nn, 2))
+                return 0
+            cb = _capi.PCG_CALLBACK(_cb)
+        check(_lib().vfem_mg2_pcg(self._h, ptr(x), ptr(b), int(maxIter), float(tol), int(mgIterations),
+                                  int(mgSmoothingIterations), int(bool(fullMultigrid)), 0, cb, None, C.byref(stats)))
+        self.lastStats = stats
+        return x
+
+    def timeKernel(self, kernel, reps=20):
+        """Average device milliseconds of one launch (0 applyK, 1 GS sweep, 2 V-cycle, 3 PCG iteration)."""
+        ms = C.c_double()
+        check(_lib().vfem_mg2_time_kernel(self._h, int(kernel), int(reps), C.byref(ms)))
+        return ms.value
