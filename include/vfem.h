@@ -333,6 +333,13 @@ int vfem_langelaar_create(const int64_t dims[3], vfem_langelaar **out);
 int vfem_langelaar_destroy(vfem_langelaar *h);
 int vfem_langelaar_apply(vfem_langelaar *h, const double *in, double *out);
 int vfem_langelaar_backprop(vfem_langelaar *h, const double *g, const double *vars, double *out);
+/* The same filters on 2D grids (the reference's N = 2 instantiations; the Langelaar region is the
+ * voxel below and its x neighbours). The 2D Langelaar handle takes vfem_langelaar_apply/_backprop/_destroy. */
+int vfem_upsample_filter2(const int64_t in_dims[2], int64_t factor, const double *in, double *out);
+int vfem_upsample_filter2_backprop(const int64_t in_dims[2], int64_t factor, const double *g, double *out);
+int vfem_vertex_to_cell_filter2(const int64_t vertex_dims[2], const double *in, double *out);
+int vfem_vertex_to_cell_filter2_backprop(const int64_t vertex_dims[2], const double *g, double *out);
+int vfem_langelaar2_create(const int64_t dims[2], vfem_langelaar **out);
 
 /* ---------------- 2D: TensorProductSimulator<double, 1, 1> / MultigridSolver<double, 1, 1> ----------------
  * The bilinear-quadrilateral instantiation the module registers beside the 3D one
@@ -399,6 +406,14 @@ int vfem_mg2_pcg(vfem_mg2 *mg, double *x_inout, const double *b, int64_t max_ite
 int vfem_mg2_time_kernel(vfem_mg2 *mg, int kernel, int reps, double *ms);
 /* TopologyOptimizationProblem + MultigridComplianceObjective over the 2D solver; the handle takes
  * every vfem_problem_* call (filters as in vfem_problem_create, smoothing over the 2D neighbourhood). */
+/* Layer-by-layer evaluation over a 2D simulator: as vfem_lbl_create / _set_init / _run (FP64 solves). */
+typedef struct vfem_lbl2 vfem_lbl2;
+int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, vfem_lbl2 **out);
+int vfem_lbl2_destroy(vfem_lbl2 *e);
+int vfem_lbl2_set_init(vfem_lbl2 *e, int kind, int history);
+int vfem_lbl2_run(vfem_lbl2 *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
+                  int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, int zero_init,
+                  double *compliance_out, int64_t *iterations_out, double *gradient_sum_out);
 /* SmoothingFilter::apply on a 2D (dims[0], dims[1]) grid (ApplyImpl<2>, TopologyOptimizationFilter.hh:329-397) */
 int vfem_smoothing_filter2(const int64_t dims[2], int radius, int type, const double *in, double *out);
 int vfem_problem2_create(vfem_mg2 *mg, int num_filters, const int *kinds, const int *radii, const int *types,

@@ -1,6 +1,7 @@
 """numpy restatements of the reference's UpsampleFilter, VertexToCellFilter and LangelaarFilter
 (TopologyOptimizationFilter.hh:402-709), the oracle of the GPU filters (test infrastructure
-only). Grids are row-major 3D arrays (x slowest, z fastest)."""
+only). Grids are row-major 3D arrays (x slowest, z fastest); the *_2d functions and
+Langelaar(shape, ndim=2) restate the N = 2 instantiations on (x, y) arrays."""
 import numpy as np
 
 
@@ -57,11 +58,13 @@ def vertex_to_cell_backprop(g):
 class Langelaar:
     """LangelaarFilter (:577-709) with NDVector::visitSupportingRegion (NDVector.hh:211-229) as
     written: below, x -/+ 1 below, two below, and the voxel itself (whose output value is the one
-    left by the previous application; the output buffer starts at zero)."""
+    left by the previous application; the output buffer starts at zero). For N = 2 the loop over
+    d stops after d = 0: below and x -/+ 1 below only (shape (nx, ny), held as (nx, ny, 1))."""
     P, Q, EPS = 40.0, 40.0 - 1.58, 1e-4
 
-    def __init__(self, shape):
-        self.shape = tuple(shape)
+    def __init__(self, shape, ndim=3):
+        self.ndim = ndim
+        self.shape = tuple(shape) + ((1,) if ndim == 2 else ())
         self.out = np.zeros(self.shape)
 
     def region(self, i, j, k):
@@ -70,6 +73,8 @@ class Langelaar:
             r.append((i - 1, j - 1, k))
         if i + 1 < self.shape[0]:
             r.append((i + 1, j - 1, k))
+        if self.ndim == 2:
+            return r
         if j - 2 >= 0:
             r.append((i, j - 2, k))
         r.append((i, j, k))
@@ -112,3 +117,43 @@ class Langelaar:
         d1 = 0.5 * (1 - (v - self.smax) / np.sqrt((v - self.smax) ** 2 + E))
         out[:, 1:, :] = lam[:, 1:, :] * d1[:, 1:, :]
         return out
+
+
+def _flat3(a):
+    a = np.asarray(a, dtype=np.float64)
+    return a[:, :, None]
+
+
+def upsample_2d(a, F):
+    """UpsampleFilter::ApplyImpl<1, 1>: bilinear upsampling of an (x, y) node grid."""
+    a = np.asarray(a, dtype=np.float64)
+    out = np.zeros(tuple((s - 1) * F + 1 for s in a.shape))
+    t = np.arange(F + 1) / F
+    w = [1.0 - t, t]
+    for i in range(a.shape[0] - 1):
+        for j in range(a.shape[1] - 1):
+            blk = np.zeros((F + 1, F + 1))
+            for c in range(4):
+                b0, b1 = (c >> 1) & 1, c & 1
+                blk += a[i + b0, j + b1] * (w[b0][:, None] * w[b1][None, :])
+            out[i * F:i * F + F + 1, j * F:j * F + F + 1] = blk
+    return out
+
+
+def upsample_backprop_2d(g, in_shape, F):
+    """UpsampleFilter::BackpropImpl<1, 1>."""
+    return upsample_backprop(_flat3(g), tuple(in_shape) + (1,), F)[:, :, 0]
+
+
+def vertex_to_cell_2d(v):
+    v = np.asarray(v, dtype=np.float64)
+    return 0.25 * sum(v[a:a + v.shape[0] - 1, b:b + v.shape[1] - 1] for a in (0, 1) for b in (0, 1))
+
+
+def vertex_to_cell_backprop_2d(g):
+    g = np.asarray(g, dtype=np.float64)
+    out = np.zeros(tuple(s + 1 for s in g.shape))
+    for a in (0, 1):
+        for b in (0, 1):
+            out[a:a + g.shape[0], b:b + g.shape[1]] += g
+    return 0.25 * out

@@ -646,3 +646,62 @@ class TOP2:
             if viol > 0:
                 self.lambda_max = lmid
         self.setVars(step(lmid))
+
+
+def _lbl_init(method):
+    if method == "zero":
+        return "zero", 0
+    if method == "constant":
+        return "fd", 1
+    if method == "fd":
+        return "fd", 2
+    if isinstance(method, str) and method.startswith("N="):
+        return "subspace", int(method[2:])
+    raise RuntimeError("Unrecognized method " + str(method))
+
+
+def layer_by_layer(sim, mg, method="N=3", zero_init=True, layer_increment=1, max_iter=500, tol=1e-8,
+                   mg_iterations=1, mg_smoothing_iterations=1, fmg=False, u_full=None):
+    """LayerByLayerEvaluator::run (LayerByLayer.hh:223-296) with its initial-guess generators
+    (LayerByLayer.hh:55-209) on the 2D simulator: heights ny, ny - inc, ..., each solved from a
+    guess built from the previous heights' solutions ("fd": u(0) or 2 u(0) - u(1); "constant":
+    u(0); "N=<s>": Galerkin projection onto the last s solutions, A_ij = u_i . K u_j,
+    b_i = u_i . f over the nondetached nodes of the new mask, minimum-norm least squares with
+    singular values <= s eps sigma_max dropped). Returns (layers, compliances, PCG iterations,
+    gradient sum, full-design solution)."""
+    kind, nmax = _lbl_init(method)
+    ny = sim.ne[1]
+    hist, layers, comps, iters = [], [], [], []
+    grad = np.zeros(sim.NE)
+    l = ny
+    while l > 0:
+        mg.setFabricationMaskHeightByLayer(l)
+        live = np.tile(sim.nJ <= l, 2)
+        f = sim.buildLoadVector()
+        s = len(hist)
+        if not zero_init and l == ny and u_full is not None:
+            g = u_full.copy()
+        elif kind == "zero" or s == 0:
+            g = np.zeros(2 * sim.NN)
+        elif kind == "fd":
+            g = hist[0].copy() if s == 1 else 2.0 * hist[0] - hist[1]
+        else:
+            Ku = [sim.applyK(u) for u in hist]
+            A = np.array([[float(np.dot(hist[i][live], Ku[j][live])) for j in range(s)] for i in range(s)])
+            A = 0.5 * (A + A.T)
+            b = np.array([float(np.dot(hist[i][live], f[live])) for i in range(s)])
+            c = np.linalg.lstsq(A, b, rcond=s * np.finfo(np.float64).eps)[0]
+            g = sum(c[i] * hist[i] for i in range(s))
+        g[~live] = 0.0
+        u = mg.pcg(g, f, max_iter, tol, mg_iterations, mg_smoothing_iterations, fmg, dirichletSatisfied=True)
+        layers.append(l)
+        comps.append(float(np.dot(f[live], u[live])))
+        iters.append(mg.lastIterations)
+        grad += sim.complianceGradient(u)
+        if l == ny:
+            u_full = u.copy()
+        if l >= layer_increment and nmax > 0:
+            hist.insert(0, u.copy())
+            del hist[nmax:]
+        l -= min(layer_increment, l)
+    return np.array(layers), np.array(comps), np.array(iters), grad, u_full

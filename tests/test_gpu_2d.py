@@ -239,3 +239,41 @@ def test_bc_file_2d(gpu, tmp_path):
     assert f[16 * nn[1] + 0, 1] == -1.0 and np.count_nonzero(f) == 1
     V, F = tps.getMesh()
     assert V.shape == (tps.numNodes(), 3) and F.shape == (tps.numElements(), 4)
+
+
+def lbl_pair(ne=(32, 16), seed=11):
+    rng = np.random.default_rng(seed)
+    bbox = ((0.0, 0.0), (2.0, 1.0))
+    tps = pv.TensorProductSimulator([1, 1], [list(bbox[0]), list(bbox[1])], list(ne))
+    sim = o2.Sim2(ne, bbox[0], bbox[1])
+    tps.ETensor = (1.0, 0.3)
+    sim.setMaterial(1.0, 0.3)
+    rho = rng.uniform(0.3, 1.0, sim.NE)
+    tps.setDensities(rho)
+    sim.setDensities(rho)
+    mn, mx = [-1e-9, -1e-9], [bbox[1][0] + 1e-9, 1e-9]
+    tps.addDirichletCondition([0, 0], mn, mx, "xy")
+    sim.addDirichletCondition([0, 0], mn, mx, "xy")
+    tps.gravity = [0.0, -1.0]
+    sim.grav = np.array([0.0, -1.0])
+    return tps, sim
+
+
+@pytest.mark.parametrize("method,slots,inc", [("zero", 4, 1), ("fd", 1, 1), ("N=3", 1, 1), ("N=2", 2, 3),
+                                              ("constant", 1, 2)])
+def test_layer_by_layer_2d(gpu, method, slots, inc):
+    tps, sim = lbl_pair()
+    mg = tps.multigridSolver(2)
+    lbl = pv.LayerByLayerEvaluator(tps)
+    lbl.selectInitMethod(method)
+    lbl.run(mg, True, inc, 200, 1e-8, None, 1, 1, False, slots=slots)
+    omg = o2.MG2(sim, 2)
+    layers, comps, iters, grad, _ = o2.layer_by_layer(sim, omg, method, True, inc, 200, 1e-8, 1, 1, False)
+    np.testing.assert_array_equal(lbl.layers, layers)
+    same_path = slots == 1 or method == "zero"
+    assert rel(lbl.compliances, comps) < (1e-9 if same_path else 1e-6)
+    if same_path:
+        np.testing.assert_array_equal(lbl.iterations, iters)
+    n = len(layers)
+    assert rel(lbl.gradient(), grad / n) < 1e-6
+    assert abs(lbl.objective() - 0.5 * comps.sum() / n) < 1e-7 * abs(lbl.objective())

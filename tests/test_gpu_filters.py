@@ -78,3 +78,40 @@ def test_filter_chain_dimensions(gpu):
     g = rng.standard_normal(int(np.prod(out)))
     gb = chain.backprop(g)
     assert gb.size == 125
+
+
+# ---- 2D instantiations ----
+@pytest.mark.parametrize("shape,factor", [((5, 4), 2), ((3, 6), 3)])
+def test_upsample_2d(gpu, shape, factor):
+    rng = np.random.default_rng(10)
+    x = rng.uniform(0, 1, shape)
+    f = pv.UpsampleFilter(factor)
+    f.setInputDimensions(shape)
+    y = f.apply(x.ravel())
+    assert rel(y, of.upsample_2d(x, factor)) < 1e-14
+    g = rng.standard_normal(tuple((s - 1) * factor + 1 for s in shape))
+    assert rel(f.backprop(g.ravel()), of.upsample_backprop_2d(g, shape, factor)) < 1e-13
+
+
+def test_vertex_to_cell_2d(gpu):
+    rng = np.random.default_rng(11)
+    v = rng.uniform(0, 1, (7, 5))
+    f = pv.VertexToCellFilter()
+    f.setInputDimensions(v.shape)
+    np.testing.assert_array_equal(f.outputDimensions, (6, 4))
+    assert rel(f.apply(v.ravel()), of.vertex_to_cell_2d(v)) < 1e-15
+    g = rng.standard_normal((6, 4))
+    assert rel(f.backprop(g.ravel()), of.vertex_to_cell_backprop_2d(g)) < 1e-15
+
+
+def test_langelaar_2d(gpu):
+    rng = np.random.default_rng(12)
+    shape = (9, 7)
+    f = pv.LangelaarFilter()
+    f.setInputDimensions(shape)
+    ref = of.Langelaar(shape, ndim=2)
+    for _ in range(2):
+        x = rng.uniform(0.05, 1, shape)
+        assert rel(f.apply(x.ravel()), ref.apply(x).ravel()) < 1e-11
+        g = rng.standard_normal(shape)
+        assert rel(f.backprop(g.ravel(), x.ravel()), ref.backprop(g, x).ravel()) < 1e-11

@@ -106,3 +106,23 @@ def test_compliance_gradient_fd():
         d[e] = 1e-6
         fd = (compliance(rho + d)[0] - compliance(rho - d)[0]) / 2e-6
         assert abs(fd - g[e]) < 1e-6 * max(abs(g[e]), 1e-3)
+
+
+def test_langelaar_2d_gradient_fd():
+    from oracle import filters as of
+    rng = np.random.default_rng(3)
+    shape = (6, 5)
+    x = rng.uniform(0.2, 0.9, shape)
+    g = rng.standard_normal(shape)
+    L = of.Langelaar(shape, ndim=2)
+    L.apply(x)
+    grad = L.backprop(g, x)[:, :, 0]
+
+    def J(xx):
+        return float(np.sum(g * of.Langelaar(shape, ndim=2).apply(xx)[:, :, 0]))
+
+    for idx in [(0, 0), (3, 2), (5, 4), (2, 1)]:
+        d = np.zeros(shape)
+        d[idx] = 1e-6
+        fd = (J(x + d) - J(x - d)) / 2e-6
+        assert abs(fd - grad[idx]) < 1e-6 * max(1.0, abs(grad[idx]))

@@ -186,6 +186,16 @@ _SIGS = {
     "vfem_mg2_pcg": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
                               PCG_CALLBACK, C.c_void_p, C.POINTER(PcgStats)]),
     "vfem_mg2_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _d]),
+    "vfem_lbl2_create": (C.c_int, [_vp, C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]),
+    "vfem_lbl2_destroy": (C.c_int, [_vp]),
+    "vfem_lbl2_set_init": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "vfem_lbl2_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                                _vp, _vp, _vp]),
+    "vfem_upsample_filter2": (C.c_int, [_i64, C.c_int64, _vp, _vp]),
+    "vfem_upsample_filter2_backprop": (C.c_int, [_i64, C.c_int64, _vp, _vp]),
+    "vfem_vertex_to_cell_filter2": (C.c_int, [_i64, _vp, _vp]),
+    "vfem_vertex_to_cell_filter2_backprop": (C.c_int, [_i64, _vp, _vp]),
+    "vfem_langelaar2_create": (C.c_int, [_i64, C.POINTER(_vp)]),
     "vfem_smoothing_filter2": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp]),
     "vfem_problem2_create": (C.c_int, [_vp, C.c_int, _i32, _i32, _i32, _d, C.c_double, C.POINTER(_vp)]),
 }

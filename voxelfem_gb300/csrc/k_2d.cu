@@ -580,6 +580,25 @@ __global__ void gravity2_kernel(Geom2 g, const double *__restrict__ rho, double 
     f[g.NN + n] += gy * s;
 }
 
+// x = sum_i c_i u_i on the nondetached rows, 0 on the detached ones (the layer-by-layer
+// initial guesses, LayerByLayer.hh:55-209); c from device memory (cDev) or by value
+__global__ void __launch_bounds__(BS) subspace_combine2_kernel(Geom2 g, LblVectors U, int s, const double *cDev,
+                                                               LblCoeffs cv, double *__restrict__ x) {
+    const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (n >= g.NN) return;
+    const bool live = (int)(n % g.nn[1]) < g.nyv();
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        double v = 0.0;
+        if (live) {
+#pragma unroll
+            for (int i = 0; i < LBL_MAX_HISTORY; ++i)
+                if (i < s) v += (cDev ? cDev[i] : cv.c[i]) * U.u[i][c * g.NN + n];
+        }
+        x[c * g.NN + n] = v;
+    }
+}
+
 unsigned colorBlocks(const Geom2 &g) {
     const int64_t per = (int64_t)((g.nn[0] + 1) / 2) * ((g.nn[1] + 1) / 2);
     return gridFor(per, BS);
@@ -716,6 +735,13 @@ void launch2_element_energy(const Geom2 &g, const double *Y, const double *u, do
 void launch2_gravity_load(const Geom2 &g, const double *rho, double *f, const double grav[2], double vol,
                           cudaStream_t st) {
     gravity2_kernel<<<gridFor(g.NN, BS), BS, 0, st>>>(g, rho, f, grav[0], grav[1], vol);
+    VFEM_LAUNCH_CHECK();
+}
+
+void launch2_subspace_combine(const Geom2 &g, const LblVectors &U, int s, const double *cDev, const LblCoeffs &cv,
+                              double *x, cudaStream_t st) {
+    if (s < 0 || s > LBL_MAX_HISTORY) throw Error(ERR_ARG, "history size out of range");
+    subspace_combine2_kernel<<<gridFor(g.NN, BS), BS, 0, st>>>(g, U, s, cDev, cv, x);
     VFEM_LAUNCH_CHECK();
 }
 

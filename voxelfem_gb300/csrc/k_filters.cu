@@ -20,7 +20,7 @@ __device__ __forceinline__ int64_t flat3(int i, int j, int k, int d1, int d2) {
 // c = min(n / F, in - 2) at local coordinate t = (n - F c) / F; the trilinear interpolant of the
 // cell's 8 coarse values is sampled there. Nodes shared by cells get weights exactly 0 or 1, so
 // every cell gives them the same value.
-__global__ void upsample_kernel(int a0, int a1, int a2, int F, const double *__restrict__ in,
+__global__ void upsample_kernel(int a0, int a1, int a2, int F, int flat, const double *__restrict__ in,
                                 double *__restrict__ out) {
     const int f1 = (a1 - 1) * F + 1, f2 = (a2 - 1) * F + 1;
     const int64_t nf = (int64_t)((a0 - 1) * F + 1) * f1 * f2;
@@ -32,13 +32,14 @@ __global__ void upsample_kernel(int a0, int a1, int a2, int F, const double *__r
     double x[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        c[d] = min(n[d] / F, a[d] - 2);
+        c[d] = (flat && d == 2) ? 0 : min(n[d] / F, a[d] - 2);
         x[d] = (double)(n[d] - F * c[d]) / (double)F;
     }
     double v = 0.0;
 #pragma unroll
     for (int corner = 0; corner < 8; ++corner) {
         const int b0 = (corner >> 2) & 1, b1 = (corner >> 1) & 1, b2 = corner & 1;
+        if (flat && b2) continue;  // 2D grid: no z axis
         const double w = (b0 ? x[0] : 1.0 - x[0]) * (b1 ? x[1] : 1.0 - x[1]) * (b2 ? x[2] : 1.0 - x[2]);
         v += w * in[flat3(c[0] + b0, c[1] + b1, c[2] + b2, a1, a2)];
     }
@@ -77,31 +78,36 @@ __global__ void upsample_backprop_kernel(int a0, int a1, int a2, int F, const do
 
 // VertexToCellFilter (:536-575): cell value = mean of its 8 corner values; backprop gives each
 // vertex 1/8 of the gradients of the cells containing it.
-__global__ void vertex_to_cell_kernel(int v0, int v1, int v2, const double *__restrict__ in, double *__restrict__ out) {
-    const int e1 = v1 - 1, e2 = v2 - 1;
+// flat: a 2D grid (v2 == 1, no z axis): cell = mean of its 4 corners.
+__global__ void vertex_to_cell_kernel(int v0, int v1, int v2, int flat, const double *__restrict__ in,
+                                      double *__restrict__ out) {
+    const int e1 = v1 - 1, e2 = flat ? 1 : v2 - 1;
     const int64_t ne = (int64_t)(v0 - 1) * e1 * e2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= ne) return;
     const int k = (int)(t % e2), j = (int)((t / e2) % e1), i = (int)(t / ((int64_t)e1 * e2));
     double s = 0.0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) s += in[flat3(i + ((c >> 2) & 1), j + ((c >> 1) & 1), k + (c & 1), v1, v2)];
-    out[t] = s * 0.125;
+    for (int c = 0; c < 8; ++c) {
+        if (flat && (c & 1)) continue;
+        s += in[flat3(i + ((c >> 2) & 1), j + ((c >> 1) & 1), k + (c & 1), v1, v2)];
+    }
+    out[t] = s * (flat ? 0.25 : 0.125);
 }
 
-__global__ void vertex_to_cell_backprop_kernel(int v0, int v1, int v2, const double *__restrict__ g,
+__global__ void vertex_to_cell_backprop_kernel(int v0, int v1, int v2, int flat, const double *__restrict__ g,
                                                double *__restrict__ out) {
     const int64_t nv = (int64_t)v0 * v1 * v2;
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= nv) return;
-    const int e0 = v0 - 1, e1 = v1 - 1, e2 = v2 - 1;
+    const int e0 = v0 - 1, e1 = v1 - 1, e2 = flat ? 1 : v2 - 1;
     const int k = (int)(t % v2), j = (int)((t / v2) % v1), i = (int)(t / ((int64_t)v1 * v2));
     double s = 0.0;
     for (int a = i - 1; a <= i; ++a)
         for (int b = j - 1; b <= j; ++b)
-            for (int c = k - 1; c <= k; ++c)
+            for (int c = flat ? k : k - 1; c <= k; ++c)
                 if (a >= 0 && b >= 0 && c >= 0 && a < e0 && b < e1 && c < e2) s += g[flat3(a, b, c, e1, e2)];
-    out[t] = s * 0.125;
+    out[t] = s * (flat ? 0.25 : 0.125);
 }
 
 // ---- LangelaarFilter (:577-709), build direction y ----
@@ -110,7 +116,8 @@ __global__ void vertex_to_cell_backprop_kernel(int v0, int v1, int v2, const dou
 // (i-1, j-1, k) and (i+1, j-1, k), and for d = 1 (the build axis itself) (i, j-2, k) and
 // (i, j, k) -- the voxel itself, whose output value at that point is the one left by the
 // previous application. z neighbours are not in the region, so every z plane is independent:
-// one CTA per plane walks the layers with a barrier between them.
+// one CTA per plane walks the layers with a barrier between them. On a 2D grid (flat: N = 2,
+// d2 == 1) the loop over d stops after d = 0: the region is the voxel below and its x neighbours.
 constexpr double LP = 40.0, LQ = 40.0 - 1.58, LEPS = 1e-4;
 
 __device__ __forceinline__ double lsmin(double a, double b) {
@@ -124,10 +131,11 @@ __device__ __forceinline__ double dsmin2(double a, double b) {
 }
 
 // sum over the supporting region of f^P (with the indices of the region's members)
-__device__ __forceinline__ double support_sum(const double *f, int i, int j, int k, int d0, int d1, int d2) {
+__device__ __forceinline__ double support_sum(const double *f, int i, int j, int k, int d0, int d1, int d2, int flat) {
     double s = pow(f[flat3(i, j - 1, k, d1, d2)], LP);
     if (i - 1 >= 0) s += pow(f[flat3(i - 1, j - 1, k, d1, d2)], LP);
     if (i + 1 < d0) s += pow(f[flat3(i + 1, j - 1, k, d1, d2)], LP);
+    if (flat) return s;
     if (j - 2 >= 0) s += pow(f[flat3(i, j - 2, k, d1, d2)], LP);
     s += pow(f[flat3(i, j, k, d1, d2)], LP);
     return s;
@@ -135,14 +143,14 @@ __device__ __forceinline__ double support_sum(const double *f, int i, int j, int
 
 // out holds the previous application's output on entry (its own-voxel term); smax and the
 // filtered field are kept for the backprop.
-__global__ void langelaar_apply_kernel(int d0, int d1, int d2, const double *__restrict__ in, double *out,
+__global__ void langelaar_apply_kernel(int d0, int d1, int d2, int flat, const double *__restrict__ in, double *out,
                                        double *__restrict__ smaxOut) {
     const int k = blockIdx.x;
     for (int i = threadIdx.x; i < d0; i += blockDim.x) out[flat3(i, 0, k, d1, d2)] = in[flat3(i, 0, k, d1, d2)];
     __syncthreads();
     for (int j = 1; j < d1; ++j) {
         for (int i = threadIdx.x; i < d0; i += blockDim.x) {
-            const double sm = pow(support_sum(out, i, j, k, d0, d1, d2), 1.0 / LQ);
+            const double sm = pow(support_sum(out, i, j, k, d0, d1, d2, flat), 1.0 / LQ);
             const int64_t e = flat3(i, j, k, d1, d2);
             smaxOut[e] = sm;
             out[e] = lsmin(in[e], sm);
@@ -153,7 +161,7 @@ __global__ void langelaar_apply_kernel(int d0, int d1, int d2, const double *__r
 
 // computeLagrangeMultipliers (:620-640) and backprop (:598-606). vars: the filter's input,
 // filt / smax: cached from the last apply. lam: scratch (the multipliers).
-__global__ void langelaar_backprop_kernel(int d0, int d1, int d2, const double *__restrict__ g,
+__global__ void langelaar_backprop_kernel(int d0, int d1, int d2, int flat, const double *__restrict__ g,
                                           const double *__restrict__ vars, const double *__restrict__ filt,
                                           const double *__restrict__ smax, double *lam, double *__restrict__ out) {
     const int k = blockIdx.x;
@@ -168,7 +176,7 @@ __global__ void langelaar_backprop_kernel(int d0, int d1, int d2, const double *
             for (int ip = i - 1; ip <= i + 1; ++ip) {
                 if (ip < 0 || ip >= d0) continue;
                 const int64_t e = flat3(ip, up, k, d1, d2);
-                const double S = support_sum(filt, ip, up, k, d0, d1, d2);
+                const double S = support_sum(filt, ip, up, k, d0, d1, d2, flat);
                 const double fm = filt[flat3(i, L, k, d1, d2)];
                 const double der = dsmin2(vars[e], smax[e]) * (LP * pow(fm, LP - 1) / LQ * pow(S, 1.0 / LQ - 1));
                 acc += lam[e] * der;
@@ -176,10 +184,10 @@ __global__ void langelaar_backprop_kernel(int d0, int d1, int d2, const double *
             lam[flat3(i, L, k, d1, d2)] = acc;
         }
         __syncthreads();
-        // the own-voxel term of layer L+1 (the last member visited, :631-637)
-        for (int i = threadIdx.x; i < d0; i += blockDim.x) {
+        // the own-voxel term of layer L+1 (the last member visited, :631-637); not a member in 2D
+        for (int i = threadIdx.x; i < d0 && !flat; i += blockDim.x) {
             const int64_t e = flat3(i, up, k, d1, d2);
-            const double S = support_sum(filt, i, up, k, d0, d1, d2);
+            const double S = support_sum(filt, i, up, k, d0, d1, d2, flat);
             const double der = dsmin2(vars[e], smax[e]) * (LP * pow(filt[e], LP - 1) / LQ * pow(S, 1.0 / LQ - 1));
             lam[e] += lam[e] * der;
         }
@@ -194,9 +202,9 @@ __global__ void langelaar_backprop_kernel(int d0, int d1, int d2, const double *
 
 }  // namespace
 
-void launch_upsample(const int dims[3], int factor, const double *in, double *out, cudaStream_t st) {
+void launch_upsample(const int dims[3], int factor, const double *in, double *out, cudaStream_t st, int ndim) {
     const int64_t nf = (int64_t)((dims[0] - 1) * factor + 1) * ((dims[1] - 1) * factor + 1) * ((dims[2] - 1) * factor + 1);
-    upsample_kernel<<<gridFor(nf, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], factor, in, out);
+    upsample_kernel<<<gridFor(nf, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], factor, ndim == 2 ? 1 : 0, in, out);
     VFEM_LAUNCH_CHECK();
 }
 void launch_upsample_backprop(const int dims[3], int factor, const double *g, double *out, cudaStream_t st) {
@@ -204,25 +212,27 @@ void launch_upsample_backprop(const int dims[3], int factor, const double *g, do
                                                                                               dims[2], factor, g, out);
     VFEM_LAUNCH_CHECK();
 }
-void launch_vertex_to_cell(const int vdims[3], const double *in, double *out, cudaStream_t st) {
-    vertex_to_cell_kernel<<<gridFor((int64_t)(vdims[0] - 1) * (vdims[1] - 1) * (vdims[2] - 1), BS), BS, 0, st>>>(
-        vdims[0], vdims[1], vdims[2], in, out);
+void launch_vertex_to_cell(const int vdims[3], const double *in, double *out, cudaStream_t st, int ndim) {
+    const int flat = ndim == 2 ? 1 : 0;
+    vertex_to_cell_kernel<<<gridFor((int64_t)(vdims[0] - 1) * (vdims[1] - 1) * (flat ? 1 : vdims[2] - 1), BS), BS, 0,
+                            st>>>(vdims[0], vdims[1], vdims[2], flat, in, out);
     VFEM_LAUNCH_CHECK();
 }
-void launch_vertex_to_cell_backprop(const int vdims[3], const double *g, double *out, cudaStream_t st) {
+void launch_vertex_to_cell_backprop(const int vdims[3], const double *g, double *out, cudaStream_t st, int ndim) {
     vertex_to_cell_backprop_kernel<<<gridFor((int64_t)vdims[0] * vdims[1] * vdims[2], BS), BS, 0, st>>>(
-        vdims[0], vdims[1], vdims[2], g, out);
+        vdims[0], vdims[1], vdims[2], ndim == 2 ? 1 : 0, g, out);
     VFEM_LAUNCH_CHECK();
 }
-void launch_langelaar(const int dims[3], const double *in, double *out, double *smax, cudaStream_t st) {
+void launch_langelaar(const int dims[3], const double *in, double *out, double *smax, cudaStream_t st, int ndim) {
     const int threads = dims[0] >= 256 ? 256 : ((dims[0] + 31) / 32) * 32;
-    langelaar_apply_kernel<<<dims[2], threads, 0, st>>>(dims[0], dims[1], dims[2], in, out, smax);
+    langelaar_apply_kernel<<<dims[2], threads, 0, st>>>(dims[0], dims[1], dims[2], ndim == 2 ? 1 : 0, in, out, smax);
     VFEM_LAUNCH_CHECK();
 }
 void launch_langelaar_backprop(const int dims[3], const double *g, const double *vars, const double *filt,
-                               const double *smax, double *lam, double *out, cudaStream_t st) {
+                               const double *smax, double *lam, double *out, cudaStream_t st, int ndim) {
     const int threads = dims[0] >= 256 ? 256 : ((dims[0] + 31) / 32) * 32;
-    langelaar_backprop_kernel<<<dims[2], threads, 0, st>>>(dims[0], dims[1], dims[2], g, vars, filt, smax, lam, out);
+    langelaar_backprop_kernel<<<dims[2], threads, 0, st>>>(dims[0], dims[1], dims[2], ndim == 2 ? 1 : 0, g, vars, filt,
+                                                           smax, lam, out);
     VFEM_LAUNCH_CHECK();
 }
 

@@ -4,8 +4,10 @@
 #include "vfem_2d.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "vfem_kernels.hpp"
 
@@ -291,6 +293,19 @@ void Grid2::elementEnergy(const double *u, double *out) {
     viewOut(vo, out, g.NE * sizeof(double));
     launch2_element_energy(g, Y.p, (const double *)vu.d, (double *)vo.d, K0, stream);
     finishOut(vo, stream);
+}
+
+std::unique_ptr<Grid2> Grid2::clone() const {
+    std::unique_ptr<Grid2> c(new Grid2(g.ne, bmin, bmax));
+    if (c->Eyoung != Eyoung || c->nu != nu) c->setETensor(Eyoung, nu);
+    c->E0 = E0; c->Emin = Emin; c->gamma = gamma; c->q = q; c->law = law;
+    c->grav[0] = grav[0];
+    c->grav[1] = grav[1];
+    c->hmask = hmask;
+    c->hval = hval;
+    c->hforce = hforce;
+    c->uploadBC();
+    return c;
 }
 
 // ---------------------------------------------------------------------------
@@ -666,6 +681,11 @@ static double readDev(const double *dev, cudaStream_t st) {
 // MultigridSolver.hh:1047-1152; x and b are device vectors of 2 NN doubles
 PcgStats MG2::pcgDev(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
                      bool dirichletSatisfied, PcgCallback cb, void *user) {
+    if (L() > 1 && useGraphs && !cb) {
+        // one graph launch runs every iteration (conditional WHILE node)
+        pcgStart(x, b, maxIter, tol, mgIter, sweeps, fmg, dirichletSatisfied);
+        return pcgFinish();
+    }
     syncFine();
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
@@ -696,17 +716,6 @@ PcgStats MG2::pcgDev(double *x, const double *b, int64_t maxIter, double tol, in
             if (cb) cb(user, 1, std::sqrt(rsq), x, rbuf.p);
         }
         stats.rsq = rsq;
-    } else if (useGraphs && !cb) {
-        // one graph launch runs every iteration (conditional WHILE node)
-        VFEM_CUDA(cudaGraphLaunch(loopGraph(x, mgIter, sweeps, fmg), st));
-        VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        VFEM_CUDA(cudaStreamSynchronize(st));
-        stats.iterations = (int64_t)hostSc[9];
-        stats.rsq = hostSc[5];
-        const Key key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, x};
-        launchCounter() += 1 + (graphKernels[key] + 1) * (uint64_t)stats.iterations;
-        if (hostSc[11] < 0.0) throw Error(ERR_NAN, "NaN encountered");
-        if (hostSc[11] > 0.0) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string((int64_t)hostSc[11]));
     } else {
         int64_t i = 0;
         while (i < maxIter && rsq > tol * tol * bnorm2) {
@@ -720,6 +729,43 @@ PcgStats MG2::pcgDev(double *x, const double *b, int64_t maxIter, double tol, in
         stats.rsq = rsq;
     }
     stats.relres = bnorm2 > 0 ? std::sqrt(stats.rsq / bnorm2) : std::sqrt(stats.rsq);
+    return stats;
+}
+
+void MG2::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                   bool dirichletSatisfied) {
+    if (L() == 1) throw Error(ERR_ARG, "the asynchronous solve needs at least one coarsening level");
+    if (pending) throw Error(ERR_STATE, "a solve is already in flight on this solver");
+    if (mgIter > 0) ensureStiffness();
+    else syncFine();
+    cudaStream_t st = fine->stream;
+    const Geom2 &g = lv[0].g;
+    if (!dirichletSatisfied) launch2_enforce_dirichlet(g, x, fine->dmask.p, fine->dval.p, st);
+    launch2_dot_partials(g, b, b, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
+    launch2_applyk_fine(g, fine->Y.p, fine->K0, x, rbuf.p, 1, b, fine->dmask.p, true, nullptr, nullptr, st);
+    launch2_dot_partials(g, rbuf.p, rbuf.p, partials.p, st);
+    launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
+    launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
+    launch_fill<double>(dvec.p, 0.0, 2 * g.NN, st);
+    pendingKey = Key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, x};
+    VFEM_CUDA(cudaGraphLaunch(loopGraph(x, mgIter, sweeps, fmg), st));
+    VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    pending = true;
+}
+
+PcgStats MG2::pcgFinish() {
+    if (!pending) throw Error(ERR_STATE, "no solve in flight");
+    pending = false;
+    VFEM_CUDA(cudaStreamSynchronize(fine->stream));
+    PcgStats stats;
+    stats.iterations = (int64_t)hostSc[9];
+    stats.rsq = hostSc[5];
+    stats.bnorm2 = hostSc[7];
+    launchCounter() += 1 + (graphKernels[pendingKey] + 1) * (uint64_t)stats.iterations;
+    if (hostSc[11] < 0.0) throw Error(ERR_NAN, "NaN encountered");
+    if (hostSc[11] > 0.0) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string((int64_t)hostSc[11]));
+    stats.relres = stats.bnorm2 > 0 ? std::sqrt(stats.rsq / stats.bnorm2) : std::sqrt(stats.rsq);
     return stats;
 }
 
@@ -862,6 +908,219 @@ double MG2::timeKernel(int which, int reps) {
     cudaGraphExecDestroy(ex);
     cudaGraphDestroy(gr);
     return ms / reps;
+}
+
+// ---------------------------------------------------------------------------
+// LBL2: layer-by-layer evaluation (LayerByLayerEvaluator::run, LayerByLayer.hh:223-296)
+// ---------------------------------------------------------------------------
+LBL2::Slot::~Slot() {
+    if (done) cudaEventDestroy(done);
+}
+
+LBL2::LBL2(Grid2 *src_, int coarsenings_, int64_t slots) : src(src_), coarsenings(coarsenings_) {
+    if (coarsenings < 1) throw Error(ERR_ARG, "layer-by-layer solves need at least one coarsening level");
+    if (slots < 1) throw Error(ERR_ARG, "slots must be positive");
+    const int64_t NN = src->g.NN, NE = src->g.NE;
+    for (int64_t s = 0; s < slots; ++s) {
+        std::unique_ptr<Slot> sl(new Slot());
+        sl->grid = src->clone();
+        sl->mg.reset(new MG2(sl->grid.get(), coarsenings));
+        sl->x.alloc(2 * NN);
+        sl->f.alloc(2 * NN);
+        sl->gtmp.alloc(NE);
+        sl->gacc.alloc(NE);
+        sl->cpl.alloc(1);
+        sl->part.alloc(REDUCE_BLOCKS + 8);
+        VFEM_CUDA(cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming));
+        S.push_back(std::move(sl));
+    }
+    VFEM_CUDA(cudaMallocHost(&cplHost, slots * sizeof(double)));
+}
+
+LBL2::~LBL2() {
+    for (auto &sl : S) cudaStreamSynchronize(sl->grid->stream);
+    if (cplHost) cudaFreeHost(cplHost);
+}
+
+// Bring every slot's simulator to the source's densities, material and loads.
+void LBL2::syncSource() {
+    VFEM_CUDA(cudaStreamSynchronize(src->stream));
+    for (auto &sl : S) {
+        Grid2 &g = *sl->grid;
+        if (g.Eyoung != src->Eyoung || g.nu != src->nu) g.setETensor(src->Eyoung, src->nu);
+        g.E0 = src->E0; g.Emin = src->Emin; g.gamma = src->gamma; g.q = src->q; g.law = src->law;
+        g.grav[0] = src->grav[0];
+        g.grav[1] = src->grav[1];
+        if (g.hmask != src->hmask || g.hval != src->hval)
+            throw Error(ERR_STATE, "supports changed after the layer-by-layer evaluator was created");
+        if (g.hforce != src->hforce) {
+            g.hforce = src->hforce;
+            g.uploadBC();
+        }
+        VFEM_CUDA(cudaMemcpyAsync(g.rho.p, src->rho.p, src->g.NE * sizeof(double), cudaMemcpyDeviceToDevice, g.stream));
+        g.updateYoungModuli();
+    }
+}
+
+void LBL2::setInit(int kind, int history) {
+    if (kind < LBL_INIT_ZERO || kind > LBL_INIT_SUBSPACE) throw Error(ERR_ARG, "Unrecognized init method");
+    if (kind == LBL_INIT_SUBSPACE && (history < 1 || history > LBL_MAX_HISTORY))
+        throw Error(ERR_ARG, "subspace size must lie in 1.." + std::to_string(LBL_MAX_HISTORY));
+    initKind = kind;
+    historySize = kind == LBL_INIT_CONSTANT ? 1 : kind == LBL_INIT_FD ? 2 : kind == LBL_INIT_SUBSPACE ? history : 0;
+}
+
+// The slot's initial guess for `layer` into sl.x (mask and load of the layer already set),
+// LayerByLayer.hh:55-209.
+void LBL2::guess(Slot &sl, int64_t layer, int ny, bool zeroInit) {
+    Grid2 &g = *sl.grid;
+    MG2 &mg = *sl.mg;
+    cudaStream_t st = g.stream;
+    const int64_t n2 = 2 * g.g.NN;
+    const Geom2 &gl = mg.lv[0].g;  // level 0 with the device mask
+    if (!zeroInit && layer == ny && haveFull) {
+        VFEM_CUDA(cudaMemcpyAsync(sl.x.p, uFull.p, n2 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        return;
+    }
+    const int hs = sl.hs;
+    LblVectors U{};
+    for (int i = 0; i < hs; ++i) U.u[i] = sl.hist[sl.order[i]].p;
+    LblCoeffs cv{};
+    if (initKind == LBL_INIT_ZERO || hs == 0) {
+        launch_fill<double>(sl.x.p, 0.0, n2, st);
+    } else if (initKind == LBL_INIT_CONSTANT || (initKind == LBL_INIT_FD && hs == 1)) {
+        cv.c[0] = 1.0;
+        launch2_subspace_combine(gl, U, 1, nullptr, cv, sl.x.p, st);
+    } else if (initKind == LBL_INIT_FD) {
+        cv.c[0] = 2.0;  // 2 u(0) - u(1)
+        cv.c[1] = -1.0;
+        launch2_subspace_combine(gl, U, 2, nullptr, cv, sl.x.p, st);
+    } else {
+        // InitGenSubspace: A_ij = u_i . K u_j, b_i = u_i . f over the nondetached nodes
+        const int np = hs * (hs + 1) / 2 + hs;
+        sl.subPart.alloc((int64_t)np * REDUCE_BLOCKS);
+        sl.subC.alloc(LBL_MAX_HISTORY);
+        for (int j = 0; j < hs; ++j) {
+            sl.Ku[j].alloc(n2);
+            launch2_applyk_fine(gl, g.Y.p, g.K0, U.u[j], sl.Ku[j].p, 0, nullptr, g.dmask.p, true, nullptr, nullptr, st);
+        }
+        int p = 0;
+        for (int i = 0; i < hs; ++i)
+            for (int j = i; j < hs; ++j, ++p)
+                launch2_dot_partials(gl, U.u[i], sl.Ku[j].p, sl.subPart.p + (int64_t)p * REDUCE_BLOCKS, st);
+        for (int i = 0; i < hs; ++i, ++p)
+            launch2_dot_partials(gl, U.u[i], sl.f.p, sl.subPart.p + (int64_t)p * REDUCE_BLOCKS, st);
+        launch_subspace_solve(sl.subPart.p, REDUCE_BLOCKS, hs, sl.subC.p, st);
+        launch2_subspace_combine(gl, U, hs, sl.subC.p, cv, sl.x.p, st);
+    }
+}
+
+void LBL2::pushHistory(Slot &sl) {
+    if (historySize == 0) return;
+    const int64_t n2 = 2 * sl.grid->g.NN;
+    int slot;
+    if (sl.hs < historySize) {
+        slot = sl.hs;
+        for (int i = sl.hs; i > 0; --i) sl.order[i] = sl.order[i - 1];
+        ++sl.hs;
+    } else {
+        slot = sl.order[sl.hs - 1];
+        for (int i = sl.hs - 1; i > 0; --i) sl.order[i] = sl.order[i - 1];
+    }
+    sl.order[0] = slot;
+    sl.hist[slot].alloc(n2);
+    VFEM_CUDA(cudaMemcpyAsync(sl.hist[slot].p, sl.x.p, n2 * sizeof(double), cudaMemcpyDeviceToDevice, sl.grid->stream));
+}
+
+void LBL2::run(const int64_t *layers, int64_t count, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
+               bool fmg, bool zeroInit, double *compliance, int64_t *iterations, double *gradSum) {
+    if (count <= 0) return;
+    const int ny = src->g.ne[BUILD_DIR];
+    for (int64_t t = 0; t < count; ++t)
+        if (layers[t] < 1 || layers[t] > ny) throw Error(ERR_ARG, "layer height out of range");
+    syncSource();
+    const int64_t ns = std::min<int64_t>((int64_t)S.size(), count);
+    const int64_t NN = src->g.NN, NE = src->g.NE;
+    const bool warm = initKind != LBL_INIT_ZERO;
+    for (auto &slp : S) {
+        slp->queue.clear();
+        slp->qpos = 0;
+        slp->hs = 0;
+        slp->idx = -1;
+    }
+    if (warm) {
+        int64_t t = 0;
+        for (int64_t s = 0; s < ns; ++s) {
+            const int64_t len = count / ns + (s < count % ns ? 1 : 0);
+            for (int64_t k = 0; k < len; ++k) S[s]->queue.push_back(t++);
+        }
+    }
+    for (int64_t s = 0; s < ns; ++s)
+        VFEM_CUDA(cudaMemsetAsync(S[s]->gacc.p, 0, NE * sizeof(double), S[s]->grid->stream));
+    if (!uFull.p) uFull.alloc(2 * NN);
+
+    auto start = [&](int64_t s, int64_t idx) {
+        Slot &sl = *S[s];
+        Grid2 &g = *sl.grid;
+        MG2 &mg = *sl.mg;
+        cudaStream_t st = g.stream;
+        mg.setMaskLayer(layers[idx]);
+        g.buildLoadDev(sl.f.p);
+        guess(sl, layers[idx], ny, zeroInit);
+        mg.pcgStart(sl.x.p, sl.f.p, maxIter, tol, mgIter, sweeps, fmg, true);
+        // compliance f.u over the nondetached nodes
+        launch2_dot_partials(mg.lv[0].g, sl.f.p, sl.x.p, sl.part.p, st);
+        launch_finalize(sl.part.p, REDUCE_BLOCKS, sl.cpl.p, st);
+        VFEM_CUDA(cudaMemcpyAsync(cplHost + s, sl.cpl.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        launch2_adjoint(g.g, g.rho.p, sl.x.p, sl.x.p, sl.gtmp.p, g.K0, g.E0, g.Emin, g.gamma, g.q, g.law, g.grav, g.vol(),
+                        1.0, 0.5, st);
+        launch_axpy(NE, 1.0, sl.gtmp.p, sl.gacc.p, st);
+        if (layers[idx] == ny)
+            VFEM_CUDA(cudaMemcpyAsync(uFull.p, sl.x.p, 2 * NN * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        if (warm && sl.qpos < sl.queue.size()) pushHistory(sl);
+        VFEM_CUDA(cudaEventRecord(sl.done, st));
+        sl.idx = idx;
+    };
+    auto nextOf = [&](int64_t s, int64_t &next) -> int64_t {
+        Slot &sl = *S[s];
+        if (warm) return sl.qpos < sl.queue.size() ? sl.queue[sl.qpos++] : -1;
+        return next < count ? next++ : -1;
+    };
+    int64_t next = 0, remaining = count;
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t idx = nextOf(s, next);
+        if (idx >= 0) start(s, idx);
+    }
+    while (remaining > 0) {
+        bool progressed = false;
+        for (int64_t s = 0; s < ns; ++s) {
+            Slot &sl = *S[s];
+            if (sl.idx < 0) continue;
+            const cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaErrorNotReady) continue;
+            VFEM_CUDA(q);
+            const PcgStats st = sl.mg->pcgFinish();
+            compliance[sl.idx] = cplHost[s];
+            if (iterations) iterations[sl.idx] = st.iterations;
+            sl.idx = -1;
+            --remaining;
+            progressed = true;
+            const int64_t idx = nextOf(s, next);
+            if (idx >= 0) start(s, idx);
+        }
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    haveFull = haveFull || std::find(layers, layers + count, (int64_t)ny) != layers + count;
+    if (gradSum) {
+        Slot &s0 = *S[0];
+        cudaStream_t st = s0.grid->stream;
+        for (int64_t s = 1; s < ns; ++s) {
+            VFEM_CUDA(cudaStreamSynchronize(S[s]->grid->stream));
+            launch_axpy(NE, 1.0, S[s]->gacc.p, s0.gacc.p, st);
+        }
+        VFEM_CUDA(cudaMemcpyAsync(gradSum, s0.gacc.p, NE * sizeof(double), cudaMemcpyDefault, st));
+    }
+    for (auto &sl : S) VFEM_CUDA(cudaStreamSynchronize(sl->grid->stream));
 }
 
 // ---------------------------------------------------------------------------

@@ -100,6 +100,9 @@ void launch2_element_energy(const Geom2 &g, const double *Y, const double *u, do
 void launch2_gravity_load(const Geom2 &g, const double *rho, double *f, const double grav[2], double vol,
                           cudaStream_t st);
 
+void launch2_subspace_combine(const Geom2 &g, const LblVectors &U, int s, const double *cDev, const LblCoeffs &cv,
+                              double *x, cudaStream_t st);
+
 // ---------------- host engine (vfem_2d.cpp) ----------------
 class Grid2 {
 public:
@@ -141,6 +144,8 @@ public:
     void buildLoadDev(double *f);
     void adjoint(const double *lam, const double *u, double wF, double wK, double *out);
     void elementEnergy(const double *u, double *out);
+    // same dimensions, material, loads and supports (densities are copied by the caller)
+    std::unique_ptr<Grid2> clone() const;
 };
 
 class MG2 {
@@ -182,6 +187,11 @@ public:
     // x, b device arrays
     PcgStats pcgDev(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
                     bool dirichletSatisfied, PcgCallback cb, void *user);
+    // Asynchronous device-resident solve: pcgStart enqueues it on the simulator's stream (no host
+    // synchronisation once the stiffness is built), pcgFinish waits and returns the statistics.
+    void pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
+                  bool dirichletSatisfied);
+    PcgStats pcgFinish();
     double timeKernel(int which, int reps);
     void syncFine();
 
@@ -206,6 +216,7 @@ private:
     DevBuf<int> freeIdx, redIdx, status, nfreeDev;
     int nfree = 0, nfreeCap = 0;
     double *hostSc = nullptr;
+    bool pending = false;
     struct Key {
         int64_t mgIter, sweeps;
         int fmg, sym;
@@ -220,6 +231,46 @@ private:
     };
     std::map<Key, cudaGraphExec_t> graphs;
     std::map<Key, uint64_t> graphKernels;
+    Key pendingKey{};
+};
+
+// Layer-by-layer evaluation over 2D simulators (LayerByLayerEvaluator::run, LayerByLayer.hh:223-296),
+// organised like the 3D evaluator: `slots` persistent solver copies on their own streams, zero
+// initial guesses spread over them, warm starts (constant / fd / subspace) as chains of heights.
+class LBL2 {
+public:
+    LBL2(Grid2 *src, int coarsenings, int64_t slots);
+    ~LBL2();
+    LBL2(const LBL2 &) = delete;
+    LBL2 &operator=(const LBL2 &) = delete;
+    void setInit(int kind, int history);
+    void run(const int64_t *layers, int64_t count, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps,
+             bool fmg, bool zeroInit, double *compliance, int64_t *iterations, double *gradSum);
+
+private:
+    struct Slot {
+        std::unique_ptr<Grid2> grid;
+        std::unique_ptr<MG2> mg;
+        DevBuf<double> x, f, gtmp, gacc, cpl, part, subPart, subC;
+        DevBuf<double> hist[LBL_MAX_HISTORY], Ku[LBL_MAX_HISTORY];
+        int order[LBL_MAX_HISTORY] = {0};
+        int hs = 0;
+        std::vector<int64_t> queue;
+        size_t qpos = 0;
+        int64_t idx = -1;
+        cudaEvent_t done = nullptr;
+        ~Slot();
+    };
+    Grid2 *src;
+    int coarsenings;
+    int initKind = LBL_INIT_SUBSPACE, historySize = 3;
+    std::vector<std::unique_ptr<Slot>> S;
+    double *cplHost = nullptr;
+    DevBuf<double> uFull;
+    bool haveFull = false;
+    void syncSource();
+    void guess(Slot &sl, int64_t layer, int ny, bool zeroInit);
+    void pushHistory(Slot &sl);
 };
 
 // Problem backend of the 2D simulator (compliance objective, filters and OC over a Grid2 + MG2).

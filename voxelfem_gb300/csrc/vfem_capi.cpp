@@ -32,6 +32,10 @@ struct vfem_mg2 {
     MG2 m;
     vfem_mg2(Grid2 *g, int l) : m(g, l) {}
 };
+struct vfem_lbl2 {
+    LBL2 e;
+    vfem_lbl2(Grid2 *g, int c, int64_t s) : e(g, c, s) {}
+};
 
 namespace {
 thread_local std::string g_last_error;
@@ -370,6 +374,27 @@ int vfem_kernel_launch_count(uint64_t *count) {
     return guarded([&] { *count = launchCounter(); });
 }
 
+int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, vfem_lbl2 **out) {
+    return guarded([&] {
+        need(g, "grid"); need(out, "out");
+        *out = new vfem_lbl2(&g->g, (int)coarsenings, slots);
+    });
+}
+int vfem_lbl2_destroy(vfem_lbl2 *e) {
+    return guarded([&] { delete e; });
+}
+int vfem_lbl2_set_init(vfem_lbl2 *e, int kind, int history) {
+    return guarded([&] { need(e, "evaluator"); e->e.setInit(kind, history); });
+}
+int vfem_lbl2_run(vfem_lbl2 *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
+                  int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, int zero_init,
+                  double *compliance_out, int64_t *iterations_out, double *gradient_sum_out) {
+    return guarded([&] {
+        need(e, "evaluator"); need(layers, "layers"); need(compliance_out, "compliance_out");
+        e->e.run(layers, count, max_iter, tol, mg_iterations, mg_smoothing_iterations, full_multigrid != 0,
+                 zero_init != 0, compliance_out, iterations_out, gradient_sum_out);
+    });
+}
 int vfem_smoothing_filter2(const int64_t dims[2], int radius, int type, const double *in, double *out) {
     return guarded([&] {
         need(dims, "dims");
@@ -991,6 +1016,7 @@ int vfem_vertex_to_cell_filter_backprop(const int64_t vertex_dims[3], const doub
 
 struct vfem_langelaar {
     int d[3];
+    int ndim = 3;
     int64_t n;
     vfem::DevBuf<double> out, smax, filt, lam, vars, g;
 };
@@ -999,6 +1025,76 @@ int vfem_langelaar_create(const int64_t dims[3], vfem_langelaar **h) {
         need(h, "handle");
         auto f = std::make_unique<vfem_langelaar>();
         dims3(dims, f->d, 1, "invalid grid dimensions");
+        f->n = prod3(f->d);
+        for (auto *b : {&f->out, &f->smax, &f->filt, &f->lam, &f->vars, &f->g}) b->alloc(f->n);
+        VFEM_CUDA(cudaMemset(f->out.p, 0, f->n * sizeof(double)));
+        VFEM_CUDA(cudaMemset(f->smax.p, 0, f->n * sizeof(double)));
+        VFEM_CUDA(cudaMemset(f->filt.p, 0, f->n * sizeof(double)));
+        *h = f.release();
+    });
+}
+// ---- 2D variants (the N = 2 instantiations of the same filters) ----
+namespace {
+void dims2(const int64_t *d, int out[3], int64_t minimum, const char *msg) {
+    if (!d) throw vfem::Error(vfem::ERR_ARG, "null dims");
+    for (int a = 0; a < 2; ++a) {
+        if (d[a] < minimum || d[a] > (int64_t)1 << 30) throw vfem::Error(vfem::ERR_ARG, msg);
+        out[a] = (int)d[a];
+    }
+    out[2] = 1;
+}
+}  // namespace
+int vfem_upsample_filter2(const int64_t in_dims[2], int64_t factor, const double *in, double *out) {
+    return guarded([&] {
+        need(in, "in");
+        need(out, "out");
+        int d[3];
+        dims2(in_dims, d, 2, "Interpolation can only be applied to a 2^d grid or larger");
+        if (factor < 1) throw vfem::Error(vfem::ERR_ARG, "factor must be positive");
+        const int F = (int)factor;
+        const int o[3] = {(d[0] - 1) * F + 1, (d[1] - 1) * F + 1, 1};
+        filter_call(in, prod3(d), out, prod3(o), [&](const double *a, double *b) { vfem::launch_upsample(d, F, a, b, 0, 2); });
+    });
+}
+int vfem_upsample_filter2_backprop(const int64_t in_dims[2], int64_t factor, const double *g, double *out) {
+    return guarded([&] {
+        need(g, "g");
+        need(out, "out");
+        int d[3];
+        dims2(in_dims, d, 2, "Interpolation can only be applied to a 2^d grid or larger");
+        if (factor < 1) throw vfem::Error(vfem::ERR_ARG, "factor must be positive");
+        const int F = (int)factor;
+        const int o[3] = {(d[0] - 1) * F + 1, (d[1] - 1) * F + 1, 1};
+        filter_call(g, prod3(o), out, prod3(d), [&](const double *a, double *b) { vfem::launch_upsample_backprop(d, F, a, b, 0); });
+    });
+}
+int vfem_vertex_to_cell_filter2(const int64_t vertex_dims[2], const double *in, double *out) {
+    return guarded([&] {
+        need(in, "in");
+        need(out, "out");
+        int d[3];
+        dims2(vertex_dims, d, 2, "Input grid must be 2^d or larger.");
+        const int e[3] = {d[0] - 1, d[1] - 1, 1};
+        filter_call(in, prod3(d), out, prod3(e), [&](const double *a, double *b) { vfem::launch_vertex_to_cell(d, a, b, 0, 2); });
+    });
+}
+int vfem_vertex_to_cell_filter2_backprop(const int64_t vertex_dims[2], const double *g, double *out) {
+    return guarded([&] {
+        need(g, "g");
+        need(out, "out");
+        int d[3];
+        dims2(vertex_dims, d, 2, "Input grid must be 2^d or larger.");
+        const int e[3] = {d[0] - 1, d[1] - 1, 1};
+        filter_call(g, prod3(e), out, prod3(d),
+                    [&](const double *a, double *b) { vfem::launch_vertex_to_cell_backprop(d, a, b, 0, 2); });
+    });
+}
+int vfem_langelaar2_create(const int64_t dims[2], vfem_langelaar **h) {
+    return guarded([&] {
+        need(h, "handle");
+        auto f = std::make_unique<vfem_langelaar>();
+        dims2(dims, f->d, 1, "invalid grid dimensions");
+        f->ndim = 2;
         f->n = prod3(f->d);
         for (auto *b : {&f->out, &f->smax, &f->filt, &f->lam, &f->vars, &f->g}) b->alloc(f->n);
         VFEM_CUDA(cudaMemset(f->out.p, 0, f->n * sizeof(double)));
@@ -1016,7 +1112,7 @@ int vfem_langelaar_apply(vfem_langelaar *h, const double *in, double *out) {
         need(in, "in");
         need(out, "out");
         VFEM_CUDA(cudaMemcpy(h->vars.p, in, h->n * sizeof(double), cudaMemcpyDefault));
-        vfem::launch_langelaar(h->d, h->vars.p, h->out.p, h->smax.p, 0);
+        vfem::launch_langelaar(h->d, h->vars.p, h->out.p, h->smax.p, 0, h->ndim);
         VFEM_CUDA(cudaMemcpy(h->filt.p, h->out.p, h->n * sizeof(double), cudaMemcpyDeviceToDevice));
         VFEM_CUDA(cudaMemcpy(out, h->out.p, h->n * sizeof(double), cudaMemcpyDefault));
     });
@@ -1030,7 +1126,7 @@ int vfem_langelaar_backprop(vfem_langelaar *h, const double *g, const double *va
         VFEM_CUDA(cudaMemcpy(h->g.p, g, h->n * sizeof(double), cudaMemcpyDefault));
         VFEM_CUDA(cudaMemcpy(h->vars.p, vars, h->n * sizeof(double), cudaMemcpyDefault));
         vfem::DevBuf<double> res(h->n);
-        vfem::launch_langelaar_backprop(h->d, h->g.p, h->vars.p, h->filt.p, h->smax.p, h->lam.p, res.p, 0);
+        vfem::launch_langelaar_backprop(h->d, h->g.p, h->vars.p, h->filt.p, h->smax.p, h->lam.p, res.p, 0, h->ndim);
         VFEM_CUDA(cudaMemcpy(out, res.p, h->n * sizeof(double), cudaMemcpyDefault));
     });
 }

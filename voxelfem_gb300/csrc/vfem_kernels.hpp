@@ -223,15 +223,16 @@ void launch_subspace_combine(const Geom &g, const LblVectors &U, int s, const do
                              double *x, cudaStream_t st);
 
 // ---------------- further density filters (k_filters.cu) ----------------
-// dims: the input grid (Upsample: coarse nodes; VertexToCell: vertices; Langelaar: cells)
-void launch_upsample(const int dims[3], int factor, const double *in, double *out, cudaStream_t st);
+// dims: the input grid (Upsample: coarse nodes; VertexToCell: vertices; Langelaar: cells). ndim 2:
+// a 2D grid given as (dims[0], dims[1], 1) (the reference's N = 2 instantiations).
+void launch_upsample(const int dims[3], int factor, const double *in, double *out, cudaStream_t st, int ndim = 3);
 void launch_upsample_backprop(const int dims[3], int factor, const double *g, double *out, cudaStream_t st);
-void launch_vertex_to_cell(const int vdims[3], const double *in, double *out, cudaStream_t st);
-void launch_vertex_to_cell_backprop(const int vdims[3], const double *g, double *out, cudaStream_t st);
+void launch_vertex_to_cell(const int vdims[3], const double *in, double *out, cudaStream_t st, int ndim = 3);
+void launch_vertex_to_cell_backprop(const int vdims[3], const double *g, double *out, cudaStream_t st, int ndim = 3);
 // out: the previous output on entry (the own-voxel term of the supporting region); smax: cached
-void launch_langelaar(const int dims[3], const double *in, double *out, double *smax, cudaStream_t st);
+void launch_langelaar(const int dims[3], const double *in, double *out, double *smax, cudaStream_t st, int ndim = 3);
 void launch_langelaar_backprop(const int dims[3], const double *g, const double *vars, const double *filt,
-                               const double *smax, double *lam, double *out, cudaStream_t st);
+                               const double *smax, double *lam, double *out, cudaStream_t st, int ndim = 3);
 
 // ---------------- Method of Moving Asymptotes (k_mma.cu) ----------------
 // Row-major (m+1) x n arrays for df, p, q and m x n for G; partials are K rows of

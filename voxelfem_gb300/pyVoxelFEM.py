@@ -914,7 +914,8 @@ class UpsampleFilter(_ReshapingFilter):
         a = _as_elems(x, int(np.prod(self._in)))
         out = np.empty(int(np.prod(self._out)))
         dims = np.array(self._in, dtype=np.int64)
-        check(_lib().vfem_upsample_filter(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
+        fn = _lib().vfem_upsample_filter2 if len(self._in) == 2 else _lib().vfem_upsample_filter
+        check(fn(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
         return out
 
     def backprop(self, g, vars_=None):
@@ -922,7 +923,8 @@ class UpsampleFilter(_ReshapingFilter):
         a = _as_elems(g, int(np.prod(self._out)))
         out = np.empty(int(np.prod(self._in)))
         dims = np.array(self._in, dtype=np.int64)
-        check(_lib().vfem_upsample_filter_backprop(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
+        fn = _lib().vfem_upsample_filter2_backprop if len(self._in) == 2 else _lib().vfem_upsample_filter_backprop
+        check(fn(dims.ctypes.data_as(_capi._i64), self.factor, ptr(a), ptr(out)))
         return out
 
 
@@ -948,7 +950,8 @@ class VertexToCellFilter(_ReshapingFilter):
         a = _as_elems(x, int(np.prod(self._in)))
         out = np.empty(int(np.prod(self._out)))
         dims = np.array(self._in, dtype=np.int64)
-        check(_lib().vfem_vertex_to_cell_filter(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
+        fn = _lib().vfem_vertex_to_cell_filter2 if len(self._in) == 2 else _lib().vfem_vertex_to_cell_filter
+        check(fn(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
         return out
 
     def backprop(self, g, vars_=None):
@@ -956,7 +959,9 @@ class VertexToCellFilter(_ReshapingFilter):
         a = _as_elems(g, int(np.prod(self._out)))
         out = np.empty(int(np.prod(self._in)))
         dims = np.array(self._in, dtype=np.int64)
-        check(_lib().vfem_vertex_to_cell_filter_backprop(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
+        fn = (_lib().vfem_vertex_to_cell_filter2_backprop if len(self._in) == 2
+              else _lib().vfem_vertex_to_cell_filter_backprop)
+        check(fn(dims.ctypes.data_as(_capi._i64), ptr(a), ptr(out)))
         return out
 
 
@@ -975,7 +980,8 @@ class LangelaarFilter(_ReshapingFilter):
         self._release()
         h = C.c_void_p()
         dims = np.array(self._in, dtype=np.int64)
-        check(_lib().vfem_langelaar_create(dims.ctypes.data_as(_capi._i64), C.byref(h)))
+        fn = _lib().vfem_langelaar2_create if len(self._in) == 2 else _lib().vfem_langelaar_create
+        check(fn(dims.ctypes.data_as(_capi._i64), C.byref(h)))
         self._h = h
 
     setOutputDimensions = setInputDimensions
@@ -1396,7 +1402,10 @@ class LayerByLayerEvaluator:
     def _release(self):
         if getattr(self, "_h", None) is not None:
             try:
-                _lib().vfem_lbl_destroy(self._h)
+                if self.sim._nc == 2:
+                    _lib().vfem_lbl2_destroy(self._h)
+                else:
+                    _lib().vfem_lbl_destroy(self._h)
             except Exception:
                 pass
             self._h = None
@@ -1406,7 +1415,10 @@ class LayerByLayerEvaluator:
         if self._h is None or self._key != key:
             self._release()
             h = C.c_void_p()
-            check(_lib().vfem_lbl_create(self.sim._h, coarsenings, slots, precision, C.byref(h)))
+            if self.sim._nc == 2:
+                check(_lib().vfem_lbl2_create(self.sim._h, coarsenings, slots, C.byref(h)))
+            else:
+                check(_lib().vfem_lbl_create(self.sim._h, coarsenings, slots, precision, C.byref(h)))
             self._h, self._key = h, key
         return self._h
 
@@ -1451,10 +1463,11 @@ class LayerByLayerEvaluator:
         if slots is None:
             slots = 8 if kind == 0 else 1
         h = self._handle(int(solver.numLevels - 1), int(slots), precision)
-        check(_lib().vfem_lbl_set_init(h, kind, hist))
-        check(_lib().vfem_lbl_run(h, ptr(self.layers), n, int(maxIter), float(tol), int(mgIterations),
-                                  int(mgSmoothingIterations), int(bool(fmg)), int(bool(zeroInit)),
-                                  ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
+        two = self.sim._nc == 2
+        check((_lib().vfem_lbl2_set_init if two else _lib().vfem_lbl_set_init)(h, kind, hist))
+        run = _lib().vfem_lbl2_run if two else _lib().vfem_lbl_run
+        check(run(h, ptr(self.layers), n, int(maxIter), float(tol), int(mgIterations), int(mgSmoothingIterations),
+                  int(bool(fmg)), int(bool(zeroInit)), ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
         for t, lay in enumerate(layers):
             if verbose:
                 print("Layer %d: %g" % (lay, self.compliances[t]))
