@@ -447,6 +447,8 @@ def run_ours(args):
         line["q2"] = run_q2(hbm)
     if rank == 0 and ws == 1 and not args.no_mma:
         line["mma"] = run_mma(args.no_cpu)
+    if rank == 0 and ws == 1 and not args.no_2d:
+        line["2d"] = run_2d(hbm, args.no_cpu)
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
     if rank == 0:
@@ -648,6 +650,127 @@ def run_q2_solve(g, ne):
             "note": "host buffers in and out; includes the h2d of f and x0 and the d2h of u"}
 
 
+D2_DEMO = (384, 192)      # the reference's 2D topology-optimisation demo resolution
+D2_DEMO_LEVELS = 4        # its optMGLevel([384, 192], 2)
+D2_LARGE = (4096, 2048)   # 8.4M nodes: operator traffic well above L2
+D2_LARGE_LEVELS = 7       # optMGLevel([4096, 2048], 2): coarsest 32 x 16
+
+
+def setup_2d(ne, rho=None):
+    """2D cantilever on [0, 2] x [0, 1] (B9Creator material: E 1, nu 0.3): x = 0 edge fixed, unit
+    -y load at the (x = 2, y = 0) corner (the reference's cantilever_flexion_SE regions)."""
+    from voxelfem_gb300 import pyVoxelFEM as pv
+
+    tps = pv.TensorProductSimulator([1, 1], [[0.0, 0.0], [2.0, 1.0]], list(ne))
+    tps.ETensor = (1.0, 0.3)
+    tps.addDirichletCondition([0.0, 0.0], [-2e-4, -1e-4], [2e-4, 1.0001], "xy")
+    f = np.zeros((tps.numNodes(), 2), order="F")
+    f[ne[0] * (ne[1] + 1), 1] = -1.0
+    tps.setNodalForces(f)
+    if rho is not None:
+        tps.setDensities(rho)
+    return tps, f
+
+
+def run_2d(hbm, no_cpu):
+    """The bilinear-quadrilateral path. Demo case (384 x 192, 4 coarsenings, the demo's filters
+    SmoothingFilter(3, Linear) + ProjectionFilter(1), volume 0.33): wall time of setVars (filters +
+    MG-PCG to 1e-5 with the objective's defaults: FMG, 2 sweeps) and of one OC step, host arrays
+    in and out; a FP64 PCG solve to 1e-8 with the numpy oracle timed beside it on the same problem.
+    Large case (4096 x 2048, 7 coarsenings): device time per launch of the fine operator, the
+    4-colour Gauss-Seidel sweep, one V-cycle and one PCG iteration on resident data, and a solve
+    to 1e-8."""
+    import time
+
+    from voxelfem_gb300 import pyVoxelFEM as pv
+
+    out = {}
+    tps, f = setup_2d(D2_DEMO)
+    sf = pv.SmoothingFilter(3, pv.SmoothingFilter.Type.Linear)
+    pf = pv.ProjectionFilter(1.0)
+    obj = pv.MultigridComplianceObjective(tps.multigridSolver(D2_DEMO_LEVELS))
+    top = pv.TopologyOptimizationProblem(tps, obj, [pv.TotalVolumeConstraint(0.33)], [sf, pf])
+    x0 = np.full(top.numVars(), pf.invert(0.33))
+    top.setVars(x0)  # graph capture, stiffness
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        top.setVars(x0)
+        ts.append(time.perf_counter() - t0)
+    oc = pv.OCOptimizer(top)
+    oc.step()
+    to = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        oc.step()
+        to.append(time.perf_counter() - t0)
+    demo = {"workload": "2D cantilever 384x192, 4 coarsenings, filters Smoothing(3, Linear) + Projection(1), "
+                        "volume 0.33 (the reference's 2D topology-optimisation demo setup)",
+            "set_vars_s": float(np.median(ts)), "oc_step_s": float(np.median(to)),
+            "pcg_iterations": int(top.lastSolveStats().iterations), "compliance": top.evaluateObjective()}
+    # plain FP64 PCG to 1e-8 (1 V-cycle, 1 sweep) on uniform rho 0.5, and the oracle on the same problem
+    tps2, f2 = setup_2d(D2_DEMO, np.full(D2_DEMO[0] * D2_DEMO[1], 0.5))
+    mg = tps2.multigridSolver(D2_DEMO_LEVELS)
+    x = np.zeros_like(f2)
+    mg.preconditionedConjugateGradient(x, f2, 2, 1e-8, None, 1, 1, False)
+    t0 = time.perf_counter()
+    u = mg.preconditionedConjugateGradient(x, f2, 200, 1e-8, None, 1, 1, False)
+    demo["pcg_1e-8_s"] = time.perf_counter() - t0
+    demo["pcg_1e-8_iterations"] = int(mg.lastStats.iterations)
+    if not no_cpu:
+        sys.path.insert(0, ROOT)
+        from oracle import oracle2d as o2
+        sim = o2.Sim2(D2_DEMO, (0.0, 0.0), (2.0, 1.0))
+        sim.setMaterial(1.0, 0.3)
+        sim.setDensities(np.full(sim.NE, 0.5))
+        sim.addDirichletCondition([0.0, 0.0], [-2e-4, -1e-4], [2e-4, 1.0001])
+        sim.force = np.asarray(f2).T.ravel().copy()
+        omg = o2.MG2(sim, D2_DEMO_LEVELS)
+        t0 = time.perf_counter()
+        uo = omg.pcg(np.zeros(2 * sim.NN), sim.buildLoadVector(), 200, 1e-8, 1, 1, False)
+        cpu_s = time.perf_counter() - t0
+        demo["cpu_baseline"] = {"value": cpu_s, "unit": "s", "cores": 1, "kind": "port",
+                                "sample": "numpy restatement (oracle/oracle2d.py), same solve",
+                                "iterations": int(omg.lastIterations),
+                                "solution_rel_diff": float(np.max(np.abs(np.asarray(u).T.ravel() - uo)) /
+                                                           np.max(np.abs(uo)))}
+    out["demo"] = demo
+    # large case: kernels on resident data and a solve
+    ne = D2_LARGE
+    rho = np.random.default_rng(0).uniform(0.1, 1.0, ne[0] * ne[1])
+    tpsL, fL = setup_2d(ne, rho)
+    mgL = tpsL.multigridSolver(D2_LARGE_LEVELS)
+    nn, nel = tpsL.numNodes(), tpsL.numElements()
+    xL = np.zeros_like(fL)
+    mgL.preconditionedConjugateGradient(xL, fL, 2, 1e-8, None, 1, 1, False)
+    t0 = time.perf_counter()
+    uL = mgL.preconditionedConjugateGradient(xL, fL, 500, 1e-8, None, 1, 1, False)
+    large = {"workload": "2D cantilever 4096x2048 (%d nodes), rho U[0.1,1] seed 0, 7 coarsenings" % nn,
+             "pcg_1e-8_s": time.perf_counter() - t0, "pcg_1e-8_iterations": int(mgL.lastStats.iterations),
+             "relres": float(mgL.lastStats.relres)}
+    # algorithmic bytes: operator u (16 B/node) in, K u (16 B/node) out, moduli (8 B/element); a
+    # sweep's minimum adds b in and u out once (16 + 16 B/node) and the 1 B/node Dirichlet mask
+    alg = {"applyk_fine": 32.0 * nn + 8.0 * nel, "gs_sweep_fine": 49.0 * nn + 8.0 * nel}
+    # FP64 work per node: 4 incident elements x 2 rows x (8 FMA + scale + add) = 144 flop; the
+    # sweep adds the 2 x 2 diagonal block (8 flop) and the block solve (about 10 flop)
+    flops = {"applyk_fine": 144.0 * nn, "gs_sweep_fine": 162.0 * nn}
+    fp64_peak = fp64_peak_tflops()
+    for name, which, reps in (("applyk_fine", 0, 20), ("gs_sweep_fine", 1, 10), ("vcycle", 2, 5), ("pcg_iteration", 3, 5)):
+        ms = mgL.timeKernel(which, reps)
+        ent = {"ms": ms}
+        if name in alg:
+            gbs = alg[name] / (ms * 1e-3) / 1e9
+            tf = flops[name] / (ms * 1e-3) / 1e12
+            ent.update({"bytes": alg[name], "gbs": gbs, "hbm_frac": gbs / hbm,
+                        "fp64_compute": {"flops": flops[name], "achieved": tf, "unit": "TFLOP/s",
+                                         "peak": fp64_peak, "frac": tf / fp64_peak,
+                                         "peak_kind": "measured (cuBLAS DGEMM 4096^3 in this run)"},
+                        "bound": "fp64"})
+        large[name] = ent
+    out["large"] = large
+    return out
+
+
 def run_kernel_case(args):
     """One hot kernel of the workload, launched a handful of times (profiler captures)."""
     import ctypes as C
@@ -671,6 +794,19 @@ def run_kernel_case(args):
     print(json.dumps({"kernel": KERNEL_NAMES[args.kernel_case], "ms": ms.value, "bytes": nbytes.value}))
 
 
+def run_kernel_2d(args):
+    """The 2D large case's hot kernel `args.kernel_2d` (0 applyK, 1 GS sweep), launched a few times
+    (profiler captures)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    ne = D2_LARGE
+    tps, _ = setup_2d(ne, np.random.default_rng(0).uniform(0.1, 1.0, ne[0] * ne[1]))
+    mg = tps.multigridSolver(D2_LARGE_LEVELS)
+    ms = mg.timeKernel(args.kernel_2d, 1)
+    print(json.dumps({"kernel_2d": args.kernel_2d, "ms": ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -682,8 +818,11 @@ def main():
     ap.add_argument("--no-lbl", action="store_true", help="skip the layer-by-layer batching measurement")
     ap.add_argument("--no-q2", action="store_true", help="skip the triquadratic applyK measurement")
     ap.add_argument("--no-mma", action="store_true", help="skip the MMA optimiser measurement")
+    ap.add_argument("--no-2d", action="store_true", help="skip the bilinear-quadrilateral (2D) measurement")
     ap.add_argument("--host-loop", action="store_true",
                     help="iterate PCG from the host (one graph per iteration) instead of the device-resident loop")
+    ap.add_argument("--kernel-2d", type=int, default=None,
+                    help="only set up the 2D large case and launch one of its kernels (0 applyK, 1 GS sweep)")
     ap.add_argument("--kernel-case", type=int, default=None,
                     help="only set up the workload and launch one hot kernel (id of vfem_mg_time_kernel) twice")
     args = ap.parse_args()
@@ -693,6 +832,8 @@ def main():
         run_reference(args)
     elif args.kernel_case is not None:
         run_kernel_case(args)
+    elif args.kernel_2d is not None:
+        run_kernel_2d(args)
     else:
         run_ours(args)
 

@@ -149,9 +149,9 @@ class Sim2:
 
     def scatter(self, fe):
         out = np.zeros(2 * self.NN)
-        for l in range(4):
-            for c in range(2):
-                np.add.at(out, c * self.NN + self.en[:, l], fe[:, 2 * l + c])
+        for c in range(2):
+            idx = self.en.ravel()
+            out[c * self.NN:(c + 1) * self.NN] = np.bincount(idx, weights=fe[:, c::2].ravel(), minlength=self.NN)
         return out
 
     def elementMatrices(self):
@@ -159,13 +159,21 @@ class Sim2:
 
     # TPSStencils.hh:189-390 (ZeroInit applyK; detached rows come out zero)
     def applyK(self, u):
-        return self.scatter(np.einsum("eij,ej->ei", self.elementMatrices(), self.elemDisp(u)))
+        ue = self.elemDisp(u)
+        if self.Ke is None:
+            return self.scatter((ue @ self.K0.T) * self.Y[:, None])
+        return self.scatter(np.matmul(self.Ke, ue[:, :, None])[:, :, 0])
 
     def diagBlocks(self):
-        Ke = self.elementMatrices()
         M = np.zeros((self.NN, 2, 2))
         for l in range(4):
-            np.add.at(M, self.en[:, l], Ke[:, 2 * l:2 * l + 2, 2 * l:2 * l + 2])
+            if self.Ke is None:
+                blk = self.Y[:, None, None] * self.K0[None, 2 * l:2 * l + 2, 2 * l:2 * l + 2]
+            else:
+                blk = self.Ke[:, 2 * l:2 * l + 2, 2 * l:2 * l + 2]
+            for r in range(2):
+                for c in range(2):
+                    M[:, r, c] += np.bincount(self.en[:, l], weights=blk[:, r, c], minlength=self.NN)
         return M
 
     # TensorProductSimulator.hh:1269-1288 (integrated Q1 shape function = 1/4)
@@ -291,7 +299,7 @@ class MG2:
                 for b in range(2):
                     child = (2 * s.eI + a) * f.ne[1] + 2 * s.eJ + b
                     I = self.I2[ci]
-                    Ke += np.einsum("ji,ejk,kl->eil", I, Kf[child], I)
+                    Ke += np.matmul(np.matmul(I.T[None], Kf[child]), I[None])
                     ci += 1
             Ke[s.eJ >= s.firstMaskedE] = 0.0
             s.Ke = Ke
@@ -329,52 +337,70 @@ class MG2:
         self.zeroDirichlet(s, res)
         return res
 
-    # smoothingMulticoloredGS + m_smoothNode (MultigridSolver.hh:348-458)
+    # smoothingMulticoloredGS + m_smoothNode (MultigridSolver.hh:348-458). Nodes of one colour
+    # share no element, so each colour is one vectorised block update.
     def smooth(self, l, u, b, forward=True):
         if l > 0:
             self._ensure()
         s = self.sims[l]
-        M = s.diagBlocks()
+        key = (id(s.Ke), s.Y.ctypes.data, float(s.Y.sum()))
+        cached = getattr(self, "_diag", {}).get(l)
+        if cached is None or cached[0] != key:
+            self._diag = getattr(self, "_diag", {})
+            self._diag[l] = (key, s.diagBlocks())
+        M = self._diag[l][1]
         nyv = s.nondetNodes()
+        NN = s.NN
         for ci in range(4):
             col = ci if forward else 3 - ci
             sel = np.nonzero((s.nI % 2 == (col >> 1)) & (s.nJ % 2 == (col & 1)) & (s.nJ < nyv) & (s.dmask != 3))[0]
+            if sel.size == 0:
+                continue
             Ku = s.applyK(u)
-            for n in sel:
-                bms = np.array([b[n] - Ku[n], b[s.NN + n] - Ku[s.NN + n]])
-                Mn = M[n]
-                dm = s.dmask[n]
-                if dm:
-                    ud = np.zeros(2)
-                    order = (0, 1) if forward else (1, 0)
-                    for i in order:
-                        ud[i] = (bms[i] - (Mn[i, 0] * ud[0] + Mn[i, 1] * ud[1])) * (float(not (dm >> i) & 1) / Mn[i, i])
-                    du = ud
-                else:
-                    du = np.linalg.inv(Mn) @ bms
-                u[n] += du[0]
-                u[s.NN + n] += du[1]
+            bms = np.stack([b[sel] - Ku[sel], b[NN + sel] - Ku[NN + sel]], axis=1)
+            Mn = M[sel]
+            dm = s.dmask[sel]
+            du = np.zeros_like(bms)
+            full = dm == 0
+            det = Mn[:, 0, 0] * Mn[:, 1, 1] - Mn[:, 0, 1] * Mn[:, 1, 0]
+            du[full, 0] = ((Mn[:, 1, 1] * bms[:, 0] - Mn[:, 0, 1] * bms[:, 1]) / det)[full]
+            du[full, 1] = ((Mn[:, 0, 0] * bms[:, 1] - Mn[:, 1, 0] * bms[:, 0]) / det)[full]
+            part = ~full
+            if part.any():
+                ud = np.zeros((part.sum(), 2))
+                Mp, bp, dp = Mn[part], bms[part], dm[part]
+                for i in ((0, 1) if forward else (1, 0)):
+                    free = ((dp >> i) & 1) == 0
+                    ud[:, i] = (bp[:, i] - (Mp[:, i, 0] * ud[:, 0] + Mp[:, i, 1] * ud[:, 1])) * free / Mp[:, i, i]
+                du[part] = ud
+            u[sel] += du[:, 0]
+            u[NN + sel] += du[:, 1]
         return u
 
-    # MultigridSolver.hh:217-275
+    @staticmethod
+    def _prolong1d(nc):
+        """Bilinear prolongation along one axis, (2 (nc - 1) + 1) x nc (MultigridSolver.hh:163-212)."""
+        nf = 2 * (nc - 1) + 1
+        P = np.zeros((nf, nc))
+        for f in range(nf):
+            if f % 2 == 0:
+                P[f, f // 2] = 1.0
+            else:
+                P[f, f // 2] = P[f, f // 2 + 1] = 0.5
+        return P
+
+    # MultigridSolver.hh:217-275 (full weighting = P^T over the nondetached fine rows)
     def restrict(self, l, vals):
         fs, cs = self.sims[l], self.sims[l + 1]
         cyv, fyv = cs.nondetNodes(), fs.nondetNodes()
+        Px, Py = self._prolong1d(cs.nn[0]), self._prolong1d(cs.nn[1])
         res = np.zeros(2 * cs.NN)
-        for i in range(cs.nn[0]):
-            for j in range(cyv):
-                v = np.zeros(2)
-                for a in range(max(2 * i - 1, 0), min(2 * i + 2, fs.nn[0])):
-                    for bb in range(max(2 * j - 1, 0), min(2 * j + 2, fyv)):
-                        w = (1 - abs(a - 2 * i) * 0.5) * (1 - abs(bb - 2 * j) * 0.5)
-                        fn = fs.node(a, bb)
-                        v += w * np.array([vals[fn], vals[fs.NN + fn]])
-                cn = cs.node(i, j)
-                res[cn], res[cs.NN + cn] = v
-        if cyv != cs.nn[1]:
-            for i in range(cs.nn[0]):
-                cn = cs.node(i, cyv)
-                res[cn] = res[cs.NN + cn] = 0.0
+        for c in range(2):
+            F = np.asarray(vals[c * fs.NN:(c + 1) * fs.NN]).reshape(fs.nn).copy()
+            F[:, fyv:] = 0.0
+            C = Px.T @ F @ Py
+            C[:, cyv:] = 0.0
+            res[c * cs.NN:(c + 1) * cs.NN] = C.ravel()
         return res
 
     # MultigridSolver.hh:163-212
@@ -382,23 +408,14 @@ class MG2:
         fs, cs = self.sims[l], self.sims[l + 1]
         out = np.zeros(2 * fs.NN) if out is None else out
         fyv = fs.nondetNodes() if accumulate else fs.nn[1]
-        for i in range(fs.nn[0]):
-            for j in range(fyv):
-                f = (i, j)
-                ec = [min(f[d] // 2, cs.ne[d]) for d in range(2)]
-                lf = [f[d] - 2 * ec[d] for d in range(2)]
-                fn = fs.node(i, j)
-                acc = np.array([out[fn], out[fs.NN + fn]]) if accumulate else np.zeros(2)
-                for cn in range(4):
-                    cb = (cn >> 1, cn & 1)
-                    coeff = 1.0
-                    for d in range(2):
-                        coeff *= 0.5 if lf[d] == 1 else ((0.0 if cb[d] else 1.0) if lf[d] == 0 else (1.0 if cb[d] else 0.0))
-                    if coeff == 0:
-                        continue
-                    cidx = cs.node(ec[0] + cb[0], ec[1] + cb[1])
-                    acc += coeff * np.array([cvals[cidx], cvals[cs.NN + cidx]])
-                out[fn], out[fs.NN + fn] = acc
+        Px, Py = self._prolong1d(cs.nn[0]), self._prolong1d(cs.nn[1])
+        for c in range(2):
+            Fv = Px @ np.asarray(cvals[c * cs.NN:(c + 1) * cs.NN]).reshape(cs.nn) @ Py.T
+            O = out[c * fs.NN:(c + 1) * fs.NN].reshape(fs.nn)
+            if accumulate:
+                O[:, :fyv] += Fv[:, :fyv]
+            else:
+                O[:, :fyv] = Fv[:, :fyv]
         return out
 
     @staticmethod

@@ -873,6 +873,9 @@ double MG2::timeKernel(int which, int reps) {
     ensureStiffness();
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
+    DevBuf<double> xt(2 * g.NN);
+    VFEM_CUDA(cudaMemsetAsync(xt.p, 0, 2 * g.NN * sizeof(double), st));
+    launch_cg_init(sc.p, 0.0, 1.0, st);
     auto body = [&]() {
         switch (which) {
         case 0:
@@ -881,7 +884,7 @@ double MG2::timeKernel(int which, int reps) {
             break;
         case 1: smoothLevel(0, lv[0].x.p, lv[0].b.p, true); break;
         case 2: runCycles(1, 1, true, false); break;
-        default: cgIteration(sbuf.p, 1, 1, false); break;
+        default: cgIteration(xt.p, 1, 1, false); break;
         }
     };
     cudaGraph_t gr;
