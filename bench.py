@@ -767,6 +767,24 @@ def run_2d(hbm, no_cpu):
                                          "peak_kind": "measured (cuBLAS DGEMM 4096^3 in this run)"},
                         "bound": "fp64"})
         large[name] = ent
+    # the same solve and the preconditioner's kernels with the V-cycle in FP32 (mixed)
+    mgL.setPrecision("mixed")
+    mgL.preconditionedConjugateGradient(xL, fL, 2, 1e-8, None, 1, 1, False)
+    t0 = time.perf_counter()
+    uM = mgL.preconditionedConjugateGradient(xL, fL, 500, 1e-8, None, 1, 1, False)
+    mixed = {"pcg_1e-8_s": time.perf_counter() - t0, "pcg_1e-8_iterations": int(mgL.lastStats.iterations),
+             "relres": float(mgL.lastStats.relres),
+             "compliance_rel_diff_vs_fp64": float(abs(np.sum(fL * uM) - np.sum(fL * uL)) / abs(np.sum(fL * uL)))}
+    for name, which, reps in (("gs_sweep_fine_fp32", 1, 20), ("vcycle_fp32", 2, 10), ("pcg_iteration", 3, 10),
+                              ("applyk_fine_df", 4, 20)):
+        mixed[name] = {"ms": mgL.timeKernel(which, reps)}
+    ms = mixed["applyk_fine_df"]["ms"]
+    mixed["applyk_fine_df"].update({"bytes": alg["applyk_fine"], "gbs": alg["applyk_fine"] / (ms * 1e-3) / 1e9,
+                                    "hbm_frac": alg["applyk_fine"] / (ms * 1e-3) / 1e9 / hbm,
+                                    "fp64_equivalent_tflops": flops["applyk_fine"] / (ms * 1e-3) / 1e12})
+    gbs = 0.5 * alg["gs_sweep_fine"] / (mixed["gs_sweep_fine_fp32"]["ms"] * 1e-3) / 1e9
+    mixed["gs_sweep_fine_fp32"].update({"bytes": 0.5 * alg["gs_sweep_fine"], "gbs": gbs, "hbm_frac": gbs / hbm})
+    large["mixed"] = mixed
     out["large"] = large
     return out
 

@@ -385,6 +385,12 @@ int vfem_mg2_destroy(vfem_mg2 *mg);
 int vfem_mg2_num_levels(const vfem_mg2 *mg, int *levels);
 int vfem_mg2_level_dims(const vfem_mg2 *mg, int level, int64_t elems[2]);
 int vfem_mg2_level_dirichlet_mask(const vfem_mg2 *mg, int level, uint8_t *mask_out);
+/* precision: VFEM_PREC_FP64 (the reference's method) or VFEM_PREC_MIXED (the PCG preconditioner's
+ * V-cycle in FP32 inside FP64 CG; no reference counterpart). The per-level entry points and
+ * vfem_mg2_solve stay FP64. */
+int vfem_mg2_set_precision(vfem_mg2 *mg, int precision);
+/* CG matvec of the mixed solve: VFEM_MATVEC_DF (default, double-float on the FP32 units) or VFEM_MATVEC_FP64 */
+int vfem_mg2_set_outer_matvec(vfem_mg2 *mg, int kind);
 int vfem_mg2_set_use_graphs(vfem_mg2 *mg, int use);
 int vfem_mg2_set_symmetric_gs(vfem_mg2 *mg, int symmetric);
 int vfem_mg2_set_mask_layer(vfem_mg2 *mg, int64_t layer);
@@ -402,13 +408,14 @@ int vfem_mg2_pcg(vfem_mg2 *mg, double *x_inout, const double *b, int64_t max_ite
                  int64_t mg_smoothing_iterations, int full_multigrid, int dirichlet_already_satisfied,
                  vfem_pcg_callback cb, void *user, vfem_pcg_stats *stats);
 /* Benchmark hook (no reference counterpart): average device time of one launch on resident data.
- * kernel 0: fine applyK, 1: fine 4-colour Gauss-Seidel sweep, 2: one V-cycle, 3: one PCG iteration. */
+ * kernel 0: fine applyK (FP64), 1: fine 4-colour Gauss-Seidel sweep, 2: one V-cycle (1 and 2 in the
+ * solver's precision), 3: one PCG iteration, 4: fine applyK in double-float. */
 int vfem_mg2_time_kernel(vfem_mg2 *mg, int kernel, int reps, double *ms);
 /* TopologyOptimizationProblem + MultigridComplianceObjective over the 2D solver; the handle takes
  * every vfem_problem_* call (filters as in vfem_problem_create, smoothing over the 2D neighbourhood). */
-/* Layer-by-layer evaluation over a 2D simulator: as vfem_lbl_create / _set_init / _run (FP64 solves). */
+/* Layer-by-layer evaluation over a 2D simulator: as vfem_lbl_create / _set_init / _run. */
 typedef struct vfem_lbl2 vfem_lbl2;
-int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, vfem_lbl2 **out);
+int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, int precision, vfem_lbl2 **out);
 int vfem_lbl2_destroy(vfem_lbl2 *e);
 int vfem_lbl2_set_init(vfem_lbl2 *e, int kind, int history);
 int vfem_lbl2_run(vfem_lbl2 *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,

@@ -277,3 +277,45 @@ def test_layer_by_layer_2d(gpu, method, slots, inc):
     n = len(layers)
     assert rel(lbl.gradient(), grad / n) < 1e-6
     assert abs(lbl.objective() - 0.5 * comps.sum() / n) < 1e-7 * abs(lbl.objective())
+
+
+@pytest.mark.parametrize("fmg,sweeps", [(False, 1), (True, 2)])
+def test_pcg_mixed_2d(gpu, fmg, sweeps):
+    tps, sim, rng = make_pair(ne=(64, 32), seed=13)
+    mg = tps.multigridSolver(3)
+    mg.setPrecision("mixed")
+    omg = o2.MG2(sim, 3)
+    f = tps.buildLoadVector()
+    x = mg.preconditionedConjugateGradient(np.zeros_like(f), f, 200, 1e-10, None, 1, sweeps, fmg)
+    xo = omg.pcg(np.zeros(2 * sim.NN), soa(f), 200, 1e-10, 1, sweeps, fmg)
+    r = soa(f) - sim.applyK(soa(x))
+    o2.MG2.zeroDirichlet(sim, r)
+    assert np.linalg.norm(r) < 1e-9 * np.linalg.norm(soa(f))
+    assert rel(soa(x), xo) < 1e-8
+    assert abs(mg.lastStats.iterations - omg.lastIterations) <= 2
+
+
+def test_lbl_and_problem_mixed_2d(gpu):
+    tps, sim = lbl_pair(seed=14)
+    mg = tps.multigridSolver(2)
+    mg.setPrecision("mixed")
+    lbl = pv.LayerByLayerEvaluator(tps)
+    lbl.selectInitMethod("N=3")
+    lbl.run(mg, True, 2, 200, 1e-9, None, 1, 1, False)
+    layers, comps, iters, grad, _ = o2.layer_by_layer(sim, o2.MG2(sim, 2), "N=3", True, 2, 200, 1e-9, 1, 1, False)
+    np.testing.assert_array_equal(lbl.layers, layers)
+    assert rel(lbl.compliances, comps) < 1e-7
+    assert rel(lbl.gradient(), grad / len(layers)) < 1e-6
+    # the problem's solve follows the solver's precision
+    tps2, sim2, _ = make_pair(ne=(32, 16), seed=15)
+    mg2 = tps2.multigridSolver(2)
+    mg2.setPrecision("mixed")
+    obj = pv.MultigridComplianceObjective(mg2)
+    obj.tol = 1e-10
+    top = pv.TopologyOptimizationProblem(tps2, obj, [pv.TotalVolumeConstraint(0.5)], [pv.ProjectionFilter(1.0)])
+    otop = o2.TOP2(o2.MG2(sim2, 2), [("proj", 1.0)], 0.5, tol=1e-10)
+    x0 = np.full(top.numVars(), 0.6)
+    top.setVars(x0)
+    otop.setVars(x0)
+    assert rel(top.evaluateObjective(), otop.evaluateObjective()) < 1e-8
+    assert rel(top.evaluateObjectiveGradient(), otop.evaluateObjectiveGradient()) < 1e-7

@@ -186,7 +186,9 @@ _SIGS = {
     "vfem_mg2_pcg": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
                               PCG_CALLBACK, C.c_void_p, C.POINTER(PcgStats)]),
     "vfem_mg2_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _d]),
-    "vfem_lbl2_create": (C.c_int, [_vp, C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]),
+    "vfem_lbl2_create": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "vfem_mg2_set_precision": (C.c_int, [_vp, C.c_int]),
+    "vfem_mg2_set_outer_matvec": (C.c_int, [_vp, C.c_int]),
     "vfem_lbl2_destroy": (C.c_int, [_vp]),
     "vfem_lbl2_set_init": (C.c_int, [_vp, C.c_int, C.c_int]),
     "vfem_lbl2_run": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,

@@ -5,6 +5,7 @@
 #include <algorithm>
 
 #include "vfem_2d.hpp"
+#include "vfem_df.cuh"
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 
@@ -14,11 +15,13 @@ namespace {
 constexpr int BS = 256;
 
 // 3 x 3 patch of node displacements around (i, j); out-of-grid nodes read as zero.
+template <typename T>
 struct Patch {
-    double u[3][3][2];
+    T u[3][3][2];
 };
 
-__device__ __forceinline__ void load_patch(const Geom2 &g, const double *__restrict__ u, int i, int j, Patch &p) {
+template <typename T>
+__device__ __forceinline__ void load_patch(const Geom2 &g, const T *__restrict__ u, int i, int j, Patch<T> &p) {
 #pragma unroll
     for (int di = 0; di < 3; ++di)
 #pragma unroll
@@ -26,30 +29,30 @@ __device__ __forceinline__ void load_patch(const Geom2 &g, const double *__restr
             const int ii = i - 1 + di, jj = j - 1 + dj;
             const bool in = ii >= 0 && jj >= 0 && ii < g.nn[0] && jj < g.nn[1];
             const int64_t m = in ? g.node(ii, jj) : 0;
-            p.u[di][dj][0] = in ? u[m] : 0.0;
-            p.u[di][dj][1] = in ? u[g.NN + m] : 0.0;
+            p.u[di][dj][0] = in ? u[m] : T(0);
+            p.u[di][dj][1] = in ? u[g.NN + m] : T(0);
         }
 }
 
 // (K u)_n and the diagonal block of K at node (i, j) from the four incident elements
 // (TPSStencils.hh:189-390; m_smoothNode's Finest stencil, MultigridSolver.hh:277-292).
-template <bool DIAG>
-__device__ __forceinline__ void fine_row(const Geom2 &g, const double *__restrict__ Y, const Mat8 &K0, const Patch &p,
-                                         int i, int j, double f[2], double M[4]) {
-    f[0] = f[1] = 0.0;
-    if (DIAG) M[0] = M[1] = M[2] = M[3] = 0.0;
+template <bool DIAG, typename T>
+__device__ __forceinline__ void fine_row(const Geom2 &g, const T *__restrict__ Y, const Mat8T<T> &K0,
+                                         const Patch<T> &p, int i, int j, T f[2], T M[4]) {
+    f[0] = f[1] = T(0);
+    if (DIAG) M[0] = M[1] = M[2] = M[3] = T(0);
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
             const int ei = i - a, ej = j - b;
             if (ei < 0 || ej < 0 || ei >= g.ne[0] || ej >= g.ne[1]) continue;
-            const double E = Y[g.elem(ei, ej)];
+            const T E = Y[g.elem(ei, ej)];
             const int ln = 2 * a + b;
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 const int row = 2 * ln + c;
-                double acc = 0.0;
+                T acc = T(0);
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     const int pi = 1 - a + (m >> 1), pj = 1 - b + (m & 1);
@@ -65,71 +68,131 @@ __device__ __forceinline__ void fine_row(const Geom2 &g, const double *__restric
 }
 
 // m_smoothNode (MultigridSolver.hh:348-378): block solve, pointwise on partially fixed nodes.
-__device__ __forceinline__ void node_solve(uint8_t dm, const double bms[2], const double M[4], bool forward,
-                                           double du[2]) {
+template <typename T>
+__device__ __forceinline__ void node_solve(uint8_t dm, const T bms[2], const T M[4], bool forward, T du[2]) {
     if (dm) {
-        double ud[2] = {0.0, 0.0};
+        T ud[2] = {T(0), T(0)};
         if (forward) {
-            ud[0] = (bms[0] - (M[0] * ud[0] + M[1] * ud[1])) * ((double)!(dm & 1) / M[0]);
-            ud[1] = (bms[1] - (M[2] * ud[0] + M[3] * ud[1])) * ((double)!(dm >> 1 & 1) / M[3]);
+            ud[0] = (bms[0] - (M[0] * ud[0] + M[1] * ud[1])) * ((T)!(dm & 1) / M[0]);
+            ud[1] = (bms[1] - (M[2] * ud[0] + M[3] * ud[1])) * ((T)!(dm >> 1 & 1) / M[3]);
         } else {
-            ud[1] = (bms[1] - (M[2] * ud[0] + M[3] * ud[1])) * ((double)!(dm >> 1 & 1) / M[3]);
-            ud[0] = (bms[0] - (M[0] * ud[0] + M[1] * ud[1])) * ((double)!(dm & 1) / M[0]);
+            ud[1] = (bms[1] - (M[2] * ud[0] + M[3] * ud[1])) * ((T)!(dm >> 1 & 1) / M[3]);
+            ud[0] = (bms[0] - (M[0] * ud[0] + M[1] * ud[1])) * ((T)!(dm & 1) / M[0]);
         }
         du[0] = ud[0];
         du[1] = ud[1];
     } else {
-        const double det = M[0] * M[3] - M[1] * M[2];
-        const double id = 1.0 / det;
+        const T det = M[0] * M[3] - M[1] * M[2];
+        const T id = T(1) / det;
         du[0] = (M[3] * bms[0] - M[1] * bms[1]) * id;
         du[1] = (M[0] * bms[1] - M[2] * bms[0]) * id;
     }
 }
 
 // Shared epilogue of the operator kernels (mode 0 apply, mode 1 residual).
-__device__ __forceinline__ double finish_row(const Geom2 &g, int64_t n, int j, int nyv, int mode, const double f[2],
-                                             const double *__restrict__ b, const uint8_t *__restrict__ dmask,
-                                             int zeroDir, const double *__restrict__ dotv, double *__restrict__ out) {
+template <typename T>
+__device__ __forceinline__ double finish_row(const Geom2 &g, int64_t n, int j, int nyv, int mode, const T f[2],
+                                             const T *__restrict__ b, const uint8_t *__restrict__ dmask, int zeroDir,
+                                             const double *__restrict__ dotv, T *__restrict__ out) {
     const uint8_t dm = dmask ? dmask[n] : 0;
-    double v[2];
+    T v[2];
     if (mode == 0) {
         const bool live = j < nyv;
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
-            v[c] = live ? f[c] : 0.0;
-            if (zeroDir && (dm >> c & 1)) v[c] = 0.0;
+            v[c] = live ? f[c] : T(0);
+            if (zeroDir && (dm >> c & 1)) v[c] = T(0);
             out[c * g.NN + n] = v[c];
         }
-        if (dotv && live) return dotv[n] * v[0] + dotv[g.NN + n] * v[1];
+        if (dotv && live) return dotv[n] * (double)v[0] + dotv[g.NN + n] * (double)v[1];
         return 0.0;
     }
     const int h = min(nyv + MARGIN, g.nn[1]);
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-        if (j < h) v[c] = b[c * g.NN + n] - (j < nyv ? f[c] : 0.0);
+        if (j < h) v[c] = b[c * g.NN + n] - (j < nyv ? f[c] : T(0));
         else v[c] = out[c * g.NN + n];
-        if (dm >> c & 1) v[c] = 0.0;
+        if (dm >> c & 1) v[c] = T(0);
         out[c * g.NN + n] = v[c];
     }
     return 0.0;
 }
 
-__global__ void __launch_bounds__(BS) applyk2_fine_kernel(Geom2 g, const double *__restrict__ Y, Mat8 K0,
-                                                          const double *__restrict__ u, double *__restrict__ out,
-                                                          int mode, const double *__restrict__ b,
-                                                          const uint8_t *__restrict__ dmask, int zeroDir,
-                                                          const double *__restrict__ dotv,
+template <typename T>
+__global__ void __launch_bounds__(BS) applyk2_fine_kernel(Geom2 g, const T *__restrict__ Y, Mat8T<T> K0,
+                                                          const T *__restrict__ u, T *__restrict__ out, int mode,
+                                                          const T *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                          int zeroDir, const double *__restrict__ dotv,
                                                           double *__restrict__ partials) {
     VFEM_PDL_ENTRY();
     const int nyv = g.nyv();
     double dacc = 0.0;
     for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
         const int i = (int)(n / g.nn[1]), j = (int)(n - (int64_t)i * g.nn[1]);
-        double f[2] = {0.0, 0.0}, M[4];
+        T f[2] = {T(0), T(0)}, M[4];
         if (j < nyv) {
-            Patch p;
+            Patch<T> p;
             load_patch(g, u, i, j, p);
             fine_row<false>(g, Y, K0, p, i, j, f, M);
+        }
+        dacc += finish_row(g, n, j, nyv, mode, f, b, dmask, zeroDir, dotv, out);
+    }
+    if (partials) {
+        const double s = block_sum<BS>(dacc);
+        if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    }
+}
+
+// The fine operator in double-float on the FP32 pipe: FP64-class accuracy (about 2^-44 per
+// operation) without FP64 arithmetic. u and Y arrive pre-split into hi/lo floats (the split's
+// FP64 subtraction stays out of the per-node loop), K0 as hi/lo float tables; only the epilogue
+// (result, residual form, dot partial) is FP64. Modes as applyk2_fine_kernel.
+__global__ void __launch_bounds__(BS) applyk2_df_kernel(Geom2 g, const float *__restrict__ Yh,
+                                                        const float *__restrict__ Yl, Mat8T<float> Kh,
+                                                        Mat8T<float> Kl, const float *__restrict__ uh,
+                                                        const float *__restrict__ ul, double *__restrict__ out,
+                                                        int mode, const double *__restrict__ b,
+                                                        const uint8_t *__restrict__ dmask, int zeroDir,
+                                                        const double *__restrict__ dotv,
+                                                        double *__restrict__ partials) {
+    VFEM_PDL_ENTRY();
+    const int nyv = g.nyv();
+    double dacc = 0.0;
+    for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
+        const int i = (int)(n / g.nn[1]), j = (int)(n - (int64_t)i * g.nn[1]);
+        double f[2] = {0.0, 0.0};
+        if (j < nyv) {
+            Patch<float> ph, pl;
+            load_patch(g, uh, i, j, ph);
+            load_patch(g, ul, i, j, pl);
+            float fh[2] = {0.f, 0.f}, fl[2] = {0.f, 0.f};
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int bb = 0; bb < 2; ++bb) {
+                    const int ei = i - a, ej = j - bb;
+                    if (ei < 0 || ej < 0 || ei >= g.ne[0] || ej >= g.ne[1]) continue;
+                    const int64_t e = g.elem(ei, ej);
+                    const float eh = Yh[e], el = Yl[e];
+                    const int ln = 2 * a + bb;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const int row = 2 * ln + c;
+                        float ah = 0.f, al = 0.f;
+#pragma unroll
+                        for (int m = 0; m < 4; ++m) {
+                            const int pi = 1 - a + (m >> 1), pj = 1 - bb + (m & 1);
+#pragma unroll
+                            for (int d = 0; d < 2; ++d) {
+                                const int k = (2 * m + d) * 8 + row;
+                                df_fma_acc(Kh.a[k], Kl.a[k], ph.u[pi][pj][d], pl.u[pi][pj][d], ah, al);
+                            }
+                        }
+                        df_fma_acc(eh, el, ah, al, fh[c], fl[c]);
+                    }
+                }
+            f[0] = (double)fh[0] + (double)fl[0];
+            f[1] = (double)fh[1] + (double)fl[1];
         }
         dacc += finish_row(g, n, j, nyv, mode, f, b, dmask, zeroDir, dotv, out);
     }
@@ -152,8 +215,9 @@ __device__ __forceinline__ bool color_node(const Geom2 &g, int color, int nyv, i
 }
 
 // visitNodesMulticolored with 4 colours (MultigridSolver.hh:409-458) on the fine level
-__global__ void __launch_bounds__(BS) gs2_fine_kernel(Geom2 g, const double *__restrict__ Y, Mat8 K0,
-                                                      double *__restrict__ u, const double *__restrict__ b,
+template <typename T>
+__global__ void __launch_bounds__(BS) gs2_fine_kernel(Geom2 g, const T *__restrict__ Y, Mat8T<T> K0,
+                                                      T *__restrict__ u, const T *__restrict__ b,
                                                       const uint8_t *__restrict__ dmask, int color, int forward) {
     VFEM_PDL_ENTRY();
     int i, j;
@@ -161,12 +225,12 @@ __global__ void __launch_bounds__(BS) gs2_fine_kernel(Geom2 g, const double *__r
     const int64_t n = g.node(i, j);
     const uint8_t dm = dmask[n];
     if (dm == 3) return;
-    Patch p;
+    Patch<T> p;
     load_patch(g, u, i, j, p);
-    double f[2], M[4];
+    T f[2], M[4];
     fine_row<true>(g, Y, K0, p, i, j, f, M);
-    const double bms[2] = {b[n] - f[0], b[g.NN + n] - f[1]};
-    double du[2];
+    const T bms[2] = {b[n] - f[0], b[g.NN + n] - f[1]};
+    T du[2];
     node_solve(dm, bms, M, forward != 0, du);
     u[n] = p.u[1][1][0] + du[0];
     u[g.NN + n] = p.u[1][1][1] + du[1];
@@ -227,15 +291,15 @@ __global__ void __launch_bounds__(BS) stencil2_from_ke_kernel(Geom2 g, const dou
     for (int k = 0; k < 36; ++k) S[(int64_t)k * g.NN + n] = acc[k];
 }
 
-template <bool DIAG>
-__device__ __forceinline__ void stencil_row(const Geom2 &g, const double *__restrict__ S, const Patch &p, int64_t n,
-                                            double f[2], double M[4]) {
-    f[0] = f[1] = 0.0;
+template <bool DIAG, typename T>
+__device__ __forceinline__ void stencil_row(const Geom2 &g, const T *__restrict__ S, const Patch<T> &p, int64_t n,
+                                            T f[2], T M[4]) {
+    f[0] = f[1] = T(0);
 #pragma unroll
     for (int o = 0; o < 9; ++o) {
         const int di = o / 3, dj = o % 3;
-        const double s00 = S[(int64_t)(o * 4 + 0) * g.NN + n], s01 = S[(int64_t)(o * 4 + 1) * g.NN + n];
-        const double s10 = S[(int64_t)(o * 4 + 2) * g.NN + n], s11 = S[(int64_t)(o * 4 + 3) * g.NN + n];
+        const T s00 = S[(int64_t)(o * 4 + 0) * g.NN + n], s01 = S[(int64_t)(o * 4 + 1) * g.NN + n];
+        const T s10 = S[(int64_t)(o * 4 + 2) * g.NN + n], s11 = S[(int64_t)(o * 4 + 3) * g.NN + n];
         f[0] += s00 * p.u[di][dj][0] + s01 * p.u[di][dj][1];
         f[1] += s10 * p.u[di][dj][0] + s11 * p.u[di][dj][1];
         if (DIAG && o == 4) {
@@ -244,60 +308,62 @@ __device__ __forceinline__ void stencil_row(const Geom2 &g, const double *__rest
     }
 }
 
-__global__ void __launch_bounds__(BS) stencil2_apply_kernel(Geom2 g, const double *__restrict__ S,
-                                                            const double *__restrict__ u, double *__restrict__ out,
-                                                            int mode, const double *__restrict__ b,
+template <typename T>
+__global__ void __launch_bounds__(BS) stencil2_apply_kernel(Geom2 g, const T *__restrict__ S, const T *__restrict__ u,
+                                                            T *__restrict__ out, int mode, const T *__restrict__ b,
                                                             const uint8_t *__restrict__ dmask) {
     VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     const int nyv = g.nyv();
     const int i = (int)(n / g.nn[1]), j = (int)(n - (int64_t)i * g.nn[1]);
-    double f[2] = {0.0, 0.0}, M[4];
+    T f[2] = {T(0), T(0)}, M[4];
     if (j < nyv) {
-        Patch p;
+        Patch<T> p;
         load_patch(g, u, i, j, p);
         stencil_row<false>(g, S, p, n, f, M);
     }
     finish_row(g, n, j, nyv, mode, f, b, dmask, 0, nullptr, out);
 }
 
-__global__ void __launch_bounds__(BS) gs2_stencil_kernel(Geom2 g, const double *__restrict__ S,
-                                                         double *__restrict__ u, const double *__restrict__ b,
-                                                         const uint8_t *__restrict__ dmask, int color, int forward) {
+template <typename T>
+__global__ void __launch_bounds__(BS) gs2_stencil_kernel(Geom2 g, const T *__restrict__ S, T *__restrict__ u,
+                                                         const T *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                         int color, int forward) {
     VFEM_PDL_ENTRY();
     int i, j;
     if (!color_node(g, color, g.nyv(), blockIdx.x * (int64_t)BS + threadIdx.x, i, j)) return;
     const int64_t n = g.node(i, j);
     const uint8_t dm = dmask[n];
     if (dm == 3) return;
-    Patch p;
+    Patch<T> p;
     load_patch(g, u, i, j, p);
-    double f[2], M[4];
+    T f[2], M[4];
     stencil_row<true>(g, S, p, n, f, M);
-    const double bms[2] = {b[n] - f[0], b[g.NN + n] - f[1]};
-    double du[2];
+    const T bms[2] = {b[n] - f[0], b[g.NN + n] - f[1]};
+    T du[2];
     node_solve(dm, bms, M, forward != 0, du);
     u[n] = p.u[1][1][0] + du[0];
     u[g.NN + n] = p.u[1][1][1] + du[1];
 }
 
 // MultigridSolver.hh:217-275 (full weighting over the nondetached fine rows)
-__global__ void __launch_bounds__(BS) restrict2_kernel(Geom2 gf, Geom2 gc, const double *__restrict__ fine,
-                                                       double *__restrict__ coarse) {
+template <typename T>
+__global__ void __launch_bounds__(BS) restrict2_kernel(Geom2 gf, Geom2 gc, const T *__restrict__ fine,
+                                                       T *__restrict__ coarse) {
     VFEM_PDL_ENTRY();
     const int64_t cn = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (cn >= gc.NN) return;
     const int i = (int)(cn / gc.nn[1]), j = (int)(cn - (int64_t)i * gc.nn[1]);
     const int cyv = gc.nyv(), fyv = gf.nyv();
     if (j > cyv || (j == cyv && cyv == gc.nn[1])) return;
-    double v0 = 0.0, v1 = 0.0;
+    T v0 = T(0), v1 = T(0);
     if (j < cyv) {
         const int alo = max(2 * i - 1, 0), ahi = min(2 * i + 2, gf.nn[0]);
         const int blo = max(2 * j - 1, 0), bhi = min(2 * j + 2, fyv);
         for (int a = alo; a < ahi; ++a)
             for (int b = blo; b < bhi; ++b) {
-                const double w = (1 - abs(a - 2 * i) * 0.5) * (1 - abs(b - 2 * j) * 0.5);
+                const T w = (T(1) - abs(a - 2 * i) * T(0.5)) * (T(1) - abs(b - 2 * j) * T(0.5));
                 const int64_t fn = gf.node(a, b);
                 v0 += w * fine[fn];
                 v1 += w * fine[gf.NN + fn];
@@ -308,8 +374,9 @@ __global__ void __launch_bounds__(BS) restrict2_kernel(Geom2 gf, Geom2 gc, const
 }
 
 // MultigridSolver.hh:163-212
-__global__ void __launch_bounds__(BS) interp2_kernel(Geom2 gf, Geom2 gc, const double *__restrict__ coarse,
-                                                     double *__restrict__ fine, int accumulate) {
+template <typename T>
+__global__ void __launch_bounds__(BS) interp2_kernel(Geom2 gf, Geom2 gc, const T *__restrict__ coarse,
+                                                     T *__restrict__ fine, int accumulate) {
     VFEM_PDL_ENTRY();
     const int64_t fn = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (fn >= gf.NN) return;
@@ -323,15 +390,15 @@ __global__ void __launch_bounds__(BS) interp2_kernel(Geom2 gf, Geom2 gc, const d
         ec[d] = min(f[d] / 2, gc.ne[d]);
         lf[d] = f[d] - 2 * ec[d];
     }
-    double acc0 = accumulate ? fine[fn] : 0.0, acc1 = accumulate ? fine[gf.NN + fn] : 0.0;
+    T acc0 = accumulate ? fine[fn] : T(0), acc1 = accumulate ? fine[gf.NN + fn] : T(0);
 #pragma unroll
     for (int cn = 0; cn < 4; ++cn) {
         const int cb[2] = {cn >> 1, cn & 1};
-        double coeff = 1.0;
+        T coeff = T(1);
 #pragma unroll
         for (int d = 0; d < 2; ++d)
-            coeff *= (lf[d] == 1) ? 0.5 : ((lf[d] == 0) ? (cb[d] ? 0.0 : 1.0) : (cb[d] ? 1.0 : 0.0));
-        if (coeff == 0.0) continue;
+            coeff *= (lf[d] == 1) ? T(0.5) : ((lf[d] == 0) ? (cb[d] ? T(0) : T(1)) : (cb[d] ? T(1) : T(0)));
+        if (coeff == T(0)) continue;
         const int64_t c = gc.node(ec[0] + cb[0], ec[1] + cb[1]);
         acc0 += coeff * coarse[c];
         acc1 += coeff * coarse[gc.NN + c];
@@ -340,33 +407,36 @@ __global__ void __launch_bounds__(BS) interp2_kernel(Geom2 gf, Geom2 gc, const d
     fine[gf.NN + fn] = acc1;
 }
 
-__global__ void zero_dirichlet2_kernel(Geom2 g, double *__restrict__ u, const uint8_t *__restrict__ dmask) {
+template <typename T>
+__global__ void zero_dirichlet2_kernel(Geom2 g, T *__restrict__ u, const uint8_t *__restrict__ dmask) {
     VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     const uint8_t dm = dmask[n];
-    if (dm & 1) u[n] = 0.0;
-    if (dm & 2) u[g.NN + n] = 0.0;
+    if (dm & 1) u[n] = T(0);
+    if (dm & 2) u[g.NN + n] = T(0);
 }
 
-__global__ void enforce_dirichlet2_kernel(Geom2 g, double *__restrict__ u, const uint8_t *__restrict__ dmask,
+template <typename T>
+__global__ void enforce_dirichlet2_kernel(Geom2 g, T *__restrict__ u, const uint8_t *__restrict__ dmask,
                                           const double *__restrict__ dval) {
     VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     const uint8_t dm = dmask[n];
-    if (dm & 1) u[n] = dval ? dval[n] : 0.0;
-    if (dm & 2) u[g.NN + n] = dval ? dval[g.NN + n] : 0.0;
+    if (dm & 1) u[n] = dval ? (T)dval[n] : T(0);
+    if (dm & 2) u[g.NN + n] = dval ? (T)dval[g.NN + n] : T(0);
 }
 
-__global__ void masked_zero2_kernel(Geom2 g, double *__restrict__ u, int margin) {
+template <typename T>
+__global__ void masked_zero2_kernel(Geom2 g, T *__restrict__ u, int margin) {
     VFEM_PDL_ENTRY();
     const int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (n >= g.NN) return;
     const int j = (int)(n % g.nn[1]);
     if (j >= min(g.nyv() + margin, g.nn[1])) return;
-    u[n] = 0.0;
-    u[g.NN + n] = 0.0;
+    u[n] = T(0);
+    u[g.NN + n] = T(0);
 }
 
 __global__ void dense2_from_stencil_kernel(Geom2 g, const double *__restrict__ S, const int *__restrict__ red,
@@ -392,19 +462,21 @@ __global__ void dense2_from_stencil_kernel(Geom2 g, const double *__restrict__ S
     }
 }
 
+template <typename T>
 __global__ void gather_free2_kernel(Geom2 g, const int *__restrict__ freeIdx, const int *__restrict__ nfreeDev,
-                                    const double *__restrict__ b, double *__restrict__ out) {
+                                    const T *__restrict__ b, double *__restrict__ out) {
     VFEM_PDL_ENTRY();
     const int nfree = *nfreeDev;
     const int t = blockIdx.x * BS + threadIdx.x;
     if (t >= nfree) return;
     const int d = freeIdx[t];
-    out[t] = b[(int64_t)(d & 1) * g.NN + (d >> 1)];
+    out[t] = (double)b[(int64_t)(d & 1) * g.NN + (d >> 1)];
 }
 
+template <typename T>
 __global__ void symv_scatter2_kernel(Geom2 g, const double *__restrict__ Ainv, const int *__restrict__ freeIdx,
                                      const int *__restrict__ nfreeDev, const double *__restrict__ bf,
-                                     double *__restrict__ x) {
+                                     T *__restrict__ x) {
     VFEM_PDL_ENTRY();
     const int nfree = *nfreeDev;
     const int row = blockIdx.x * (BS / 32) + (threadIdx.x >> 5);
@@ -416,13 +488,14 @@ __global__ void symv_scatter2_kernel(Geom2 g, const double *__restrict__ Ainv, c
     acc = warp_sum(acc);
     if (lane == 0) {
         const int d = freeIdx[row];
-        x[(int64_t)(d & 1) * g.NN + (d >> 1)] = acc;
+        x[(int64_t)(d & 1) * g.NN + (d >> 1)] = (T)acc;
     }
 }
 
-__global__ void fill2_kernel(double *__restrict__ p, int64_t n) {
+template <typename T>
+__global__ void fill2_kernel(T *__restrict__ p, int64_t n) {
     VFEM_PDL_ENTRY();
-    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) p[t] = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < n; t += (int64_t)gridDim.x * BS) p[t] = T(0);
 }
 
 // ---------------- CG vector kernels (MultigridSolver.hh:1047-1152) ----------------
@@ -439,7 +512,8 @@ __global__ void __launch_bounds__(BS) dot2_kernel(Geom2 g, const double *__restr
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-__global__ void __launch_bounds__(BS) precond_out2_kernel(Geom2 g, const double *__restrict__ src,
+template <typename Ts>
+__global__ void __launch_bounds__(BS) precond_out2_kernel(Geom2 g, const Ts *__restrict__ src,
                                                           double *__restrict__ s, const double *__restrict__ r,
                                                           const uint8_t *__restrict__ dmask,
                                                           double *__restrict__ partials) {
@@ -448,7 +522,7 @@ __global__ void __launch_bounds__(BS) precond_out2_kernel(Geom2 g, const double 
     double acc = 0.0;
     for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
         const uint8_t dm = dmask[n];
-        const double s0 = (dm & 1) ? 0.0 : src[n], s1 = (dm & 2) ? 0.0 : src[g.NN + n];
+        const double s0 = (dm & 1) ? 0.0 : (double)src[n], s1 = (dm & 2) ? 0.0 : (double)src[g.NN + n];
         s[n] = s0;
         s[g.NN + n] = s1;
         if ((int)(n % g.nn[1]) < nyv) acc += r[n] * s0 + r[g.NN + n] * s1;
@@ -457,12 +531,16 @@ __global__ void __launch_bounds__(BS) precond_out2_kernel(Geom2 g, const double 
     if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 
+// d = beta d + s; when dh is given also the double-float split of the new d (dh + dl)
 __global__ void direction2_kernel(Geom2 g, const double *__restrict__ s, double *__restrict__ d,
-                                  const double *__restrict__ sc) {
+                                  const double *__restrict__ sc, float *__restrict__ dh, float *__restrict__ dl) {
     VFEM_PDL_ENTRY();
     const double beta = sc[2];
-    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < 2 * g.NN; t += (int64_t)gridDim.x * BS)
-        d[t] = beta * d[t] + s[t];
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < 2 * g.NN; t += (int64_t)gridDim.x * BS) {
+        const double v = beta * d[t] + s[t];
+        d[t] = v;
+        if (dh) df_split(v, dh[t], dl[t]);
+    }
 }
 
 __global__ void __launch_bounds__(BS) cg_update2_kernel(Geom2 g, double *__restrict__ x, double *__restrict__ r,
@@ -613,18 +691,29 @@ void launch2_young(const Geom2 &g, const double *rho, double *Y, double E0, doub
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_applyk_fine(const Geom2 &g, const double *Y, const Mat8 &K0, const double *u, double *out, int mode,
-                         const double *b, const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials,
-                         cudaStream_t st) {
+template <typename T>
+void launch2_applyk_fine(const Geom2 &g, const T *Y, const Mat8T<T> &K0, const T *u, T *out, int mode, const T *b,
+                         const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials, cudaStream_t st) {
     const unsigned grid = partials ? (unsigned)REDUCE_BLOCKS : gridFor(g.NN, BS);
-    launch_pdl(applyk2_fine_kernel, grid, BS, 0, st, g, Y, K0, u, out, mode, b, dmask, zeroDir ? 1 : 0, dotv,
+    launch_pdl(applyk2_fine_kernel<T>, grid, BS, 0, st, g, Y, K0, u, out, mode, b, dmask, zeroDir ? 1 : 0, dotv,
                partials);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_gs_fine(const Geom2 &g, const double *Y, const Mat8 &K0, double *u, const double *b,
-                     const uint8_t *dmask, int color, bool forward, cudaStream_t st) {
-    launch_pdl(gs2_fine_kernel, colorBlocks(g), BS, 0, st, g, Y, K0, u, b, dmask, color, forward ? 1 : 0);
+void launch2_applyk_df(const Geom2 &g, const float *Yh, const float *Yl, const Mat8T<float> &Kh,
+                       const Mat8T<float> &Kl, const float *uh, const float *ul, double *out, int mode,
+                       const double *b, const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials,
+                       cudaStream_t st) {
+    const unsigned grid = partials ? (unsigned)REDUCE_BLOCKS : gridFor(g.NN, BS);
+    launch_pdl(applyk2_df_kernel, grid, BS, 0, st, g, Yh, Yl, Kh, Kl, uh, ul, out, mode, b, dmask, zeroDir ? 1 : 0,
+               dotv, partials);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch2_gs_fine(const Geom2 &g, const T *Y, const Mat8T<T> &K0, T *u, const T *b, const uint8_t *dmask, int color,
+                     bool forward, cudaStream_t st) {
+    launch_pdl(gs2_fine_kernel<T>, colorBlocks(g), BS, 0, st, g, Y, K0, u, b, dmask, color, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -639,41 +728,47 @@ void launch2_stencil_from_ke(const Geom2 &g, const double *Ke, double *S, cudaSt
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_stencil_apply(const Geom2 &g, const double *S, const double *u, double *out, int mode, const double *b,
-                           const uint8_t *dmask, cudaStream_t st) {
-    launch_pdl(stencil2_apply_kernel, gridFor(g.NN, BS), BS, 0, st, g, S, u, out, mode, b, dmask);
+template <typename T>
+void launch2_stencil_apply(const Geom2 &g, const T *S, const T *u, T *out, int mode, const T *b, const uint8_t *dmask,
+                           cudaStream_t st) {
+    launch_pdl(stencil2_apply_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, S, u, out, mode, b, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_gs_stencil(const Geom2 &g, const double *S, double *u, const double *b, const uint8_t *dmask, int color,
-                        bool forward, cudaStream_t st) {
-    launch_pdl(gs2_stencil_kernel, colorBlocks(g), BS, 0, st, g, S, u, b, dmask, color, forward ? 1 : 0);
+template <typename T>
+void launch2_gs_stencil(const Geom2 &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
+                        cudaStream_t st) {
+    launch_pdl(gs2_stencil_kernel<T>, colorBlocks(g), BS, 0, st, g, S, u, b, dmask, color, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_restrict(const Geom2 &gf, const Geom2 &gc, const double *fine, double *coarse, cudaStream_t st) {
-    launch_pdl(restrict2_kernel, gridFor(gc.NN, BS), BS, 0, st, gf, gc, fine, coarse);
+template <typename T>
+void launch2_restrict(const Geom2 &gf, const Geom2 &gc, const T *fine, T *coarse, cudaStream_t st) {
+    launch_pdl(restrict2_kernel<T>, gridFor(gc.NN, BS), BS, 0, st, gf, gc, fine, coarse);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_interpolate(const Geom2 &gf, const Geom2 &gc, const double *coarse, double *fine, bool accumulate,
-                         cudaStream_t st) {
-    launch_pdl(interp2_kernel, gridFor(gf.NN, BS), BS, 0, st, gf, gc, coarse, fine, accumulate ? 1 : 0);
+template <typename T>
+void launch2_interpolate(const Geom2 &gf, const Geom2 &gc, const T *coarse, T *fine, bool accumulate, cudaStream_t st) {
+    launch_pdl(interp2_kernel<T>, gridFor(gf.NN, BS), BS, 0, st, gf, gc, coarse, fine, accumulate ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_zero_dirichlet(const Geom2 &g, double *u, const uint8_t *dmask, cudaStream_t st) {
-    launch_pdl(zero_dirichlet2_kernel, gridFor(g.NN, BS), BS, 0, st, g, u, dmask);
+template <typename T>
+void launch2_zero_dirichlet(const Geom2 &g, T *u, const uint8_t *dmask, cudaStream_t st) {
+    launch_pdl(zero_dirichlet2_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, u, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_enforce_dirichlet(const Geom2 &g, double *u, const uint8_t *dmask, const double *dval, cudaStream_t st) {
-    launch_pdl(enforce_dirichlet2_kernel, gridFor(g.NN, BS), BS, 0, st, g, u, dmask, dval);
+template <typename T>
+void launch2_enforce_dirichlet(const Geom2 &g, T *u, const uint8_t *dmask, const double *dval, cudaStream_t st) {
+    launch_pdl(enforce_dirichlet2_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, u, dmask, dval);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_masked_zero(const Geom2 &g, double *u, int margin, cudaStream_t st) {
-    launch_pdl(masked_zero2_kernel, gridFor(g.NN, BS), BS, 0, st, g, u, margin);
+template <typename T>
+void launch2_masked_zero(const Geom2 &g, T *u, int margin, cudaStream_t st) {
+    launch_pdl(masked_zero2_kernel<T>, gridFor(g.NN, BS), BS, 0, st, g, u, margin);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -684,14 +779,15 @@ void launch2_dense_from_stencil(const Geom2 &g, const double *S, const int *red,
     VFEM_LAUNCH_CHECK();
 }
 
+template <typename T>
 void launch2_coarse_solve(const Geom2 &g, const double *Ainv, const int *freeIdx, const int *nfreeDev, int nfreeCap,
-                          const double *b, double *x, double *scratch, cudaStream_t st) {
-    launch_pdl(fill2_kernel, std::min<unsigned>(gridFor(2 * g.NN, BS), 4 * NUM_SMS), BS, 0, st, x, 2 * g.NN);
+                          const T *b, T *x, double *scratch, cudaStream_t st) {
+    launch_pdl(fill2_kernel<T>, std::min<unsigned>(gridFor(2 * g.NN, BS), 4 * NUM_SMS), BS, 0, st, x, 2 * g.NN);
     VFEM_LAUNCH_CHECK();
     if (nfreeCap <= 0) return;
-    launch_pdl(gather_free2_kernel, gridFor(nfreeCap, BS), BS, 0, st, g, freeIdx, nfreeDev, b, scratch);
+    launch_pdl(gather_free2_kernel<T>, gridFor(nfreeCap, BS), BS, 0, st, g, freeIdx, nfreeDev, b, scratch);
     VFEM_LAUNCH_CHECK();
-    launch_pdl(symv_scatter2_kernel, gridFor(nfreeCap, BS / 32), BS, 0, st, g, Ainv, freeIdx, nfreeDev,
+    launch_pdl(symv_scatter2_kernel<T>, gridFor(nfreeCap, BS / 32), BS, 0, st, g, Ainv, freeIdx, nfreeDev,
                (const double *)scratch, x);
     VFEM_LAUNCH_CHECK();
 }
@@ -701,14 +797,17 @@ void launch2_dot_partials(const Geom2 &g, const double *a, const double *b, doub
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_precond_out(const Geom2 &g, const double *src, double *s, const double *r, const uint8_t *dmask,
+template <typename Ts>
+void launch2_precond_out(const Geom2 &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                          double *partials, cudaStream_t st) {
-    launch_pdl(precond_out2_kernel, REDUCE_BLOCKS, BS, 0, st, g, src, s, r, dmask, partials);
+    launch_pdl(precond_out2_kernel<Ts>, REDUCE_BLOCKS, BS, 0, st, g, src, s, r, dmask, partials);
     VFEM_LAUNCH_CHECK();
 }
 
-void launch2_direction(const Geom2 &g, const double *s, double *d, const double *sc, cudaStream_t st) {
-    launch_pdl(direction2_kernel, std::min<unsigned>(gridFor(2 * g.NN, BS), 4 * NUM_SMS), BS, 0, st, g, s, d, sc);
+void launch2_direction(const Geom2 &g, const double *s, double *d, const double *sc, cudaStream_t st, float *dh,
+                       float *dl) {
+    launch_pdl(direction2_kernel, std::min<unsigned>(gridFor(2 * g.NN, BS), 4 * NUM_SMS), BS, 0, st, g, s, d, sc, dh,
+               dl);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -744,5 +843,27 @@ void launch2_subspace_combine(const Geom2 &g, const LblVectors &U, int s, const 
     subspace_combine2_kernel<<<gridFor(g.NN, BS), BS, 0, st>>>(g, U, s, cDev, cv, x);
     VFEM_LAUNCH_CHECK();
 }
+
+
+#define VFEM_2D_INSTANTIATE(T)                                                                                         \
+    template void launch2_applyk_fine<T>(const Geom2 &, const T *, const Mat8T<T> &, const T *, T *, int, const T *,   \
+                                         const uint8_t *, bool, const double *, double *, cudaStream_t);               \
+    template void launch2_gs_fine<T>(const Geom2 &, const T *, const Mat8T<T> &, T *, const T *, const uint8_t *, int, \
+                                     bool, cudaStream_t);                                                              \
+    template void launch2_stencil_apply<T>(const Geom2 &, const T *, const T *, T *, int, const T *, const uint8_t *,  \
+                                           cudaStream_t);                                                              \
+    template void launch2_gs_stencil<T>(const Geom2 &, const T *, T *, const T *, const uint8_t *, int, bool,          \
+                                        cudaStream_t);                                                                 \
+    template void launch2_restrict<T>(const Geom2 &, const Geom2 &, const T *, T *, cudaStream_t);                     \
+    template void launch2_interpolate<T>(const Geom2 &, const Geom2 &, const T *, T *, bool, cudaStream_t);            \
+    template void launch2_zero_dirichlet<T>(const Geom2 &, T *, const uint8_t *, cudaStream_t);                        \
+    template void launch2_enforce_dirichlet<T>(const Geom2 &, T *, const uint8_t *, const double *, cudaStream_t);     \
+    template void launch2_masked_zero<T>(const Geom2 &, T *, int, cudaStream_t);                                       \
+    template void launch2_coarse_solve<T>(const Geom2 &, const double *, const int *, const int *, int, const T *, T *, \
+                                          double *, cudaStream_t);                                                     \
+    template void launch2_precond_out<T>(const Geom2 &, const T *, double *, const double *, const uint8_t *, double *, \
+                                         cudaStream_t);
+VFEM_2D_INSTANTIATE(float)
+VFEM_2D_INSTANTIATE(double)
 
 }  // namespace vfem

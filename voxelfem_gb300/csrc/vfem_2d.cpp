@@ -266,7 +266,7 @@ void Grid2::applyK(const double *u, double *out) {
     View vu, vo;
     viewIn(vu, u, 2 * g.NN * sizeof(double), stream);
     viewOut(vo, out, 2 * g.NN * sizeof(double));
-    launch2_applyk_fine(g, Y.p, K0, (const double *)vu.d, (double *)vo.d, 0, nullptr, nullptr, false, nullptr,
+    launch2_applyk_fine<double>(g, Y.p, K0, (const double *)vu.d, (double *)vo.d, 0, nullptr, nullptr, false, nullptr,
                         nullptr, stream);
     finishOut(vo, stream);
 }
@@ -495,6 +495,7 @@ void MG2::ensureStiffness() {
         VFEM_CUDA(cudaStreamSynchronize(st));
         if (bad) throw Error(ERR_NOT_SPD, "Coarsest matrix not positive definite");
     }
+    if (precision == PREC_MIXED) refreshSingle();
     VFEM_CUDA(cudaStreamSynchronize(st));
     builtVersion = fine->version;
     stiffValid = true;
@@ -505,67 +506,180 @@ void MG2::updateStiffness() {
     ensureStiffness();
 }
 
-// operator of level l (fine: matrix-free; coarser: stencils); mode 0 apply, 1 residual
-void MG2::levelOperator(int l, const double *u, double *out, int mode, const double *b) {
-    cudaStream_t st = fine->stream;
-    if (l == 0)
-        launch2_applyk_fine(lv[0].g, fine->Y.p, fine->K0, u, out, mode, b, fine->dmask.p, false, nullptr, nullptr, st);
-    else launch2_stencil_apply(lv[l].g, lv[l].S.p, u, out, mode, b, lv[l].dmask.p, st);
+template <>
+MG2::LB<double> MG2::lb<double>(int l) {
+    return {lv[l].x.p, lv[l].b.p, lv[l].r.p, lv[l].S.p};
+}
+template <>
+MG2::LB<float> MG2::lb<float>(int l) {
+    return {lv[l].x32.p, lv[l].b32.p, lv[l].r32.p, lv[l].S32.p};
+}
+template <>
+const double *MG2::fineY<double>() const {
+    return fine->Y.p;
+}
+template <>
+const float *MG2::fineY<float>() const {
+    return Y32.p;
+}
+template <>
+const Mat8T<double> &MG2::fineK0<double>() const {
+    return fine->K0;
+}
+template <>
+const Mat8T<float> &MG2::fineK0<float>() const {
+    return K0f;
 }
 
-void MG2::smoothLevel(int l, double *u, const double *b, bool forward) {
+// operator of level l (fine: matrix-free; coarser: stencils); mode 0 apply, 1 residual
+template <typename T>
+void MG2::levelOperatorT(int l, const T *u, T *out, int mode, const T *b) {
+    cudaStream_t st = fine->stream;
+    if (l == 0)
+        launch2_applyk_fine<T>(lv[0].g, fineY<T>(), fineK0<T>(), u, out, mode, b, fine->dmask.p, false, nullptr, nullptr,
+                               st);
+    else launch2_stencil_apply<T>(lv[l].g, lb<T>(l).S, u, out, mode, b, lv[l].dmask.p, st);
+}
+
+template <typename T>
+void MG2::smoothLevelT(int l, T *u, const T *b, bool forward) {
     cudaStream_t st = fine->stream;
     for (int ci = 0; ci < 4; ++ci) {
         const int color = forward ? ci : 3 - ci;
-        if (l == 0) launch2_gs_fine(lv[0].g, fine->Y.p, fine->K0, u, b, fine->dmask.p, color, forward, st);
-        else launch2_gs_stencil(lv[l].g, lv[l].S.p, u, b, lv[l].dmask.p, color, forward, st);
+        if (l == 0) launch2_gs_fine<T>(lv[0].g, fineY<T>(), fineK0<T>(), u, b, fine->dmask.p, color, forward, st);
+        else launch2_gs_stencil<T>(lv[l].g, lb<T>(l).S, u, b, lv[l].dmask.p, color, forward, st);
     }
 }
 
-void MG2::coarseSolveDev(const double *b, double *x) {
+template <typename T>
+void MG2::coarseSolveDevT(const T *b, T *x) {
     const Level &C = lv.back();
-    launch2_coarse_solve(C.g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, b, x, cscratch.p, fine->stream);
+    launch2_coarse_solve<T>(C.g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, b, x, cscratch.p, fine->stream);
 }
 
 // MultigridSolver.hh:617-658
-void MG2::vcycle(int l, int64_t sweeps, bool residualSystem) {
+template <typename T>
+void MG2::vcycleT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
-    Level &v = lv[l];
+    const LB<T> v = lb<T>(l);
     if (l == L() - 1) {
-        coarseSolveDev(v.b.p, v.x.p);
+        coarseSolveDevT<T>(v.b, v.x);
         return;
     }
-    if (residualSystem || l > 0 || !fine->dvalNonzero) launch2_zero_dirichlet(v.g, v.x.p, levelMask(l), st);
-    else launch2_enforce_dirichlet(v.g, v.x.p, levelMask(l), fine->dval.p, st);
-    for (int64_t t = 0; t < sweeps; ++t) smoothLevel(l, v.x.p, v.b.p, true);
-    levelOperator(l, v.x.p, v.r.p, 1, v.b.p);
-    launch2_restrict(v.g, lv[l + 1].g, v.r.p, lv[l + 1].b.p, st);
-    launch2_masked_zero(lv[l + 1].g, lv[l + 1].x.p, MARGIN, st);
-    vcycle(l + 1, sweeps, true);
-    launch2_interpolate(v.g, lv[l + 1].g, lv[l + 1].x.p, v.x.p, true, st);
-    for (int64_t t = 0; t < sweeps; ++t) smoothLevel(l, v.x.p, v.b.p, !symmetricGS);
+    const Geom2 &g = lv[l].g;
+    if (residualSystem || l > 0 || !fine->dvalNonzero) launch2_zero_dirichlet<T>(g, v.x, levelMask(l), st);
+    else launch2_enforce_dirichlet<T>(g, v.x, levelMask(l), fine->dval.p, st);
+    for (int64_t t = 0; t < sweeps; ++t) smoothLevelT<T>(l, v.x, v.b, true);
+    levelOperatorT<T>(l, v.x, v.r, 1, v.b);
+    const LB<T> c = lb<T>(l + 1);
+    launch2_restrict<T>(g, lv[l + 1].g, v.r, c.b, st);
+    launch2_masked_zero<T>(lv[l + 1].g, c.x, MARGIN, st);
+    vcycleT<T>(l + 1, sweeps, true);
+    launch2_interpolate<T>(g, lv[l + 1].g, c.x, v.x, true, st);
+    for (int64_t t = 0; t < sweeps; ++t) smoothLevelT<T>(l, v.x, v.b, !symmetricGS);
 }
 
 // MultigridSolver.hh:587-609
-void MG2::fmgDown(int l, int64_t sweeps, bool residualSystem) {
+template <typename T>
+void MG2::fmgDownT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
+    const LB<T> v = lb<T>(l);
     if (l == L() - 1) {
-        coarseSolveDev(lv[l].b.p, lv[l].x.p);
+        coarseSolveDevT<T>(v.b, v.x);
         return;
     }
-    launch2_restrict(lv[l].g, lv[l + 1].g, lv[l].b.p, lv[l + 1].b.p, st);
-    fmgDown(l + 1, sweeps, residualSystem);
-    launch2_interpolate(lv[l].g, lv[l + 1].g, lv[l + 1].x.p, lv[l].x.p, false, st);
-    vcycle(l, sweeps, residualSystem);
+    const LB<T> c = lb<T>(l + 1);
+    launch2_restrict<T>(lv[l].g, lv[l + 1].g, v.b, c.b, st);
+    fmgDownT<T>(l + 1, sweeps, residualSystem);
+    launch2_interpolate<T>(lv[l].g, lv[l + 1].g, c.x, v.x, false, st);
+    vcycleT<T>(l, sweeps, residualSystem);
 }
 
-void MG2::runCycles(int64_t steps, int64_t sweeps, bool residualSystem, bool fmg) {
+template <typename T>
+void MG2::runCyclesT(int64_t steps, int64_t sweeps, bool residualSystem, bool fmg) {
     if (fmg) {
-        fmgDown(0, sweeps, residualSystem);
-        for (int64_t i = 1; i < steps; ++i) vcycle(0, sweeps, residualSystem);
+        fmgDownT<T>(0, sweeps, residualSystem);
+        for (int64_t i = 1; i < steps; ++i) vcycleT<T>(0, sweeps, residualSystem);
     } else {
-        for (int64_t i = 0; i < steps; ++i) vcycle(0, sweeps, residualSystem);
+        for (int64_t i = 0; i < steps; ++i) vcycleT<T>(0, sweeps, residualSystem);
     }
+}
+
+void MG2::levelOperator(int l, const double *u, double *out, int mode, const double *b) {
+    levelOperatorT<double>(l, u, out, mode, b);
+}
+void MG2::smoothLevel(int l, double *u, const double *b, bool forward) { smoothLevelT<double>(l, u, b, forward); }
+void MG2::coarseSolveDev(const double *b, double *x) { coarseSolveDevT<double>(b, x); }
+void MG2::runCycles(int64_t steps, int64_t sweeps, bool residualSystem, bool fmg) {
+    runCyclesT<double>(steps, sweeps, residualSystem, fmg);
+}
+
+void MG2::refreshDF() {
+    if (!dfOuter() || dfVersion == fine->version) return;
+    const int64_t ne = lv[0].g.NE, n2 = 2 * lv[0].g.NN;
+    Yh.alloc(ne);
+    Yl.alloc(ne);
+    dh.alloc(n2);
+    dl.alloc(n2);
+    launch_split_df(fine->Y.p, Yh.p, Yl.p, ne, fine->stream);
+    for (int t = 0; t < 64; ++t) {
+        K0f.a[t] = (float)fine->K0.a[t];
+        K0lo.a[t] = (float)(fine->K0.a[t] - (double)K0f.a[t]);
+    }
+    dfVersion = fine->version;
+}
+
+void MG2::outerOperator(const double *u, double *out, int mode, const double *b, bool zeroDir, const double *dotv,
+                        double *partials, bool uSplit) {
+    const Geom2 &g = lv[0].g;
+    if (dfOuter()) {
+        if (!uSplit) launch_split_df(u, dh.p, dl.p, 2 * g.NN, fine->stream);
+        launch2_applyk_df(g, Yh.p, Yl.p, K0f, K0lo, dh.p, dl.p, out, mode, b, fine->dmask.p, zeroDir, dotv, partials,
+                          fine->stream);
+    } else {
+        launch2_applyk_fine<double>(g, fine->Y.p, fine->K0, u, out, mode, b, fine->dmask.p, zeroDir, dotv, partials,
+                                    fine->stream);
+    }
+}
+
+void MG2::setOuterMatvec(int kind) {
+    if (kind != MATVEC_FP64 && kind != MATVEC_DF) throw Error(ERR_ARG, "unknown outer matvec");
+    if (kind == outerMatvec) return;
+    outerMatvec = kind;
+    clearGraphs();
+}
+
+void MG2::setPrecision(int p) {
+    if (p != PREC_FP64 && p != PREC_MIXED) throw Error(ERR_ARG, "unknown precision");
+    if (p == precision) return;
+    precision = p;
+    clearGraphs();
+    if (p == PREC_MIXED) {
+        for (int l = 0; l < L(); ++l) {
+            Level &v = lv[l];
+            const int64_t n2 = 2 * v.g.NN;
+            v.x32.alloc(n2);
+            v.b32.alloc(n2);
+            v.r32.alloc(n2);
+            VFEM_CUDA(cudaMemset(v.x32.p, 0, n2 * sizeof(float)));
+            VFEM_CUDA(cudaMemset(v.b32.p, 0, n2 * sizeof(float)));
+            VFEM_CUDA(cudaMemset(v.r32.p, 0, n2 * sizeof(float)));
+            if (l > 0) v.S32.alloc(36 * v.g.NN);
+        }
+        Y32.alloc(lv[0].g.NE);
+    }
+    stiffValid = false;
+}
+
+// the FP32 copies of the fine moduli, K0 and the coarse stencils (mixed precision)
+void MG2::refreshSingle() {
+    cudaStream_t st = fine->stream;
+    launch_cast<float, double>(fine->Y.p, Y32.p, lv[0].g.NE, st);
+    for (int t = 0; t < 64; ++t) {
+        K0f.a[t] = (float)fine->K0.a[t];
+        K0lo.a[t] = (float)(fine->K0.a[t] - (double)K0f.a[t]);
+    }
+    for (int l = 1; l < L(); ++l) launch_cast<float, double>(lv[l].S.p, lv[l].S32.p, 36 * lv[l].g.NN, st);
 }
 
 // MultigridSolver.hh:547-573
@@ -592,19 +706,30 @@ void MG2::solve(const double *u, const double *f, int64_t steps, int64_t sweeps,
 void MG2::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
-    const double *src = rbuf.p;
-    if (mgIter > 0) {
+    if (mgIter > 0 && precision == PREC_MIXED) {
+        // FP32 V-cycle on the FP64 residual (its rounding is the only precision change)
         if (sweeps != 0) {
-            launch_fill<double>(lv[0].x.p, 0.0, 2 * g.NN, st);  // zero initial guess
-            VFEM_CUDA(cudaMemcpyAsync(lv[0].b.p, rbuf.p, 2 * g.NN * sizeof(double), cudaMemcpyDeviceToDevice, st));
-            runCycles(mgIter, sweeps, true, fmg);
+            launch_fill<float>(lv[0].x32.p, 0.f, 2 * g.NN, st);
+            launch_cast<float, double>(rbuf.p, lv[0].b32.p, 2 * g.NN, st);
+            runCyclesT<float>(mgIter, sweeps, true, fmg);
         }
-        src = lv[0].x.p;
+        launch2_precond_out<float>(g, lv[0].x32.p, sbuf.p, rbuf.p, fine->dmask.p, partials.p, st);
+    } else {
+        const double *src = rbuf.p;
+        if (mgIter > 0) {
+            if (sweeps != 0) {
+                launch_fill<double>(lv[0].x.p, 0.0, 2 * g.NN, st);  // zero initial guess
+                VFEM_CUDA(cudaMemcpyAsync(lv[0].b.p, rbuf.p, 2 * g.NN * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                runCycles(mgIter, sweeps, true, fmg);
+            }
+            src = lv[0].x.p;
+        }
+        launch2_precond_out<double>(g, src, sbuf.p, rbuf.p, fine->dmask.p, partials.p, st);
     }
-    launch2_precond_out(g, src, sbuf.p, rbuf.p, fine->dmask.p, partials.p, st);
     launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
-    launch2_direction(g, sbuf.p, dvec.p, sc.p, st);
-    launch2_applyk_fine(g, fine->Y.p, fine->K0, dvec.p, Ad.p, 0, nullptr, fine->dmask.p, true, dvec.p, partials.p, st);
+    if (dfOuter()) launch2_direction(g, sbuf.p, dvec.p, sc.p, st, dh.p, dl.p);
+    else launch2_direction(g, sbuf.p, dvec.p, sc.p, st);
+    outerOperator(dvec.p, Ad.p, 0, nullptr, true, dvec.p, partials.p, dfOuter());
     launch_cg_alpha(partials.p, REDUCE_BLOCKS, sc.p, st);
     launch2_cg_update(g, x, rbuf.p, dvec.p, Ad.p, sc.p, partials.p, st);
     launch_cg_rsq(partials.p, REDUCE_BLOCKS, sc.p, nullptr, st);
@@ -626,7 +751,7 @@ static uint64_t countKernels(cudaGraph_t gr) {
 
 // [loop control (initial)] -> WHILE( [one PCG iteration] -> [loop control] )
 cudaGraphExec_t MG2::loopGraph(double *x, int64_t mgIter, int64_t sweeps, bool fmg) {
-    const Key key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, x};
+    const Key key{mgIter, sweeps, fmg ? 1 : 0, (symmetricGS ? 1 : 0) | (precision << 1) | (outerMatvec << 2), x};
     auto it = graphs.find(key);
     if (it != graphs.end()) return it->second;
     cudaStream_t st = fine->stream;
@@ -690,10 +815,11 @@ PcgStats MG2::pcgDev(double *x, const double *b, int64_t maxIter, double tol, in
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
     PcgStats stats;
-    if (!dirichletSatisfied) launch2_enforce_dirichlet(g, x, fine->dmask.p, fine->dval.p, st);
+    if (!dirichletSatisfied) launch2_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch2_dot_partials(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
-    launch2_applyk_fine(g, fine->Y.p, fine->K0, x, rbuf.p, 1, b, fine->dmask.p, true, nullptr, nullptr, st);
+    refreshDF();
+    outerOperator(x, rbuf.p, 1, b, true, nullptr, nullptr, false);
     launch2_dot_partials(g, rbuf.p, rbuf.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
     launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
@@ -708,7 +834,7 @@ PcgStats MG2::pcgDev(double *x, const double *b, int64_t maxIter, double tol, in
         // direct solve branch (MultigridSolver.hh:1056-1064)
         if (!(rsq < tol * tol * bnorm2)) {
             coarseSolveDev(b, x);
-            launch2_applyk_fine(g, fine->Y.p, fine->K0, x, rbuf.p, 1, b, fine->dmask.p, true, nullptr, nullptr, st);
+            launch2_applyk_fine<double>(g, fine->Y.p, fine->K0, x, rbuf.p, 1, b, fine->dmask.p, true, nullptr, nullptr, st);
             launch2_dot_partials(g, rbuf.p, rbuf.p, partials.p, st);
             launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
             rsq = readDev(sc.p + 5, st);
@@ -740,15 +866,16 @@ void MG2::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int6
     else syncFine();
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
-    if (!dirichletSatisfied) launch2_enforce_dirichlet(g, x, fine->dmask.p, fine->dval.p, st);
+    if (!dirichletSatisfied) launch2_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch2_dot_partials(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
-    launch2_applyk_fine(g, fine->Y.p, fine->K0, x, rbuf.p, 1, b, fine->dmask.p, true, nullptr, nullptr, st);
+    refreshDF();
+    outerOperator(x, rbuf.p, 1, b, true, nullptr, nullptr, false);  // initial residual through the CG matvec
     launch2_dot_partials(g, rbuf.p, rbuf.p, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 5, st);
     launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
     launch_fill<double>(dvec.p, 0.0, 2 * g.NN, st);
-    pendingKey = Key{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, x};
+    pendingKey = Key{mgIter, sweeps, fmg ? 1 : 0, (symmetricGS ? 1 : 0) | (precision << 1) | (outerMatvec << 2), x};
     VFEM_CUDA(cudaGraphLaunch(loopGraph(x, mgIter, sweeps, fmg), st));
     VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
     pending = true;
@@ -868,22 +995,44 @@ void MG2::zeroDirichlet(int l, double *u) {
 }
 
 // Benchmark hook: average device time of one launch of a hot kernel on resident data.
-// which: 0 fine applyK, 1 fine 4-colour GS sweep, 2 one V-cycle (graph), 3 one PCG iteration.
+// which: 0 fine applyK (FP64), 1 fine 4-colour GS sweep, 2 one V-cycle, 3 one PCG iteration, 4 fine
+// applyK in double-float (sweeps and cycles in the solver's precision).
 double MG2::timeKernel(int which, int reps) {
     ensureStiffness();
     cudaStream_t st = fine->stream;
     const Geom2 &g = lv[0].g;
     DevBuf<double> xt(2 * g.NN);
     VFEM_CUDA(cudaMemsetAsync(xt.p, 0, 2 * g.NN * sizeof(double), st));
+    const int savedOuter = outerMatvec, savedPrec = precision;
+    if (which == 4) {  // the double-float operator on a split copy of the fine iterate
+        precision = PREC_MIXED;
+        outerMatvec = MATVEC_DF;
+        dfVersion = ~0ull;
+        refreshDF();
+        launch_split_df(lv[0].x.p, dh.p, dl.p, 2 * g.NN, st);
+        precision = savedPrec;
+        outerMatvec = savedOuter;
+        dfVersion = ~0ull;
+    }
     launch_cg_init(sc.p, 0.0, 1.0, st);
     auto body = [&]() {
         switch (which) {
         case 0:
-            launch2_applyk_fine(g, fine->Y.p, fine->K0, lv[0].x.p, lv[0].r.p, 0, nullptr, nullptr, false, nullptr,
+            launch2_applyk_fine<double>(g, fine->Y.p, fine->K0, lv[0].x.p, lv[0].r.p, 0, nullptr, nullptr, false, nullptr,
                                 nullptr, st);
             break;
-        case 1: smoothLevel(0, lv[0].x.p, lv[0].b.p, true); break;
-        case 2: runCycles(1, 1, true, false); break;
+        case 1:
+            if (precision == PREC_MIXED) smoothLevelT<float>(0, lv[0].x32.p, lv[0].b32.p, true);
+            else smoothLevel(0, lv[0].x.p, lv[0].b.p, true);
+            break;
+        case 2:
+            if (precision == PREC_MIXED) runCyclesT<float>(1, 1, true, false);
+            else runCycles(1, 1, true, false);
+            break;
+        case 4:
+            launch2_applyk_df(g, Yh.p, Yl.p, K0f, K0lo, dh.p, dl.p, lv[0].r.p, 0, nullptr, nullptr, false, nullptr,
+                              nullptr, st);
+            break;
         default: cgIteration(xt.p, 1, 1, false); break;
         }
     };
@@ -920,7 +1069,7 @@ LBL2::Slot::~Slot() {
     if (done) cudaEventDestroy(done);
 }
 
-LBL2::LBL2(Grid2 *src_, int coarsenings_, int64_t slots) : src(src_), coarsenings(coarsenings_) {
+LBL2::LBL2(Grid2 *src_, int coarsenings_, int64_t slots, int precision) : src(src_), coarsenings(coarsenings_) {
     if (coarsenings < 1) throw Error(ERR_ARG, "layer-by-layer solves need at least one coarsening level");
     if (slots < 1) throw Error(ERR_ARG, "slots must be positive");
     const int64_t NN = src->g.NN, NE = src->g.NE;
@@ -928,6 +1077,7 @@ LBL2::LBL2(Grid2 *src_, int coarsenings_, int64_t slots) : src(src_), coarsening
         std::unique_ptr<Slot> sl(new Slot());
         sl->grid = src->clone();
         sl->mg.reset(new MG2(sl->grid.get(), coarsenings));
+        sl->mg->setPrecision(precision);
         sl->x.alloc(2 * NN);
         sl->f.alloc(2 * NN);
         sl->gtmp.alloc(NE);
@@ -1005,7 +1155,7 @@ void LBL2::guess(Slot &sl, int64_t layer, int ny, bool zeroInit) {
         sl.subC.alloc(LBL_MAX_HISTORY);
         for (int j = 0; j < hs; ++j) {
             sl.Ku[j].alloc(n2);
-            launch2_applyk_fine(gl, g.Y.p, g.K0, U.u[j], sl.Ku[j].p, 0, nullptr, g.dmask.p, true, nullptr, nullptr, st);
+            launch2_applyk_fine<double>(gl, g.Y.p, g.K0, U.u[j], sl.Ku[j].p, 0, nullptr, g.dmask.p, true, nullptr, nullptr, st);
         }
         int p = 0;
         for (int i = 0; i < hs; ++i)

@@ -47,22 +47,32 @@ inline Geom2 makeGeom2(const int ne[2]) {
 }
 
 // 8 x 8 element matrix passed by value (kernel parameters live in the constant bank).
-struct Mat8 {
-    double a[64];
+template <typename T>
+struct Mat8T {
+    T a[64];
 };
+using Mat8 = Mat8T<double>;
 
 // ---------------- kernels (k_2d.cu) ----------------
 void launch2_young(const Geom2 &g, const double *rho, double *Y, double E0, double Emin, double gamma, double q,
                    int law, bool masking, cudaStream_t st);
+// The V-cycle kernels exist for T = float (mixed precision) and T = double.
 // Fine-level matrix-free operator. mode 0: out = K u on the nondetached rows, 0 on detached
 // rows; Dirichlet components zeroed when zeroDir; partials (when given) of dotv . out over the
 // nondetached rows. mode 1: residual, out = b - K u on rows < nyv + MARGIN (rows above keep
 // their values) and Dirichlet components zeroed everywhere (MultigridSolver.hh:527-541).
-void launch2_applyk_fine(const Geom2 &g, const double *Y, const Mat8 &K0, const double *u, double *out, int mode,
-                         const double *b, const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials,
-                         cudaStream_t st);
-void launch2_gs_fine(const Geom2 &g, const double *Y, const Mat8 &K0, double *u, const double *b,
-                     const uint8_t *dmask, int color, bool forward, cudaStream_t st);
+template <typename T>
+void launch2_applyk_fine(const Geom2 &g, const T *Y, const Mat8T<T> &K0, const T *u, T *out, int mode, const T *b,
+                         const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials, cudaStream_t st);
+// The same operator in double-float arithmetic on the FP32 pipe: Y = Yh + Yl, K0 = Kh + Kl,
+// u = uh + ul (pre-split), FP64 result.
+void launch2_applyk_df(const Geom2 &g, const float *Yh, const float *Yl, const Mat8T<float> &Kh,
+                       const Mat8T<float> &Kl, const float *uh, const float *ul, double *out, int mode,
+                       const double *b, const uint8_t *dmask, bool zeroDir, const double *dotv, double *partials,
+                       cudaStream_t st);
+template <typename T>
+void launch2_gs_fine(const Geom2 &g, const T *Y, const Mat8T<T> &K0, T *u, const T *b, const uint8_t *dmask, int color,
+                     bool forward, cudaStream_t st);
 // Element matrices of coarse level l: Ke[E] = sum over the 4^l fine elements f of E of
 // Y0[f] Kc[pos(f)] (Kc: 4^l x 64, the fine K0 carried up through the interpolation);
 // zero for masked coarse elements.
@@ -71,24 +81,35 @@ void launch2_ke_coarse(const Geom2 &gc, const Geom2 &g0, int level, const double
 // 9-point block stencils S[(o * 4 + 2 r + c) * NN + n], o = 3 (di + 1) + (dj + 1), from Ke.
 void launch2_stencil_from_ke(const Geom2 &g, const double *Ke, double *S, cudaStream_t st);
 // Stencil operator, modes as launch2_applyk_fine (detached rows of a stencil are zero).
-void launch2_stencil_apply(const Geom2 &g, const double *S, const double *u, double *out, int mode, const double *b,
-                           const uint8_t *dmask, cudaStream_t st);
-void launch2_gs_stencil(const Geom2 &g, const double *S, double *u, const double *b, const uint8_t *dmask, int color,
-                        bool forward, cudaStream_t st);
-void launch2_restrict(const Geom2 &gf, const Geom2 &gc, const double *fine, double *coarse, cudaStream_t st);
-void launch2_interpolate(const Geom2 &gf, const Geom2 &gc, const double *coarse, double *fine, bool accumulate,
-                         cudaStream_t st);
-void launch2_zero_dirichlet(const Geom2 &g, double *u, const uint8_t *dmask, cudaStream_t st);
-void launch2_enforce_dirichlet(const Geom2 &g, double *u, const uint8_t *dmask, const double *dval, cudaStream_t st);
-void launch2_masked_zero(const Geom2 &g, double *u, int margin, cudaStream_t st);
+template <typename T>
+void launch2_stencil_apply(const Geom2 &g, const T *S, const T *u, T *out, int mode, const T *b, const uint8_t *dmask,
+                           cudaStream_t st);
+template <typename T>
+void launch2_gs_stencil(const Geom2 &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
+                        cudaStream_t st);
+template <typename T>
+void launch2_restrict(const Geom2 &gf, const Geom2 &gc, const T *fine, T *coarse, cudaStream_t st);
+template <typename T>
+void launch2_interpolate(const Geom2 &gf, const Geom2 &gc, const T *coarse, T *fine, bool accumulate, cudaStream_t st);
+template <typename T>
+void launch2_zero_dirichlet(const Geom2 &g, T *u, const uint8_t *dmask, cudaStream_t st);
+template <typename T>
+void launch2_enforce_dirichlet(const Geom2 &g, T *u, const uint8_t *dmask, const double *dval, cudaStream_t st);
+template <typename T>
+void launch2_masked_zero(const Geom2 &g, T *u, int margin, cudaStream_t st);
 void launch2_dense_from_stencil(const Geom2 &g, const double *S, const int *red, double *A, int nfree, cudaStream_t st);
 // x = A^{-1} b on the free DOFs (nfreeDev[0] of them, at most nfreeCap), zero elsewhere
+template <typename T>
 void launch2_coarse_solve(const Geom2 &g, const double *Ainv, const int *freeIdx, const int *nfreeDev, int nfreeCap,
-                          const double *b, double *x, double *scratch, cudaStream_t st);
+                          const T *b, T *x, double *scratch, cudaStream_t st);
 void launch2_dot_partials(const Geom2 &g, const double *a, const double *b, double *partials, cudaStream_t st);
-void launch2_precond_out(const Geom2 &g, const double *src, double *s, const double *r, const uint8_t *dmask,
+// s = src (FP64 or FP32) with Dirichlet components zeroed; partials of r . s (nondetached rows)
+template <typename Ts>
+void launch2_precond_out(const Geom2 &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                          double *partials, cudaStream_t st);
-void launch2_direction(const Geom2 &g, const double *s, double *d, const double *sc, cudaStream_t st);
+// d = beta d + s (beta = sc[2]); with dh, dl also the double-float split of d
+void launch2_direction(const Geom2 &g, const double *s, double *d, const double *sc, cudaStream_t st,
+                       float *dh = nullptr, float *dl = nullptr);
 void launch2_cg_update(const Geom2 &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
                        double *partials, cudaStream_t st);
 // Sensitivity lam^T (wF df/drho - wK dK/drho u) per element (compliance: lam = u, wF = 1, wK = 1/2).
@@ -161,13 +182,19 @@ public:
         DevBuf<uint8_t> dmask;  // levels >= 1 (level 0 uses the simulator's)
         DevBuf<int> dyn;
         DevBuf<double> x, b, r, Ke, S, Kc;
+        DevBuf<float> x32, b32, r32, S32;  // mixed precision: the FP32 V-cycle's vectors and stencils
         double maskH = std::numeric_limits<double>::infinity();
     };
     Grid2 *fine;
     std::vector<Level> lv;
     bool symmetricGS = true, useGraphs = true;
+    int precision = PREC_FP64;  // PREC_MIXED: FP32 V-cycle as the preconditioner of FP64 CG
+    // CG matvec of the mixed solve: MATVEC_DF (default: double-float on the FP32 pipe) or MATVEC_FP64
+    int outerMatvec = MATVEC_DF;
+    void setOuterMatvec(int kind);
     int L() const { return (int)lv.size(); }
     int64_t levelNN(int l) const;
+    void setPrecision(int p);
     const uint8_t *levelMask(int l) const;
 
     void setMaskLayer(int64_t l);
@@ -196,12 +223,44 @@ public:
     void syncFine();
 
 private:
+    template <typename T>
+    struct LB {
+        T *x, *b, *r;
+        const T *S;
+    };
+    template <typename T>
+    LB<T> lb(int l);
+    template <typename T>
+    const T *fineY() const;
+    template <typename T>
+    const Mat8T<T> &fineK0() const;
+    template <typename T>
+    void levelOperatorT(int l, const T *u, T *out, int mode, const T *b);
+    template <typename T>
+    void smoothLevelT(int l, T *u, const T *b, bool forward);
+    template <typename T>
+    void coarseSolveDevT(const T *b, T *x);
+    template <typename T>
+    void vcycleT(int l, int64_t sweeps, bool residualSystem);
+    template <typename T>
+    void fmgDownT(int l, int64_t sweeps, bool residualSystem);
+    template <typename T>
+    void runCyclesT(int64_t steps, int64_t sweeps, bool residualSystem, bool fmg);
+    void refreshSingle();
+    // CG matvec (and the initial residual when b is given): FP64, or double-float in mixed mode.
+    // uSplit: u is the CG direction, whose split the direction kernel already wrote into dh, dl.
+    void outerOperator(const double *u, double *out, int mode, const double *b, bool zeroDir, const double *dotv,
+                       double *partials, bool uSplit);
+    bool dfOuter() const { return precision == PREC_MIXED && outerMatvec == MATVEC_DF; }
+    void refreshDF();  // the split moduli and K0 (outside captured regions)
+    DevBuf<float> Y32, Yh, Yl, dh, dl;
+    Mat8T<float> K0f, K0lo;
+    uint64_t dfVersion = ~0ull;
+
     void ensureStiffness();
     void levelOperator(int l, const double *u, double *out, int mode, const double *b);
     void smoothLevel(int l, double *u, const double *b, bool forward);
     void coarseSolveDev(const double *b, double *x);
-    void vcycle(int l, int64_t sweeps, bool residualSystem);
-    void fmgDown(int l, int64_t sweeps, bool residualSystem);
     void runCycles(int64_t steps, int64_t sweeps, bool residualSystem, bool fmg);
     void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg);
     cudaGraphExec_t loopGraph(double *x, int64_t mgIter, int64_t sweeps, bool fmg);
@@ -239,7 +298,7 @@ private:
 // initial guesses spread over them, warm starts (constant / fd / subspace) as chains of heights.
 class LBL2 {
 public:
-    LBL2(Grid2 *src, int coarsenings, int64_t slots);
+    LBL2(Grid2 *src, int coarsenings, int64_t slots, int precision);
     ~LBL2();
     LBL2(const LBL2 &) = delete;
     LBL2 &operator=(const LBL2 &) = delete;

@@ -34,7 +34,7 @@ struct vfem_mg2 {
 };
 struct vfem_lbl2 {
     LBL2 e;
-    vfem_lbl2(Grid2 *g, int c, int64_t s) : e(g, c, s) {}
+    vfem_lbl2(Grid2 *g, int c, int64_t s, int p) : e(g, c, s, p) {}
 };
 
 namespace {
@@ -374,10 +374,10 @@ int vfem_kernel_launch_count(uint64_t *count) {
     return guarded([&] { *count = launchCounter(); });
 }
 
-int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, vfem_lbl2 **out) {
+int vfem_lbl2_create(vfem_grid2 *g, int64_t coarsenings, int64_t slots, int precision, vfem_lbl2 **out) {
     return guarded([&] {
         need(g, "grid"); need(out, "out");
-        *out = new vfem_lbl2(&g->g, (int)coarsenings, slots);
+        *out = new vfem_lbl2(&g->g, (int)coarsenings, slots, precision);
     });
 }
 int vfem_lbl2_destroy(vfem_lbl2 *e) {
@@ -825,6 +825,12 @@ int vfem_mg2_level_dirichlet_mask(const vfem_mg2 *mg, int level, uint8_t *mask_o
         const std::vector<uint8_t> &m = level == 0 ? mg->m.fine->hmask : mg->m.lv[level].hmask;
         VFEM_CUDA(cudaMemcpy(mask_out, m.data(), m.size(), cudaMemcpyDefault));
     });
+}
+int vfem_mg2_set_precision(vfem_mg2 *mg, int precision) {
+    return guarded([&] { need(mg, "mg"); mg->m.setPrecision(precision); });
+}
+int vfem_mg2_set_outer_matvec(vfem_mg2 *mg, int kind) {
+    return guarded([&] { need(mg, "mg"); mg->m.setOuterMatvec(kind); });
 }
 int vfem_mg2_set_use_graphs(vfem_mg2 *mg, int use) {
     return guarded([&] { need(mg, "mg"); mg->m.useGraphs = use != 0; });

@@ -1416,7 +1416,7 @@ class LayerByLayerEvaluator:
             self._release()
             h = C.c_void_p()
             if self.sim._nc == 2:
-                check(_lib().vfem_lbl2_create(self.sim._h, coarsenings, slots, C.byref(h)))
+                check(_lib().vfem_lbl2_create(self.sim._h, coarsenings, slots, precision, C.byref(h)))
             else:
                 check(_lib().vfem_lbl_create(self.sim._h, coarsenings, slots, precision, C.byref(h)))
             self._h, self._key = h, key
@@ -1925,6 +1925,7 @@ class MultigridSolver2D:
         check(_lib().vfem_mg2_num_levels(h, C.byref(n)))
         self.numLevels = n.value
         self.lastStats = None
+        self._prec = "fp64"
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -1943,9 +1944,14 @@ class MultigridSolver2D:
         return _LevelSimulator2D(self, l)
 
     def setPrecision(self, precision="fp64", outerMatvec="df"):
-        """The 2D solver runs in FP64 only."""
-        if precision != "fp64":
-            raise RuntimeError("the 2D multigrid solver supports precision 'fp64' only")
+        """'fp64' (the reference's method) or 'mixed': the PCG preconditioner's V-cycle in FP32
+        inside FP64 CG, whose matvec is 'df' (default: double-float on the FP32 units, FP64-class
+        accuracy) or 'fp64'."""
+        p = {"fp64": 0, "mixed": 1}[precision]
+        m = {"fp64": 0, "df": 1}[outerMatvec]
+        check(_lib().vfem_mg2_set_precision(self._h, p))
+        check(_lib().vfem_mg2_set_outer_matvec(self._h, m))
+        self._prec = precision
 
     def setUseGraphs(self, use):
         check(_lib().vfem_mg2_set_use_graphs(self._h, int(bool(use))))
