@@ -319,3 +319,75 @@ def test_lbl_and_problem_mixed_2d(gpu):
     otop.setVars(x0)
     assert rel(top.evaluateObjective(), otop.evaluateObjective()) < 1e-8
     assert rel(top.evaluateObjectiveGradient(), otop.evaluateObjectiveGradient()) < 1e-7
+
+
+def test_helpers_2d(gpu):
+    tps, sim, rng = make_pair(ne=(8, 6), seed=16)
+    u = rng.standard_normal((sim.NN, 2))
+    K = tps.getK()
+    Ku = (K @ u.reshape(-1)).reshape(-1, 2)
+    assert rel(soa(Ku), sim.applyK(soa(u))) < 1e-13
+    # bilinear sampling reproduces nodal values at nodes and linear fields everywhere
+    P = np.array([tps.nodePosition(n) for n in (0, 7, sim.NN - 1)])
+    np.testing.assert_allclose(tps.sampleNodalField(u, P), u[[0, 7, sim.NN - 1]], atol=1e-14)
+    V, F = tps.getMesh()
+    lin = V[:, 0] * 0.7 - V[:, 1] * 0.2
+    q = rng.uniform([0, 0], [2, 1], (5, 2))
+    np.testing.assert_allclose(tps.sampleNodalField(lin[:, None], q)[:, 0], q[:, 0] * 0.7 - q[:, 1] * 0.2, atol=1e-14)
+    # downsampling: densities averaged 2 x 2, gradients spread back
+    c = tps.downsample(1)
+    np.testing.assert_array_equal(c.NbElementsPerDimension, (4, 3))
+    rho = rng.uniform(0, 1, sim.NE)
+    tps.downsampleDensityFieldTo(rho, c)
+    np.testing.assert_allclose(c.getDensities(), rho.reshape(4, 2, 3, 2).mean(axis=(1, 3)).ravel(), atol=1e-15)
+    gc = rng.standard_normal(c.numElements())
+    gf = tps.upsampleDensityGradientFrom(c, gc)
+    assert abs(gf.sum() - gc.sum()) < 1e-12
+    # symmetry conditions pin the normal component on the chosen face
+    s2 = pv.TensorProductSimulator([1, 1], [[0, 0], [2, 1]], [8, 6])
+    s2.applySymmetryConditions([1, 0], [False, False])
+    m = s2.getDirichletMask()
+    x0 = np.arange(s2.numNodes()) < 7
+    assert m[x0, 0].all() and not m[x0, 1].any() and not m[~x0].any()
+
+
+def test_intermediate_shape_2d(gpu):
+    tps, sim = lbl_pair(ne=(16, 8), seed=17)
+    rho = tps.getDensities()
+    it = tps.getIntermediateFabricationShape(0.5)
+    np.testing.assert_array_equal(it.NbElementsPerDimension, (16, 4))
+    np.testing.assert_allclose(it.getDensities(), rho.reshape(16, 8)[:, :4].ravel())
+    assert it.getDirichletMask()[np.arange(it.numNodes()) % 5 == 0].all()
+    # its compliance equals the masked full grid's at the same height
+    mgi = it.multigridSolver(1)
+    fi = it.buildLoadVector()
+    ui = mgi.preconditionedConjugateGradient(np.zeros_like(fi), fi, 200, 1e-12, None, 1, 2, False)
+    mg = tps.multigridSolver(1)
+    mg.setFabricationMaskHeightByLayer(4)
+    f = tps.buildLoadVector()
+    u = mg.preconditionedConjugateGradient(np.zeros_like(f), f, 200, 1e-12, None, 1, 2, False)
+    live = (np.arange(tps.numNodes()) % 9) <= 4
+    assert abs(np.sum(fi * ui) - np.sum((f * u)[live])) < 1e-9 * abs(np.sum(fi * ui))
+
+
+def test_autograd_compliance_2d(gpu):
+    torch = pytest.importorskip("torch")
+    from voxelfem_gb300 import autograd as vag
+    tps, sim, rng = make_pair(ne=(8, 4), seed=18)
+    tps.gravity = [0.0, -0.4]
+    rho0 = rng.uniform(0.3, 1.0, sim.NE)
+    mg = tps.multigridSolver(1)
+    solver = vag.SolverContext(tps, mg, cgIter=400, tol=1e-13)
+    rho = torch.tensor(rho0, dtype=torch.float64, requires_grad=True)
+    C = vag.compliance(rho, solver)
+    C.backward()
+    g = rho.grad.numpy()
+
+    def comp(r):
+        return float(vag.compliance(torch.tensor(r, dtype=torch.float64), solver))
+
+    for e in (0, 13, 31):
+        d = np.zeros_like(rho0)
+        d[e] = 1e-6
+        fd = (comp(rho0 + d) - comp(rho0 - d)) / 2e-6
+        assert abs(fd - g[e]) < 1e-5 * max(abs(g[e]), 1e-3)

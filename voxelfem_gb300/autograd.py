@@ -90,7 +90,7 @@ class LoadVector(torch.autograd.Function):
     def backward(ctx, grad_f):
         solver = ctx.solver
         solver.set_densities(ctx.rho)
-        g = _np(grad_f).reshape(-1, 3)
+        g = _np(grad_f).reshape(-1, getattr(solver.sim, "_nc", 3))
         zero = np.zeros_like(g)
         grad = solver.sim.adjointSensitivity(g, zero, 1.0, 0.0)
         return torch.from_numpy(grad).to(grad_f.device), None
