@@ -458,12 +458,15 @@ def run_ours(args):
 
 
 LBL_NE = (128, 128, 128)
-LBL_COARSENINGS = 4
+# 5 coarsenings (coarsest 4^3 elements): every height rebuilds the hierarchy, whose FP64 dense
+# inverse of the coarsest level costs 7.0 ms at 4 coarsenings (8^3, ~1,944 free DOFs) and 1.2 ms
+# here; the PCG iteration counts are identical (1456 / 1477 / 1776 for N=3 x 1, N=3 x 8, zero).
+LBL_COARSENINGS = 5
 
 
 def run_lbl(slots_list=(1, 8, 16)):
     """Layer-by-layer workload: 128^3 Q1, rho U[0.1, 1] seed 0, base fixed, gravity (0, -1, 0),
-    heights 1..128 each solved from a zero guess (mixed precision, tol 1e-8, 2+2 sweeps, 4
+    heights 1..128 each solved from a zero guess (mixed precision, tol 1e-8, 2+2 sweeps, 5
     coarsenings). Wall time of the 128 solves one height at a time (1 slot) and spread over
     concurrent solver slots; each evaluator warmed up once (graph capture) before its timed run."""
     import torch
@@ -477,7 +480,7 @@ def run_lbl(slots_list=(1, 8, 16)):
     mg = sim.multigridSolver(LBL_COARSENINGS)
     mg.setPrecision("mixed")
     out = {"workload": "layer-by-layer 128^3 Q1, rho U[0.1,1] seed 0, base fixed, gravity -y, heights 1..128, "
-                       "zero initial guesses, mixed precision, tol 1e-8, 2+2 sweeps, 4 coarsenings",
+                       "zero initial guesses, mixed precision, tol 1e-8, 2+2 sweeps, 5 coarsenings",
            "heights": ne[1]}
     ref = None
     for slots in slots_list:
