@@ -77,3 +77,29 @@ def test_intermediate_shape_matches_masked_solve(gpu):
     acc = np.zeros(sim.numElements())
     sim.accumElementScalarFieldFromIntermediateFabricationShape(part, np.ones(part.numElements()), acc)
     assert acc.sum() == part.numElements()
+
+
+def test_reference_script_idioms(gpu):
+    """The idioms of the reference's Python drivers: ETensor as an object with setIsotropic, and a
+    problem subclass obtained through getClassName (python/LayerByLayerOptimization.py:55-93)."""
+    import numpy as np
+    from voxelfem_gb300 import pyVoxelFEM
+    tps = pyVoxelFEM.TensorProductSimulator([1, 1], [[0, 0], [2, 1]], [16, 8])
+    e = tps.ETensor
+    e.setIsotropic(1, 0.3)
+    tps.ETensor = e
+    assert tps.ETensor == (1.0, 0.3)
+    tps.addDirichletCondition([0, 0], [0, 0], [0, 1], "xy")
+    f = np.zeros((tps.numNodes(), 2))
+    f[16 * 9, 1] = -1.0
+    tps.setNodalForces(f)
+    base = eval(pyVoxelFEM.getClassName(tps, "TopologyOptimizationProblem"))
+
+    class Weighted(base):
+        def evaluateObjective(self):
+            return 2.0 * super().evaluateObjective()
+
+    obj = pyVoxelFEM.MultigridComplianceObjective(tps.multigridSolver(2))
+    top = Weighted(tps, obj, [pyVoxelFEM.TotalVolumeConstraint(0.5)], [pyVoxelFEM.ProjectionFilter(1.0)])
+    top.setVars(np.full(top.numVars(), 0.5))
+    assert abs(top.evaluateObjective() - 2.0 * base.evaluateObjective(top)) < 1e-15 * abs(top.evaluateObjective())

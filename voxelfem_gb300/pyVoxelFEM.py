@@ -76,6 +76,37 @@ def _arr3(v):
     return a
 
 
+class ElasticityTensor:
+    """The isotropic elasticity tensor held by a simulator's ``ETensor`` property: it unpacks and
+    compares as the pair (young, poisson), and ``setIsotropic(E, nu)`` is the method the
+    reference's scripts call on MeshFEM's tensor (``e = tps.ETensor; e.setIsotropic(1, nu);
+    tps.ETensor = e``)."""
+
+    def __init__(self, young=1.0, poisson=0.0):
+        self.young, self.poisson = float(young), float(poisson)
+
+    def setIsotropic(self, young, poisson):
+        self.young, self.poisson = float(young), float(poisson)
+
+    def __iter__(self):
+        return iter((self.young, self.poisson))
+
+    def __getitem__(self, i):
+        return (self.young, self.poisson)[i]
+
+    def __len__(self):
+        return 2
+
+    def __eq__(self, other):
+        try:
+            return tuple(self) == tuple(other)
+        except TypeError:
+            return NotImplemented
+
+    def __repr__(self):
+        return "ElasticityTensor(young=%g, poisson=%g)" % (self.young, self.poisson)
+
+
 def TensorProductSimulator(degreesPerDimension, domainBBox, elementsPerDimension, numberType=NumberType.DOUBLE):
     """Factory of pyVoxelFEM.TensorProductSimulator (VoxelFEM.cc:423-430)."""
     degs = [int(d) for d in degreesPerDimension]
@@ -177,7 +208,7 @@ class TensorProductSimulator_3D:
     def ETensor(self):
         E, nu = C.c_double(), C.c_double()
         check(_lib().vfem_grid_get_etensor(self._h, C.byref(E), C.byref(nu)))
-        return (E.value, nu.value)
+        return ElasticityTensor(E.value, nu.value)
 
     @ETensor.setter
     def ETensor(self, value):
@@ -1261,7 +1292,7 @@ class TensorProductSimulator_3D_Q2:
 
     @property
     def ETensor(self):
-        return self._E
+        return ElasticityTensor(*self._E)
 
     @ETensor.setter
     def ETensor(self, value):
@@ -1573,7 +1604,7 @@ class TensorProductSimulator_2D:
     def ETensor(self):
         E, nu = C.c_double(), C.c_double()
         check(_lib().vfem_grid2_get_etensor(self._h, C.byref(E), C.byref(nu)))
-        return (E.value, nu.value)
+        return ElasticityTensor(E.value, nu.value)
 
     @ETensor.setter
     def ETensor(self, value):
@@ -2050,3 +2081,28 @@ class MultigridSolver2D:
         ms = C.c_double()
         check(_lib().vfem_mg2_time_kernel(self._h, int(kernel), int(reps), C.byref(ms)))
         return ms.value
+
+
+def getClassName(simulator, name):
+    """pyVoxelFEM.getClassName (VoxelFEM.cc:250-254): the name under which the class `name` for
+    this simulator's instantiation is reachable, for scripts that subclass it via eval."""
+    if not hasattr(detail, name):
+        raise RuntimeError("Unknown class " + name)
+    return "pyVoxelFEM.detail." + name
+
+
+class _Detail:
+    """The module's ``detail`` namespace (VoxelFEM.cc:405): the instantiated classes by name."""
+
+    TopologyOptimizationProblem = TopologyOptimizationProblem
+    MultigridComplianceObjective = MultigridComplianceObjective
+    OCOptimizer = OCOptimizer
+    LayerByLayerEvaluator = LayerByLayerEvaluator
+    MultigridSolver = MultigridSolver
+    MultigridSolver2D = MultigridSolver2D
+    TensorProductSimulator_2D = TensorProductSimulator_2D
+    TensorProductSimulator_3D = TensorProductSimulator_3D
+    TensorProductSimulator_3D_Q2 = TensorProductSimulator_3D_Q2
+
+
+detail = _Detail
