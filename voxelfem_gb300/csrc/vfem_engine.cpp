@@ -456,6 +456,8 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
 MG::~MG() {
     clearGraphs();
     if (hostSc) cudaFreeHost(hostSc);
+    if (copyDone) cudaEventDestroy(copyDone);
+    if (copyStream) cudaStreamDestroy(copyStream);
 }
 
 void MG::clearGraphs() {
@@ -1192,16 +1194,32 @@ PcgStats MG::pcgDevice(double *x, const double *b, int64_t maxIter, double tol, 
 PcgStats MG::pcg(double *x, const double *b, int64_t maxIter, double tol, int64_t mgIter, int64_t sweeps, bool fmg,
                  bool dirichletSatisfied, PcgCallback cb, void *user) {
     cudaStream_t st = fine->stream;
-    const size_t bytes = 3 * fine->g.NN * sizeof(double);
-    View vb;
-    viewIn(vb, b, bytes, st);
+    const int64_t n3 = 3 * fine->g.NN;
+    const size_t bytes = n3 * sizeof(double);
     // iterate in an internal buffer so that captured graphs stay valid across calls
-    xbuf.alloc(3 * fine->g.NN);
-    DevBuf<double> &xb = xbuf;
-    VFEM_CUDA(cudaMemcpyAsync(xb.p, x, bytes, cudaMemcpyDefault, st));
-    PcgStats stats = pcgDevice(xb.p, (const double *)vb.d, maxIter, tol, mgIter, sweeps, fmg, dirichletSatisfied, cb,
-                               user);
-    VFEM_CUDA(cudaMemcpyAsync(x, xb.p, bytes, cudaMemcpyDefault, st));
+    xbuf.alloc(n3);
+    const bool bHost = !isDevicePtr(b);
+    if (bHost) bbuf.alloc(n3);
+    const double *bd = bHost ? bbuf.p : b;
+    syncFineGeom(*this);
+    if (mgIter > 0 && L() > 1) {
+        // the uploads run on a side stream while the Galerkin rebuild (which needs only the
+        // densities) runs on the solver stream; the solve waits for both
+        if (!copyStream) {
+            VFEM_CUDA(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
+            VFEM_CUDA(cudaEventCreateWithFlags(&copyDone, cudaEventDisableTiming));
+        }
+        VFEM_CUDA(cudaMemcpyAsync(xbuf.p, x, bytes, cudaMemcpyDefault, copyStream));
+        if (bHost) VFEM_CUDA(cudaMemcpyAsync(bbuf.p, b, bytes, cudaMemcpyHostToDevice, copyStream));
+        VFEM_CUDA(cudaEventRecord(copyDone, copyStream));
+        ensureStiffness(true);
+        VFEM_CUDA(cudaStreamWaitEvent(st, copyDone, 0));
+    } else {
+        VFEM_CUDA(cudaMemcpyAsync(xbuf.p, x, bytes, cudaMemcpyDefault, st));
+        if (bHost) VFEM_CUDA(cudaMemcpyAsync(bbuf.p, b, bytes, cudaMemcpyHostToDevice, st));
+    }
+    PcgStats stats = pcgDevice(xbuf.p, bd, maxIter, tol, mgIter, sweeps, fmg, dirichletSatisfied, cb, user);
+    VFEM_CUDA(cudaMemcpyAsync(x, xbuf.p, bytes, cudaMemcpyDefault, st));
     VFEM_CUDA(cudaStreamSynchronize(st));
     return stats;
 }

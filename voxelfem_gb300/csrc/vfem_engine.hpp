@@ -210,7 +210,10 @@ public:
     uint64_t stiffnessDensVersion = 0, stiffnessMaskVersion = 0, stiffnessBcVersion = 0;
 
     // CG workspace
-    DevBuf<double> rbuf, s, dvec, Ad, partials, sc, xbuf;
+    DevBuf<double> rbuf, s, dvec, Ad, partials, sc, xbuf, bbuf;
+    // side stream of the host-buffer solve: its uploads overlap the Galerkin rebuild
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t copyDone = nullptr;
     DevBuf<float> dhi, dlo;  // double-float split of the search direction
     DevBuf<double> umax;     // partial maxima of |operand| of the tensor-core matvec
     // kind of the mixed outer matvec in use: 0 FP64, 1 double-float (FP32 units), 2 tensor cores
