@@ -105,7 +105,7 @@ def test_c3_topology_optimisation_full_size(gpu, oracle):
             fs = sim.buildLoadVector()
             us = mg64.preconditionedConjugateGradient(ub, fs, 500, 1e-13, None, 1, 2, False)
             vals.append(0.5 * float(np.sum(fs * us)))
-        solver._rho = None  # the FD solves changed the simulator's densities
+        solver.invalidate()  # the FD solves changed the simulator's densities
         fd = (vals[0] - vals[1]) / (2 * h)
         gv = float(np.dot(g, v))
         print("oracle rel %.2e, directional FD rel %.2e" % (float(np.max(np.abs(g - gref)) / np.max(np.abs(gref))),
