@@ -337,16 +337,29 @@ def run_ours(args):
     b_p = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
     x_p = torch.zeros(3, nn, dtype=torch.float64).pin_memory()
 
+    e2e_parts = {"zero_x0": 0.0, "set_densities": 0.0, "pcg_call": 0.0, "compliance_dot": 0.0}
+
     def step_host():
+        t = [time.perf_counter()]
         x_p.zero_()
+        t.append(time.perf_counter())
         _capi.check(lib.vfem_grid_set_densities(sim._h, C.c_void_p(rho_p.data_ptr())))
+        t.append(time.perf_counter())
         _capi.check(lib.vfem_mg_pcg(mg._h, C.c_void_p(x_p.data_ptr()), C.c_void_p(b_p.data_ptr()), 500, TOL, 1, 2,
                                     0, 0, cb, None, C.byref(stats)))
-        return 0.5 * float(np.dot(b_p.numpy().ravel(), x_p.numpy().ravel()))
+        t.append(time.perf_counter())
+        c = 0.5 * float(np.dot(b_p.numpy().ravel(), x_p.numpy().ravel()))
+        t.append(time.perf_counter())
+        for key, a, b in zip(e2e_parts, t, t[1:]):
+            e2e_parts[key] += b - a
+        return c
 
     step_host()
+    for key in e2e_parts:
+        e2e_parts[key] = 0.0
     _, e2e_wall, _ = timed(step_host, args.steps)
     e2e = e2e_wall / args.steps
+    e2e_parts_ms = {k: v / args.steps * 1e3 for k, v in e2e_parts.items()}
     h2d = rho.nbytes + 2 * 3 * nn * 8  # densities, b, x0
     d2h = 3 * nn * 8
 
@@ -425,7 +438,8 @@ def run_ours(args):
                                       "tensor-core (integer-slice bf16)" if outer_kind == "tensor"
                                       else "double-float"),
                        "l2": "no flush: working set of every step (> 2 GB) exceeds the 129 MB L2"},
-            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "parts_ms": e2e_parts_ms},
             "roofline": roofline,
             "rooflines": rooflines,
             "clocks": clk,

@@ -74,60 +74,65 @@ __device__ __forceinline__ double rsqrt_newton(double d) {
     return y;
 }
 
-// One block of 32x32 threads: factor tile (k, k) in shared memory, write L_kk (lower) back
-// to A and L_kk^{-1} (lower) to Dinv[k]. FP64 issue rate is a few operations per clock per
-// SM, so each pivot reciprocal is formed once, by the thread that owns the pivot, as soon
-// as its last update lands; one barrier per pivot step.
-__device__ __forceinline__ void chol_pivot(int j, double d, int nb, double *rinv, double *rr, double *piv,
-                                           int *status) {
+// 1/d: single-precision seed refined by two Newton-Raphson steps for the reciprocal,
+// y <- y + y (1 - d y), each doubling the number of correct bits (24 -> 48 -> full).
+// Pivots outside the single-precision normal range take the plain quotient.
+__device__ __forceinline__ double recip_newton(double d) {
+    if (!(d > 1e-30 && d < 1e30)) return 1.0 / d;
+    double y = (double)__frcp_rn((float)d);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) y = fma(y, fma(-d, y, 1.0), y);
+    return y;
+}
+
+__device__ __forceinline__ void ldl_pivot(int j, double d, int nb, double *rd, double *dv, int *status) {
     if (!(d > 0.0)) {
         if (j < nb) atomicExch(status, 1);
         d = 1.0;
     }
-    const double r = rsqrt_newton(d);
-    rinv[j] = r;
-    rr[j] = r * r;
-    piv[j] = d * r;
+    dv[j] = d;
+    rd[j] = recip_newton(d);
 }
 
+// One block of 32x32 threads factors tile (k, k) in shared memory as U D U^T (U unit lower)
+// and inverts U in the same sweep: W = U^{-1} follows from the elimination's row operations
+// W_y -= U_yj W_j, which in step j touch the columns <= j of the rows below j while the
+// rank-one update a_yx -= U_yj a_xj touches the columns > j, so one barrier per pivot serves
+// both and a thread updates either an entry of the trailing triangle or one of W with the same
+// two instructions. FP64 operations issue at about two per clock per SM here and a dependent
+// one waits tens of cycles, so the only chain between steps is the next pivot's reciprocal,
+// formed by its owner thread as soon as its last update lands. Written back: the Cholesky factor
+// L = U D^{1/2} (lower tile of A) and L^{-1} = D^{-1/2} W (Dinv[k]).
 __global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *status) {
-    __shared__ double sa[TB][TB + 1], sL[TB][TB + 1];
-    __shared__ double rinv[TB], rr[TB], piv[TB];
+    VFEM_PDL_ENTRY();
+    __shared__ double sa[TB][TB + 1], sw[TB][TB + 1];
+    __shared__ double rd[TB], dv[TB], rs[TB];
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int kb = k * TB;
     const int nb = min(TB, n - kb);
     load_tile(A, n, kb, kb, sa);
     if (!(ty < nb && tx < nb)) sa[ty][tx] = (ty == tx) ? 1.0 : 0.0;
-    sL[ty][tx] = 0.0;
+    sw[ty][tx] = (ty == tx) ? 1.0 : 0.0;
     __syncthreads();
-    if (ty == 0 && tx == 0) chol_pivot(0, sa[0][0], nb, rinv, rr, piv, status);
+    if (ty == 0 && tx == 0) ldl_pivot(0, sa[0][0], nb, rd, dv, status);
     __syncthreads();
-    // step j: column j of L, and the rank-one update of the trailing lower triangle made
-    // from the unscaled column (a_yx -= a_yj a_xj / a_jj), so column j is only read
     for (int j = 0; j < TB; ++j) {
-        if (tx == j && ty >= j) {
-            sL[ty][j] = (ty == j) ? piv[j] : sa[ty][j] * rinv[j];
-        } else if (tx > j && ty >= tx) {
-            const double v = fma(-sa[ty][j] * rr[j], sa[tx][j], sa[ty][tx]);
-            sa[ty][tx] = v;
-            if (ty == j + 1 && tx == j + 1) chol_pivot(j + 1, v, nb, rinv, rr, piv, status);
+        if (ty > j && tx <= ty) {
+            const bool trailing = tx > j;
+            const double m = sa[ty][j] * rd[j];  // U_yj; column j is final after step j - 1
+            double *t = trailing ? &sa[ty][tx] : &sw[ty][tx];
+            const double o = trailing ? sa[tx][j] : sw[j][tx];  // row j of W is final too
+            const double v = fma(-m, o, *t);
+            *t = v;
+            if (tx == j + 1 && ty == j + 1) ldl_pivot(j + 1, v, nb, rd, dv, status);
         }
         __syncthreads();
     }
-    // L Z = I: with W_r = L_rr Z_r, W = I - (strictly lower sweep) W_y -= (L_yr / L_rr) W_r;
-    // row r of W is final after step r - 1 and only read in step r
-    double w = (ty == tx) ? 1.0 : 0.0;
-    sa[ty][tx] = w;
+    if (ty == 0) rs[tx] = rsqrt_newton(dv[tx]);
     __syncthreads();
-    for (int r = 0; r + 1 < TB; ++r) {
-        if (ty > r && tx <= r) {
-            w = fma(-sL[ty][r] * rinv[r], sa[r][tx], w);
-            sa[ty][tx] = w;
-        }
-        __syncthreads();
-    }
-    if (ty < nb && tx < nb) A[(int64_t)(kb + ty) * n + kb + tx] = (tx <= ty) ? sL[ty][tx] : 0.0;
-    Dinv[(int64_t)k * TB * TB + ty * TB + tx] = (tx <= ty) ? w * rinv[ty] : 0.0;
+    if (ty < nb && tx < nb)
+        A[(int64_t)(kb + ty) * n + kb + tx] = (tx < ty) ? sa[ty][tx] * rs[tx] : (tx == ty) ? dv[ty] * rs[ty] : 0.0;
+    Dinv[(int64_t)k * TB * TB + ty * TB + tx] = (tx <= ty) ? sw[ty][tx] * rs[ty] : 0.0;
 }
 
 // 32-term dot product of rows of two shared tiles, four independent chains
@@ -145,6 +150,7 @@ __device__ __forceinline__ double tile_dot(const double *a, int sa, const double
 
 // tiles (i, k), i > k: L_ik = A_ik L_kk^{-T}
 __global__ void chol_trsm_kernel(double *A, const double *Dinv, int n, int k) {
+    VFEM_PDL_ENTRY();
     __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int kb = k * TB, r0 = kb + TB * (1 + blockIdx.x);
@@ -164,6 +170,7 @@ __device__ __forceinline__ void lower_tile_of(int idx, int &ii, int &jj) {
 
 // trailing tiles (i, j), k < j <= i: A_ij -= L_ik L_jk^T
 __global__ void chol_syrk_kernel(double *A, int n, int k) {
+    VFEM_PDL_ENTRY();
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
     int ii, jj;
     lower_tile_of(blockIdx.x, ii, jj);
@@ -181,6 +188,7 @@ __global__ void chol_syrk_kernel(double *A, int n, int k) {
 // Z = L^{-1}, right-looking over block rows. Step k: Z[k][c] = L_kk^{-1} Z[k][c] (c <= k),
 // then Z[i][c] -= L[i][k] Z[k][c] for i > k.
 __global__ void trinv_diag_kernel(const double *Dinv, double *Z, int n, int k) {
+    VFEM_PDL_ENTRY();
     __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
     const int c = blockIdx.x;
     const int ty = threadIdx.y, tx = threadIdx.x;
@@ -193,6 +201,7 @@ __global__ void trinv_diag_kernel(const double *Dinv, double *Z, int n, int k) {
 }
 
 __global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
+    VFEM_PDL_ENTRY();
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
     const int c = blockIdx.x % (k + 1);
     const int i = k + 1 + blockIdx.x / (k + 1);
@@ -206,6 +215,7 @@ __global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
 }
 
 __global__ void identity_kernel(double *Z, int n) {
+    VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= (int64_t)n * n) return;
     Z[t] = (t / n == t % n) ? 1.0 : 0.0;
@@ -213,6 +223,7 @@ __global__ void identity_kernel(double *Z, int n) {
 
 // Ainv = Z^T Z (lower tiles computed, mirrored). Z is lower triangular.
 __global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
+    VFEM_PDL_ENTRY();
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
     // map blockIdx.x to lower tile (bi, bj), bj <= bi
     int idx = blockIdx.x, bi = 0;
@@ -238,6 +249,7 @@ __global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
 }
 
 __global__ void zero_upper_kernel(double *A, int n) {
+    VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= (int64_t)n * n) return;
     const int i = (int)(t / n), j = (int)(t % n);
@@ -470,36 +482,36 @@ void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t
     const int nbt = (n + TB - 1) / TB;
     double *Dinv = work + (size_t)n * n;
     for (int k = 0; k < nbt; ++k) {
-        chol_diag_kernel<<<1, tb, 0, st>>>(A, Dinv, n, k, status);
+        launch_pdl(chol_diag_kernel, 1, tb, 0, st, A, Dinv, n, k, status);
         VFEM_LAUNCH_CHECK();
         if (mark) mark("coarsest:chol diag tiles");
         const int m = nbt - k - 1;
         if (m > 0) {
-            chol_trsm_kernel<<<m, tb, 0, st>>>(A, Dinv, n, k);
+            launch_pdl(chol_trsm_kernel, m, tb, 0, st, A, (const double *)Dinv, n, k);
             VFEM_LAUNCH_CHECK();
             if (mark) mark("coarsest:chol panel solves");
-            chol_syrk_kernel<<<m * (m + 1) / 2, tb, 0, st>>>(A, n, k);
+            launch_pdl(chol_syrk_kernel, m * (m + 1) / 2, tb, 0, st, A, n, k);
             VFEM_LAUNCH_CHECK();
             if (mark) mark("coarsest:chol trailing updates");
         }
     }
-    zero_upper_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(A, n);
+    launch_pdl(zero_upper_kernel, gridFor((int64_t)n * n, BS), BS, 0, st, A, n);
     VFEM_LAUNCH_CHECK();
-    identity_kernel<<<gridFor((int64_t)n * n, BS), BS, 0, st>>>(work, n);
+    launch_pdl(identity_kernel, gridFor((int64_t)n * n, BS), BS, 0, st, work, n);
     VFEM_LAUNCH_CHECK();
     if (mark) mark("coarsest:inverse init");
     for (int k = 0; k < nbt; ++k) {
-        trinv_diag_kernel<<<k + 1, tb, 0, st>>>(Dinv, work, n, k);
+        launch_pdl(trinv_diag_kernel, k + 1, tb, 0, st, (const double *)Dinv, work, n, k);
         VFEM_LAUNCH_CHECK();
         if (mark) mark("coarsest:trinv diag solves");
         const int m = nbt - k - 1;
         if (m > 0) {
-            trinv_update_kernel<<<m * (k + 1), tb, 0, st>>>(A, work, n, k);
+            launch_pdl(trinv_update_kernel, m * (k + 1), tb, 0, st, (const double *)A, work, n, k);
             VFEM_LAUNCH_CHECK();
             if (mark) mark("coarsest:trinv updates");
         }
     }
-    ztz_kernel<<<nbt * (nbt + 1) / 2, tb, 0, st>>>(work, A, n, nbt);
+    launch_pdl(ztz_kernel, nbt * (nbt + 1) / 2, tb, 0, st, (const double *)work, A, n, nbt);
     VFEM_LAUNCH_CHECK();
     if (mark) mark("coarsest:Z^T Z");
 }
