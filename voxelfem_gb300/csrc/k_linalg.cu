@@ -11,7 +11,7 @@ namespace vfem {
 namespace {
 
 constexpr int BS = 256;
-constexpr int TB = 32;  // dense tile size
+constexpr int TB = DENSE_TILE;
 
 // ---------------- dense assembly ----------------
 template <typename T>
@@ -50,9 +50,9 @@ __global__ void symmetrize_kernel(double *A, int n) {
 // ---------------- blocked right-looking Cholesky (lower, in place, row-major) ----------------
 // Step k: factor the diagonal tile and invert it (tile factor L_kk and its inverse), then
 // the tiles below it are X = A_ik L_kk^{-T} and every trailing lower tile is updated with
-// one 32x32x32 product per block. Dependent FP64 operations cost tens of cycles and a
+// one TB x TB x TB product per block. Dependent FP64 operations cost tens of cycles and a
 // division or square root hundreds on this part, so the only sequential chains are the
-// 32 pivot steps of each diagonal tile; panel solves and the triangular inverse become
+// TB pivot steps of each diagonal tile; panel solves and the triangular inverse become
 // plain tile products against the inverted diagonal tiles.
 __device__ __forceinline__ void load_tile(const double *A, int n, int r0, int c0, double (*t)[TB + 1]) {
     const int ty = threadIdx.y, tx = threadIdx.x;
@@ -94,7 +94,7 @@ __device__ __forceinline__ void ldl_pivot(int j, double d, int nb, double *rd, d
     rd[j] = recip_newton(d);
 }
 
-// One block of 32x32 threads factors tile (k, k) in shared memory as U D U^T (U unit lower)
+// One block of TB x TB threads factors tile (k, k) in shared memory as U D U^T (U unit lower)
 // and inverts U in the same sweep: W = U^{-1} follows from the elimination's row operations
 // W_y -= U_yj W_j, which in step j touch the columns <= j of the rows below j while the
 // rank-one update a_yx -= U_yj a_xj touches the columns > j, so one barrier per pivot serves
@@ -135,7 +135,7 @@ __global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *sta
     Dinv[(int64_t)k * TB * TB + ty * TB + tx] = (tx <= ty) ? sw[ty][tx] * rs[ty] : 0.0;
 }
 
-// 32-term dot product of rows of two shared tiles, four independent chains
+// TB-term dot product of rows of two shared tiles, four independent chains
 __device__ __forceinline__ double tile_dot(const double *a, int sa, const double *b, int sb) {
     double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
 #pragma unroll

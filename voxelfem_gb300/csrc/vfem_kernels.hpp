@@ -172,7 +172,12 @@ void launch_symmetrize(double *A, int n, cudaStream_t st);
 // In place: A (n x n, row-major) -> A^{-1} via blocked Cholesky; status[0] set nonzero if not SPD.
 // work holds dense_inverse_work_size(n) doubles.
 // mark(name), when given, is called after each phase has been enqueued (profiling).
-inline size_t dense_inverse_work_size(int n) { return (size_t)n * n + (size_t)32 * 32 * ((n + 31) / 32); }
+// Tile edge of the blocked factorisation: the sequential chain is one diagonal tile per step,
+// so small tiles shorten it; the FP64 work of the whole inverse does not depend on the tile.
+constexpr int DENSE_TILE = 16;
+inline size_t dense_inverse_work_size(int n) {
+    return (size_t)n * n + (size_t)DENSE_TILE * DENSE_TILE * ((n + DENSE_TILE - 1) / DENSE_TILE);
+}
 void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
                        const std::function<void(const std::string &)> &mark = nullptr);
 // x = A^{-1} b on the free DOFs (nfreeDev[0] of them, at most nfreeCap), zero elsewhere.
