@@ -353,6 +353,24 @@ __global__ void cg_rsq_kernel(const double *partials, int n, double *sc, double 
     }
 }
 
+// FP32 -> FP64 widening with integer operations: FP64 instructions, conversions included,
+// issue at about two lanes per clock per SM here, while these vector kernels widen one float
+// per degree of freedom. Normal numbers keep sign and mantissa (moved from 23 to 52 bits) and
+// rebias the exponent by 1023 - 127 = 896; zeros keep their sign; subnormals, infinities and
+// NaNs take the hardware conversion. Equal to (double)f for every float.
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0xffu || (e == 0u && (b & 0x7fffffu))) return (double)f;
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    const uint64_t bits = (b & 0x7fffffffu) ? (sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29))
+                                            : sign;
+    return __longlong_as_double((long long)bits);
+}
+
+// All loads are issued before the Dirichlet mask is applied (a load guarded by the mask would
+// wait for it).
 template <typename Ts>
 __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__restrict__ src, double *__restrict__ s,
                                                             const double *__restrict__ r,
@@ -363,17 +381,50 @@ __global__ void __launch_bounds__(BS) cg_precond_out_kernel(Geom g, const Ts *__
     double acc = 0.0;
     for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
         const uint8_t dm = dmask[n];
-        const double s0 = (dm & 1) ? 0.0 : (double)src[n];
-        const double s1 = (dm & 2) ? 0.0 : (double)src[g.ld + n];
-        const double s2 = (dm & 4) ? 0.0 : (double)src[2 * g.ld + n];
-        s[n] = s0;
-        s[g.ld + n] = s1;
-        s[2 * g.ld + n] = s2;
+        const Ts a0 = src[n], a1 = src[g.ld + n], a2 = src[2 * g.ld + n];
+        const double r0 = r[n], r1 = r[g.ld + n], r2 = r[2 * g.ld + n];
+        const double s0 = (dm & 1) ? 0.0 : widen(a0);
+        const double s1 = (dm & 2) ? 0.0 : widen(a1);
+        const double s2 = (dm & 4) ? 0.0 : widen(a2);
+        if (s) {
+            s[n] = s0;
+            s[g.ld + n] = s1;
+            s[2 * g.ld + n] = s2;
+        }
         const int j = (int)(((uint32_t)n / (uint32_t)g.nn[2]) % (uint32_t)g.nn[1]);
-        if (j < rows) acc += r[n] * s0 + r[g.ld + n] * s1 + r[2 * g.ld + n] * s2;
+        if (j < rows) acc = fma(r2, s2, fma(r1, s1, fma(r0, s0, acc)));
     }
     const double t = block_sum<BS>(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// Block maximum of the |v| bit patterns (see cg_direction_kernel) into amax[blockIdx.x].
+__device__ __forceinline__ void block_absmax_store(unsigned long long m, double *amax) {
+    __shared__ unsigned long long sh[BS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long a = __shfl_xor_sync(0xffffffffu, m, o);
+        m = a > m ? a : m;
+    }
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long r = 0ull;
+        for (int w = 0; w < BS / 32; ++w) r = sh[w] > r ? sh[w] : r;
+        amax[blockIdx.x] = __longlong_as_double((long long)r);
+    }
+}
+
+__device__ __forceinline__ void direction_store(double v, int64_t t, double *__restrict__ d, float *__restrict__ dh,
+                                                float *__restrict__ dl, unsigned long long &m) {
+    d[t] = v;
+    if (dh) {
+        const float h = __double2float_rn(v);
+        dh[t] = h;
+        dl[t] = __double2float_rn(v - (double)h);
+    }
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    m = a > m ? a : m;
 }
 
 __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double *__restrict__ d,
@@ -386,32 +437,39 @@ __global__ void cg_direction_kernel(Geom g, const double *__restrict__ s, double
     // of the patterns is the numeric order, and NaN patterns exceed every number, so an integer
     // maximum (integer units; the FP64 units are the scarce ones here) propagates NaN
     unsigned long long m = 0ull;
-    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS) {
-        const double v = beta * d[t] + s[t];
-        d[t] = v;
-        if (dh) {
-            const float h = __double2float_rn(v);
-            dh[t] = h;
-            dl[t] = __double2float_rn(v - (double)h);
-        }
-        const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-        m = a > m ? a : m;
-    }
-    if (amax) {
-        __shared__ unsigned long long sh[BS / 32];
+    for (int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x; t < N3; t += (int64_t)gridDim.x * BS)
+        direction_store(beta * d[t] + s[t], t, d, dh, dl, m);
+    if (amax) block_absmax_store(m, amax);
+}
+
+// The same direction update with s formed on the fly from the preconditioner's iterate, as
+// cg_precond_out_kernel forms it (Dirichlet components zeroed), so that s is never stored:
+// the preconditioner step then only reduces r . s. Entries past NN in each component's
+// stride are not touched (d stays zero there).
+template <typename Ts>
+__global__ void cg_direction_precond_kernel(Geom g, const Ts *__restrict__ src, const uint8_t *__restrict__ dmask,
+                                            double *__restrict__ d, const double *__restrict__ sc,
+                                            float *__restrict__ dh, float *__restrict__ dl,
+                                            double *__restrict__ amax) {
+    VFEM_PDL_ENTRY();
+    const double beta = sc[2];
+    unsigned long long m = 0ull;
+    for (int64_t n = blockIdx.x * (int64_t)BS + threadIdx.x; n < g.NN; n += (int64_t)gridDim.x * BS) {
+        const uint8_t dm = dmask[n];
+        Ts a[3];
+        double dv[3];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long a = __shfl_xor_sync(0xffffffffu, m, o);
-            m = a > m ? a : m;
+        for (int c = 0; c < 3; ++c) {
+            a[c] = src[c * g.ld + n];
+            dv[c] = d[c * g.ld + n];
         }
-        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long r = 0ull;
-            for (int w = 0; w < BS / 32; ++w) r = sh[w] > r ? sh[w] : r;
-            amax[blockIdx.x] = __longlong_as_double((long long)r);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double sv = ((dm >> c) & 1) ? 0.0 : widen(a[c]);
+            direction_store(beta * dv[c] + sv, c * g.ld + n, d, dh, dl, m);
         }
     }
+    if (amax) block_absmax_store(m, amax);
 }
 
 __global__ void __launch_bounds__(BS) cg_update_kernel(Geom g, double *__restrict__ x, double *__restrict__ r,
@@ -625,6 +683,13 @@ void launch_cg_direction(const Geom &g, const double *s, double *d, const double
     VFEM_LAUNCH_CHECK();
 }
 
+template <typename Ts>
+void launch_cg_direction_precond(const Geom &g, const Ts *src, const uint8_t *dmask, double *d, const double *sc,
+                                 float *dh, float *dl, cudaStream_t st, double *amax) {
+    launch_pdl(cg_direction_precond_kernel<Ts>, REDUCE_BLOCKS, BS, 0, st, g, src, dmask, d, sc, dh, dl, amax);
+    VFEM_LAUNCH_CHECK();
+}
+
 void launch_cg_update(const Geom &g, double *x, double *r, const double *d, const double *Ad, const double *sc,
                       double *partials, cudaStream_t st, float *b32, float *x32) {
     launch_pdl(cg_update_kernel, REDUCE_BLOCKS, BS, 0, st, g, x, r, d, Ad, sc, partials, b32, x32);
@@ -654,6 +719,8 @@ template void launch_masked_dot_partials<double, double>(const Geom &, const dou
                                                          cudaStream_t);
 template void launch_masked_dot_partials<float, float>(const Geom &, const float *, const float *, double *,
                                                        cudaStream_t);
+template void launch_cg_direction_precond<float>(const Geom &, const float *, const uint8_t *, double *,
+                                                const double *, float *, float *, cudaStream_t, double *);
 template void launch_cg_precond_out<double>(const Geom &, const double *, double *, const double *, const uint8_t *,
                                             double *, cudaStream_t);
 template void launch_cg_precond_out<float>(const Geom &, const float *, double *, const double *, const uint8_t *,

@@ -865,13 +865,14 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool h
         } else {
             // the previous cg_update (or the solve's start) left b32 = (float) r and x32 = 0
             preconditionT<float>(rbuf.p, mgIter, sweeps, fmg, fusedInit());
-            launch_cg_precond_out<float>(g, lv[0].d32.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+            // s is not stored: the direction update forms it again from the FP32 iterate
+            launch_cg_precond_out<float>(g, lv[0].d32.x.p, (double *)nullptr, rbuf.p, fine->dmask.p, partials.p, st);
         }
     } else {
         launch_cg_precond_out<double>(g, rbuf.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
     }
     launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
-    outerDirection();
+    outerDirection(mgIter > 0 && precision != PREC_FP64 ? lv[0].d32.x.p : nullptr);
     const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
     launch_cg_alpha(partials.p, nb, sc.p, st);
     if (fusedInit())
@@ -888,11 +889,16 @@ int MG::outerKind() const {
     return 1;
 }
 
-void MG::outerDirection() {
+void MG::outerDirection(const float *precondIterate) {
     const int kind = outerKind();
     if (kind == 2) umax.alloc(REDUCE_BLOCKS);
-    launch_cg_direction(lv[0].g, s.p, dvec.p, sc.p, kind == 1 ? dhi.p : nullptr, kind == 1 ? dlo.p : nullptr,
-                        fine->stream, kind == 2 ? umax.p : nullptr);
+    float *dh = kind == 1 ? dhi.p : nullptr, *dl = kind == 1 ? dlo.p : nullptr;
+    double *am = kind == 2 ? umax.p : nullptr;
+    if (precondIterate)
+        launch_cg_direction_precond<float>(lv[0].g, precondIterate, fine->dmask.p, dvec.p, sc.p, dh, dl, fine->stream,
+                                           am);
+    else
+        launch_cg_direction(lv[0].g, s.p, dvec.p, sc.p, dh, dl, fine->stream, am);
 }
 
 int MG::outerMatvecApply(const double *u, double *out, double *partialsOut, const double *rhs, bool uReady) {
@@ -1833,7 +1839,8 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
             });
         }
         timed("cg:precond_out+beta", [&] {
-            launch_cg_precond_out<T>(g, D0.x.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
+            launch_cg_precond_out<T>(g, D0.x.p, std::is_same<T, float>::value ? nullptr : s.p, rbuf.p,
+                                     fine->dmask.p, partials.p, st);
             launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
         });
     };
@@ -1841,7 +1848,7 @@ std::vector<std::pair<std::string, double>> MG::profile(int64_t mgIter, int64_t 
     for (int r = 0; r < reps; ++r) {
         if (precision == PREC_FP64) body(double());
         else body(float());
-        timed("cg:direction", [&] { outerDirection(); });
+        timed("cg:direction", [&] { outerDirection(precision == PREC_FP64 ? nullptr : lv[0].d32.x.p); });
         timed("cg:matvec+alpha", [&] {
             const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
             launch_cg_alpha(partials.p, nb, sc.p, st);

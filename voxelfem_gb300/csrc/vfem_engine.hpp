@@ -219,7 +219,8 @@ public:
     // kind of the mixed outer matvec in use: 0 FP64, 1 double-float (FP32 units), 2 tensor cores
     int outerKind() const;
     // d = beta d + s with the side outputs the outer matvec needs
-    void outerDirection();
+    // d = beta d + s; with the FP32 V-cycle iterate given, s is formed from it on the fly
+    void outerDirection(const float *precondIterate = nullptr);
     // out = K u (rhs: rhs - K u) with the outer matvec; uReady: u's side data (split or maxima)
     // are current. Returns the number of partial dots written when partialsOut is given.
     int outerMatvecApply(const double *u, double *out, double *partialsOut, const double *rhs, bool uReady);

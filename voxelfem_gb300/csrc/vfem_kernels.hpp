@@ -204,7 +204,8 @@ void launch_finalize(const double *partials, int n, double *out, cudaStream_t st
 void launch_cg_beta(const double *partials, int n, double *sc, cudaStream_t st);
 void launch_cg_alpha(const double *partials, int n, double *sc, cudaStream_t st);
 void launch_cg_rsq(const double *partials, int n, double *sc, double *hostMirror, cudaStream_t st);
-// s <- (s with Dirichlet comps zeroed) where s comes from src (FP64 or FP32); partials of r.s (masked)
+// s <- (s with Dirichlet comps zeroed) where s comes from src (FP64 or FP32); partials of r.s (masked).
+// With s == nullptr only the partials are formed (launch_cg_direction_precond forms s itself).
 template <typename Ts>
 void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double *r, const uint8_t *dmask,
                            double *partials, cudaStream_t st);
@@ -212,6 +213,11 @@ void launch_cg_precond_out(const Geom &g, const Ts *src, double *s, const double
 // amax is given the REDUCE_BLOCKS partial maxima of |d| (NaN propagates).
 void launch_cg_direction(const Geom &g, const double *s, double *d, const double *sc, float *dh, float *dl,
                          cudaStream_t st, double *amax = nullptr);
+// launch_cg_direction with s formed from the preconditioner iterate src as launch_cg_precond_out
+// forms it (instantiated for FP32 iterates).
+template <typename Ts>
+void launch_cg_direction_precond(const Geom &g, const Ts *src, const uint8_t *dmask, double *d, const double *sc,
+                                 float *dh, float *dl, cudaStream_t st, double *amax = nullptr);
 
 // ---------------- warm starts of the layer-by-layer evaluation (k_lbl.cu) ----------------
 constexpr int LBL_MAX_HISTORY = 8;
