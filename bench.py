@@ -212,6 +212,8 @@ def run_reference(args):
         return
     cfg = args.config
     vals, last = [], None
+    for _ in range(args.warmup):  # untimed: page-in of the oracle library and the grids
+        cpu_baseline_sample(cfg, FP64_ITERATIONS.get(cfg))
     for _ in range(args.steps):
         last = cpu_baseline_sample(cfg, FP64_ITERATIONS.get(cfg))
         vals.append(last["value"])
