@@ -5,6 +5,7 @@
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 #include "vfem_stencil.cuh"
+#include "vfem_widen.h"
 
 namespace vfem {
 
@@ -353,20 +354,12 @@ __global__ void cg_rsq_kernel(const double *partials, int n, double *sc, double 
     }
 }
 
-// FP32 -> FP64 widening with integer operations: FP64 instructions, conversions included,
-// issue at about two lanes per clock per SM here, while these vector kernels widen one float
-// per degree of freedom. Normal numbers keep sign and mantissa (moved from 23 to 52 bits) and
-// rebias the exponent by 1023 - 127 = 896; zeros keep their sign; subnormals, infinities and
-// NaNs take the hardware conversion. Equal to (double)f for every float.
+// FP32 -> FP64 widening on the integer units (vfem_widen.h): FP64 instructions, conversions
+// included, issue at about two lanes per clock per SM here, and these vector kernels widen one
+// float per degree of freedom. Equal to (double)f for every float.
 __device__ __forceinline__ double widen(double v) { return v; }
 __device__ __forceinline__ double widen(float f) {
-    const uint32_t b = __float_as_uint(f);
-    const uint32_t e = (b >> 23) & 0xffu;
-    if (e == 0xffu || (e == 0u && (b & 0x7fffffu))) return (double)f;
-    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
-    const uint64_t bits = (b & 0x7fffffffu) ? (sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29))
-                                            : sign;
-    return __longlong_as_double((long long)bits);
+    return __longlong_as_double((long long)vfem_widen_bits(__float_as_uint(f)));
 }
 
 // All loads are issued before the Dirichlet mask is applied (a load guarded by the mask would
