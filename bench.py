@@ -39,12 +39,7 @@ CONFIGS = {
     "c2": ((256, 128, 128), 0.01, 5),
     "c1": ((64, 32, 32), 0.3, 3),
 }
-# FP64 MG-PCG iterations to 1e-8 of these workloads, from full solves of the CPU oracle
-# (tests/golden/cantilever_256x128x128_oracle.json for c2); the GPU FP64 path runs the same
-# algorithm and reports its own count in every run.
-FP64_ITERATIONS = {"c2": 16, "c1": 10}
 TOL = 1e-8
-FP32_PEAK_TFLOPS = 74.0  # FFMA-loop probe on this machine's GB300 (dependent-free FMA chains, all SMs)
 KERNEL_NAMES = {0: "applyk_fine_fp64", 1: "applyk_fine_fp32", 2: "applyk_fine_df", 3: "gs_fine_sweep_fp32",
                 4: "gs_fine_sweep_fp64", 5: "residual_fine_fp32", 6: "gs_level1_sweep_fp32",
                 7: "residual_level1_fp32", 8: "gs_level2_sweep_fp32", 9: "residual_level2_fp32",
@@ -99,6 +94,34 @@ def fp64_peak_tflops(n=4096, reps=5):
         e1.synchronize()
         t = e0.elapsed_time(e1) * 1e-3 / reps
         best = t if best is None else min(best, t)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def fp32_peak_tflops(n=8192, reps=5):
+    """FP32 FMA throughput of this GPU, measured with a cuBLAS SGEMM with TF32 off (FFMA on the
+    CUDA cores; best of two timed batches), the denominator of the FP32-pipe rooflines."""
+    import torch
+
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(2):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1e-3 / reps
+            best = t if best is None else min(best, t)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
     return 2.0 * n ** 3 / best / 1e12
 
 
@@ -171,52 +194,48 @@ def phase_breakdown(lib, capi, mg_h, reps=3):
     return {k: round(ms[i], 4) for i, k in enumerate(keys[: n.value])}
 
 
-def cpu_baseline_sample(cfg_name, iterations_to_tol, threads=None):
-    """Time the CPU oracle (a restatement of the reference's solver) on a bounded sample of
-    the workload: set-up plus the first PCG iterations, extrapolated to the iteration count
-    of the full solve."""
+def cpu_baseline_solve(cfg_name, threads=None):
+    """One complete FP64 MG-PCG solve of the workload by the CPU oracle (a restatement of the
+    reference's solver), timed like the GPU step: from the density upload (which invalidates the
+    hierarchy) through the Galerkin rebuild (the oracle's PCG rebuilds the hierarchy's operators on
+    entry, as the reference's does) and the PCG iterations to relative residual 1e-8."""
     from oracle import pyoracle as po
     from voxelfem_gb300 import workloads as wl
     ne, rho_lo, levels = CONFIGS[cfg_name]
     threads = threads or os.cpu_count()
     po.set_num_threads(threads)
     sim = po.Sim(ne)
-    wl.setup_cantilever(sim, ne, rho_lo, 0)
+    rho, _ = wl.setup_cantilever(sim, ne, rho_lo, 0)
     mg = po.MG(sim, levels)
     b = sim.buildLoadVector()
-    stamps = []
-    sample_iters = 3 if cfg_name == "c2" else 100
+    x0 = np.zeros_like(b)
     t0 = time.perf_counter()
-    mg.preconditionedConjugateGradient(np.zeros_like(b), b, sample_iters, TOL, lambda i, r: stamps.append(time.perf_counter()),
-                                       1, 2, False)
+    sim.setDensities(rho)
+    x = mg.preconditionedConjugateGradient(x0, b, 500, TOL, None, 1, 2, False)
     t1 = time.perf_counter()
-    done = mg.lastIterations
-    if iterations_to_tol is None or done >= iterations_to_tol or mg.lastRelativeResidual <= TOL:
-        est = t1 - t0
-        n_it = done
-        how = "full solve"
-    else:
-        first = stamps[0] - t0
-        per = (stamps[-1] - stamps[0]) / max(len(stamps) - 1, 1)
-        est = first + (iterations_to_tol - 1) * per
-        n_it = iterations_to_tol
-        how = "set-up + %d PCG iterations timed (%.2f s), extrapolated to %d iterations" % (done, t1 - t0, n_it)
-    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": "CPU oracle FP64 MG-PCG, %s cantilever %dx%dx%d, %s" % (cfg_name, ne[0], ne[1], ne[2], how),
-            "iterations": n_it, "sample_seconds": t1 - t0}
+    return {"value": t1 - t0, "unit": "s", "cores": threads, "kind": "port",
+            "sample": "complete CPU-oracle FP64 MG-PCG solve of the %s cantilever %dx%dx%d (density upload, Galerkin "
+                      "rebuild, %d PCG iterations to relres %.2e), OpenMP over %d host threads"
+                      % (cfg_name, ne[0], ne[1], ne[2], mg.lastIterations, mg.lastRelativeResidual, threads),
+            "iterations": int(mg.lastIterations), "relres": float(mg.lastRelativeResidual),
+            "compliance": float(0.5 * np.sum(b * x))}
 
 
 def run_reference(args):
+    """The reference arm: the CPU oracle's complete FP64 solves of the same workload on the host
+    cores, one solve per step (no extrapolation)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     cfg = args.config
     vals, last = [], None
-    for _ in range(args.warmup):  # untimed: page-in of the oracle library and the grids
-        cpu_baseline_sample(cfg, FP64_ITERATIONS.get(cfg))
+    for _ in range(args.warmup):  # untimed: page-in of the oracle library, thread pool, first-touch
+        cpu_baseline_solve(cfg)
+    t_all = time.perf_counter()
     for _ in range(args.steps):
-        last = cpu_baseline_sample(cfg, FP64_ITERATIONS.get(cfg))
+        last = cpu_baseline_solve(cfg)
         vals.append(last["value"])
+    t_all = time.perf_counter() - t_all
     v = float(np.mean(vals))
     ne = CONFIGS[cfg][0]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps,
@@ -226,6 +245,8 @@ def run_reference(args):
                        % (ne[0], ne[1], ne[2], CONFIGS[cfg][1], CONFIGS[cfg][2])},
             "cpu_baseline": {"value": v, "unit": "s", "cores": last["cores"], "kind": last["kind"],
                              "sample": last["sample"]},
+            "iterations": last["iterations"], "compliance": last["compliance"],
+            "timed_region_s": t_all, "min_s": float(min(vals)), "max_s": float(max(vals)),
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -401,6 +422,7 @@ def run_ours(args):
                         "traffic": traffic_tab.get(k), "algorithmic_bytes": kd["bytes"], "ms_per_launch": kd["ms"],
                         "ms_per_iteration": share[k]}
     p64 = fp64_peak_tflops()
+    peaks_measured = {"fp64_tflops": p64, "fp64_how": "cuBLAS DGEMM 4096^3 in this run"}
     for k in ("applyk_fine_df", "applyk_fine_tc"):
         if k not in rooflines:
             continue
@@ -420,14 +442,16 @@ def run_ours(args):
                                                  "frac": tflops / bf16 if bf16 else None}
     # the matrix-free FP32 fine-level kernels are bound by the FP32 pipe: 2 * 24^2 flops per node
     # (the 8 incident element rows of K0 times u) against the FFMA rate of this GPU
+    p32 = fp32_peak_tflops()
+    peaks_measured.update(fp32_tflops=p32, fp32_how="cuBLAS SGEMM 8192^3 with TF32 off, in this run")
     for k in ("gs_fine_sweep_fp32", "residual_fine_fp32"):
         if k in rooflines:
             flops = 2.0 * 24 * 24 * nn
             achieved = flops / (kernels[k]["ms"] * 1e-3) / 1e12
             rooflines[k]["fp32_compute"] = {"flops": flops, "achieved": achieved, "unit": "TFLOP/s",
-                                            "peak": FP32_PEAK_TFLOPS,
-                                            "peak_kind": "measured (FFMA-loop probe on this pool's GB300)",
-                                            "frac": achieved / FP32_PEAK_TFLOPS}
+                                            "peak": p32,
+                                            "peak_kind": "measured (cuBLAS SGEMM 8192^3, TF32 off, in this run)",
+                                            "frac": achieved / p32}
     roofline = dict(rooflines[dom], kernel=dom, peak_kind=peak_kind)
 
     line = {"metric": METRIC, "value": tmix_step if ws == 1 else tmix / (ws * args.steps), "unit": "s",
@@ -445,6 +469,7 @@ def run_ours(args):
             "roofline": roofline,
             "rooflines": rooflines,
             "clocks": clk,
+            "peaks_measured": peaks_measured,
             "gpu_launches": int(cnt1.value - cnt0.value),
             "mixed": {"s_per_solve": tmix_step, "iterations": int(itmix), "relres": rrmix, "true_relres": true_rel,
                       "compliance": compm},
@@ -466,7 +491,16 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_2d:
         line["2d"] = run_2d(hbm, args.no_cpu)
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_sample(args.config, int(it64))
+        cb_line = cpu_baseline_solve(args.config)
+        line["cpu_baseline"] = cb_line
+        # the CPU solve against both GPU forms: the plain method (FP64) and the headline (mixed)
+        line["vs_cpu_baseline"] = {"fp64_gpu_speedup": cb_line["value"] / t64,
+                                   "mixed_gpu_speedup": cb_line["value"] / tmix_step,
+                                   "mixed_e2e_speedup": cb_line["value"] / e2e,
+                                   "cpu_iterations": cb_line["iterations"], "gpu_fp64_iterations": int(it64),
+                                   "gpu_mixed_iterations": int(itmix),
+                                   "compliance_rel_diff_fp64_gpu_vs_cpu":
+                                       abs(comp64 - cb_line["compliance"]) / abs(cb_line["compliance"])}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -634,7 +668,8 @@ def run_q2(hbm, solve=True):
     g = pv.TensorProductSimulator([2, 2, 2], [[0.0, 0.0, 0.0], [float(v) for v in ne]], ne)
     g.ETensor = (1.0, 0.3)
     g.E_0, g.E_min, g.gamma = 1.0, 1e-9, 3.0
-    g.setDensities(np.random.default_rng(0).uniform(0.01, 1.0, int(np.prod(ne))))
+    rho = np.random.default_rng(0).uniform(0.01, 1.0, int(np.prod(ne)))
+    g.setDensities(rho)
     flops = 2.0 * 81 * 81 * g.numElements()
     out = {"workload": "128^3 Q2 applyK (%d nodes), rho U[0.01,1] seed 0" % g.numNodes()}
     for name, prec, reps in (("fp64", 0, 2), ("df", 2, 3), ("fp32", 1, 10)):
@@ -649,16 +684,20 @@ def run_q2(hbm, solve=True):
         gbs = nbytes.value / (ms.value * 1e-3) / 1e9
         out[name] = {"ms": ms.value, "bytes": nbytes.value, "gbs": gbs, "hbm_frac": gbs / hbm}
     if solve:
-        out["solve"] = run_q2_solve(g, ne)
+        out["solve"] = run_q2_solve(g, ne, rho)
     return out
 
 
-def run_q2_solve(g, ne):
+def run_q2_solve(g, ne, rho):
     """Time to relative residual 1e-8 of the 128^3 Q2 cantilever (x = 0 face fixed, unit total -y
     load spread over the nodes of the x = max, z = mid edge): FP64 CG with the double-float
     matvec, p-multigrid preconditioner (Q2 block Gauss-Seidel around an FP32 trilinear V-cycle with
-    5 coarsenings). The accuracy check is the true FP64 residual |f - K u| / |f| of the returned
-    u."""
+    5 coarsenings). Accuracy against FP64:
+    - the true FP64 residual |f - K u| / |f| of the returned u, with K applied by the library's
+      FP64 kernel and, independently, by the CPU oracle's triquadratic applyK (the reference's
+      generic stencil restated, with its own K0 quadrature);
+    - the error of u and of the compliance against an FP64 solve of the same system (CG with the
+      FP64 matvec) to relative residual 1e-11."""
     import time
 
     nx, ny, nz = ne
@@ -676,12 +715,37 @@ def run_q2_solve(g, ne):
     u = mg.preconditionedConjugateGradient(x0, f, 500, 1e-8, None, 1, 1, False)
     seconds = time.perf_counter() - t0
     st = mg.lastStats
+    dmask = g.getDirichletMask()
     r = f - g.applyK(u, zeroDirichlet=True)
-    r[g.getDirichletMask()] = 0.0
-    return {"seconds_to_1e-8": seconds, "iterations": int(st.iterations), "relres": float(st.relres),
-            "true_relres_fp64": float(np.linalg.norm(r) / np.linalg.norm(f)),
-            "compliance": float(np.sum(f * u)), "dofs": 3 * nn,
-            "note": "host buffers in and out; includes the h2d of f and x0 and the d2h of u"}
+    r[dmask] = 0.0
+    out = {"seconds_to_1e-8": seconds, "iterations": int(st.iterations), "relres": float(st.relres),
+           "true_relres_fp64": float(np.linalg.norm(r) / np.linalg.norm(f)),
+           "compliance": float(np.sum(f * u)), "dofs": 3 * nn,
+           "note": "host buffers in and out; includes the h2d of f and x0 and the d2h of u"}
+    # the FP64 reference solve of the same system
+    mg.setOuterMatvec("fp64")
+    t0 = time.perf_counter()
+    u64 = mg.preconditionedConjugateGradient(x0, f, 1000, 1e-11, None, 1, 1, False)
+    out["fp64_reference"] = {"tol": 1e-11, "iterations": int(mg.lastStats.iterations),
+                             "relres": float(mg.lastStats.relres), "seconds": time.perf_counter() - t0,
+                             "u_rel_err_mixed": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
+                             "u_max_rel_err_mixed": float(np.max(np.abs(u - u64)) / np.max(np.abs(u64))),
+                             "compliance_rel_err_mixed": float(abs(np.sum(f * u) - np.sum(f * u64))
+                                                               / abs(np.sum(f * u64)))}
+    mg.setOuterMatvec("df")
+    try:
+        from oracle import pyoracle as po
+        K0 = po.q2_k0(1.0, 0.3, (1.0, 1.0, 1.0), 3)
+        Y = 1e-9 + rho ** 3 * (1.0 - 1e-9)
+        t0 = time.perf_counter()
+        ro = f - po.q2_apply_k(ne, K0, Y, u)
+        ro[dmask] = 0.0
+        out["oracle_relres_fp64"] = float(np.linalg.norm(ro) / np.linalg.norm(f))
+        out["oracle_apply_seconds"] = time.perf_counter() - t0
+    except Exception as e:  # the oracle library is not built: report why
+        out["oracle_relres_fp64"] = None
+        out["oracle_error"] = str(e)[:200]
+    return out
 
 
 D2_DEMO = (384, 192)      # the reference's 2D topology-optimisation demo resolution

@@ -162,6 +162,10 @@ int vfem_mg_outer_apply(vfem_mg *mg, const double *u, const double *rhs, double 
  * scale times a small-integer matrix that keeps the tensor-core matvec exact, and its bf16 B
  * tiles. */
 int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, int *ok);
+/* Diagnostic (no reference counterpart): 1/d and 1/sqrt(d) for n doubles through the pivot
+ * helpers of the coarsest dense inverse (single-precision seed plus two Newton-Raphson steps;
+ * the plain quotient outside (1e-30, 1e30)). Host or device arrays. */
+int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, double *rsqrt_out);
 /* CUDA-graph capture of the CG iteration (default on); no reference counterpart */
 int vfem_mg_set_use_graphs(vfem_mg *mg, int use);
 /* Execution option (no reference counterpart): with graphs on, a solve without a callback runs as
@@ -216,15 +220,20 @@ int vfem_mg_profile(vfem_mg *mg, int64_t mg_iterations, int64_t mg_smoothing_ite
 /* SmoothingFilter::apply (= backprop) (TopologyOptimizationFilter.hh:285-400); type 0 Const, 1 Linear */
 int vfem_smoothing_filter(const int64_t dims[3], int radius, int type, const double *in, double *out);
 /* Allocation-free variant of vfem_smoothing_filter; it has no counterpart in the reference.
- * For callers that cannot call cudaMalloc (code capturing the filter into its own CUDA graph,
- * code under a fixed device-memory budget, loops that cannot afford the device synchronisation
- * of cudaMalloc/cudaFree). It allocates nothing: the tap table lives in a fixed device array
- * inside libvfem.so, held by every GPU that loads the library until exit, which bounds the
- * radius to 6 (larger radii are rejected with VFEM_ERR_ARG). in_dev and out_dev must be device
- * pointers; the work is enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the
- * call returns without waiting. The first call on a device looks up the array's device address
- * and should come before any stream capture. Calls share the array: calls that overlap on the
- * GPU (e.g. on two streams) race on it. */
+ * For callers that cannot call cudaMalloc: code under a fixed device-memory budget or inside a
+ * host application that owns every device allocation (a plug-in may use only the buffers it is
+ * handed), and loops that cannot afford the device synchronisation of cudaMalloc/cudaFree (the
+ * tens of filter applications of every OC bisection). It allocates nothing: the tap table lives
+ * in a fixed device array inside libvfem.so (about 44 KB), held by every GPU that loads the
+ * library until exit, which bounds the radius to 6 (larger radii are rejected with
+ * VFEM_ERR_ARG). The filter is the 3D one: its result equals vfem_smoothing_filter on the same
+ * dims (a grid one voxel thick is filtered in 3D, its z offsets reflected onto the one layer;
+ * 2D callers use vfem_smoothing_filter2). in_dev and out_dev must be device pointers; the work is
+ * enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the call returns without
+ * waiting. The first call on a device, with that device current, looks up the array's device
+ * address; make that first call before any stream capture on the device. Every call rebuilds the
+ * tap table in the shared array, so calls that overlap on the GPU (e.g. on two streams) race on
+ * it. */
 int vfem_smoothing_filter_noalloc(const int64_t dims[3], int radius, int type, const double *in_dev, double *out_dev,
                                   void *stream);
 /* ProjectionFilter::apply / backprop (TopologyOptimizationFilter.hh:199-225) */
@@ -257,6 +266,11 @@ int vfem_problem_get_physical(vfem_problem *p, double *x_out);
 int vfem_problem_last_solve(vfem_problem *p, vfem_pcg_stats *stats);
 /* OCOptimizer::step(m, p, ctol) (OptimalityCriterion.hh:51-138); probes = constraint evaluations */
 int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, int64_t *probes);
+/* The same OC step with the objective gradient (numVars doubles, host or device) supplied by the
+ * caller instead of evaluateObjectiveGradient, e.g. from a torch.autograd backward pass through
+ * the same problem; no reference counterpart (the reference's step always evaluates it). */
+int vfem_problem_oc_step_with_gradient(vfem_problem *p, double m, double pexp, double ctol,
+                                       const double *objective_gradient, int64_t *probes);
 
 /* ---- triquadratic voxels (TensorProductSimulator<double, 2, 2, 2>, TPSStencils.hh:135-186) ----
  * Nodes (2 nx + 1)(2 ny + 1)(2 nz + 1), index (I ny' + J) nz' + K; nodal fields (nn, 3)

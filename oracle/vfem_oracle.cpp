@@ -1408,7 +1408,10 @@ void q2K0(double E, double nu, const double h[3], int npts, double *K) {
 
 void q2ApplyK(const Q2Grid &g, const double *K, const double *Y, const double *u, double *out) {
     std::fill(out, out + 3 * g.NN, 0.0);
-    for (long i = 0; i < g.ne[0]; ++i)
+    // element layers of one x parity share no node: each parity's layers run in parallel
+    for (int parity = 0; parity < 2; ++parity)
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long i = parity; i < g.ne[0]; i += 2)
         for (long j = 0; j < g.ne[1]; ++j)
             for (long k = 0; k < g.ne[2]; ++k) {
                 size_t nodes[27];

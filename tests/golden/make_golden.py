@@ -12,9 +12,14 @@
   the 256x128x128 cantilever (5 coarsenings, tol 1e-8): iterations, final
   relative residual and compliance. Regenerate with ``--full`` (about 1.5
   minutes on 8 cores).
+* lbl_128_oracle.json -- oracle FP64 MG-PCG solves of the 128^3 layer-by-layer
+  workload (rho U[0.1,1] seed 0, base fixed, gravity -y, 5 coarsenings, zero
+  guess, tol 1e-8, 2+2 sweeps) at build heights 1, 16, 64 and 128: per height the
+  iteration count, the relative residual and f.u (the evaluator's per-height
+  compliance). Regenerate with ``--lbl`` (about 2 minutes on 8 cores).
 
-Run from the repository root:  python tests/golden/make_golden.py   (``--full`` only redoes the
-large solve).
+Run from the repository root:  python tests/golden/make_golden.py   (``--full`` and ``--lbl``
+only redo the large solves).
 """
 import json
 import os
@@ -100,7 +105,38 @@ def oracle_full():
             "seconds": time.time() - t0}
 
 
+LBL_HEIGHTS = (1, 16, 64, 128)
+
+
+def oracle_lbl():
+    import time
+    from oracle import pyoracle as po
+    from voxelfem_gb300 import workloads as wl
+    ne = (128, 128, 128)
+    out = {"workload": "layer-by-layer 128^3 Q1, rho U[0.1,1] seed 0, E0=1, Emin=1e-9, nu=0.3, p=3, base y=0 "
+                       "fixed, gravity (0,-1,0), 5 coarsenings, mgIterations=1, mgSmoothingIterations=2, "
+                       "V-cycle, tol 1e-8, x0=0",
+           "heights": [], "threads": po.num_threads()}
+    for h in LBL_HEIGHTS:
+        s = po.Sim(ne)
+        wl.setup_layer_by_layer(s, ne, 0.1, 0)
+        s.setFabricationMaskHeightByLayer(h)
+        mg = po.MG(s, 5)
+        mg.setFabricationMaskHeightByLayer(h)
+        b = s.buildLoadVector()
+        t0 = time.time()
+        x = mg.preconditionedConjugateGradient(np.zeros_like(b), b, 500, 1e-8, None, 1, 2, False)
+        out["heights"].append({"height": h, "iterations": int(mg.lastIterations),
+                               "relres": float(mg.lastRelativeResidual), "f_dot_u": float(np.sum(b * x)),
+                               "seconds": time.time() - t0})
+    return out
+
+
 def main():
+    if "--lbl" in sys.argv:
+        with open(os.path.join(HERE, "lbl_128_oracle.json"), "w") as f:
+            json.dump(oracle_lbl(), f, indent=1)
+        return
     if "--full" in sys.argv:
         full = oracle_full()
         with open(os.path.join(HERE, "cantilever_256x128x128_oracle.json"), "w") as f:

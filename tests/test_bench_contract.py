@@ -24,3 +24,6 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "64x32x32" in d["config"]["workload"]
+    # each step is a complete solve: the claimed time fits in the measured timed region
+    assert d["timed_region_s"] >= d["steps"] * d["value"] * 0.999
+    assert "complete" in d["cpu_baseline"]["sample"] and d["iterations"] > 0

@@ -151,21 +151,61 @@ def test_masked_layers(gpu, oracle, stencil_layout, levels):
 
 
 def test_pcg_mixed_precision(gpu, oracle, stencil_layout):
+    """Mixed precision (FP32 V-cycle inside FP64 CG) at 32x16x16 for each outer matvec: relative
+    residual 1e-8, a true FP64 residual below 2e-8 and a compliance within 1e-8 of the FP64 GPU
+    solve of the same system (and of the oracle's)."""
     ne = (32, 16, 16)
     g, o, gm, om = make_pair(oracle, ne, levels=3)
     b = g.buildLoadVector()
     x0 = np.zeros_like(b)
     xo = om.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
-    for matvec in ("df", "fp64"):
+    gm.setPrecision("fp64")
+    x64 = gm.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
+    c64 = 0.5 * np.sum(b * x64)
+    co = 0.5 * np.sum(b * xo)
+    for matvec, kind in (("df", "tensor"), ("df-simt", "df-simt"), ("fp64", "fp64")):
         gm.setPrecision("mixed", matvec)
+        assert gm.outerMatvecKind() == kind
         xg = gm.preconditionedConjugateGradient(x0, b, 100, 1e-8, None, 1, 2, False)
         assert gm.lastStats.relres <= 1e-8
         # true residual of the mixed solution, evaluated in FP64
         r = b - g.applyK(xg)
         r[g.getDirichletMask()] = 0
         assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-8
-        cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
-        assert abs(cg - co) / abs(co) < 1e-6
+        cg = 0.5 * np.sum(b * xg)
+        assert abs(cg - c64) / abs(c64) < 1e-8, (matvec, abs(cg - c64) / abs(c64))
+        assert abs(cg - co) / abs(co) < 1e-8, (matvec, abs(cg - co) / abs(co))
+    gm.setPrecision("fp64")
+
+
+C1_NE = (64, 32, 32)
+
+
+def test_c1_plain_method_against_oracle(gpu, oracle):
+    """The plain method at its CPU-runnable size: the 64x32x32 cantilever, rho U[0.3, 1] seed 0,
+    E0 = 1, Emin = 1e-9, nu = 0.3, p = 3, 3 coarsenings, one V-cycle with 2 + 2 sweeps per CG
+    iteration, tol 1e-8, zero guess, FP64 throughout. The GPU takes the oracle's iteration count;
+    displacements and compliance agree to 1e-8 and sensitivities to 1e-6. The mixed form of the
+    same solve lands within 1e-8 of the FP64 GPU compliance."""
+    g, o, gm, om = make_pair(oracle, C1_NE, rho_lo=0.3, seed=0, levels=3)
+    assert gm.numLevels == 4
+    b = g.buildLoadVector()
+    np.testing.assert_array_equal(b, o.buildLoadVector())
+    x0 = np.zeros_like(b)
+    xg = gm.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    xo = om.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    assert gm.lastStats.iterations == om.lastIterations
+    assert gm.lastStats.relres <= 1e-8
+    assert rel(xg, xo) < 1e-8
+    cg, co = 0.5 * np.sum(b * xg), 0.5 * np.sum(b * xo)
+    assert abs(cg - co) / abs(co) < 1e-8
+    assert rel(g.complianceGradient(xg), o.complianceGradient(xo)) < 1e-6
+    gm.setPrecision("mixed")
+    xm = gm.preconditionedConjugateGradient(x0, b, 200, 1e-8, None, 1, 2, False)
+    assert gm.lastStats.relres <= 1e-8
+    cm = 0.5 * np.sum(b * xm)
+    assert abs(cm - cg) / abs(cg) < 1e-8, abs(cm - cg) / abs(cg)
+    assert rel(g.complianceGradient(xm), o.complianceGradient(xo)) < 1e-6
     gm.setPrecision("fp64")
 
 

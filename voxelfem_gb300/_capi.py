@@ -123,6 +123,7 @@ _SIGS = {
     "vfem_kernel_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
     "vfem_mg_profile": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int, C.c_char_p, C.c_int64, _d, C.c_int, _i32]),
     "vfem_smoothing_filter": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp]),
+    "vfem_debug_pivot_reciprocals": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
     "vfem_smoothing_filter_noalloc": (C.c_int, [_i64, C.c_int, C.c_int, _vp, _vp, _vp]),
     "vfem_projection_apply": (C.c_int, [C.c_int64, C.c_double, _vp, _vp]),
     "vfem_projection_backprop": (C.c_int, [C.c_int64, C.c_double, _vp, _vp, _vp]),
@@ -139,6 +140,7 @@ _SIGS = {
     "vfem_problem_get_physical": (C.c_int, [_vp, _vp]),
     "vfem_problem_last_solve": (C.c_int, [_vp, C.POINTER(PcgStats)]),
     "vfem_problem_oc_step": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _i64]),
+    "vfem_problem_oc_step_with_gradient": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _vp, _i64]),
     # ---- 2D (bilinear quadrilaterals) ----
     "vfem_grid2_create": (C.c_int, [_i64, _d, _d, C.POINTER(_vp)]),
     "vfem_grid2_destroy": (C.c_int, [_vp]),

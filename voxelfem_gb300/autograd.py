@@ -107,6 +107,9 @@ class SolverContext:
 
     def load_dev(self):
         f = torch.empty(self.nc, self.nn, dtype=torch.float64, device=_DEV)
+        # the caching allocator may hand out a block that kernels queued on torch's stream
+        # still read; the library writes f on its own stream
+        _sync()
         _capi.check(self._load(self.sim._h, _p(f)))
         return f
 

@@ -511,7 +511,22 @@ __global__ void enforce_dirichlet_kernel(Geom g, T *__restrict__ u, const uint8_
         if ((dm >> c) & 1) u[c * g.ld + n] = dval ? (T)dval[c * g.ld + n] : T(0);
 }
 
+// The pivot reciprocals of the dense inverse applied elementwise (diagnostic).
+__global__ void newton_helpers_kernel(const double *__restrict__ d, int64_t n, double *__restrict__ recip,
+                                      double *__restrict__ rsqrt) {
+    const int64_t i = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (i >= n) return;
+    recip[i] = recip_newton(d[i]);
+    rsqrt[i] = rsqrt_newton(d[i]);
+}
+
 }  // namespace
+
+void launch_newton_helpers(const double *d, int64_t n, double *recip, double *rsqrt, cudaStream_t st) {
+    if (n <= 0) return;
+    newton_helpers_kernel<<<gridFor(n, BS), BS, 0, st>>>(d, n, recip, rsqrt);
+    VFEM_LAUNCH_CHECK();
+}
 
 template <typename T>
 void launch_dense_from_stencil(const Geom &g, const T *S, const int *redIdx, double *A, int nfree, bool rows,

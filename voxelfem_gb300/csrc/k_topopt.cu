@@ -80,65 +80,106 @@ __global__ void __launch_bounds__(BS) sum_kernel(const double *__restrict__ x, i
 // ---------------------------------------------------------------------------
 // Allocation-free variant of the density filter.
 //
-// For callers that cannot call cudaMalloc: code that captures the filter into its own CUDA
-// graph (allocation is illegal during stream capture), code running under a fixed device
-// memory budget or a caching allocator that must not be bypassed, and loops that cannot
-// afford the implicit device synchronisation of cudaMalloc/cudaFree (e.g. the tens of filter
-// applications of every OC bisection). The tap table lives in the file-scope array below,
-// which every GPU that loads this library holds until the process exits. Its size bounds the
-// filter radius to NOALLOC_MAX_RADIUS. Every call rewrites the table on the caller's stream,
-// so calls that overlap on the GPU (different streams) race on it.
+// For callers that cannot call cudaMalloc: code running under a fixed device-memory budget
+// or inside a host application that owns every device allocation (a plug-in that may only
+// use the buffers it is handed), and loops that cannot afford the implicit device
+// synchronisation of cudaMalloc/cudaFree (e.g. the tens of filter applications of every OC
+// bisection). The tap table lives in the file-scope array below, which every GPU that loads
+// this library holds until the process exits. Its size bounds the filter radius to
+// NOALLOC_MAX_RADIUS. Every call rewrites the table on the caller's stream, so calls that
+// overlap on the GPU (different streams) race on it.
+//
+// Layout: [0] total weight W, [1] number of positive taps, then NOALLOC_MAX_TAPS weights,
+// then the taps' offsets as 3 ints each. The taps keep the reference's lexicographic order
+// over [-r, r]^3 with the non-positive weights left out, as the allocating path's table does.
 // ---------------------------------------------------------------------------
 constexpr int NOALLOC_MAX_RADIUS = 6;
 constexpr int NOALLOC_MAX_TAPS = (2 * NOALLOC_MAX_RADIUS + 1) * (2 * NOALLOC_MAX_RADIUS + 1) *
                                  (2 * NOALLOC_MAX_RADIUS + 1);
-// [0] = total weight, then 4 doubles per candidate offset: dx, dy, dz, weight (0 if discarded)
-constexpr int NOALLOC_SCRATCH_DOUBLES = 1 + 4 * NOALLOC_MAX_TAPS;
+constexpr int NOALLOC_HEADER = 2;
+constexpr int NOALLOC_SCRATCH_DOUBLES = NOALLOC_HEADER + NOALLOC_MAX_TAPS + (3 * NOALLOC_MAX_TAPS + 1) / 2;
 static __device__ __align__(256) double g_filter_scratch[NOALLOC_SCRATCH_DOUBLES];
 
-// One thread writes the candidate offsets of [-r, r]^3 in the reference's lexicographic order
-// with weight max(w, 0) and sums the positive weights in that same order.
-__global__ void noalloc_taps_kernel(int radius, int type, double *scratch) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+constexpr int TAPS_BS = 1024;
+
+// One thread per candidate offset computes its weight; an ordered block-wide prefix count
+// places the positive ones in lexicographic order. W is then summed by one warp in a fixed
+// order (each lane a contiguous run of taps, then the 32 partial sums in lane order), so the
+// result is deterministic and within a few units in the last place of the allocating path's
+// sequential sum (a single FP64 chain of up to 2197 dependent adds would be ~70 us here).
+__global__ void __launch_bounds__(TAPS_BS) noalloc_taps_kernel(int radius, int type, double *scratch) {
+    __shared__ int warpCount[TAPS_BS / 32];
+    __shared__ int runBase;
+    const int side = 2 * radius + 1, ncand = side * side * side;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double *wts = scratch + NOALLOC_HEADER;
+    int *offs = reinterpret_cast<int *>(wts + NOALLOC_MAX_TAPS);
     const double rp1 = 1.0 + radius;
-    double W = 0.0;
-    int q = 0;
-    for (int a = -radius; a <= radius; ++a)
-        for (int b = -radius; b <= radius; ++b)
-            for (int c = -radius; c <= radius; ++c, ++q) {
-                double w = type == 1 ? rp1 - sqrt((double)(a * a + b * b + c * c)) : 1.0;
-                if (!(w > 0)) w = 0.0;
-                else W += w;
-                double *t = scratch + 1 + 4 * q;
-                t[0] = a;
-                t[1] = b;
-                t[2] = c;
-                t[3] = w;
-            }
-    scratch[0] = W;
+    if (threadIdx.x == 0) runBase = 0;
+    __syncthreads();
+    for (int base = 0; base < ncand; base += TAPS_BS) {
+        const int q = base + (int)threadIdx.x;
+        int a = 0, b = 0, c = 0;
+        double w = 0.0;
+        if (q < ncand) {
+            a = q / (side * side) - radius;
+            b = (q / side) % side - radius;
+            c = q % side - radius;
+            w = type == 1 ? rp1 - sqrt((double)(a * a + b * b + c * c)) : 1.0;
+        }
+        const bool keep = q < ncand && w > 0;
+        const unsigned ball = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) warpCount[warp] = __popc(ball);
+        __syncthreads();
+        int before = runBase;
+        for (int v = 0; v < warp; ++v) before += warpCount[v];
+        before += __popc(ball & ((1u << lane) - 1u));
+        if (keep) {
+            wts[before] = w;
+            offs[3 * before] = a;
+            offs[3 * before + 1] = b;
+            offs[3 * before + 2] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int v = 0; v < TAPS_BS / 32; ++v) tot += warpCount[v];
+            runBase += tot;
+        }
+        __syncthreads();
+    }
+    if (warp == 0) {
+        const int ntaps = runBase;
+        const int per = (ntaps + 31) / 32;
+        double part = 0.0;
+        for (int t = lane * per; t < min(ntaps, (lane + 1) * per); ++t) part += wts[t];
+        double W = 0.0;
+        for (int v = 0; v < 32; ++v) W += __shfl_sync(0xffffffffu, part, v);
+        if (lane == 0) {
+            scratch[0] = W;
+            scratch[1] = (double)ntaps;
+        }
+    }
 }
 
-// Zero-weight candidates add exactly 0 to the accumulator, so the sum equals the one over the
-// positive taps only (the allocating entry point's compacted table).
 __global__ void __launch_bounds__(BS) smoothing_filter_noalloc_kernel(int d0, int d1, int d2,
                                                                       const double *__restrict__ in,
                                                                       double *__restrict__ out,
-                                                                      const double *__restrict__ scratch,
-                                                                      int ncand) {
+                                                                      const double *__restrict__ scratch) {
     const int64_t e = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (e >= (int64_t)d0 * d1 * d2) return;
     const int k = (int)(e % d2);
     const int64_t t = e / d2;
     const int j = (int)(t % d1), i = (int)(t / d1);
+    const double *wts = scratch + NOALLOC_HEADER;
+    const int *offs = reinterpret_cast<const int *>(wts + NOALLOC_MAX_TAPS);
+    const int ntaps = __double2int_rn(scratch[1]);
     double acc = 0.0;
-    for (int q = 0; q < ncand; ++q) {
-        const double *tp = scratch + 1 + 4 * q;
-        const double w = tp[3];
-        if (w == 0.0) continue;
-        const int ni = reflect_index(i + (int)tp[0], d0);
-        const int nj = reflect_index(j + (int)tp[1], d1);
-        const int nk = reflect_index(k + (int)tp[2], d2);
-        acc += w * in[((int64_t)ni * d1 + nj) * d2 + nk];
+    for (int q = 0; q < ntaps; ++q) {
+        const int ni = reflect_index(i + offs[3 * q], d0);
+        const int nj = reflect_index(j + offs[3 * q + 1], d1);
+        const int nk = reflect_index(k + offs[3 * q + 2], d2);
+        acc += wts[q] * in[((int64_t)ni * d1 + nj) * d2 + nk];
     }
     out[e] = acc / scratch[0];
 }
@@ -242,12 +283,10 @@ void launch_smoothing_filter_noalloc(const int dims[3], int radius, int type, co
         throw Error(ERR_ARG, "filter radius " + std::to_string(radius) + " exceeds the maximum " +
                                  std::to_string(NOALLOC_MAX_RADIUS) + " of the allocation-free filter");
     double *scratch = noalloc_scratch_address();
-    const int ncand = (2 * radius + 1) * (2 * radius + 1) * (2 * radius + 1);
-    noalloc_taps_kernel<<<1, 32, 0, st>>>(radius, type, scratch);
+    noalloc_taps_kernel<<<1, TAPS_BS, 0, st>>>(radius, type, scratch);
     VFEM_LAUNCH_CHECK();
     const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
-    smoothing_filter_noalloc_kernel<<<gridFor(n, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], in, out, scratch,
-                                                                    ncand);
+    smoothing_filter_noalloc_kernel<<<gridFor(n, BS), BS, 0, st>>>(dims[0], dims[1], dims[2], in, out, scratch);
     VFEM_LAUNCH_CHECK();
 }
 

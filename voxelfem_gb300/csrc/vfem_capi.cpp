@@ -275,6 +275,23 @@ int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, in
         *ok = tc_fit_k0(k0_576, scale, tiles_2048) ? 1 : 0;
     });
 }
+int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, double *rsqrt_out) {
+    return guarded([&] {
+        need(d, "d");
+        need(recip_out, "recip");
+        need(rsqrt_out, "rsqrt");
+        if (n < 0) throw Error(ERR_ARG, "Invalid input size");
+        if (n == 0) return;
+        cudaStream_t st = nullptr;
+        View vi, vr, vs;
+        viewIn(vi, d, n * sizeof(double), st);
+        viewOut(vr, recip_out, n * sizeof(double));
+        viewOut(vs, rsqrt_out, n * sizeof(double));
+        launch_newton_helpers((const double *)vi.d, n, (double *)vr.d, (double *)vs.d, st);
+        finishOut(vr, st);
+        finishOut(vs, st);
+    });
+}
 int vfem_mg_set_device_loop(vfem_mg *mg, int on) {
     return guarded([&] {
         need(mg, "mg");
@@ -528,6 +545,15 @@ int vfem_problem_oc_step(vfem_problem *p, double m, double pexp, double ctol, in
     return guarded([&] {
         need(p, "problem");
         const int64_t n = p->p.ocStep(m, pexp, ctol);
+        if (probes) *probes = n;
+    });
+}
+int vfem_problem_oc_step_with_gradient(vfem_problem *p, double m, double pexp, double ctol,
+                                       const double *objective_gradient, int64_t *probes) {
+    return guarded([&] {
+        need(p, "problem");
+        need(objective_gradient, "objective gradient");
+        const int64_t n = p->p.ocStep(m, pexp, ctol, objective_gradient);
         if (probes) *probes = n;
     });
 }

@@ -1581,11 +1581,14 @@ double Problem::constraintAtVars(const double *x) {
 }
 
 // OptimalityCriterion.hh:51-138
-int64_t Problem::ocStep(double m, double p, double ctol) {
+int64_t Problem::ocStep(double m, double p, double ctol, const double *objectiveGradient) {
     if (!varsSet) throw Error(ERR_STATE, "Must call setVars first!");
     cudaStream_t st = be->stream();
     const int64_t ne = be->numElems();
-    gradientDev(dJ.p);
+    if (objectiveGradient)
+        VFEM_CUDA(cudaMemcpyAsync(dJ.p, objectiveGradient, ne * sizeof(double), cudaMemcpyDefault, st));
+    else
+        gradientDev(dJ.p);
     jacobianDev(dc.p);
     VFEM_CUDA(cudaMemcpyAsync(x0.p, vars[0].p, ne * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int64_t probes = 0;

@@ -341,7 +341,9 @@ public:
     void gradient(double *out, bool device);
     double constraint();
     void jacobian(double *out, bool device);
-    int64_t ocStep(double m, double p, double ctol);
+    // objectiveGradient (host or device, numVars doubles): use it instead of evaluating the
+    // objective gradient (a gradient computed elsewhere, e.g. by an autograd backward)
+    int64_t ocStep(double m, double p, double ctol, const double *objectiveGradient = nullptr);
     void getU(double *out, bool device);
     void getPhysical(double *out, bool device);
     void filterApply(const double *x_dev, double *out_dev);

@@ -178,6 +178,9 @@ constexpr int DENSE_TILE = 16;
 inline size_t dense_inverse_work_size(int n) {
     return (size_t)n * n + (size_t)DENSE_TILE * DENSE_TILE * ((n + DENSE_TILE - 1) / DENSE_TILE);
 }
+// 1/d and 1/sqrt(d) through the dense inverse's pivot helpers (single-precision seed and two
+// Newton-Raphson steps), elementwise; a diagnostic of their accuracy.
+void launch_newton_helpers(const double *d, int64_t n, double *recip, double *rsqrt, cudaStream_t st);
 void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
                        const std::function<void(const std::string &)> &mark = nullptr);
 // x = A^{-1} b on the free DOFs (nfreeDev[0] of them, at most nfreeCap), zero elsewhere.

@@ -1240,10 +1240,30 @@ class OCOptimizer:
         self.problem = problem
         self.lastProbes = 0
 
-    def step(self, m=0.2, p=0.5, ctol=1e-6, inplace=True):
+    def step(self, m=0.2, p=0.5, ctol=1e-6, inplace=True, objectiveGradient=None):
+        """One OC step. ``objectiveGradient`` (optional, not in the reference): a gradient of the
+        objective with respect to the design variables computed elsewhere (a numpy array, or a
+        CUDA float64 tensor passed as a device pointer), used instead of
+        evaluateObjectiveGradient."""
         probes = C.c_int64()
         self.problem._sync_solver()
-        check(_lib().vfem_problem_oc_step(self.problem._h, float(m), float(p), float(ctol), C.byref(probes)))
+        if objectiveGradient is None:
+            check(_lib().vfem_problem_oc_step(self.problem._h, float(m), float(p), float(ctol), C.byref(probes)))
+        else:
+            g = objectiveGradient
+            if hasattr(g, "data_ptr"):
+                if g.numel() != self.problem.numVars() or not g.is_contiguous():
+                    raise RuntimeError("Invalid input size")
+                import torch
+                torch.cuda.current_stream().synchronize()
+                gp = C.c_void_p(g.data_ptr())
+            else:
+                g = np.ascontiguousarray(g, dtype=np.float64)
+                if g.size != self.problem.numVars():
+                    raise RuntimeError("Invalid input size")
+                gp = g.ctypes.data_as(C.c_void_p)
+            check(_lib().vfem_problem_oc_step_with_gradient(self.problem._h, float(m), float(p), float(ctol), gp,
+                                                            C.byref(probes)))
         self.lastProbes = probes.value
         self.problem.filterChain.setDesignVars(self.problem.getVars())
 
