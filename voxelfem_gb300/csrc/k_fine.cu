@@ -10,6 +10,8 @@
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 
+#include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 namespace vfem {
@@ -362,6 +364,39 @@ __device__ __forceinline__ void gs_visit_planes(const KV &K, const T (&Plo)[9][3
         for (int c = 0; c < 3; ++c) M[3 * r + c] += e * K(3 * LN + r, 3 * LN + c);
 }
 
+// FP32 block Gauss-Seidel update of node (i, j, k) from its register neighbourhood (incident
+// elements in elementsAdjacentNode order, TPSStencils.hh:47-73; node solve
+// MultigridSolver.hh:348-378). Shared by the per-colour and the plane-pair sweeps, so both give
+// bit-identical iterates.
+template <typename KV>
+__device__ __forceinline__ void gs_node_fp32(const Geom &g, const KV &Kv, const float *__restrict__ Y, float *u,
+                                             const float *__restrict__ b, const uint8_t *__restrict__ dmask, int i,
+                                             int j, int k, bool forward) {
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    float s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    float M[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float E[8], Pa[9][3], Pb[9][3];
+    load_elem_moduli<float>(g, Y, i, j, k, E);
+    load_plane<float>(g, u, n, 0, Pa);
+    load_plane<float>(g, u, n, 1, Pb);
+    gs_visit_planes<float, 1, 1, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 0, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 1, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 0, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    float u0 = Pb[4][0], u1 = Pb[4][1], u2 = Pb[4][2];
+    load_plane<float>(g, u, n, 2, Pa);
+    gs_visit_planes<float, 0, 1, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 0, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 1, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 0, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    smooth_node_solve<float>(dm, s0, s1, s2, M, forward, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
 // One colour (x%2, y%2, z%2) = (cx, cy, cz) of multicoloured block Gauss-Seidel
 // (MultigridSolver.hh:409-458); incident elements in elementsAdjacentNode order
 // (TPSStencils.hh:47-73).
@@ -378,33 +413,15 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kern
     decode3(t, n1, n2, ii, jj, kk);
     const int i = cx + 2 * ii, j = cy + 2 * jj, k = cz + 2 * kk;
     if (j >= g.nyv()) return;
+    if constexpr (sizeof(T) == 4) {
+        gs_node_fp32(g, K0View<T, Cube>(K), Y, u, b, dmask, i, j, k, forward != 0);
+        return;
+    }
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const uint8_t dm = dmask[n];
     if (dm == 7) return;
     T s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
     T M[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-    if constexpr (sizeof(T) == 4) {
-        const K0View<T, Cube> Kv(K);
-        T E[8], Pa[9][3], Pb[9][3];
-        load_elem_moduli<T>(g, Y, i, j, k, E);
-        load_plane<T>(g, u, n, 0, Pa);
-        load_plane<T>(g, u, n, 1, Pb);
-        gs_visit_planes<T, 1, 1, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
-        gs_visit_planes<T, 1, 0, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
-        gs_visit_planes<T, 1, 1, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
-        gs_visit_planes<T, 1, 0, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
-        T u0 = Pb[4][0], u1 = Pb[4][1], u2 = Pb[4][2];
-        load_plane<T>(g, u, n, 2, Pa);
-        gs_visit_planes<T, 0, 1, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
-        gs_visit_planes<T, 0, 0, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
-        gs_visit_planes<T, 0, 1, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
-        gs_visit_planes<T, 0, 0, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
-        smooth_node_solve<T>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
-        u[n] = u0;
-        u[ld + n] = u1;
-        u[2 * ld + n] = u2;
-        return;
-    }
     gs_visit<T, 1, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
     gs_visit<T, 0, 1, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
     gs_visit<T, 1, 0, 1>(g, K, Y, u, i, j, k, s0, s1, s2, M);
@@ -418,6 +435,51 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 3 : 1) gs_fine_color_kern
     u[n] = u0;
     u[ld + n] = u1;
     u[2 * ld + n] = u2;
+}
+
+// Barrier over the CTAs of one thread-block cluster with release / acquire semantics: the u
+// updates of one sub-colour (global stores) are visible to every CTA of the cluster before any
+// of them gathers the next sub-colour's neighbourhoods.
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Plane-pair sweep: the four colours with x % 2 == cx in one launch. The stencil reaches only
+// x +- 1, so while those colours run every x-plane of parity cx reads planes of the other parity
+// (not updated in this launch) and its own: the planes are independent and the launch runs them
+// all at once, one thread-block cluster per plane. Inside a plane the four colours (y % 2,
+// z % 2) follow the reference's order (forward 0 -> 3, backward 3 -> 0) separated by cluster
+// barriers; each CTA of the cluster owns a strip of rowsPerStrip y-rows. A sweep is two such
+// launches (cx = 0 then 1 forward; 1 then 0 backward): the same node updates with the same
+// operands as eight colour launches, so the iterates are identical, but u, E and b stream
+// through DRAM about twice per sweep instead of once per colour.
+template <bool Cube>
+__global__ void __launch_bounds__(BS, 3) gs_fine_planes_kernel(Geom g, const float *__restrict__ Y, float *u,
+                                                              const float *__restrict__ b,
+                                                              const uint8_t *__restrict__ dmask, int cx,
+                                                              int rowsPerStrip, int forward, const Mat24<float> K) {
+    VFEM_PDL_ENTRY();
+    const int i = cx + 2 * (int)blockIdx.y;
+    const int j0 = (int)blockIdx.x * rowsPerStrip;
+    const int j1 = min(j0 + rowsPerStrip, g.nyv());
+    const K0View<float, Cube> Kv(K);
+#pragma unroll 1
+    for (int s = 0; s < 4; ++s) {
+        const int sc = forward ? s : 3 - s;
+        const int cy = sc >> 1, cz = sc & 1;
+        const int jf = j0 + ((j0 & 1) != cy ? 1 : 0);
+        const int nj = j1 > jf ? (j1 - jf + 1) / 2 : 0;
+        const int nk = (g.nn[2] - cz + 1) / 2;
+        const int cnt = nj * nk;
+        for (int t = threadIdx.x; t < cnt; t += BS) {
+            const int jj = (int)((uint32_t)t / (uint32_t)nk), kk = t - jj * nk;
+            gs_node_fp32(g, Kv, Y, u, b, dmask, i, jf + 2 * jj, cz + 2 * kk, forward != 0);
+        }
+        if (s < 3) {
+            if (gridDim.x > 1) cluster_barrier();
+            else __syncthreads();
+        }
+    }
 }
 
 // ---------------- double-float FP64-accurate matvec ----------------
@@ -719,6 +781,57 @@ void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *
                           const uint8_t *dmask, cudaStream_t st) {
     if (sizeof(T) == 4 && K0.isCube) launch_pdl(residual_fine_kernel<T, true>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
     else launch_pdl(residual_fine_kernel<T, false>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
+    VFEM_LAUNCH_CHECK();
+}
+
+// Strips per x-plane (the cluster size) of the plane-pair sweep: about three resident CTAs per SM
+// over the planes of one parity, at most 8 (the portable cluster size) and at least two rows per
+// strip.
+static int gsPlaneStrips(const Geom &g) {
+    const int planes = (g.nn[0] + 1) / 2;
+    int c = (3 * NUM_SMS + planes / 2) / planes;
+    c = std::max(1, std::min(c, 8));
+    while (c > 1 && (g.nn[1] + c - 1) / c < 2) --c;
+    return c;
+}
+
+bool gsPlanesEnabled() {
+    const char *e = std::getenv("VFEM_GS_PLANES");
+    return !(e && e[0] == '0');
+}
+
+void launch_gs_fine_planes(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                           bool forward, const Mat24<float> &K0, cudaStream_t st) {
+    const int planes = (g.nn[0] - cx + 1) / 2;
+    if (planes <= 0) return;
+    const int strips = gsPlaneStrips(g);
+    const int rows = (g.nn[1] + strips - 1) / strips;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(strips, planes, 1);
+    cfg.blockDim = dim3(BS, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    int na = 0;
+    attr[na].id = cudaLaunchAttributeClusterDimension;
+    attr[na].val.clusterDim.x = strips;
+    attr[na].val.clusterDim.y = 1;
+    attr[na].val.clusterDim.z = 1;
+    ++na;
+    if (pdlEnabled()) {
+        attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    cfg.attrs = attr;
+    cfg.numAttrs = na;
+    const int fw = forward ? 1 : 0;
+    if (K0.isCube)
+        cudaCheck(cudaLaunchKernelEx(&cfg, gs_fine_planes_kernel<true>, g, Y, u, b, dmask, cx, rows, fw, K0),
+                  "kernel launch");
+    else
+        cudaCheck(cudaLaunchKernelEx(&cfg, gs_fine_planes_kernel<false>, g, Y, u, b, dmask, cx, rows, fw, K0),
+                  "kernel launch");
     VFEM_LAUNCH_CHECK();
 }
 

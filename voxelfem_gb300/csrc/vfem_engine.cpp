@@ -745,6 +745,15 @@ void MG::smoothT(int l, bool forward) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+    if constexpr (std::is_same<T, float>::value) {
+        if (l == 0 && gsPlanesEnabled()) {
+            // two launches: the x-even colours then the x-odd ones (reversed backward)
+            for (int h = 0; h < 2; ++h)
+                launch_gs_fine_planes(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, forward ? h : 1 - h, forward,
+                                      Tr<T>::K0(*fine), st);
+            return;
+        }
+    }
     for (int c = 0; c < 8; ++c) {
         const int color = forward ? c : 7 - c;
         if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);

@@ -77,6 +77,12 @@ template <typename T>
 void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
                           const uint8_t *dmask, cudaStream_t st);
 // One colour pass of block Gauss-Seidel on the fine level.
+// One FP32 fine sweep's four colours with x % 2 == cx (all x-planes of that parity at once, one
+// thread-block cluster per plane); identical iterates to the four colour launches.
+void launch_gs_fine_planes(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                           bool forward, const Mat24<float> &K0, cudaStream_t st);
+// The plane-pair sweep is used unless VFEM_GS_PLANES=0 (then eight colour launches per sweep).
+bool gsPlanesEnabled();
 template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                           const Mat24<T> &K0, cudaStream_t st);
