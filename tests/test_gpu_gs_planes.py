@@ -39,9 +39,9 @@ def _solve(monkeypatch, planes, ne, levels, bbox=None, mask_layer=None, partial=
 
 @pytest.mark.parametrize("ne,levels,kw", [
     ((16, 8, 8), 2, {}),
-    ((33, 20, 17), 2, {}),
+    ((36, 28, 20), 2, {}),
     ((64, 32, 32), 3, {}),
-    ((24, 21, 10), 2, {"partial": True}),
+    ((24, 20, 12), 2, {"partial": True}),
     ((16, 16, 8), 2, {"mask_layer": 9}),
     ((20, 12, 12), 2, {"bbox": [[0.0, 0.0, 0.0], [20.0, 6.0, 18.0]]}),
     ((16, 8, 8), 2, {"symmetric": False}),

@@ -451,10 +451,20 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     VFEM_CUDA(cudaMallocHost(&hostSc, 17 * sizeof(double)));  // [16]: coarse SPD flag
     std::memset(hostSc, 0, 17 * sizeof(double));
     setupCoarsestIndex();
+    if (const char *env = std::getenv("VFEM_OVERLAP_STIFFNESS")) overlapStiffness = env[0] != '0';
+    VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
+    VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
+    VFEM_CUDA(cudaEventCreateWithFlags(&evLevelsReady, cudaEventDisableTiming));
+    VFEM_CUDA(cudaEventCreateWithFlags(&evCoarseReady, cudaEventDisableTiming));
 }
 
 MG::~MG() {
     clearGraphs();
+    if (stiffStream) cudaStreamSynchronize(stiffStream);
+    if (evStiffFork) cudaEventDestroy(evStiffFork);
+    if (evLevelsReady) cudaEventDestroy(evLevelsReady);
+    if (evCoarseReady) cudaEventDestroy(evCoarseReady);
+    if (stiffStream) cudaStreamDestroy(stiffStream);
     if (hostSc) cudaFreeHost(hostSc);
     if (copyDone) cudaEventDestroy(copyDone);
     if (copyStream) cudaStreamDestroy(copyStream);
@@ -629,7 +639,7 @@ static void uploadConst(DevBuf<T> &dst, const double *src, size_t n) {
 // MultigridSolver.hh:846-905: element matrices level by level, assembled stencils for the
 // smoothing levels, and the dense inverse of the reduced coarsest operator.
 template <typename T>
-void MG::updateStiffnessT() {
+void MG::updateStiffnessT(bool overlap) {
     syncFineGeom(*this);
     allocLevels();
     cudaStream_t st = fine->stream;
@@ -651,7 +661,14 @@ void MG::updateStiffnessT() {
         }
         constVersion[std::is_same<T, double>::value ? 1 : 0] = constKey;
     }
-    const T *Y0 = Tr<T>::Y(*fine);
+    const T *Y0 = Tr<T>::Y(*fine);  // may enqueue the FP32 conversion on the solver stream
+    // gs: the stream the rebuild runs on (the side stream forks after everything it reads)
+    cudaStream_t gs = st;
+    if (overlap && !stiffMarks && L() > 1 && stiffStream) {
+        VFEM_CUDA(cudaEventRecord(evStiffFork, st));
+        VFEM_CUDA(cudaStreamWaitEvent(stiffStream, evStiffFork, 0));
+        gs = stiffStream;
+    }
     auto mark = [&](const std::string &name) {
         if (!stiffMarks) return;
         cudaEvent_t e;
@@ -680,56 +697,70 @@ void MG::updateStiffnessT() {
             if (l == 1) {
                 // the level-1 stencil comes straight from the fine moduli; no level-1 element
                 // matrices are stored
-                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, st);
+                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs);
                 mark("galerkin:L1 stencil");
             } else {
                 D.Ke.alloc((size_t)lv[l].g.NE * 576);
                 if (l == 2)
-                    launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, st);
+                    launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, gs);
                 else
                     launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p,
-                                         st);
+                                         gs);
                 mark("galerkin:L" + std::to_string(l) + " element matrices");
-                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, st);
+                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, gs);
                 mark("galerkin:L" + std::to_string(l) + " stencil");
             }
         }
     }
+    VFEM_CUDA(cudaEventRecord(evLevelsReady, gs));
     // dense reduced coarsest operator, FP64 inverse
     const Level &C = lv.back();
     if (nfree > 0) {
-        launch_dense_from_stencil<T>(C.g, lv.back().data<T>().S.p, redIdx.p, Ainv.p, nfree, lv.back().rows, st);
-        launch_symmetrize(Ainv.p, nfree, st);
-        VFEM_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+        launch_dense_from_stencil<T>(C.g, lv.back().data<T>().S.p, redIdx.p, Ainv.p, nfree, lv.back().rows, gs);
+        launch_symmetrize(Ainv.p, nfree, gs);
+        VFEM_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), gs));
         mark("coarsest:dense assembly");
-        if (stiffMarks) dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st, mark);
-        else dense_spd_inverse(Ainv.p, work.p, nfree, status.p, st);
+        if (stiffMarks) dense_spd_inverse(Ainv.p, work.p, nfree, status.p, gs, mark);
+        else dense_spd_inverse(Ainv.p, work.p, nfree, status.p, gs);
         // the positive-definiteness flag is read back once the stream reaches it
-        VFEM_CUDA(cudaMemcpyAsync(&hostSc[16], status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        VFEM_CUDA(cudaMemcpyAsync(&hostSc[16], status.p, sizeof(int), cudaMemcpyDeviceToHost, gs));
         spdCheckPending = true;
     }
+    VFEM_CUDA(cudaEventRecord(evCoarseReady, gs));
     stiffnessValid = true;
     stiffnessPrecision = precision;
     stiffnessDensVersion = fine->densVersion;
     stiffnessMaskVersion = fine->maskVersion;
 }
 
-void MG::updateStiffness() {
-    if (precision == PREC_FP64) updateStiffnessT<double>();
-    else updateStiffnessT<float>();
+void MG::updateStiffness(bool overlap) {
+    // a rebuild still in flight on the side stream finishes before this one starts
+    VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
+    if (precision == PREC_FP64) updateStiffnessT<double>(overlap);
+    else updateStiffnessT<float>(overlap);
+    if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
 }
 
-void MG::ensureStiffness(bool deferCheck) {
+void MG::waitStiffnessEvent(cudaEvent_t e) {
+    cudaStream_t st = fine->stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    VFEM_CUDA(cudaStreamIsCapturing(st, &cs));
+    VFEM_CUDA(cudaStreamWaitEvent(st, e, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0));
+}
+
+void MG::ensureStiffness(bool deferCheck, bool overlap) {
     syncFineGeom(*this);
     if (!stiffnessValid || stiffnessPrecision != precision || stiffnessDensVersion != fine->densVersion ||
         stiffnessMaskVersion != fine->maskVersion)
-        updateStiffness();
+        updateStiffness(overlap);
+    if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
     if (!deferCheck) checkStiffness();
 }
 
 // Raise the coarsest factorisation's positive-definiteness failure, if one is pending.
 void MG::checkStiffness() {
     if (!spdCheckPending) return;
+    VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
     VFEM_CUDA(cudaStreamSynchronize(fine->stream));
     spdCheckPending = false;
     int hs = 0;
@@ -780,6 +811,7 @@ template <typename T>
 void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
+    if (l == 1) waitStiffnessEvent(evLevelsReady);
     if (std::is_same<T, float>::value && residualSystem && l >= 1 && l == tailStart()) {
         // small levels: one CTA runs the down leg, the dense solve runs on the whole GPU,
         // one CTA runs the up leg
@@ -794,11 +826,13 @@ void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
         }
         launch_tail_down<T>(P, st);
         auto &Dc = lv.back().data<T>();
+        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
         launch_tail_up<T>(P, st);
         return;
     }
     if (l == L() - 1) {
+        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
@@ -821,6 +855,7 @@ void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (l == L() - 1) {
+        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
@@ -1040,6 +1075,18 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     if (pending) throw Error(ERR_STATE, "a solve is already in flight on this solver");
     cudaStream_t st = fine->stream;
     const Geom &g = lv[0].g;
+    if (precision == PREC_MIXED) {
+        fine->youngF();
+        fine->youngFPad();
+        const float *yh, *yl;
+        if (outerMatvec != MATVEC_FP64) fine->youngDF(&yh, &yl);
+        if (outerKind() == 2) umax.alloc(REDUCE_BLOCKS);
+    }
+    allocLevels();
+    // the hierarchy rebuild (if the densities or the mask changed) forks onto the side stream
+    // here; the solve's start below and the first V-cycle's fine level run meanwhile (positive
+    // definiteness is checked in pcgFinish)
+    if (mgIter > 0) ensureStiffness(true, overlapStiffness);
     if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
@@ -1050,15 +1097,6 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     launch_cg_init(sc.p, tol * tol, (double)maxIter, st);
     prepareFusedInit(mgIter, sweeps);
     launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
-    if (precision == PREC_MIXED) {
-        fine->youngF();
-        fine->youngFPad();
-        const float *yh, *yl;
-        if (outerMatvec != MATVEC_FP64) fine->youngDF(&yh, &yl);
-        if (outerKind() == 2) umax.alloc(REDUCE_BLOCKS);
-    }
-    allocLevels();
-    if (mgIter > 0) ensureStiffness(true);  // positive definiteness checked in pcgFinish
     pendingKey = GraphKey{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
     VFEM_CUDA(cudaGraphLaunch(loopGraph(pendingKey, x, mgIter, sweeps, fmg), st));
     pending = true;
@@ -1068,6 +1106,8 @@ PcgStats MG::pcgFinish() {
     if (!pending) throw Error(ERR_STATE, "no solve in flight");
     pending = false;
     cudaStream_t st = fine->stream;
+    // the solve may end before its first V-cycle reached the side-stream rebuild
+    VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));
     VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
     checkStiffness();  // synchronises the stream
     VFEM_CUDA(cudaStreamSynchronize(st));
@@ -1227,7 +1267,10 @@ PcgStats MG::pcg(double *x, const double *b, int64_t maxIter, double tol, int64_
         VFEM_CUDA(cudaMemcpyAsync(xbuf.p, x, bytes, cudaMemcpyDefault, copyStream));
         if (bHost) VFEM_CUDA(cudaMemcpyAsync(bbuf.p, b, bytes, cudaMemcpyHostToDevice, copyStream));
         VFEM_CUDA(cudaEventRecord(copyDone, copyStream));
-        ensureStiffness(true);
+        // the device-resident solve leaves the rebuild on the side stream (the V-cycle waits for
+        // it); every other path joins it here
+        const bool overlap = overlapStiffness && useGraphs && deviceLoop && !cb;
+        ensureStiffness(true, overlap);
         VFEM_CUDA(cudaStreamWaitEvent(st, copyDone, 0));
     } else {
         VFEM_CUDA(cudaMemcpyAsync(xbuf.p, x, bytes, cudaMemcpyDefault, st));

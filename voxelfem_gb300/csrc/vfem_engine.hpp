@@ -165,7 +165,18 @@ public:
     int L() const { return (int)lv.size(); }
     void setPrecision(int p);
     void setMaskLayer(int64_t l);
-    void updateStiffness();
+    // overlap: build on stiffStream (see below) instead of the solver stream
+    void updateStiffness(bool overlap = false);
+    // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (initial
+    // residual, first direction set-up) and the first V-cycle's fine-level work run while the
+    // Galerkin operators (evLevelsReady) and the coarsest dense inverse (evCoarseReady) are built;
+    // the V-cycle waits for each event just before its first use. VFEM_OVERLAP_STIFFNESS=0 keeps
+    // the rebuild on the solver stream.
+    cudaStream_t stiffStream = nullptr;
+    cudaEvent_t evStiffFork = nullptr, evLevelsReady = nullptr, evCoarseReady = nullptr;
+    bool overlapStiffness = true;
+    // the solver stream waits for e (an external-event wait node when the stream is capturing)
+    void waitStiffnessEvent(cudaEvent_t e);
 
     // per-level operations on caller FP64 vectors (level sizes)
     void applyK(int l, const double *u, double *out);
@@ -261,7 +272,7 @@ private:
     void coarsenDirichlet();
     void setupCoarsestIndex();
     template <typename T>
-    void updateStiffnessT();
+    void updateStiffnessT(bool overlap);
     template <typename T>
     void smoothT(int l, bool forward);
     template <typename T>
@@ -285,7 +296,8 @@ public:
     // One FP32 V-cycle on the fine level's right-hand side lv[0].d32.b (zero initial guess),
     // result in lv[0].d32.x (mixed precision; stiffness must be current).
     void vcycleOnFineRhs(int64_t sweeps);
-    void ensureStiffness(bool deferCheck = false);
+    // overlap = false joins any side-stream rebuild still in flight before returning
+    void ensureStiffness(bool deferCheck = false, bool overlap = false);
     void checkStiffness();
     bool spdCheckPending = false;
     uint64_t constVersion[2] = {0, 0};  // K0 version of the uploaded coarsening tables (FP32, FP64)
