@@ -741,13 +741,6 @@ void MG::updateStiffness(bool overlap) {
     if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
 }
 
-void MG::waitStiffnessEvent(cudaEvent_t e) {
-    cudaStream_t st = fine->stream;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    VFEM_CUDA(cudaStreamIsCapturing(st, &cs));
-    VFEM_CUDA(cudaStreamWaitEvent(st, e, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0));
-}
-
 void MG::ensureStiffness(bool deferCheck, bool overlap) {
     syncFineGeom(*this);
     if (!stiffnessValid || stiffnessPrecision != precision || stiffnessDensVersion != fine->densVersion ||
@@ -811,7 +804,6 @@ template <typename T>
 void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
-    if (l == 1) waitStiffnessEvent(evLevelsReady);
     if (std::is_same<T, float>::value && residualSystem && l >= 1 && l == tailStart()) {
         // small levels: one CTA runs the down leg, the dense solve runs on the whole GPU,
         // one CTA runs the up leg
@@ -826,13 +818,11 @@ void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
         }
         launch_tail_down<T>(P, st);
         auto &Dc = lv.back().data<T>();
-        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
         launch_tail_up<T>(P, st);
         return;
     }
     if (l == L() - 1) {
-        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
@@ -855,7 +845,6 @@ void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (l == L() - 1) {
-        waitStiffnessEvent(evCoarseReady);
         launch_coarse_solve<T>(lv[l].g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, D.b.p, D.x.p, cscratch.p, st);
         return;
     }
@@ -1084,8 +1073,8 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     }
     allocLevels();
     // the hierarchy rebuild (if the densities or the mask changed) forks onto the side stream
-    // here; the solve's start below and the first V-cycle's fine level run meanwhile (positive
-    // definiteness is checked in pcgFinish)
+    // here and the solve's start below runs meanwhile (positive definiteness is checked in
+    // pcgFinish)
     if (mgIter > 0) ensureStiffness(true, overlapStiffness);
     if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
@@ -1098,7 +1087,9 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     prepareFusedInit(mgIter, sweeps);
     launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
     pendingKey = GraphKey{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
-    VFEM_CUDA(cudaGraphLaunch(loopGraph(pendingKey, x, mgIter, sweeps, fmg), st));
+    cudaGraphExec_t exec = loopGraph(pendingKey, x, mgIter, sweeps, fmg);
+    VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));  // join the side-stream rebuild
+    VFEM_CUDA(cudaGraphLaunch(exec, st));
     pending = true;
 }
 
@@ -1106,8 +1097,6 @@ PcgStats MG::pcgFinish() {
     if (!pending) throw Error(ERR_STATE, "no solve in flight");
     pending = false;
     cudaStream_t st = fine->stream;
-    // the solve may end before its first V-cycle reached the side-stream rebuild
-    VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));
     VFEM_CUDA(cudaMemcpyAsync(hostSc, sc.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
     checkStiffness();  // synchronises the stream
     VFEM_CUDA(cudaStreamSynchronize(st));
@@ -1267,8 +1256,8 @@ PcgStats MG::pcg(double *x, const double *b, int64_t maxIter, double tol, int64_
         VFEM_CUDA(cudaMemcpyAsync(xbuf.p, x, bytes, cudaMemcpyDefault, copyStream));
         if (bHost) VFEM_CUDA(cudaMemcpyAsync(bbuf.p, b, bytes, cudaMemcpyHostToDevice, copyStream));
         VFEM_CUDA(cudaEventRecord(copyDone, copyStream));
-        // the device-resident solve leaves the rebuild on the side stream (the V-cycle waits for
-        // it); every other path joins it here
+        // the device-resident solve leaves the rebuild on the side stream (joined before its
+        // graph launch); every other path joins it here
         const bool overlap = overlapStiffness && useGraphs && deviceLoop && !cb;
         ensureStiffness(true, overlap);
         VFEM_CUDA(cudaStreamWaitEvent(st, copyDone, 0));

@@ -167,16 +167,15 @@ public:
     void setMaskLayer(int64_t l);
     // overlap: build on stiffStream (see below) instead of the solver stream
     void updateStiffness(bool overlap = false);
-    // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (initial
-    // residual, first direction set-up) and the first V-cycle's fine-level work run while the
-    // Galerkin operators (evLevelsReady) and the coarsest dense inverse (evCoarseReady) are built;
-    // the V-cycle waits for each event just before its first use. VFEM_OVERLAP_STIFFNESS=0 keeps
-    // the rebuild on the solver stream.
+    // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (the
+    // initial residual through the outer matvec, its norms, the first preconditioner input) runs
+    // on the solver stream while the Galerkin operators (evLevelsReady) and the coarsest dense
+    // inverse (evCoarseReady) are built, and the solve's graph waits for evCoarseReady. (The wait
+    // cannot sit inside the device-side WHILE loop, whose body admits no event nodes.)
+    // VFEM_OVERLAP_STIFFNESS=0 keeps the rebuild on the solver stream.
     cudaStream_t stiffStream = nullptr;
     cudaEvent_t evStiffFork = nullptr, evLevelsReady = nullptr, evCoarseReady = nullptr;
     bool overlapStiffness = true;
-    // the solver stream waits for e (an external-event wait node when the stream is capturing)
-    void waitStiffnessEvent(cudaEvent_t e);
 
     // per-level operations on caller FP64 vectors (level sizes)
     void applyK(int l, const double *u, double *out);
