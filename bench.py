@@ -403,14 +403,15 @@ def run_ours(args):
         _capi.check(lib.vfem_mg_time_kernel(mg._h, kid, reps, C.byref(ms), C.byref(nbytes)))
         kernels[KERNEL_NAMES[kid]] = {"ms": ms.value, "bytes": nbytes.value,
                                       "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
-    # the same fine sweep as eight colour launches (one per colour of the reference's order) for
-    # comparison with the plane-pair form the solve uses (two launches)
-    os.environ["VFEM_GS_PLANES"] = "0"
-    ms, nbytes = C.c_double(), C.c_double()
-    _capi.check(lib.vfem_mg_time_kernel(mg._h, 3, 20, C.byref(ms), C.byref(nbytes)))
-    del os.environ["VFEM_GS_PLANES"]
-    kernels["gs_fine_sweep_fp32_colour_launches"] = {"ms": ms.value, "bytes": nbytes.value,
-                                                     "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
+    # the other forms of the fine sweep (the solve uses the default one): eight colour launches
+    # (one per colour of the reference's order), two plane-pair launches (one cluster per x-plane)
+    for mode in ("colours", "planes", "lines"):
+        os.environ["VFEM_GS_MODE"] = mode
+        ms, nbytes = C.c_double(), C.c_double()
+        _capi.check(lib.vfem_mg_time_kernel(mg._h, 3, 20, C.byref(ms), C.byref(nbytes)))
+        kernels["gs_fine_sweep_fp32_" + mode] = {"ms": ms.value, "bytes": nbytes.value,
+                                                  "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
+    del os.environ["VFEM_GS_MODE"]
     # launches per PCG iteration of the hot kernels of the mixed solve (2 pre + 2 post sweeps per level)
     outer_name = "applyk_fine_tc" if outer_kind == "tensor" else "applyk_fine_df"
     per_iter_launches = {outer_name: 1, "gs_fine_sweep_fp32": 4, "residual_fine_fp32": 1,

@@ -1,11 +1,14 @@
-"""The plane-pair FP32 fine sweep (two launches per sweep: all x-even planes, then all x-odd
-planes, one thread-block cluster per plane running its four (y, z) colours between cluster
-barriers) against the eight colour launches of the reference's order (MultigridSolver.hh:409-458).
+"""The fused forms of the FP32 fine sweep against the eight colour launches of the reference's
+order (MultigridSolver.hh:409-458):
+- line pairs: four launches per sweep, each running two colours adjacent in the order, (x, y)
+  parity fixed and z parity 0 then 1, on whole z-lines per CTA with a block barrier between;
+- plane pairs: two launches per sweep, all x-even planes then all x-odd planes, one thread-block
+  cluster per plane running its four (y, z) colours between cluster barriers.
 
-Both run the same node updates on the same operands in the same order, so mixed-precision solves
-whose V-cycles use one or the other give bit-identical iterates: pre- and post-smoothing
-(forward and colour-reversed), odd and even plane counts, strips of one to eight CTAs, detached
-rows (layer-by-layer masks), partially constrained nodes and non-cube voxels.
+All forms run the same node updates on the same operands in the same order, so mixed-precision
+solves whose V-cycles use one or another give bit-identical iterates: pre- and post-smoothing
+(forward and colour-reversed), odd and even plane and line counts, detached rows (layer-by-layer
+masks), partially constrained nodes and non-cube voxels.
 """
 import numpy as np
 import pytest
@@ -16,8 +19,8 @@ from voxelfem_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-def _solve(monkeypatch, planes, ne, levels, bbox=None, mask_layer=None, partial=False, symmetric=True):
-    monkeypatch.setenv("VFEM_GS_PLANES", "1" if planes else "0")
+def _solve(monkeypatch, mode, ne, levels, bbox=None, mask_layer=None, partial=False, symmetric=True):
+    monkeypatch.setenv("VFEM_GS_MODE", mode)
     if bbox is None:
         bbox = [[0.0, 0.0, 0.0], [float(v) for v in ne]]
     g = pv.TensorProductSimulator([1, 1, 1], bbox, ne)
@@ -47,8 +50,9 @@ def _solve(monkeypatch, planes, ne, levels, bbox=None, mask_layer=None, partial=
     ((16, 8, 8), 2, {"symmetric": False}),
     ((128, 48, 40), 3, {}),
 ])
-def test_plane_pair_sweep_equals_colour_sweeps(gpu, monkeypatch, ne, levels, kw):
-    xa, ia = _solve(monkeypatch, False, ne, levels, **kw)
-    xb, ib = _solve(monkeypatch, True, ne, levels, **kw)
-    assert ia == ib
-    np.testing.assert_array_equal(xa, xb)
+def test_fused_sweeps_equal_colour_sweeps(gpu, monkeypatch, ne, levels, kw):
+    xa, ia = _solve(monkeypatch, "colours", ne, levels, **kw)
+    for mode in ("lines", "planes"):
+        xb, ib = _solve(monkeypatch, mode, ne, levels, **kw)
+        assert ia == ib, mode
+        np.testing.assert_array_equal(xa, xb, err_msg=mode)

@@ -482,6 +482,41 @@ __global__ void __launch_bounds__(BS, 3) gs_fine_planes_kernel(Geom g, const flo
     }
 }
 
+// Line-pair sweep: colours (cx, cy, 0) and (cx, cy, 1), adjacent in the reference's order, in
+// one launch. Their nodes lie on the z-lines i % 2 == cx, j % 2 == cy, and among the nodes these
+// two colours update a node reads only its own line's (k +- 1): the lines are independent. A CTA
+// owns linesPerCta whole lines, updates the first colour's nodes on them, passes a block barrier,
+// then updates the second colour's (z parity 0 then 1 forward, 1 then 0 backward). A sweep is
+// four such launches; the node updates and their operands are those of the eight colour
+// launches, so the iterates are identical.
+template <bool Cube>
+__global__ void __launch_bounds__(BS, 3) gs_fine_lines_kernel(Geom g, const float *__restrict__ Y, float *u,
+                                                             const float *__restrict__ b,
+                                                             const uint8_t *__restrict__ dmask, int cx, int cy,
+                                                             int linesPerCta, int forward, const Mat24<float> K) {
+    VFEM_PDL_ENTRY();
+    const int n1 = (g.nn[1] - cy + 1) / 2;  // lines of this class per x-plane
+    const int nlines = ((g.nn[0] - cx + 1) / 2) * n1;
+    const int l0 = (int)blockIdx.x * linesPerCta;
+    const int nl = min(linesPerCta, nlines - l0);
+    const int nyv = g.nyv();
+    const K0View<float, Cube> Kv(K);
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        const int cz = forward ? s : 1 - s;
+        const int nk = (g.nn[2] - cz + 1) / 2;
+        const int cnt = nl > 0 ? nl * nk : 0;
+        for (int t = threadIdx.x; t < cnt; t += BS) {
+            const int q = (int)((uint32_t)t / (uint32_t)nk), kk = t - q * nk;
+            const int line = l0 + q;
+            const int ii = (int)((uint32_t)line / (uint32_t)n1), jj = line - ii * n1;
+            const int j = cy + 2 * jj;
+            if (j < nyv) gs_node_fp32(g, Kv, Y, u, b, dmask, cx + 2 * ii, j, cz + 2 * kk, forward != 0);
+        }
+        if (s == 0) __syncthreads();
+    }
+}
+
 // ---------------- double-float FP64-accurate matvec ----------------
 template <int LN, typename KV>
 __device__ __forceinline__ void df_elem(const Geom &g, const KV &K, const float *__restrict__ uh_,
@@ -788,16 +823,39 @@ void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *
 // over the planes of one parity, at most 8 (the portable cluster size) and at least two rows per
 // strip.
 static int gsPlaneStrips(const Geom &g) {
+    if (const char *e = std::getenv("VFEM_GS_PLANE_STRIPS")) {
+        const int c = std::atoi(e);
+        if (c >= 1 && c <= 8) return std::min(c, std::max(1, g.nn[1] / 2));
+    }
     const int planes = (g.nn[0] + 1) / 2;
-    int c = (3 * NUM_SMS + planes / 2) / planes;
+    int c = (3 * NUM_SMS) / planes;  // one wave of three CTAs per SM
     c = std::max(1, std::min(c, 8));
     while (c > 1 && (g.nn[1] + c - 1) / c < 2) --c;
     return c;
 }
 
-bool gsPlanesEnabled() {
-    const char *e = std::getenv("VFEM_GS_PLANES");
-    return !(e && e[0] == '0');
+int gsFineMode() {
+    const char *e = std::getenv("VFEM_GS_MODE");
+    if (!e) return GS_LINES;
+    const std::string m(e);
+    if (m == "colours") return GS_COLOURS;
+    if (m == "planes") return GS_PLANES;
+    return GS_LINES;
+}
+
+void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                          int cy, bool forward, const Mat24<float> &K0, cudaStream_t st) {
+    const int nlines = ((g.nn[0] - cx + 1) / 2) * ((g.nn[1] - cy + 1) / 2);
+    if (nlines <= 0) return;
+    // about one wave of three CTAs per SM, whole lines per CTA
+    const int per = std::max(1, (nlines + 3 * NUM_SMS - 1) / (3 * NUM_SMS));
+    const unsigned grid = (unsigned)((nlines + per - 1) / per);
+    const int fw = forward ? 1 : 0;
+    if (K0.isCube)
+        launch_pdl(gs_fine_lines_kernel<true>, grid, BS, 0, st, g, Y, u, b, dmask, cx, cy, per, fw, K0);
+    else
+        launch_pdl(gs_fine_lines_kernel<false>, grid, BS, 0, st, g, Y, u, b, dmask, cx, cy, per, fw, K0);
+    VFEM_LAUNCH_CHECK();
 }
 
 void launch_gs_fine_planes(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,

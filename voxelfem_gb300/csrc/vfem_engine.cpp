@@ -770,11 +770,21 @@ void MG::smoothT(int l, bool forward) {
     auto &D = lv[l].data<T>();
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
     if constexpr (std::is_same<T, float>::value) {
-        if (l == 0 && gsPlanesEnabled()) {
+        const int mode = l == 0 ? gsFineMode() : GS_COLOURS;
+        if (mode == GS_PLANES) {
             // two launches: the x-even colours then the x-odd ones (reversed backward)
             for (int h = 0; h < 2; ++h)
                 launch_gs_fine_planes(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, forward ? h : 1 - h, forward,
                                       Tr<T>::K0(*fine), st);
+            return;
+        }
+        if (mode == GS_LINES) {
+            // four launches: colour pairs (0, 1), (2, 3), (4, 5), (6, 7), reversed backward
+            for (int h = 0; h < 4; ++h) {
+                const int c = forward ? h : 3 - h;
+                launch_gs_fine_lines(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1, forward,
+                                     Tr<T>::K0(*fine), st);
+            }
             return;
         }
     }

@@ -81,8 +81,15 @@ void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *
 // thread-block cluster per plane); identical iterates to the four colour launches.
 void launch_gs_fine_planes(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
                            bool forward, const Mat24<float> &K0, cudaStream_t st);
-// The plane-pair sweep is used unless VFEM_GS_PLANES=0 (then eight colour launches per sweep).
-bool gsPlanesEnabled();
+// The FP32 fine sweep's colours (x%2, y%2) = (cx, cy) with z parity 0 then 1 (1 then 0
+// backward): all z-lines of that class at once, whole lines per CTA; identical iterates to the
+// two colour launches.
+void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                          int cy, bool forward, const Mat24<float> &K0, cudaStream_t st);
+// Form of the FP32 fine sweep: four line-pair launches (default), two plane-pair launches or
+// eight colour launches (VFEM_GS_MODE = lines / planes / colours).
+enum { GS_COLOURS = 0, GS_LINES = 1, GS_PLANES = 2 };
+int gsFineMode();
 template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                           const Mat24<T> &K0, cudaStream_t st);
