@@ -593,6 +593,30 @@ def run_lbl(slots_list=(1, 8, 16)):
     out["warm_N3_chains_8_4_coarsenings_iterations_total"] = int(ev.iterations.sum())
     ev._release()
     del mg4
+    # where one height's solve spends its time: a mixed solve from zero at a few heights (CUDA
+    # events around the library call) and the warm-cache per-phase breakdown of one iteration
+    import ctypes as C
+
+    from voxelfem_gb300 import _capi
+    lib = _capi.load()
+    per_height = {}
+    for h in (8, 32, 64, 128):
+        mg.setFabricationMaskHeightByLayer(h)
+        f = sim.buildLoadVector()
+        x0 = np.zeros_like(f)
+        mg.preconditionedConjugateGradient(x0, f, 500, TOL, None, 1, 2, False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mg.preconditionedConjugateGradient(x0, f, 500, TOL, None, 1, 2, False)
+        dt = time.perf_counter() - t0
+        bd = phase_breakdown(lib, _capi, mg._h, reps=2)
+        iter_ms = sum(v for k, v in bd.items() if not k.startswith(("galerkin", "coarsest:")) or k == "coarsest:solve")
+        top = sorted(((v, k) for k, v in bd.items() if not k.startswith("galerkin")), reverse=True)[:8]
+        per_height[str(h)] = {"solve_s_host_buffers": dt, "iterations": int(mg.lastStats.iterations),
+                              "iteration_ms": iter_ms, "rebuild_ms": bd.get("galerkin+coarse_inverse"),
+                              "top_phases_ms": {k: v for v, k in top}}
+    mg.setFabricationMaskHeightByLayer(ne[1])
+    out["per_height_mixed"] = per_height
     # the plain method: 128 sequential FP64 solves on the same GPU
     mg.setPrecision("fp64")
     ev = pv.LayerByLayerEvaluator(sim)
