@@ -166,6 +166,10 @@ int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, in
  * helpers of the coarsest dense inverse (single-precision seed plus two Newton-Raphson steps;
  * the plain quotient outside (1e-30, 1e30)). Host or device arrays. */
 int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, double *rsqrt_out);
+/* Diagnostic (no reference counterpart): how many hierarchy rebuilds this solver ran in full and
+ * how many as band-partial updates after a fabrication-mask change (the reference's
+ * m_partialStiffnessMatrixUpdate, MultigridSolver.hh:907-1017). */
+int vfem_mg_stiffness_rebuilds(const vfem_mg *mg, int64_t *full, int64_t *band);
 /* CUDA-graph capture of the CG iteration (default on); no reference counterpart */
 int vfem_mg_set_use_graphs(vfem_mg *mg, int use);
 /* Execution option (no reference counterpart): with graphs on, a solve without a callback runs as

@@ -347,12 +347,14 @@ __global__ void __launch_bounds__(ROW) stencil_level1_kernel(Geom g1, Geom g0, c
 // all nine entries.
 template <typename T>
 __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
-                                                                const T *__restrict__ Kc, T *__restrict__ S) {
+                                                                const T *__restrict__ Kc, T *__restrict__ S, int rowLo,
+                                                                int rowHi) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
     const int o = 13 + blockIdx.y;
     if (p >= g1.NN) return;
     int i, j, k;
     stencil::colour_node(g1, p, i, j, k);
+    if (j < rowLo || j >= rowHi) return;  // outside the band being rebuilt
     const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
     T acc[9];
 #pragma unroll
@@ -397,10 +399,19 @@ __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0
 constexpr int EB2 = 8;
 template <typename T>
 __global__ void __launch_bounds__(576) ke_level2_kernel(Geom g2, Geom g1, Geom g0, const T *__restrict__ Y0,
-                                                        const T *__restrict__ K2, T *__restrict__ Ke2) {
+                                                        const T *__restrict__ K2, T *__restrict__ Ke2, int rowLo,
+                                                        int rowHi) {
     __shared__ T sY[EB2][64];
     const int t = threadIdx.x;
     const int64_t e0 = (int64_t)blockIdx.x * EB2;
+    // elements outside the row band [rowLo, rowHi) keep their matrices
+    auto inBand = [&](int64_t e) {
+        const int ej = (int)((e / g2.ne[2]) % g2.ne[1]);
+        return e < g2.NE && ej >= rowLo && ej < rowHi;
+    };
+    bool any = false;
+    for (int eb = 0; eb < EB2; ++eb) any = any || inBand(e0 + eb);
+    if (!any) return;
     for (int q = t; q < EB2 * 64; q += 576) {
         const int eb = q >> 6, f = q & 63;
         const int64_t e = e0 + eb;
@@ -428,23 +439,25 @@ __global__ void __launch_bounds__(576) ke_level2_kernel(Geom g2, Geom g1, Geom g
     }
 #pragma unroll
     for (int eb = 0; eb < EB2; ++eb)
-        if (e0 + eb < g2.NE) Ke2[(e0 + eb) * 576 + t] = acc[eb];
+        if (inBand(e0 + eb)) Ke2[(e0 + eb) * 576 + t] = acc[eb];
 }
 
 // Ke_c = sum_fi Phi_fi^T Ke_child(fi) Phi_fi (MultigridSolver.hh:712-722, 745-819).
 // One block per coarse element, thread t owns entry t of the coarse matrix.
 template <typename T>
 __global__ void __launch_bounds__(576) ke_coarsen_kernel(Geom gc, Geom gf, const T *__restrict__ Kef,
-                                                         const T *__restrict__ phis, T *__restrict__ Kec) {
+                                                         const T *__restrict__ phis, T *__restrict__ Kec, int rowLo,
+                                                         int rowHi) {
     __shared__ T sK[576];
     __shared__ T sT[576];
     __shared__ T sP[8 * 64];
     const int64_t e = blockIdx.x;
     const int t = threadIdx.x;
-    for (int q = t; q < 512; q += 576) sP[q] = phis[q];
     const int ek = (int)(e % gc.ne[2]);
     const int64_t q = e / gc.ne[2];
     const int ej = (int)(q % gc.ne[1]), ei = (int)(q / gc.ne[1]);
+    if (ej < rowLo || ej >= rowHi) return;  // outside the band being rebuilt (block-uniform)
+    for (int qq = t; qq < 512; qq += 576) sP[qq] = phis[qq];
     const bool masked = ej >= gc.maskedE();
     T acc = T(0);
     const int row = t / 24, col = t % 24;
@@ -515,12 +528,13 @@ __global__ void __launch_bounds__(ROW) stencil_from_ke_kernel(Geom g, const T *_
 
 template <typename T>
 __global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T *__restrict__ Ke,
-                                                                 T *__restrict__ S) {
+                                                                 T *__restrict__ S, int rowLo, int rowHi) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
     const int o = 13 + blockIdx.y;
     if (p >= g.NN) return;
     int i, j, k;
     stencil::colour_node(g, p, i, j, k);
+    if (j < rowLo || j >= rowHi) return;  // outside the band being rebuilt
     const int oo[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
     T acc[9];
 #pragma unroll
@@ -645,23 +659,31 @@ void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, 
 }
 
 template <typename T>
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st) {
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st,
+                           int rowLo, int rowHi) {
     if (g1.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
-    if (rows) stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
-    else stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g1, g0, Y0, Kc, S);
+    if (rows) {
+        if (rowLo > 0 || rowHi < g1.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
+        stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
+    } else {
+        stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g1, g0, Y0, Kc,
+                                                                                                     S, rowLo, rowHi);
+    }
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
-void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis, T *Kec, cudaStream_t st) {
+void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis, T *Kec, cudaStream_t st, int rowLo,
+                       int rowHi) {
     if (gc.NE > 2147483647LL) throw Error(ERR_ARG, "too many coarse elements");
-    ke_coarsen_kernel<T><<<(unsigned)gc.NE, 576, 0, st>>>(gc, gf, Kef, phis, Kec);
+    ke_coarsen_kernel<T><<<(unsigned)gc.NE, 576, 0, st>>>(gc, gf, Kef, phis, Kec, rowLo, rowHi);
     VFEM_LAUNCH_CHECK();
 }
 
 template <typename T>
-void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st) {
-    ke_level2_kernel<T><<<gridFor(g2.NE, EB2), 576, 0, st>>>(g2, g1, g0, Y0, K2, Ke2);
+void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st,
+                      int rowLo, int rowHi) {
+    ke_level2_kernel<T><<<gridFor(g2.NE, EB2), 576, 0, st>>>(g2, g1, g0, Y0, K2, Ke2, rowLo, rowHi);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -672,10 +694,15 @@ void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_
 }
 
 template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st) {
+void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st, int rowLo, int rowHi) {
     if (g.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
-    if (rows) stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
-    else stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g, Ke, S);
+    if (rows) {
+        if (rowLo > 0 || rowHi < g.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
+        stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
+    } else {
+        stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g, Ke, S, rowLo,
+                                                                                                     rowHi);
+    }
     VFEM_LAUNCH_CHECK();
 }
 
@@ -691,11 +718,12 @@ void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStr
     template void launch_masked_zero<T>(const Geom &, T *, int, cudaStream_t);                                        \
     template void launch_fill<T>(T *, T, int64_t, cudaStream_t);                                                      \
     template void launch_ke_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);           \
-    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, bool, cudaStream_t); \
-    template void launch_ke_coarsen<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);          \
+    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, bool, cudaStream_t, \
+                                           int, int);                                                                \
+    template void launch_ke_coarsen<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t, int, int); \
     template void launch_ke_level2<T>(const Geom &, const Geom &, const Geom &, const T *, const T *, T *,            \
-                                      cudaStream_t);                                                                  \
-    template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, bool, cudaStream_t);                        \
+                                      cudaStream_t, int, int);                                                        \
+    template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, bool, cudaStream_t, int, int);              \
     template void launch_ke_scaled<T>(const Geom &, const T *, const T *, T *, cudaStream_t);
 VFEM_INST_COARSE(double)
 VFEM_INST_COARSE(float)

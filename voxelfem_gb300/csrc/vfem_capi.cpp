@@ -292,6 +292,15 @@ int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, 
         finishOut(vs, st);
     });
 }
+int vfem_mg_stiffness_rebuilds(const vfem_mg *mg, int64_t *full, int64_t *band) {
+    return guarded([&] {
+        need(mg, "mg");
+        need(full, "full");
+        need(band, "band");
+        *full = mg->m.fullRebuilds;
+        *band = mg->m.bandRebuilds;
+    });
+}
 int vfem_mg_set_device_loop(vfem_mg *mg, int on) {
     return guarded([&] {
         need(mg, "mg");

@@ -142,6 +142,7 @@ void Grid::setETensor(double E, double nu_) {
         K0df.cubeLo[c] = (float)(K0.cube[c] - (double)K0df.cubeHi[c]);
     }
     ++densVersion;  // stiffness depends on K0
+    ++materialVersion;
 }
 
 void Grid::setParams(double E0_, double Emin_, double gamma_, double q_, int law_) {
@@ -153,13 +154,14 @@ void Grid::setParams(double E0_, double Emin_, double gamma_, double q_, int law
     updateYoungModuli();
 }
 
-void Grid::updateYoungModuli() {
+void Grid::updateYoungModuli(bool maskOnly) {
     const bool masking = maskH < bmax[BUILD_DIR];
     launch_young_moduli<double>(g, rho.p, Y.p, E0, Emin, gamma, q, law, masking, stream);
     YfValid = false;
     YfpValid = false;
     YdfValid = false;
     ++densVersion;
+    if (!maskOnly) ++materialVersion;
 }
 
 void Grid::youngDF(const float **hi, const float **lo) {
@@ -307,7 +309,7 @@ void Grid::setMaskHeight(double hgt, bool update) {
     g.firstDetN = g.firstMaskedE + 1;
     uploadMask();
     ++maskVersion;
-    if (update) updateYoungModuli();
+    if (update) updateYoungModuli(true);
 }
 
 void Grid::uploadMask() { launch_set_pair(dynMask.p, g.firstMaskedE, g.firstDetN, stream); }
@@ -452,6 +454,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     std::memset(hostSc, 0, 17 * sizeof(double));
     setupCoarsestIndex();
     if (const char *env = std::getenv("VFEM_OVERLAP_STIFFNESS")) overlapStiffness = env[0] != '0';
+    if (const char *env = std::getenv("VFEM_BAND_UPDATE")) bandUpdates = env[0] != '0';
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
     VFEM_CUDA(cudaEventCreateWithFlags(&evLevelsReady, cudaEventDisableTiming));
@@ -639,7 +642,7 @@ static void uploadConst(DevBuf<T> &dst, const double *src, size_t n) {
 // MultigridSolver.hh:846-905: element matrices level by level, assembled stencils for the
 // smoothing levels, and the dense inverse of the reduced coarsest operator.
 template <typename T>
-void MG::updateStiffnessT(bool overlap) {
+void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
     syncFineGeom(*this);
     allocLevels();
     cudaStream_t st = fine->stream;
@@ -690,24 +693,29 @@ void MG::updateStiffnessT(bool overlap) {
         launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, lv[0].rows, st);
         VFEM_CUDA(cudaStreamSynchronize(st));
     } else {
-        for (int l = 1; l < L(); ++l) {
+        const bool band = bandLo >= 0;
+        for (int l = 1; l < L() && (!band || bandLo < bandHi); ++l) {
             auto &D = lv[l].data<T>();
             lv[l].rows = lv[l].g.NN <= rowsMaxNodes;
             D.S.alloc((size_t)(lv[l].rows ? 256 : STENCIL_PLANES) * lv[l].g.NN);
+            // level-l element rows whose matrices change, and the node rows whose stencils do
+            const int eLo = band ? (bandLo >> l) : 0;
+            const int eHi = band ? ((bandHi - 1) >> l) + 1 : lv[l].g.ne[1];
+            const int nLo = eLo, nHi = band ? eHi + 1 : lv[l].g.nn[1];
             if (l == 1) {
                 // the level-1 stencil comes straight from the fine moduli; no level-1 element
                 // matrices are stored
-                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs);
+                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs, nLo, nHi);
                 mark("galerkin:L1 stencil");
             } else {
                 D.Ke.alloc((size_t)lv[l].g.NE * 576);
                 if (l == 2)
-                    launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, gs);
+                    launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, gs, eLo, eHi);
                 else
                     launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p,
-                                         gs);
+                                         gs, eLo, eHi);
                 mark("galerkin:L" + std::to_string(l) + " element matrices");
-                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, gs);
+                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, gs, nLo, nHi);
                 mark("galerkin:L" + std::to_string(l) + " stencil");
             }
         }
@@ -731,21 +739,37 @@ void MG::updateStiffnessT(bool overlap) {
     stiffnessPrecision = precision;
     stiffnessDensVersion = fine->densVersion;
     stiffnessMaskVersion = fine->maskVersion;
+    stiffnessMaterialVersion = fine->materialVersion;
+    stiffnessMaskE = fine->g.firstMaskedE;
+    if (bandLo >= 0) ++bandRebuilds;
+    else ++fullRebuilds;
 }
 
-void MG::updateStiffness(bool overlap) {
+void MG::updateStiffness(bool overlap, int bandLo, int bandHi) {
     // a rebuild still in flight on the side stream finishes before this one starts
     VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
-    if (precision == PREC_FP64) updateStiffnessT<double>(overlap);
-    else updateStiffnessT<float>(overlap);
+    if (precision == PREC_FP64) updateStiffnessT<double>(overlap, bandLo, bandHi);
+    else updateStiffnessT<float>(overlap, bandLo, bandHi);
     if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
 }
 
 void MG::ensureStiffness(bool deferCheck, bool overlap) {
     syncFineGeom(*this);
     if (!stiffnessValid || stiffnessPrecision != precision || stiffnessDensVersion != fine->densVersion ||
-        stiffnessMaskVersion != fine->maskVersion)
-        updateStiffness(overlap);
+        stiffnessMaskVersion != fine->maskVersion) {
+        // only the fabrication mask moved since the last build: rebuild the band of level
+        // operators between the old and the new masked element row
+        bool band = bandUpdates && stiffnessValid && stiffnessPrecision == precision &&
+                    stiffnessMaterialVersion == fine->materialVersion && stiffnessMaskE >= 0 && L() > 1;
+        for (int l = 1; band && l < L(); ++l) band = lv[l].g.NN > rowsMaxNodes;  // plane-layout stencils only
+        if (band) {
+            const int ne1 = fine->g.ne[BUILD_DIR];
+            const int a = std::min(stiffnessMaskE, ne1), b = std::min(fine->g.firstMaskedE, ne1);
+            updateStiffness(overlap, std::min(a, b), std::max(a, b));
+        } else {
+            updateStiffness(overlap);
+        }
+    }
     if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
     if (!deferCheck) checkStiffness();
 }

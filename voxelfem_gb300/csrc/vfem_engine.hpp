@@ -74,6 +74,9 @@ public:
     DevBuf<double> dval;
     bool dvalNonzero = false;
     uint64_t densVersion = 1, bcVersion = 1, maskVersion = 1, k0Version = 1;
+    // bumped by every change of the moduli except a fabrication-mask change (densities, material,
+    // interpolation parameters, K0): a mask-only change allows a band-partial Galerkin update
+    uint64_t materialVersion = 1;
     cudaStream_t stream = nullptr;
 
     void setETensor(double E, double nu);
@@ -82,7 +85,7 @@ public:
     void setUniformDensities(double v);
     void getDensities(double *out);
     void getYoungModuli(double *out);
-    void updateYoungModuli();
+    void updateYoungModuli(bool maskOnly = false);
     const float *youngFPad();  // zero-padded FP32 moduli (Geom::padElem layout)
     const float *youngF();
     void youngDF(const float **hi, const float **lo);  // double-float split of Y
@@ -165,8 +168,16 @@ public:
     int L() const { return (int)lv.size(); }
     void setPrecision(int p);
     void setMaskLayer(int64_t l);
-    // overlap: build on stiffStream (see below) instead of the solver stream
-    void updateStiffness(bool overlap = false);
+    // overlap: build on stiffStream (see below) instead of the solver stream. bandLo < bandHi: a
+    // band-partial update after a fabrication-mask change (MultigridSolver.hh:907-1017): only the
+    // level operators that the fine element rows [bandLo, bandHi) reach are rebuilt (the coarsest
+    // inverse is always refactored, as the reference refactors its CHOLMOD factor).
+    void updateStiffness(bool overlap = false, int bandLo = -1, int bandHi = -1);
+    // band-partial updates are on unless VFEM_BAND_UPDATE=0
+    bool bandUpdates = true;
+    int stiffnessMaskE = -1;              // fine masked element row the operators were built for
+    uint64_t stiffnessMaterialVersion = 0;
+    int64_t fullRebuilds = 0, bandRebuilds = 0;  // counters (diagnostic)
     // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (the
     // initial residual through the outer matvec, its norms, the first preconditioner input) runs
     // on the solver stream while the Galerkin operators (evLevelsReady) and the coarsest dense
@@ -271,7 +282,7 @@ private:
     void coarsenDirichlet();
     void setupCoarsestIndex();
     template <typename T>
-    void updateStiffnessT(bool overlap);
+    void updateStiffnessT(bool overlap, int bandLo, int bandHi);
     template <typename T>
     void smoothT(int l, bool forward);
     template <typename T>

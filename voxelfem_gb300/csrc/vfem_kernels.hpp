@@ -143,16 +143,22 @@ template <typename T>
 void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc /*8*576*/, T *Ke1, cudaStream_t st);
 // Level-1 stencil assembled directly from the fine Young's moduli (no element matrices).
 template <typename T>
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st);
+// rowLo, rowHi: only the (level-1 node / level-l element / level-l node) rows in [rowLo, rowHi)
+// are rebuilt (band-partial update); the defaults rebuild everything
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st,
+                           int rowLo = 0, int rowHi = 2147483647);
 // Level-2 element matrices from the fine moduli and the 64 folded constant matrices K2.
 template <typename T>
-void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st);
+void launch_ke_level2(const Geom &g2, const Geom &g1, const Geom &g0, const T *Y0, const T *K2, T *Ke2, cudaStream_t st,
+                      int rowLo = 0, int rowHi = 2147483647);
 template <typename T>
-void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis /*8*64*/, T *Kec, cudaStream_t st);
+void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *phis /*8*64*/, T *Kec, cudaStream_t st,
+                       int rowLo = 0, int rowHi = 2147483647);
 template <typename T>
 void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_t st);
 template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st);
+void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st, int rowLo = 0,
+                            int rowHi = 2147483647);
 template <typename Tdst, typename Tsrc>
 void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st);
 

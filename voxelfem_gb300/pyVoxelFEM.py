@@ -664,6 +664,13 @@ class MultigridSolver:
         check(_lib().vfem_mg_set_precision(self._h, p, m))
         self._prec = precision
 
+    def stiffnessRebuilds(self):
+        """(full, band): hierarchy rebuilds run in full and as band-partial updates after a
+        fabrication-mask change (diagnostic)."""
+        full, band = C.c_int64(), C.c_int64()
+        check(_lib().vfem_mg_stiffness_rebuilds(self._h, C.byref(full), C.byref(band)))
+        return full.value, band.value
+
     def outerMatvecKind(self):
         """'fp64', 'df-simt' or 'tensor': the outer matvec the mixed solve uses now."""
         k = C.c_int()
