@@ -412,6 +412,15 @@ def run_ours(args):
         kernels["gs_fine_sweep_fp32_" + mode] = {"ms": ms.value, "bytes": nbytes.value,
                                                   "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
     del os.environ["VFEM_GS_MODE"]
+    # register budgets of the FP32 fine kernels: fitted to 3 or 4 resident 256-thread blocks per SM
+    for occ in ("3", "4"):
+        os.environ["VFEM_FINE_OCC"] = occ
+        for kid, name in ((3, "gs_fine_sweep_fp32"), (5, "residual_fine_fp32")):
+            ms, nbytes = C.c_double(), C.c_double()
+            _capi.check(lib.vfem_mg_time_kernel(mg._h, kid, 20, C.byref(ms), C.byref(nbytes)))
+            kernels[name + "_occ" + occ] = {"ms": ms.value, "bytes": nbytes.value,
+                                            "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
+    del os.environ["VFEM_FINE_OCC"]
     # launches per PCG iteration of the hot kernels of the mixed solve (2 pre + 2 post sweeps per level)
     outer_name = "applyk_fine_tc" if outer_kind == "tensor" else "applyk_fine_df"
     per_iter_launches = {outer_name: 1, "gs_fine_sweep_fp32": 4, "residual_fine_fp32": 1,

@@ -271,8 +271,9 @@ __global__ void __launch_bounds__(BS, 2) applyk_fine_kernel(Geom g, const T *__r
 }
 
 // r = b - K u (MultigridSolver.hh:527-541): b copied, stencil subtracted, Dirichlet zeroed.
-template <typename T, bool Cube>
-__global__ void __launch_bounds__(BS, 2) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
+// MB: resident blocks per SM the register budget is fitted to.
+template <typename T, bool Cube, int MB = 2>
+__global__ void __launch_bounds__(BS, MB) residual_fine_kernel(Geom g, const T *__restrict__ Y, const T *__restrict__ u,
                                                            const T *__restrict__ b, T *__restrict__ r,
                                                            const uint8_t *__restrict__ dmask, const Mat24<T> K) {
     VFEM_PDL_ENTRY();
@@ -489,8 +490,8 @@ __global__ void __launch_bounds__(BS, 3) gs_fine_planes_kernel(Geom g, const flo
 // then updates the second colour's (z parity 0 then 1 forward, 1 then 0 backward). A sweep is
 // four such launches; the node updates and their operands are those of the eight colour
 // launches, so the iterates are identical.
-template <bool Cube>
-__global__ void __launch_bounds__(BS, 3) gs_fine_lines_kernel(Geom g, const float *__restrict__ Y, float *u,
+template <bool Cube, int MB = 3>
+__global__ void __launch_bounds__(BS, MB) gs_fine_lines_kernel(Geom g, const float *__restrict__ Y, float *u,
                                                              const float *__restrict__ b,
                                                              const uint8_t *__restrict__ dmask, int cx, int cy,
                                                              int linesPerCta, int forward, const Mat24<float> K) {
@@ -814,7 +815,11 @@ void launch_applyk_fine(const Geom &g, const T *Y, const T *u, T *out, const Mat
 template <typename T>
 void launch_residual_fine(const Geom &g, const T *Y, const T *u, const T *b, T *r, const Mat24<T> &K0,
                           const uint8_t *dmask, cudaStream_t st) {
-    if (sizeof(T) == 4 && K0.isCube) launch_pdl(residual_fine_kernel<T, true>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
+    if (sizeof(T) == 4 && K0.isCube && fineOccupancy() == 4)
+        launch_pdl(residual_fine_kernel<T, true, 4>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
+    else if (sizeof(T) == 4 && K0.isCube && fineOccupancy() == 3)
+        launch_pdl(residual_fine_kernel<T, true, 3>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
+    else if (sizeof(T) == 4 && K0.isCube) launch_pdl(residual_fine_kernel<T, true>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
     else launch_pdl(residual_fine_kernel<T, false>, gridFor(g.NN, BS), BS, 0, st, g, Y, u, b, r, dmask, K0);
     VFEM_LAUNCH_CHECK();
 }
@@ -834,6 +839,11 @@ static int gsPlaneStrips(const Geom &g) {
     return c;
 }
 
+int fineOccupancy() {
+    const char *e = std::getenv("VFEM_FINE_OCC");
+    return e ? std::atoi(e) : 0;
+}
+
 int gsFineMode() {
     const char *e = std::getenv("VFEM_GS_MODE");
     if (!e) return GS_LINES;
@@ -851,7 +861,9 @@ void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *
     const int per = std::max(1, (nlines + 3 * NUM_SMS - 1) / (3 * NUM_SMS));
     const unsigned grid = (unsigned)((nlines + per - 1) / per);
     const int fw = forward ? 1 : 0;
-    if (K0.isCube)
+    if (K0.isCube && fineOccupancy() == 4)
+        launch_pdl(gs_fine_lines_kernel<true, 4>, grid, BS, 0, st, g, Y, u, b, dmask, cx, cy, per, fw, K0);
+    else if (K0.isCube)
         launch_pdl(gs_fine_lines_kernel<true>, grid, BS, 0, st, g, Y, u, b, dmask, cx, cy, per, fw, K0);
     else
         launch_pdl(gs_fine_lines_kernel<false>, grid, BS, 0, st, g, Y, u, b, dmask, cx, cy, per, fw, K0);

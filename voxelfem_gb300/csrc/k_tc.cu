@@ -248,6 +248,25 @@ __global__ void __launch_bounds__(TCT, 4)
     const int ny0 = Y0 - 1, nz0 = Z0 - 1;     // first patch node / first tile element
     const int X0 = sx * segLen, X1 = min(X0 + segLen, g.nn[0]);
 
+    if (Y0 >= g.nyv()) {
+        // every node row this CTA owns is detached (a partial-build mask): the outputs are those
+        // the full computation writes there (zero, or the right-hand side's unconstrained
+        // components in residual form) and the tensor core is not needed
+        if (tid < OY * OZ) {
+            const int nj = Y0 + tid / OZ, nk = Z0 + tid % OZ;
+            if (nj < g.nn[1] && nk < g.nn[2]) {
+                for (int Lp = X0; Lp < X1; ++Lp) {
+                    const int64_t n = g.node(Lp, nj, nk);
+                    const uint8_t dm = rhs ? dmask[n] : 0;
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) out[r * g.ld + n] = (rhs && !((dm >> r) & 1)) ? rhs[r * g.ld + n] : 0.0;
+                }
+            }
+        }
+        if (withDot && tid == 0) partials[b] = 0.0;
+        return;
+    }
+
     // B tiles (4 KB) into shared memory
     for (int t = tid; t < 256; t += TCT) reinterpret_cast<uint4 *>(smem + OFF_B)[t] = bTiles[t];
     // global scale: |u| < 2^s

@@ -90,6 +90,9 @@ void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *
 // eight colour launches (VFEM_GS_MODE = lines / planes / colours).
 enum { GS_COLOURS = 0, GS_LINES = 1, GS_PLANES = 2 };
 int gsFineMode();
+// Resident blocks per SM the FP32 cube-voxel fine kernels are compiled for (VFEM_FINE_OCC = 3 or
+// 4; 0 keeps the defaults)
+int fineOccupancy();
 template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                           const Mat24<T> &K0, cudaStream_t st);
