@@ -569,6 +569,7 @@ void MG::setPrecision(int p) {
     if (p != precision) {
         precision = p;
         stiffnessValid = false;
+        levelsValid = false;
         clearGraphs();
     }
 }
@@ -741,6 +742,7 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
     stiffnessMaskVersion = fine->maskVersion;
     stiffnessMaterialVersion = fine->materialVersion;
     stiffnessMaskE = fine->g.firstMaskedE;
+    levelsValid = true;
     if (bandLo >= 0) ++bandRebuilds;
     else ++fullRebuilds;
 }
@@ -759,7 +761,7 @@ void MG::ensureStiffness(bool deferCheck, bool overlap) {
         stiffnessMaskVersion != fine->maskVersion) {
         // only the fabrication mask moved since the last build: rebuild the band of level
         // operators between the old and the new masked element row
-        bool band = bandUpdates && stiffnessValid && stiffnessPrecision == precision &&
+        bool band = bandUpdates && levelsValid && stiffnessPrecision == precision &&
                     stiffnessMaterialVersion == fine->materialVersion && stiffnessMaskE >= 0 && L() > 1;
         for (int l = 1; band && l < L(); ++l) band = lv[l].g.NN > rowsMaxNodes;  // plane-layout stencils only
         if (band) {
@@ -784,6 +786,7 @@ void MG::checkStiffness() {
     std::memcpy(&hs, &hostSc[16], sizeof(int));
     if (hs) {
         stiffnessValid = false;
+        levelsValid = false;
         throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
     }
 }

@@ -176,6 +176,9 @@ public:
     // band-partial updates are on unless VFEM_BAND_UPDATE=0
     bool bandUpdates = true;
     int stiffnessMaskE = -1;              // fine masked element row the operators were built for
+    // the level operators (levels >= 1) are current for stiffnessMaskE; stiffnessValid also
+    // covers the coarsest dense inverse, which a change of the free coarsest DOFs invalidates
+    bool levelsValid = false;
     uint64_t stiffnessMaterialVersion = 0;
     int64_t fullRebuilds = 0, bandRebuilds = 0;  // counters (diagnostic)
     // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (the
