@@ -626,6 +626,27 @@ def run_lbl(slots_list=(1, 8, 16)):
                               "top_phases_ms": {k: v for v, k in top}}
     mg.setFabricationMaskHeightByLayer(ne[1])
     out["per_height_mixed"] = per_height
+    # the autotuner (slots x fine-sweep form x smoothing sweeps, on every 8th height), then all
+    # 128 heights with its choice
+    import tempfile
+
+    from voxelfem_gb300 import autotune
+    with tempfile.TemporaryDirectory() as tdir:
+        entry = autotune.tune_layer_by_layer(sim, mg, "zero", tol=TOL, path=os.path.join(tdir, "cache.json"))
+    out["autotune"] = {"key": autotune.key(sim, mg, "zero"), "entry": entry}
+    ev = pv.LayerByLayerEvaluator(sim)
+    ev.selectInitMethod("zero")
+    kw = dict(maxIter=500, tol=TOL, mgIterations=1, mgSmoothingIterations=entry["mgSmoothingIterations"],
+              slots=entry["slots"], sweepForm=entry["sweepForm"])
+    ev.run(mg, True, 1, **kw)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev.run(mg, True, 1, **kw)
+    torch.cuda.synchronize()
+    out["tuned_zero_s"] = time.perf_counter() - t0
+    out["tuned_zero_iterations_total"] = int(ev.iterations.sum())
+    out["tuned_zero_max_rel_diff_vs_2_sweeps"] = float(np.max(np.abs(ev.compliances - ref) / np.abs(ref)))
+    ev._release()
     # the plain method: 128 sequential FP64 solves on the same GPU
     mg.setPrecision("fp64")
     ev = pv.LayerByLayerEvaluator(sim)

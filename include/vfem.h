@@ -126,6 +126,8 @@ int vfem_lbl_destroy(vfem_lbl *e);
  * chains, each in order on one slot (one slot: the reference's sequential algorithm); with
  * "zero" the heights are independent and spread over the slots. */
 int vfem_lbl_set_init(vfem_lbl *e, int kind, int history);
+/* Form of every slot's FP32 fine sweep, as vfem_mg_set_sweep_form (no reference counterpart). */
+int vfem_lbl_set_sweep_form(vfem_lbl *e, int form);
 /* zero_init 0: the full-design height starts from the previous run's full-design solution */
 int vfem_lbl_run(vfem_lbl *e, const int64_t *layers, int64_t count, int64_t max_iter, double tol,
                  int64_t mg_iterations, int64_t mg_smoothing_iterations, int full_multigrid, int zero_init,
@@ -166,6 +168,14 @@ int vfem_tc_fit_k0(const double *k0_576, double *scale, uint16_t *tiles_2048, in
  * helpers of the coarsest dense inverse (single-precision seed plus two Newton-Raphson steps;
  * the plain quotient outside (1e-30, 1e30)). Host or device arrays. */
 int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, double *rsqrt_out);
+/* Form of the FP32 fine Gauss-Seidel sweep of the mixed V-cycle (no reference counterpart; every
+ * form runs the reference's colour order and gives identical iterates): VFEM_SWEEP_LINES (default:
+ * four launches, colour pairs on whole z-lines), VFEM_SWEEP_COLOURS (eight colour launches) or
+ * VFEM_SWEEP_PLANES (two launches, one thread-block cluster per x-plane). */
+#define VFEM_SWEEP_COLOURS 0
+#define VFEM_SWEEP_LINES 1
+#define VFEM_SWEEP_PLANES 2
+int vfem_mg_set_sweep_form(vfem_mg *mg, int form);
 /* Diagnostic (no reference counterpart): how many hierarchy rebuilds this solver ran in full and
  * how many as band-partial updates after a fabrication-mask change (the reference's
  * m_partialStiffnessMatrixUpdate, MultigridSolver.hh:907-1017). */

@@ -157,3 +157,29 @@ def test_lbl_warm_chains_and_restart(gpu, oracle):
     ev1.run(mg, False, INC, 500, TOL, mgSmoothingIterations=2, slots=1)
     assert ev1.iterations[0] == 0
     assert np.max(np.abs(ev3.compliances - ev1.compliances) / np.abs(ev1.compliances)) < 1e-8
+
+
+def test_autotuner_and_tuned_run(gpu, tmp_path, monkeypatch):
+    """The autotuner times slot counts and fine-sweep forms (which leave the results unchanged)
+    and caches the fastest; a tuned run reads the cache and reproduces the plain run."""
+    from voxelfem_gb300 import autotune
+
+    sim, rho = _gpu_sim()
+    mg = sim.multigridSolver(LEVELS - 1)
+    mg.setPrecision("mixed")
+    path = str(tmp_path / "cache.json")
+    entry = autotune.tune_layer_by_layer(sim, mg, "zero", tol=TOL, sample_increment=3,
+                                         candidates={"slots": (1, 3), "sweepForm": ("lines", "colours", "planes"),
+                                                     "mgSmoothingIterations": (2,)}, path=path)
+    assert len(entry["candidates"]) == 6
+    assert all(c["max_rel_diff"] == 0.0 for c in entry["candidates"])
+    monkeypatch.setattr(autotune, "CACHE", path)
+    assert autotune.lookup(sim, mg, "zero")["sweepForm"] == entry["sweepForm"]
+    plain = pv.LayerByLayerEvaluator(sim)
+    plain.selectInitMethod("zero")
+    plain.run(mg, True, INC, 500, TOL, mgSmoothingIterations=2)
+    tuned = pv.LayerByLayerEvaluator(sim)
+    tuned.selectInitMethod("zero")
+    tuned.run(mg, True, INC, 500, TOL, mgSmoothingIterations="tuned", tuned=True)
+    np.testing.assert_array_equal(tuned.compliances, plain.compliances)
+    np.testing.assert_array_equal(tuned.iterations, plain.iterations)

@@ -183,6 +183,12 @@ int vfem_lbl_create(vfem_grid *g, int64_t coarsenings, int64_t slots, int precis
 int vfem_lbl_destroy(vfem_lbl *e) {
     return guarded([&] { delete e; });
 }
+int vfem_lbl_set_sweep_form(vfem_lbl *e, int form) {
+    return guarded([&] {
+        need(e, "evaluator");
+        e->e.setSweepForm(form);
+    });
+}
 int vfem_lbl_set_init(vfem_lbl *e, int kind, int history) {
     return guarded([&] {
         need(e, "evaluator");
@@ -290,6 +296,12 @@ int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, 
         launch_newton_helpers((const double *)vi.d, n, (double *)vr.d, (double *)vs.d, st);
         finishOut(vr, st);
         finishOut(vs, st);
+    });
+}
+int vfem_mg_set_sweep_form(vfem_mg *mg, int form) {
+    return guarded([&] {
+        need(mg, "mg");
+        mg->m.setSweepForm(form);
     });
 }
 int vfem_mg_stiffness_rebuilds(const vfem_mg *mg, int64_t *full, int64_t *band) {

@@ -564,6 +564,14 @@ void MG::setupCoarsestIndex() {
     stiffnessValid = false;
 }
 
+void MG::setSweepForm(int form) {
+    if (form != GS_LINES && form != GS_COLOURS && form != GS_PLANES) throw Error(ERR_ARG, "unknown sweep form");
+    if (form != sweepForm) {
+        sweepForm = form;
+        clearGraphs();  // captured V-cycles hold the launches of the previous form
+    }
+}
+
 void MG::setPrecision(int p) {
     if (p != PREC_FP64 && p != PREC_MIXED) throw Error(ERR_ARG, "unknown precision");
     if (p != precision) {
@@ -797,7 +805,7 @@ void MG::smoothT(int l, bool forward) {
     auto &D = lv[l].data<T>();
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
     if constexpr (std::is_same<T, float>::value) {
-        const int mode = l == 0 ? gsFineMode() : GS_COLOURS;
+        const int mode = l == 0 ? (sweepForm >= 0 ? sweepForm : gsFineMode()) : GS_COLOURS;
         if (mode == GS_PLANES) {
             // two launches: the x-even colours then the x-odd ones (reversed backward)
             for (int h = 0; h < 2; ++h)

@@ -175,6 +175,10 @@ public:
     void updateStiffness(bool overlap = false, int bandLo = -1, int bandHi = -1);
     // band-partial updates are on unless VFEM_BAND_UPDATE=0
     bool bandUpdates = true;
+    // form of the FP32 fine Gauss-Seidel sweep (GS_LINES, GS_COLOURS or GS_PLANES; VFEM_GS_MODE
+    // gives the default); every form gives identical iterates
+    int sweepForm = -1;
+    void setSweepForm(int form);
     int stiffnessMaskE = -1;              // fine masked element row the operators were built for
     // the level operators (levels >= 1) are current for stiffnessMaskE; stiffnessValid also
     // covers the coarsest dense inverse, which a change of the free coarsest DOFs invalidates
@@ -465,6 +469,8 @@ public:
     LBL &operator=(const LBL &) = delete;
     // kind LblInit; history: the subspace size N of "N=<N>" (LBL_INIT_SUBSPACE)
     void setInit(int kind, int history);
+    // fine-sweep form of every slot's solver (MG::setSweepForm)
+    void setSweepForm(int form);
     // Heights layers[0..count) in the given order (the reference runs them from the full design
     // down). Zero guesses: every height is independent and the heights are spread over the
     // slots. Warm starts: the heights are cut into min(slots, count) contiguous chains, each

@@ -73,6 +73,10 @@ void LBL::syncSource() {
     }
 }
 
+void LBL::setSweepForm(int form) {
+    for (auto &sl : S) sl->mg->setSweepForm(form);
+}
+
 void LBL::setInit(int kind, int history) {
     if (kind < LBL_INIT_ZERO || kind > LBL_INIT_SUBSPACE) throw Error(ERR_ARG, "Unrecognized init method");
     if (kind == LBL_INIT_SUBSPACE && (history < 1 || history > LBL_MAX_HISTORY))

@@ -664,6 +664,13 @@ class MultigridSolver:
         check(_lib().vfem_mg_set_precision(self._h, p, m))
         self._prec = precision
 
+    SWEEP_FORMS = {"colours": 0, "lines": 1, "planes": 2}
+
+    def setSweepForm(self, form):
+        """Form of the FP32 fine Gauss-Seidel sweep of the mixed V-cycle: 'lines' (default),
+        'colours' or 'planes'; every form gives identical iterates."""
+        check(_lib().vfem_mg_set_sweep_form(self._h, self.SWEEP_FORMS[form]))
+
     def stiffnessRebuilds(self):
         """(full, band): hierarchy rebuilds run in full and as band-partial updates after a
         fabrication-mask change (diagnostic)."""
@@ -1499,7 +1506,23 @@ class LayerByLayerEvaluator:
         raise RuntimeError("Unrecognized method " + str(method))
 
     def run(self, solver, zeroInit=True, layerIncrement=1, maxIter=500, tol=1e-8, it_callback=None,
-            mgIterations=1, mgSmoothingIterations=1, fmg=False, verbose=False, lblCallback=None, slots=None):
+            mgIterations=1, mgSmoothingIterations=1, fmg=False, verbose=False, lblCallback=None, slots=None,
+            sweepForm=None, tuned=False):
+        """``slots`` and ``sweepForm`` (the fine sweep's launch form, MultigridSolver.setSweepForm)
+        shape the execution only. ``tuned=True`` takes both from the autotuner's cache entry for
+        this grid, solver and initial-guess method (voxelfem_gb300.autotune), when there is one;
+        ``mgSmoothingIterations="tuned"`` also takes the tuned smoothing sweep count."""
+        if tuned or mgSmoothingIterations == "tuned":
+            from . import autotune
+            best = autotune.lookup(self.sim, solver, self.initMethod)
+            if best is not None:
+                if tuned:
+                    slots = best["slots"] if slots is None else slots
+                    sweepForm = best["sweepForm"] if sweepForm is None else sweepForm
+                if mgSmoothingIterations == "tuned":
+                    mgSmoothingIterations = best["mgSmoothingIterations"]
+            if mgSmoothingIterations == "tuned":
+                mgSmoothingIterations = 1
         if it_callback is not None:
             raise RuntimeError("per-iteration callbacks are not available for device-resident solves")
         ny = int(self.sim.NbElementsPerDimension[1])
@@ -1523,6 +1546,8 @@ class LayerByLayerEvaluator:
         h = self._handle(int(solver.numLevels - 1), int(slots), precision)
         two = self.sim._nc == 2
         check((_lib().vfem_lbl2_set_init if two else _lib().vfem_lbl_set_init)(h, kind, hist))
+        if not two:
+            check(_lib().vfem_lbl_set_sweep_form(h, MultigridSolver.SWEEP_FORMS[sweepForm or "lines"]))
         run = _lib().vfem_lbl2_run if two else _lib().vfem_lbl_run
         check(run(h, ptr(self.layers), n, int(maxIter), float(tol), int(mgIterations), int(mgSmoothingIterations),
                   int(bool(fmg)), int(bool(zeroInit)), ptr(self.compliances), ptr(self.iterations), ptr(self._grad)))
