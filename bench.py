@@ -413,7 +413,7 @@ def run_ours(args):
                                                   "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
     del os.environ["VFEM_GS_MODE"]
     # register budgets of the FP32 fine kernels: fitted to 3 or 4 resident 256-thread blocks per SM
-    for occ in ("3", "4"):
+    for occ in ("2", "3", "4"):
         os.environ["VFEM_FINE_OCC"] = occ
         for kid, name in ((3, "gs_fine_sweep_fp32"), (5, "residual_fine_fp32")):
             ms, nbytes = C.c_double(), C.c_double()

@@ -56,3 +56,30 @@ def test_fused_sweeps_equal_colour_sweeps(gpu, monkeypatch, ne, levels, kw):
         xb, ib = _solve(monkeypatch, mode, ne, levels, **kw)
         assert ia == ib, mode
         np.testing.assert_array_equal(xa, xb, err_msg=mode)
+
+
+@pytest.mark.parametrize("prec,kw", [("mixed", {}), ("fp64", {}), ("mixed", {"mask_layer": 11}),
+                                     ("mixed", {"partial": True})])
+def test_stencil_line_pairs_equal_colour_passes(gpu, monkeypatch, prec, kw):
+    """Coarse plane-layout levels: colour pairs on whole z-lines (four launches per sweep)
+    against eight colour launches, bit for bit (FP64 and mixed V-cycles)."""
+    ne = (32, 24, 16)
+
+    def solve(lines):
+        monkeypatch.setenv("VFEM_STENCIL_LINES_MAX_NODES", "100000000" if lines else "0")
+        g = pv.TensorProductSimulator([1, 1, 1], [[0.0, 0.0, 0.0], [float(v) for v in ne]], ne)
+        wl.setup_cantilever(g, ne, 0.3, 0)
+        if kw.get("partial"):
+            g.addDirichletCondition([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [float(ne[0]), 0.0, float(ne[2])], "y")
+        mg = g.multigridSolver(3)
+        if "mask_layer" in kw:
+            mg.setFabricationMaskHeightByLayer(kw["mask_layer"])
+        mg.setPrecision(prec)
+        b = g.buildLoadVector()
+        x = mg.preconditionedConjugateGradient(np.zeros_like(b), b, 100, 1e-9, None, 1, 2, False)
+        return x, mg.lastStats.iterations
+
+    xa, ia = solve(False)
+    xb, ib = solve(True)
+    assert ia == ib
+    np.testing.assert_array_equal(xa, xb)

@@ -10,6 +10,8 @@
 //  * planes (large levels): S[(o*9 + 3r + c) * NN + p], p the node's colour-ordered position
 //    (stencil::colour_pos); one thread per node, and a colour pass reads contiguous slices.
 // Element-matrix layout (levels >= 1): Ke[e*576 + 24*row + col].
+#include <algorithm>
+
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
 #include "vfem_stencil.cuh"
@@ -208,6 +210,84 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     u[n] = uu[0];
     u[ld + n] = uu[1];
     u[2 * ld + n] = uu[2];
+}
+
+// Line-pair colour passes on a plane-layout level: colours (cx, cy, 0) and (cx, cy, 1), adjacent
+// in the reference's order, in one launch (z parity 0 then 1 forward, 1 then 0 backward). Among
+// the nodes these two colours update, a node's stencil reaches only its own z-line, so each
+// block owns linesPerBlock whole lines of the class and runs the first colour's nodes on them,
+// a block barrier, then the second colour's; nodes go 32 at a time through the split form of
+// gs_stencil_color_soa_kernel (same partial sums, same order, so the iterates are identical).
+// Four launches per sweep instead of eight: the small levels' passes are launch-latency bound.
+template <typename T>
+__global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
+    gs_stencil_lines_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+                                const uint8_t *__restrict__ dmask, int cx, int cy, int linesPerBlock, int forward) {
+    VFEM_PDL_ENTRY();
+    __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
+    const int n1 = (g.nn[1] - cy + 1) / 2, n0 = (g.nn[0] - cx + 1) / 2;
+    const int nlines = n0 * n1;
+    const int l0 = (int)blockIdx.x * linesPerBlock;
+    const int nl = max(0, min(linesPerBlock, nlines - l0));
+    const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    const int nyv = g.nyv();
+    const int64_t ld = g.ld;
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        const int cz = forward ? s : 1 - s;
+        const int nk = (g.nn[2] - cz + 1) / 2;
+        const int cnt = nl * nk;
+        for (int base = 0; base < cnt; base += SPLIT_NODES) {  // block-uniform trip count
+            const int t = base + lane;
+            bool valid = t < cnt;
+            int i = cx, j = cy, k = cz;
+            if (valid) {
+                const int q = t / nk, kk = t - q * nk;
+                const int line = l0 + q;
+                const int ii = line / n1, jj = line - ii * n1;
+                i = cx + 2 * ii;
+                j = cy + 2 * jj;
+                k = cz + 2 * kk;
+                valid = j < nyv;
+            }
+            const int64_t n = g.node(i, j, k);
+            const int64_t p = stencil::colour_pos(g, i, j, k);
+            if (sub > 0) {
+                T f0 = T(0), f1 = T(0), f2 = T(0);
+                if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
+                part[0][sub - 1][lane] = f0;
+                part[1][sub - 1][lane] = f1;
+                part[2][sub - 1][lane] = f2;
+                split_barrier();  // partial sums ready
+                split_barrier();  // warp 0 is done with them
+            } else {
+                T M[9], bb[3], uu[3];
+                uint8_t dm = 7;
+                if (valid) {
+                    dm = dmask[n];
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)e * ld + p];  // diagonal block (offset 13)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        bb[c] = b[c * ld + n];
+                        uu[c] = u[c * ld + n];
+                    }
+                }
+                split_barrier();
+                if (valid && dm != 7) {
+                    T f0, f1, f2;
+                    stencil::split_sum<T>(part, lane, f0, f1, f2);
+                    stencil::node_solve<T>(dm, bb[0] - f0, bb[1] - f1, bb[2] - f2, M, forward != 0, uu[0], uu[1],
+                                           uu[2]);
+                    u[n] = uu[0];
+                    u[ld + n] = uu[1];
+                    u[2 * ld + n] = uu[2];
+                }
+                split_barrier();
+            }
+        }
+        __syncthreads();  // the first colour's updates are visible before the second gathers
+    }
 }
 
 // Full-weighting restriction (MultigridSolver.hh:217-275): coarse node gathers the
@@ -612,6 +692,19 @@ void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const 
 }
 
 template <typename T>
+void launch_gs_stencil_lines(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
+                             bool forward, cudaStream_t st) {
+    const int nlines = ((g.nn[0] - cx + 1) / 2) * ((g.nn[1] - cy + 1) / 2);
+    if (nlines <= 0) return;
+    // short lines share a 32-node round
+    const int nk = (g.nn[2] + 1) / 2;
+    const int per = std::max(1, SPLIT_NODES / nk);
+    launch_pdl(gs_stencil_lines_soa_kernel<T>, (unsigned)((nlines + per - 1) / per), SPLIT_BS, 0, st, g, S, u, b,
+               dmask, cx, cy, per, forward ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st) {
     launch_pdl(restrict_kernel<T>, gridFor(gc.NN, BS), BS, 0, st, gf, gc, fine, coarse);
     VFEM_LAUNCH_CHECK();
@@ -713,6 +806,8 @@ void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStr
     template void launch_gs_stencil_color<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, bool,     \
                                              bool, cudaStream_t);                                                     \
     template void launch_restrict<T>(const Geom &, const Geom &, const T *, T *, cudaStream_t);                       \
+    template void launch_gs_stencil_lines<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, int,      \
+                                             bool, cudaStream_t);                                                     \
     template void launch_interpolate<T>(const Geom &, const Geom &, const T *, T *, bool, cudaStream_t);              \
     template void launch_zero_dirichlet<T>(const Geom &, T *, const uint8_t *, cudaStream_t);                         \
     template void launch_masked_zero<T>(const Geom &, T *, int, cudaStream_t);                                        \

@@ -455,6 +455,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     setupCoarsestIndex();
     if (const char *env = std::getenv("VFEM_OVERLAP_STIFFNESS")) overlapStiffness = env[0] != '0';
     if (const char *env = std::getenv("VFEM_BAND_UPDATE")) bandUpdates = env[0] != '0';
+    if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
     VFEM_CUDA(cudaEventCreateWithFlags(&evLevelsReady, cudaEventDisableTiming));
@@ -822,6 +823,14 @@ void MG::smoothT(int l, bool forward) {
             }
             return;
         }
+    }
+    if (l > 0 && !lv[l].rows && lv[l].g.NN <= stencilLinesMaxNodes) {
+        // small plane-layout levels: colour pairs on whole z-lines, four launches per sweep
+        for (int h = 0; h < 4; ++h) {
+            const int c = forward ? h : 3 - h;
+            launch_gs_stencil_lines<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1, forward, st);
+        }
+        return;
     }
     for (int c = 0; c < 8; ++c) {
         const int color = forward ? c : 7 - c;

@@ -162,6 +162,9 @@ public:
     int tailStart() const;
     int64_t tailMaxNodes = 0;
     int64_t rowsMaxNodes = 0;  // levels up to this size store node-contiguous stencil rows (default: none)
+    // plane-layout levels up to this size sweep colour pairs on whole z-lines (four launches per
+    // sweep instead of eight; VFEM_STENCIL_LINES_MAX_NODES overrides)
+    int64_t stencilLinesMaxNodes = 100000;
     // When set, the stiffness update records a CUDA event after each of its steps (profiling).
     std::vector<std::pair<std::string, cudaEvent_t>> *stiffMarks = nullptr;
 

@@ -90,8 +90,9 @@ void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *
 // eight colour launches (VFEM_GS_MODE = lines / planes / colours).
 enum { GS_COLOURS = 0, GS_LINES = 1, GS_PLANES = 2 };
 int gsFineMode();
-// Resident blocks per SM the FP32 cube-voxel fine kernels are compiled for (VFEM_FINE_OCC = 3 or
-// 4; 0 keeps the defaults)
+// Resident blocks per SM the FP32 cube-voxel fine kernels are fitted to (VFEM_FINE_OCC = 2, 3 or
+// 4; 0: the defaults, four for the residual and three for the Gauss-Seidel sweep, whose 80-register
+// form is faster than its 64-register one)
 int fineOccupancy();
 template <typename T>
 void launch_gs_fine_color(const Geom &g, const T *Y, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
@@ -131,6 +132,11 @@ void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, 
 template <typename T>
 void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
                              bool rows, cudaStream_t st);
+// Colours (cx, cy, 0) and (cx, cy, 1) of a plane-layout level in one launch (whole z-lines per
+// block); identical iterates to the two colour launches.
+template <typename T>
+void launch_gs_stencil_lines(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
+                             bool forward, cudaStream_t st);
 template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st);
 template <typename T>
