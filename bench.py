@@ -418,7 +418,7 @@ def run_ours(args):
                                       "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
     # the other forms of the fine sweep (the solve uses the default one): eight colour launches
     # (one per colour of the reference's order), two plane-pair launches (one cluster per x-plane)
-    for mode in ("colours", "planes", "lines"):
+    for mode in ("colours", "planes", "lines", "staged"):
         os.environ["VFEM_GS_MODE"] = mode
         ms, nbytes = C.c_double(), C.c_double()
         _capi.check(lib.vfem_mg_time_kernel(mg._h, 3, 20, C.byref(ms), C.byref(nbytes)))

@@ -175,6 +175,7 @@ int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, 
 #define VFEM_SWEEP_COLOURS 0
 #define VFEM_SWEEP_LINES 1
 #define VFEM_SWEEP_PLANES 2
+#define VFEM_SWEEP_STAGED 3 /* VFEM_SWEEP_LINES with each CTA's neighbourhood staged in shared memory */
 int vfem_mg_set_sweep_form(vfem_mg *mg, int form);
 /* Diagnostic (no reference counterpart): how many hierarchy rebuilds this solver ran in full and
  * how many as band-partial updates after a fabrication-mask change (the reference's

@@ -30,5 +30,5 @@ def test_shipped_cache_is_well_formed():
     data = autotune.load()
     for k, e in data.items():
         assert k.startswith("lbl|")
-        assert e["sweepForm"] in ("lines", "colours", "planes")
+        assert e["sweepForm"] in ("lines", "colours", "planes", "staged")
         assert e["slots"] >= 1 and e["mgSmoothingIterations"] >= 1

@@ -3,7 +3,9 @@ order (MultigridSolver.hh:409-458):
 - line pairs: four launches per sweep, each running two colours adjacent in the order, (x, y)
   parity fixed and z parity 0 then 1, on whole z-lines per CTA with a block barrier between;
 - plane pairs: two launches per sweep, all x-even planes then all x-odd planes, one thread-block
-  cluster per plane running its four (y, z) colours between cluster barriers.
+  cluster per plane running its four (y, z) colours between cluster barriers;
+- staged line pairs: the line-pair schedule with each CTA's neighbourhood tile (u of three
+  planes, the lines' rows and their neighbours, and the moduli) copied to shared memory first.
 
 All forms run the same node updates on the same operands in the same order, so mixed-precision
 solves whose V-cycles use one or another give bit-identical iterates: pre- and post-smoothing
@@ -52,7 +54,7 @@ def _solve(monkeypatch, mode, ne, levels, bbox=None, mask_layer=None, partial=Fa
 ])
 def test_fused_sweeps_equal_colour_sweeps(gpu, monkeypatch, ne, levels, kw):
     xa, ia = _solve(monkeypatch, "colours", ne, levels, **kw)
-    for mode in ("lines", "planes"):
+    for mode in ("lines", "planes", "staged"):
         xb, ib = _solve(monkeypatch, mode, ne, levels, **kw)
         assert ia == ib, mode
         np.testing.assert_array_equal(xa, xb, err_msg=mode)

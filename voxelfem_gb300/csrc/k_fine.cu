@@ -90,12 +90,14 @@ __device__ __forceinline__ void gather_ku(const Geom &g, const Mat24<T> &K, cons
 // cube elements, the 10 class values of k0_cube_class held in registers.
 template <typename T, bool Cube>
 struct K0View {
+    static constexpr bool kCube = false;
     const Mat24<T> &K;
     __device__ explicit K0View(const Mat24<T> &K_) : K(K_) {}
     __device__ __forceinline__ T operator()(int row, int col) const { return K.a[row * 24 + col]; }
 };
 template <typename T>
 struct K0View<T, true> {
+    static constexpr bool kCube = true;
     T kv[10];
     __device__ explicit K0View(const Mat24<T> &K) {
 #pragma unroll
@@ -359,10 +361,34 @@ __device__ __forceinline__ void gs_visit_planes(const KV &K, const T (&Plo)[9][3
     s0 -= e * c0;
     s1 -= e * c1;
     s2 -= e * c2;
+    if constexpr (!KV::kCube) {
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) M[3 * r + c] += e * K(3 * LN + r, 3 * LN + c);
+            for (int c = 0; c < 3; ++c) M[3 * r + c] += e * K(3 * LN + r, 3 * LN + c);
+    }
+}
+
+// Diagonal block of a node for cube elements: K0's node blocks have the diagonal entry of class
+// 0 and the off-diagonal entries (d, r) of class 8 with sign xi[d] xi[r], the node's sides
+// along axes d and r (k0_cube_class), so M = kv[0] sum(E) I + kv[8] (signed sums of E): 28
+// additions instead of 72 FMAs.
+template <typename T>
+__device__ __forceinline__ void cube_diag_block(const K0View<T, true> &K, const T (&E)[8], T *M) {
+    T sE = T(0), sxy = T(0), sxz = T(0), syz = T(0);
+#pragma unroll
+    for (int ln = 0; ln < 8; ++ln) {
+        const int bx = (ln >> 2) & 1, by = (ln >> 1) & 1, bz = ln & 1;
+        sE += E[ln];
+        sxy += (bx == by) ? E[ln] : -E[ln];
+        sxz += (bx == bz) ? E[ln] : -E[ln];
+        syz += (by == bz) ? E[ln] : -E[ln];
+    }
+    const T d = K.kv[0], o = K.kv[8];
+    M[0] = M[4] = M[8] = d * sE;
+    M[1] = M[3] = o * sxy;
+    M[2] = M[6] = o * sxz;
+    M[5] = M[7] = o * syz;
 }
 
 // FP32 block Gauss-Seidel update of node (i, j, k) from its register neighbourhood (incident
@@ -392,6 +418,7 @@ __device__ __forceinline__ void gs_node_fp32(const Geom &g, const KV &Kv, const 
     gs_visit_planes<float, 0, 0, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
     gs_visit_planes<float, 0, 1, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
     gs_visit_planes<float, 0, 0, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    if constexpr (KV::kCube) cube_diag_block<float>(Kv, E, M);
     smooth_node_solve<float>(dm, s0, s1, s2, M, forward, u0, u1, u2);
     u[n] = u0;
     u[ld + n] = u1;
@@ -513,6 +540,124 @@ __global__ void __launch_bounds__(BS, MB) gs_fine_lines_kernel(Geom g, const flo
             const int ii = (int)((uint32_t)line / (uint32_t)n1), jj = line - ii * n1;
             const int j = cy + 2 * jj;
             if (j < nyv) gs_node_fp32(g, Kv, Y, u, b, dmask, cx + 2 * ii, j, cz + 2 * kk, forward != 0);
+        }
+        if (s == 0) __syncthreads();
+    }
+}
+
+// Staged line-pair sweep: the line-pair schedule with the CTA's neighbourhood in shared memory.
+// A CTA owns linesPerCta consecutive lines (rows j = cy + 2 jj) of one x-plane i. It copies the
+// u values of planes i-1..i+1, rows jbase..jbase+R-1 (R = 2 lines + 1, jbase the row below the
+// first line) and z = -1..nz into shared memory, and the padded moduli of element planes
+// i-1, i and element rows jbase..jbase+R-2, from the very addresses the other forms read. Each
+// node then gathers its neighbourhood from shared memory; an update is written to shared and
+// global memory (the second colour reads the first colour's updates from the tile). No other
+// CTA reads this CTA's lines during the launch, so the tile stays exact; the arithmetic is the
+// other forms', so are the iterates.
+struct StagedTile {
+    int R, NZ2, EZ2;  // rows, z extent with halo (nz + 2), padded element z extent (ne + 2)
+    __device__ int uIdx(int c, int a, int r, int kk) const { return ((c * 3 + a) * R + r) * NZ2 + kk; }
+    __device__ int eIdx(int a, int r, int kk) const { return (a * (R - 1) + r) * EZ2 + kk; }
+};
+
+template <typename KV>
+__device__ __forceinline__ void gs_node_fp32_staged(const Geom &g, const KV &Kv, const StagedTile &T,
+                                                    const float *sU0, float *sU, const float *sE, float *u,
+                                                    const float *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                    int i, int j, int k, int jbase, bool forward) {
+    const int64_t n = g.node(i, j, k), ld = g.ld;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    float s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    float M[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float E[8], Pa[9][3], Pb[9][3];
+    const int r0 = j - jbase, kk0 = k + 1;  // the node's tile row and z index
+    // E[4A + 2B + C]: element (i - A, j - B, k - C), element plane a = 1 - A, row r0 - B
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int A = (s >> 2) & 1, B = (s >> 1) & 1, C = s & 1;
+        E[s] = sE[T.eIdx(1 - A, r0 - B, k - C + 1)];
+    }
+    auto plane = [&](int a, float (&P)[9][3]) {
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) P[3 * bb + c][d] = sU0[T.uIdx(d, a, r0 + bb - 1, kk0 + c - 1)];
+    };
+    plane(0, Pa);
+    plane(1, Pb);
+    gs_visit_planes<float, 1, 1, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 0, 1>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 1, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    gs_visit_planes<float, 1, 0, 0>(Kv, Pa, Pb, E, s0, s1, s2, M);
+    float u0 = Pb[4][0], u1 = Pb[4][1], u2 = Pb[4][2];
+    plane(2, Pa);
+    gs_visit_planes<float, 0, 1, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 0, 1>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 1, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    gs_visit_planes<float, 0, 0, 0>(Kv, Pb, Pa, E, s0, s1, s2, M);
+    if constexpr (KV::kCube) cube_diag_block<float>(Kv, E, M);
+    smooth_node_solve<float>(dm, s0, s1, s2, M, forward, u0, u1, u2);
+    sU[T.uIdx(0, 1, r0, kk0)] = u0;
+    sU[T.uIdx(1, 1, r0, kk0)] = u1;
+    sU[T.uIdx(2, 1, r0, kk0)] = u2;
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
+template <bool Cube>
+__global__ void __launch_bounds__(BS, 3) gs_fine_staged_kernel(Geom g, const float *__restrict__ Y, float *u,
+                                                              const float *__restrict__ b,
+                                                              const uint8_t *__restrict__ dmask, int cx, int cy,
+                                                              int linesPerCta, int forward, const Mat24<float> K) {
+    VFEM_PDL_ENTRY();
+    extern __shared__ float staged[];
+    const int n1 = (g.nn[1] - cy + 1) / 2;
+    const int i = cx + 2 * (int)blockIdx.y;
+    const int jj0 = (int)blockIdx.x * linesPerCta;
+    const int nl = min(linesPerCta, n1 - jj0);
+    const int nyv = g.nyv();
+    StagedTile T;
+    T.R = 2 * linesPerCta + 1;
+    T.NZ2 = g.nn[2] + 2;
+    T.EZ2 = g.ne[2] + 2;
+    const int jbase = cy + 2 * jj0 - 1;
+    float *sU = staged;
+    float *sE = staged + 9 * T.R * T.NZ2;
+    // the tile: the addresses the unstaged forms gather from (guarded vector, padded moduli)
+    const int64_t ld = g.ld;
+    const int nU = 9 * T.R * T.NZ2;
+    for (int q = threadIdx.x; q < nU; q += BS) {
+        const int kk = q % T.NZ2, rest = q / T.NZ2;
+        const int r = rest % T.R, ca = rest / T.R;
+        const int a = ca % 3, c = ca / 3;
+        // rows past nn[1] belong only to missing lines of the last CTA; row nn[1] itself (the one
+        // past the last line) and planes / rows / z at -1 stay inside the vector's guard
+        const int jr = jbase + r;
+        sU[q] = jr <= g.nn[1] ? u[c * ld + g.node(i - 1 + a, jr, kk - 1)] : 0.f;
+    }
+    const int nE = 2 * (T.R - 1) * T.EZ2;
+    for (int q = threadIdx.x; q < nE; q += BS) {
+        const int kk = q % T.EZ2, rest = q / T.EZ2;
+        const int r = rest % (T.R - 1), a = rest / (T.R - 1);
+        const int je = min(jbase + r, g.ne[1]);  // rows past the grid read the zero ghost row
+        sE[q] = Y[g.padElem(i - 1 + a, je, kk - 1)];
+    }
+    __syncthreads();
+    const K0View<float, Cube> Kv(K);
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        const int cz = forward ? s : 1 - s;
+        const int nk = (g.nn[2] - cz + 1) / 2;
+        const int cnt = nl > 0 ? nl * nk : 0;
+        for (int t = threadIdx.x; t < cnt; t += BS) {
+            const int q = (int)((uint32_t)t / (uint32_t)nk), kk = t - q * nk;
+            const int j = cy + 2 * (jj0 + q);
+            if (j < nyv)
+                gs_node_fp32_staged(g, Kv, T, sU, sU, sE, u, b, dmask, i, j, cz + 2 * kk, jbase, forward != 0);
         }
         if (s == 0) __syncthreads();
     }
@@ -853,7 +998,37 @@ int gsFineMode() {
     const std::string m(e);
     if (m == "colours") return GS_COLOURS;
     if (m == "planes") return GS_PLANES;
+    if (m == "staged") return GS_STAGED;
     return GS_LINES;
+}
+
+// Lines per CTA of the staged sweep and its shared-memory bytes: about one 256-thread round of
+// nodes per colour, within the 227 KB a CTA may use.
+static int stagedLines(const Geom &g) { return std::max(1, BS / ((g.nn[2] + 1) / 2)); }
+static size_t stagedBytes(const Geom &g, int lines) {
+    const int R = 2 * lines + 1;
+    return sizeof(float) * ((size_t)9 * R * (g.nn[2] + 2) + (size_t)2 * (R - 1) * (g.ne[2] + 2));
+}
+
+bool gsStagedFits(const Geom &g) { return stagedBytes(g, stagedLines(g)) <= 72 * 1024; }  // three CTAs per SM
+
+void launch_gs_fine_staged(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                           int cy, bool forward, const Mat24<float> &K0, cudaStream_t st) {
+    const int planes = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2;
+    if (planes <= 0 || n1 <= 0) return;
+    const int L = stagedLines(g);
+    const size_t smem = stagedBytes(g, L);
+    if (smem > 227 * 1024) throw Error(ERR_ARG, "staged sweep: tile too large for shared memory");
+    static bool attrSet[2] = {false, false};
+    auto kern = K0.isCube ? gs_fine_staged_kernel<true> : gs_fine_staged_kernel<false>;
+    const int ki = K0.isCube ? 1 : 0;
+    if (!attrSet[ki]) {
+        VFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attrSet[ki] = true;
+    }
+    const dim3 grid((unsigned)((n1 + L - 1) / L), (unsigned)planes);
+    launch_pdl(kern, grid, BS, smem, st, g, Y, u, b, dmask, cx, cy, L, forward ? 1 : 0, K0);
+    VFEM_LAUNCH_CHECK();
 }
 
 void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,

@@ -566,7 +566,8 @@ void MG::setupCoarsestIndex() {
 }
 
 void MG::setSweepForm(int form) {
-    if (form != GS_LINES && form != GS_COLOURS && form != GS_PLANES) throw Error(ERR_ARG, "unknown sweep form");
+    if (form != GS_LINES && form != GS_COLOURS && form != GS_PLANES && form != GS_STAGED)
+        throw Error(ERR_ARG, "unknown sweep form");
     if (form != sweepForm) {
         sweepForm = form;
         clearGraphs();  // captured V-cycles hold the launches of the previous form
@@ -814,12 +815,17 @@ void MG::smoothT(int l, bool forward) {
                                       Tr<T>::K0(*fine), st);
             return;
         }
-        if (mode == GS_LINES) {
+        if (mode == GS_LINES || mode == GS_STAGED) {
             // four launches: colour pairs (0, 1), (2, 3), (4, 5), (6, 7), reversed backward
+            const bool staged = mode == GS_STAGED && gsStagedFits(lv[0].g);
             for (int h = 0; h < 4; ++h) {
                 const int c = forward ? h : 3 - h;
-                launch_gs_fine_lines(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1, forward,
-                                     Tr<T>::K0(*fine), st);
+                if (staged)
+                    launch_gs_fine_staged(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1,
+                                          forward, Tr<T>::K0(*fine), st);
+                else
+                    launch_gs_fine_lines(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1,
+                                         forward, Tr<T>::K0(*fine), st);
             }
             return;
         }

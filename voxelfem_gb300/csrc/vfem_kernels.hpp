@@ -88,7 +88,12 @@ void launch_gs_fine_lines(const Geom &g, const float *Y, float *u, const float *
                           int cy, bool forward, const Mat24<float> &K0, cudaStream_t st);
 // Form of the FP32 fine sweep: four line-pair launches (default), two plane-pair launches or
 // eight colour launches (VFEM_GS_MODE = lines / planes / colours).
-enum { GS_COLOURS = 0, GS_LINES = 1, GS_PLANES = 2 };
+enum { GS_COLOURS = 0, GS_LINES = 1, GS_PLANES = 2, GS_STAGED = 3 };
+// The line-pair sweep with each CTA's neighbourhood staged in shared memory; gsStagedFits says
+// whether the tile of this grid fits (long z lines do not).
+void launch_gs_fine_staged(const Geom &g, const float *Y, float *u, const float *b, const uint8_t *dmask, int cx,
+                           int cy, bool forward, const Mat24<float> &K0, cudaStream_t st);
+bool gsStagedFits(const Geom &g);
 int gsFineMode();
 // Resident blocks per SM the FP32 cube-voxel fine kernels are fitted to (VFEM_FINE_OCC = 2, 3 or
 // 4; 0: the defaults, four for the residual and three for the Gauss-Seidel sweep, whose 80-register

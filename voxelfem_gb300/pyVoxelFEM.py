@@ -664,11 +664,11 @@ class MultigridSolver:
         check(_lib().vfem_mg_set_precision(self._h, p, m))
         self._prec = precision
 
-    SWEEP_FORMS = {"colours": 0, "lines": 1, "planes": 2}
+    SWEEP_FORMS = {"colours": 0, "lines": 1, "planes": 2, "staged": 3}
 
     def setSweepForm(self, form):
         """Form of the FP32 fine Gauss-Seidel sweep of the mixed V-cycle: 'lines' (default),
-        'colours' or 'planes'; every form gives identical iterates."""
+        'staged', 'colours' or 'planes'; every form gives identical iterates."""
         check(_lib().vfem_mg_set_sweep_form(self._h, self.SWEEP_FORMS[form]))
 
     def stiffnessRebuilds(self):
