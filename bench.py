@@ -368,6 +368,17 @@ def run_ours(args):
     r[sim.getDirichletMask()] = 0
     true_rel = float(np.linalg.norm(r) / np.linalg.norm(b_host))
 
+    # ---------------- the same mixed solve with bf16 smoothing-level stencils ----------------
+    _capi.check(lib.vfem_mg_set_stencil_bf16(mg._h, 1))
+    for _ in range(2):
+        step_device()
+    tbf, _, (itbf, rrbf) = timed(step_device, args.steps)
+    compbf = 0.5 * float(torch.dot(b_d.flatten(), x_d.flatten()))
+    _capi.check(lib.vfem_mg_set_stencil_bf16(mg._h, 0))
+    bf16_stencils = {"s_per_solve": tbf / args.steps, "iterations": int(itbf), "relres": rrbf,
+                     "compliance_rel_err_vs_fp64": abs(compbf - comp64) / abs(comp64)}
+    step_device()  # back to the FP32 stencils before the end-to-end leg
+
     # ---------------- end to end through the public API, pinned host buffers ----------------
     rho_p = torch.from_numpy(rho).pin_memory()
     b_p = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
@@ -425,6 +436,13 @@ def run_ours(args):
         kernels["gs_fine_sweep_fp32_" + mode] = {"ms": ms.value, "bytes": nbytes.value,
                                                   "gbs": nbytes.value / (ms.value * 1e-3) / 1e9}
     del os.environ["VFEM_GS_MODE"]
+    # the level-1 and level-2 passes with bf16 stencils
+    _capi.check(lib.vfem_mg_set_stencil_bf16(mg._h, 1))
+    for kid in (6, 7, 8):
+        ms, nbytes = C.c_double(), C.c_double()
+        _capi.check(lib.vfem_mg_time_kernel(mg._h, kid, 20, C.byref(ms), C.byref(nbytes)))
+        kernels[KERNEL_NAMES[kid] + "_bf16_stencil"] = {"ms": ms.value}
+    _capi.check(lib.vfem_mg_set_stencil_bf16(mg._h, 0))
     # register budgets of the FP32 fine kernels: fitted to 3 or 4 resident 256-thread blocks per SM
     for occ in ("2", "3", "4"):
         os.environ["VFEM_FINE_OCC"] = occ
@@ -507,6 +525,7 @@ def run_ours(args):
             "fp64": {"s_per_solve": t64, "iterations": int(it64), "relres": rr64, "compliance": comp64,
                      "steps": k64},
             "speedup_mixed_vs_fp64": t64 / tmix_step,
+            "mixed_bf16_stencils": bf16_stencils,
             "compliance_rel_err_mixed_vs_fp64": abs(compm - comp64) / abs(comp64),
             "applyk_gbs": {"fp32": kernels["applyk_fine_fp32"]["gbs"], "fp64": kernels["applyk_fine_fp64"]["gbs"],
                            "df": kernels["applyk_fine_df"]["gbs"],

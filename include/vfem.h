@@ -177,6 +177,10 @@ int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, 
 #define VFEM_SWEEP_PLANES 2
 #define VFEM_SWEEP_STAGED 3 /* VFEM_SWEEP_LINES with each CTA's neighbourhood staged in shared memory */
 int vfem_mg_set_sweep_form(vfem_mg *mg, int form);
+/* Mixed precision (no reference counterpart): store the assembled stencils of the smoothing
+ * levels 1 .. L-2 in bf16 (on != 0) instead of FP32; they are read and applied in FP32 and the
+ * coarsest level stays FP32. The outer FP64 CG keeps the solution's accuracy. */
+int vfem_mg_set_stencil_bf16(vfem_mg *mg, int on);
 /* Diagnostic (no reference counterpart): how many hierarchy rebuilds this solver ran in full and
  * how many as band-partial updates after a fabrication-mask change (the reference's
  * m_partialStiffnessMatrixUpdate, MultigridSolver.hh:907-1017). */

@@ -107,6 +107,7 @@ _SIGS = {
     "vfem_mg_set_device_loop": (C.c_int, [_vp, C.c_int]),
     "vfem_mg_stiffness_rebuilds": (C.c_int, [_vp, _i64, _i64]),
     "vfem_mg_set_sweep_form": (C.c_int, [_vp, C.c_int]),
+    "vfem_mg_set_stencil_bf16": (C.c_int, [_vp, C.c_int]),
     "vfem_lbl_set_sweep_form": (C.c_int, [_vp, C.c_int]),
     "vfem_mg_set_symmetric_gs": (C.c_int, [_vp, C.c_int]),
     "vfem_mg_set_mask_layer": (C.c_int, [_vp, C.c_int64]),

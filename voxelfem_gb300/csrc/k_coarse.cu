@@ -11,6 +11,7 @@
 //    (stencil::colour_pos); one thread per node, and a colour pass reads contiguous slices.
 // Element-matrix layout (levels >= 1): Ke[e*576 + 24*row + col].
 #include <algorithm>
+#include <type_traits>
 
 #include "vfem_kernels.hpp"
 #include "vfem_reduce.cuh"
@@ -90,21 +91,21 @@ constexpr int SPLIT_BS = SPLIT_SUB * SPLIT_NODES;
 
 __device__ __forceinline__ void split_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(SPLIT_BS) : "memory"); }
 
-template <typename T>
-__device__ __forceinline__ void split_rows(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+template <typename T, typename TS>
+__device__ __forceinline__ void split_rows(const Geom &g, const TS *__restrict__ S, const T *__restrict__ u,
                                            int64_t n, int64_t p, int i, int j, int k, bool active, int sub, int lane,
                                            T (*part)[SPLIT_ROWS][SPLIT_NODES]) {
     T f0 = T(0), f1 = T(0), f2 = T(0);
-    if (active) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
+    if (active) stencil::stencil_row_part<T, TS>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
     part[0][sub - 1][lane] = f0;
     part[1][sub - 1][lane] = f1;
     part[2][sub - 1][lane] = f2;
     split_barrier();
 }
 
-template <typename T, bool ZeroInit, bool Negate>
+template <typename T, typename TS, bool ZeroInit, bool Negate>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
-    stencil_apply_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, T *__restrict__ out) {
+    stencil_apply_soa_kernel(Geom g, const TS *__restrict__ S, const T *__restrict__ u, T *__restrict__ out) {
     VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
     const int lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     if (valid) stencil::colour_node(g, p, i, j, k);
     const int64_t n = g.node(i, j, k), ld = g.ld;
     if (sub > 0) {
-        split_rows<T>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
+        split_rows<T, TS>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
         return;
     }
     T o[3] = {T(0), T(0), T(0)};
@@ -132,9 +133,9 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     out[2 * ld + n] = o[2] + f2;
 }
 
-template <typename T>
+template <typename T, typename TS>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
-    stencil_residual_soa_kernel(Geom g, const T *__restrict__ S, const T *__restrict__ u, const T *__restrict__ b,
+    stencil_residual_soa_kernel(Geom g, const TS *__restrict__ S, const T *__restrict__ u, const T *__restrict__ b,
                                 T *__restrict__ r, const uint8_t *__restrict__ dmask) {
     VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     if (valid) stencil::colour_node(g, p, i, j, k);
     const int64_t n = g.node(i, j, k), ld = g.ld;
     if (sub > 0) {
-        split_rows<T>(g, S, u, n, p, i, j, k, valid && j < g.nyv(), sub, lane, part);
+        split_rows<T, TS>(g, S, u, n, p, i, j, k, valid && j < g.nyv(), sub, lane, part);
         return;
     }
     T bb[3] = {T(0), T(0), T(0)};
@@ -164,9 +165,9 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     r[2 * ld + n] = (dm & 4) ? T(0) : bb[2] - f2;
 }
 
-template <typename T>
+template <typename T, typename TS>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
-    gs_stencil_color_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+    gs_stencil_color_soa_kernel(Geom g, const TS *__restrict__ S, T *u, const T *__restrict__ b,
                                 const uint8_t *__restrict__ dmask, int cx, int cy, int cz, int forward) {
     VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     const int64_t n = g.node(i, j, k), ld = g.ld;
     const int64_t p = stencil::colour_pos(g, i, j, k);
     if (sub > 0) {
-        split_rows<T>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
+        split_rows<T, TS>(g, S, u, n, p, i, j, k, valid, sub, lane, part);
         return;
     }
     T M[9], bb[3], uu[3];
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
     if (valid) {
         dm = dmask[n];
 #pragma unroll
-        for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)e * ld + p];  // diagonal block (offset 13)
+        for (int e = 0; e < 9; ++e) M[e] = stencil::sval<T>(S[(int64_t)e * ld + p]);  // diagonal block (offset 13)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             bb[c] = b[c * ld + n];
@@ -219,9 +220,9 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
 // a block barrier, then the second colour's; nodes go 32 at a time through the split form of
 // gs_stencil_color_soa_kernel (same partial sums, same order, so the iterates are identical).
 // Four launches per sweep instead of eight: the small levels' passes are launch-latency bound.
-template <typename T>
+template <typename T, typename TS>
 __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
-    gs_stencil_lines_soa_kernel(Geom g, const T *__restrict__ S, T *u, const T *__restrict__ b,
+    gs_stencil_lines_soa_kernel(Geom g, const TS *__restrict__ S, T *u, const T *__restrict__ b,
                                 const uint8_t *__restrict__ dmask, int cx, int cy, int linesPerBlock, int forward) {
     VFEM_PDL_ENTRY();
     __shared__ T part[3][SPLIT_ROWS][SPLIT_NODES];
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
             const int64_t p = stencil::colour_pos(g, i, j, k);
             if (sub > 0) {
                 T f0 = T(0), f1 = T(0), f2 = T(0);
-                if (valid) stencil::stencil_row_part<T>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
+                if (valid) stencil::stencil_row_part<T, TS>(g, S, u, n, p, i, j, k, sub - 1, f0, f1, f2);
                 part[0][sub - 1][lane] = f0;
                 part[1][sub - 1][lane] = f1;
                 part[2][sub - 1][lane] = f2;
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(SPLIT_BS, sizeof(T) == 4 ? 4 : 2)
                 if (valid) {
                     dm = dmask[n];
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) M[e] = S[(int64_t)e * ld + p];  // diagonal block (offset 13)
+                    for (int e = 0; e < 9; ++e) M[e] = stencil::sval<T>(S[(int64_t)e * ld + p]);  // diagonal block (offset 13)
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         bb[c] = b[c * ld + n];
@@ -425,9 +426,9 @@ __global__ void __launch_bounds__(ROW) stencil_level1_kernel(Geom g1, Geom g0, c
 // stored half), writing the nine entries of block (n, n+o). The Kc indices are warp-uniform (constant-cache
 // broadcasts) and the eight fine moduli of each shared coarse element are loaded once for
 // all nine entries.
-template <typename T>
+template <typename T, typename TS>
 __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0, const T *__restrict__ Y0,
-                                                                const T *__restrict__ Kc, T *__restrict__ S, int rowLo,
+                                                                const T *__restrict__ Kc, TS *__restrict__ S, int rowLo,
                                                                 int rowHi) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
     const int o = 13 + blockIdx.y;
@@ -467,7 +468,7 @@ __global__ void __launch_bounds__(BS) stencil_level1_soa_kernel(Geom g1, Geom g0
                     }
             }
 #pragma unroll
-    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g1.ld + p] = acc[e];
+    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g1.ld + p] = stencil::sstore<TS>(acc[e]);
 }
 
 // Level-2 element matrices straight from the fine moduli: Ke_2(e) = sum over the 64 fine
@@ -606,9 +607,9 @@ __global__ void __launch_bounds__(ROW) stencil_from_ke_kernel(Geom g, const T *_
     S[n * ROW + q] = acc;
 }
 
-template <typename T>
+template <typename T, typename TS>
 __global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T *__restrict__ Ke,
-                                                                 T *__restrict__ S, int rowLo, int rowHi) {
+                                                                 TS *__restrict__ S, int rowLo, int rowHi) {
     const int64_t p = blockIdx.x * (int64_t)BS + threadIdx.x;
     const int o = 13 + blockIdx.y;
     if (p >= g.NN) return;
@@ -637,70 +638,91 @@ __global__ void __launch_bounds__(BS) stencil_from_ke_soa_kernel(Geom g, const T
                     for (int c = 0; c < 3; ++c) acc[3 * r + c] += ke[(3 * ln + r) * 24 + 3 * lm + c];
             }
 #pragma unroll
-    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g.ld + p] = acc[e];
+    for (int e = 0; e < 9; ++e) S[(int64_t)((o - 13) * 9 + e) * g.ld + p] = stencil::sstore<TS>(acc[e]);
 }
 
 }  // namespace
 
-template <typename T>
-void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
+// Node-contiguous rows keep the arithmetic type; only plane-layout stencils may be stored in bf16.
+template <typename T, typename TS>
+static void rowsNeedSameType(bool rows) {
+    if (rows && !std::is_same<T, TS>::value) throw Error(ERR_ARG, "bf16 stencils need the plane layout");
+}
+
+template <typename T, typename TS>
+void launch_stencil_apply(const Geom &g, const TS *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
                           cudaStream_t st) {
+    rowsNeedSameType<T, TS>(rows);
     if (!rows) {
         const unsigned gs = gridFor(g.NN, SPLIT_NODES);
         if (zeroInit) {
-            if (negate) launch_pdl(stencil_apply_soa_kernel<T, true, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
-            else launch_pdl(stencil_apply_soa_kernel<T, true, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            if (negate) launch_pdl(stencil_apply_soa_kernel<T, TS, true, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_soa_kernel<T, TS, true, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
         } else {
-            if (negate) launch_pdl(stencil_apply_soa_kernel<T, false, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
-            else launch_pdl(stencil_apply_soa_kernel<T, false, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            if (negate) launch_pdl(stencil_apply_soa_kernel<T, TS, false, true>, gs, SPLIT_BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_soa_kernel<T, TS, false, false>, gs, SPLIT_BS, 0, st, g, S, u, out);
         }
         VFEM_LAUNCH_CHECK();
         return;
     }
-    const unsigned grid = gridFor(g.NN, WPB);
-    if (zeroInit) {
-        if (negate) launch_pdl(stencil_apply_kernel<T, true, true>, grid, BS, 0, st, g, S, u, out);
-        else launch_pdl(stencil_apply_kernel<T, true, false>, grid, BS, 0, st, g, S, u, out);
-    } else {
-        if (negate) launch_pdl(stencil_apply_kernel<T, false, true>, grid, BS, 0, st, g, S, u, out);
-        else launch_pdl(stencil_apply_kernel<T, false, false>, grid, BS, 0, st, g, S, u, out);
+    if constexpr (std::is_same<T, TS>::value) {
+        const unsigned grid = gridFor(g.NN, WPB);
+        if (zeroInit) {
+            if (negate) launch_pdl(stencil_apply_kernel<T, true, true>, grid, BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_kernel<T, true, false>, grid, BS, 0, st, g, S, u, out);
+        } else {
+            if (negate) launch_pdl(stencil_apply_kernel<T, false, true>, grid, BS, 0, st, g, S, u, out);
+            else launch_pdl(stencil_apply_kernel<T, false, false>, grid, BS, 0, st, g, S, u, out);
+        }
+        VFEM_LAUNCH_CHECK();
     }
-    VFEM_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
+template <typename T, typename TS>
+void launch_stencil_residual(const Geom &g, const TS *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st) {
-    if (rows) launch_pdl(stencil_residual_kernel<T>, gridFor(g.NN, WPB), BS, 0, st, g, S, u, b, r, dmask);
-    else launch_pdl(stencil_residual_soa_kernel<T>, gridFor(g.NN, SPLIT_NODES), SPLIT_BS, 0, st, g, S, u, b, r, dmask);
+    rowsNeedSameType<T, TS>(rows);
+    if constexpr (std::is_same<T, TS>::value) {
+        if (rows) {
+            launch_pdl(stencil_residual_kernel<T>, gridFor(g.NN, WPB), BS, 0, st, g, S, u, b, r, dmask);
+            VFEM_LAUNCH_CHECK();
+            return;
+        }
+    }
+    launch_pdl(stencil_residual_soa_kernel<T, TS>, gridFor(g.NN, SPLIT_NODES), SPLIT_BS, 0, st, g, S, u, b, r, dmask);
     VFEM_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
-                             bool rows, cudaStream_t st) {
+template <typename T, typename TS>
+void launch_gs_stencil_color(const Geom &g, const TS *S, T *u, const T *b, const uint8_t *dmask, int color,
+                             bool forward, bool rows, cudaStream_t st) {
+    rowsNeedSameType<T, TS>(rows);
     const int cx = (color >> 2) & 1, cy = (color >> 1) & 1, cz = color & 1;
     const int64_t n0 = (g.nn[0] - cx + 1) / 2, n1 = (g.nn[1] - cy + 1) / 2, n2 = (g.nn[2] - cz + 1) / 2;
     if (n1 <= 0) return;
-    if (rows)
-        launch_pdl(gs_stencil_color_kernel<T>, gridFor(n0 * n1 * n2, WPB), BS, 0, st, g, S, u, b, dmask, cx, cy, cz,
-                                                                               forward ? 1 : 0);
-    else
-        launch_pdl(gs_stencil_color_soa_kernel<T>, gridFor(n0 * n1 * n2, SPLIT_NODES), SPLIT_BS, 0, st, 
-            g, S, u, b, dmask, cx, cy, cz, forward ? 1 : 0);
+    if constexpr (std::is_same<T, TS>::value) {
+        if (rows) {
+            launch_pdl(gs_stencil_color_kernel<T>, gridFor(n0 * n1 * n2, WPB), BS, 0, st, g, S, u, b, dmask, cx, cy,
+                       cz, forward ? 1 : 0);
+            VFEM_LAUNCH_CHECK();
+            return;
+        }
+    }
+    launch_pdl(gs_stencil_color_soa_kernel<T, TS>, gridFor(n0 * n1 * n2, SPLIT_NODES), SPLIT_BS, 0, st, g, S, u, b,
+               dmask, cx, cy, cz, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_gs_stencil_lines(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
+template <typename T, typename TS>
+void launch_gs_stencil_lines(const Geom &g, const TS *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
                              bool forward, cudaStream_t st) {
     const int nlines = ((g.nn[0] - cx + 1) / 2) * ((g.nn[1] - cy + 1) / 2);
     if (nlines <= 0) return;
     // short lines share a 32-node round
     const int nk = (g.nn[2] + 1) / 2;
     const int per = std::max(1, SPLIT_NODES / nk);
-    launch_pdl(gs_stencil_lines_soa_kernel<T>, (unsigned)((nlines + per - 1) / per), SPLIT_BS, 0, st, g, S, u, b,
-               dmask, cx, cy, per, forward ? 1 : 0);
+    launch_pdl(gs_stencil_lines_soa_kernel<T, TS>, (unsigned)((nlines + per - 1) / per), SPLIT_BS, 0, st, g, S, u,
+               b, dmask, cx, cy, per, forward ? 1 : 0);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -751,17 +773,21 @@ void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, 
     VFEM_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st,
+template <typename T, typename TS>
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, TS *S, bool rows, cudaStream_t st,
                            int rowLo, int rowHi) {
     if (g1.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
-    if (rows) {
-        if (rowLo > 0 || rowHi < g1.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
-        stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
-    } else {
-        stencil_level1_soa_kernel<T><<<dim3(gridFor(g1.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g1, g0, Y0, Kc,
-                                                                                                     S, rowLo, rowHi);
+    rowsNeedSameType<T, TS>(rows);
+    if constexpr (std::is_same<T, TS>::value) {
+        if (rows) {
+            if (rowLo > 0 || rowHi < g1.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
+            stencil_level1_kernel<T><<<(unsigned)g1.NN, ROW, 0, st>>>(g1, g0, Y0, Kc, S);
+            VFEM_LAUNCH_CHECK();
+            return;
+        }
     }
+    stencil_level1_soa_kernel<T, TS><<<dim3(gridFor(g1.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g1, g0, Y0, Kc, S,
+                                                                                                     rowLo, rowHi);
     VFEM_LAUNCH_CHECK();
 }
 
@@ -786,39 +812,48 @@ void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_
     VFEM_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st, int rowLo, int rowHi) {
+template <typename T, typename TS>
+void launch_stencil_from_ke(const Geom &g, const T *Ke, TS *S, bool rows, cudaStream_t st, int rowLo, int rowHi) {
     if (g.NN > 2147483647LL) throw Error(ERR_ARG, "too many nodes");
-    if (rows) {
-        if (rowLo > 0 || rowHi < g.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
-        stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
-    } else {
-        stencil_from_ke_soa_kernel<T><<<dim3(gridFor(g.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g, Ke, S, rowLo,
-                                                                                                     rowHi);
+    rowsNeedSameType<T, TS>(rows);
+    if constexpr (std::is_same<T, TS>::value) {
+        if (rows) {
+            if (rowLo > 0 || rowHi < g.nn[1]) throw Error(ERR_ARG, "band updates need plane-layout stencils");
+            stencil_from_ke_kernel<T><<<(unsigned)g.NN, ROW, 0, st>>>(g, Ke, S);
+            VFEM_LAUNCH_CHECK();
+            return;
+        }
     }
+    stencil_from_ke_soa_kernel<T, TS><<<dim3(gridFor(g.NN, BS), stencil::HALF_OFFSETS), BS, 0, st>>>(g, Ke, S, rowLo,
+                                                                                                     rowHi);
     VFEM_LAUNCH_CHECK();
 }
 
+#define VFEM_INST_STENCIL(T, TS)                                                                                      \
+    template void launch_stencil_apply<T, TS>(const Geom &, const TS *, const T *, T *, bool, bool, bool, cudaStream_t); \
+    template void launch_stencil_residual<T, TS>(const Geom &, const TS *, const T *, const T *, T *, const uint8_t *,   \
+                                                 bool, cudaStream_t);                                                    \
+    template void launch_gs_stencil_color<T, TS>(const Geom &, const TS *, T *, const T *, const uint8_t *, int, bool,   \
+                                                 bool, cudaStream_t);                                                    \
+    template void launch_gs_stencil_lines<T, TS>(const Geom &, const TS *, T *, const T *, const uint8_t *, int, int,    \
+                                                 bool, cudaStream_t);                                                    \
+    template void launch_stencil_level1<T, TS>(const Geom &, const Geom &, const T *, const T *, TS *, bool,             \
+                                               cudaStream_t, int, int);                                                 \
+    template void launch_stencil_from_ke<T, TS>(const Geom &, const T *, TS *, bool, cudaStream_t, int, int);
+VFEM_INST_STENCIL(double, double)
+VFEM_INST_STENCIL(float, float)
+VFEM_INST_STENCIL(float, __nv_bfloat16)
+
 #define VFEM_INST_COARSE(T)                                                                                           \
-    template void launch_stencil_apply<T>(const Geom &, const T *, const T *, T *, bool, bool, bool, cudaStream_t);   \
-    template void launch_stencil_residual<T>(const Geom &, const T *, const T *, const T *, T *, const uint8_t *,     \
-                                             bool, cudaStream_t);                                                     \
-    template void launch_gs_stencil_color<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, bool,     \
-                                             bool, cudaStream_t);                                                     \
     template void launch_restrict<T>(const Geom &, const Geom &, const T *, T *, cudaStream_t);                       \
-    template void launch_gs_stencil_lines<T>(const Geom &, const T *, T *, const T *, const uint8_t *, int, int,      \
-                                             bool, cudaStream_t);                                                     \
     template void launch_interpolate<T>(const Geom &, const Geom &, const T *, T *, bool, cudaStream_t);              \
     template void launch_zero_dirichlet<T>(const Geom &, T *, const uint8_t *, cudaStream_t);                         \
     template void launch_masked_zero<T>(const Geom &, T *, int, cudaStream_t);                                        \
     template void launch_fill<T>(T *, T, int64_t, cudaStream_t);                                                      \
     template void launch_ke_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t);           \
-    template void launch_stencil_level1<T>(const Geom &, const Geom &, const T *, const T *, T *, bool, cudaStream_t, \
-                                           int, int);                                                                \
     template void launch_ke_coarsen<T>(const Geom &, const Geom &, const T *, const T *, T *, cudaStream_t, int, int); \
     template void launch_ke_level2<T>(const Geom &, const Geom &, const Geom &, const T *, const T *, T *,            \
                                       cudaStream_t, int, int);                                                        \
-    template void launch_stencil_from_ke<T>(const Geom &, const T *, T *, bool, cudaStream_t, int, int);              \
     template void launch_ke_scaled<T>(const Geom &, const T *, const T *, T *, cudaStream_t);
 VFEM_INST_COARSE(double)
 VFEM_INST_COARSE(float)

@@ -298,6 +298,12 @@ int vfem_debug_pivot_reciprocals(const double *d, int64_t n, double *recip_out, 
         finishOut(vs, st);
     });
 }
+int vfem_mg_set_stencil_bf16(vfem_mg *mg, int on) {
+    return guarded([&] {
+        need(mg, "mg");
+        mg->m.setBf16Stencils(on != 0);
+    });
+}
 int vfem_mg_set_sweep_form(vfem_mg *mg, int form) {
     return guarded([&] {
         need(mg, "mg");

@@ -455,6 +455,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     setupCoarsestIndex();
     if (const char *env = std::getenv("VFEM_OVERLAP_STIFFNESS")) overlapStiffness = env[0] != '0';
     if (const char *env = std::getenv("VFEM_BAND_UPDATE")) bandUpdates = env[0] != '0';
+    if (const char *env = std::getenv("VFEM_STENCIL_BF16")) bf16Stencils = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
@@ -563,6 +564,15 @@ void MG::setupCoarsestIndex() {
     // pageable-memory copies return once staged, so red / fr may go out of scope
     launch_set_pair(nfreeDev.p, nf, 0, st);
     stiffnessValid = false;
+}
+
+void MG::setBf16Stencils(bool on) {
+    if (on != bf16Stencils) {
+        bf16Stencils = on;
+        stiffnessValid = false;
+        levelsValid = false;
+        clearGraphs();
+    }
 }
 
 void MG::setSweepForm(int form) {
@@ -708,7 +718,9 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
         for (int l = 1; l < L() && (!band || bandLo < bandHi); ++l) {
             auto &D = lv[l].data<T>();
             lv[l].rows = lv[l].g.NN <= rowsMaxNodes;
-            D.S.alloc((size_t)(lv[l].rows ? 256 : STENCIL_PLANES) * lv[l].g.NN);
+            const bool half = std::is_same<T, float>::value && halfStencil(l);
+            if (half) D.Sh.alloc((size_t)STENCIL_PLANES * lv[l].g.NN);
+            else D.S.alloc((size_t)(lv[l].rows ? 256 : STENCIL_PLANES) * lv[l].g.NN);
             // level-l element rows whose matrices change, and the node rows whose stencils do
             const int eLo = band ? (bandLo >> l) : 0;
             const int eHi = band ? ((bandHi - 1) >> l) + 1 : lv[l].g.ne[1];
@@ -716,7 +728,12 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
             if (l == 1) {
                 // the level-1 stencil comes straight from the fine moduli; no level-1 element
                 // matrices are stored
-                launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs, nLo, nHi);
+                if (half)
+                    launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Sh.p, lv[1].rows, gs, nLo,
+                                             nHi);
+                else
+                    launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs, nLo,
+                                             nHi);
                 mark("galerkin:L1 stencil");
             } else {
                 D.Ke.alloc((size_t)lv[l].g.NE * 576);
@@ -726,7 +743,8 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
                     launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p,
                                          gs, eLo, eHi);
                 mark("galerkin:L" + std::to_string(l) + " element matrices");
-                launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, gs, nLo, nHi);
+                if (half) launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.Sh.p, lv[l].rows, gs, nLo, nHi);
+                else launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, gs, nLo, nHi);
                 mark("galerkin:L" + std::to_string(l) + " stencil");
             }
         }
@@ -834,14 +852,19 @@ void MG::smoothT(int l, bool forward) {
         // small plane-layout levels: colour pairs on whole z-lines, four launches per sweep
         for (int h = 0; h < 4; ++h) {
             const int c = forward ? h : 3 - h;
-            launch_gs_stencil_lines<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1, forward, st);
+            withStencil<T>(l, [&](auto S) {
+                launch_gs_stencil_lines<T>(lv[l].g, S, D.x.p, D.b.p, dm, (c >> 1) & 1, c & 1, forward, st);
+            });
         }
         return;
     }
     for (int c = 0; c < 8; ++c) {
         const int color = forward ? c : 7 - c;
         if (l == 0) launch_gs_fine_color<T>(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, dm, color, forward, Tr<T>::K0(*fine), st);
-        else launch_gs_stencil_color<T>(lv[l].g, D.S.p, D.x.p, D.b.p, dm, color, forward, lv[l].rows, st);
+        else
+            withStencil<T>(l, [&](auto S) {
+                launch_gs_stencil_color<T>(lv[l].g, S, D.x.p, D.b.p, dm, color, forward, lv[l].rows, st);
+            });
     }
 }
 
@@ -850,12 +873,16 @@ void MG::residualT(int l) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (l == 0) launch_residual_fine<T>(lv[0].g, Tr<T>::Yfine(*fine), D.x.p, D.b.p, D.r.p, Tr<T>::K0(*fine), fine->dmask.p, st);
-    else launch_stencil_residual<T>(lv[l].g, D.S.p, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, lv[l].rows, st);
+    else
+        withStencil<T>(l, [&](auto S) {
+            launch_stencil_residual<T>(lv[l].g, S, D.x.p, D.b.p, D.r.p, lv[l].dmask.p, lv[l].rows, st);
+        });
 }
 
 int MG::tailStart() const {
     int t = L() - 1;  // the coarsest level always ends the tail
-    while (t - 1 >= 1 && lv[t - 1].g.NN <= tailMaxNodes) --t;
+    // the tail kernels read FP32 node-contiguous rows: bf16 plane-layout levels stay outside
+    while (t - 1 >= 1 && lv[t - 1].g.NN <= tailMaxNodes && !halfStencil(t - 1)) --t;
     return (t < L() - 1) ? t : L();
 }
 
@@ -1356,7 +1383,10 @@ void MG::applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate) {
     if (l == 0)
         launch_applyk_fine<T>(lv[0].g, Tr<T>::Yfine(*fine), u, out, Tr<T>::K0(*fine), zeroInit, negate, fine->dmask.p, false,
                               nullptr, 0, st);
-    else launch_stencil_apply<T>(lv[l].g, lv[l].data<T>().S.p, u, out, zeroInit, negate, lv[l].rows, st);
+    else
+        withStencil<T>(l, [&](auto S) {
+            launch_stencil_apply<T>(lv[l].g, S, u, out, zeroInit, negate, lv[l].rows, st);
+        });
 }
 
 template <typename T>

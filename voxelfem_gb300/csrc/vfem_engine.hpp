@@ -116,6 +116,7 @@ public:
 template <typename T>
 struct LevelData {
     DevBuf<T> x, b, r, S, Ke;
+    DevBuf<__nv_bfloat16> Sh;  // the stencil in bf16 (FP32 smoothing levels with bf16 stencils)
 };
 
 struct Level {
@@ -185,6 +186,26 @@ public:
     // gives the default); every form gives identical iterates
     int sweepForm = -1;
     void setSweepForm(int form);
+    // Mixed precision: the assembled stencils of the smoothing levels (1 .. L-2, plane layout)
+    // stored in bf16, rounded once when built (the operator stays symmetric), read and applied
+    // in FP32; the coarsest level stays FP32 for its dense inverse. VFEM_STENCIL_BF16 sets it.
+    bool bf16Stencils = false;
+    void setBf16Stencils(bool on);
+    bool halfStencil(int l) const {
+        return precision == PREC_MIXED && bf16Stencils && l >= 1 && l < L() - 1 && !lv[l].rows;
+    }
+    // fn(S) with the level's stencil pointer in its stored type
+    template <typename T, typename F>
+    void withStencil(int l, F &&fn) {
+        auto &D = lv[l].data<T>();
+        if constexpr (std::is_same<T, float>::value) {
+            if (halfStencil(l)) {
+                fn((const __nv_bfloat16 *)D.Sh.p);
+                return;
+            }
+        }
+        fn((const T *)D.S.p);
+    }
     int stiffnessMaskE = -1;              // fine masked element row the operators were built for
     // the level operators (levels >= 1) are current for stiffnessMaskE; stiffnessValid also
     // covers the coarsest dense inverse, which a change of the free coarsest DOFs invalidates

@@ -1,6 +1,8 @@
 // Launchers for the VoxelFEM GB300 kernels (sm_103a). All nodal vectors are SoA with
 // component stride Geom::ld; element fields are flat row-major (x slowest, z fastest).
 #pragma once
+#include <cuda_bf16.h>
+
 #include <functional>
 #include <string>
 
@@ -128,19 +130,21 @@ void launch_build_gravity_load(const Geom &g, const double *rho, double *f, cons
 // ---------------- coarse levels (k_coarse.cu) ----------------
 // Stencil kernels take the level's layout: rows (node-contiguous, 256 entries per node, one
 // warp per node) or planes (243 planes of NN, one thread per node).
-template <typename T>
-void launch_stencil_apply(const Geom &g, const T *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
+// Stencil kernels: T the arithmetic type, TS the stored entries' type (T, or bf16 for the
+// plane-layout FP32 levels of the mixed preconditioner).
+template <typename T, typename TS>
+void launch_stencil_apply(const Geom &g, const TS *S, const T *u, T *out, bool zeroInit, bool negate, bool rows,
                           cudaStream_t st);
-template <typename T>
-void launch_stencil_residual(const Geom &g, const T *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
+template <typename T, typename TS>
+void launch_stencil_residual(const Geom &g, const TS *S, const T *u, const T *b, T *r, const uint8_t *dmask, bool rows,
                              cudaStream_t st);
-template <typename T>
-void launch_gs_stencil_color(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int color, bool forward,
-                             bool rows, cudaStream_t st);
+template <typename T, typename TS>
+void launch_gs_stencil_color(const Geom &g, const TS *S, T *u, const T *b, const uint8_t *dmask, int color,
+                             bool forward, bool rows, cudaStream_t st);
 // Colours (cx, cy, 0) and (cx, cy, 1) of a plane-layout level in one launch (whole z-lines per
 // block); identical iterates to the two colour launches.
-template <typename T>
-void launch_gs_stencil_lines(const Geom &g, const T *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
+template <typename T, typename TS>
+void launch_gs_stencil_lines(const Geom &g, const TS *S, T *u, const T *b, const uint8_t *dmask, int cx, int cy,
                              bool forward, cudaStream_t st);
 template <typename T>
 void launch_restrict(const Geom &gf, const Geom &gc, const T *fine, T *coarse, cudaStream_t st);
@@ -156,10 +160,10 @@ void launch_fill(T *p, T v, int64_t n, cudaStream_t st);
 template <typename T>
 void launch_ke_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc /*8*576*/, T *Ke1, cudaStream_t st);
 // Level-1 stencil assembled directly from the fine Young's moduli (no element matrices).
-template <typename T>
 // rowLo, rowHi: only the (level-1 node / level-l element / level-l node) rows in [rowLo, rowHi)
 // are rebuilt (band-partial update); the defaults rebuild everything
-void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, T *S, bool rows, cudaStream_t st,
+template <typename T, typename TS>
+void launch_stencil_level1(const Geom &g1, const Geom &g0, const T *Y0, const T *Kc, TS *S, bool rows, cudaStream_t st,
                            int rowLo = 0, int rowHi = 2147483647);
 // Level-2 element matrices from the fine moduli and the 64 folded constant matrices K2.
 template <typename T>
@@ -170,8 +174,8 @@ void launch_ke_coarsen(const Geom &gc, const Geom &gf, const T *Kef, const T *ph
                        int rowLo = 0, int rowHi = 2147483647);
 template <typename T>
 void launch_ke_scaled(const Geom &g, const T *Y, const T *K0, T *Ke, cudaStream_t st);
-template <typename T>
-void launch_stencil_from_ke(const Geom &g, const T *Ke, T *S, bool rows, cudaStream_t st, int rowLo = 0,
+template <typename T, typename TS>
+void launch_stencil_from_ke(const Geom &g, const T *Ke, TS *S, bool rows, cudaStream_t st, int rowLo = 0,
                             int rowHi = 2147483647);
 template <typename Tdst, typename Tsrc>
 void launch_cast(const Tsrc *src, Tdst *dst, int64_t n, cudaStream_t st);

@@ -1,10 +1,24 @@
 // Device building blocks of the assembled 27-point block-stencil levels, shared by the
 // per-colour kernels (k_coarse.cu) and the coarse-tail kernels (k_tail.cu).
 #pragma once
+#include <cuda_bf16.h>
+
 #include "vfem_common.cuh"
 
 namespace vfem {
 namespace stencil {
+
+// Stored stencil entries: the arithmetic type T itself, or bf16 for the FP32 levels of the mixed
+// preconditioner (half the bytes a colour pass streams; the entries are rounded once, when the
+// Galerkin operator is built, so the stored operator stays exactly symmetric).
+template <typename T, typename TS>
+__device__ __forceinline__ T sval(TS v) { return (T)v; }
+template <>
+__device__ __forceinline__ float sval<float, __nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <typename TS, typename T>
+__device__ __forceinline__ TS sstore(T v) { return (TS)v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 sstore<__nv_bfloat16, float>(float v) { return __float2bfloat16_rn(v); }
 
 // Node and element counts stay below 2^31 (checked when a grid is created), so index
 // decodes use 32-bit unsigned division; a 64-bit division is a long software sequence.
@@ -228,8 +242,8 @@ constexpr int SPLIT_SUB = 8;
 constexpr int SPLIT_ROWS = SPLIT_SUB - 1;
 constexpr int SPLIT_NODES = 32;
 
-template <typename T>
-__device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restrict__ S, const T *__restrict__ u,
+template <typename T, typename TS = T>
+__device__ __forceinline__ void stencil_row_part(const Geom &g, const TS *__restrict__ S, const T *__restrict__ u,
                                                  int64_t n, int64_t p, int i, int j, int k, int sub, T &f0, T &f1,
                                                  T &f2) {  // sub in [0, SPLIT_ROWS)
     const int64_t ld = g.ld;
@@ -247,16 +261,16 @@ __device__ __forceinline__ void stencil_row_part(const Geom &g, const T *__restr
 #pragma unroll
             for (int c = 0; c < 3; ++c) uu[t][c] = u[c * ld + m];
             if (o >= 13) {
-                const T *blk = S + (int64_t)((o - 13) * 9) * ld + p;
+                const TS *blk = S + (int64_t)((o - 13) * 9) * ld + p;
 #pragma unroll
-                for (int e = 0; e < 9; ++e) ss[t][e] = blk[e * ld];
+                for (int e = 0; e < 9; ++e) ss[t][e] = sval<T>(blk[e * ld]);
             } else if (in) {
                 // transpose of the neighbour's block towards this node (offset 26 - o)
-                const T *blk = S + (int64_t)((13 - o) * 9) * ld + colour_pos(g, i + ox, j + oy, k + oz);
+                const TS *blk = S + (int64_t)((13 - o) * 9) * ld + colour_pos(g, i + ox, j + oy, k + oz);
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) ss[t][3 * r + c] = blk[(3 * c + r) * ld];
+                    for (int c = 0; c < 3; ++c) ss[t][3 * r + c] = sval<T>(blk[(3 * c + r) * ld]);
             } else {
 #pragma unroll
                 for (int e = 0; e < 9; ++e) ss[t][e] = T(0);

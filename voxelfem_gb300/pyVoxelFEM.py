@@ -671,6 +671,11 @@ class MultigridSolver:
         'staged', 'colours' or 'planes'; every form gives identical iterates."""
         check(_lib().vfem_mg_set_sweep_form(self._h, self.SWEEP_FORMS[form]))
 
+    def setStencilStorage(self, kind="fp32"):
+        """Mixed precision: 'bf16' stores the smoothing levels' assembled stencils in bf16 (half
+        the bytes a colour pass streams), 'fp32' (default) in FP32; both are applied in FP32."""
+        check(_lib().vfem_mg_set_stencil_bf16(self._h, {"fp32": 0, "bf16": 1}[kind]))
+
     def stiffnessRebuilds(self):
         """(full, band): hierarchy rebuilds run in full and as band-partial updates after a
         fabrication-mask change (diagnostic)."""
