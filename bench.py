@@ -538,6 +538,7 @@ def run_ours(args):
         line["q2"] = run_q2(hbm)
     if rank == 0 and ws == 1 and not args.no_mma:
         line["mma"] = run_mma(args.no_cpu)
+        line["filters"] = run_filters()
     if rank == 0 and ws == 1 and not args.no_2d:
         line["2d"] = run_2d(hbm, args.no_cpu)
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -705,6 +706,43 @@ Q2_NE = (128, 128, 128)
 
 
 MMA_N = 192 * 96 * 96  # the 192x96x96 MBB design's element count
+
+
+def run_filters():
+    """The density filter at the MBB size (192x96x96 elements, radius 2, linear weights) on device
+    arrays: the allocating entry point and the allocation-free one (which rebuilds its tap table
+    every call), CUDA events over 20 calls each."""
+    import ctypes as C
+
+    import torch
+
+    from voxelfem_gb300 import _capi
+    lib = _capi.load()
+    dims = (192, 96, 96)
+    dims_c = (C.c_int64 * 3)(*dims)
+    n = dims[0] * dims[1] * dims[2]
+    x = torch.rand(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+    out = {"workload": "smoothing filter 192x96x96, radius 2, linear (93 taps)", "bytes": 2 * 8 * n}
+
+    def time_calls(fn, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out["allocating_ms"] = time_calls(lambda: _capi.check(lib.vfem_smoothing_filter(
+        dims_c, 2, 1, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))))
+    out["noalloc_ms"] = time_calls(lambda: _capi.check(lib.vfem_smoothing_filter_noalloc(
+        dims_c, 2, 1, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(stream.cuda_stream))))
+    return out
 
 
 def run_mma(no_cpu):
