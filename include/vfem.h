@@ -324,14 +324,43 @@ int vfem_q2_time_apply_k(vfem_q2 *g, int precision, int reps, double *ms, double
  * resident data, with its algorithmic bytes s (9 nn + ne). */
 int vfem_q2_time_smooth(vfem_q2 *g, int precision, int reps, double *ms, double *bytes);
 /* preconditionedConjugateGradient on a triquadratic grid (MultigridSolver.hh:1047-1152 recurrences,
- * FP64 outer iteration). The preconditioner is this library's p-multigrid cycle: Q2 block
- * Gauss-Seidel sweeps (mg_smoothing_iterations before and after) around one FP32 V-cycle of the
- * trilinear problem on the same mesh with `coarsenings` coarsenings. x in/out. The CG matvec is
- * double-float unless vfem_q2_set_outer_matvec chose FP64. */
-/* outer matvec of vfem_q2_pcg: VFEM_MATVEC_FP64 or VFEM_MATVEC_DF (default); no reference counterpart */
+ * FP64 outer iteration, one V-cycle from zero per iteration with mg_smoothing_iterations sweeps
+ * before and after). x in/out. The preconditioner's hierarchy (vfem_q2_set_hierarchy):
+ *   VFEM_Q2_HIERARCHY_Q2 (default): the reference's MultigridSolver<double, 2, 2, 2>, replacing
+ *     MultigridSolver(fineSimulator, numCoarseningLevels) of a degree-2 simulator
+ *     (MultigridSolver.hh:35-121): `coarsenings` halvings of the Q2 mesh; level 1 applies the fine
+ *     moduli to the 8 coarsened full-density element matrices, the levels below hold Galerkin
+ *     element matrices, the coarsest is solved directly (FP64 dense inverse in place of CHOLMOD);
+ *   VFEM_Q2_HIERARCHY_P: Q2 block Gauss-Seidel around one FP32 V-cycle of the trilinear problem on
+ *     the same mesh with `coarsenings` coarsenings (a p-multigrid step; mixed precision only).
+ * vfem_q2_set_precision: VFEM_PREC_FP64 (the reference's method: FP64 V-cycle and CG matvec) or
+ * VFEM_PREC_MIXED (default: FP32 V-cycle, double-float CG matvec). */
+#define VFEM_Q2_HIERARCHY_Q2 0
+#define VFEM_Q2_HIERARCHY_P 1
+int vfem_q2_set_hierarchy(vfem_q2 *g, int hierarchy);
+int vfem_q2_set_precision(vfem_q2 *g, int precision);
+/* outer matvec of vfem_q2_pcg: VFEM_MATVEC_FP64 or VFEM_MATVEC_DF; no reference counterpart */
 int vfem_q2_set_outer_matvec(vfem_q2 *g, int outer_matvec);
 int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *b, int64_t max_iter, double tol,
                 int64_t mg_smoothing_iterations, vfem_pcg_stats *stats);
+/* Levels of the Q2 hierarchy with `coarsenings` coarsenings (level 0 = this grid), built on
+ * demand in `precision`; vectors (numNodes(level), 3) column-major, host or device.
+ * num_nodes: MultigridSolver::getSimulator(l).numNodes(); dirichlet: the coarsened support bits
+ * (MultigridSolver.hh:57-104); ke: the level's element matrices (levels 1..coarsenings,
+ * numElements x 81 x 81, row-major; m_getCoarsenedStiffnessMatrix, MultigridSolver.hh:745-819);
+ * smooth: smoothingMulticoloredGS(l, u, b, forward) (MultigridSolver.hh:452-458); residual:
+ * computeResidual(l, u, b, r) (MultigridSolver.hh:527-541); coarse_solve: the coarsest
+ * direct solve; vcycle: applyPreconditionerInv(b) with one V-cycle (MultigridSolver.hh:576-580). */
+int vfem_q2_mg_num_nodes(vfem_q2 *g, int64_t coarsenings, int level, int64_t *num_nodes);
+int vfem_q2_mg_level_dirichlet(vfem_q2 *g, int64_t coarsenings, int level, uint8_t *mask_out);
+int vfem_q2_mg_level_ke(vfem_q2 *g, int64_t coarsenings, int level, int precision, double *out);
+int vfem_q2_mg_smooth(vfem_q2 *g, int64_t coarsenings, int level, double *u_inout, const double *b, int forward,
+                      int precision);
+int vfem_q2_mg_residual(vfem_q2 *g, int64_t coarsenings, int level, const double *u, const double *b, double *r,
+                        int precision);
+int vfem_q2_mg_coarse_solve(vfem_q2 *g, int64_t coarsenings, const double *b, double *x, int precision);
+int vfem_q2_mg_vcycle(vfem_q2 *g, int64_t coarsenings, const double *b, double *x, int64_t mg_smoothing_iterations,
+                      int precision);
 
 /* ---------------- Method of Moving Asymptotes (MethodOfMovingAsymptotes.hh; pyOptimizer.MMA,
  * python_bindings/Optimizer.cc:16-22) ----------------

@@ -84,6 +84,17 @@ def lib():
             "ovf_q2_smooth": (None, [_l, _d, _d, _u8, _d, _d, C.c_int]),
             "ovf_q2_interp": (None, [_l, _d, _d, C.c_int]),
             "ovf_q2_restrict": (None, [_l, _d, _d]),
+            "ovf_q2mg_create": (C.c_void_p, [_l, _d, _d, _u8, C.c_int]),
+            "ovf_q2mg_destroy": (None, [C.c_void_p]),
+            "ovf_q2mg_level_dims": (None, [C.c_void_p, C.c_int, _l]),
+            "ovf_q2mg_level_dirichlet": (None, [C.c_void_p, C.c_int, _u8]),
+            "ovf_q2mg_level_ke": (None, [C.c_void_p, C.c_int, _d]),
+            "ovf_q2mg_coarsened_k0": (None, [C.c_void_p, _d]),
+            "ovf_q2mg_smooth": (C.c_int, [C.c_void_p, C.c_int, _d, _d, C.c_int]),
+            "ovf_q2mg_residual": (C.c_int, [C.c_void_p, C.c_int, _d, _d, _d]),
+            "ovf_q2mg_coarse_solve": (C.c_int, [C.c_void_p, _d, _d]),
+            "ovf_q2mg_vcycle": (C.c_int, [C.c_void_p, _d, _d, C.c_long]),
+            "ovf_q2mg_pcg": (C.c_int, [C.c_void_p, _d, _d, C.c_long, C.c_double, C.c_long, _l, _d]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -461,6 +472,84 @@ def q2_restrict(ne_fine, fine):
     out = np.zeros((nc, 3), order="F")
     lib().ovf_q2_restrict(_ne(ne_fine), _dp(f), _dp(out))
     return out
+
+
+class Q2Multigrid:
+    """The reference's triquadratic hierarchy (MultigridSolver<double, 2, 2, 2>): halved Q2 meshes,
+    level-1 operator from the 8 coarsened full-density element matrices, Galerkin element
+    matrices below, dense Cholesky on the coarsest free DOFs."""
+
+    def __init__(self, ne, K0, Y, dmask_bits, coarsenings):
+        self.ne = [int(v) for v in ne]
+        self.coarsenings = int(coarsenings)
+        m = np.ascontiguousarray(dmask_bits, dtype=np.uint8)
+        self.h = lib().ovf_q2mg_create(_ne(ne), _dp(np.ascontiguousarray(K0, dtype=np.float64)),
+                                       _dp(np.ascontiguousarray(Y, dtype=np.float64)), m.ctypes.data_as(_u8),
+                                       int(coarsenings))
+        if not self.h:
+            raise RuntimeError(lib().ovf_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ovf_q2mg_destroy(self.h)
+            self.h = None
+
+    def level_ne(self, l):
+        out = (C.c_long * 3)()
+        lib().ovf_q2mg_level_dims(self.h, int(l), out)
+        return [int(v) for v in out]
+
+    def num_nodes(self, l):
+        return q2_num_nodes(self.level_ne(l))
+
+    def dirichlet_bits(self, l):
+        out = np.empty(self.num_nodes(l), dtype=np.uint8)
+        lib().ovf_q2mg_level_dirichlet(self.h, int(l), out.ctypes.data_as(_u8))
+        return out
+
+    def element_matrices(self, l):
+        ne = self.level_ne(l)
+        out = np.empty(int(np.prod(ne)) * 6561)
+        lib().ovf_q2mg_level_ke(self.h, int(l), _dp(out))
+        return out.reshape(-1, 81, 81)
+
+    def coarsened_k0(self):
+        out = np.empty(8 * 6561)
+        lib().ovf_q2mg_coarsened_k0(self.h, _dp(out))
+        return out.reshape(8, 81, 81)
+
+    def smooth(self, l, u, b, forward=True):
+        nn = self.num_nodes(l)
+        x = vfield(u, nn).copy(order="F")
+        _check(lib().ovf_q2mg_smooth(self.h, int(l), _dp(x), _dp(vfield(b, nn)), int(bool(forward))))
+        return x
+
+    def residual(self, l, u, b):
+        nn = self.num_nodes(l)
+        out = np.zeros((nn, 3), order="F")
+        _check(lib().ovf_q2mg_residual(self.h, int(l), _dp(vfield(u, nn)), _dp(vfield(b, nn)), _dp(out)))
+        return out
+
+    def coarse_solve(self, b):
+        nn = self.num_nodes(self.coarsenings)
+        out = np.zeros((nn, 3), order="F")
+        _check(lib().ovf_q2mg_coarse_solve(self.h, _dp(vfield(b, nn)), _dp(out)))
+        return out
+
+    def vcycle(self, b, sweeps):
+        nn = self.num_nodes(0)
+        out = np.zeros((nn, 3), order="F")
+        _check(lib().ovf_q2mg_vcycle(self.h, _dp(vfield(b, nn)), _dp(out), int(sweeps)))
+        return out
+
+    def pcg(self, b, maxIter=500, tol=1e-8, sweeps=2, x0=None):
+        nn = self.num_nodes(0)
+        x = np.zeros((nn, 3), order="F") if x0 is None else vfield(x0, nn).copy(order="F")
+        it = C.c_long(0)
+        rr = C.c_double(0.0)
+        _check(lib().ovf_q2mg_pcg(self.h, _dp(x), _dp(vfield(b, nn)), int(maxIter), float(tol), int(sweeps),
+                                  C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
 
 
 

@@ -1548,6 +1548,335 @@ void q2Restrict(const long neF[3], const double *fine, double *coarse) {
             }
 }
 
+// ---------------------------------------------------------------------------
+// Triquadratic multigrid hierarchy (MultigridSolver<double, 2, 2, 2>): every level is a Q2 mesh
+// with half the elements of the one above (MultigridSolver.hh:35-121). Level 1 applies the
+// fine moduli to the 8 coarsened full-density element matrices (:294-321, :471-500, :724-738);
+// levels 2 and below hold Galerkin element matrices I_f^T K_f I_f summed over the 8 children
+// (:745-819), which the reference assembles into blockK (here they stay per element: the same
+// operator); the coarsest level is solved directly on its free DOFs (TensorProductSimulator.hh:
+// 1181-1230, dense Cholesky in place of CHOLMOD).
+// ---------------------------------------------------------------------------
+
+// phis[f](fine_n, coarse_n) (MultigridSolver.hh:664-687): coarse shape function coarse_n at
+// fine node fine_n of child f = 4 fx + 2 fy + fz, whose local node (a, b, c) lies at coarse
+// reference coordinates ((2 fx + a) / 4, (2 fy + b) / 4, (2 fz + c) / 4).
+double q2Phi(int f, int fn, int cn) {
+    const int fd[3] = {f >> 2 & 1, f >> 1 & 1, f & 1};
+    const int fa[3] = {fn / 9, (fn / 3) % 3, fn % 3}, ca[3] = {cn / 9, (cn / 3) % 3, cn % 3};
+    double v = 1.0;
+    for (int d = 0; d < 3; ++d) v *= lag2(ca[d], (2.0 * fd[d] + fa[d]) / 4.0);
+    return v;
+}
+
+// Kc += I_f^T Kf I_f with I_f[3i + c, 3j + d] = phi_f(i, j) delta_cd (MultigridSolver.hh:712-722)
+void q2AccumulateCoarsened(int f, const double *Kf, double *Kc) {
+    double phi[27 * 27];
+    for (int i = 0; i < 27; ++i)
+        for (int j = 0; j < 27; ++j) phi[i * 27 + j] = q2Phi(f, i, j);
+    std::vector<double> T(6561);
+    for (int r = 0; r < 81; ++r)
+        for (int j = 0; j < 27; ++j)
+            for (int d = 0; d < 3; ++d) {
+                double acc = 0.0;
+                for (int i = 0; i < 27; ++i) acc += Kf[r * 81 + 3 * i + d] * phi[i * 27 + j];
+                T[r * 81 + 3 * j + d] = acc;
+            }
+    for (int j = 0; j < 27; ++j)
+        for (int c = 0; c < 3; ++c)
+            for (int q = 0; q < 81; ++q) {
+                double acc = 0.0;
+                for (int i = 0; i < 27; ++i) acc += phi[i * 27 + j] * T[(3 * i + c) * 81 + q];
+                Kc[(3 * j + c) * 81 + q] += acc;
+            }
+}
+
+struct Q2MG {
+    std::vector<Q2Grid> g;                   // levels 0..L
+    std::vector<std::vector<uint8_t>> dm;    // Dirichlet component bits per level
+    std::vector<double> K0, Y;               // fine element matrix, fine moduli
+    std::vector<double> Kc;                  // 8 x 6561 coarsened full-density matrices
+    std::vector<std::vector<double>> Ke;     // level l >= 1: NE_l x 6561
+    std::vector<std::vector<double>> x, b, r;
+    DenseChol chol;
+    bool symmetricGS = true;
+    int L() const { return (int)g.size() - 1; }
+};
+
+// Dirichlet coarsening (MultigridSolver.hh:57-104): a constrained fine node marks every coarse
+// node of the vertex, edge or face of its coarse element on which it lies (all nodes along an
+// axis where it is interior), with the fine node's components.
+void q2CoarsenDirichlet(const Q2Grid &F, const std::vector<uint8_t> &dmF, const Q2Grid &C, std::vector<uint8_t> &dmC) {
+    dmC.assign(C.NN, 0);
+    for (long I = 0; I < F.nn[0]; ++I)
+        for (long J = 0; J < F.nn[1]; ++J)
+            for (long K = 0; K < F.nn[2]; ++K) {
+                const uint8_t m = dmF[F.node(I, J, K)];
+                if (!m) continue;
+                const long P[3] = {I, J, K};
+                long ec[3], pb[3];
+                for (int d = 0; d < 3; ++d) {
+                    ec[d] = std::min(P[d] / 4, C.ne[d] - 1);
+                    const long t = P[d] - 4 * ec[d];
+                    pb[d] = t == 0 ? 0 : (t == 4 ? 2 : -1);
+                }
+                for (int ln = 0; ln < 27; ++ln) {
+                    const long la[3] = {ln / 9, (ln / 3) % 3, ln % 3};
+                    bool on = true;
+                    for (int d = 0; d < 3; ++d)
+                        if (pb[d] != -1 && pb[d] != la[d]) on = false;
+                    if (on) dmC[C.node(2 * ec[0] + la[0], 2 * ec[1] + la[1], 2 * ec[2] + la[2])] |= m;
+                }
+            }
+}
+
+long q2Child(const Q2Grid &F, long ci, long cj, long ck, int f) {
+    return (long)F.elem(2 * ci + (f >> 2 & 1), 2 * cj + (f >> 1 & 1), 2 * ck + (f & 1));
+}
+
+// Element matrices of every level below the fine one (MultigridSolver.hh:745-819, 846-905)
+void q2BuildLevels(Q2MG &m) {
+    m.Kc.assign(8 * 6561, 0.0);
+    for (int f = 0; f < 8; ++f) q2AccumulateCoarsened(f, m.K0.data(), m.Kc.data() + (size_t)f * 6561);
+    m.Ke.assign(m.g.size(), {});
+    for (int l = 1; l <= m.L(); ++l) {
+        const Q2Grid &C = m.g[l], &F = m.g[l - 1];
+        std::vector<double> &K = m.Ke[l];
+        K.assign(C.NE * 6561, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long e = 0; e < (long)C.NE; ++e) {
+            const long ci = e / (C.ne[1] * C.ne[2]), cj = (e / C.ne[2]) % C.ne[1], ck = e % C.ne[2];
+            double *out = K.data() + (size_t)e * 6561;
+            for (int f = 0; f < 8; ++f) {
+                const long ef = q2Child(F, ci, cj, ck, f);
+                if (l == 1) {
+                    const double E = m.Y[ef];
+                    const double *Kc = m.Kc.data() + (size_t)f * 6561;
+                    for (int q = 0; q < 6561; ++q) out[q] = (f == 0) ? E * Kc[q] : out[q] + E * Kc[q];
+                } else {
+                    q2AccumulateCoarsened(f, m.Ke[l - 1].data() + (size_t)ef * 6561, out);
+                }
+            }
+        }
+    }
+    // coarsest: reduced dense system on the free DOFs (node-major 3 n + c)
+    const Q2Grid &C = m.g[m.L()];
+    std::vector<long> red(3 * C.NN, -1);
+    m.chol.freeIdx.clear();
+    for (size_t n = 0; n < C.NN; ++n)
+        for (int c = 0; c < 3; ++c)
+            if (!(m.dm[m.L()][n] >> c & 1)) { red[3 * n + c] = (long)m.chol.freeIdx.size(); m.chol.freeIdx.push_back((long)(3 * n + c)); }
+    const long nf = (long)m.chol.freeIdx.size();
+    std::vector<double> A((size_t)nf * nf, 0.0);
+    for (long e = 0; e < (long)C.NE; ++e) {
+        const long ci = e / (C.ne[1] * C.ne[2]), cj = (e / C.ne[2]) % C.ne[1], ck = e % C.ne[2];
+        const double *K = m.Ke[m.L()].data() + (size_t)e * 6561;
+        for (int a = 0; a < 27; ++a) {
+            const size_t na = C.node(2 * ci + a / 9, 2 * cj + (a / 3) % 3, 2 * ck + a % 3);
+            for (int bb = 0; bb < 27; ++bb) {
+                const size_t nb = C.node(2 * ci + bb / 9, 2 * cj + (bb / 3) % 3, 2 * ck + bb % 3);
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) {
+                        const long ra = red[3 * na + r], cb = red[3 * nb + c];
+                        if (ra < 0 || cb < 0) continue;
+                        A[(size_t)ra * nf + cb] += K[(3 * a + r) * 81 + 3 * bb + c];
+                    }
+            }
+        }
+    }
+    m.chol.factor(A, nf);
+}
+
+Q2MG *q2mgCreate(const long ne[3], const double *K0, const double *Y, const uint8_t *dmask, int coarsenings) {
+    if (coarsenings < 1) throw std::runtime_error("the triquadratic hierarchy needs at least one coarsening");
+    auto m = std::make_unique<Q2MG>();
+    long n[3] = {ne[0], ne[1], ne[2]};
+    for (int l = 0; l <= coarsenings; ++l) {
+        if (l > 0)
+            for (int d = 0; d < 3; ++d) {
+                if (n[d] % 2) throw std::runtime_error("Grid size currently must be divisible by 2^numCoarseningLevels");
+                n[d] /= 2;
+            }
+        m->g.push_back(q2grid(n));
+    }
+    m->K0.assign(K0, K0 + 6561);
+    m->Y.assign(Y, Y + m->g[0].NE);
+    m->dm.resize(m->g.size());
+    m->dm[0].assign(dmask, dmask + m->g[0].NN);
+    for (int l = 1; l <= coarsenings; ++l) q2CoarsenDirichlet(m->g[l - 1], m->dm[l - 1], m->g[l], m->dm[l]);
+    q2BuildLevels(*m);
+    for (const Q2Grid &g : m->g) {
+        m->x.emplace_back(3 * g.NN, 0.0);
+        m->b.emplace_back(3 * g.NN, 0.0);
+        m->r.emplace_back(3 * g.NN, 0.0);
+    }
+    return m.release();
+}
+
+// out = K_l u with the level's element matrices (element loop, cached-Ke applyK)
+void q2ElemApply(const Q2Grid &g, const double *Ke, const double *u, double *out) {
+    std::fill(out, out + 3 * g.NN, 0.0);
+    for (int parity = 0; parity < 2; ++parity)
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long i = parity; i < g.ne[0]; i += 2)
+            for (long j = 0; j < g.ne[1]; ++j)
+                for (long k = 0; k < g.ne[2]; ++k) {
+                    size_t nodes[27];
+                    double ue[81];
+                    for (int l = 0; l < 27; ++l) {
+                        nodes[l] = g.node(2 * i + l / 9, 2 * j + (l / 3) % 3, 2 * k + l % 3);
+                        for (int c = 0; c < 3; ++c) ue[3 * l + c] = u[c * g.NN + nodes[l]];
+                    }
+                    const double *K = Ke + (size_t)g.elem(i, j, k) * 6561;
+                    for (int rr = 0; rr < 81; ++rr) {
+                        double acc = 0.0;
+                        for (int t = 0; t < 81; ++t) acc += K[rr * 81 + t] * ue[t];
+                        out[(rr % 3) * g.NN + nodes[rr / 3]] += acc;
+                    }
+                }
+}
+
+// 27-colour block Gauss-Seidel with the level's element matrices (NodeSmoothStencilSecondFinest
+// and NodeSmoothStencilBlockK, MultigridSolver.hh:294-334, 409-442)
+void q2ElemSmooth(const Q2Grid &g, const double *Ke, const uint8_t *dmask, double *u, const double *b, bool forward) {
+    for (int ci = 0; ci < 27; ++ci) {
+        const int col = forward ? ci : 26 - ci;
+        const long lo[3] = {col / 9, (col / 3) % 3, col % 3};
+        long inc[3];
+        for (int d = 0; d < 3; ++d) inc[d] = (lo[d] == 1) ? 2 : 4;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long I = lo[0]; I < g.nn[0]; I += inc[0])
+            for (long J = lo[1]; J < g.nn[1]; J += inc[1])
+                for (long Kk = lo[2]; Kk < g.nn[2]; Kk += inc[2]) {
+                    const size_t n = g.node(I, J, Kk);
+                    const uint8_t dmn = dmask[n];
+                    if (dmn == 7) continue;
+                    double bms[3] = {b[n], b[g.NN + n], b[2 * g.NN + n]};
+                    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    const long P[3] = {I, J, Kk};
+                    long el[3][2], ll[3][2];
+                    int cnt[3];
+                    for (int d = 0; d < 3; ++d) {
+                        cnt[d] = 0;
+                        if (P[d] % 2) { el[d][0] = (P[d] - 1) / 2; ll[d][0] = 1; cnt[d] = 1; }
+                        else {
+                            if (P[d] / 2 - 1 >= 0) { el[d][cnt[d]] = P[d] / 2 - 1; ll[d][cnt[d]] = 2; ++cnt[d]; }
+                            if (P[d] / 2 < g.ne[d]) { el[d][cnt[d]] = P[d] / 2; ll[d][cnt[d]] = 0; ++cnt[d]; }
+                        }
+                    }
+                    for (int a = 0; a < cnt[0]; ++a)
+                        for (int bb = 0; bb < cnt[1]; ++bb)
+                            for (int c = 0; c < cnt[2]; ++c) {
+                                const long ei = el[0][a], ej = el[1][bb], ek = el[2][c];
+                                const int ln = 9 * ll[0][a] + 3 * ll[1][bb] + ll[2][c];
+                                const double *K = Ke + (size_t)g.elem(ei, ej, ek) * 6561;
+                                for (int rr = 0; rr < 3; ++rr) {
+                                    double acc = 0.0;
+                                    for (int mm = 0; mm < 27; ++mm) {
+                                        const size_t nm = g.node(2 * ei + mm / 9, 2 * ej + (mm / 3) % 3, 2 * ek + mm % 3);
+                                        for (int cc = 0; cc < 3; ++cc) acc += K[(3 * ln + rr) * 81 + 3 * mm + cc] * u[cc * g.NN + nm];
+                                    }
+                                    bms[rr] -= acc;
+                                    for (int cc = 0; cc < 3; ++cc) M[3 * rr + cc] += K[(3 * ln + rr) * 81 + 3 * ln + cc];
+                                }
+                            }
+                    double un[3] = {u[n], u[g.NN + n], u[2 * g.NN + n]};
+                    smoothNodeSolve(dmn, bms, M, un, forward);
+                    for (int c = 0; c < 3; ++c) u[c * g.NN + n] = un[c];
+                }
+    }
+}
+
+void q2mgZeroDirichlet(const Q2Grid &g, const std::vector<uint8_t> &dm, double *u) {
+    for (size_t n = 0; n < g.NN; ++n)
+        for (int c = 0; c < 3; ++c)
+            if (dm[n] >> c & 1) u[c * g.NN + n] = 0.0;
+}
+
+void q2mgSmooth(Q2MG &m, int l, double *u, const double *b, bool forward) {
+    if (l == 0) q2Smooth(m.g[0], m.K0.data(), m.Y.data(), m.dm[0].data(), u, b, forward);
+    else q2ElemSmooth(m.g[l], m.Ke[l].data(), m.dm[l].data(), u, b, forward);
+}
+
+// computeResidual (MultigridSolver.hh:527-541): r = b - K_l u, zero on constrained components
+void q2mgResidual(Q2MG &m, int l, const double *u, const double *b, double *r) {
+    const Q2Grid &g = m.g[l];
+    std::vector<double> Ku(3 * g.NN);
+    if (l == 0) q2ApplyK(g, m.K0.data(), m.Y.data(), u, Ku.data());
+    else q2ElemApply(g, m.Ke[l].data(), u, Ku.data());
+    for (size_t t = 0; t < 3 * g.NN; ++t) r[t] = b[t] - Ku[t];
+    q2mgZeroDirichlet(g, m.dm[l], r);
+}
+
+void q2mgCoarseSolve(Q2MG &m, const double *bvec, double *xout) {
+    const size_t NN = m.g[m.L()].NN;
+    std::vector<double> rhs(m.chol.n);
+    for (long t = 0; t < m.chol.n; ++t) {
+        const long d = m.chol.freeIdx[t];
+        rhs[t] = bvec[(d % 3) * NN + d / 3];
+    }
+    m.chol.solve(rhs);
+    std::fill(xout, xout + 3 * NN, 0.0);
+    for (long t = 0; t < m.chol.n; ++t) {
+        const long d = m.chol.freeIdx[t];
+        xout[(d % 3) * NN + d / 3] = rhs[t];
+    }
+}
+
+// MultigridSolver.hh:617-658 (residual system: zero Dirichlet values)
+void q2mgVcycle(Q2MG &m, int l, long sweeps) {
+    if (l == m.L()) { q2mgCoarseSolve(m, m.b[l].data(), m.x[l].data()); return; }
+    q2mgZeroDirichlet(m.g[l], m.dm[l], m.x[l].data());
+    for (long t = 0; t < sweeps; ++t) q2mgSmooth(m, l, m.x[l].data(), m.b[l].data(), true);
+    q2mgResidual(m, l, m.x[l].data(), m.b[l].data(), m.r[l].data());
+    const long neF[3] = {m.g[l].ne[0], m.g[l].ne[1], m.g[l].ne[2]};
+    q2Restrict(neF, m.r[l].data(), m.b[l + 1].data());
+    std::fill(m.x[l + 1].begin(), m.x[l + 1].end(), 0.0);
+    q2mgVcycle(m, l + 1, sweeps);
+    q2Interp(neF, m.x[l + 1].data(), m.x[l].data(), true);
+    for (long t = 0; t < sweeps; ++t) q2mgSmooth(m, l, m.x[l].data(), m.b[l].data(), !m.symmetricGS);
+}
+
+double q2Dot(size_t n, const double *a, const double *b) {
+    double acc = 0.0;
+    for (size_t t = 0; t < n; ++t) acc += a[t] * b[t];
+    return acc;
+}
+
+// MultigridSolver.hh:1047-1152 with one V-cycle from zero as the preconditioner
+void q2mgPcg(Q2MG &m, double *x, const double *bvec, long maxIter, double tol, long sweeps, long *itersOut,
+             double *relresOut) {
+    const Q2Grid &g = m.g[0];
+    const size_t n3 = 3 * g.NN;
+    std::vector<double> r(n3), s, d, Ad(n3);
+    q2mgZeroDirichlet(g, m.dm[0], x);
+    const double bnorm2 = q2Dot(n3, bvec, bvec);
+    q2mgResidual(m, 0, x, bvec, r.data());
+    double rsq = q2Dot(n3, r.data(), r.data()), rMr = 0.0;
+    long i = 0;
+    while ((i++ < maxIter) && (rsq > tol * tol * bnorm2)) {
+        std::copy(r.begin(), r.end(), m.b[0].begin());
+        std::fill(m.x[0].begin(), m.x[0].end(), 0.0);
+        q2mgVcycle(m, 0, sweeps);
+        s = m.x[0];
+        q2mgZeroDirichlet(g, m.dm[0], s.data());
+        const double old = rMr;
+        rMr = q2Dot(n3, r.data(), s.data());
+        if (d.empty()) d = s;
+        else
+            for (size_t t = 0; t < n3; ++t) d[t] = rMr / old * d[t] + s[t];
+        q2ApplyK(g, m.K0.data(), m.Y.data(), d.data(), Ad.data());
+        q2mgZeroDirichlet(g, m.dm[0], Ad.data());
+        const double alpha = rMr / q2Dot(n3, d.data(), Ad.data());
+        for (size_t t = 0; t < n3; ++t) x[t] += alpha * d[t];
+        for (size_t t = 0; t < n3; ++t) r[t] -= alpha * Ad[t];
+        rsq = q2Dot(n3, r.data(), r.data());
+        if (std::isnan(rsq)) throw std::logic_error("NaN encountered at iteration" + std::to_string(i));
+    }
+    if (itersOut) *itersOut = std::min(i, maxIter + 1) - 1;
+    if (relresOut) *relresOut = bnorm2 > 0 ? std::sqrt(rsq / bnorm2) : std::sqrt(rsq);
+}
+
 extern "C" {
 
 const char *ovf_last_error() { return g_err.c_str(); }
@@ -1731,4 +2060,49 @@ void ovf_q2_interp(const long neF[3], const double *coarse, double *fine, int ac
     q2Interp(neF, coarse, fine, accumulate != 0);
 }
 void ovf_q2_restrict(const long neF[3], const double *fine, double *coarse) { q2Restrict(neF, fine, coarse); }
+// ---- triquadratic multigrid hierarchy ----
+void *ovf_q2mg_create(const long ne[3], const double *K0, const double *Y, const uint8_t *dmask, int coarsenings) {
+    Q2MG *m = nullptr;
+    guarded([&] { m = q2mgCreate(ne, K0, Y, dmask, coarsenings); });
+    return m;
+}
+void ovf_q2mg_destroy(void *m) { delete (Q2MG *)m; }
+void ovf_q2mg_level_dims(void *mp, int l, long *ne) {
+    const Q2Grid &g = ((Q2MG *)mp)->g.at(l);
+    for (int d = 0; d < 3; ++d) ne[d] = g.ne[d];
+}
+void ovf_q2mg_level_dirichlet(void *mp, int l, uint8_t *out) {
+    const auto &v = ((Q2MG *)mp)->dm.at(l);
+    std::copy(v.begin(), v.end(), out);
+}
+void ovf_q2mg_level_ke(void *mp, int l, double *out) {
+    const auto &v = ((Q2MG *)mp)->Ke.at(l);
+    std::copy(v.begin(), v.end(), out);
+}
+void ovf_q2mg_coarsened_k0(void *mp, double *out) {
+    const auto &v = ((Q2MG *)mp)->Kc;
+    std::copy(v.begin(), v.end(), out);
+}
+int ovf_q2mg_smooth(void *mp, int l, double *u, const double *b, int forward) {
+    return guarded([&] { q2mgSmooth(*(Q2MG *)mp, l, u, b, forward != 0); });
+}
+int ovf_q2mg_residual(void *mp, int l, const double *u, const double *b, double *r) {
+    return guarded([&] { q2mgResidual(*(Q2MG *)mp, l, u, b, r); });
+}
+int ovf_q2mg_coarse_solve(void *mp, const double *b, double *x) {
+    return guarded([&] { q2mgCoarseSolve(*(Q2MG *)mp, b, x); });
+}
+int ovf_q2mg_vcycle(void *mp, const double *b, double *x, long sweeps) {
+    return guarded([&] {
+        Q2MG &m = *(Q2MG *)mp;
+        std::copy(b, b + m.b[0].size(), m.b[0].begin());
+        std::fill(m.x[0].begin(), m.x[0].end(), 0.0);
+        q2mgVcycle(m, 0, sweeps);
+        std::copy(m.x[0].begin(), m.x[0].end(), x);
+    });
+}
+int ovf_q2mg_pcg(void *mp, double *x, const double *b, long maxIter, double tol, long sweeps, long *iters,
+                 double *relres) {
+    return guarded([&] { q2mgPcg(*(Q2MG *)mp, x, b, maxIter, tol, sweeps, iters, relres); });
+}
 }  // extern "C"

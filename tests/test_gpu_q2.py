@@ -76,9 +76,11 @@ def test_q2_factory(gpu):
         g.multigridSolver(0)
 
 
-@pytest.mark.parametrize("coarsenings,matvec", [(1, "df"), (2, "df"), (2, "fp64")])
-def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings, matvec):
-    """The PCG solution equals a dense direct solve of the oracle's Q2 operator on the free DOFs."""
+@pytest.mark.parametrize("coarsenings,matvec,hierarchy", [(1, "df", "q2"), (2, "df", "q2"), (2, "fp64", "q2"),
+                                                          (1, "df", "p"), (2, "df", "p"), (2, "fp64", "p")])
+def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings, matvec, hierarchy):
+    """The PCG solution equals a dense direct solve of the oracle's Q2 operator on the free DOFs,
+    with either preconditioner hierarchy."""
     ne = (8, 4, 4)
     g, Y, bits = make(ne, seed=5)
     K0 = g.fullDensityElementStiffnessMatrix()
@@ -100,6 +102,7 @@ def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings, matvec):
     xs[~fixed] = np.linalg.solve(Kd[np.ix_(~fixed, ~fixed)], bvec[~fixed])
     xref = xs.reshape(3, nn).T
     mg = g.multigridSolver(coarsenings)
+    mg.setHierarchy(hierarchy)
     mg.setOuterMatvec(matvec)
     x = mg.preconditionedConjugateGradient(np.zeros((nn, 3)), f, 200, 1e-11, None, 1, 2, False)
     assert mg.lastStats.relres <= 1e-11

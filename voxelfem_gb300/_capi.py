@@ -74,6 +74,15 @@ _SIGS = {
     "vfem_q2_time_apply_k": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "vfem_q2_time_smooth": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "vfem_q2_set_outer_matvec": (C.c_int, [_vp, C.c_int]),
+    "vfem_q2_set_hierarchy": (C.c_int, [_vp, C.c_int]),
+    "vfem_q2_set_precision": (C.c_int, [_vp, C.c_int]),
+    "vfem_q2_mg_num_nodes": (C.c_int, [_vp, C.c_int64, C.c_int, _vp]),
+    "vfem_q2_mg_level_dirichlet": (C.c_int, [_vp, C.c_int64, C.c_int, _vp]),
+    "vfem_q2_mg_level_ke": (C.c_int, [_vp, C.c_int64, C.c_int, C.c_int, _vp]),
+    "vfem_q2_mg_smooth": (C.c_int, [_vp, C.c_int64, C.c_int, _vp, _vp, C.c_int, C.c_int]),
+    "vfem_q2_mg_residual": (C.c_int, [_vp, C.c_int64, C.c_int, _vp, _vp, _vp, C.c_int]),
+    "vfem_q2_mg_coarse_solve": (C.c_int, [_vp, C.c_int64, _vp, _vp, C.c_int]),
+    "vfem_q2_mg_vcycle": (C.c_int, [_vp, C.c_int64, _vp, _vp, C.c_int64, C.c_int]),
     "vfem_q2_pcg": (C.c_int, [_vp, C.c_int64, _vp, _vp, C.c_int64, C.c_double, C.c_int64, _vp]),
     "vfem_mg_outer_matvec_kind": (C.c_int, [_vp, C.POINTER(C.c_int)]),
     "vfem_mg_outer_apply": (C.c_int, [_vp, _vp, _vp, _vp]),

@@ -548,6 +548,246 @@ __global__ void __launch_bounds__(BS) q2_residual_combine_kernel(int64_t NN, con
     for (int c = 0; c < 3; ++c) r[c * NN + n] = ((dm >> c) & 1) ? T(0) : b[c * NN + n] - Ku[c * NN + n];
 }
 
+// ---- the triquadratic multigrid hierarchy (MultigridSolver<double, 2, 2, 2>) ----
+// Levels below the fine one hold one 81 x 81 element matrix per element, element-major
+// (Ke[e * 6561 + 81 r + c]), as the operator that the reference applies through its level-1
+// stencil (the 8 coarsened full-density matrices weighted by the fine moduli) and its blockK.
+
+// Level 1: Ke[e] = sum_f Y[child_f(e)] Kc_f over the 8 children f = 4 fx + 2 fy + fz
+// (MultigridSolver.hh:724-738)
+template <typename T>
+__global__ void __launch_bounds__(BS) q2mg_level1_kernel(Q2Dims dc, Q2Dims df, const T *__restrict__ Kc,
+                                                         const T *__restrict__ Y, T *__restrict__ Ke) {
+    const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
+    if (t >= dc.NE * 6561) return;
+    const int64_t e = t / 6561;
+    const int q = (int)(t - e * 6561);
+    const int ck = (int)(e % dc.ne[2]), cj = (int)((e / dc.ne[2]) % dc.ne[1]), ci = (int)(e / ((int64_t)dc.ne[1] * dc.ne[2]));
+    T acc = T(0);
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const int64_t ef = ((int64_t)(2 * ci + (f >> 2 & 1)) * df.ne[1] + 2 * cj + (f >> 1 & 1)) * df.ne[2] + 2 * ck + (f & 1);
+        const T v = __ldg(Y + ef) * __ldg(Kc + f * 6561 + q);
+        acc = f == 0 ? v : acc + v;
+    }
+    Ke[t] = acc;
+}
+
+// Level l >= 2: Ke_c[e] = sum_f I_f^T Ke_f[child_f(e)] I_f (MultigridSolver.hh:712-722, 745-819).
+// I_f[3i + c, 3j + d] = phi_f(i, j) delta_cd; phi_f(i, j) is a product of 1-D weights with at
+// most 2 nonzeros per coarse node and axis, so a coarse node j draws on at most 8 fine nodes i.
+// One CTA per coarse element; the child's matrix and the right product I_f stage in shared
+// memory, the left product accumulates in registers (26 entries per thread).
+constexpr int GAL_THREADS = 256;
+constexpr int GAL_PER_THREAD = (6561 + GAL_THREADS - 1) / GAL_THREADS;
+
+template <typename T>
+__global__ void __launch_bounds__(GAL_THREADS) q2mg_galerkin_kernel(Q2Dims dc, Q2Dims df, const T *__restrict__ Kf,
+                                                                    T *__restrict__ Kc) {
+    extern __shared__ __align__(16) unsigned char gal_smem[];
+    T *S = reinterpret_cast<T *>(gal_smem);
+    T *Tm = S + 6561;
+    T *nzw = Tm + 6561;                                     // [27][8] weights
+    int *nzi = reinterpret_cast<int *>(nzw + 27 * 8);       // [27][8] fine local nodes
+    int *nzc = nzi + 27 * 8;                                // [27] counts
+    const int64_t e = blockIdx.x;
+    const int ck = (int)(e % dc.ne[2]), cj = (int)((e / dc.ne[2]) % dc.ne[1]), ci = (int)(e / ((int64_t)dc.ne[1] * dc.ne[2]));
+    T acc[GAL_PER_THREAD];
+#pragma unroll
+    for (int s = 0; s < GAL_PER_THREAD; ++s) acc[s] = T(0);
+    for (int f = 0; f < 8; ++f) {
+        const int fd[3] = {f >> 2 & 1, f >> 1 & 1, f & 1};
+        const int64_t ef = ((int64_t)(2 * ci + fd[0]) * df.ne[1] + 2 * cj + fd[1]) * df.ne[2] + 2 * ck + fd[2];
+        const T *src = Kf + ef * 6561;
+        for (int q = threadIdx.x; q < 6561; q += GAL_THREADS) S[q] = src[q];
+        if (threadIdx.x < 27) {
+            // nonzeros of column j of phi_f, fine local node i ascending
+            const int j = threadIdx.x, ja[3] = {j / 9, (j / 3) % 3, j % 3};
+            int n = 0;
+            for (int a = 0; a < 3; ++a) {
+                const double wa = q2_basis(ja[0], 0.25 * (2 * fd[0] + a));
+                if (wa == 0.0) continue;
+                for (int b = 0; b < 3; ++b) {
+                    const double wb = q2_basis(ja[1], 0.25 * (2 * fd[1] + b));
+                    if (wb == 0.0) continue;
+                    for (int c = 0; c < 3; ++c) {
+                        const double wc = q2_basis(ja[2], 0.25 * (2 * fd[2] + c));
+                        if (wc == 0.0) continue;
+                        nzw[8 * j + n] = (T)(wa * wb * wc);
+                        nzi[8 * j + n] = 9 * a + 3 * b + c;
+                        ++n;
+                    }
+                }
+            }
+            nzc[j] = n;
+        }
+        __syncthreads();
+        // Tm[r][3 j + d] = sum_i S[r][3 i + d] phi_f(i, j)
+        for (int q = threadIdx.x; q < 6561; q += GAL_THREADS) {
+            const int r = q / 81, cc = q - 81 * r, j = cc / 3, d = cc - 3 * j;
+            T v = T(0);
+            for (int t = 0; t < nzc[j]; ++t) v += S[81 * r + 3 * nzi[8 * j + t] + d] * nzw[8 * j + t];
+            Tm[q] = v;
+        }
+        __syncthreads();
+        // acc[3 j + c][q] += sum_i phi_f(i, j) Tm[3 i + c][q]
+#pragma unroll
+        for (int s = 0; s < GAL_PER_THREAD; ++s) {
+            const int q = threadIdx.x + GAL_THREADS * s;
+            if (q < 6561) {
+                const int R = q / 81, Q = q - 81 * R, j = R / 3, c = R - 3 * j;
+                T v = T(0);
+                for (int t = 0; t < nzc[j]; ++t) v += nzw[8 * j + t] * Tm[81 * (3 * nzi[8 * j + t] + c) + Q];
+                acc[s] += v;
+            }
+        }
+        __syncthreads();
+    }
+    T *dst = Kc + e * 6561;
+#pragma unroll
+    for (int s = 0; s < GAL_PER_THREAD; ++s) {
+        const int q = threadIdx.x + GAL_THREADS * s;
+        if (q < 6561) dst[q] = acc[s];
+    }
+}
+
+// Incident elements of node I along one axis in ascending element order (local coordinate 2 in
+// element I/2 - 1, then 0 in element I/2; 1 in element (I-1)/2 for an odd I)
+__device__ __forceinline__ int axis_elems_asc(int I, int ne, int *ei, int *la) {
+    if (I & 1) {
+        ei[0] = (I - 1) >> 1;
+        la[0] = 1;
+        return 1;
+    }
+    int n = 0;
+    if ((I >> 1) - 1 >= 0) { ei[n] = (I >> 1) - 1; la[n] = 2; ++n; }
+    if ((I >> 1) < ne) { ei[n] = I >> 1; la[n] = 0; ++n; }
+    return n;
+}
+
+// One warp per node: s_r = sum over the incident elements of row 3 ln + r of Ke times the
+// element's nodal values; lanes 0..8 also sum the 3 x 3 diagonal block M (lane 3 r + c).
+template <typename T>
+__device__ __forceinline__ void q2mg_node_rows(const Q2Dims &d, const T *__restrict__ Ke, const T *u, int I, int J,
+                                               int K, int lane, T &a0, T &a1, T &a2, T &mv) {
+    int ex[2], lx[2], ey[2], ly[2], ez[2], lz[2];
+    const int cx = axis_elems_asc(I, d.ne[0], ex, lx), cy = axis_elems_asc(J, d.ne[1], ey, ly),
+              cz = axis_elems_asc(K, d.ne[2], ez, lz);
+    const int64_t ld = d.NN;
+    for (int a = 0; a < cx; ++a)
+        for (int b = 0; b < cy; ++b)
+            for (int c = 0; c < cz; ++c) {
+                const int64_t e = ((int64_t)ex[a] * d.ne[1] + ey[b]) * d.ne[2] + ez[c];
+                const int ln = 9 * lx[a] + 3 * ly[b] + lz[c];
+                const T *Kr = Ke + e * 6561 + 243 * ln;
+                const int bx = 2 * ex[a], by = 2 * ey[b], bz = 2 * ez[c];
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    const int q = lane + 32 * s;
+                    if (q < 243) {
+                        const int r = q >= 162 ? 2 : (q >= 81 ? 1 : 0);
+                        const int cc = q - 81 * r, m = cc / 3, comp = cc - 3 * m;
+                        const int64_t nm = q2node(d, bx + m / 9, by + (m / 3) % 3, bz + m % 3);
+                        const T v = __ldg(Kr + q) * u[comp * ld + nm];
+                        if (r == 0) a0 += v;
+                        else if (r == 1) a1 += v;
+                        else a2 += v;
+                    }
+                }
+                if (lane < 9) mv += __ldg(Kr + 81 * (lane / 3) + 3 * ln + lane % 3);
+            }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+}
+
+// One colour (a, b, c) of the 27-colour block Gauss-Seidel sweep on a level with element
+// matrices (NodeSmoothStencilSecondFinest / NodeSmoothStencilBlockK, MultigridSolver.hh:294-378)
+template <typename T>
+__global__ void __launch_bounds__(BS) q2mg_gs_kernel(Q2Dims d, const T *__restrict__ Ke, T *u,
+                                                     const T *__restrict__ b, const uint8_t *__restrict__ dmask,
+                                                     int ca, int cb, int cc, int forward) {
+    const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
+    const int n0 = (d.nn[0] - 1 - ca) / ia + 1, n1 = (d.nn[1] - 1 - cb) / ib + 1, n2 = (d.nn[2] - 1 - cc) / ic + 1;
+    const int64_t w = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (int64_t)n0 * n1 * n2) return;  // uniform over the warp
+    const int64_t q = w / n2;
+    const int K = cc + ic * (int)(w - q * n2);
+    const int J = cb + ib * (int)(q % n1), I = ca + ia * (int)(q / n1);
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    T a0 = T(0), a1 = T(0), a2 = T(0), mv = T(0);
+    q2mg_node_rows<T>(d, Ke, u, I, J, K, lane, a0, a1, a2, mv);
+    T M[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) M[t] = __shfl_sync(0xffffffffu, mv, t);
+    if (lane == 0) {
+        T u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+        q2_node_update<T>(dm, b[n] - a0, b[ld + n] - a1, b[2 * ld + n] - a2, M, forward != 0, u0, u1, u2);
+        u[n] = u0;
+        u[ld + n] = u1;
+        u[2 * ld + n] = u2;
+    }
+}
+
+// out = K u (Residual: out = b - K u), zero on the constrained components when zeroDirichlet
+// (computeResidual, MultigridSolver.hh:527-541); one warp per node
+template <typename T, bool Residual>
+__global__ void __launch_bounds__(BS) q2mg_apply_kernel(Q2Dims d, const T *__restrict__ Ke, const T *__restrict__ u,
+                                                        const T *__restrict__ b, T *__restrict__ out,
+                                                        const uint8_t *__restrict__ dmask, int zeroDirichlet) {
+    const int64_t w = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= d.NN) return;
+    const int64_t q = w / d.nn[2];
+    const int K = (int)(w - q * d.nn[2]), J = (int)(q % d.nn[1]), I = (int)(q / d.nn[1]);
+    T a0 = T(0), a1 = T(0), a2 = T(0), mv = T(0);
+    q2mg_node_rows<T>(d, Ke, u, I, J, K, lane, a0, a1, a2, mv);
+    if (lane == 0) {
+        const uint8_t dm = zeroDirichlet ? dmask[w] : 0;
+        const T v[3] = {a0, a1, a2};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T r = Residual ? b[c * d.NN + w] - v[c] : v[c];
+            out[c * d.NN + w] = ((dm >> c) & 1) ? T(0) : r;
+        }
+    }
+}
+
+// Dense reduced coarsest operator: one thread per free row (DOF 3 n + c), summing its element
+// rows over the incident elements in ascending order (TensorProductSimulator.hh:1198-1230)
+template <typename T>
+__global__ void __launch_bounds__(BS) q2mg_dense_kernel(Q2Dims d, const T *__restrict__ Ke, const int *__restrict__ freeIdx,
+                                                        const int *__restrict__ redIdx, int nfree, double *A) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    if (i >= nfree) return;
+    const int dof = freeIdx[i], n = dof / 3, c = dof - 3 * n;
+    const int K = n % d.nn[2], J = (n / d.nn[2]) % d.nn[1], I = n / (d.nn[2] * d.nn[1]);
+    int ex[2], lx[2], ey[2], ly[2], ez[2], lz[2];
+    const int cx = axis_elems_asc(I, d.ne[0], ex, lx), cy = axis_elems_asc(J, d.ne[1], ey, ly),
+              cz = axis_elems_asc(K, d.ne[2], ez, lz);
+    double *row = A + (int64_t)i * nfree;
+    for (int a = 0; a < cx; ++a)
+        for (int b = 0; b < cy; ++b)
+            for (int z = 0; z < cz; ++z) {
+                const int64_t e = ((int64_t)ex[a] * d.ne[1] + ey[b]) * d.ne[2] + ez[z];
+                const int ln = 9 * lx[a] + 3 * ly[b] + lz[z];
+                const T *Kr = Ke + e * 6561 + 81 * (3 * ln + c);
+                for (int m = 0; m < 27; ++m) {
+                    const int64_t nm = q2node(d, 2 * ex[a] + m / 9, 2 * ey[b] + (m / 3) % 3, 2 * ez[z] + m % 3);
+                    for (int dd = 0; dd < 3; ++dd) {
+                        const int col = redIdx[3 * nm + dd];
+                        if (col >= 0) row[col] += (double)Kr[3 * m + dd];
+                    }
+                }
+            }
+}
+
 Q2Dims dims_of(const int ne[3]) {
     Q2Dims d;
     for (int a = 0; a < 3; ++a) {
@@ -676,6 +916,65 @@ void launch_q2_residual_combine(int64_t NN, const T *b, const T *Ku, T *r, const
     VFEM_LAUNCH_CHECK();
 }
 
+// ---- triquadratic multigrid hierarchy ----
+template <typename T>
+void launch_q2mg_level1(const int neCoarse[3], const T *Kc, const T *Y, T *Ke, cudaStream_t st) {
+    const int nef[3] = {2 * neCoarse[0], 2 * neCoarse[1], 2 * neCoarse[2]};
+    const Q2Dims dc = dims_of(neCoarse), df = dims_of(nef);
+    q2mg_level1_kernel<T><<<gridFor(dc.NE * 6561, BS), BS, 0, st>>>(dc, df, Kc, Y, Ke);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_q2mg_galerkin(const int neCoarse[3], const T *KeFine, T *KeCoarse, cudaStream_t st) {
+    const int nef[3] = {2 * neCoarse[0], 2 * neCoarse[1], 2 * neCoarse[2]};
+    const Q2Dims dc = dims_of(neCoarse), df = dims_of(nef);
+    const size_t smem = sizeof(T) * (2 * 6561 + 27 * 8) + sizeof(int) * (27 * 8 + 27);
+    static bool attrSet[2] = {false, false};
+    bool &set = attrSet[sizeof(T) == 8 ? 1 : 0];
+    if (!set) {
+        VFEM_CUDA(cudaFuncSetAttribute(q2mg_galerkin_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set = true;
+    }
+    if (dc.NE > 0) q2mg_galerkin_kernel<T><<<(unsigned)dc.NE, GAL_THREADS, smem, st>>>(dc, df, KeFine, KeCoarse);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_q2mg_gs_sweep(const int ne[3], const T *Ke, T *u, const T *b, const uint8_t *dmask, bool forward,
+                          cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    for (int s = 0; s < 27; ++s) {
+        const int col = forward ? s : 26 - s;
+        const int ca = col / 9, cb = (col / 3) % 3, cc = col % 3;
+        const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
+        if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2]) continue;
+        const int64_t cnt = (int64_t)((d.nn[0] - 1 - ca) / ia + 1) * ((d.nn[1] - 1 - cb) / ib + 1) *
+                            ((d.nn[2] - 1 - cc) / ic + 1);
+        q2mg_gs_kernel<T><<<gridFor(32 * cnt, BS), BS, 0, st>>>(d, Ke, u, b, dmask, ca, cb, cc, forward ? 1 : 0);
+        VFEM_LAUNCH_CHECK();
+    }
+}
+
+template <typename T>
+void launch_q2mg_apply(const int ne[3], const T *Ke, const T *u, const T *b, T *out, const uint8_t *dmask,
+                       bool zeroDirichlet, cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    const unsigned gs = gridFor(32 * d.NN, BS);
+    if (b) q2mg_apply_kernel<T, true><<<gs, BS, 0, st>>>(d, Ke, u, b, out, dmask, zeroDirichlet ? 1 : 0);
+    else q2mg_apply_kernel<T, false><<<gs, BS, 0, st>>>(d, Ke, u, nullptr, out, dmask, zeroDirichlet ? 1 : 0);
+    VFEM_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_q2mg_dense(const int ne[3], const T *Ke, const int *freeIdx, const int *redIdx, int nfree, double *A,
+                       cudaStream_t st) {
+    const Q2Dims d = dims_of(ne);
+    VFEM_CUDA(cudaMemsetAsync(A, 0, sizeof(double) * (size_t)nfree * nfree, st));
+    if (nfree > 0) q2mg_dense_kernel<T><<<gridFor(nfree, BS), BS, 0, st>>>(d, Ke, freeIdx, redIdx, nfree, A);
+    VFEM_LAUNCH_CHECK();
+}
+
 #define VFEM_INST_Q2(T)                                                                                               \
     template void launch_applyk_q2<T>(const int[3], const T *, const T *, const T *, T *, const uint8_t *, bool,      \
                                       cudaStream_t);                                                                  \
@@ -685,7 +984,14 @@ void launch_q2_residual_combine(int64_t NN, const T *b, const T *Ku, T *r, const
     template void launch_interp_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);                              \
     template void launch_interp_q1_q2<T>(const int[3], const T *, T *, bool, cudaStream_t);                           \
     template void launch_restrict_q2_q1<T>(const int[3], const T *, T *, cudaStream_t);                               \
-    template void launch_q2_residual_combine<T>(int64_t, const T *, const T *, T *, const uint8_t *, cudaStream_t);
+    template void launch_q2_residual_combine<T>(int64_t, const T *, const T *, T *, const uint8_t *, cudaStream_t); \
+    template void launch_q2mg_level1<T>(const int[3], const T *, const T *, T *, cudaStream_t);                       \
+    template void launch_q2mg_galerkin<T>(const int[3], const T *, T *, cudaStream_t);                                \
+    template void launch_q2mg_gs_sweep<T>(const int[3], const T *, T *, const T *, const uint8_t *, bool,             \
+                                          cudaStream_t);                                                              \
+    template void launch_q2mg_apply<T>(const int[3], const T *, const T *, const T *, T *, const uint8_t *, bool,     \
+                                       cudaStream_t);                                                                 \
+    template void launch_q2mg_dense<T>(const int[3], const T *, const int *, const int *, int, double *, cudaStream_t);
 VFEM_INST_Q2(double)
 VFEM_INST_Q2(float)
 

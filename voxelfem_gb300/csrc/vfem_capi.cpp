@@ -700,6 +700,89 @@ int vfem_q2_pcg(vfem_q2 *g, int64_t coarsenings, double *x_inout, const double *
         }
     });
 }
+int vfem_q2_set_hierarchy(vfem_q2 *g, int hierarchy) {
+    return guarded([&] {
+        need(g, "grid");
+        g->g.setHierarchy(hierarchy);
+    });
+}
+int vfem_q2_set_precision(vfem_q2 *g, int precision) {
+    return guarded([&] {
+        need(g, "grid");
+        g->g.setPrecision(precision);
+    });
+}
+static void q2Level(vfem_q2 *g, int64_t coarsenings, int level) {
+    need(g, "grid");
+    if (coarsenings < 1 || coarsenings > 30) throw Error(ERR_ARG, "the triquadratic hierarchy needs at least one coarsening");
+    if (level < 0 || level > coarsenings) throw Error(ERR_ARG, "level out of range");
+}
+static void q2Precision(int precision) {
+    if (precision != PREC_FP64 && precision != PREC_MIXED) throw Error(ERR_ARG, "precision must be fp64 or mixed");
+}
+int vfem_q2_mg_num_nodes(vfem_q2 *g, int64_t coarsenings, int level, int64_t *num_nodes) {
+    return guarded([&] {
+        q2Level(g, coarsenings, level);
+        need(num_nodes, "num_nodes");
+        *num_nodes = g->g.mgLevelNodes((int)coarsenings, level);
+    });
+}
+int vfem_q2_mg_level_dirichlet(vfem_q2 *g, int64_t coarsenings, int level, uint8_t *mask_out) {
+    return guarded([&] {
+        q2Level(g, coarsenings, level);
+        need(mask_out, "mask_out");
+        g->g.mgLevelDirichlet((int)coarsenings, level, mask_out);
+    });
+}
+int vfem_q2_mg_level_ke(vfem_q2 *g, int64_t coarsenings, int level, int precision, double *out) {
+    return guarded([&] {
+        q2Level(g, coarsenings, level);
+        q2Precision(precision);
+        need(out, "out");
+        g->g.mgLevelKe((int)coarsenings, level, precision, out);
+    });
+}
+int vfem_q2_mg_smooth(vfem_q2 *g, int64_t coarsenings, int level, double *u_inout, const double *b, int forward,
+                      int precision) {
+    return guarded([&] {
+        q2Level(g, coarsenings, level);
+        q2Precision(precision);
+        need(u_inout, "u");
+        need(b, "b");
+        g->g.mgSmooth((int)coarsenings, level, u_inout, b, forward != 0, precision);
+    });
+}
+int vfem_q2_mg_residual(vfem_q2 *g, int64_t coarsenings, int level, const double *u, const double *b, double *r,
+                        int precision) {
+    return guarded([&] {
+        q2Level(g, coarsenings, level);
+        q2Precision(precision);
+        need(u, "u");
+        need(b, "b");
+        need(r, "r");
+        g->g.mgResidual((int)coarsenings, level, u, b, r, precision);
+    });
+}
+int vfem_q2_mg_coarse_solve(vfem_q2 *g, int64_t coarsenings, const double *b, double *x, int precision) {
+    return guarded([&] {
+        q2Level(g, coarsenings, 0);
+        q2Precision(precision);
+        need(b, "b");
+        need(x, "x");
+        g->g.mgCoarseSolve((int)coarsenings, b, x, precision);
+    });
+}
+int vfem_q2_mg_vcycle(vfem_q2 *g, int64_t coarsenings, const double *b, double *x, int64_t mg_smoothing_iterations,
+                      int precision) {
+    return guarded([&] {
+        q2Level(g, coarsenings, 0);
+        q2Precision(precision);
+        need(b, "b");
+        need(x, "x");
+        if (mg_smoothing_iterations < 0) throw Error(ERR_ARG, "mgSmoothingIterations must be non-negative");
+        g->g.mgVcycle((int)coarsenings, b, x, mg_smoothing_iterations, precision);
+    });
+}
 int vfem_q2_time_smooth(vfem_q2 *g, int precision, int reps, double *ms, double *bytes) {
     return guarded([&] {
         need(g, "grid");

@@ -413,8 +413,26 @@ private:
     void jacobianDev(double *out);
 };
 
-// Triquadratic voxel grid (vfem_q2.cpp): K0, moduli, supports, applyK and the 27-colour
-// block Gauss-Seidel sweep.
+// A level below the fine one of the triquadratic multigrid hierarchy: a Q2 mesh with half the
+// elements per axis of the level above, its coarsened supports, one 81 x 81 element matrix per
+// element (element-major) and its work vectors.
+struct Q2Level {
+    int ne[3];
+    int64_t NN, NE;
+    std::vector<uint8_t> dmask_h;
+    DevBuf<uint8_t> dmask;
+    DevBuf<double> Ke64;
+    DevBuf<float> Ke32;
+    LevelData<double> w64;
+    LevelData<float> w32;
+};
+
+// Preconditioner of the triquadratic PCG: the reference's hierarchy of halved Q2 meshes
+// (MultigridSolver<double, 2, 2, 2>), or a p-multigrid step onto the trilinear mesh.
+enum Q2Hierarchy { Q2_HIER_Q2 = 0, Q2_HIER_P = 1 };
+
+// Triquadratic voxel grid (vfem_q2.cpp): K0, moduli, supports, applyK, the 27-colour block
+// Gauss-Seidel sweep and the PCG with its multigrid preconditioner.
 class GridQ2 {
 public:
     GridQ2(const int ne[3], const double bmin[3], const double bmax[3]);
@@ -453,8 +471,55 @@ public:
     // preconditioner: Q2 block Gauss-Seidel smoothing around one FP32 V-cycle of the trilinear
     // problem on the same mesh (`coarsenings` coarsenings); x in/out.
     PcgStats pcg(double *x, const double *b, int64_t maxIter, double tol, int coarsenings, int64_t sweeps);
+    int hierarchy = Q2_HIER_Q2;   // preconditioner of pcg (Q2Hierarchy)
+    int vprecision = PREC_MIXED;  // V-cycle precision of the Q2 hierarchy
+    bool symmetricGS = true;      // backward post-smoothing sweeps
+    void setHierarchy(int kind);
+    // PREC_FP64: FP64 V-cycle and outer matvec (the reference's method); PREC_MIXED: FP32 V-cycle
+    // and double-float outer matvec
+    void setPrecision(int precision);
+    // The Q2 hierarchy with `coarsenings` coarsenings, built on demand in `precision`; level 0 is
+    // this grid. Vectors are host or device (numNodes(l), 3) fields.
+    int64_t mgLevelNodes(int coarsenings, int l);
+    void mgLevelDirichlet(int coarsenings, int l, uint8_t *out);
+    void mgLevelKe(int coarsenings, int l, int precision, double *out);
+    void mgSmooth(int coarsenings, int l, double *u, const double *b, bool forward, int precision);
+    void mgResidual(int coarsenings, int l, const double *u, const double *b, double *r, int precision);
+    void mgCoarseSolve(int coarsenings, const double *b, double *x, int precision);
+    // x = one V-cycle from zero on K x = b (the preconditioner of pcg)
+    void mgVcycle(int coarsenings, const double *b, double *x, int64_t sweeps, int precision);
 
 private:
+    uint64_t version = 1;                // bumped when the moduli, K0 or the supports change
+    std::vector<double> Kc;              // 8 x 6561 coarsened full-density element matrices
+    std::vector<Q2Level> qlv;            // levels 1..L of the Q2 hierarchy
+    int qCoarsenings = -1, qPrecision = -1;
+    uint64_t qVersion = 0;
+    int qNfree = 0;
+    DevBuf<double> Kc64;
+    DevBuf<float> Kc32;
+    DevBuf<int> qFreeIdx, qRedIdx, qNfreeDev, qStatus;
+    DevBuf<double> qAinv, qWork, qScratch;
+    void prepareHierarchy(int coarsenings, int precision);
+    template <typename T>
+    void buildHierarchyT();
+    template <typename T>
+    LevelData<T> &qwork(int l);
+    template <typename T>
+    const T *qKe(int l);
+    template <typename T>
+    void qSmoothT(int l, T *u, const T *b, bool forward);
+    template <typename T>
+    void qResidualT(int l, const T *u, const T *b, T *r);
+    template <typename T>
+    void qCoarseSolveT(const T *b, T *x);
+    template <typename T>
+    void vcycleQ2T(int l, int64_t sweeps);
+    template <typename T>
+    void preconditionQ2T(const double *r, int64_t sweeps);
+    const int *levelNe(int l) const { return l == 0 ? ne : qlv[l - 1].ne; }
+    const uint8_t *levelMask(int l) const { return l == 0 ? dmask.p : qlv[l - 1].dmask.p; }
+    int64_t levelNN(int l) const { return l == 0 ? NN : qlv[l - 1].NN; }
     struct Box {
         double mn[3], mx[3];
         unsigned cmask;
@@ -481,6 +546,8 @@ private:
 };
 // Q2 restriction / prolongation between a grid with neFine elements per axis and its 2x coarsening.
 void q2Restrict(const int neFine[3], const double *fine, double *coarse);
+// Kc[f] = I_f^T K0 I_f, f = 4 fx + 2 fy + fz: the 8 coarsened full-density Q2 element matrices
+void q2CoarsenedK0(const double *K0, std::vector<double> &Kc);
 void q2Interpolate(const int neFine[3], const double *coarse, double *fine, bool accumulate);
 
 // Layer-by-layer solves of partial-build heights (layers[t] element layers built) over

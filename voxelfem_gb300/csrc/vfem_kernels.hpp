@@ -389,4 +389,25 @@ void launch_restrict_q2_q1(const int ne[3], const T *q2, T *q1, cudaStream_t st)
 template <typename T>
 void launch_q2_residual_combine(int64_t NN, const T *b, const T *Ku, T *r, const uint8_t *dmask, cudaStream_t st);
 
+// Triquadratic multigrid hierarchy: element matrices Ke (element-major, 6561 per element) on the
+// levels below the fine one.
+// level 1 (neCoarse elements per axis): Ke[e] = sum_f Y[child_f(e)] Kc[f], Kc 8 x 6561
+template <typename T>
+void launch_q2mg_level1(const int neCoarse[3], const T *Kc, const T *Y, T *Ke, cudaStream_t st);
+// level l >= 2: KeCoarse[e] = sum_f I_f^T KeFine[child_f(e)] I_f
+template <typename T>
+void launch_q2mg_galerkin(const int neCoarse[3], const T *KeFine, T *KeCoarse, cudaStream_t st);
+// one block Gauss-Seidel sweep over the 27 colours with the element matrices
+template <typename T>
+void launch_q2mg_gs_sweep(const int ne[3], const T *Ke, T *u, const T *b, const uint8_t *dmask, bool forward,
+                          cudaStream_t st);
+// out = K u, or out = b - K u when b is given; constrained components zeroed when zeroDirichlet
+template <typename T>
+void launch_q2mg_apply(const int ne[3], const T *Ke, const T *u, const T *b, T *out, const uint8_t *dmask,
+                       bool zeroDirichlet, cudaStream_t st);
+// A (nfree x nfree, zeroed here) = the operator on the free DOFs freeIdx (3 n + c; redIdx inverse)
+template <typename T>
+void launch_q2mg_dense(const int ne[3], const T *Ke, const int *freeIdx, const int *redIdx, int nfree, double *A,
+                       cudaStream_t st);
+
 }  // namespace vfem

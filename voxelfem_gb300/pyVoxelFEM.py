@@ -1389,22 +1389,83 @@ class TensorProductSimulator_3D_Q2:
         return x
 
     def multigridSolver(self, numCoarseningLevels):
-        """A PCG solver for this grid: FP64 outer iteration, p-multigrid preconditioner (Q2 block
-        Gauss-Seidel around a trilinear V-cycle with numCoarseningLevels coarsenings)."""
+        """MultigridSolver(self, numCoarseningLevels) for this grid (MultigridSolver<double, 2, 2, 2>):
+        FP64 outer PCG, preconditioned by the reference's hierarchy of halved Q2 meshes (default)
+        or by a p-multigrid step onto the trilinear mesh (``setHierarchy("p")``)."""
         return _Q2MultigridSolver(self, int(numCoarseningLevels))
+
+
+_Q2_PREC = {"fp64": 0, "mixed": 1}
 
 
 class _Q2MultigridSolver:
     def __init__(self, tps, numCoarseningLevels):
         if numCoarseningLevels < 1:
-            raise RuntimeError("the triquadratic solver needs at least one coarsening of the trilinear mesh")
+            raise RuntimeError("the triquadratic solver needs at least one coarsening")
         self.tps = tps
         self.coarsenings = numCoarseningLevels
         self.lastStats = None
 
     def setOuterMatvec(self, outerMatvec="df"):
-        """CG matvec in 'df' (double-float, default) or 'fp64'."""
+        """CG matvec in 'df' (double-float) or 'fp64'."""
         check(_lib().vfem_q2_set_outer_matvec(self.tps._h, {"fp64": 0, "df": 1}[outerMatvec]))
+
+    def setHierarchy(self, hierarchy="q2"):
+        """Preconditioner hierarchy: 'q2' (the reference's halved Q2 meshes, default) or 'p'
+        (Q2 smoothing around a trilinear V-cycle on the same mesh; mixed precision only)."""
+        check(_lib().vfem_q2_set_hierarchy(self.tps._h, {"q2": 0, "p": 1}[hierarchy]))
+
+    def setPrecision(self, precision="mixed"):
+        """'fp64' (the reference's method: FP64 V-cycle and CG matvec) or 'mixed' (default: FP32
+        V-cycle, double-float CG matvec)."""
+        check(_lib().vfem_q2_set_precision(self.tps._h, _Q2_PREC[precision]))
+
+    # ---- per-level access to the Q2 hierarchy (MultigridSolver.hh) ----
+    def numNodes(self, l):
+        n = C.c_int64()
+        check(_lib().vfem_q2_mg_num_nodes(self.tps._h, self.coarsenings, int(l), C.byref(n)))
+        return n.value
+
+    def levelDirichletMask(self, l):
+        m = np.empty(self.numNodes(l), dtype=np.uint8)
+        check(_lib().vfem_q2_mg_level_dirichlet(self.tps._h, self.coarsenings, int(l), m.ctypes.data_as(C.c_void_p)))
+        return np.stack([(m >> c) & 1 for c in range(3)], axis=1).astype(bool)
+
+    def levelElementMatrices(self, l, precision="fp64"):
+        ne = [v >> int(l) for v in self.tps._ne]
+        out = np.empty(int(np.prod(ne)) * 6561)
+        check(_lib().vfem_q2_mg_level_ke(self.tps._h, self.coarsenings, int(l), _Q2_PREC[precision], _capi.dptr(out)))
+        return out.reshape(-1, 81, 81)
+
+    def smoothing(self, l, u, b, forwardSweep=True, precision="fp64"):
+        nn = self.numNodes(l)
+        x = _as_vfield(u, nn).copy(order="F")
+        b = _as_vfield(b, nn)
+        check(_lib().vfem_q2_mg_smooth(self.tps._h, self.coarsenings, int(l), ptr(x), ptr(b), int(bool(forwardSweep)),
+                                       _Q2_PREC[precision]))
+        return x
+
+    def computeResidual(self, l, u, b, precision="fp64"):
+        nn = self.numNodes(l)
+        out = _new_vfield(nn)
+        check(_lib().vfem_q2_mg_residual(self.tps._h, self.coarsenings, int(l), ptr(_as_vfield(u, nn)),
+                                         ptr(_as_vfield(b, nn)), ptr(out), _Q2_PREC[precision]))
+        return out
+
+    def coarseSolve(self, b, precision="fp64"):
+        nn = self.numNodes(self.coarsenings)
+        out = _new_vfield(nn)
+        check(_lib().vfem_q2_mg_coarse_solve(self.tps._h, self.coarsenings, ptr(_as_vfield(b, nn)), ptr(out),
+                                             _Q2_PREC[precision]))
+        return out
+
+    def applyPreconditionerInv(self, r, mgSmoothingIterations=1, precision="fp64"):
+        """One V-cycle from zero on K x = r (MultigridSolver.hh:576-580)."""
+        nn = self.tps.numNodes()
+        out = _new_vfield(nn)
+        check(_lib().vfem_q2_mg_vcycle(self.tps._h, self.coarsenings, ptr(_as_vfield(r, nn)), ptr(out),
+                                       int(mgSmoothingIterations), _Q2_PREC[precision]))
+        return out
 
     def preconditionedConjugateGradient(self, u, b, maxIter, tol, it_callback=None, mgIterations=1,
                                         mgSmoothingIterations=1, fullMultigrid=False):
