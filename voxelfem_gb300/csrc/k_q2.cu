@@ -383,23 +383,47 @@ __global__ void __launch_bounds__(BS) gs_q2_color_kernel(Q2Dims d, const T *Kg, 
     u[2 * ld + n] = u2;
 }
 
-// Coarse Q2 shape functions along one axis at fine node f (0 <= f <= 4 nec): the coarse element
-// e = min(f / 4, nec - 1), reference coordinate x = (f - 4e) / 4, equispaced quadratic Lagrange
-// basis N0 = 2 (x - 1/2)(x - 1), N1 = -4 x (x - 1), N2 = 2 x (x - 1/2) on coarse nodes 2e + lc.
-__device__ __forceinline__ double q2_basis(int lc, double x) {
-    return lc == 0 ? 2 * (x - 0.5) * (x - 1.0) : (lc == 1 ? -4 * x * (x - 1.0) : 2 * x * (x - 0.5));
+// Weights of the coarse Q2 shape functions lc = 0, 1, 2 at the fine node with local position
+// t = f - 4e in 0..4 of its coarse element e (reference coordinate t / 4): N0 = 2 (x - 1/2)(x - 1),
+// N1 = -4 x (x - 1), N2 = 2 x (x - 1/2). All are dyadic, exact in FP32.
+__device__ __forceinline__ double q2_axis_weight(int t, int lc) {
+    switch (3 * t + lc) {
+    case 0: return 1.0;
+    case 3: return 0.375;
+    case 4: return 0.75;
+    case 5: return -0.125;
+    case 7: return 1.0;
+    case 9: return -0.125;
+    case 10: return 0.75;
+    case 11: return 0.375;
+    case 14: return 1.0;
+    default: return 0.0;
+    }
 }
 
-__device__ __forceinline__ void q2_axis(int f, int nec, int &base, double w[3]) {
+// Coarse nodes (base + lc) and weights of fine node f along one axis: one node for an even local
+// position (coinciding nodes), three for an odd one.
+template <typename T>
+__device__ __forceinline__ int q2_axis(int f, int nec, int &base, int *lc, T *w) {
     int e = f >> 2;
     if (e >= nec) e = nec - 1;
     base = 2 * e;
-    const double x = 0.25 * (f - 4 * e);
+    const int t = f - 4 * e;
+    if (!(t & 1)) {
+        lc[0] = t >> 1;
+        w[0] = T(1);
+        return 1;
+    }
 #pragma unroll
-    for (int lc = 0; lc < 3; ++lc) w[lc] = q2_basis(lc, x);
+    for (int c = 0; c < 3; ++c) {
+        lc[c] = c;
+        w[c] = (T)q2_axis_weight(t, c);
+    }
+    return 3;
 }
 
-// fine (=|+=) P coarse: the coarse Q2 interpolant evaluated at the fine nodes (MultigridSolver.hh:137-212)
+// fine (=|+=) P coarse: the coarse Q2 interpolant evaluated at the fine nodes (MultigridSolver.hh:137-212),
+// summed in the vectors' precision
 template <typename T>
 __global__ void __launch_bounds__(BS) interp_q2_kernel(Q2Dims df, Q2Dims dc, const T *__restrict__ coarse,
                                                        T *__restrict__ fine, int accumulate) {
@@ -407,27 +431,24 @@ __global__ void __launch_bounds__(BS) interp_q2_kernel(Q2Dims df, Q2Dims dc, con
     if (t >= df.NN) return;
     const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)df.nn[2];
     const int F[3] = {(int)(q / (uint32_t)df.nn[1]), (int)(q % (uint32_t)df.nn[1]), (int)(tt - q * (uint32_t)df.nn[2])};
-    int base[3];
-    double w[3][3];
+    int base[3], lc[3][3], cnt[3];
+    T w[3][3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) q2_axis(F[a], dc.ne[a], base[a], w[a]);
-    double acc[3] = {0.0, 0.0, 0.0};
-    for (int a = 0; a < 3; ++a) {
-        if (w[0][a] == 0.0) continue;
-        for (int b = 0; b < 3; ++b) {
-            if (w[1][b] == 0.0) continue;
-            for (int c = 0; c < 3; ++c) {
-                const double wt = w[0][a] * w[1][b] * w[2][c];
-                if (wt == 0.0) continue;
-                const int64_t cn = q2node(dc, base[0] + a, base[1] + b, base[2] + c);
+    for (int a = 0; a < 3; ++a) cnt[a] = q2_axis<T>(F[a], dc.ne[a], base[a], lc[a], w[a]);
+    T acc[3] = {T(0), T(0), T(0)};
+    for (int a = 0; a < cnt[0]; ++a)
+        for (int b = 0; b < cnt[1]; ++b) {
+            const T wab = w[0][a] * w[1][b];
+            for (int c = 0; c < cnt[2]; ++c) {
+                const T wt = wab * w[2][c];
+                const int64_t cn = q2node(dc, base[0] + lc[0][a], base[1] + lc[1][b], base[2] + lc[2][c]);
 #pragma unroll
-                for (int r = 0; r < 3; ++r) acc[r] += wt * (double)coarse[r * dc.NN + cn];
+                for (int r = 0; r < 3; ++r) acc[r] += wt * coarse[r * dc.NN + cn];
             }
         }
-    }
     const int64_t n = q2node(df, F[0], F[1], F[2]);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) fine[r * df.NN + n] = (accumulate ? fine[r * df.NN + n] : T(0)) + (T)acc[r];
+    for (int r = 0; r < 3; ++r) fine[r * df.NN + n] = (accumulate ? fine[r * df.NN + n] : T(0)) + acc[r];
 }
 
 // coarse = P^T fine: coarse node C gathers the fine nodes [2C - 3, 2C + 3] (per axis) whose
@@ -439,38 +460,40 @@ __global__ void __launch_bounds__(BS) restrict_q2_kernel(Q2Dims df, Q2Dims dc, c
     if (t >= dc.NN) return;
     const uint32_t tt = (uint32_t)t, q = tt / (uint32_t)dc.nn[2];
     const int C[3] = {(int)(q / (uint32_t)dc.nn[1]), (int)(q % (uint32_t)dc.nn[1]), (int)(tt - q * (uint32_t)dc.nn[2])};
-    double wt[3][7];
+    int fo[3][7], cnt[3];
+    T wt[3][7];
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a) {
+        cnt[a] = 0;
 #pragma unroll
         for (int s = 0; s < 7; ++s) {
             const int f = 2 * C[a] - 3 + s;
-            double wv = 0.0;
-            if (f >= 0 && f < df.nn[a]) {
-                int e = f >> 2;
-                if (e >= dc.ne[a]) e = dc.ne[a] - 1;
-                const int lc = C[a] - 2 * e;
-                if (lc >= 0 && lc <= 2) wv = q2_basis(lc, 0.25 * (f - 4 * e));
-            }
-            wt[a][s] = wv;
-        }
-    double acc[3] = {0.0, 0.0, 0.0};
-    for (int s = 0; s < 7; ++s) {
-        if (wt[0][s] == 0.0) continue;
-        for (int v = 0; v < 7; ++v) {
-            if (wt[1][v] == 0.0) continue;
-            for (int z = 0; z < 7; ++z) {
-                const double w = wt[0][s] * wt[1][v] * wt[2][z];
-                if (w == 0.0) continue;
-                const int64_t fn = q2node(df, 2 * C[0] - 3 + s, 2 * C[1] - 3 + v, 2 * C[2] - 3 + z);
-#pragma unroll
-                for (int r = 0; r < 3; ++r) acc[r] += w * (double)fine[r * df.NN + fn];
-            }
+            if (f < 0 || f >= df.nn[a]) continue;
+            int e = f >> 2;
+            if (e >= dc.ne[a]) e = dc.ne[a] - 1;
+            const int lc = C[a] - 2 * e;
+            if (lc < 0 || lc > 2) continue;
+            const double wv = q2_axis_weight(f - 4 * e, lc);
+            if (wv == 0.0) continue;
+            fo[a][cnt[a]] = f;
+            wt[a][cnt[a]] = (T)wv;
+            ++cnt[a];
         }
     }
+    T acc[3] = {T(0), T(0), T(0)};
+    for (int s = 0; s < cnt[0]; ++s)
+        for (int v = 0; v < cnt[1]; ++v) {
+            const T wsv = wt[0][s] * wt[1][v];
+            for (int z = 0; z < cnt[2]; ++z) {
+                const T w = wsv * wt[2][z];
+                const int64_t fn = q2node(df, fo[0][s], fo[1][v], fo[2][z]);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += w * fine[r * df.NN + fn];
+            }
+        }
     const int64_t cn = q2node(dc, C[0], C[1], C[2]);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) coarse[r * dc.NN + cn] = (T)acc[r];
+    for (int r = 0; r < 3; ++r) coarse[r * dc.NN + cn] = acc[r];
 }
 
 // ---- Q2 <-> Q1 on the same mesh (the p-multigrid step of the Q2 preconditioner) ----
@@ -605,13 +628,13 @@ __global__ void __launch_bounds__(GAL_THREADS) q2mg_galerkin_kernel(Q2Dims dc, Q
             const int j = threadIdx.x, ja[3] = {j / 9, (j / 3) % 3, j % 3};
             int n = 0;
             for (int a = 0; a < 3; ++a) {
-                const double wa = q2_basis(ja[0], 0.25 * (2 * fd[0] + a));
+                const double wa = q2_axis_weight(2 * fd[0] + a, ja[0]);
                 if (wa == 0.0) continue;
                 for (int b = 0; b < 3; ++b) {
-                    const double wb = q2_basis(ja[1], 0.25 * (2 * fd[1] + b));
+                    const double wb = q2_axis_weight(2 * fd[1] + b, ja[1]);
                     if (wb == 0.0) continue;
                     for (int c = 0; c < 3; ++c) {
-                        const double wc = q2_basis(ja[2], 0.25 * (2 * fd[2] + c));
+                        const double wc = q2_axis_weight(2 * fd[2] + c, ja[2]);
                         if (wc == 0.0) continue;
                         nzw[8 * j + n] = (T)(wa * wb * wc);
                         nzi[8 * j + n] = 9 * a + 3 * b + c;
@@ -665,34 +688,69 @@ __device__ __forceinline__ int axis_elems_asc(int I, int ne, int *ei, int *la) {
     return n;
 }
 
+// Offsets of an element's 81 nodal values (column 3 m + comp, m = 9 a + 3 b + c) from its
+// first node's x-component, for the level's node layout; filled by the first 81 threads.
+__device__ __forceinline__ void q2mg_column_offsets(const Q2Dims &d, int *off) {
+    const int t = threadIdx.x;
+    if (t < 81) {
+        const int m = t / 3, comp = t - 3 * m;
+        off[t] = (int)(comp * d.NN + ((int64_t)(m / 9) * d.nn[1] + (m / 3) % 3) * d.nn[2] + m % 3);
+    }
+}
+
+// Incident element slot s (0..N-1) of node I along one axis: N = 1 for an odd I (local 1 of
+// element (I-1)/2), N = 2 for an even I (local 2 of element I/2 - 1, then local 0 of element
+// I/2). Returns false when the slot's element lies outside the grid.
+template <int N>
+__device__ __forceinline__ bool axis_slot(int I, int ne, int s, int &e, int &l) {
+    if (N == 1) {
+        e = (I - 1) >> 1;
+        l = 1;
+        return true;
+    }
+    e = (I >> 1) - 1 + s;
+    l = s ? 0 : 2;
+    return e >= 0 && e < ne;
+}
+
 // One warp per node: s_r = sum over the incident elements of row 3 ln + r of Ke times the
-// element's nodal values; lanes 0..8 also sum the 3 x 3 diagonal block M (lane 3 r + c).
-template <typename T>
-__device__ __forceinline__ void q2mg_node_rows(const Q2Dims &d, const T *__restrict__ Ke, const T *u, int I, int J,
-                                               int K, int lane, T &a0, T &a1, T &a2, T &mv) {
-    int ex[2], lx[2], ey[2], ly[2], ez[2], lz[2];
-    const int cx = axis_elems_asc(I, d.ne[0], ex, lx), cy = axis_elems_asc(J, d.ne[1], ey, ly),
-              cz = axis_elems_asc(K, d.ne[2], ez, lz);
-    const int64_t ld = d.NN;
-    for (int a = 0; a < cx; ++a)
-        for (int b = 0; b < cy; ++b)
-            for (int c = 0; c < cz; ++c) {
-                const int64_t e = ((int64_t)ex[a] * d.ne[1] + ey[b]) * d.ne[2] + ez[c];
-                const int ln = 9 * lx[a] + 3 * ly[b] + lz[c];
-                const T *Kr = Ke + e * 6561 + 243 * ln;
-                const int bx = 2 * ex[a], by = 2 * ey[b], bz = 2 * ez[c];
+// element's nodal values. The number of incident elements per axis (NX, NY, NZ: 1 for an odd
+// coordinate, 2 for an even one) is fixed per launch; a slot outside the grid reads the zero
+// element matrix stored after the last element (index NE), so every launch runs the same fully
+// unrolled loop and the loads of successive elements overlap. Lane t takes columns t, t + 32,
+// t + 64 of the 3 rows (each nodal value loaded once for its 3 products); lanes 0..8 also sum the
+// 3 x 3 diagonal block M (lane 3 r + c). The sums end reduced over the warp in every lane.
+template <typename T, int NX, int NY, int NZ>
+__device__ __forceinline__ void q2mg_node_rows(const Q2Dims &d, const T *__restrict__ Ke, const T *u,
+                                               const int *off, int I, int J, int K, int lane, T &a0, T &a1, T &a2,
+                                               T &mv) {
+    const int o0 = off[lane], o1 = off[lane + 32], o2 = lane < 17 ? off[lane + 64] : 0;
 #pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    const int q = lane + 32 * s;
-                    if (q < 243) {
-                        const int r = q >= 162 ? 2 : (q >= 81 ? 1 : 0);
-                        const int cc = q - 81 * r, m = cc / 3, comp = cc - 3 * m;
-                        const int64_t nm = q2node(d, bx + m / 9, by + (m / 3) % 3, bz + m % 3);
-                        const T v = __ldg(Kr + q) * u[comp * ld + nm];
-                        if (r == 0) a0 += v;
-                        else if (r == 1) a1 += v;
-                        else a2 += v;
-                    }
+    for (int sa = 0; sa < NX; ++sa)
+#pragma unroll
+        for (int sb = 0; sb < NY; ++sb)
+#pragma unroll
+            for (int sc = 0; sc < NZ; ++sc) {
+                int eX, eY, eZ, lX, lY, lZ;
+                const bool in = axis_slot<NX>(I, d.ne[0], sa, eX, lX) & axis_slot<NY>(J, d.ne[1], sb, eY, lY) &
+                                axis_slot<NZ>(K, d.ne[2], sc, eZ, lZ);
+                const int ln = 9 * lX + 3 * lY + lZ;
+                const int64_t e = in ? ((int64_t)eX * d.ne[1] + eY) * d.ne[2] + eZ : d.NE;
+                const T *Kr = Ke + e * 6561 + 243 * ln;
+                const T *ub = u + (in ? q2node(d, 2 * eX, 2 * eY, 2 * eZ) : 0);
+                T v = ub[o0];
+                a0 += __ldg(Kr + lane) * v;
+                a1 += __ldg(Kr + 81 + lane) * v;
+                a2 += __ldg(Kr + 162 + lane) * v;
+                v = ub[o1];
+                a0 += __ldg(Kr + 32 + lane) * v;
+                a1 += __ldg(Kr + 113 + lane) * v;
+                a2 += __ldg(Kr + 194 + lane) * v;
+                if (lane < 17) {
+                    v = ub[o2];
+                    a0 += __ldg(Kr + 64 + lane) * v;
+                    a1 += __ldg(Kr + 145 + lane) * v;
+                    a2 += __ldg(Kr + 226 + lane) * v;
                 }
                 if (lane < 9) mv += __ldg(Kr + 81 * (lane / 3) + 3 * ln + lane % 3);
             }
@@ -705,11 +763,15 @@ __device__ __forceinline__ void q2mg_node_rows(const Q2Dims &d, const T *__restr
 }
 
 // One colour (a, b, c) of the 27-colour block Gauss-Seidel sweep on a level with element
-// matrices (NodeSmoothStencilSecondFinest / NodeSmoothStencilBlockK, MultigridSolver.hh:294-378)
-template <typename T>
+// matrices (NodeSmoothStencilSecondFinest / NodeSmoothStencilBlockK, MultigridSolver.hh:294-378);
+// NX = 1 for the middle colour a = 1, else 2 (likewise NY, NZ)
+template <typename T, int NX, int NY, int NZ>
 __global__ void __launch_bounds__(BS) q2mg_gs_kernel(Q2Dims d, const T *__restrict__ Ke, T *u,
                                                      const T *__restrict__ b, const uint8_t *__restrict__ dmask,
                                                      int ca, int cb, int cc, int forward) {
+    __shared__ int off[81];
+    q2mg_column_offsets(d, off);
+    __syncthreads();
     const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4, ic = cc == 1 ? 2 : 4;
     const int n0 = (d.nn[0] - 1 - ca) / ia + 1, n1 = (d.nn[1] - 1 - cb) / ib + 1, n2 = (d.nn[2] - 1 - cc) / ic + 1;
     const int64_t w = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 5;
@@ -722,7 +784,7 @@ __global__ void __launch_bounds__(BS) q2mg_gs_kernel(Q2Dims d, const T *__restri
     const uint8_t dm = dmask[n];
     if (dm == 7) return;
     T a0 = T(0), a1 = T(0), a2 = T(0), mv = T(0);
-    q2mg_node_rows<T>(d, Ke, u, I, J, K, lane, a0, a1, a2, mv);
+    q2mg_node_rows<T, NX, NY, NZ>(d, Ke, u, off, I, J, K, lane, a0, a1, a2, mv);
     T M[9];
 #pragma unroll
     for (int t = 0; t < 9; ++t) M[t] = __shfl_sync(0xffffffffu, mv, t);
@@ -735,26 +797,32 @@ __global__ void __launch_bounds__(BS) q2mg_gs_kernel(Q2Dims d, const T *__restri
     }
 }
 
-// out = K u (Residual: out = b - K u), zero on the constrained components when zeroDirichlet
-// (computeResidual, MultigridSolver.hh:527-541); one warp per node
-template <typename T, bool Residual>
+// out = K u (Residual: out = b - K u) at the nodes of one parity class (PX, PY, PZ: odd
+// coordinates), zero on the constrained components when zeroDirichlet (computeResidual,
+// MultigridSolver.hh:527-541); one warp per node
+template <typename T, bool Residual, int PX, int PY, int PZ>
 __global__ void __launch_bounds__(BS) q2mg_apply_kernel(Q2Dims d, const T *__restrict__ Ke, const T *__restrict__ u,
                                                         const T *__restrict__ b, T *__restrict__ out,
                                                         const uint8_t *__restrict__ dmask, int zeroDirichlet) {
+    __shared__ int off[81];
+    q2mg_column_offsets(d, off);
+    __syncthreads();
+    const int n0 = (d.nn[0] - PX + 1) / 2, n1 = (d.nn[1] - PY + 1) / 2, n2 = (d.nn[2] - PZ + 1) / 2;
     const int64_t w = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (w >= d.NN) return;
-    const int64_t q = w / d.nn[2];
-    const int K = (int)(w - q * d.nn[2]), J = (int)(q % d.nn[1]), I = (int)(q / d.nn[1]);
+    if (w >= (int64_t)n0 * n1 * n2) return;
+    const int64_t q = w / n2;
+    const int K = 2 * (int)(w - q * n2) + PZ, J = 2 * (int)(q % n1) + PY, I = 2 * (int)(q / n1) + PX;
     T a0 = T(0), a1 = T(0), a2 = T(0), mv = T(0);
-    q2mg_node_rows<T>(d, Ke, u, I, J, K, lane, a0, a1, a2, mv);
+    q2mg_node_rows<T, 2 - PX, 2 - PY, 2 - PZ>(d, Ke, u, off, I, J, K, lane, a0, a1, a2, mv);
     if (lane == 0) {
-        const uint8_t dm = zeroDirichlet ? dmask[w] : 0;
+        const int64_t n = q2node(d, I, J, K);
+        const uint8_t dm = zeroDirichlet ? dmask[n] : 0;
         const T v[3] = {a0, a1, a2};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const T r = Residual ? b[c * d.NN + w] - v[c] : v[c];
-            out[c * d.NN + w] = ((dm >> c) & 1) ? T(0) : r;
+            const T r = Residual ? b[c * d.NN + n] - v[c] : v[c];
+            out[c * d.NN + n] = ((dm >> c) & 1) ? T(0) : r;
         }
     }
 }
@@ -940,6 +1008,12 @@ void launch_q2mg_galerkin(const int neCoarse[3], const T *KeFine, T *KeCoarse, c
     VFEM_LAUNCH_CHECK();
 }
 
+template <typename T, int NX, int NY, int NZ>
+static void gs_colour(const Q2Dims &d, unsigned gs, const T *Ke, T *u, const T *b, const uint8_t *dmask, int ca,
+                      int cb, int cc, int fw, cudaStream_t st) {
+    q2mg_gs_kernel<T, NX, NY, NZ><<<gs, BS, 0, st>>>(d, Ke, u, b, dmask, ca, cb, cc, fw);
+}
+
 template <typename T>
 void launch_q2mg_gs_sweep(const int ne[3], const T *Ke, T *u, const T *b, const uint8_t *dmask, bool forward,
                           cudaStream_t st) {
@@ -951,18 +1025,48 @@ void launch_q2mg_gs_sweep(const int ne[3], const T *Ke, T *u, const T *b, const 
         if (ca >= d.nn[0] || cb >= d.nn[1] || cc >= d.nn[2]) continue;
         const int64_t cnt = (int64_t)((d.nn[0] - 1 - ca) / ia + 1) * ((d.nn[1] - 1 - cb) / ib + 1) *
                             ((d.nn[2] - 1 - cc) / ic + 1);
-        q2mg_gs_kernel<T><<<gridFor(32 * cnt, BS), BS, 0, st>>>(d, Ke, u, b, dmask, ca, cb, cc, forward ? 1 : 0);
+        const unsigned gs = gridFor(32 * cnt, BS);
+        const int fw = forward ? 1 : 0;
+        switch (4 * (ca == 1) + 2 * (cb == 1) + (cc == 1)) {
+        case 0: gs_colour<T, 2, 2, 2>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 1: gs_colour<T, 2, 2, 1>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 2: gs_colour<T, 2, 1, 2>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 3: gs_colour<T, 2, 1, 1>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 4: gs_colour<T, 1, 2, 2>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 5: gs_colour<T, 1, 2, 1>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        case 6: gs_colour<T, 1, 1, 2>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        default: gs_colour<T, 1, 1, 1>(d, gs, Ke, u, b, dmask, ca, cb, cc, fw, st); break;
+        }
         VFEM_LAUNCH_CHECK();
     }
+}
+
+template <typename T, bool R, int PX, int PY, int PZ>
+static void apply_class(const Q2Dims &d, const T *Ke, const T *u, const T *b, T *out, const uint8_t *dmask, int zd,
+                        cudaStream_t st) {
+    const int64_t cnt = (int64_t)((d.nn[0] - PX + 1) / 2) * ((d.nn[1] - PY + 1) / 2) * ((d.nn[2] - PZ + 1) / 2);
+    q2mg_apply_kernel<T, R, PX, PY, PZ><<<gridFor(32 * cnt, BS), BS, 0, st>>>(d, Ke, u, b, out, dmask, zd);
+}
+
+template <typename T, bool R>
+static void apply_classes(const Q2Dims &d, const T *Ke, const T *u, const T *b, T *out, const uint8_t *dmask, int zd,
+                          cudaStream_t st) {
+    apply_class<T, R, 0, 0, 0>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 0, 0, 1>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 0, 1, 0>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 0, 1, 1>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 1, 0, 0>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 1, 0, 1>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 1, 1, 0>(d, Ke, u, b, out, dmask, zd, st);
+    apply_class<T, R, 1, 1, 1>(d, Ke, u, b, out, dmask, zd, st);
 }
 
 template <typename T>
 void launch_q2mg_apply(const int ne[3], const T *Ke, const T *u, const T *b, T *out, const uint8_t *dmask,
                        bool zeroDirichlet, cudaStream_t st) {
     const Q2Dims d = dims_of(ne);
-    const unsigned gs = gridFor(32 * d.NN, BS);
-    if (b) q2mg_apply_kernel<T, true><<<gs, BS, 0, st>>>(d, Ke, u, b, out, dmask, zeroDirichlet ? 1 : 0);
-    else q2mg_apply_kernel<T, false><<<gs, BS, 0, st>>>(d, Ke, u, nullptr, out, dmask, zeroDirichlet ? 1 : 0);
+    if (b) apply_classes<T, true>(d, Ke, u, b, out, dmask, zeroDirichlet ? 1 : 0, st);
+    else apply_classes<T, false>(d, Ke, u, nullptr, out, dmask, zeroDirichlet ? 1 : 0, st);
     VFEM_LAUNCH_CHECK();
 }
 

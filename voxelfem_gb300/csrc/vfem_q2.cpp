@@ -439,7 +439,9 @@ void GridQ2::buildHierarchyT() {
         if constexpr (std::is_same<T, double>::value) C.Ke32 = DevBuf<float>();
         else C.Ke64 = DevBuf<double>();
         DevBuf<T> &Ke = keBuf<T>(C);
-        Ke.alloc(C.NE * 6561);
+        // one zero matrix after the last element: the level kernels' out-of-grid incidences read it
+        Ke.alloc((C.NE + 1) * 6561);
+        VFEM_CUDA(cudaMemsetAsync(Ke.p + C.NE * 6561, 0, 6561 * sizeof(T), st));
         if (l == 1) launch_q2mg_level1<T>(C.ne, KcT.p, Yt, Ke.p, st);
         else launch_q2mg_galerkin<T>(C.ne, keBuf<T>(qlv[l - 2]).p, Ke.p, st);
     }

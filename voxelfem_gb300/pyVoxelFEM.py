@@ -1448,22 +1448,24 @@ class _Q2MultigridSolver:
     def computeResidual(self, l, u, b, precision="fp64"):
         nn = self.numNodes(l)
         out = _new_vfield(nn)
-        check(_lib().vfem_q2_mg_residual(self.tps._h, self.coarsenings, int(l), ptr(_as_vfield(u, nn)),
-                                         ptr(_as_vfield(b, nn)), ptr(out), _Q2_PREC[precision]))
+        u, b = _as_vfield(u, nn), _as_vfield(b, nn)  # held: ptr() keeps no reference
+        check(_lib().vfem_q2_mg_residual(self.tps._h, self.coarsenings, int(l), ptr(u), ptr(b), ptr(out),
+                                         _Q2_PREC[precision]))
         return out
 
     def coarseSolve(self, b, precision="fp64"):
         nn = self.numNodes(self.coarsenings)
         out = _new_vfield(nn)
-        check(_lib().vfem_q2_mg_coarse_solve(self.tps._h, self.coarsenings, ptr(_as_vfield(b, nn)), ptr(out),
-                                             _Q2_PREC[precision]))
+        b = _as_vfield(b, nn)
+        check(_lib().vfem_q2_mg_coarse_solve(self.tps._h, self.coarsenings, ptr(b), ptr(out), _Q2_PREC[precision]))
         return out
 
     def applyPreconditionerInv(self, r, mgSmoothingIterations=1, precision="fp64"):
         """One V-cycle from zero on K x = r (MultigridSolver.hh:576-580)."""
         nn = self.tps.numNodes()
         out = _new_vfield(nn)
-        check(_lib().vfem_q2_mg_vcycle(self.tps._h, self.coarsenings, ptr(_as_vfield(r, nn)), ptr(out),
+        r = _as_vfield(r, nn)
+        check(_lib().vfem_q2_mg_vcycle(self.tps._h, self.coarsenings, ptr(r), ptr(out),
                                        int(mgSmoothingIterations), _Q2_PREC[precision]))
         return out
 
@@ -1923,7 +1925,8 @@ class TensorProductSimulator_2D:
     def setDensities(self, rho):
         if np.asarray(rho).size != self._nel:
             raise RuntimeError("Incorrect rho size")
-        check(_lib().vfem_grid2_set_densities(self._h, ptr(_as_elems(rho, self._nel))))
+        rho = _as_elems(rho, self._nel)  # held: ptr() keeps no reference
+        check(_lib().vfem_grid2_set_densities(self._h, ptr(rho)))
 
     def setUniformDensities(self, density):
         check(_lib().vfem_grid2_set_uniform_densities(self._h, float(density)))
