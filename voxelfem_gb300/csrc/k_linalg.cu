@@ -3,6 +3,9 @@
 // PCG vector kernels with deterministic warp-shuffle reductions
 // (MultigridSolver.hh:1047-1152, TensorProductSimulator.hh:414-459).
 #include "vfem_kernels.hpp"
+
+#include <algorithm>
+#include <cstdlib>
 #include "vfem_reduce.cuh"
 #include "vfem_stencil.cuh"
 #include "vfem_widen.h"
@@ -55,9 +58,11 @@ __global__ void symmetrize_kernel(double *A, int n) {
 // division or square root hundreds on this part, so the only sequential chains are the
 // TB pivot steps of each diagonal tile; panel solves and the triangular inverse become
 // plain tile products against the inverted diagonal tiles.
+// Tiles are read through L2 (ld.global.cg): in the persistent form other blocks rewrite them
+// between the phases, and a stale line in this SM's L1 must not be used.
 __device__ __forceinline__ void load_tile(const double *A, int n, int r0, int c0, double (*t)[TB + 1]) {
     const int ty = threadIdx.y, tx = threadIdx.x;
-    t[ty][tx] = (r0 + ty < n && c0 + tx < n) ? A[(int64_t)(r0 + ty) * n + c0 + tx] : 0.0;
+    t[ty][tx] = (r0 + ty < n && c0 + tx < n) ? __ldcg(A + (int64_t)(r0 + ty) * n + c0 + tx) : 0.0;
 }
 
 // 1/sqrt(d): single-precision seed refined by two Newton-Raphson steps,
@@ -88,7 +93,7 @@ __device__ __forceinline__ double recip_newton(double d) {
 
 __device__ __forceinline__ void ldl_pivot(int j, double d, int nb, double *rd, double *dv, int *status) {
     if (!(d > 0.0)) {
-        if (j < nb) atomicExch(status, 1);
+        if (j < nb) atomicMax(status, 1);
         d = 1.0;
     }
     dv[j] = d;
@@ -104,8 +109,7 @@ __device__ __forceinline__ void ldl_pivot(int j, double d, int nb, double *rd, d
 // one waits tens of cycles, so the only chain between steps is the next pivot's reciprocal,
 // formed by its owner thread as soon as its last update lands. Written back: the Cholesky factor
 // L = U D^{1/2} (lower tile of A) and L^{-1} = D^{-1/2} W (Dinv[k]).
-__global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *status) {
-    VFEM_PDL_ENTRY();
+__device__ __forceinline__ void chol_diag_body(double *A, double *Dinv, int n, int k, int *status) {
     __shared__ double sa[TB][TB + 1], sw[TB][TB + 1];
     __shared__ double rd[TB], dv[TB], rs[TB];
     const int ty = threadIdx.y, tx = threadIdx.x;
@@ -134,6 +138,12 @@ __global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *sta
     if (ty < nb && tx < nb)
         A[(int64_t)(kb + ty) * n + kb + tx] = (tx < ty) ? sa[ty][tx] * rs[tx] : (tx == ty) ? dv[ty] * rs[ty] : 0.0;
     Dinv[(int64_t)k * TB * TB + ty * TB + tx] = (tx <= ty) ? sw[ty][tx] * rs[ty] : 0.0;
+    __syncthreads();
+}
+
+__global__ void chol_diag_kernel(double *A, double *Dinv, int n, int k, int *status) {
+    VFEM_PDL_ENTRY();
+    chol_diag_body(A, Dinv, n, k, status);
 }
 
 // TB-term dot product of rows of two shared tiles, four independent chains
@@ -150,17 +160,22 @@ __device__ __forceinline__ double tile_dot(const double *a, int sa, const double
 }
 
 // tiles (i, k), i > k: L_ik = A_ik L_kk^{-T}
-__global__ void chol_trsm_kernel(double *A, const double *Dinv, int n, int k) {
-    VFEM_PDL_ENTRY();
+__device__ __forceinline__ void chol_trsm_body(double *A, const double *Dinv, int n, int k, int tile) {
     __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
     const int ty = threadIdx.y, tx = threadIdx.x;
-    const int kb = k * TB, r0 = kb + TB * (1 + blockIdx.x);
+    const int kb = k * TB, r0 = kb + TB * (1 + tile);
     const int nb = min(TB, n - kb);
-    sz[ty][tx] = Dinv[(int64_t)k * TB * TB + ty * TB + tx];
+    sz[ty][tx] = __ldcg(Dinv + (int64_t)k * TB * TB + ty * TB + tx);
     load_tile(A, n, r0, kb, sx);
     __syncthreads();
     const double v = tile_dot(&sx[ty][0], 1, &sz[tx][0], 1);
     if (r0 + ty < n && tx < nb) A[(int64_t)(r0 + ty) * n + kb + tx] = v;
+    __syncthreads();
+}
+
+__global__ void chol_trsm_kernel(double *A, const double *Dinv, int n, int k) {
+    VFEM_PDL_ENTRY();
+    chol_trsm_body(A, Dinv, n, k, blockIdx.x);
 }
 
 __device__ __forceinline__ void lower_tile_of(int idx, int &ii, int &jj) {
@@ -170,11 +185,10 @@ __device__ __forceinline__ void lower_tile_of(int idx, int &ii, int &jj) {
 }
 
 // trailing tiles (i, j), k < j <= i: A_ij -= L_ik L_jk^T
-__global__ void chol_syrk_kernel(double *A, int n, int k) {
-    VFEM_PDL_ENTRY();
+__device__ __forceinline__ void chol_syrk_body(double *A, int n, int k, int tile) {
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
     int ii, jj;
-    lower_tile_of(blockIdx.x, ii, jj);
+    lower_tile_of(tile, ii, jj);
     const int i = k + 1 + ii, j = k + 1 + jj;
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int kb = k * TB;
@@ -183,36 +197,51 @@ __global__ void chol_syrk_kernel(double *A, int n, int k) {
     __syncthreads();
     const double acc = tile_dot(&sa[ty][0], 1, &sb[tx][0], 1);
     const int gr = i * TB + ty, gc = j * TB + tx;
-    if (gr < n && gc < n) A[(int64_t)gr * n + gc] -= acc;
+    if (gr < n && gc < n) A[(int64_t)gr * n + gc] = __ldcg(A + (int64_t)gr * n + gc) - acc;
+    __syncthreads();
+}
+
+__global__ void chol_syrk_kernel(double *A, int n, int k) {
+    VFEM_PDL_ENTRY();
+    chol_syrk_body(A, n, k, blockIdx.x);
 }
 
 // Z = L^{-1}, right-looking over block rows. Step k: Z[k][c] = L_kk^{-1} Z[k][c] (c <= k),
 // then Z[i][c] -= L[i][k] Z[k][c] for i > k.
-__global__ void trinv_diag_kernel(const double *Dinv, double *Z, int n, int k) {
-    VFEM_PDL_ENTRY();
+__device__ __forceinline__ void trinv_diag_body(const double *Dinv, double *Z, int n, int k, int c) {
     __shared__ double sz[TB][TB + 1], sx[TB][TB + 1];
-    const int c = blockIdx.x;
     const int ty = threadIdx.y, tx = threadIdx.x;
     const int r0 = k * TB, c0 = c * TB;
-    sz[ty][tx] = Dinv[(int64_t)k * TB * TB + ty * TB + tx];
+    sz[ty][tx] = __ldcg(Dinv + (int64_t)k * TB * TB + ty * TB + tx);
     load_tile(Z, n, r0, c0, sx);
     __syncthreads();
     const double v = tile_dot(&sz[ty][0], 1, &sx[0][tx], TB + 1);
     if (r0 + ty < n && c0 + tx < n) Z[(int64_t)(r0 + ty) * n + c0 + tx] = v;
+    __syncthreads();
 }
 
-__global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
+__global__ void trinv_diag_kernel(const double *Dinv, double *Z, int n, int k) {
     VFEM_PDL_ENTRY();
+    trinv_diag_body(Dinv, Z, n, k, blockIdx.x);
+}
+
+__device__ __forceinline__ void trinv_update_body(const double *L, double *Z, int n, int k, int tile) {
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
-    const int c = blockIdx.x % (k + 1);
-    const int i = k + 1 + blockIdx.x / (k + 1);
+    const int c = tile % (k + 1);
+    const int i = k + 1 + tile / (k + 1);
     const int ty = threadIdx.y, tx = threadIdx.x;
     load_tile(L, n, i * TB, k * TB, sa);
     load_tile(Z, n, k * TB, c * TB, sb);
     __syncthreads();
     const double acc = tile_dot(&sa[ty][0], 1, &sb[0][tx], TB + 1);
     const int gr = i * TB + ty, gc = c * TB + tx;
-    if (gr < n && gc < n) Z[(int64_t)gr * n + gc] -= acc;
+    if (gr < n && gc < n) Z[(int64_t)gr * n + gc] = __ldcg(Z + (int64_t)gr * n + gc) - acc;
+    __syncthreads();
+}
+
+__global__ void trinv_update_kernel(const double *L, double *Z, int n, int k) {
+    VFEM_PDL_ENTRY();
+    trinv_update_body(L, Z, n, k, blockIdx.x);
 }
 
 __global__ void identity_kernel(double *Z, int n) {
@@ -223,11 +252,10 @@ __global__ void identity_kernel(double *Z, int n) {
 }
 
 // Ainv = Z^T Z (lower tiles computed, mirrored). Z is lower triangular.
-__global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
-    VFEM_PDL_ENTRY();
+__device__ __forceinline__ void ztz_body(const double *Z, double *Ainv, int n, int nbt, int tile) {
     __shared__ double sa[TB][TB + 1], sb[TB][TB + 1];
-    // map blockIdx.x to lower tile (bi, bj), bj <= bi
-    int idx = blockIdx.x, bi = 0;
+    // map the tile index to lower tile (bi, bj), bj <= bi
+    int idx = tile, bi = 0;
     while (idx > bi) { idx -= bi + 1; ++bi; }
     const int bj = idx;
     const int ty = threadIdx.y, tx = threadIdx.x;
@@ -235,8 +263,8 @@ __global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
     double acc = 0.0;
     for (int bk = bi; bk < nbt; ++bk) {
         const int k0 = bk * TB;
-        sa[ty][tx] = (k0 + ty < n && r0 + tx < n) ? Z[(int64_t)(k0 + ty) * n + r0 + tx] : 0.0;
-        sb[ty][tx] = (k0 + ty < n && c0 + tx < n) ? Z[(int64_t)(k0 + ty) * n + c0 + tx] : 0.0;
+        sa[ty][tx] = (k0 + ty < n && r0 + tx < n) ? __ldcg(Z + (int64_t)(k0 + ty) * n + r0 + tx) : 0.0;
+        sb[ty][tx] = (k0 + ty < n && c0 + tx < n) ? __ldcg(Z + (int64_t)(k0 + ty) * n + c0 + tx) : 0.0;
         __syncthreads();
 #pragma unroll 8
         for (int q = 0; q < TB; ++q) acc += sa[q][ty] * sb[q][tx];
@@ -249,12 +277,91 @@ __global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
     }
 }
 
+__global__ void ztz_kernel(const double *Z, double *Ainv, int n, int nbt) {
+    VFEM_PDL_ENTRY();
+    ztz_body(Z, Ainv, n, nbt, blockIdx.x);
+}
+
 __global__ void zero_upper_kernel(double *A, int n) {
     VFEM_PDL_ENTRY();
     const int64_t t = blockIdx.x * (int64_t)BS + threadIdx.x;
     if (t >= (int64_t)n * n) return;
     const int i = (int)(t / n), j = (int)(t % n);
     if (j > i) A[t] = 0.0;
+}
+
+// ---------------- the whole inverse in one cooperative launch ----------------
+// Grid-wide barrier: a monotone arrival counter, barrier number e completes when it reaches
+// e * gridDim.x. The wait is bounded: past the limit the block records a timeout (status 2) and
+// leaves the kernel; the launch is cooperative, so every block is resident and the limit is
+// only reached if something else went wrong.
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned &epoch, int *status) {
+    __shared__ int ok;
+    ++epoch;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        const unsigned target = epoch * gridDim.x;
+        int good = 1;
+        for (int it = 0;; ++it) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+            if (v >= target) break;
+            if (it > (1 << 22)) {
+                atomicMax(status, 2);
+                good = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// The phases of dense_spd_inverse's launches, each block taking every gridDim.x-th tile of a
+// phase and a grid-wide barrier where a launch boundary was: the same tile operations in the
+// same order per tile, without ~5 nbt launch gaps on the chain of diagonal tiles.
+__global__ void __launch_bounds__(TB *TB) dense_inverse_persistent_kernel(double *A, double *work, int n, int nbt,
+                                                                          int *status, unsigned *count) {
+    double *Z = work;
+    double *Dinv = work + (size_t)n * n;
+    const int G = gridDim.x, b = blockIdx.x;
+    unsigned epoch = 0;
+    for (int k = 0; k < nbt; ++k) {
+        if (b == 0) chol_diag_body(A, Dinv, n, k, status);
+        if (!grid_barrier(count, epoch, status)) return;
+        const int m = nbt - k - 1;
+        if (m > 0) {
+            for (int t = b; t < m; t += G) chol_trsm_body(A, Dinv, n, k, t);
+            if (!grid_barrier(count, epoch, status)) return;
+            for (int t = b; t < m * (m + 1) / 2; t += G) chol_syrk_body(A, n, k, t);
+            if (!grid_barrier(count, epoch, status)) return;
+        }
+    }
+    const int tid = threadIdx.y * TB + threadIdx.x;
+    for (int64_t t = (int64_t)b * TB * TB + tid; t < (int64_t)n * n; t += (int64_t)G * TB * TB) {
+        const int i = (int)(t / n), j = (int)(t % n);
+        if (j > i) A[t] = 0.0;
+        Z[t] = (i == j) ? 1.0 : 0.0;
+    }
+    if (!grid_barrier(count, epoch, status)) return;
+    for (int k = 0; k < nbt; ++k) {
+        for (int c = b; c <= k; c += G) trinv_diag_body(Dinv, Z, n, k, c);
+        if (!grid_barrier(count, epoch, status)) return;
+        const int m = nbt - k - 1;
+        if (m > 0) {
+            for (int t = b; t < m * (k + 1); t += G) trinv_update_body(A, Z, n, k, t);
+            if (!grid_barrier(count, epoch, status)) return;
+        }
+    }
+    for (int t = b; t < nbt * (nbt + 1) / 2; t += G) {
+        ztz_body(Z, A, n, nbt, t);
+        __syncthreads();
+    }
 }
 
 // ---------------- coarse solve ----------------
@@ -541,12 +648,36 @@ void launch_symmetrize(double *A, int n, cudaStream_t st) {
     VFEM_LAUNCH_CHECK();
 }
 
+// VFEM_DENSE_PERSISTENT=0 selects the form with one launch per phase
+static bool densePersistent() {
+    const char *e = std::getenv("VFEM_DENSE_PERSISTENT");
+    return !(e && e[0] == '0');
+}
+
 void dense_spd_inverse(double *A, double *work, int n, int *status, cudaStream_t st,
                        const std::function<void(const std::string &)> &mark) {
     if (n <= 0) return;
     const dim3 tb(TB, TB);
     const int nbt = (n + TB - 1) / TB;
     double *Dinv = work + (size_t)n * n;
+    if (!mark && densePersistent()) {
+        // one cooperative launch: every block resident, at most one per SM, no more blocks than
+        // the largest phase has tiles
+        static int maxBlocks = 0;
+        if (!maxBlocks) {
+            int perSM = 0, dev = 0, sms = 0;
+            VFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, dense_inverse_persistent_kernel, TB * TB, 0));
+            VFEM_CUDA(cudaGetDevice(&dev));
+            VFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            maxBlocks = std::max(1, std::min(perSM, 1) * sms);
+        }
+        const int G = std::max(1, std::min(maxBlocks, nbt * (nbt + 1) / 2));
+        unsigned *count = reinterpret_cast<unsigned *>(Dinv + (size_t)TB * TB * nbt);
+        VFEM_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned), st));
+        void *args[] = {&A, &work, &n, (void *)&nbt, &status, &count};
+        VFEM_CUDA(cudaLaunchCooperativeKernel((const void *)dense_inverse_persistent_kernel, dim3(G), tb, args, 0, st));
+        return;
+    }
     for (int k = 0; k < nbt; ++k) {
         launch_pdl(chol_diag_kernel, 1, tb, 0, st, A, Dinv, n, k, status);
         VFEM_LAUNCH_CHECK();
@@ -606,12 +737,24 @@ __global__ void cg_loop_control_kernel(cudaGraphConditionalHandle h, double *sc,
     }
     unsigned cont = 1;
     if (isnan(rsq)) {
-        sc[11] = initial ? -1.0 : it;
+        if (sc[11] == 0.0) sc[11] = initial ? -1.0 : it;  // the first NaN is the one reported
         cont = 0;
     } else if (!(rsq > sc[8] * sc[7]) || it >= sc[10]) {
         cont = 0;
     }
     cudaGraphSetConditional(h, cont);
+}
+
+// The count and NaN record of cg_loop_control_kernel after an iteration run outside the loop
+__global__ void cg_count_kernel(double *sc) {
+    const double it = sc[9] + 1.0;
+    sc[9] = it;
+    if (isnan(sc[5]) && sc[11] == 0.0) sc[11] = it;
+}
+
+void launch_cg_count(double *sc, cudaStream_t st) {
+    cg_count_kernel<<<1, 1, 0, st>>>(sc);
+    VFEM_LAUNCH_CHECK();
 }
 
 void launch_cg_loop_control(cudaGraphConditionalHandle h, double *sc, bool initial, cudaStream_t st) {

@@ -493,6 +493,7 @@ void MG2::ensureStiffness() {
         int bad = 0;
         VFEM_CUDA(cudaMemcpyAsync(&bad, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         VFEM_CUDA(cudaStreamSynchronize(st));
+        if (bad == 2) check_dense_status(bad);
         if (bad) throw Error(ERR_NOT_SPD, "Coarsest matrix not positive definite");
     }
     if (precision == PREC_MIXED) refreshSingle();

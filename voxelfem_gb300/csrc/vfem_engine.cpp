@@ -454,6 +454,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     std::memset(hostSc, 0, 17 * sizeof(double));
     setupCoarsestIndex();
     if (const char *env = std::getenv("VFEM_OVERLAP_STIFFNESS")) overlapStiffness = env[0] != '0';
+    if (const char *env = std::getenv("VFEM_PEEL_FIRST")) peelFirst = env[0] != '0';
     if (const char *env = std::getenv("VFEM_BAND_UPDATE")) bandUpdates = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_BF16")) bf16Stencils = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
@@ -482,6 +483,10 @@ void MG::clearGraphs() {
     for (auto &kv : loopGraphs) cudaGraphExecDestroy(kv.second);
     loopGraphs.clear();
     loopKernels.clear();
+    for (auto &kv : peelGraphs)
+        for (auto &e : kv.second.part)
+            if (e) cudaGraphExecDestroy(e);
+    peelGraphs.clear();
     graphX = nullptr;
 }
 
@@ -781,6 +786,7 @@ void MG::updateStiffness(bool overlap, int bandLo, int bandHi) {
     if (precision == PREC_FP64) updateStiffnessT<double>(overlap, bandLo, bandHi);
     else updateStiffnessT<float>(overlap, bandLo, bandHi);
     if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
+    rebuildInFlight = overlap;
 }
 
 void MG::ensureStiffness(bool deferCheck, bool overlap) {
@@ -800,7 +806,10 @@ void MG::ensureStiffness(bool deferCheck, bool overlap) {
             updateStiffness(overlap);
         }
     }
-    if (!overlap) VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
+    if (!overlap) {
+        VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
+        rebuildInFlight = false;
+    }
     if (!deferCheck) checkStiffness();
 }
 
@@ -808,6 +817,7 @@ void MG::ensureStiffness(bool deferCheck, bool overlap) {
 void MG::checkStiffness() {
     if (!spdCheckPending) return;
     VFEM_CUDA(cudaStreamWaitEvent(fine->stream, evCoarseReady, 0));
+    rebuildInFlight = false;
     VFEM_CUDA(cudaStreamSynchronize(fine->stream));
     spdCheckPending = false;
     int hs = 0;
@@ -815,7 +825,7 @@ void MG::checkStiffness() {
     if (hs) {
         stiffnessValid = false;
         levelsValid = false;
-        throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
+        check_dense_status(hs);
     }
 }
 
@@ -926,6 +936,53 @@ void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
     for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, !symmetricGS);
 }
 
+template <typename T>
+void MG::vcyclePartT(int part, int64_t sweeps) {
+    cudaStream_t st = fine->stream;
+    const int ts = tailStart();
+    const bool tail = std::is_same<T, float>::value && ts < L();  // the tail takes over at level ts >= 1
+    const int bottom = tail ? ts : L() - 1;
+    TailParams<T> P;
+    if (tail) {
+        P.nlev = L() - ts;
+        if (P.nlev > MAX_TAIL_LEVELS) throw Error(ERR_ARG, "too many tail levels");
+        P.sweeps = (int)sweeps;
+        P.symmetric = symmetricGS ? 1 : 0;
+        for (int t = 0; t < P.nlev; ++t) {
+            auto &Q = lv[ts + t].data<T>();
+            P.lv[t] = TailLevel<T>{lv[ts + t].g, Q.S.p, Q.x.p, Q.b.p, Q.r.p, lv[ts + t].dmask.p};
+        }
+    }
+    auto down = [&](int l) {
+        auto &D = lv[l].data<T>();
+        const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
+        launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
+        for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, true);
+        residualT<T>(l);
+        auto &Dc = lv[l + 1].data<T>();
+        launch_restrict<T>(lv[l].g, lv[l + 1].g, D.r.p, Dc.b.p, st);
+        launch_masked_zero<T>(lv[l + 1].g, Dc.x.p, MARGIN, st);
+    };
+    if (part == 0) {
+        down(0);
+        return;
+    }
+    if (part == 1) {
+        for (int l = 1; l < bottom; ++l) down(l);
+        if (tail) launch_tail_down<T>(P, st);
+        return;
+    }
+    auto &Dc = lv.back().data<T>();
+    launch_coarse_solve<T>(lv.back().g, Ainv.p, freeIdx.p, nfreeDev.p, nfreeCap, Dc.b.p, Dc.x.p, cscratch.p, st);
+    if (tail) launch_tail_up<T>(P, st);
+    for (int l = bottom - 1; l >= 0; --l) {
+        auto &D = lv[l].data<T>();
+        auto &Dn = lv[l + 1].data<T>();
+        launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dn.x.p, D.x.p, true, st);
+        for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, !symmetricGS);
+    }
+}
+
 // MultigridSolver.hh:587-609
 template <typename T>
 void MG::fmgT(int l, int64_t sweeps, bool residualSystem) {
@@ -991,6 +1048,12 @@ void MG::cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool h
     } else {
         launch_cg_precond_out<double>(g, rbuf.p, s.p, rbuf.p, fine->dmask.p, partials.p, st);
     }
+    cgIterationRest(x, mgIter, hostMirror);
+}
+
+void MG::cgIterationRest(double *x, int64_t mgIter, bool hostMirror) {
+    cudaStream_t st = fine->stream;
+    const Geom &g = lv[0].g;
     launch_cg_beta(partials.p, REDUCE_BLOCKS, sc.p, st);
     outerDirection(mgIter > 0 && precision != PREC_FP64 ? lv[0].d32.x.p : nullptr);
     const int nb = outerMatvecApply(dvec.p, Ad.p, partials.p, nullptr, true);
@@ -1137,6 +1200,69 @@ cudaGraphExec_t MG::loopGraph(const GraphKey &key, double *x, int64_t mgIter, in
     return loopGraphs.emplace(key, exec).first->second;
 }
 
+// [set IF from the loop's initial condition] -> IF( part `part` of the first iteration )
+const MG::PeelGraphs &MG::peelGraph(const GraphKey &key, double *x, int64_t sweeps) {
+    auto it = peelGraphs.find(key);
+    if (it != peelGraphs.end()) return it->second;
+    cudaStream_t st = fine->stream;
+    PeelGraphs pg;
+    try {
+        for (int part = 0; part < 3; ++part) {
+            cudaGraph_t top;
+            VFEM_CUDA(cudaGraphCreate(&top, 0));
+            try {
+                cudaGraphConditionalHandle h;
+                VFEM_CUDA(cudaGraphConditionalHandleCreate(&h, top, 0, cudaGraphCondAssignDefault));
+                VFEM_CUDA(cudaStreamBeginCaptureToGraph(st, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+                launch_cg_loop_control(h, sc.p, true, st);
+                VFEM_CUDA(cudaStreamEndCapture(st, &top));
+                cudaGraphNode_t init;
+                size_t n = 1;
+                VFEM_CUDA(cudaGraphGetNodes(top, &init, &n));
+                cudaGraphNodeParams p = {};
+                p.type = cudaGraphNodeTypeConditional;
+                p.conditional.handle = h;
+                p.conditional.type = cudaGraphCondTypeIf;
+                p.conditional.size = 1;
+                cudaGraphNode_t node;
+                VFEM_CUDA(cudaGraphAddNode(&node, top, &init, nullptr, 1, &p));
+                cudaGraph_t body = p.conditional.phGraph_out[0];
+                VFEM_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+                try {
+                    if (part == 0 && !fusedInit()) {
+                        const int64_t n3 = 3 * lv[0].g.NN;
+                        launch_fill<float>(lv[0].d32.x.p, 0.f, n3, st);
+                        launch_cast<float, double>(rbuf.p, lv[0].d32.b.p, n3, st);
+                    }
+                    vcyclePartT<float>(part, sweeps);
+                    if (part == 2) {
+                        launch_cg_precond_out<float>(lv[0].g, lv[0].d32.x.p, (double *)nullptr, rbuf.p,
+                                                     fine->dmask.p, partials.p, st);
+                        cgIterationRest(x, 1, false);
+                        launch_cg_count(sc.p, st);
+                    }
+                } catch (...) {
+                    cudaStreamEndCapture(st, &body);
+                    throw;
+                }
+                VFEM_CUDA(cudaStreamEndCapture(st, &body));
+                pg.kernels += countKernelNodes(body) + 1;
+                VFEM_CUDA(cudaGraphInstantiate(&pg.part[part], top, 0));
+            } catch (...) {
+                cudaGraphDestroy(top);
+                throw;
+            }
+            cudaGraphDestroy(top);
+        }
+    } catch (...) {
+        for (auto &e : pg.part)
+            if (e) cudaGraphExecDestroy(e);
+        throw;
+    }
+    launchCounter() -= pg.kernels;  // the captures launched nothing
+    return peelGraphs.emplace(key, pg).first->second;
+}
+
 static double readScalar(double *dev, cudaStream_t st) {
     double v = 0;
     VFEM_CUDA(cudaMemcpyAsync(&v, dev, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1163,6 +1289,7 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     // here and the solve's start below runs meanwhile (positive definiteness is checked in
     // pcgFinish)
     if (mgIter > 0) ensureStiffness(true, overlapStiffness);
+    const bool rebuilding = rebuildInFlight;  // forked here or by the caller (MG::pcg)
     if (!dirichletSatisfied) launch_enforce_dirichlet<double>(g, x, fine->dmask.p, fine->dval.p, st);
     launch_masked_dot_partials<double, double>(g, b, b, partials.p, st);
     launch_finalize(partials.p, REDUCE_BLOCKS, sc.p + 7, st);
@@ -1175,7 +1302,19 @@ void MG::pcgStart(double *x, const double *b, int64_t maxIter, double tol, int64
     launch_fill<double>(dvec.p, 0.0, 3 * g.NN, st);
     pendingKey = GraphKey{mgIter, sweeps, fmg ? 1 : 0, symmetricGS ? 1 : 0, precision, outerMatvec};
     cudaGraphExec_t exec = loopGraph(pendingKey, x, mgIter, sweeps, fmg);
-    VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));  // join the side-stream rebuild
+    pendingPeeled = peelFirst && rebuilding && precision == PREC_MIXED && mgIter == 1 && !fmg && sweeps > 0;
+    if (pendingPeeled) {
+        // the first iteration joins the rebuild where it needs it
+        const PeelGraphs &pg = peelGraph(pendingKey, x, sweeps);
+        VFEM_CUDA(cudaGraphLaunch(pg.part[0], st));
+        VFEM_CUDA(cudaStreamWaitEvent(st, evLevelsReady, 0));
+        VFEM_CUDA(cudaGraphLaunch(pg.part[1], st));
+        VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));
+        VFEM_CUDA(cudaGraphLaunch(pg.part[2], st));
+    } else {
+        VFEM_CUDA(cudaStreamWaitEvent(st, evCoarseReady, 0));  // join the side-stream rebuild
+    }
+    rebuildInFlight = false;
     VFEM_CUDA(cudaGraphLaunch(exec, st));
     pending = true;
 }
@@ -1192,7 +1331,10 @@ PcgStats MG::pcgFinish() {
     stats.iterations = (int64_t)hostSc[9];
     stats.rsq = hostSc[5];
     stats.bnorm2 = hostSc[7];
-    launchCounter() += 1 + (loopKernels[pendingKey] + 1) * (uint64_t)stats.iterations;
+    if (pendingPeeled && stats.iterations > 0)
+        launchCounter() += 3 + peelGraphs[pendingKey].kernels + 1 + (loopKernels[pendingKey] + 1) * (uint64_t)(stats.iterations - 1);
+    else
+        launchCounter() += (pendingPeeled ? 3 : 0) + 1 + (loopKernels[pendingKey] + 1) * (uint64_t)stats.iterations;
     if (hostSc[11] < 0.0) throw Error(ERR_NAN, "NaN encountered");
     if (hostSc[11] > 0.0) throw Error(ERR_NAN, "NaN encountered at iteration" + std::to_string((int64_t)hostSc[11]));
     stats.relres = stats.bnorm2 > 0 ? std::sqrt(stats.rsq / stats.bnorm2) : std::sqrt(stats.rsq);

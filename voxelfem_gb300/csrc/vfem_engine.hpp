@@ -221,6 +221,7 @@ public:
     cudaStream_t stiffStream = nullptr;
     cudaEvent_t evStiffFork = nullptr, evLevelsReady = nullptr, evCoarseReady = nullptr;
     bool overlapStiffness = true;
+    bool rebuildInFlight = false;  // a side-stream rebuild forked and not yet joined by the solver stream
 
     // per-level operations on caller FP64 vectors (level sizes)
     void applyK(int l, const double *u, double *out);
@@ -310,6 +311,21 @@ public:
     cudaGraphExec_t loopGraph(const GraphKey &key, double *x, int64_t mgIter, int64_t sweeps, bool fmg);
     const double *graphX = nullptr;  // buffers baked into captured graphs
     void clearGraphs();
+    // The first iteration of a mixed solve whose hierarchy is being rebuilt on the side stream
+    // runs as three graphs split where the rebuild's events are joined: level 0's down leg (needs
+    // nothing rebuilt), the down legs below it (after evLevelsReady), and the coarsest solve, the
+    // up legs and the rest of the iteration (after evCoarseReady); the device-resident loop
+    // follows. Each graph runs its part under an IF node that holds the loop's own condition, so
+    // the iterates and the iteration count are those of the single loop graph.
+    // VFEM_PEEL_FIRST=0 keeps the single graph.
+    struct PeelGraphs {
+        cudaGraphExec_t part[3] = {nullptr, nullptr, nullptr};
+        uint64_t kernels = 0;  // kernel nodes of the three IF bodies
+    };
+    std::map<GraphKey, PeelGraphs> peelGraphs;
+    bool peelFirst = true;
+    bool pendingPeeled = false;
+    const PeelGraphs &peelGraph(const GraphKey &key, double *x, int64_t sweeps);
 
 private:
     void allocLevels();
@@ -335,6 +351,12 @@ private:
     template <typename T>
     void applyKLevelT(int l, const T *u, T *out, bool zeroInit, bool negate);
     void cgIteration(double *x, int64_t mgIter, int64_t sweeps, bool fmg, bool hostMirror = true);
+    // the iteration after its preconditioner: direction, matvec, step, residual norm
+    void cgIterationRest(double *x, int64_t mgIter, bool hostMirror);
+    // vcycleT<T>(0, sweeps, true) in three parts with the same launches in the same order:
+    // 0 = level 0's down leg, 1 = the down legs below it, 2 = the coarsest solve and the up legs
+    template <typename T>
+    void vcyclePartT(int part, int64_t sweeps);
 
 public:
     // One FP32 V-cycle on the fine level's right-hand side lv[0].d32.b (zero initial guess),

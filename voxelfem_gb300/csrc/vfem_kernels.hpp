@@ -213,7 +213,14 @@ void launch_symmetrize(double *A, int n, cudaStream_t st);
 // so small tiles shorten it; the FP64 work of the whole inverse does not depend on the tile.
 constexpr int DENSE_TILE = 16;
 inline size_t dense_inverse_work_size(int n) {
-    return (size_t)n * n + (size_t)DENSE_TILE * DENSE_TILE * ((n + DENSE_TILE - 1) / DENSE_TILE);
+    // Z, the inverted diagonal tiles, and one word for the persistent form's grid barrier
+    return (size_t)n * n + (size_t)DENSE_TILE * DENSE_TILE * ((n + DENSE_TILE - 1) / DENSE_TILE) + 1;
+}
+// The dense inverse's status word: 1 = not positive definite, 2 = a grid-wide barrier of the
+// single-launch form timed out.
+inline void check_dense_status(int s) {
+    if (s == 2) throw Error(ERR_CUDA, "coarsest inverse: a grid-wide barrier timed out");
+    if (s) throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
 }
 // 1/d and 1/sqrt(d) through the dense inverse's pivot helpers (single-precision seed and two
 // Newton-Raphson steps), elementwise; a diagnostic of their accuracy.
@@ -227,6 +234,8 @@ void launch_coarse_solve(const Geom &g, const double *Ainv, const int *freeIdx, 
 // Sets the WHILE condition of a device-resident PCG loop from the CG scalars (initial: before
 // the first iteration, else after one; counts iterations, flags a NaN residual).
 void launch_cg_loop_control(cudaGraphConditionalHandle h, double *sc, bool initial, cudaStream_t st);
+// the iteration count and NaN record of one iteration run outside the loop
+void launch_cg_count(double *sc, cudaStream_t st);
 // sc[0] = 0, first-iteration flag, tolerance, iteration counter and limit, NaN flag
 void launch_cg_init(double *sc, double tol2, double maxIter, cudaStream_t st);
 // y += a x

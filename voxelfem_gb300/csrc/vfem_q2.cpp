@@ -456,7 +456,7 @@ void GridQ2::buildHierarchyT() {
         VFEM_CUDA(cudaStreamSynchronize(st));
         if (status) {
             qVersion = 0;
-            throw Error(ERR_NOT_SPD, "Coarsest stiffness matrix is not positive definite");
+            check_dense_status(status);
         }
     }
     VFEM_CUDA(cudaStreamSynchronize(st));
