@@ -1,5 +1,5 @@
 """The coarsest dense inverse in one cooperative launch (phases separated by a bounded grid
-barrier) against the form with one launch per phase: the same tile operations in the same order,
+barrier; VFEM_DENSE_PERSISTENT=1) against the default form with one launch per phase: the same tile operations in the same order,
 so bit-identical inverses, for coarsest systems of one to dozens of tiles; and both against the
 oracle's Cholesky solve (1e-10)."""
 import numpy as np
