@@ -839,6 +839,8 @@ def run_q2_solve(g, ne, rho):
       to relative residual 1e-11."""
     import time
 
+    import torch
+
     nx, ny, nz = ne
     g.addDirichletCondition([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, float(ny), float(nz)], "xyz")
     nnd = [2 * v + 1 for v in ne]
@@ -854,9 +856,11 @@ def run_q2_solve(g, ne, rho):
         mg.setHierarchy(hierarchy)
         mg.setPrecision(precision)
         mg.preconditionedConjugateGradient(x0, f, 1, tol, None, 1, sweeps, False)  # hierarchy, buffers
+        torch.cuda.nvtx.range_push("vfem_q2_solve_%s_%s" % (hierarchy, precision))
         t0 = time.perf_counter()
         u = mg.preconditionedConjugateGradient(x0, f, maxIter, tol, None, 1, sweeps, False)
         seconds = time.perf_counter() - t0
+        torch.cuda.nvtx.range_pop()
         st = mg.lastStats
         return u, {"seconds": seconds, "iterations": int(st.iterations), "relres": float(st.relres),
                    "hierarchy": hierarchy, "precision": precision, "sweeps": sweeps,
