@@ -219,18 +219,6 @@ __device__ __forceinline__ void build_tables(const double pf[PF][3], int sh0, ui
 
 __device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
 
-// x 2^k as a double, built on the integer units from the float's bit pattern (rebiased exponent
-// plus k, mantissa moved from 23 to 52 bits) when x is normal and the result is a normal double;
-// otherwise through the FP64 units. Exact either way: the same value as (double)x * 2^k.
-__device__ __forceinline__ double widen_scaled(float x, int k, double scale) {
-    const uint32_t b = __float_as_uint(x);
-    const int e = (int)((b >> 23) & 0xffu);
-    const int eb = e + 896 + k;
-    if (e == 0 || e == 0xff || eb < 1 || eb > 2046) return (double)x * scale;
-    const uint64_t bits = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)eb << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
-}
-
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     const float bb = s - a;
@@ -309,9 +297,6 @@ __global__ void __launch_bounds__(TCT, 4)
     const int sh0 = 1020 + s;
     // a NaN or infinite operand makes every output NaN (the solver's NaN check sees it)
     const double outScale = finite ? ldexp(1.0, s - 13) : __longlong_as_double(0x7FF8000000000000ll);
-    // the scale's exponent, out of range when the operand is not finite (every product then
-    // takes the FP64 path and carries the NaN)
-    const int outExp = finite ? s - 13 : 4096;
 
     // this thread's element row of the MMA tile
     const int ey = tid % TY, ez = tid / TY;
@@ -363,9 +348,7 @@ __global__ void __launch_bounds__(TCT, 4)
                 double f = 0.0;
                 if (nj < g.nyv()) {
                     const uint8_t dm = zeroDir ? dmask[n] : 0;
-                    // (h + l) 2^(s - 13): the two scaled widenings are exact and their sum rounds
-                    // once, as (double(h) + double(l)) * 2^(s - 13) does, with one FP64 operation
-                    f = ((dm >> r) & 1) ? 0.0 : widen_scaled(h, outExp, outScale) + widen_scaled(l, outExp, outScale);
+                    f = ((dm >> r) & 1) ? 0.0 : ((double)h + (double)l) * outScale;
                     if (withDot) dot += u[r * g.ld + n] * f;
                 }
                 if (rhs) {

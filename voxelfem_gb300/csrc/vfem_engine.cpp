@@ -458,6 +458,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     if (const char *env = std::getenv("VFEM_BAND_UPDATE")) bandUpdates = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_BF16")) bf16Stencils = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
+    if (const char *env = std::getenv("VFEM_TAIL_MAX_NODES")) tailMaxNodes = std::atoll(env);
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
     VFEM_CUDA(cudaEventCreateWithFlags(&evLevelsReady, cudaEventDisableTiming));
