@@ -125,6 +125,42 @@ def fp32_peak_tflops(n=8192, reps=5):
     return 2.0 * n ** 3 / best / 1e12
 
 
+def level1_contraction_tc_probe(nc_elems, reps=20):
+    """The level-1 operator as the reference applies it, Sum_f E_f Kc_f u_c over the coarse
+    elements (MultigridSolver.hh:475-499), cast as one tensor-core GEMM [Kc_0 ... Kc_7] (192 x 24)
+    times U_c (24 x coarse elements) through cuBLAS: device time in bf16 (one product; FP32-class
+    accuracy would need a three-way split of both operands, six products) and in TF32, with the
+    192-row output written in the operands' precision. The E-weighted combine and the gather of
+    U_c are not included, so this is a lower bound on a tensor-core level-1 residual."""
+    import torch
+
+    out = {"shape": [192, 24, int(nc_elems)], "flops": 2.0 * 192 * 24 * nc_elems}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    try:
+        for name, dt, tf32 in (("bf16", torch.bfloat16, False), ("tf32", torch.float32, True)):
+            torch.backends.cuda.matmul.allow_tf32 = tf32
+            a = torch.randn(192, 24, dtype=dt, device="cuda")
+            b = torch.randn(24, int(nc_elems), dtype=dt, device="cuda")
+            torch.matmul(a, b)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out[name + "_ms"] = ms
+            out[name + "_tflops"] = out["flops"] / (ms * 1e-3) / 1e12
+            out[name + "_output_bytes"] = 192 * int(nc_elems) * (2 if dt == torch.bfloat16 else 4)
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    out["bf16_split3_ms_estimate"] = 6 * out["bf16_ms"]
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -502,6 +538,10 @@ def run_ours(args):
                                             "peak_kind": "measured (cuBLAS SGEMM 8192^3, TF32 off, in this run)",
                                             "frac": achieved / p32}
     roofline = dict(rooflines[dom], kernel=dom, peak_kind=peak_kind)
+    # the tensor-core alternative for the level-1 operator, beside the stored FP32 stencil
+    tc_probe = level1_contraction_tc_probe(ne[0] * ne[1] * ne[2] // 8)
+    tc_probe["stored_stencil_residual_ms"] = kernels.get("residual_level1_fp32", {}).get("ms")
+    tc_probe["stored_stencil_sweep_ms"] = kernels.get("gs_level1_sweep_fp32", {}).get("ms")
 
     line = {"metric": METRIC, "value": aggregate_per_solve(tmix, ws, args.steps), "unit": "s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmix_step * 1000,
@@ -531,6 +571,7 @@ def run_ours(args):
                            "df": kernels["applyk_fine_df"]["gbs"],
                            "tc": kernels.get("applyk_fine_tc", {}).get("gbs")},
             "kernels": kernels,
+            "level1_tc_probe": tc_probe,
             "breakdown_ms": {"mixed_per_iteration": breakdown_mixed, "fp64_per_iteration": breakdown_fp64}}
     if rank == 0 and ws == 1 and not args.no_lbl:
         line["lbl"] = run_lbl()

@@ -892,8 +892,8 @@ void MG::residualT(int l) {
 
 int MG::tailStart() const {
     int t = L() - 1;  // the coarsest level always ends the tail
-    // the tail kernels read FP32 node-contiguous rows: bf16 plane-layout levels stay outside
-    while (t - 1 >= 1 && lv[t - 1].g.NN <= tailMaxNodes && !halfStencil(t - 1)) --t;
+    // the tail kernels read FP32 node-contiguous rows: plane-layout and bf16 levels stay outside
+    while (t - 1 >= 1 && lv[t - 1].g.NN <= tailMaxNodes && lv[t - 1].rows && !halfStencil(t - 1)) --t;
     return (t < L() - 1) ? t : L();
 }
 
