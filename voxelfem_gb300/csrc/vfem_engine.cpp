@@ -460,6 +460,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
     if (const char *env = std::getenv("VFEM_TAIL_MAX_NODES")) tailMaxNodes = std::atoll(env);
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
+    VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream2, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
     VFEM_CUDA(cudaEventCreateWithFlags(&evLevelsReady, cudaEventDisableTiming));
     VFEM_CUDA(cudaEventCreateWithFlags(&evCoarseReady, cudaEventDisableTiming));
@@ -472,6 +473,11 @@ MG::~MG() {
     if (evLevelsReady) cudaEventDestroy(evLevelsReady);
     if (evCoarseReady) cudaEventDestroy(evCoarseReady);
     if (stiffStream) cudaStreamDestroy(stiffStream);
+    if (stiffStream2) {
+        cudaStreamSynchronize(stiffStream2);
+        cudaStreamDestroy(stiffStream2);
+    }
+    for (cudaEvent_t e : evKe) cudaEventDestroy(e);
     if (hostSc) cudaFreeHost(hostSc);
     if (copyDone) cudaEventDestroy(copyDone);
     if (copyStream) cudaStreamDestroy(copyStream);
@@ -719,6 +725,55 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
         launch_ke_scaled<T>(lv[0].g, Y0, K0d.p, D.Ke.p, st);
         launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, lv[0].rows, st);
         VFEM_CUDA(cudaStreamSynchronize(st));
+    } else if (gs != st && L() > 2) {
+        // Two side streams. gs: the element-matrix chain of levels 2.., the coarsest level's
+        // stencil, its dense operator and inverse (the critical path of the rebuild); gs2: the
+        // stencils of the smoothing levels, each after its level's element matrices. gs joins gs2
+        // before evCoarseReady, so that event still stands for the whole rebuild.
+        const bool band = bandLo >= 0;
+        VFEM_CUDA(cudaStreamWaitEvent(stiffStream2, evStiffFork, 0));
+        cudaStream_t gs2 = stiffStream2;
+        if ((int)evKe.size() < L()) {
+            for (int l = (int)evKe.size(); l < L(); ++l) {
+                cudaEvent_t e;
+                VFEM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                evKe.push_back(e);
+            }
+        }
+        for (int l = 1; l < L() && (!band || bandLo < bandHi); ++l) {
+            auto &D = lv[l].data<T>();
+            lv[l].rows = lv[l].g.NN <= rowsMaxNodes;
+            const bool half = std::is_same<T, float>::value && halfStencil(l);
+            if (half) D.Sh.alloc((size_t)STENCIL_PLANES * lv[l].g.NN);
+            else D.S.alloc((size_t)(lv[l].rows ? 256 : STENCIL_PLANES) * lv[l].g.NN);
+            const int eLo = band ? (bandLo >> l) : 0;
+            const int eHi = band ? ((bandHi - 1) >> l) + 1 : lv[l].g.ne[1];
+            const int nLo = eLo, nHi = band ? eHi + 1 : lv[l].g.nn[1];
+            if (l == 1) {
+                if (half)
+                    launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.Sh.p, lv[1].rows, gs2, nLo,
+                                             nHi);
+                else
+                    launch_stencil_level1<T>(lv[1].g, lv[0].g, Y0, Tr<T>::Kc(*this).p, D.S.p, lv[1].rows, gs2, nLo,
+                                             nHi);
+                continue;
+            }
+            D.Ke.alloc((size_t)lv[l].g.NE * 576);
+            if (l == 2)
+                launch_ke_level2<T>(lv[2].g, lv[1].g, lv[0].g, Y0, Tr<T>::K2(*this).p, D.Ke.p, gs, eLo, eHi);
+            else
+                launch_ke_coarsen<T>(lv[l].g, lv[l - 1].g, lv[l - 1].data<T>().Ke.p, Tr<T>::phis(*this).p, D.Ke.p, gs,
+                                     eLo, eHi);
+            // the coarsest level's stencil feeds the dense operator (gs); the others smooth (gs2)
+            cudaStream_t ss = (l == L() - 1) ? gs : gs2;
+            if (ss == gs2) {
+                VFEM_CUDA(cudaEventRecord(evKe[l], gs));
+                VFEM_CUDA(cudaStreamWaitEvent(gs2, evKe[l], 0));
+            }
+            if (half) launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.Sh.p, lv[l].rows, ss, nLo, nHi);
+            else launch_stencil_from_ke<T>(lv[l].g, D.Ke.p, D.S.p, lv[l].rows, ss, nLo, nHi);
+        }
+        VFEM_CUDA(cudaEventRecord(evLevelsReady, gs2));
     } else {
         const bool band = bandLo >= 0;
         for (int l = 1; l < L() && (!band || bandLo < bandHi); ++l) {
@@ -754,8 +809,9 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
                 mark("galerkin:L" + std::to_string(l) + " stencil");
             }
         }
+        VFEM_CUDA(cudaEventRecord(evLevelsReady, gs));
     }
-    VFEM_CUDA(cudaEventRecord(evLevelsReady, gs));
+    if (L() == 1) VFEM_CUDA(cudaEventRecord(evLevelsReady, gs));
     // dense reduced coarsest operator, FP64 inverse
     const Level &C = lv.back();
     if (nfree > 0) {
@@ -769,6 +825,7 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
         VFEM_CUDA(cudaMemcpyAsync(&hostSc[16], status.p, sizeof(int), cudaMemcpyDeviceToHost, gs));
         spdCheckPending = true;
     }
+    if (gs != st) VFEM_CUDA(cudaStreamWaitEvent(gs, evLevelsReady, 0));  // the stencils' stream
     VFEM_CUDA(cudaEventRecord(evCoarseReady, gs));
     stiffnessValid = true;
     stiffnessPrecision = precision;

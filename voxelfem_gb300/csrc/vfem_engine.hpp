@@ -219,6 +219,8 @@ public:
     // cannot sit inside the device-side WHILE loop, whose body admits no event nodes.)
     // VFEM_OVERLAP_STIFFNESS=0 keeps the rebuild on the solver stream.
     cudaStream_t stiffStream = nullptr;
+    cudaStream_t stiffStream2 = nullptr;  // the smoothing levels' stencils beside the chain
+    std::vector<cudaEvent_t> evKe;        // level l's element matrices written (stiffStream)
     cudaEvent_t evStiffFork = nullptr, evLevelsReady = nullptr, evCoarseReady = nullptr;
     bool overlapStiffness = true;
     bool rebuildInFlight = false;  // a side-stream rebuild forked and not yet joined by the solver stream
