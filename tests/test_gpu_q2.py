@@ -110,3 +110,18 @@ def test_q2_pcg_matches_dense_solve(gpu, oracle, coarsenings, matvec, hierarchy)
     assert mg.lastStats.iterations < 60
     c, cref = np.sum(f * x), np.sum(f * xref)
     assert abs(c - cref) / abs(cref) < 1e-9
+
+
+@pytest.mark.parametrize("ne", [(2, 2, 2), (3, 2, 5), (8, 4, 6), (16, 8, 12)])
+def test_q2_fp32_line_sweep_matches_colour_launches(gpu, monkeypatch, ne):
+    """The FP32 sweep's line form (one launch per (a, b) class, its three colours on whole
+    z-lines) gives the same iterate, bit for bit, as 27 colour launches."""
+    g, Y, bits = make(ne, seed=6)
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal((g.numNodes(), 3))
+    b = rng.standard_normal((g.numNodes(), 3))
+    for fwd in (True, False):
+        monkeypatch.setenv("VFEM_Q2_GS_FORM", "colours")
+        ref = g.smoothingMulticoloredGS(u, b, fwd, precision="fp32")
+        monkeypatch.setenv("VFEM_Q2_GS_FORM", "lines")
+        np.testing.assert_array_equal(g.smoothingMulticoloredGS(u, b, fwd, precision="fp32"), ref)

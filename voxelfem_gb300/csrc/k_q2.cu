@@ -12,6 +12,9 @@
 #include "vfem_df.cuh"
 #include "vfem_kernels.hpp"
 
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <type_traits>
 
 namespace vfem {
@@ -331,6 +334,60 @@ __global__ void __launch_bounds__(BS) gs_q2_f32_kernel(Q2Dims d, const float *__
     u[n] = u0;
     u[ld + n] = u1;
     u[2 * ld + n] = u2;
+}
+
+// Node update of gs_q2_f32_kernel for node (I, J, K) of parity (PX, PY, PZ)
+template <int PX, int PY, int PZ>
+__device__ __forceinline__ void gs_q2_node_f32(const Q2Dims &d, const float *__restrict__ Y, float *u,
+                                               const float *__restrict__ b, const uint8_t *__restrict__ dmask, int I,
+                                               int J, int K, int forward) {
+    const int64_t n = q2node(d, I, J, K), ld = d.NN;
+    const uint8_t dm = dmask[n];
+    if (dm == 7) return;
+    float s0 = b[n], s1 = b[ld + n], s2 = b[2 * ld + n];
+    float M[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    q2_gather_f32<PX, PY, PZ, true>(d, Y, u, I, J, K, s0, s1, s2, M);
+    float u0 = u[n], u1 = u[ld + n], u2 = u[2 * ld + n];
+    q2_node_update<float>(dm, s0, s1, s2, M, forward != 0, u0, u1, u2);
+    u[n] = u0;
+    u[ld + n] = u1;
+    u[2 * ld + n] = u2;
+}
+
+// The three colours (a, b, 0..2) of the FP32 sweep in one launch (2..0 backward): they are
+// consecutive in the reference's order, and a node of the class (a, b) couples to the nodes of
+// its own class only along its own z-line (the next line of the class is one or two elements
+// away on either side), so each block owns linesPerBlock whole lines and runs the three colours
+// on them with a block barrier between. The same node updates in the same order as the three
+// colour launches, with u read from DRAM once per class instead of once per colour.
+template <int PX, int PY>
+__global__ void __launch_bounds__(BS, 4) gs_q2_lines_f32_kernel(Q2Dims d, const float *__restrict__ Y, float *u,
+                                                             const float *__restrict__ b,
+                                                             const uint8_t *__restrict__ dmask, int ca, int cb,
+                                                             int linesPerBlock, int forward) {
+    const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4;
+    const int n0 = (d.nn[0] - 1 - ca) / ia + 1, n1 = (d.nn[1] - 1 - cb) / ib + 1;
+    const int nlines = n0 * n1;
+    const int l0 = (int)blockIdx.x * linesPerBlock;
+    const int nl = max(0, min(linesPerBlock, nlines - l0));
+#pragma unroll 1
+    for (int s = 0; s < 3; ++s) {
+        const int cc = forward ? s : 2 - s;
+        if (cc < d.nn[2]) {
+            const int ic = cc == 1 ? 2 : 4;
+            const int nk = (d.nn[2] - 1 - cc) / ic + 1;
+            const int cnt = nl * nk;
+            for (int t = threadIdx.x; t < cnt; t += BS) {
+                const int q = t / nk, kk = t - q * nk;
+                const int line = l0 + q;
+                const int ii = line / n1, jj = line - ii * n1;
+                const int I = ca + ia * ii, J = cb + ib * jj, K = cc + ic * kk;
+                if (cc == 1) gs_q2_node_f32<PX, PY, 1>(d, Y, u, b, dmask, I, J, K, forward);
+                else gs_q2_node_f32<PX, PY, 0>(d, Y, u, b, dmask, I, J, K, forward);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // One colour (a, b, c) of the 27-colour block Gauss-Seidel sweep: nodes a + inc_a * s along x
@@ -916,10 +973,47 @@ void launch_applyk_q2(const int ne[3], const T *K0, const T *Y, const T *u, T *o
     VFEM_LAUNCH_CHECK();
 }
 
+// Form of the FP32 triquadratic sweep: one launch per (a, b) class with its three colours on
+// whole z-lines (default), or one launch per colour (VFEM_Q2_GS_FORM=colours).
+static bool q2GsLines() {
+    const char *e = std::getenv("VFEM_Q2_GS_FORM");
+    return !(e && std::strcmp(e, "colours") == 0);
+}
+
+template <int PX, int PY>
+static void gs_q2_lines(const Q2Dims &d, const float *Y, float *u, const float *b, const uint8_t *dmask, int ca,
+                        int cb, bool forward, cudaStream_t st) {
+    const int ia = ca == 1 ? 2 : 4, ib = cb == 1 ? 2 : 4;
+    const int nlines = ((d.nn[0] - 1 - ca) / ia + 1) * ((d.nn[1] - 1 - cb) / ib + 1);
+    // lines per block (VFEM_Q2_LINES_PER_BLOCK): on the 128^3 grid a sweep took 3.46 ms with 2,
+    // 3.89 ms with 4, 4.24 ms with 3, 5.49 ms with 1, against 4.27 ms for the 27 colour launches
+    int lpb = 2;
+    if (const char *e = std::getenv("VFEM_Q2_LINES_PER_BLOCK")) lpb = std::max(1, std::atoi(e));
+    const unsigned blocks = (unsigned)((nlines + lpb - 1) / lpb);
+    gs_q2_lines_f32_kernel<PX, PY><<<blocks, BS, 0, st>>>(d, Y, u, b, dmask, ca, cb, lpb, forward ? 1 : 0);
+}
+
 template <typename T>
 void launch_gs_q2_sweep(const int ne[3], const T *K0, const T *Y, T *u, const T *b, const uint8_t *dmask, bool forward,
                         cudaStream_t st) {
     const Q2Dims d = dims_of(ne);
+    if constexpr (std::is_same<T, float>::value) {
+        if (q2GsLines()) {
+            for (int s = 0; s < 9; ++s) {
+                const int cls = forward ? s : 8 - s;
+                const int ca = cls / 3, cb = cls % 3;
+                if (ca >= d.nn[0] || cb >= d.nn[1]) continue;
+                switch (2 * (ca == 1) + (cb == 1)) {
+                case 0: gs_q2_lines<0, 0>(d, Y, u, b, dmask, ca, cb, forward, st); break;
+                case 1: gs_q2_lines<0, 1>(d, Y, u, b, dmask, ca, cb, forward, st); break;
+                case 2: gs_q2_lines<1, 0>(d, Y, u, b, dmask, ca, cb, forward, st); break;
+                default: gs_q2_lines<1, 1>(d, Y, u, b, dmask, ca, cb, forward, st); break;
+                }
+                VFEM_LAUNCH_CHECK();
+            }
+            return;
+        }
+    }
     for (int s = 0; s < 27; ++s) {
         const int col = forward ? s : 26 - s;
         const int ca = col / 9, cb = (col / 3) % 3, cc = col % 3;
