@@ -212,12 +212,13 @@ public:
     bool levelsValid = false;
     uint64_t stiffnessMaterialVersion = 0;
     int64_t fullRebuilds = 0, bandRebuilds = 0;  // counters (diagnostic)
-    // The asynchronous solve rebuilds the hierarchy on a side stream: the solve's start (the
-    // initial residual through the outer matvec, its norms, the first preconditioner input) runs
-    // on the solver stream while the Galerkin operators (evLevelsReady) and the coarsest dense
-    // inverse (evCoarseReady) are built, and the solve's graph waits for evCoarseReady. (The wait
-    // cannot sit inside the device-side WHILE loop, whose body admits no event nodes.)
-    // VFEM_OVERLAP_STIFFNESS=0 keeps the rebuild on the solver stream.
+    // The asynchronous solve rebuilds the hierarchy on side streams: the solve's start (the
+    // initial residual through the outer matvec, its norms, the first preconditioner input) and
+    // the split first iteration (PeelGraphs) run on the solver stream while the smoothing levels'
+    // stencils (evLevelsReady) and the coarsest dense inverse (evCoarseReady, which also covers the
+    // stencils) are built; the loop graph follows evCoarseReady. (No wait can sit inside the
+    // device-side WHILE loop, whose body admits no event nodes.) VFEM_OVERLAP_STIFFNESS=0 keeps the
+    // rebuild on the solver stream.
     cudaStream_t stiffStream = nullptr;
     cudaStream_t stiffStream2 = nullptr;  // the smoothing levels' stencils beside the chain
     std::vector<cudaEvent_t> evKe;        // level l's element matrices written (stiffStream)
