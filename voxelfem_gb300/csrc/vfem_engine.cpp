@@ -459,6 +459,7 @@ MG::MG(Grid *fine_, int coarsenings) : fine(fine_) {
     if (const char *env = std::getenv("VFEM_STENCIL_BF16")) bf16Stencils = env[0] != '0';
     if (const char *env = std::getenv("VFEM_STENCIL_LINES_MAX_NODES")) stencilLinesMaxNodes = std::atoll(env);
     if (const char *env = std::getenv("VFEM_TAIL_MAX_NODES")) tailMaxNodes = std::atoll(env);
+    if (const char *env = std::getenv("VFEM_REBUILD_STREAMS")) twoStreamRebuild = env[0] != '1';
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream, cudaStreamNonBlocking));
     VFEM_CUDA(cudaStreamCreateWithFlags(&stiffStream2, cudaStreamNonBlocking));
     VFEM_CUDA(cudaEventCreateWithFlags(&evStiffFork, cudaEventDisableTiming));
@@ -725,7 +726,7 @@ void MG::updateStiffnessT(bool overlap, int bandLo, int bandHi) {
         launch_ke_scaled<T>(lv[0].g, Y0, K0d.p, D.Ke.p, st);
         launch_stencil_from_ke<T>(lv[0].g, D.Ke.p, D.S.p, lv[0].rows, st);
         VFEM_CUDA(cudaStreamSynchronize(st));
-    } else if (gs != st && L() > 2) {
+    } else if (gs != st && L() > 2 && twoStreamRebuild) {
         // Two side streams. gs: the element-matrix chain of levels 2.., the coarsest level's
         // stencil, its dense operator and inverse (the critical path of the rebuild); gs2: the
         // stencils of the smoothing levels, each after its level's element matrices. gs joins gs2

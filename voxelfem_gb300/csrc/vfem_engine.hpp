@@ -222,6 +222,7 @@ public:
     cudaStream_t stiffStream = nullptr;
     cudaStream_t stiffStream2 = nullptr;  // the smoothing levels' stencils beside the chain
     std::vector<cudaEvent_t> evKe;        // level l's element matrices written (stiffStream)
+    bool twoStreamRebuild = true;         // VFEM_REBUILD_STREAMS=1: the whole rebuild on stiffStream
     cudaEvent_t evStiffFork = nullptr, evLevelsReady = nullptr, evCoarseReady = nullptr;
     bool overlapStiffness = true;
     bool rebuildInFlight = false;  // a side-stream rebuild forked and not yet joined by the solver stream
