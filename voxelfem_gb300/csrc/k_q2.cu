@@ -1092,12 +1092,8 @@ void launch_q2mg_galerkin(const int neCoarse[3], const T *KeFine, T *KeCoarse, c
     const int nef[3] = {2 * neCoarse[0], 2 * neCoarse[1], 2 * neCoarse[2]};
     const Q2Dims dc = dims_of(neCoarse), df = dims_of(nef);
     const size_t smem = sizeof(T) * (2 * 6561 + 27 * 8) + sizeof(int) * (27 * 8 + 27);
-    static bool attrSet[2] = {false, false};
-    bool &set = attrSet[sizeof(T) == 8 ? 1 : 0];
-    if (!set) {
-        VFEM_CUDA(cudaFuncSetAttribute(q2mg_galerkin_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        set = true;
-    }
+    // set on every call (once per hierarchy build): the attribute belongs to the current device
+    VFEM_CUDA(cudaFuncSetAttribute(q2mg_galerkin_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (dc.NE > 0) q2mg_galerkin_kernel<T><<<(unsigned)dc.NE, GAL_THREADS, smem, st>>>(dc, df, KeFine, KeCoarse);
     VFEM_LAUNCH_CHECK();
 }
