@@ -502,7 +502,7 @@ void MG::vcycleOnFineRhs(int64_t sweeps) {
     if (precision != PREC_MIXED) throw Error(ERR_STATE, "the fine-rhs V-cycle runs in mixed precision");
     auto &D = lv[0].d32;
     launch_fill<float>(D.x.p, 0.f, 3 * lv[0].g.NN, fine->stream);
-    vcycleT<float>(0, sweeps, true);
+    vcycleT<float>(0, sweeps, true, true);
 }
 
 // Dirichlet coarsening (MultigridSolver.hh:58-103): a fine constrained node on a coarse
@@ -957,7 +957,7 @@ int MG::tailStart() const {
 
 // MultigridSolver.hh:617-658
 template <typename T>
-void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
+void MG::vcycleT(int l, int64_t sweeps, bool residualSystem, bool xZero) {
     cudaStream_t st = fine->stream;
     auto &D = lv[l].data<T>();
     if (std::is_same<T, float>::value && residualSystem && l >= 1 && l == tailStart()) {
@@ -983,14 +983,18 @@ void MG::vcycleT(int l, int64_t sweeps, bool residualSystem) {
         return;
     }
     const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
-    if (residualSystem || l > 0 || !fine->dvalNonzero) launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
-    else launch_enforce_dirichlet<T>(lv[l].g, D.x.p, dm, fine->dval.p, st);
+    // enforceDirichletConditions (MultigridSolver.hh:628): a no-op on an iterate that is zero on
+    // every row the level reads (the fresh preconditioner iterate, a just masked-zeroed coarse one)
+    if (!xZero) {
+        if (residualSystem || l > 0 || !fine->dvalNonzero) launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
+        else launch_enforce_dirichlet<T>(lv[l].g, D.x.p, dm, fine->dval.p, st);
+    }
     for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, true);
     residualT<T>(l);
     auto &Dc = lv[l + 1].data<T>();
     launch_restrict<T>(lv[l].g, lv[l + 1].g, D.r.p, Dc.b.p, st);
     launch_masked_zero<T>(lv[l + 1].g, Dc.x.p, MARGIN, st);
-    vcycleT<T>(l + 1, sweeps, true);
+    vcycleT<T>(l + 1, sweeps, true, true);
     launch_interpolate<T>(lv[l].g, lv[l + 1].g, Dc.x.p, D.x.p, true, st);
     for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, !symmetricGS);
 }
@@ -1013,9 +1017,8 @@ void MG::vcyclePartT(int part, int64_t sweeps) {
         }
     }
     auto down = [&](int l) {
+        // the first iteration's iterates are zero on every row read: no Dirichlet zeroing (vcycleT)
         auto &D = lv[l].data<T>();
-        const uint8_t *dm = (l == 0) ? fine->dmask.p : lv[l].dmask.p;
-        launch_zero_dirichlet<T>(lv[l].g, D.x.p, dm, st);
         for (int64_t i = 0; i < sweeps; ++i) smoothT<T>(l, true);
         residualT<T>(l);
         auto &Dc = lv[l + 1].data<T>();
@@ -1076,7 +1079,7 @@ void MG::preconditionT(const double *r, int64_t mgIter, int64_t sweeps, bool fmg
         fmgT<T>(0, sweeps, true);
         for (int64_t i = 1; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
     } else {
-        for (int64_t i = 0; i < mgIter; ++i) vcycleT<T>(0, sweeps, true);
+        for (int64_t i = 0; i < mgIter; ++i) vcycleT<T>(0, sweeps, true, i == 0);
     }
 }
 

@@ -341,8 +341,9 @@ private:
     void smoothT(int l, bool forward);
     template <typename T>
     void residualT(int l);
+    // xZero: the level's iterate is known to be zero on every row the level reads
     template <typename T>
-    void vcycleT(int l, int64_t sweeps, bool residualSystem);
+    void vcycleT(int l, int64_t sweeps, bool residualSystem, bool xZero = false);
     template <typename T>
     void fmgT(int l, int64_t sweeps, bool residualSystem);
     template <typename T>
